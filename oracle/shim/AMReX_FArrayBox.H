@@ -1,0 +1,2 @@
+// Shim: forwards to the project-written AMReX stand-ins.
+#include "amrex_shim.H"
