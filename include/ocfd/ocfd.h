@@ -1,0 +1,145 @@
+/* ocfd.h - C ABI of the GB300 (sm_103a) right-hand-side and update path for
+ * OpenCFD-AMR.
+ *
+ * Every entry point is stream-ordered, takes plain pointers and sizes, returns an
+ * ocfd_status and never traps on the device.  Device-side failures (a non-finite
+ * value found by a checking kernel, a bounded wait that ran out) set a
+ * per-context error word read by ocfd_context_check().
+ *
+ * Data layout mirrors AMReX so a caller can pass its own objects:
+ *   ocfd_array4  has the member order and types of amrex::Array4<double>
+ *                (p, jstride, kstride, nstride, begin, end, ncomp; begin/end are
+ *                Dim3 = three ints, end exclusive), element (i,j,k,n) at
+ *                p[(i-begin[0]) + (j-begin[1])*jstride + (k-begin[2])*kstride + n*nstride];
+ *   ocfd_box     holds amrex::Box smallEnd/bigEnd (inclusive cell indices);
+ *   ocfd_parm    has the member order of the reference's Parm
+ *                (Source/Constants.H:7-64, CHEM build); a non-CHEM Parm is
+ *                layout-identical to its first 16 doubles.
+ * State arrays carry OCFD_NUM_GROW ghost cells (Source/EBR.H:207); face
+ * arrays of direction d cover amrex::surroundingNodes(bx, d).
+ */
+#ifndef OCFD_OCFD_H
+#define OCFD_OCFD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OCFD_NUM_GROW 4
+#define OCFD_NCONS 5
+#define OCFD_NSPEC 9
+
+typedef enum ocfd_status {
+    OCFD_OK = 0,
+    OCFD_BAD_ARG = 1,        /* argument checks failed; nothing was launched */
+    OCFD_LAUNCH_FAIL = 2,    /* a CUDA launch or runtime call failed */
+    OCFD_TIMEOUT = 3,        /* a bounded device wait ran out */
+    OCFD_NONFINITE = 4,      /* a checking kernel found NaN/Inf */
+    OCFD_GUARD_FALLBACK = 5, /* a surrogate guard rejected cells (they were redone in FP64) */
+    OCFD_NO_DEVICE = 6,      /* no CUDA device, or the device is not sm_103 */
+    OCFD_OUT_OF_MEMORY = 7,
+    OCFD_UNSUPPORTED = 8     /* valid request this build does not serve */
+} ocfd_status;
+
+/* amrex::Array4<double> */
+typedef struct ocfd_array4 {
+    double* p;
+    int64_t jstride, kstride, nstride;
+    int32_t begin[3];
+    int32_t end[3];
+    int32_t ncomp;
+} ocfd_array4;
+
+/* amrex::Array4<amrex::EBCellFlag const>: 32-bit flag words.  Bits 0-1 cell
+ * type (0 regular, 1 single-valued cut, 3 covered); bit 4+(i+1)+3(j+1)+9(k+1)
+ * set when the neighbour at offset (i,j,k) is connected. */
+typedef struct ocfd_flag4 {
+    const uint32_t* p;
+    int64_t jstride, kstride, nstride;
+    int32_t begin[3];
+    int32_t end[3];
+    int32_t ncomp;
+} ocfd_flag4;
+
+/* amrex::Box: inclusive cell-centred bounds */
+typedef struct ocfd_box {
+    int32_t lo[3];
+    int32_t hi[3];
+} ocfd_box;
+
+/* Parm, Source/Constants.H:7-64 (CHEM member set).  Table pointers may be NULL
+ * (the built-in Li-Dryer tables of Source/Constants.cpp:15-150 are used) or
+ * point to host or device memory holding the reference's table layout. */
+typedef struct ocfd_parm {
+    double eos_gamma, eos_m, Patm;
+    double cv, cp, Ru, Rg, kOverMu;
+    double Pr, C_s, T_s;
+    double smallr, smallp, eps;
+    double twoThirds, oneSix;
+    const double* mw;
+    const double *H2_lo, *H2_hi, *O2_lo, *O2_hi, *H2O_lo, *H2O_hi, *H_lo, *H_hi, *O_lo, *O_hi;
+    const double *OH_lo, *OH_hi, *HO2_lo, *HO2_hi, *H2O2_lo, *H2O2_hi, *N2_lo, *N2_hi;
+    const double* HP;
+    const double* A0;
+    const double* visccoeff;
+    const double* conductcoeff;
+    const double* diffcoeff;
+} ocfd_parm;
+
+/* Flags of the RHS entry points */
+#define OCFD_VISC 1u           /* EBR::do_visc (Source/EBR.cpp:25) */
+#define OCFD_REDISTRIBUTE 2u   /* EBR::do_redistribute (Source/EBR.cpp:27), cut boxes only */
+#define OCFD_FLUX_FP32 4u      /* mixed precision: split + WENO-Z in FP32, FP64 divergence */
+
+typedef struct ocfd_context ocfd_context;
+
+/* ---------------------------------------------------------------- setup */
+/* Reference defaults (Source/Constants.H:9-30) followed by Parm::Initialize
+ * (Source/Constants.cpp:7-12); table pointers set to the library's host copies
+ * of the Li-Dryer data.  Host only; needs no device. */
+ocfd_status ocfd_parm_default(ocfd_parm* parm);
+
+/* Binds `device`, uploads the mechanism tables and allocates the context's
+ * scratch pool and error word.  One context per host thread and stream. */
+ocfd_status ocfd_context_create(const ocfd_parm* parm, int device, ocfd_context** ctx);
+ocfd_status ocfd_context_destroy(ocfd_context* ctx);
+
+/* Synchronises `stream`, returns the device error word (0 = none) and clears it.
+ * Returns OCFD_NONFINITE / OCFD_TIMEOUT when the word says so. */
+ocfd_status ocfd_context_check(ocfd_context* ctx, void* stream, uint32_t* device_error);
+
+const char* ocfd_status_string(ocfd_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* ocfd_last_error(void);
+/* Library version, and the compute capability it was built for (e.g. 1030). */
+int ocfd_version(void);
+int ocfd_built_arch(void);
+
+/* ------------------------------------------------------- box right-hand sides */
+/* Regular (uncut) box, ideal gas: c2prim -> Steger-Warming split -> WENO-Z face
+ * flux (+ viscous flux with OCFD_VISC) -> divergence, for all three directions,
+ * in one fused launch.  Replaces the kernel chain of EBR::compute_dSdt,
+ * Source/Advance.cpp:231-329 (point kernels Source/kernel/Kernels.H:13-40,84-97,
+ * FluxSplit.H:11-193, Reconstruction.H:70-279, Diffusion.H:7-131).
+ *   S     state, ncomp >= 5, covering grow(bx, 4)
+ *   dSdt  output over bx, ncomp >= 5
+ *   flux  NULL or three face arrays (x, y, z) over surroundingNodes(bx, d) that
+ *         receive the face fluxes the reflux registers consume (Advance.cpp:219-222)
+ *   dxinv inverse cell sizes (geom.InvCellSizeArray()) */
+ocfd_status ocfd_rhs_regular_box_f64(ocfd_context* ctx, const ocfd_array4* S,
+                                     const ocfd_array4* dSdt, const ocfd_array4* flux,
+                                     ocfd_box bx, const double dxinv[3], unsigned flags,
+                                     void* stream);
+
+/* ----------------------------------------------------------- measurement */
+/* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops
+ * per FMA), from register-only FMA chains over all SMs. */
+ocfd_status ocfd_measure_fma_peaks(double* fp64_gflops, double* fp32_gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

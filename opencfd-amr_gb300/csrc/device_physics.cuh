@@ -1,0 +1,118 @@
+// Point-level physics of the ideal-gas path, written for the GPU.  Each
+// function keeps the operation order of the reference expression it replaces,
+// so the FP64 kernels agree with the reference to rounding (the parity tests
+// use 1e-12 norm-wise; differences come only from FMA contraction).
+#pragma once
+
+#include "ocfd_internal.h"
+
+namespace ocfd {
+
+enum { URHO = 0, UMX = 1, UMY = 2, UMZ = 3, UEDEN = 4, NCONS = 5 };
+enum { QRHO = 0, QU = 1, QV = 2, QW = 3, QPRES = 4, QT = 5, QC = 6, QGAMA = 7 };
+
+__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+
+// c2prim, Source/kernel/Kernels.H:13-40.  q = rho, u, v, w, p, T, c.
+__device__ __forceinline__ void c2prim_ideal(const DevParm& P, double u0, double u1, double u2,
+                                             double u3, double u4, double* q) {
+    double rho = dmax(u0, P.smallr);
+    double rhoinv = 1.0 / rho;
+    double ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
+    double kineng = 0.5 * (ux * ux + uy * uy + uz * uz);
+    double ei = u4 - rho * kineng;
+    double p = dmax((P.gamma - 1.0) * ei, P.smallp);
+    double T = p / (rho * P.Rg);
+    q[QRHO] = rho;
+    q[QU] = ux;
+    q[QV] = uy;
+    q[QW] = uz;
+    q[QPRES] = p;
+    q[QT] = T;
+    q[QC] = sqrt(P.gamma * P.Rg * T);
+}
+
+// Steger-Warming split along D (Source/kernel/FluxSplit.H:11-193), given the
+// split constants t1 = 1/(2g), t2 = 2(g-1), t3 = (3-g)/(2(g-1)), gm1 = g-1.
+template <int D>
+__device__ __forceinline__ void sw_split(double d, double u, double v, double w, double c,
+                                         double t1, double t2, double t3, double gm1,
+                                         double* fp, double* fm) {
+    const double vel[3] = {u, v, w};
+    const double un = vel[D];
+    const double uc1 = un - c, uc2 = un + c;
+    double a0 = u, a1 = v, a2 = w, b0 = u, b1 = v, b2 = w;
+    if (D == 0) { a0 = uc1; b0 = uc2; }
+    if (D == 1) { a1 = uc1; b1 = uc2; }
+    if (D == 2) { a2 = uc1; b2 = uc2; }
+    const double vvc1 = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
+    const double vvc2 = 0.5 * (b0 * b0 + b1 * b1 + b2 * b2);
+    const double v2 = gm1 * (u * u + v * v + w * w);
+    const double w2 = t3 * c * c;
+    const double E1 = un, E2 = un - c, E3 = un + c;
+    const double E1P = (E1 + fabs(E1)) * 0.5, E2P = (E2 + fabs(E2)) * 0.5, E3P = (E3 + fabs(E3)) * 0.5;
+    const double E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
+    const double t0 = d * t1;
+    const double sp = t2 * E1P + E2P + E3P, sm = t2 * E1M + E2M + E3M;
+    fp[URHO] = t0 * sp;
+    fm[URHO] = t0 * sm;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        if (m == D) {
+            fp[UMX + m] = t0 * (t2 * E1P * un + E2P * uc1 + E3P * uc2);
+            fm[UMX + m] = t0 * (t2 * E1M * un + E2M * uc1 + E3M * uc2);
+        } else {
+            fp[UMX + m] = t0 * vel[m] * sp;
+            fm[UMX + m] = t0 * vel[m] * sm;
+        }
+    }
+    fp[UEDEN] = t0 * (E1P * v2 + E2P * vvc1 + E3P * vvc2 + w2 * (E2P + E3P));
+    fm[UEDEN] = t0 * (E1M * v2 + E2M * vvc1 + E3M * vvc2 + w2 * (E2M + E3M));
+}
+
+// WENO-Z, Source/kernel/Reconstruction.H:83-138: f+ stencil at cells i-3..i+1
+__device__ __forceinline__ double wenoz_plus(double V1, double V2, double V3, double V4, double V5) {
+    const double eps = 1e-6;
+    double s11 = (13.0 / 12.0) * (V1 - 2.0 * V2 + V3) * (V1 - 2.0 * V2 + V3) +
+                 0.25 * (V1 - 4.0 * V2 + 3.0 * V3) * (V1 - 4.0 * V2 + 3.0 * V3);
+    double s22 = (13.0 / 12.0) * (V2 - 2.0 * V3 + V4) * (V2 - 2.0 * V3 + V4) + 0.25 * (V2 - V4) * (V2 - V4);
+    double s33 = (13.0 / 12.0) * (V3 - 2.0 * V4 + V5) * (V3 - 2.0 * V4 + V5) +
+                 0.25 * (3.0 * V3 - 4.0 * V4 + V5) * (3.0 * V3 - 4.0 * V4 + V5);
+    double s55 = fabs(s11 - s33);
+    s11 = 1.0 + (s55 / (eps + s11)) * (s55 / (eps + s11));
+    s22 = 1.0 + (s55 / (eps + s22)) * (s55 / (eps + s22));
+    s33 = 1.0 + (s55 / (eps + s33)) * (s55 / (eps + s33));
+    double a1 = s11, a2 = 6.0 * s22, a3 = 3.0 * s33;
+    double invsum = 1.0 / (a1 + a2 + a3);
+    double v1 = 2.0 * V1 - 7.0 * V2 + 11.0 * V3;
+    double v2 = -V2 + 5.0 * V3 + 2.0 * V4;
+    double v3 = 2.0 * V3 + 5.0 * V4 - V5;
+    return (1.0 / 6.0) * invsum * (a1 * v1 + a2 * v2 + a3 * v3);
+}
+
+// ... and the mirrored f- stencil at cells i-2..i+2
+__device__ __forceinline__ double wenoz_minus(double V1, double V2, double V3, double V4, double V5) {
+    const double eps = 1e-6;
+    double s11 = (13.0 / 12.0) * (V5 - 2.0 * V4 + V3) * (V5 - 2.0 * V4 + V3) +
+                 0.25 * (V5 - 4.0 * V4 + 3.0 * V3) * (V5 - 4.0 * V4 + 3.0 * V3);
+    double s22 = (13.0 / 12.0) * (V2 - 2.0 * V3 + V4) * (V2 - 2.0 * V3 + V4) + 0.25 * (V4 - V2) * (V4 - V2);
+    double s33 = (13.0 / 12.0) * (V3 - 2.0 * V2 + V1) * (V3 - 2.0 * V2 + V1) +
+                 0.25 * (3.0 * V3 - 4.0 * V2 + V1) * (3.0 * V3 - 4.0 * V2 + V1);
+    double s55 = fabs(s11 - s33);
+    s11 = 1.0 + (s55 / (eps + s11)) * (s55 / (eps + s11));
+    s22 = 1.0 + (s55 / (eps + s22)) * (s55 / (eps + s22));
+    s33 = 1.0 + (s55 / (eps + s33)) * (s55 / (eps + s33));
+    double a1 = s11, a2 = 6.0 * s22, a3 = 3.0 * s33;
+    double invsum = 1.0 / (a1 + a2 + a3);
+    double v1 = 11.0 * V3 - 7.0 * V4 + 2.0 * V5;
+    double v2 = -V4 + 5.0 * V3 + 2.0 * V2;
+    double v3 = 2.0 * V3 + 5.0 * V2 - V1;
+    return (1.0 / 6.0) * invsum * (a1 * v1 + a2 * v2 + a3 * v3);
+}
+
+__device__ __forceinline__ double sutherland(const DevParm& P, double T) {
+    return P.C_s * T * sqrt(T) / (T + P.T_s);
+}
+
+}  // namespace ocfd

@@ -1,0 +1,20 @@
+"""Python access to the ocfd C ABI (include/ocfd/ocfd.h).
+
+The product is libocfd.so: hand-written sm_103a kernels behind a C ABI, with
+the level driver (box tables, ghost fill, RK stages, graph capture) in C++ in
+the same library.  This package only binds that ABI with ctypes so tests and
+the benchmark can drive it with device buffers owned by PyTorch; there is no
+computational fallback here - a call without the library or without a GPU
+raises.
+"""
+from ._abi import (Array4, Box, Flag4, OcfdError, Parm, array4, box, flag4, lib, load,  # noqa: F401
+                   status_string, check)
+from .context import Context  # noqa: F401
+
+NUM_GROW = 4
+NCONS = 5
+NSPEC = 9
+
+VISC = 1
+REDISTRIBUTE = 2
+FLUX_FP32 = 4

@@ -1,0 +1,68 @@
+"""Context object and per-box calls of the C ABI (host-side mirror of the
+reference's per-box RHS interface, Source/Advance.cpp:182-418)."""
+from __future__ import annotations
+
+import ctypes
+
+from ._abi import Array4, Parm, array4, box, check, load
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return ctypes.c_void_p(stream)
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def default_parm():
+    p = Parm()
+    check(load().ocfd_parm_default(ctypes.byref(p)), "ocfd_parm_default")
+    return p
+
+
+class Context:
+    """Owns an ocfd_context (device tables, scratch pool, error word)."""
+
+    def __init__(self, parm=None, device=0):
+        L = load()
+        self.parm = parm if parm is not None else default_parm()
+        h = ctypes.c_void_p()
+        check(L.ocfd_context_create(ctypes.byref(self.parm), device, ctypes.byref(h)),
+              "ocfd_context_create")
+        self.h = h
+        self.lib = L
+
+    def close(self):
+        if self.h:
+            self.lib.ocfd_context_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, stream=None):
+        w = ctypes.c_uint32()
+        check(self.lib.ocfd_context_check(self.h, _stream_ptr(stream), ctypes.byref(w)),
+              "ocfd_context_check")
+        return w.value
+
+    # ---- per-box right-hand sides ------------------------------------------
+    def rhs_regular_box(self, S, dSdt, lo, hi, dxinv, flags=0, flux=None, S_begin=None,
+                        stream=None):
+        """S: (>=5, nz+8, ny+8, nx+8) tensor beginning at lo-4 (or S_begin);
+        dSdt: (>=5, nz, ny, nx) at lo; flux: None or three face tensors at lo."""
+        sb = S_begin if S_begin is not None else tuple(l - 4 for l in lo)
+        aS = array4(S, sb)
+        aD = array4(dSdt, lo)
+        fl = None
+        if flux is not None:
+            fl = (Array4 * 3)(*[array4(f, lo) for f in flux])
+        dx = (ctypes.c_double * 3)(*dxinv)
+        st = self.lib.ocfd_rhs_regular_box_f64(self.h, ctypes.byref(aS), ctypes.byref(aD), fl,
+                                               box(lo, hi), dx, flags, _stream_ptr(stream))
+        check(st, "ocfd_rhs_regular_box_f64")
