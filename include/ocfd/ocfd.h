@@ -134,6 +134,62 @@ ocfd_status ocfd_rhs_regular_box_f64(ocfd_context* ctx, const ocfd_array4* S,
                                      ocfd_box bx, const double dxinv[3], unsigned flags,
                                      void* stream);
 
+/* ------------------------------------------------------------------ level */
+/* One AMR level advanced on the device: the build's own host driver in place of
+ * AMReX's AmrLevel machinery (absent).  It owns the level's state FABs (each
+ * box grown by OCFD_NUM_GROW), fills ghost cells on the device (same-level
+ * exchange with periodic images, then the physical boundary types of
+ * Source/Setup.cpp:17-92 and the case boundary functor, direction by
+ * direction), and advances SSP-RK3 steps whose stages are fused RHS + update
+ * launches over every box of the level (Source/Advance.cpp:81-150), with the
+ * CFL step (Source/Advance.cpp:10-79, limited to 1.1x the previous step as
+ * Source/EBR.cpp:268-275) reduced on the device.  A whole step is one CUDA
+ * graph launch. */
+typedef struct ocfd_level ocfd_level;
+
+#define OCFD_BC_INTERIOR 0
+#define OCFD_BC_INFLOW 1
+#define OCFD_BC_OUTFLOW 2
+#define OCFD_BC_SYMMETRY 3
+#define OCFD_BC_SLIPWALL 4
+#define OCFD_BC_NOSLIPWALL 5
+
+#define OCFD_CASE_NONE 0
+#define OCFD_CASE_DMR 1    /* Exec/1_DMR/prob_bcfill.cpp:9-59; params = left state (5), right state (5) */
+#define OCFD_CASE_INFLOW 2 /* constant inflow state on ext_dir faces; params = state (5) */
+
+typedef struct ocfd_level_desc {
+    int32_t nbox;
+    const ocfd_box* boxes;   /* valid boxes, disjoint */
+    ocfd_box domain;         /* problem domain in cell indices of this level */
+    int32_t lo_bc[3];        /* ebr.lo_bc codes, OCFD_BC_* (0 = periodic) */
+    int32_t hi_bc[3];
+    double dx[3];
+    double prob_lo[3];
+    int32_t bc_case;         /* OCFD_CASE_* */
+    double case_params[16];
+    int32_t tile;            /* regular-RHS tile shape index, -1 = automatic */
+} ocfd_level_desc;
+
+ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, ocfd_level** level);
+ocfd_status ocfd_level_destroy(ocfd_level* level);
+/* Array4 (device) of box `ibox` of the level's current state. */
+ocfd_status ocfd_level_state(ocfd_level* level, int ibox, ocfd_array4* out);
+/* Copy the grown state FAB of every box from / to `buf` (host or device memory,
+ * boxes back to back in box order, each (ncomp, nz+8, ny+8, nx+8), i fastest). */
+ocfd_status ocfd_level_copy_in(ocfd_level* level, const double* buf, void* stream);
+ocfd_status ocfd_level_copy_out(ocfd_level* level, double* buf, void* stream);
+size_t ocfd_level_state_elems(const ocfd_level* level);
+ocfd_status ocfd_level_fill_ghosts(ocfd_level* level, double time, void* stream);
+/* Advance `nsteps` SSP-RK3 steps with CFL number `cfl` (flags: OCFD_VISC,
+ * OCFD_FLUX_FP32).  Time and dt stay on the device; read them with
+ * ocfd_level_time(). */
+ocfd_status ocfd_level_advance(ocfd_level* level, int nsteps, double cfl, unsigned flags,
+                               void* stream);
+ocfd_status ocfd_level_time(ocfd_level* level, double* time, double* last_dt, void* stream);
+/* Set the level time and forget the previous dt (the next step is not limited). */
+ocfd_status ocfd_level_set_time(ocfd_level* level, double time, void* stream);
+
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops
  * per FMA), from register-only FMA chains over all SMs. */

@@ -7,6 +7,7 @@
 
 #include "ocfd_internal.h"
 #include "mechanism.h"
+#include "rhs_regular.h"
 
 namespace ocfd {
 
@@ -132,6 +133,8 @@ ocfd_status ocfd_context_create(const ocfd_parm* parm, int device, ocfd_context*
         return fail(OCFD_OUT_OF_MEMORY, "ocfd_context_create: error word allocation");
     }
     ocfd_status s = mech_upload(*parm);
+    if (s == OCFD_OK) s = configure_rhs_regular();
+    if (s == OCFD_OK) s = configure_rhs_regular_f32();
     if (s != OCFD_OK) {
         cudaFree(ctx->d_error);
         delete ctx;

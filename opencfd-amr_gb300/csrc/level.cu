@@ -1,0 +1,695 @@
+// Level driver: box table, device ghost fill, fused SSP-RK3 steps in a CUDA graph.
+//
+// Storage: three state buffers A, B, C holding every box's FAB (box grown by
+// NUM_GROW, components slowest, i fastest), boxes back to back.  A step is
+//   k_step_begin          dt = min(cfl * CFLmin, 1.1 dt_prev)  (device)
+//   fill(A, t)      stage 1: B = A + dt L(A)
+//   fill(B, t+dt)   stage 2: C = 3/4 A + 1/4 (B + dt L(B))
+//   fill(C, t+dt/2) stage 3: A = 1/3 A + 2/3 (C + dt L(C))   + CFLmin of the new A
+//   k_step_end            t += dt
+// which is the Shu-Osher form of the SSP-RK3 that AmrLevel::RK(3, ...) runs
+// (Source/Advance.cpp:141-148), with the stage times AMReX's RK3 fills ghosts
+// at (t, t+dt, t+dt/2).
+//
+// Ghost fill = same-level exchange (incl. periodic images; AMReX FillBoundary)
+// followed by one pass per direction over the ghost cells outside the domain,
+// x then y then z, applying the BC types of Source/Setup.cpp:17-92 per
+// component and then the case functor (e.g. Exec/1_DMR/prob_bcfill.cpp).
+// Pass d covers cells outside the domain in d, the grown range in directions
+// before d and the in-domain range in directions after d, so edges and corners
+// are filled from values set by earlier passes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ocfd_internal.h"
+#include "rhs_regular.h"
+
+namespace ocfd {
+
+constexpr int NGR = OCFD_NUM_GROW;
+
+struct FabGeom {
+    int lo[3], hi[3];  // valid box
+    long long off;     // element offset of the FAB in a state buffer
+    int g[3];          // grown extents
+    long long ns;      // component stride
+};
+
+struct ExTag {
+    int dst, src;
+    int lo[3], hi[3];  // region, absolute cell indices of the destination
+    int shift[3];      // src cell = dst cell + shift
+};
+
+struct BcTag {
+    int box, side;
+    int lo[3], hi[3];
+};
+
+struct StepState {
+    double time, dt, dt_prev, cfl;
+    unsigned long long cfl_min;
+};
+
+struct BcInfo {
+    int lo_bc[3], hi_bc[3];
+    int dom_lo[3], dom_hi[3];
+    double dx[3], prob_lo[3];
+    int bc_case;
+    double params[16];
+};
+
+__device__ __forceinline__ long long fab_index(const FabGeom& f, int i, int j, int k) {
+    return f.off + (long long)(i - f.lo[0] + NGR) + (long long)(j - f.lo[1] + NGR) * f.g[0] +
+           (long long)(k - f.lo[2] + NGR) * f.g[0] * f.g[1];
+}
+
+template <class Tag>
+__device__ __forceinline__ int find_tag(const long long* start, int ntag, long long idx) {
+    int lo = 0, hi = ntag - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= idx) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void region_cell(const int* lo, const int* hi, long long local, int& i,
+                                            int& j, int& k) {
+    const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
+    i = lo[0] + (int)(local % nx);
+    j = lo[1] + (int)((local / nx) % ny);
+    k = lo[2] + (int)(local / (nx * ny));
+}
+
+__global__ void k_exchange(const ExTag* __restrict__ tags, const long long* __restrict__ start,
+                           int ntag, long long total, const FabGeom* __restrict__ fabs, double* U,
+                           int ncomp) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<ExTag>(start, ntag, idx);
+        const ExTag& T = tags[t];
+        int i, j, k;
+        region_cell(T.lo, T.hi, idx - start[t], i, j, k);
+        const FabGeom& fd = fabs[T.dst];
+        const FabGeom& fs = fabs[T.src];
+        const long long d = fab_index(fd, i, j, k);
+        const long long s = fab_index(fs, i + T.shift[0], j + T.shift[1], k + T.shift[2]);
+        for (int n = 0; n < ncomp; ++n) U[d + n * fd.ns] = U[s + n * fs.ns];
+    }
+}
+
+// BC type codes (AMReX BCType): int_dir 0, ext_dir 1, foextrap 2, reflect_even 3, reflect_odd 4
+__device__ __forceinline__ int bc_type(int phys, int comp, int d) {
+    // Source/Setup.cpp:22-35 tables, rows Interior..NoSlipWall
+    const int scalar[6] = {0, 1, 2, 3, 3, 3};
+    const int normal[6] = {0, 1, 2, 4, 4, 4};
+    const int tang[6] = {0, 1, 2, 3, 3, 4};
+    if (comp >= 1 && comp <= 3) return (comp - 1 == d) ? normal[phys] : tang[phys];
+    return scalar[phys];
+}
+
+// Exec/1_DMR/prob_bcfill.cpp:14-58 (x0 uses sin(pi/3) for amrex::Math::sinpi(1/3))
+__device__ void dmr_functor(const BcInfo& bc, double* U, const FabGeom& f, long long c, int i,
+                            int j, int k, int ncomp, double time) {
+    const double x = bc.prob_lo[0] + (i + 0.5) * bc.dx[0];
+    const double x0 = 1.0 / 6.0 + sqrt(1 / 3.0) + time * 10.0 / sin(3.14159265358979323846 * (1.0 / 3.0));
+    const double* left = bc.params;
+    const double* right = bc.params + 5;
+    if (bc.hi_bc[1] == OCFD_BC_INFLOW && j > bc.dom_hi[1]) {
+        const double* st = x < x0 ? left : right;
+        for (int n = 0; n < ncomp && n < 5; ++n) U[c + n * f.ns] = st[n];
+    }
+    if ((bc.lo_bc[1] == 3 || bc.lo_bc[1] == 4 || bc.lo_bc[1] == 5) && j < bc.dom_lo[1]) {
+        if (x < 1.0 / 6.0)
+            for (int n = 0; n < ncomp && n < 5; ++n) U[c + n * f.ns] = left[n];
+    }
+    if (bc.lo_bc[0] == OCFD_BC_INFLOW && i < bc.dom_lo[0])
+        for (int n = 0; n < ncomp && n < 5; ++n) U[c + n * f.ns] = left[n];
+}
+
+template <int D>
+__global__ void k_physbc(const BcTag* __restrict__ tags, const long long* __restrict__ start,
+                         int ntag, long long total, const FabGeom* __restrict__ fabs, double* U,
+                         int ncomp, BcInfo bc, const StepState* st, double tfrac) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<BcTag>(start, ntag, idx);
+        const BcTag& T = tags[t];
+        int c3[3];
+        region_cell(T.lo, T.hi, idx - start[t], c3[0], c3[1], c3[2]);
+        const FabGeom& f = fabs[T.box];
+        const long long c = fab_index(f, c3[0], c3[1], c3[2]);
+        const int phys = T.side == 0 ? bc.lo_bc[D] : bc.hi_bc[D];
+        for (int n = 0; n < ncomp; ++n) {
+            const int ty = bc_type(phys, n, D);
+            int s3[3] = {c3[0], c3[1], c3[2]};
+            double sign = 1.0;
+            if (ty == 2) {
+                s3[D] = T.side == 0 ? bc.dom_lo[D] : bc.dom_hi[D];
+            } else if (ty == 3 || ty == 4) {
+                s3[D] = T.side == 0 ? 2 * bc.dom_lo[D] - 1 - c3[D] : 2 * bc.dom_hi[D] + 1 - c3[D];
+                if (ty == 4) sign = -1.0;
+            } else {
+                continue;  // ext_dir: the case functor sets it; int_dir: exchange did
+            }
+            U[c + n * f.ns] = sign * U[fab_index(f, s3[0], s3[1], s3[2]) + n * f.ns];
+        }
+        if (bc.bc_case == OCFD_CASE_DMR) {
+            const double time = st->time + tfrac * st->dt;
+            dmr_functor(bc, U, f, c, c3[0], c3[1], c3[2], ncomp, time);
+        } else if (bc.bc_case == OCFD_CASE_INFLOW) {
+            if ((T.side == 0 ? bc.lo_bc[D] : bc.hi_bc[D]) == OCFD_BC_INFLOW)
+                for (int n = 0; n < ncomp && n < 5; ++n) U[c + n * f.ns] = bc.params[n];
+        }
+    }
+}
+
+__global__ void k_estdt(const FabGeom* __restrict__ fabs, const long long* __restrict__ start,
+                        int nbox, long long total, const double* __restrict__ U, DevParm P,
+                        double dx0, double dx1, double dx2, unsigned long long* out) {
+    const double dx[3] = {dx0, dx1, dx2};
+    double m = __longlong_as_double(0x7FF0000000000000LL);
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = find_tag<FabGeom>(start, nbox, idx);
+        const FabGeom& f = fabs[b];
+        int i, j, k;
+        region_cell(f.lo, f.hi, idx - start[b], i, j, k);
+        const long long c = fab_index(f, i, j, k);
+        double u[5];
+        for (int n = 0; n < 5; ++n) u[n] = U[c + n * f.ns];
+        double v = cfl_bound(P, u, dx);
+        m = v < m ? v : m;
+    }
+    block_min_atomic(m, out);
+}
+
+__global__ void k_step_begin(StepState* st) {
+    const double est = __longlong_as_double((long long)st->cfl_min);
+    double dt = st->cfl * est;
+    if (st->dt_prev > 0 && dt > 1.1 * st->dt_prev) dt = 1.1 * st->dt_prev;
+    st->dt = dt;
+    st->cfl_min = 0x7FF0000000000000ULL;
+}
+
+__global__ void k_step_end(StepState* st) {
+    st->time += st->dt;
+    st->dt_prev = st->dt;
+}
+
+__global__ void k_reset_cfl(StepState* st) { st->cfl_min = 0x7FF0000000000000ULL; }
+
+__global__ void k_set_time(StepState* st, double t) {
+    st->time = t;
+    st->dt = 0;
+    st->dt_prev = -1.0;
+    st->cfl_min = 0x7FF0000000000000ULL;
+}
+
+static int grid_for(long long total, int threads, int sms) {
+    long long b = (total + threads - 1) / threads;
+    long long cap = (long long)sms * 16;
+    return (int)std::max<long long>(1, std::min(b, cap));
+}
+
+}  // namespace ocfd
+
+using namespace ocfd;
+
+struct ocfd_level {
+    ocfd_context* ctx = nullptr;
+    ocfd_level_desc desc{};
+    std::vector<ocfd_box> boxes;
+    std::vector<FabGeom> fabs;
+    long long elems = 0;      // per state buffer
+    int ncomp = 5;
+    double* buf[3] = {nullptr, nullptr, nullptr};
+    FabGeom* d_fabs = nullptr;
+    long long* d_cell_start = nullptr;
+    long long ncells = 0;
+    // exchange
+    ExTag* d_ex = nullptr;
+    long long* d_ex_start = nullptr;
+    int nex = 0;
+    long long ex_total = 0;
+    // physical BC passes
+    BcTag* d_bc[3] = {nullptr, nullptr, nullptr};
+    long long* d_bc_start[3] = {nullptr, nullptr, nullptr};
+    int nbc[3] = {0, 0, 0};
+    long long bc_total[3] = {0, 0, 0};
+    BcInfo bcinfo{};
+    // RHS stage tables (3 stages)
+    int tile = 0;
+    RegBoxArgs* d_stage[3] = {nullptr, nullptr, nullptr};
+    int* d_tile_start = nullptr;
+    int ntiles = 0;
+    StepState* d_step = nullptr;
+    bool need_estdt = true;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    unsigned graph_flags = ~0u;
+    double graph_cfl = -1;
+};
+
+namespace ocfd {
+
+template <class T>
+static ocfd_status upload(T** dptr, const std::vector<T>& v) {
+    size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
+    if (cudaMalloc(dptr, bytes) != cudaSuccess) return fail(OCFD_OUT_OF_MEMORY, "level table allocation");
+    if (!v.empty() && cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(OCFD_LAUNCH_FAIL, "level table upload");
+    return OCFD_OK;
+}
+
+static bool intersect(const int* alo, const int* ahi, const int* blo, const int* bhi, int* lo, int* hi) {
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = std::max(alo[d], blo[d]);
+        hi[d] = std::min(ahi[d], bhi[d]);
+        if (lo[d] > hi[d]) return false;
+    }
+    return true;
+}
+
+static long long region_cells(const int* lo, const int* hi) {
+    return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+}
+
+// Exchange tags: ghost cells of box b inside the (periodically extended) domain
+// that lie in the valid region of box s (s may equal b for periodic images).
+static void build_exchange(ocfd_level* L, std::vector<ExTag>& tags) {
+    const ocfd_box& dom = L->desc.domain;
+    int period[3];
+    for (int d = 0; d < 3; ++d) period[d] = dom.hi[d] - dom.lo[d] + 1;
+    const int nb = (int)L->boxes.size();
+    for (int b = 0; b < nb; ++b) {
+        const ocfd_box& B = L->boxes[b];
+        int glo[3], ghi[3];
+        for (int d = 0; d < 3; ++d) { glo[d] = B.lo[d] - NGR; ghi[d] = B.hi[d] + NGR; }
+        for (int sx = -1; sx <= 1; ++sx)
+            for (int sy = -1; sy <= 1; ++sy)
+                for (int sz = -1; sz <= 1; ++sz) {
+                    const int sh[3] = {sx, sy, sz};
+                    bool ok = true;
+                    for (int d = 0; d < 3; ++d)
+                        if (sh[d] != 0 && L->desc.lo_bc[d] != OCFD_BC_INTERIOR) ok = false;
+                    if (!ok) continue;
+                    for (int s = 0; s < nb; ++s) {
+                        const ocfd_box& Sb = L->boxes[s];
+                        // image of Sb shifted by sh * period
+                        int ilo[3], ihi[3];
+                        for (int d = 0; d < 3; ++d) {
+                            ilo[d] = Sb.lo[d] + sh[d] * period[d];
+                            ihi[d] = Sb.hi[d] + sh[d] * period[d];
+                        }
+                        int lo[3], hi[3];
+                        if (!intersect(glo, ghi, ilo, ihi, lo, hi)) continue;
+                        if (s == b && sx == 0 && sy == 0 && sz == 0) continue;  // own valid cells
+                        // split the intersection into the parts outside box b's valid region:
+                        // the region minus B, as up to 6 slabs
+                        int rlo[3] = {lo[0], lo[1], lo[2]}, rhi[3] = {hi[0], hi[1], hi[2]};
+                        for (int d = 0; d < 3; ++d) {
+                            if (rlo[d] < B.lo[d]) {
+                                ExTag t{};
+                                t.dst = b; t.src = s;
+                                for (int e = 0; e < 3; ++e) { t.lo[e] = rlo[e]; t.hi[e] = rhi[e]; t.shift[e] = -sh[e] * period[e]; }
+                                t.hi[d] = std::min(rhi[d], B.lo[d] - 1);
+                                tags.push_back(t);
+                                rlo[d] = B.lo[d];
+                            }
+                            if (rhi[d] > B.hi[d]) {
+                                ExTag t{};
+                                t.dst = b; t.src = s;
+                                for (int e = 0; e < 3; ++e) { t.lo[e] = rlo[e]; t.hi[e] = rhi[e]; t.shift[e] = -sh[e] * period[e]; }
+                                t.lo[d] = std::max(rlo[d], B.hi[d] + 1);
+                                tags.push_back(t);
+                                rhi[d] = B.hi[d];
+                            }
+                            if (rlo[d] > rhi[d]) break;
+                        }
+                    }
+                }
+    }
+}
+
+// Physical-boundary tags of pass d for every box whose grown region leaves the domain in d.
+static void build_physbc(ocfd_level* L, int d, std::vector<BcTag>& tags) {
+    const ocfd_box& dom = L->desc.domain;
+    if (L->desc.lo_bc[d] == OCFD_BC_INTERIOR) return;  // periodic: exchange fills it
+    for (int b = 0; b < (int)L->boxes.size(); ++b) {
+        const ocfd_box& B = L->boxes[b];
+        for (int side = 0; side < 2; ++side) {
+            BcTag t{};
+            t.box = b;
+            t.side = side;
+            for (int e = 0; e < 3; ++e) {
+                t.lo[e] = B.lo[e] - NGR;
+                t.hi[e] = B.hi[e] + NGR;
+                if (e > d && L->desc.lo_bc[e] != OCFD_BC_INTERIOR) {
+                    t.lo[e] = std::max(t.lo[e], dom.lo[e]);
+                    t.hi[e] = std::min(t.hi[e], dom.hi[e]);
+                }
+            }
+            if (side == 0) t.hi[d] = std::min(t.hi[d], dom.lo[d] - 1);
+            else t.lo[d] = std::max(t.lo[d], dom.hi[d] + 1);
+            bool empty = false;
+            for (int e = 0; e < 3; ++e) empty = empty || t.lo[e] > t.hi[e];
+            if (!empty) tags.push_back(t);
+        }
+    }
+}
+
+template <class Tag>
+static ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** d_start,
+                               long long* total) {
+    std::vector<long long> start(tags.size());
+    long long acc = 0;
+    for (size_t i = 0; i < tags.size(); ++i) {
+        start[i] = acc;
+        acc += region_cells(tags[i].lo, tags[i].hi);
+    }
+    *total = acc;
+    ocfd_status s = upload(d_tags, tags);
+    if (s != OCFD_OK) return s;
+    return upload(d_start, start);
+}
+
+static ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st) {
+    const int sms = L->ctx->num_sms;
+    if (L->ex_total > 0) {
+        k_exchange<<<grid_for(L->ex_total, 256, sms), 256, 0, st>>>(L->d_ex, L->d_ex_start, L->nex,
+                                                                    L->ex_total, L->d_fabs, U, L->ncomp);
+    }
+    if (L->bc_total[0] > 0)
+        k_physbc<0><<<grid_for(L->bc_total[0], 256, sms), 256, 0, st>>>(
+            L->d_bc[0], L->d_bc_start[0], L->nbc[0], L->bc_total[0], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
+    if (L->bc_total[1] > 0)
+        k_physbc<1><<<grid_for(L->bc_total[1], 256, sms), 256, 0, st>>>(
+            L->d_bc[1], L->d_bc_start[1], L->nbc[1], L->bc_total[1], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
+    if (L->bc_total[2] > 0)
+        k_physbc<2><<<grid_for(L->bc_total[2], 256, sms), 256, 0, st>>>(
+            L->d_bc[2], L->d_bc_start[2], L->nbc[2], L->bc_total[2], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
+    return check_launch("level ghost fill");
+}
+
+static ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st) {
+    const int sms = L->ctx->num_sms;
+    k_reset_cfl<<<1, 1, 0, st>>>(L->d_step);
+    k_estdt<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(
+        L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->buf[0], L->ctx->parm,
+        L->desc.dx[0], L->desc.dx[1], L->desc.dx[2], &L->d_step->cfl_min);
+    return check_launch("level estdt");
+}
+
+static ocfd_status record_step(ocfd_level* L, unsigned flags, cudaStream_t st) {
+    const bool visc = flags & OCFD_VISC;
+    k_step_begin<<<1, 1, 0, st>>>(L->d_step);
+    const double tfrac[3] = {0.0, 1.0, 0.5};
+    const int src[3] = {0, 1, 2};
+    for (int s = 0; s < 3; ++s) {
+        ocfd_status r = fill_ghosts(L, L->buf[src[s]], tfrac[s], st);
+        if (r != OCFD_OK) return r;
+        RegBoxArgs dummy{};
+        r = (flags & OCFD_FLUX_FP32)
+                ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[s], L->d_tile_start,
+                                         (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st)
+                : launch_rhs_regular(L->tile, visc, L->d_stage[s], L->d_tile_start,
+                                     (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st);
+        if (r != OCFD_OK) return r;
+    }
+    k_step_end<<<1, 1, 0, st>>>(L->d_step);
+    return check_launch("level step");
+}
+
+}  // namespace ocfd
+
+extern "C" {
+
+ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, ocfd_level** out) {
+    if (!ctx || !desc || !out || desc->nbox <= 0 || !desc->boxes)
+        return fail(OCFD_BAD_ARG, "ocfd_level_create: bad arguments");
+    *out = nullptr;
+    for (int d = 0; d < 3; ++d) {
+        if ((desc->lo_bc[d] == OCFD_BC_INTERIOR) != (desc->hi_bc[d] == OCFD_BC_INTERIOR))
+            return fail(OCFD_BAD_ARG, "ocfd_level_create: periodic directions need interior BC on both sides");
+        if (desc->lo_bc[d] < 0 || desc->lo_bc[d] > 5 || desc->hi_bc[d] < 0 || desc->hi_bc[d] > 5)
+            return fail(OCFD_BAD_ARG, "ocfd_level_create: BC codes are 0..5");
+        if (!(desc->dx[d] > 0)) return fail(OCFD_BAD_ARG, "ocfd_level_create: dx must be positive");
+    }
+    ocfd_level* L = new ocfd_level();
+    L->ctx = ctx;
+    L->desc = *desc;
+    L->boxes.assign(desc->boxes, desc->boxes + desc->nbox);
+    L->desc.boxes = nullptr;
+    long long off = 0;
+    std::vector<long long> cell_start;
+    for (const ocfd_box& B : L->boxes) {
+        FabGeom f{};
+        for (int d = 0; d < 3; ++d) {
+            if (B.hi[d] < B.lo[d] || B.lo[d] < desc->domain.lo[d] || B.hi[d] > desc->domain.hi[d]) {
+                delete L;
+                return fail(OCFD_BAD_ARG, "ocfd_level_create: box outside the domain or empty");
+            }
+            f.lo[d] = B.lo[d];
+            f.hi[d] = B.hi[d];
+            f.g[d] = B.hi[d] - B.lo[d] + 1 + 2 * NGR;
+        }
+        f.ns = (long long)f.g[0] * f.g[1] * f.g[2];
+        f.off = off;
+        off += f.ns * L->ncomp;
+        cell_start.push_back(L->ncells);
+        L->ncells += region_cells(f.lo, f.hi);
+        L->fabs.push_back(f);
+    }
+    L->elems = off;
+    for (int i = 0; i < 3; ++i) {
+        if (cudaMalloc(&L->buf[i], sizeof(double) * L->elems) != cudaSuccess) {
+            cudaGetLastError();
+            ocfd_level_destroy(L);
+            return fail(OCFD_OUT_OF_MEMORY, "ocfd_level_create: state buffers");
+        }
+        cudaMemset(L->buf[i], 0, sizeof(double) * L->elems);
+    }
+    ocfd_status s = upload(&L->d_fabs, L->fabs);
+    if (s == OCFD_OK) s = upload(&L->d_cell_start, cell_start);
+    std::vector<ExTag> ex;
+    build_exchange(L, ex);
+    L->nex = (int)ex.size();
+    if (s == OCFD_OK) s = upload_tags(ex, &L->d_ex, &L->d_ex_start, &L->ex_total);
+    for (int d = 0; d < 3 && s == OCFD_OK; ++d) {
+        std::vector<BcTag> bt;
+        build_physbc(L, d, bt);
+        L->nbc[d] = (int)bt.size();
+        s = upload_tags(bt, &L->d_bc[d], &L->d_bc_start[d], &L->bc_total[d]);
+    }
+    for (int d = 0; d < 3; ++d) {
+        L->bcinfo.lo_bc[d] = desc->lo_bc[d];
+        L->bcinfo.hi_bc[d] = desc->hi_bc[d];
+        L->bcinfo.dom_lo[d] = desc->domain.lo[d];
+        L->bcinfo.dom_hi[d] = desc->domain.hi[d];
+        L->bcinfo.dx[d] = desc->dx[d];
+        L->bcinfo.prob_lo[d] = desc->prob_lo[d];
+    }
+    L->bcinfo.bc_case = desc->bc_case;
+    std::memcpy(L->bcinfo.params, desc->case_params, sizeof(L->bcinfo.params));
+    // RHS tile: the shape with the least padded work summed over the boxes
+    if (desc->tile >= 0 && desc->tile < kNumRegularTiles) {
+        L->tile = desc->tile;
+    } else {
+        double best = 1e300;
+        for (int t = 0; t < kNumRegularTiles; ++t) {
+            if (!regular_tile_fits(t, true)) continue;
+            const TileShape& ts = kRegularTiles[t];
+            double cost = 0;
+            for (const ocfd_box& B : L->boxes) {
+                const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
+                long long tiles = (long long)((n[0] + ts.x - 1) / ts.x) * ((n[1] + ts.y - 1) / ts.y) * ((n[2] + ts.z - 1) / ts.z);
+                cost += tiles * ((double)ts.x * ts.y * ts.z * 3.0 + 6.0 * ((double)ts.y * ts.z + (double)ts.x * ts.z + (double)ts.x * ts.y));
+            }
+            if (cost < best * 0.999) { best = cost; L->tile = t; }
+        }
+    }
+    // stage tables: stage 1 A -> B, stage 2 (A, B) -> C, stage 3 (A, C) -> A
+    const double dxinv[3] = {1.0 / desc->dx[0], 1.0 / desc->dx[1], 1.0 / desc->dx[2]};
+    std::vector<int> tile_start;
+    int nt = 0;
+    std::vector<RegBoxArgs> st[3];
+    if (s == OCFD_OK && cudaMalloc(&L->d_step, sizeof(StepState)) != cudaSuccess) s = fail(OCFD_OUT_OF_MEMORY, "step state");
+    for (size_t b = 0; b < L->boxes.size() && s == OCFD_OK; ++b) {
+        const FabGeom& f = L->fabs[b];
+        ocfd_array4 a[3];
+        for (int i = 0; i < 3; ++i) {
+            a[i].p = L->buf[i] + f.off;
+            a[i].jstride = f.g[0];
+            a[i].kstride = (long long)f.g[0] * f.g[1];
+            a[i].nstride = f.ns;
+            for (int d = 0; d < 3; ++d) {
+                a[i].begin[d] = f.lo[d] - NGR;
+                a[i].end[d] = f.hi[d] + NGR + 1;
+            }
+            a[i].ncomp = L->ncomp;
+        }
+        const int S_of[3] = {0, 1, 2}, O_of[3] = {1, 2, 0};
+        const double ra[3] = {0.0, 0.75, 1.0 / 3.0}, rb[3] = {1.0, 0.25, 2.0 / 3.0};
+        for (int k = 0; k < 3; ++k) {
+            RegBoxArgs r{};
+            fill_regular_args(r, &a[S_of[k]], nullptr, nullptr, L->boxes[b], dxinv, L->tile);
+            r.mode = RHS_FUSED_STAGE;
+            r.U0 = view_of<const double>(&a[0]);
+            r.Uout = view_of<double>(&a[O_of[k]]);
+            r.rk_a = ra[k];
+            r.rk_b = rb[k];
+            r.dt_ptr = &L->d_step->dt;
+            r.cfl_min = k == 2 ? &L->d_step->cfl_min : nullptr;
+            for (int d = 0; d < 3; ++d) r.dx[d] = desc->dx[d];
+            st[k].push_back(r);
+            if (k == 0) {
+                tile_start.push_back(nt);
+                nt += r.ntile[0] * r.ntile[1] * r.ntile[2];
+            }
+        }
+    }
+    L->ntiles = nt;
+    for (int k = 0; k < 3 && s == OCFD_OK; ++k) s = upload(&L->d_stage[k], st[k]);
+    if (s == OCFD_OK) s = upload(&L->d_tile_start, tile_start);
+    if (s == OCFD_OK) {
+        k_set_time<<<1, 1>>>(L->d_step, 0.0);
+        s = check_launch("ocfd_level_create");
+        if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = fail(OCFD_LAUNCH_FAIL, "level setup");
+    }
+    if (s != OCFD_OK) {
+        ocfd_level_destroy(L);
+        return s;
+    }
+    *out = L;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_level_destroy(ocfd_level* L) {
+    if (!L) return OCFD_OK;
+    if (L->graph) cudaGraphExecDestroy(L->graph);
+    for (int i = 0; i < 3; ++i) {
+        cudaFree(L->buf[i]);
+        cudaFree(L->d_stage[i]);
+        cudaFree(L->d_bc[i]);
+        cudaFree(L->d_bc_start[i]);
+    }
+    cudaFree(L->d_fabs);
+    cudaFree(L->d_cell_start);
+    cudaFree(L->d_ex);
+    cudaFree(L->d_ex_start);
+    cudaFree(L->d_tile_start);
+    cudaFree(L->d_step);
+    delete L;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_level_state(ocfd_level* L, int ibox, ocfd_array4* out) {
+    if (!L || !out || ibox < 0 || ibox >= (int)L->boxes.size()) return fail(OCFD_BAD_ARG, "ocfd_level_state");
+    const FabGeom& f = L->fabs[ibox];
+    out->p = L->buf[0] + f.off;
+    out->jstride = f.g[0];
+    out->kstride = (long long)f.g[0] * f.g[1];
+    out->nstride = f.ns;
+    for (int d = 0; d < 3; ++d) {
+        out->begin[d] = f.lo[d] - NGR;
+        out->end[d] = f.hi[d] + NGR + 1;
+    }
+    out->ncomp = L->ncomp;
+    return OCFD_OK;
+}
+
+size_t ocfd_level_state_elems(const ocfd_level* L) { return L ? (size_t)L->elems : 0; }
+
+ocfd_status ocfd_level_copy_in(ocfd_level* L, const double* buf, void* stream) {
+    if (!L || !buf) return fail(OCFD_BAD_ARG, "ocfd_level_copy_in");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(L->buf[0], buf, sizeof(double) * L->elems, cudaMemcpyDefault, st) != cudaSuccess)
+        return check_launch("ocfd_level_copy_in");
+    L->need_estdt = true;
+    k_set_time<<<1, 1, 0, st>>>(L->d_step, 0.0);
+    return check_launch("ocfd_level_copy_in");
+}
+
+ocfd_status ocfd_level_copy_out(ocfd_level* L, double* buf, void* stream) {
+    if (!L || !buf) return fail(OCFD_BAD_ARG, "ocfd_level_copy_out");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(buf, L->buf[0], sizeof(double) * L->elems, cudaMemcpyDefault, st) != cudaSuccess)
+        return check_launch("ocfd_level_copy_out");
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_level_fill_ghosts(ocfd_level* L, double time, void* stream) {
+    if (!L) return fail(OCFD_BAD_ARG, "ocfd_level_fill_ghosts");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    k_set_time<<<1, 1, 0, st>>>(L->d_step, time);
+    ocfd_status s = fill_ghosts(L, L->buf[0], 0.0, st);
+    L->need_estdt = true;
+    return s;
+}
+
+ocfd_status ocfd_level_set_time(ocfd_level* L, double time, void* stream) {
+    if (!L) return fail(OCFD_BAD_ARG, "ocfd_level_set_time");
+    k_set_time<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(L->d_step, time);
+    L->need_estdt = true;
+    return check_launch("ocfd_level_set_time");
+}
+
+ocfd_status ocfd_level_advance(ocfd_level* L, int nsteps, double cfl, unsigned flags, void* stream) {
+    if (!L || nsteps < 0 || !(cfl > 0)) return fail(OCFD_BAD_ARG, "ocfd_level_advance");
+    if (flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32)) return fail(OCFD_BAD_ARG, "ocfd_level_advance: flags");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (nsteps == 0) return OCFD_OK;
+    if (cudaMemcpyAsync(&L->d_step->cfl, &cfl, sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return check_launch("ocfd_level_advance");
+    if (L->need_estdt) {
+        ocfd_status s = launch_estdt(L, st);
+        if (s != OCFD_OK) return s;
+        L->need_estdt = false;
+    }
+    if (!L->graph || L->graph_flags != flags) {
+        if (L->graph) {
+            cudaGraphExecDestroy(L->graph);
+            L->graph = nullptr;
+        }
+        // capture on a private stream so the caller's stream may be the legacy default
+        cudaStream_t cap;
+        if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return check_launch("capture stream");
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return check_launch("begin capture");
+        }
+        ocfd_status s = record_step(L, flags, cap);
+        cudaError_t e = cudaStreamEndCapture(cap, &g);
+        cudaStreamDestroy(cap);
+        if (s != OCFD_OK) return s;
+        if (e != cudaSuccess) return fail(OCFD_LAUNCH_FAIL, std::string("end capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&L->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(OCFD_LAUNCH_FAIL, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        L->graph_flags = flags;
+    }
+    for (int i = 0; i < nsteps; ++i)
+        if (cudaGraphLaunch(L->graph, st) != cudaSuccess) return check_launch("graph launch");
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_level_time(ocfd_level* L, double* time, double* last_dt, void* stream) {
+    if (!L) return fail(OCFD_BAD_ARG, "ocfd_level_time");
+    StepState h{};
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(&h, L->d_step, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return check_launch("ocfd_level_time");
+    if (time) *time = h.time;
+    if (last_dt) *last_dt = h.dt_prev;
+    return OCFD_OK;
+}
+
+}  // extern "C"

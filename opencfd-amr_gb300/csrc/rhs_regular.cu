@@ -57,6 +57,8 @@ __host__ __device__ constexpr int regular_smem_doubles() {
     return m + (VISC ? 4 * Ring<TX, TY, TZ>::N : 0);
 }
 
+constexpr size_t kMaxSmem = 227 * 1024;  // opt-in dynamic shared memory per CTA
+
 // Viscous stress and heat flux of the D-face between ring cells (r - e_D) and r,
 // Source/kernel/Diffusion.H:7-131.  ring holds u, v, w, T (4 planes of RN).
 template <int D, int TX, int TY, int TZ>
@@ -233,20 +235,27 @@ __global__ void __launch_bounds__(TX* TY* TZ)
 
     const int ti = threadIdx.x % TX, tj = (threadIdx.x / TX) % TY, tk = threadIdx.x / (TX * TY);
     const int ci = i0 + ti, cj = j0 + tj, ck = k0 + tk;
-    if (ci <= B.hi[0] && cj <= B.hi[1] && ck <= B.hi[2]) {
+    const bool valid = ci <= B.hi[0] && cj <= B.hi[1] && ck <= B.hi[2];
+    double local_dt = __longlong_as_double(0x7FF0000000000000LL);
+    if (valid) {
         if (B.mode == RHS_WRITE_DSDT) {
 #pragma unroll
             for (int n = 0; n < 5; ++n) B.dsdt(ci, cj, ck, n) = acc[n];
         } else {
             // fused Shu-Osher stage: U_out = a U0 + b (U_s + dt L(U_s))
+            const double dt = B.dt_ptr ? *B.dt_ptr : B.dt;
+            double un[5];
 #pragma unroll
             for (int n = 0; n < 5; ++n) {
                 double us = B.S(ci, cj, ck, n);
                 double u0 = B.U0(ci, cj, ck, n);
-                B.Uout(ci, cj, ck, n) = B.rk_a * u0 + B.rk_b * (us + B.dt * acc[n]);
+                un[n] = B.rk_a * u0 + B.rk_b * (us + dt * acc[n]);
+                B.Uout(ci, cj, ck, n) = un[n];
             }
+            if (B.cfl_min) local_dt = cfl_bound(P, un, B.dx);
         }
     }
+    if (B.cfl_min) block_min_atomic(local_dt, B.cfl_min);
 }
 
 template <int TX, int TY, int TZ, bool VISC>
@@ -256,14 +265,52 @@ static ocfd_status launch_t(const RegBoxArgs* d_boxes, const int* d_tile_start, 
     constexpr int NT = TX * TY * TZ;
     constexpr size_t smem = sizeof(double) * regular_smem_doubles<TX, TY, TZ, VISC>();
     auto kern = k_rhs_regular<TX, TY, TZ, VISC>;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured = true;
-    }
+    if (smem > kMaxSmem) return fail(OCFD_BAD_ARG, "regular RHS tile does not fit shared memory in this mode");
     if (ntiles <= 0) return OCFD_OK;
     kern<<<ntiles, NT, smem, st>>>(d_boxes, d_tile_start, nbox, single, P);
     return check_launch("k_rhs_regular");
+}
+
+template <int TX, int TY, int TZ, bool VISC>
+static bool configure_one() {
+    const size_t smem = sizeof(double) * regular_smem_doubles<TX, TY, TZ, VISC>();
+    if (smem > kMaxSmem) return true;  // shape not offered in this mode
+    return cudaFuncSetAttribute(k_rhs_regular<TX, TY, TZ, VISC>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+}
+
+template <int TX, int TY, int TZ>
+static bool configure_t() {
+    return configure_one<TX, TY, TZ, false>() && configure_one<TX, TY, TZ, true>();
+}
+
+// Raises the dynamic shared-memory limit of every regular-RHS instantiation;
+// called once per context, outside any stream capture.
+ocfd_status configure_rhs_regular() {
+    bool ok = configure_t<8, 8, 8>() && configure_t<8, 8, 4>() && configure_t<16, 8, 4>() &&
+              configure_t<16, 16, 2>() && configure_t<32, 8, 2>() && configure_t<16, 8, 2>();
+    if (!ok) return check_launch("configure_rhs_regular");
+    return OCFD_OK;
+}
+
+template <int TX, int TY, int TZ>
+static size_t smem_t(bool visc) {
+    return visc ? sizeof(double) * regular_smem_doubles<TX, TY, TZ, true>()
+                : sizeof(double) * regular_smem_doubles<TX, TY, TZ, false>();
+}
+
+bool regular_tile_fits(int tile, bool visc) {
+    size_t b = 0;
+    switch (tile) {
+        case 0: b = smem_t<8, 8, 8>(visc); break;
+        case 1: b = smem_t<8, 8, 4>(visc); break;
+        case 2: b = smem_t<16, 8, 4>(visc); break;
+        case 3: b = smem_t<16, 16, 2>(visc); break;
+        case 4: b = smem_t<32, 8, 2>(visc); break;
+        case 5: b = smem_t<16, 8, 2>(visc); break;
+        default: return false;
+    }
+    return b <= kMaxSmem;
 }
 
 const TileShape kRegularTiles[] = {{8, 8, 8}, {8, 8, 4}, {16, 8, 4}, {16, 16, 2}, {32, 8, 2}, {16, 8, 2}};
@@ -289,10 +336,11 @@ ocfd_status launch_rhs_regular(int tile, bool visc, const RegBoxArgs* d_boxes,
 }
 
 // Default tile for a box: the shape with the least padded work.
-int pick_regular_tile(const int n[3]) {
-    int best = 0;
+int pick_regular_tile(const int n[3], bool visc) {
+    int best = 1;
     double best_cost = 1e300;
     for (int t = 0; t < kNumRegularTiles; ++t) {
+        if (!regular_tile_fits(t, visc)) continue;
         const TileShape& s = kRegularTiles[t];
         long long tiles = (long long)((n[0] + s.x - 1) / s.x) * ((n[1] + s.y - 1) / s.y) *
                           ((n[2] + s.z - 1) / s.z);
@@ -324,6 +372,8 @@ void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* d
     const int T[3] = {s.x, s.y, s.z};
     for (int d = 0; d < 3; ++d) a.ntile[d] = (bx.hi[d] - bx.lo[d] + T[d]) / T[d];
     a.mode = RHS_WRITE_DSDT;
+    a.dt_ptr = nullptr;
+    a.cfl_min = nullptr;
 }
 
 }  // namespace ocfd
@@ -347,7 +397,7 @@ extern "C" ocfd_status ocfd_rhs_regular_box_f64(ocfd_context* ctx, const ocfd_ar
         return fail(OCFD_BAD_ARG, "ocfd_rhs_regular_box_f64: unknown flags");
     if (flags & OCFD_FLUX_FP32) return rhs_regular_box_f32(ctx, S, dSdt, flux, bx, dxinv, flags, stream);
     const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
-    const int tile = pick_regular_tile(n);
+    const int tile = pick_regular_tile(n, (flags & OCFD_VISC) != 0);
     RegBoxArgs a{};
     fill_regular_args(a, S, dSdt, flux, bx, dxinv, tile);
     const int ntiles = a.ntile[0] * a.ntile[1] * a.ntile[2];

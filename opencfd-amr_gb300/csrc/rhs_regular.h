@@ -26,13 +26,58 @@ struct RegBoxArgs {
     double dxinv[3];
     int ntile[3];
     int mode;
-    // RHS_FUSED_STAGE: Uout = rk_a * U0 + rk_b * (S + dt * L(S)) over the box
+    // RHS_FUSED_STAGE: Uout = rk_a * U0 + rk_b * (S + dt * L(S)) over the box,
+    // dt read from *dt_ptr when set (device-resident step size)
     View<const double> U0;
     View<double> Uout;
     double rk_a, rk_b, dt;
+    const double* dt_ptr;
+    // optional CFL reduction over the new state (Source/Advance.cpp:10-59):
+    // atomicMin of min(dx_d / (|u_d| + c)) as ordered double bits
+    unsigned long long* cfl_min;
+    double dx[3];
 };
 
-int pick_regular_tile(const int n[3]);
+// CFL bound dx/(|u|+c) of one conserved state, Source/Advance.cpp:26-49
+__device__ __forceinline__ double cfl_bound(const DevParm& P, const double* u, const double* dx) {
+    double rho = u[0];
+    double rhoinv = 1.0 / (rho > P.smallr ? rho : P.smallr);
+    double vx = u[1] * rhoinv, vy = u[2] * rhoinv, vz = u[3] * rhoinv;
+    double pe = (P.gamma - 1.0) * (u[4] - 0.5 * rho * (vx * vx + vy * vy + vz * vz));
+    double p = pe > P.smallp ? pe : P.smallp;
+    double cs = sqrt(P.gamma * p * rhoinv);
+    double dtx = dx[0] / (fabs(vx) + cs);
+    double dty = dx[1] / (fabs(vy) + cs);
+    double dtz = dx[2] / (fabs(vz) + cs);
+    double m = dty < dtz ? dty : dtz;
+    return dtx < m ? dtx : m;
+}
+
+// block-wide min of v (all threads participate), one atomicMin per block
+__device__ __forceinline__ void block_min_atomic(double v, unsigned long long* target) {
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? red[lane] : __longlong_as_double(0x7FF0000000000000LL);
+        for (int o = 16; o > 0; o >>= 1) {
+            double w = __shfl_xor_sync(0xffffffffu, v, o);
+            v = w < v ? w : v;
+        }
+        if (lane == 0 && v >= 0.0) atomicMin(target, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+int pick_regular_tile(const int n[3], bool visc);
+bool regular_tile_fits(int tile, bool visc);
+ocfd_status configure_rhs_regular();
+ocfd_status configure_rhs_regular_f32();
 void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* dSdt,
                        const ocfd_array4* flux, const ocfd_box& bx, const double dxinv[3],
                        int tile);

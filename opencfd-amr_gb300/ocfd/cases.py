@@ -1,0 +1,57 @@
+"""Initial conditions and boundary setups of the benchmark configurations
+(fixtures; Exec/<case>/prob.H restated), on a global grown array
+(5, Nz+8, Ny+8, Nx+8) whose first cell is (-4, -4, -4)."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+NG = 4
+GAMMA = 1.4
+
+
+def _centres(n, dx, prob_lo):
+    return [prob_lo[d] + (np.arange(-NG, n[d] + NG) + 0.5) * dx[d] for d in range(3)]
+
+
+def sod(nx=512, ny=64, nz=4, gamma=GAMMA):
+    """2D Sod shock tube on [0,1] x [0,0.125] as a thin slab (Exec/0_SOD/prob.H:13-38,
+    prob_parm.H:9-12).  BCs of Exec/0_SOD/inputs:15-16: x outflow, y and z slip walls."""
+    dx = 1.0 / nx
+    n = (nx, ny, nz)
+    x, _, _ = _centres(n, (dx, dx, dx), (0.0, 0.0, 0.0))
+    G = np.zeros((5, nz + 2 * NG, ny + 2 * NG, nx + 2 * NG))
+    left = x < 0.5
+    rho = np.where(left, 1.0, 0.125)
+    p = np.where(left, 1.0, 0.1)
+    G[0] = rho[None, None, :]
+    G[4] = (p / (gamma - 1.0))[None, None, :]
+    return dict(G=G, n=n, dx=(dx, dx, dx), prob_lo=(0.0, 0.0, 0.0),
+                lo_bc=(2, 4, 4), hi_bc=(2, 4, 4), bc_case=0, case_params=())
+
+
+def dmr_states(gamma=GAMMA):
+    """Post-shock (left) and pre-shock (right) conserved states, Exec/1_DMR/prob_parm.H:10-17."""
+    rl, pl = 8.0, 116.5
+    ul, vl = 8.25 * math.cos(math.pi / 6.0), -8.25 * math.sin(math.pi / 6.0)
+    rr, pr = 1.4, 1.0
+    left = [rl, rl * ul, rl * vl, 0.0, pl / (gamma - 1.0) + 0.5 * rl * (ul * ul + vl * vl)]
+    right = [rr, 0.0, 0.0, 0.0, pr / (gamma - 1.0)]
+    return left, right
+
+
+def dmr(nx=1024, ny=256, nz=2, gamma=GAMMA, Lx=4.0):
+    """Double Mach reflection on [0,4] x [0,1] (Exec/1_DMR/prob.H:11-46), thin in z.
+    BCs of Exec/1_DMR/inputs:15-16: x inflow/outflow, y slip wall / inflow, z outflow."""
+    dx = Lx / nx
+    n = (nx, ny, nz)
+    x, y, _ = _centres(n, (dx, dx, dx), (0.0, 0.0, 0.0))
+    left, right = dmr_states(gamma)
+    X, Y = np.meshgrid(x, y, indexing="xy")          # (ny+8, nx+8)
+    post = X < 1.0 / 6.0 + math.sqrt(1 / 3.0) * Y
+    G = np.zeros((5, nz + 2 * NG, ny + 2 * NG, nx + 2 * NG))
+    for c in range(5):
+        G[c] = np.where(post, left[c], right[c])[None]
+    return dict(G=G, n=n, dx=(dx, dx, dx), prob_lo=(0.0, 0.0, 0.0),
+                lo_bc=(1, 4, 2), hi_bc=(2, 1, 2), bc_case=1, case_params=tuple(left) + tuple(right))

@@ -1413,7 +1413,8 @@ static void dmr_fill(const ocfdo_bc* bc, double* S, long long N, const box_t* b,
         const double* st = x < x0 ? bc->dmr_left : bc->dmr_right;
         for (int n = 0; n < ncomp; ++n) S[n * N + c] = st[n];
     }
-    if (bc->lo_bc[1] == 4 && aj < 0) {
+    /* scalar BC of the y-lo face is reflect_even for phys codes 3, 4, 5 (Source/Setup.cpp:22-25) */
+    if ((bc->lo_bc[1] == 3 || bc->lo_bc[1] == 4 || bc->lo_bc[1] == 5) && aj < 0) {
         if (x < 1.0 / 6.0)
             for (int n = 0; n < ncomp; ++n) S[n * N + c] = bc->dmr_left[n];
     }

@@ -1,0 +1,126 @@
+"""Level driver on the GPU: device ghost fill + fused SSP-RK3 steps + device CFL
+dt, against the oracle's single-box RK3 (Shu-Osher form) on the same inputs,
+and box-decomposition invariance (any box split gives bit-identical results)."""
+import numpy as np
+import pytest
+
+from oracle import BCStruct
+import inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_bc(case):
+    bc = BCStruct()
+    bc.lo_bc[:] = list(case["lo_bc"]); bc.hi_bc[:] = list(case["hi_bc"])
+    bc.dirichlet_case = case["bc_case"]
+    bc.prob_lo[:] = list(case["prob_lo"]); bc.dx[:] = list(case["dx"])
+    bc.dom_lo[:] = [0, 0, 0]
+    bc.dom_hi[:] = [n - 1 for n in case["n"]]
+    if case["bc_case"] == 1:
+        bc.dmr_left[:] = list(case["case_params"][:5]); bc.dmr_right[:] = list(case["case_params"][5:10])
+    return bc
+
+
+def make_level(ctx, case, max_grid, tile=-1):
+    from ocfd.level import Level, chop_domain
+    n = case["n"]
+    boxes = chop_domain(n, max_grid)
+    return Level(ctx, boxes, tuple(x - 1 for x in n), case["lo_bc"], case["hi_bc"], case["dx"],
+                 case["prob_lo"], case["bc_case"], case["case_params"], tile=tile)
+
+
+def valid(G):
+    return G[:, 4:-4, 4:-4, 4:-4]
+
+
+def relerr(a, b):
+    """max |a-b| / max |b| per conserved group: density, momentum vector, energy
+    (a momentum component that is identically ~0 is measured against the
+    momentum magnitude, not against its own rounding noise)."""
+    groups = [(0,), (1, 2, 3), (4,)] + [(c,) for c in range(5, a.shape[0])]
+    err = 0.0
+    for g in groups:
+        den = max(np.abs(b[list(g)]).max(), 1e-300)
+        err = max(err, float(np.abs(a[list(g)] - b[list(g)]).max() / den))
+    return err
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import ocfd
+    return ocfd.Context()
+
+
+def run_gpu(ctx, case, nsteps, cfl, max_grid, flags=0, tile=-1):
+    lev = make_level(ctx, case, max_grid, tile)
+    lev.set_global(case["G"])
+    lev.advance(nsteps, cfl, flags)
+    t, dt = lev.time()
+    out = lev.get_global()
+    lev.close()
+    return out, t
+
+
+def run_oracle(oracle, case, nsteps, cfl, visc=False):
+    S = np.ascontiguousarray(case["G"].copy())
+    t, dts = oracle.advance_rk3(oracle_bc(case), S, cfl, nsteps, form=1, do_visc=visc)
+    return valid(S), t
+
+
+def test_sod_vs_oracle(ctx, oracle):
+    from ocfd.cases import sod
+    case = sod(64, 16, 4)
+    ref, tr = run_oracle(oracle, case, 12, 0.5)
+    got, tg = run_gpu(ctx, case, 12, 0.5, (64, 16, 4))
+    assert tg == pytest.approx(tr, rel=1e-13)
+    assert relerr(got, ref) < 1e-10
+
+
+def test_box_split_is_bit_identical(ctx):
+    from ocfd.cases import sod
+    case = sod(64, 16, 4)
+    a, _ = run_gpu(ctx, case, 6, 0.5, (64, 16, 4))
+    b, _ = run_gpu(ctx, case, 6, 0.5, (16, 8, 4))
+    c, _ = run_gpu(ctx, case, 6, 0.5, (24, 5, 3))
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def test_tile_choice_is_bit_identical(ctx):
+    from ocfd.cases import sod
+    case = sod(48, 24, 8)
+    ref, _ = run_gpu(ctx, case, 4, 0.5, (48, 24, 8), tile=0)
+    for t in range(1, 6):
+        got, _ = run_gpu(ctx, case, 4, 0.5, (48, 24, 8), tile=t)
+        assert np.array_equal(got, ref), t
+
+
+def test_dmr_vs_oracle(ctx, oracle):
+    from ocfd.cases import dmr
+    case = dmr(64, 16, 2)
+    ref, tr = run_oracle(oracle, case, 10, 0.5)
+    got, tg = run_gpu(ctx, case, 10, 0.5, (32, 8, 2))
+    assert tg == pytest.approx(tr, rel=1e-13)
+    assert relerr(got, ref) < 1e-10
+
+
+def test_periodic_vs_oracle(ctx, oracle):
+    n = (24, 16, 8)
+    G = inputs.ideal_state(*n, seed=21, jump=False, mach=0.5)
+    case = dict(G=G, n=n, dx=(1 / 24, 1 / 24, 1 / 24), prob_lo=(0, 0, 0), lo_bc=(0, 0, 0),
+                hi_bc=(0, 0, 0), bc_case=0, case_params=())
+    ref, tr = run_oracle(oracle, case, 8, 0.4)
+    got, tg = run_gpu(ctx, case, 8, 0.4, (8, 8, 8))
+    assert relerr(got, ref) < 1e-10
+
+
+def test_viscous_level_vs_oracle(ctx, oracle):
+    from ocfd.cases import sod
+    case = sod(48, 12, 4)
+    G = case["G"].copy()
+    # dimensional air at ~300 K so that the viscous flux is visible
+    G[0] *= 1.2; G[4] *= 1.0e5
+    case = dict(case, G=G, dx=(1e-4, 1e-4, 1e-4), lo_bc=(2, 5, 4), hi_bc=(2, 5, 4))
+    ref, tr = run_oracle(oracle, case, 6, 0.4, visc=True)
+    got, tg = run_gpu(ctx, case, 6, 0.4, (16, 12, 4), flags=1)
+    assert relerr(got, ref) < 1e-10
