@@ -1,0 +1,313 @@
+"""Benchmark: cell-steps/s of the OpenCFD-AMR RHS + RK3 update path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config sod|dmr] [--form fp64|fp32]
+
+A step is one SSP-RK3 time step of every box of the workload (3 ghost fills +
+3 fused RHS/update stages + the CFL reduction), i.e. one CUDA-graph launch.
+value  = cells x steps / device time of the K timed steps (state resident in
+         HBM; L2 flushed between steps, untimed)
+e2e    = the same through the C ABI from pinned host buffers: every step uploads
+         the state, advances, downloads the state
+--impl reference times the reference algorithm on the host CPU cores (the
+         oracle port, OpenMP, all threads) on the same workload.
+Multi-GPU: independent replicas (the workload does not shard over GPUs here);
+value is summed over ranks with the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "opencfd-amr_gb300"), os.path.join(ROOT, "oracle")):
+    sys.path.insert(0, p)
+
+METRIC = "cell-steps/s on 1 GB300, plain FP64 vs mixed/batched form at matched L1 error"
+CFL = 0.5
+
+
+def workload(name):
+    from ocfd import cases
+    if name == "sod":
+        c = cases.sod(512, 64, 4)
+        c["name"] = "Sod shock tube 512x64x4 (2D slab), single level, SSP-RK3, CFL 0.5, inviscid"
+        c["max_grid"] = (128, 64, 4)
+    elif name == "dmr":
+        c = cases.dmr(1024, 256, 2)
+        c["name"] = "Double Mach reflection base level 1024x256x2, boxes 128x128x2, SSP-RK3, CFL 0.5"
+        c["max_grid"] = (128, 128, 2)
+    elif name == "cube":
+        c = cases.blast3d(256, 256, 64)
+        c["name"] = "3D periodic blast 256x256x64, boxes 64x64x64, SSP-RK3, CFL 0.5"
+        c["max_grid"] = (64, 64, 64)
+    else:
+        raise SystemExit("unknown config " + name)
+    return c
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        import statistics
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = max(smax, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU (oracle)
+def cpu_time_steps(c, steps, threads=None):
+    """Time `steps` RK3 steps of the oracle port (OpenMP) on the full workload
+    domain as one box; returns seconds and cells."""
+    import numpy as np
+    from oracle import Oracle, BCStruct
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = Oracle(openmp=True)
+    bc = BCStruct()
+    bc.lo_bc[:] = list(c["lo_bc"]); bc.hi_bc[:] = list(c["hi_bc"])
+    bc.dirichlet_case = c["bc_case"]
+    bc.prob_lo[:] = list(c["prob_lo"]); bc.dx[:] = list(c["dx"])
+    bc.dom_lo[:] = [0, 0, 0]; bc.dom_hi[:] = [n - 1 for n in c["n"]]
+    if c["bc_case"] == 1:
+        bc.dmr_left[:] = list(c["case_params"][:5]); bc.dmr_right[:] = list(c["case_params"][5:10])
+    S = np.ascontiguousarray(c["G"].copy())
+    t0 = time.perf_counter()
+    o.advance_rk3(bc, S, CFL, steps, form=1)
+    dt = time.perf_counter() - t0
+    cells = c["n"][0] * c["n"][1] * c["n"][2]
+    return dt, cells
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    c = workload(args.config)
+    threads = os.cpu_count() or 1
+    # bounded: warm-up steps then K timed steps, each a full-domain RK3 step
+    cpu_time_steps(c, max(1, min(args.warmup, 2)), threads)
+    dt, cells = cpu_time_steps(c, args.steps, threads)
+    v = cells * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": c["name"], "form": "fp64", "cells": cells},
+            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": "%d full-domain RK3 steps of the oracle restatement (OpenMP)" % args.steps},
+            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU (ours)
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    import ocfd
+    from ocfd.level import Level, chop_domain
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    flags = ocfd.FLUX_FP32 if args.form == "fp32" else 0
+    c = workload(args.config)
+    ctx = ocfd.Context(device=local)
+    boxes = chop_domain(c["n"], c["max_grid"])
+    lev = Level(ctx, boxes, tuple(n - 1 for n in c["n"]), c["lo_bc"], c["hi_bc"], c["dx"],
+                c["prob_lo"], c["bc_case"], c["case_params"])
+    cells = lev.cells()
+    flat = np.ascontiguousarray(lev.pack(c["G"]))
+    stream = torch.cuda.current_stream(dev)
+    lev.copy_in(flat)
+    l2flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    lev.advance(args.warmup, CFL, flags)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for e0, e1 in ev:
+            l2flush.fill_(1.0)            # untimed: evicts the state from L2
+            e0.record(stream)
+            lev.advance(1, CFL, flags)
+            e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    ms_max = allreduce_max(ms, world)
+    value = cells * args.steps * world / (ms_max * 1e-3)
+
+    # dominant kernel, timed live: the fused RK-stage kernel (stage 2)
+    stage_ms = lev.profile_stage(flags, reps=10)
+    alg_bytes = 120.0 * cells          # read U_s and U_0, write U_out (5 doubles each)
+    hbm_peak, peak_src = peaks()
+    achieved = alg_bytes / (stage_ms * 1e-3) / 1e9
+    fp64 = ctypes.c_double(); fp32 = ctypes.c_double()
+    ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
+
+    # end to end through the C ABI with host buffers
+    pin = torch.from_numpy(flat).pin_memory()
+    out = torch.empty_like(pin).pin_memory()
+    e2e_steps = max(2, min(args.steps, 10))
+    lev.copy_in(pin, stream)
+    lev.advance(1, CFL, flags)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        lev.lib.ocfd_level_copy_in(lev.h, ctypes.c_void_p(pin.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        lev.advance(1, CFL, flags, stream)
+        lev.lib.ocfd_level_copy_out(lev.h, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = allreduce_max(e0.elapsed_time(e1) / e2e_steps, world)
+    e2e_value = cells * world / (e2e_ms * 1e-3)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu_steps = 2
+        dt, ccells = cpu_time_steps(c, cpu_steps, os.cpu_count())
+        cpu = {"value": ccells * cpu_steps / dt, "unit": "cell-steps/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": "%d full-domain RK3 steps of the oracle restatement (OpenMP)" % cpu_steps}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.form == "fp64" else "f32-flux/f64-state", "data": "synthetic",
+            "config": {"workload": c["name"], "form": args.form, "cells": cells, "boxes": len(boxes),
+                       "l2": "flushed between timed steps (512 MB write, untimed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "k_rhs_regular fused RK stage", "ms_per_launch": stage_ms,
+                         "alg_bytes_per_cell": 120,
+                         "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s",
+                    "h2d_bytes_per_step": int(flat.nbytes), "d2h_bytes_per_step": int(flat.nbytes)},
+            "clocks": clk.summary(),
+            "gpu_launches": lev.launches_per_step(flags) * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    lev.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="sod", choices=["sod", "dmr", "cube"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -190,6 +190,16 @@ ocfd_status ocfd_level_time(ocfd_level* level, double* time, double* last_dt, vo
 /* Set the level time and forget the previous dt (the next step is not limited). */
 ocfd_status ocfd_level_set_time(ocfd_level* level, double time, void* stream);
 
+/* Cells of the level (valid cells of all boxes). */
+int64_t ocfd_level_cells(const ocfd_level* level);
+/* Kernels one ocfd_level_advance step launches with `flags`. */
+int ocfd_level_launches_per_step(const ocfd_level* level, unsigned flags);
+/* Average duration in ms of the level's fused RK-stage kernel (stage 2: reads
+ * two states, writes one) over `reps` back-to-back launches, timed with CUDA
+ * events on `stream`.  Overwrites the level's stage scratch buffer only. */
+ocfd_status ocfd_level_profile_stage(ocfd_level* level, unsigned flags, int reps, double* ms,
+                                     void* stream);
+
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops
  * per FMA), from register-only FMA chains over all SMs. */

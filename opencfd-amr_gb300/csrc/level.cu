@@ -692,4 +692,42 @@ ocfd_status ocfd_level_time(ocfd_level* L, double* time, double* last_dt, void* 
     return OCFD_OK;
 }
 
+int64_t ocfd_level_cells(const ocfd_level* L) { return L ? L->ncells : 0; }
+
+int ocfd_level_launches_per_step(const ocfd_level* L, unsigned flags) {
+    if (!L) return 0;
+    (void)flags;
+    int fill = (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0);
+    return 2 + 3 * (fill + 1);
+}
+
+ocfd_status ocfd_level_profile_stage(ocfd_level* L, unsigned flags, int reps, double* ms, void* stream) {
+    if (!L || reps <= 0 || !ms) return fail(OCFD_BAD_ARG, "ocfd_level_profile_stage");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const bool visc = flags & OCFD_VISC;
+    RegBoxArgs dummy{};
+    auto launch = [&]() {
+        return (flags & OCFD_FLUX_FP32)
+                   ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[1], L->d_tile_start,
+                                            (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st)
+                   : launch_rhs_regular(L->tile, visc, L->d_stage[1], L->d_tile_start,
+                                        (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st);
+    };
+    ocfd_status s = launch();  // warm-up
+    if (s != OCFD_OK) return s;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < reps && s == OCFD_OK; ++r) s = launch();
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / reps;
+    return s;
+}
+
 }  // extern "C"

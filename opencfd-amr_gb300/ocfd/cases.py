@@ -55,3 +55,19 @@ def dmr(nx=1024, ny=256, nz=2, gamma=GAMMA, Lx=4.0):
         G[c] = np.where(post, left[c], right[c])[None]
     return dict(G=G, n=n, dx=(dx, dx, dx), prob_lo=(0.0, 0.0, 0.0),
                 lo_bc=(1, 4, 2), hi_bc=(2, 1, 2), bc_case=1, case_params=tuple(left) + tuple(right))
+
+
+def blast3d(nx=256, ny=256, nz=64, gamma=GAMMA):
+    """3D periodic blast: rho=1, p=1 inside r < 0.2 of the box centre, 0.125 / 0.1
+    outside; unit cell size 1/nx.  A regular-box workload larger than L2."""
+    dx = 1.0 / nx
+    n = (nx, ny, nz)
+    x, y, z = _centres(n, (dx, dx, dx), (0.0, 0.0, 0.0))
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    r = np.sqrt((X - 0.5 * nx * dx) ** 2 + (Y - 0.5 * ny * dx) ** 2 + (Z - 0.5 * nz * dx) ** 2)
+    inside = r < 0.2 * min(n) * dx
+    G = np.zeros((5, nz + 2 * NG, ny + 2 * NG, nx + 2 * NG))
+    G[0] = np.where(inside, 1.0, 0.125)
+    G[4] = np.where(inside, 1.0, 0.1) / (gamma - 1.0)
+    return dict(G=G, n=n, dx=(dx, dx, dx), prob_lo=(0.0, 0.0, 0.0),
+                lo_bc=(0, 0, 0), hi_bc=(0, 0, 0), bc_case=0, case_params=())

@@ -32,6 +32,10 @@ declare("ocfd_level_advance", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double,
 declare("ocfd_level_time", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double), _vp])
 declare("ocfd_level_set_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
+declare("ocfd_level_cells", ctypes.c_int64, [_vp])
+declare("ocfd_level_launches_per_step", ctypes.c_int, [_vp, ctypes.c_uint])
+declare("ocfd_level_profile_stage", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int,
+                                                   ctypes.POINTER(ctypes.c_double), _vp])
 
 CASE_NONE, CASE_DMR, CASE_INFLOW = 0, 1, 2
 
@@ -164,6 +168,18 @@ class Level:
 
     def set_time(self, t, stream=None):
         check(self.lib.ocfd_level_set_time(self.h, t, _stream_ptr(stream)), "set_time")
+
+    def cells(self):
+        return int(self.lib.ocfd_level_cells(self.h))
+
+    def launches_per_step(self, flags=0):
+        return int(self.lib.ocfd_level_launches_per_step(self.h, flags))
+
+    def profile_stage(self, flags=0, reps=10, stream=None):
+        ms = ctypes.c_double()
+        check(self.lib.ocfd_level_profile_stage(self.h, flags, reps, ctypes.byref(ms), _stream_ptr(stream)),
+              "profile_stage")
+        return ms.value
 
     def fill_ghosts(self, time, stream=None):
         check(self.lib.ocfd_level_fill_ghosts(self.h, time, _stream_ptr(stream)), "fill_ghosts")

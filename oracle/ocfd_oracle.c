@@ -368,12 +368,18 @@ void ocfdo_rhs_regular(const ocfdo_parm* p, const double* S, int nx, int ny, int
     for (int d = 0; d < 3; ++d) {
         long long FN = fN(&b, d);
         memset(fl[d], 0, sizeof(double) * FN * NCONS);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
         for (long long c = 0; c < N; ++c) {
             double qc[7], a[5], m[5];
             for (int n = 0; n < 7; ++n) qc[n] = q[n * N + c];
             sw_split(p->eos_gamma, qc, d, a, m);
             for (int n = 0; n < 5; ++n) { fp[n * N + c] = a[n]; fm[n * N + c] = m[n]; }
         }
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
         for (int k = 0; k < nz + (d == 2); ++k)
             for (int j = 0; j < ny + (d == 1); ++j)
                 for (int i = 0; i < nx + (d == 0); ++i) {
@@ -384,6 +390,9 @@ void ocfdo_rhs_regular(const ocfdo_parm* p, const double* S, int nx, int ny, int
                 }
     }
     long long BN = bN(&b);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
     for (int k = 0; k < nz; ++k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i)
@@ -1052,6 +1061,9 @@ void ocfdo_c2prim(const ocfdo_parm* p, int chem, const double* S, const double* 
     box_t b = mkbox(nx, ny, nz);
     long long N = gN(&b);
     int nq = chem ? 8 : 7;
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
     for (long long c = 0; c < N; ++c) {
         double u[5], qc[8], r[NS];
         for (int n = 0; n < 5; ++n) u[n] = S[n * N + c];
@@ -1506,6 +1518,9 @@ double ocfdo_advance_rk3(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int
         /* stage 1 */
         ocfdo_rhs_regular(p, S, nx, ny, nz, dxinv, do_visc, k1, fl[0], fl[1], fl[2]);
         memcpy(Ss, S0, sizeof(double) * N * NCONS);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
         for (int n = 0; n < NCONS; ++n)
             for (int k = 0; k < nz; ++k)
                 for (int j = 0; j < ny; ++j)
@@ -1516,6 +1531,9 @@ double ocfdo_advance_rk3(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int
         ocfdo_fill_ghosts(bc, Ss, NCONS, nx, ny, nz, time + dt);
         /* stage 2 */
         ocfdo_rhs_regular(p, Ss, nx, ny, nz, dxinv, do_visc, k2, fl[0], fl[1], fl[2]);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
         for (int n = 0; n < NCONS; ++n)
             for (int k = 0; k < nz; ++k)
                 for (int j = 0; j < ny; ++j)
@@ -1529,6 +1547,9 @@ double ocfdo_advance_rk3(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int
         ocfdo_fill_ghosts(bc, Ss, NCONS, nx, ny, nz, time + 0.5 * dt);
         /* stage 3 */
         ocfdo_rhs_regular(p, Ss, nx, ny, nz, dxinv, do_visc, k3, fl[0], fl[1], fl[2]);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
         for (int n = 0; n < NCONS; ++n)
             for (int k = 0; k < nz; ++k)
                 for (int j = 0; j < ny; ++j)
