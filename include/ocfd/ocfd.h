@@ -134,6 +134,44 @@ ocfd_status ocfd_rhs_regular_box_f64(ocfd_context* ctx, const ocfd_array4* S,
                                      ocfd_box bx, const double dxinv[3], unsigned flags,
                                      void* stream);
 
+/* Cut-cell box (grow(bx,4) contains a cut cell), ideal gas: MUSCL-minmod
+ * reconstruction of the primitives where the neighbours are connected, Van Leer
+ * flux (+ EB-aware viscous flux with OCFD_VISC), cut-cell divergence with the
+ * wall flux, negated; OCFD_REDISTRIBUTE applies the reference's local rescale.
+ * Replaces EBR::eb_compute_dSdt_box, Source/EB/AdvanceBox.cpp:16-228 (point
+ * kernels Source/EB/EBkernels.H:9-377, EBdiffusion.H:8-203).
+ *   S       state covering grow(bx, 2), ncomp >= 5
+ *   flag    EBCellFlag words covering grow(bx, 1)
+ *   vfrac   volume fractions covering bx
+ *   apx/apy/apz  area fractions over surroundingNodes(bx, d)
+ *   fc, bcent    face / boundary centroids: accepted for interface fidelity and
+ *                not read (the reference passes them and does not read them)
+ * Scratch comes from the context pool. */
+ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* dSdt,
+                                const ocfd_array4* flux, const ocfd_flag4* flag,
+                                const ocfd_array4* vfrac, const ocfd_array4* apx,
+                                const ocfd_array4* apy, const ocfd_array4* apz,
+                                const ocfd_array4* const* fc, const ocfd_array4* bcent,
+                                ocfd_box bx, const double dxinv[3], unsigned flags, void* stream);
+
+/* ------------------------------------------------------------ chemistry */
+/* One linearised backward-Euler chemistry substep of length dt on every cell
+ * of bx, in place: T from e by bounded Newton on NASA-7 (LiDryer.H:833-888),
+ * Li-Dryer rates and analytic Jacobian (LiDryer.H:156-529), partial-pivot
+ * solve of (I - dt W J W^-1) drho = dt W wdot (LiDryer.H:890-942), species
+ * clipped at 0 and the formation-enthalpy change moved into rho E.  Replaces the
+ * kernel of EBR::chemical_advance, Source/CHEM/ChemAdvance.cpp:7-85 (the caller
+ * skips covered boxes as the reference does).
+ *   S (>= 5 comps) and spec (9 partial densities) covering bx, updated in place */
+ocfd_status ocfd_chem_advance_box_f64(ocfd_context* ctx, const ocfd_array4* S,
+                                      const ocfd_array4* spec, ocfd_box bx, double dt,
+                                      void* stream);
+
+/* Clip negative partial densities and rescale them to sum to rho, in place
+ * (EBR::post_timestep, Source/EBR.cpp:333-357). */
+ocfd_status ocfd_spec_renorm_box_f64(ocfd_context* ctx, const ocfd_array4* S,
+                                     const ocfd_array4* spec, ocfd_box bx, void* stream);
+
 /* ------------------------------------------------------------------ level */
 /* One AMR level advanced on the device: the build's own host driver in place of
  * AMReX's AmrLevel machinery (absent).  It owns the level's state FABs (each

@@ -11,6 +11,8 @@
 
 namespace ocfd {
 
+ocfd_status configure_chem();
+
 static thread_local std::string g_last_error;
 
 void set_error(const std::string& msg) { g_last_error = msg; }
@@ -135,6 +137,7 @@ ocfd_status ocfd_context_create(const ocfd_parm* parm, int device, ocfd_context*
     ocfd_status s = mech_upload(*parm);
     if (s == OCFD_OK) s = configure_rhs_regular();
     if (s == OCFD_OK) s = configure_rhs_regular_f32();
+    if (s == OCFD_OK) s = configure_chem();
     if (s != OCFD_OK) {
         cudaFree(ctx->d_error);
         delete ctx;

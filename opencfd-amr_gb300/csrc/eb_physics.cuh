@@ -1,0 +1,142 @@
+// Cut-cell (embedded boundary) point physics on the GPU, in the operation order
+// of Source/EB/EBkernels.H and Source/EB/EBdiffusion.H.
+#pragma once
+
+#include "device_physics.cuh"
+
+namespace ocfd {
+
+// EBCellFlag: bits 0-1 type, neighbour (i,j,k) at bit 4 + (i+1) + 3(j+1) + 9(k+1).
+// The reference queries offsets of -2 (EBkernels.H:22,43,64); those map to the
+// same linear bit position, and to "not connected" outside the word.
+__device__ __forceinline__ bool eb_conn(uint32_t f, int i, int j, int k) {
+    const int p = 4 + (i + 1) + 3 * (j + 1) + 9 * (k + 1);
+    return p >= 0 && p < 32 && ((f >> p) & 1u);
+}
+__device__ __forceinline__ bool eb_covered(uint32_t f) { return (f & 3u) == 3u; }
+__device__ __forceinline__ bool eb_regular(uint32_t f) { return (f & 3u) == 0u; }
+
+// minmod, Source/kernel/Reconstruction.H:8-19
+__device__ __forceinline__ double minmod(double a, double b) {
+    if (a * b > 0) return fabs(a) > fabs(b) ? b : a;
+    return 0.0;
+}
+
+// eb_recon_x/y/z for one component: left/right states at the D-face of cell c
+// given the values at c-2e, c-e, c, c+e and the flag of c.
+__device__ __forceinline__ void eb_recon(uint32_t f, int D, double vm2, double vm1, double v0,
+                                         double vp1, double& l, double& r) {
+    const int di = D == 0, dj = D == 1, dk = D == 2;
+    l = vm1;
+    r = v0;
+    if (eb_conn(f, -di, -dj, -dk)) {
+        if (eb_conn(f, -2 * di, -2 * dj, -2 * dk)) l = vm1 + 0.5 * minmod(v0 - vm1, vm1 - vm2);
+        if (eb_conn(f, di, dj, dk)) r = v0 - 0.5 * minmod(vp1 - v0, v0 - vm1);
+    }
+}
+
+// Van Leer flux vector splitting, Source/EB/EBkernels.H:73-171
+__device__ __forceinline__ void vanleer(const DevParm& P, double gamma, const double* ql,
+                                        const double* qr, int D, double* flx) {
+    double fp[5] = {0, 0, 0, 0, 0}, fm[5] = {0, 0, 0, 0, 0};
+    const double dl = ql[QRHO], ul = ql[QU], vl = ql[QV], wl = ql[QW], pl = dmax(ql[QPRES], P.smallp);
+    const double dr = qr[QRHO], ur = qr[QU], vr = qr[QV], wr = qr[QW], pr = dmax(qr[QPRES], P.smallp);
+    const double cL = ql[QC], cR = qr[QC];
+    const int nn[3] = {D == 0, D == 1, D == 2};
+    const double UL = D == 0 ? ul : (D == 1 ? vl : wl);
+    const double UR = D == 0 ? ur : (D == 1 ? vr : wr);
+    const double ML = UL / cL, MR = UR / cR;
+    const double lv[3] = {ul, vl, wl}, rv[3] = {ur, vr, wr};
+    if (ML >= 1.0) {
+        fp[0] = dl * UL;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) fp[1 + m] = dl * UL * lv[m] + nn[m] * pl;
+        fp[4] = UL * (gamma * pl / (gamma - 1.0) + 0.5 * dl * (ul * ul + vl * vl + wl * wl));
+    } else if (fabs(ML) < 1.0) {
+        const double Mp = 0.250 * (1.0 + ML) * (1.0 + ML);
+        const double t0 = dl * cL * Mp;
+        fp[0] = t0;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) fp[1 + m] = t0 * (nn[m] * (-UL + 2.0 * cL) / gamma + lv[m]);
+        fp[4] = t0 * (((gamma - 1) * UL + 2 * cL) * ((gamma - 1) * UL + 2 * cL) / (2 * (gamma * gamma - 1)) +
+                      (ul * ul + vl * vl + wl * wl - UL * UL) / 2);
+    }
+    if (fabs(MR) < 1.0) {
+        const double Mm = -0.250 * (MR - 1.0) * (MR - 1.0);
+        const double t0 = dr * cR * Mm;
+        fm[0] = t0;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) fm[1 + m] = t0 * (nn[m] * (-UR - 2.0 * cR) / gamma + rv[m]);
+        fm[4] = t0 * (((gamma - 1) * UR - 2 * cR) * ((gamma - 1) * UR - 2 * cR) / (2 * (gamma * gamma - 1)) +
+                      (ur * ur + vr * vr + wr * wr - UR * UR) / 2);
+    } else if (MR <= -1.0) {
+        fm[0] = dr * UR;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) fm[1 + m] = dr * UR * rv[m] + nn[m] * pr;
+        fm[4] = UR * (gamma * pr / (gamma - 1.0) + 0.5 * dr * (ur * ur + vr * vr + wr * wr));
+    }
+#pragma unroll
+    for (int n = 0; n < 5; ++n) flx[n] = fp[n] + fm[n];
+}
+
+// connectivity-aware transverse derivative of component `m` of q along t at the
+// D-face of cell (i,j,k), Source/EB/EBdiffusion.H:36-58
+__device__ __forceinline__ double eb_tderiv(const View<const double>& q, const View<const uint32_t>& flag,
+                                            int m, int D, int t, int i, int j, int k, double dxinv_t) {
+    const double weights[3] = {0., 1., 0.5};
+    const int ti = t == 0, tj = t == 1, tk = t == 2;
+    const int li = i - (D == 0), lj = j - (D == 1), lk = k - (D == 2);
+    const uint32_t fh = flag(i, j, k), fl = flag(li, lj, lk);
+    const int hip = eb_conn(fh, ti, tj, tk), him = eb_conn(fh, -ti, -tj, -tk);
+    const int lop = eb_conn(fl, ti, tj, tk), lom = eb_conn(fl, -ti, -tj, -tk);
+    const double whi = weights[hip + him], wlo = weights[lop + lom];
+    return (0.5 * dxinv_t) *
+           ((q(i + hip * ti, j + hip * tj, k + hip * tk, m) - q(i - him * ti, j - him * tj, k - him * tk, m)) * whi +
+            (q(li + lop * ti, lj + lop * tj, lk + lop * tk, m) - q(li - lom * ti, lj - lom * tj, lk - lom * tk, m)) * wlo);
+}
+
+// eb_compute_visc_x/y/z (Source/EB/EBdiffusion.H:8-203); with `multi` the
+// multispecies form of Source/CHEM/ChemViscous.H:357-575 (face mu / lambda
+// given, species-enthalpy flux subtracted).  f points at component 0 of the
+// face flux, fs is the component stride.
+__device__ __forceinline__ void eb_visc_face(const DevParm& P, const View<const double>& q,
+                                             const View<const uint32_t>& flag, int D, int i, int j,
+                                             int k, const double* dxinv, double* f, long long fs,
+                                             bool multi, double mu_f, double lam_f, double hflux) {
+    const int li = i - (D == 0), lj = j - (D == 1), lk = k - (D == 2);
+    const double Tc = q(i, j, k, QT), Tm = q(li, lj, lk, QT);
+    double muf, ksum = 0;
+    if (!multi) {
+        const double mutl = sutherland(P, Tc), mutr = sutherland(P, Tm);
+        muf = 0.5 * (mutl + mutr);
+        ksum = mutl * P.kOverMu + mutr * P.kOverMu;
+    } else {
+        muf = mu_f;
+    }
+    const double dT = (Tc - Tm) * dxinv[D];
+    double g[3][3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) g[m][D] = (q(i, j, k, QU + m) - q(li, lj, lk, QU + m)) * dxinv[D];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        if (t == D) continue;
+        g[D][t] = eb_tderiv(q, flag, QU + D, D, t, i, j, k, dxinv[t]);
+        g[t][t] = eb_tderiv(q, flag, QU + t, D, t, i, j, k, dxinv[t]);
+    }
+    const double divu = g[0][0] + g[1][1] + g[2][2];
+    double tau[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+        tau[m] = (m == D) ? muf * (2.0 * g[D][D] - P.twoThirds * divu) : muf * (g[m][D] + g[D][m]);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) f[(1 + m) * fs] += -tau[m];
+    const double ub0 = q(i, j, k, QU) + q(li, lj, lk, QU);
+    const double ub1 = q(i, j, k, QV) + q(li, lj, lk, QV);
+    const double ub2 = q(i, j, k, QW) + q(li, lj, lk, QW);
+    if (!multi)
+        f[4 * fs] += -0.5 * (ub0 * tau[0] + ub1 * tau[1] + ub2 * tau[2] + ksum * dT);
+    else
+        f[4 * fs] += -0.5 * (ub0 * tau[0] + ub1 * tau[1] + ub2 * tau[2]) - lam_f * dT - hflux;
+}
+
+}  // namespace ocfd

@@ -61,6 +61,11 @@ _SIGS = {
     "ocfd_rhs_regular_box_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Array4), ctypes.POINTER(Array4),
                                                 ctypes.POINTER(Array4), Box, ctypes.POINTER(ctypes.c_double),
                                                 ctypes.c_uint, ctypes.c_void_p]),
+    "ocfd_rhs_eb_box_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                           ctypes.POINTER(Array4), ctypes.POINTER(Flag4), ctypes.POINTER(Array4),
+                                           ctypes.POINTER(Array4), ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                           ctypes.c_void_p, ctypes.POINTER(Array4), Box,
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_uint, ctypes.c_void_p]),
     "ocfd_measure_fma_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 

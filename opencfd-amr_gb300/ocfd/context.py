@@ -4,7 +4,7 @@ from __future__ import annotations
 
 import ctypes
 
-from ._abi import Array4, Parm, array4, box, check, load
+from ._abi import Array4, Parm, array4, box, check, flag4, load
 
 
 def _stream_ptr(stream):
@@ -66,3 +66,24 @@ class Context:
         st = self.lib.ocfd_rhs_regular_box_f64(self.h, ctypes.byref(aS), ctypes.byref(aD), fl,
                                                box(lo, hi), dx, flags, _stream_ptr(stream))
         check(st, "ocfd_rhs_regular_box_f64")
+
+    def rhs_eb_box(self, S, dSdt, geom, lo, hi, dxinv, flags=0, flux=None, S_begin=None,
+                   stream=None):
+        """Cut-cell box.  geom: dict of CUDA tensors flag (int32 view of the
+        uint32 words, grown by 4), vfrac (grown by 4), apx, apy, apz (faces of
+        the box)."""
+        sb = S_begin if S_begin is not None else tuple(l - 4 for l in lo)
+        g4 = tuple(l - 4 for l in lo)
+        aS, aD = array4(S, sb), array4(dSdt, lo)
+        fl = None
+        if flux is not None:
+            fl = (Array4 * 3)(*[array4(f, lo) for f in flux])
+        af = flag4(geom["flag"], g4)
+        av = array4(geom["vfrac"], g4)
+        ap = [array4(geom[k], lo) for k in ("apx", "apy", "apz")]
+        dx = (ctypes.c_double * 3)(*dxinv)
+        st = self.lib.ocfd_rhs_eb_box_f64(self.h, ctypes.byref(aS), ctypes.byref(aD), fl,
+                                          ctypes.byref(af), ctypes.byref(av), ctypes.byref(ap[0]),
+                                          ctypes.byref(ap[1]), ctypes.byref(ap[2]), None, None,
+                                          box(lo, hi), dx, flags, _stream_ptr(stream))
+        check(st, "ocfd_rhs_eb_box_f64")
