@@ -154,6 +154,42 @@ ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S, const o
                                 const ocfd_array4* const* fc, const ocfd_array4* bcent,
                                 ocfd_box bx, const double dxinv[3], unsigned flags, void* stream);
 
+/* Regular box, multispecies (9-species Li-Dryer gas): real-gas primitives (T by
+ * Newton on NASA-7, p from the species, gamma = 1 + p/e), Steger-Warming split of
+ * the flow with the local gamma and of the species densities, WENO-Z of all
+ * 5 + 9 components, and with OCFD_VISC mixture-averaged transport (Wilke
+ * viscosity, averaged conductivity, mixture-averaged Fick diffusion) with the
+ * species-enthalpy flux; divergence of both.  Replaces the regular-box branch of
+ * EBR::compute_dSdt_multi, Source/CHEM/FlowAdvance.cpp:157-403.
+ *   S, spec        covering grow(bx, 4) (5 and 9 components)
+ *   dSdt, dSdt_spec over bx
+ *   flux, flux_spec NULL or three face arrays over surroundingNodes(bx, d) */
+ocfd_status ocfd_rhs_chem_box_f64(ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* spec,
+                                  const ocfd_array4* dSdt, const ocfd_array4* dSdt_spec,
+                                  const ocfd_array4* flux, const ocfd_array4* flux_spec,
+                                  ocfd_box bx, const double dxinv[3], unsigned flags,
+                                  void* stream);
+
+/* Cut-cell box, multispecies: MUSCL-minmod of the 8 primitives and 9 partial
+ * densities, Van Leer flow flux (gamma averaged over the face) and species flux,
+ * Fick diffusion + EB-aware multispecies viscous flux with OCFD_VISC, cut-cell
+ * species divergence, negated.  As in the reference, the flow dSdt of a cut
+ * multispecies box is left zero (its divc -> dSdt copy is commented out,
+ * Source/CHEM/FlowAdvanceBox.cpp:500-523); the flow face fluxes are still
+ * produced for reflux.  Replaces EBR::ebchem_compute_dSdt_box,
+ * Source/CHEM/FlowAdvanceBox.cpp:16-525.
+ *   S, spec covering grow(bx, 2); flag covering grow(bx, 1); vfrac over bx;
+ *   apx/apy/apz over surroundingNodes(bx, d); fc/bcent not read */
+ocfd_status ocfd_rhs_chem_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S,
+                                     const ocfd_array4* spec, const ocfd_array4* dSdt,
+                                     const ocfd_array4* dSdt_spec, const ocfd_array4* flux,
+                                     const ocfd_array4* flux_spec, const ocfd_flag4* flag,
+                                     const ocfd_array4* vfrac, const ocfd_array4* apx,
+                                     const ocfd_array4* apy, const ocfd_array4* apz,
+                                     const ocfd_array4* const* fc, const ocfd_array4* bcent,
+                                     ocfd_box bx, const double dxinv[3], unsigned flags,
+                                     void* stream);
+
 /* ------------------------------------------------------------ chemistry */
 /* One linearised backward-Euler chemistry substep of length dt on every cell
  * of bx, in place: T from e by bounded Newton on NASA-7 (LiDryer.H:833-888),

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "chem_physics.cuh"
+#include "eb_physics.cuh"
 #include "mechanism.h"
 #include "ocfd_internal.h"
 
@@ -174,4 +175,505 @@ extern "C" ocfd_status ocfd_spec_renorm_box_f64(ocfd_context* ctx, const ocfd_ar
     k_spec_renorm<<<(int)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
         view_of<const double>(S), view_of<double>(spec), B);
     return check_launch("ocfd_spec_renorm_box_f64");
+}
+
+// =====================================================================
+// Multispecies right-hand side of a regular box: replaces the kernel chain
+// of EBR::compute_dSdt_multi, Source/CHEM/FlowAdvance.cpp:157-403.
+//   k_chem_prims    c2prim_rgas over grow(bx, 3)        (Kernels.H:42-81)
+//   k_chem_trans    mu, lambda, D over grow(bx, 1)      (FlowAdvance.cpp:188-202)
+//   k_chem_faces<D> per face, in registers: Steger-Warming split of the 6
+//                   stencil cells (flow with the local gamma, species by the
+//                   split factor of FlowAdvance.cpp:214-242), WENO-Z of the
+//                   5 + 9 components, Fick diffusion (ChemViscous.H:108-199),
+//                   multispecies viscous + heat + species-enthalpy flux
+//                   (ChemViscous.H:201-355)
+//   k_chem_div      divop for the 5 + 9 components       (Kernels.H:84-97)
+// =====================================================================
+namespace ocfd {
+
+struct ChemBoxArgs {
+    View<const double> S, sp;
+    View<double> dsdt, dsdts;
+    View<double> flux[3], fluxs[3];
+    View<double> q;    // 8 primitives over grow(bx, qg)
+    int qg;            // primitive halo: 3 (WENO, regular boxes) or 2 (MUSCL, cut boxes)
+    View<double> tr;   // mu, lambda, D[9] over grow(bx, 1)
+    int lo[3], hi[3];
+    double dxinv[3];
+    int visc;
+    // cut-cell variant
+    int eb;
+    View<const uint32_t> flag;
+    View<const double> vfrac;
+    View<const double> ap[3];
+};
+
+// c2prim_rgas, Source/kernel/Kernels.H:42-81
+__device__ __forceinline__ void c2prim_real(const DevParm& P, const double* u, const double* rhoi, double* q) {
+    const double rho = dmax(u[0], P.smallr);
+    const double rhoinv = 1.0 / rho;
+    const double ux = u[1] * rhoinv, uy = u[2] * rhoinv, uz = u[3] * rhoinv;
+    const double kineng = 0.5 * (ux * ux + uy * uy + uz * uz);
+    const double ei = u[4] - rho * kineng;
+    q[QRHO] = rho;
+    q[QU] = ux;
+    q[QV] = uy;
+    q[QW] = uz;
+    const double T = get_t_given_ey(ei, rhoi, P.Ru);
+    const double p = ckpy(rhoi, T, P.Ru);
+    q[QT] = T;
+    q[QPRES] = p;
+    const double gama = p / ei + 1.0;
+    q[QGAMA] = gama;
+    q[QC] = sqrt(gama * p / rho);
+}
+
+__global__ void k_chem_prims(ChemBoxArgs B, DevParm P) {
+    const int g = B.qg;
+    const int gx = B.hi[0] - B.lo[0] + 1 + 2 * g, gy = B.hi[1] - B.lo[1] + 1 + 2 * g,
+              gz = B.hi[2] - B.lo[2] + 1 + 2 * g;
+    const long long n = (long long)gx * gy * gz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = B.lo[0] - g + (int)(c % gx), j = B.lo[1] - g + (int)((c / gx) % gy),
+                  k = B.lo[2] - g + (int)(c / ((long long)gx * gy));
+        double u[5], r[NSP], q[8];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) u[m] = B.S(i, j, k, m);
+#pragma unroll
+        for (int m = 0; m < NSP; ++m) r[m] = B.sp(i, j, k, m);
+        c2prim_real(P, u, r, q);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) B.q(i, j, k, m) = q[m];
+    }
+}
+
+__global__ void k_chem_trans(ChemBoxArgs B) {
+    const int gx = B.hi[0] - B.lo[0] + 3, gy = B.hi[1] - B.lo[1] + 3, gz = B.hi[2] - B.lo[2] + 3;
+    const long long n = (long long)gx * gy * gz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = B.lo[0] - 1 + (int)(c % gx), j = B.lo[1] - 1 + (int)((c / gx) % gy),
+                  k = B.lo[2] - 1 + (int)(c / ((long long)gx * gy));
+        double Yt[NSP], Xt[NSP], D[NSP];
+        const double T = B.q(i, j, k, QT), p = B.q(i, j, k, QPRES), rho = B.q(i, j, k, QRHO);
+#pragma unroll
+        for (int m = 0; m < NSP; ++m) Yt[m] = B.sp(i, j, k, m) / rho;
+        ckytx(Yt, Xt);
+        double mu, lam;
+        mixture_properties(T, Xt, mu, lam);
+        mix_diff_coeffs(T, p, Xt, D);
+        B.tr(i, j, k, 0) = mu;
+        B.tr(i, j, k, 1) = lam;
+#pragma unroll
+        for (int m = 0; m < NSP; ++m) B.tr(i, j, k, 2 + m) = D[m];
+    }
+}
+
+// Fick diffusion of the D-face (ChemViscous.H:108-199) added to the species
+// face flux fs[9]; the diffusive part is returned in fd[9].
+__device__ __forceinline__ void diffusion_face(const ChemBoxArgs& B, int D, int i, int j, int k,
+                                               double* fs, double* fd) {
+    const int li = i - (D == 0), lj = j - (D == 1), lk = k - (D == 2);
+    const double rhor = B.q(i, j, k, QRHO), rhol = B.q(li, lj, lk, QRHO);
+    const double rho = 0.5 * (rhol + rhor);
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) {
+        const double Ytr = B.sp(i, j, k, n) / rhor;
+        const double Ytl = B.sp(li, lj, lk, n) / rhol;
+        const double di = 0.5 * (B.tr(i, j, k, 2 + n) + B.tr(li, lj, lk, 2 + n));
+        const double tmp = rho * di * (Ytl - Ytr) * B.dxinv[D];
+        fd[n] = tmp;
+        fs[n] += tmp;
+    }
+}
+
+// face-averaged mu, lambda and species-enthalpy flux (ChemViscous.H:215-231)
+__device__ __forceinline__ void multi_face_props(const ChemBoxArgs& B, int D, int i, int j, int k,
+                                                 const double* fd, double& muf, double& lamf,
+                                                 double& hflux) {
+    const int li = i - (D == 0), lj = j - (D == 1), lk = k - (D == 2);
+    const double Tr = B.q(i, j, k, QT), Tl = B.q(li, lj, lk, QT);
+    const double T = 0.5 * (Tl + Tr);
+    muf = 0.5 * (B.tr(i, j, k, 0) + B.tr(li, lj, lk, 0));
+    lamf = 0.5 * (B.tr(i, j, k, 1) + B.tr(li, lj, lk, 1));
+    double h[NSP];
+    species_enthalpy(T, h);
+    double tmp = 0;
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) tmp += fd[n] * h[n];
+    hflux = tmp;
+}
+
+// multispecies viscous flux of a regular face (ChemViscous.H:201-355)
+__device__ __forceinline__ void visc_multi_face(const DevParm& P, const ChemBoxArgs& B, int D, int i,
+                                                int j, int k, double* f, double muf, double lamf,
+                                                double hflux) {
+    const int li = i - (D == 0), lj = j - (D == 1), lk = k - (D == 2);
+    const double Tr = B.q(i, j, k, QT), Tl = B.q(li, lj, lk, QT);
+    const double dT = (Tr - Tl) * B.dxinv[D];
+    double g[3][3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) g[m][D] = (B.q(i, j, k, QU + m) - B.q(li, lj, lk, QU + m)) * B.dxinv[D];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        if (t == D) continue;
+        const int ti = t == 0, tj = t == 1, tk = t == 2;
+        g[D][t] = (B.q(i + ti, j + tj, k + tk, QU + D) + B.q(li + ti, lj + tj, lk + tk, QU + D) -
+                   B.q(i - ti, j - tj, k - tk, QU + D) - B.q(li - ti, lj - tj, lk - tk, QU + D)) *
+                  (0.25 * B.dxinv[t]);
+        g[t][t] = (B.q(i + ti, j + tj, k + tk, QU + t) + B.q(li + ti, lj + tj, lk + tk, QU + t) -
+                   B.q(i - ti, j - tj, k - tk, QU + t) - B.q(li - ti, lj - tj, lk - tk, QU + t)) *
+                  (0.25 * B.dxinv[t]);
+    }
+    const double divu = g[0][0] + g[1][1] + g[2][2];
+    double tau[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+        tau[m] = (m == D) ? muf * (2.0 * g[D][D] - P.twoThirds * divu) : muf * (g[m][D] + g[D][m]);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) f[1 + m] += -tau[m];
+    f[4] += -0.5 * ((B.q(i, j, k, QU) + B.q(li, lj, lk, QU)) * tau[0] +
+                    (B.q(i, j, k, QV) + B.q(li, lj, lk, QV)) * tau[1] +
+                    (B.q(i, j, k, QW) + B.q(li, lj, lk, QW)) * tau[2]) -
+            lamf * dT - hflux;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_chem_faces(ChemBoxArgs B, DevParm P) {
+    const int fx = B.hi[0] - B.lo[0] + 1 + (D == 0), fy = B.hi[1] - B.lo[1] + 1 + (D == 1),
+              fz = B.hi[2] - B.lo[2] + 1 + (D == 2);
+    const long long nf = (long long)fx * fy * fz;
+    const int di = D == 0, dj = D == 1, dk = D == 2;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nf;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = B.lo[0] + (int)(c % fx), j = B.lo[1] + (int)((c / fx) % fy),
+                  k = B.lo[2] + (int)(c / ((long long)fx * fy));
+        double f[5], fs[NSP];
+        // split of the stencil cells i-3 .. i+2 along D; s = 0..5
+        double fp[6][5], fm[6][5], t1[6], tp[6], tm[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+            const int ci = i + (s - 3) * di, cj = j + (s - 3) * dj, ck = k + (s - 3) * dk;
+            const double d = B.q(ci, cj, ck, QRHO), u = B.q(ci, cj, ck, QU), v = B.q(ci, cj, ck, QV),
+                         w = B.q(ci, cj, ck, QW), cs = B.q(ci, cj, ck, QC), gamma = B.q(ci, cj, ck, QGAMA);
+            const double tmp1 = 1.0 / (2.0 * gamma);
+            const double tmp2 = 2.0 * (gamma - 1.0);
+            const double tmp3 = (3.0 - gamma) / (2.0 * (gamma - 1.0));
+            sw_split<D>(d, u, v, w, cs, tmp1, tmp2, tmp3, gamma - 1, fp[s], fm[s]);
+            const double un = D == 0 ? u : (D == 1 ? v : w);
+            const double E1 = un, E2 = un - cs, E3 = un + cs;
+            const double E1P = (E1 + fabs(E1)) * 0.5, E2P = (E2 + fabs(E2)) * 0.5, E3P = (E3 + fabs(E3)) * 0.5;
+            const double E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
+            t1[s] = tmp1;
+            tp[s] = tmp2 * E1P + E2P + E3P;
+            tm[s] = tmp2 * E1M + E2M + E3M;
+        }
+#pragma unroll
+        for (int n = 0; n < 5; ++n)
+            f[n] = wenoz_plus(fp[0][n], fp[1][n], fp[2][n], fp[3][n], fp[4][n]) +
+                   wenoz_minus(fm[1][n], fm[2][n], fm[3][n], fm[4][n], fm[5][n]);
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) {
+            double a[6], b[6];
+#pragma unroll
+            for (int s = 0; s < 6; ++s) {
+                const double tmp0 = B.sp(i + (s - 3) * di, j + (s - 3) * dj, k + (s - 3) * dk, n) * t1[s];
+                a[s] = tmp0 * tp[s];
+                b[s] = tmp0 * tm[s];
+            }
+            fs[n] = wenoz_plus(a[0], a[1], a[2], a[3], a[4]) + wenoz_minus(b[1], b[2], b[3], b[4], b[5]);
+        }
+        if (B.visc) {
+            double fd[NSP], muf, lamf, hflux;
+            diffusion_face(B, D, i, j, k, fs, fd);
+            multi_face_props(B, D, i, j, k, fd, muf, lamf, hflux);
+            visc_multi_face(P, B, D, i, j, k, f, muf, lamf, hflux);
+        }
+#pragma unroll
+        for (int n = 0; n < 5; ++n) B.flux[D](i, j, k, n) = f[n];
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) B.fluxs[D](i, j, k, n) = fs[n];
+    }
+}
+
+__global__ void k_chem_div(ChemBoxArgs B) {
+    const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1, nz = B.hi[2] - B.lo[2] + 1;
+    const long long n = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = B.lo[0] + (int)(c % nx), j = B.lo[1] + (int)((c / nx) % ny),
+                  k = B.lo[2] + (int)(c / ((long long)nx * ny));
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+            B.dsdt(i, j, k, m) = B.dxinv[0] * (B.flux[0](i, j, k, m) - B.flux[0](i + 1, j, k, m)) +
+                                 B.dxinv[1] * (B.flux[1](i, j, k, m) - B.flux[1](i, j + 1, k, m)) +
+                                 B.dxinv[2] * (B.flux[2](i, j, k, m) - B.flux[2](i, j, k + 1, m));
+#pragma unroll
+        for (int m = 0; m < NSP; ++m)
+            B.dsdts(i, j, k, m) = B.dxinv[0] * (B.fluxs[0](i, j, k, m) - B.fluxs[0](i + 1, j, k, m)) +
+                                  B.dxinv[1] * (B.fluxs[1](i, j, k, m) - B.fluxs[1](i, j + 1, k, m)) +
+                                  B.dxinv[2] * (B.fluxs[2](i, j, k, m) - B.fluxs[2](i, j, k + 1, m));
+    }
+}
+
+// ---- cut-cell multispecies box, Source/CHEM/FlowAdvanceBox.cpp:105-499 ----
+// Van Leer species flux of one face, FlowAdvanceBox.cpp:166-223
+__device__ __forceinline__ void vanleer_spec(const double* ql, const double* qr, const double* rl,
+                                             const double* rr, int D, double* fs) {
+    double fp[NSP], fm[NSP];
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) {
+        fp[n] = 0;
+        fm[n] = 0;
+    }
+    const double ul = ql[QU + D], ur = qr[QU + D];
+    const double cL = ql[QC], cR = qr[QC];
+    const double ML = ul / cL, MR = ur / cR, UL = ul, UR = ur;
+    if (ML >= 1.0) {
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) fp[n] = rl[n] * UL;
+    } else if (fabs(ML) < 1.0) {
+        const double Mp = 0.250 * (1.0 + ML) * (1.0 + ML);
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) fp[n] = rl[n] * cL * Mp;
+    }
+    if (fabs(MR) < 1.0) {
+        const double Mm = -0.250 * (MR - 1.0) * (MR - 1.0);
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) fm[n] = rr[n] * cR * Mm;
+    } else if (MR <= -1.0) {
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) fm[n] = rr[n] * UR;
+    }
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) fs[n] = fp[n] + fm[n];
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_chem_eb_faces(ChemBoxArgs B, DevParm P) {
+    const int fx = B.hi[0] - B.lo[0] + 1 + (D == 0), fy = B.hi[1] - B.lo[1] + 1 + (D == 1),
+              fz = B.hi[2] - B.lo[2] + 1 + (D == 2);
+    const long long nf = (long long)fx * fy * fz;
+    const int di = D == 0, dj = D == 1, dk = D == 2;
+    const View<const double> q{B.q.p, B.q.js, B.q.ks, B.q.ns, B.q.b0, B.q.b1, B.q.b2};
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nf;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = B.lo[0] + (int)(c % fx), j = B.lo[1] + (int)((c / fx) % fy),
+                  k = B.lo[2] + (int)(c / ((long long)fx * fy));
+        const uint32_t f = B.flag(i, j, k);
+        double ql[8], qr[8], rl[NSP], rr[NSP], flx[5], fs[NSP];
+#pragma unroll
+        for (int m = 0; m < 8; ++m)
+            eb_recon(f, D, q(i - 2 * di, j - 2 * dj, k - 2 * dk, m), q(i - di, j - dj, k - dk, m),
+                     q(i, j, k, m), q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
+#pragma unroll
+        for (int m = 0; m < NSP; ++m)
+            eb_recon(f, D, B.sp(i - 2 * di, j - 2 * dj, k - 2 * dk, m), B.sp(i - di, j - dj, k - dk, m),
+                     B.sp(i, j, k, m), B.sp(i + di, j + dj, k + dk, m), rl[m], rr[m]);
+        vanleer(P, 0.5 * (ql[QGAMA] + qr[QGAMA]), ql, qr, D, flx);
+        vanleer_spec(ql, qr, rl, rr, D, fs);
+        if (B.visc) {
+            double fd[NSP], muf, lamf, hflux;
+            diffusion_face(B, D, i, j, k, fs, fd);
+            multi_face_props(B, D, i, j, k, fd, muf, lamf, hflux);
+            eb_visc_face(P, q, B.flag, D, i, j, k, B.dxinv, flx, 1, true, muf, lamf, hflux);
+        }
+#pragma unroll
+        for (int n = 0; n < 5; ++n) B.flux[D](i, j, k, n) = flx[n];
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) B.fluxs[D](i, j, k, n) = fs[n];
+    }
+}
+
+// species divergence of a cut box (FlowAdvanceBox.cpp:407-460), negated; the
+// flow dSdt of a cut multispecies box is left zero as the reference leaves it
+// (its divc -> dSdt copy is commented out, FlowAdvanceBox.cpp:500-523)
+__global__ void k_chem_eb_div(ChemBoxArgs B) {
+    const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1, nz = B.hi[2] - B.lo[2] + 1;
+    const long long n = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = B.lo[0] + (int)(c % nx), j = B.lo[1] + (int)((c / nx) % ny),
+                  k = B.lo[2] + (int)(c / ((long long)nx * ny));
+#pragma unroll
+        for (int m = 0; m < 5; ++m) B.dsdt(i, j, k, m) = 0.0;
+        const uint32_t f = B.flag(i, j, k);
+        const double tmp = B.dxinv[0] / B.vfrac(i, j, k);
+        double out[NSP];
+        if (eb_covered(f)) {
+#pragma unroll
+            for (int m = 0; m < NSP; ++m) out[m] = 0.0;
+        } else if (eb_regular(f)) {
+#pragma unroll
+            for (int m = 0; m < NSP; ++m)
+                out[m] = B.dxinv[0] * (B.fluxs[0](i + 1, j, k, m) - B.fluxs[0](i, j, k, m)) +
+                         B.dxinv[1] * (B.fluxs[1](i, j + 1, k, m) - B.fluxs[1](i, j, k, m)) +
+                         B.dxinv[2] * (B.fluxs[2](i, j, k + 1, m) - B.fluxs[2](i, j, k, m));
+        } else {
+            const double axm = B.ap[0](i, j, k), axp = B.ap[0](i + 1, j, k);
+            const double aym = B.ap[1](i, j, k), ayp = B.ap[1](i, j + 1, k);
+            const double azm = B.ap[2](i, j, k), azp = B.ap[2](i, j, k + 1);
+#pragma unroll
+            for (int m = 0; m < NSP; ++m)
+                out[m] = tmp * (axp * B.fluxs[0](i + 1, j, k, m) - axm * B.fluxs[0](i, j, k, m) +
+                                ayp * B.fluxs[1](i, j + 1, k, m) - aym * B.fluxs[1](i, j, k, m) +
+                                azp * B.fluxs[2](i, j, k + 1, m) - azm * B.fluxs[2](i, j, k, m));
+            if (B.visc) {
+                const double apnorm = sqrt((axm - axp) * (axm - axp) + (aym - ayp) * (aym - ayp) +
+                                           (azm - azp) * (azm - azp));
+                const double un = B.q(i, j, k, QU) * (axm - axp) + B.q(i, j, k, QV) * (aym - ayp) +
+                                  B.q(i, j, k, QW) * (azm - azp);
+                const double lambda0 = fabs(un) + B.q(i, j, k, QC) * apnorm;
+#pragma unroll
+                for (int m = 0; m < NSP; ++m) {
+                    const double sn = B.sp(i, j, k, m);
+                    const double fpw = 0.5 * (sn * un + lambda0 * sn);
+                    const double fmw = -0.5 * (sn * un + lambda0 * sn);
+                    out[m] += (fpw + fmw) * tmp;
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < NSP; ++m) B.dsdts(i, j, k, m) = out[m] * -1.0;
+    }
+}
+
+static int chem_blocks(long long n, int threads, int sms) {
+    long long b = (n + threads - 1) / threads;
+    long long cap = (long long)sms * 64;
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+// Shared set-up of the regular and cut-cell multispecies box calls.
+static ocfd_status chem_box_setup(ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* spec,
+                                  const ocfd_array4* dSdt, const ocfd_array4* dSdt_spec,
+                                  const ocfd_array4* flux, const ocfd_array4* flux_spec,
+                                  const ocfd_box& bx, const double dxinv[3], unsigned flags,
+                                  int grow, const char* who, ChemBoxArgs& B) {
+    if (!ctx || !dxinv) return fail(OCFD_BAD_ARG, std::string(who) + ": null argument");
+    for (int d = 0; d < 3; ++d)
+        if (bx.hi[d] < bx.lo[d]) return fail(OCFD_BAD_ARG, std::string(who) + ": empty box");
+    if (!covers(S, bx, grow, 5) || !covers(spec, bx, grow, NSP))
+        return fail(OCFD_BAD_ARG, std::string(who) + ": S / spec must cover grow(bx," + std::to_string(grow) + ")");
+    if (!covers(dSdt, bx, 0, 5) || !covers(dSdt_spec, bx, 0, NSP))
+        return fail(OCFD_BAD_ARG, std::string(who) + ": dSdt / dSdt_spec must cover bx");
+    for (int d = 0; d < 3; ++d) {
+        if (flux && !covers(&flux[d], bx, 0, 5, d)) return fail(OCFD_BAD_ARG, std::string(who) + ": flux[d]");
+        if (flux_spec && !covers(&flux_spec[d], bx, 0, NSP, d))
+            return fail(OCFD_BAD_ARG, std::string(who) + ": flux_spec[d]");
+    }
+    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
+    // primitive halo: WENO needs 3 cells (regular boxes), MUSCL 2 (cut boxes)
+    const int g = grow >= 3 ? 3 : 2;
+    const long long qcells = (long long)(n[0] + 2 * g) * (n[1] + 2 * g) * (n[2] + 2 * g);
+    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    long long fcells[3];
+    for (int d = 0; d < 3; ++d) fcells[d] = (long long)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
+    size_t need = sizeof(double) * (8 * qcells + 11 * tcells);
+    if (!flux) need += sizeof(double) * 5 * (fcells[0] + fcells[1] + fcells[2]);
+    if (!flux_spec) need += sizeof(double) * NSP * (fcells[0] + fcells[1] + fcells[2]);
+    double* scr = static_cast<double*>(scratch(ctx, need));
+    if (!scr) return fail(OCFD_OUT_OF_MEMORY, std::string(who) + ": scratch");
+    B.S = view_of<const double>(S);
+    B.sp = view_of<const double>(spec);
+    B.dsdt = view_of<double>(dSdt);
+    B.dsdts = view_of<double>(dSdt_spec);
+    for (int d = 0; d < 3; ++d) {
+        B.lo[d] = bx.lo[d];
+        B.hi[d] = bx.hi[d];
+        B.dxinv[d] = dxinv[d];
+    }
+    B.q = View<double>{scr, n[0] + 2 * g, (long long)(n[0] + 2 * g) * (n[1] + 2 * g), qcells,
+                       bx.lo[0] - g, bx.lo[1] - g, bx.lo[2] - g};
+    B.qg = g;
+    scr += 8 * qcells;
+    B.tr = View<double>{scr, n[0] + 2, (long long)(n[0] + 2) * (n[1] + 2), tcells, bx.lo[0] - 1,
+                        bx.lo[1] - 1, bx.lo[2] - 1};
+    scr += 11 * tcells;
+    for (int d = 0; d < 3; ++d) {
+        const int sx = n[0] + (d == 0), sy = n[1] + (d == 1);
+        if (flux) {
+            B.flux[d] = view_of<double>(&flux[d]);
+        } else {
+            B.flux[d] = View<double>{scr, sx, (long long)sx * sy, fcells[d], bx.lo[0], bx.lo[1], bx.lo[2]};
+            scr += 5 * fcells[d];
+        }
+        if (flux_spec) {
+            B.fluxs[d] = view_of<double>(&flux_spec[d]);
+        } else {
+            B.fluxs[d] = View<double>{scr, sx, (long long)sx * sy, fcells[d], bx.lo[0], bx.lo[1], bx.lo[2]};
+            scr += NSP * fcells[d];
+        }
+    }
+    B.visc = (flags & OCFD_VISC) != 0;
+    return OCFD_OK;
+}
+
+}  // namespace ocfd
+
+extern "C" ocfd_status ocfd_rhs_chem_box_f64(ocfd_context* ctx, const ocfd_array4* S,
+                                             const ocfd_array4* spec, const ocfd_array4* dSdt,
+                                             const ocfd_array4* dSdt_spec, const ocfd_array4* flux,
+                                             const ocfd_array4* flux_spec, ocfd_box bx,
+                                             const double dxinv[3], unsigned flags, void* stream) {
+    using namespace ocfd;
+    if (flags & ~(unsigned)OCFD_VISC) return fail(OCFD_BAD_ARG, "ocfd_rhs_chem_box_f64: unsupported flags");
+    ChemBoxArgs B{};
+    ocfd_status s = chem_box_setup(ctx, S, spec, dSdt, dSdt_spec, flux, flux_spec, bx, dxinv, flags, 3,
+                                   "ocfd_rhs_chem_box_f64", B);
+    if (s != OCFD_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int sms = ctx->num_sms;
+    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
+    const long long qcells = (long long)(n[0] + 2 * B.qg) * (n[1] + 2 * B.qg) * (n[2] + 2 * B.qg);
+    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    k_chem_prims<<<chem_blocks(qcells, 128, sms), 128, 0, st>>>(B, ctx->parm);
+    if (B.visc) k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
+    k_chem_faces<0><<<chem_blocks((long long)(n[0] + 1) * n[1] * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
+    k_chem_faces<1><<<chem_blocks((long long)n[0] * (n[1] + 1) * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
+    k_chem_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, ctx->parm);
+    k_chem_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
+    return check_launch("ocfd_rhs_chem_box_f64");
+}
+
+extern "C" ocfd_status ocfd_rhs_chem_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S,
+                                                const ocfd_array4* spec, const ocfd_array4* dSdt,
+                                                const ocfd_array4* dSdt_spec, const ocfd_array4* flux,
+                                                const ocfd_array4* flux_spec, const ocfd_flag4* flag,
+                                                const ocfd_array4* vfrac, const ocfd_array4* apx,
+                                                const ocfd_array4* apy, const ocfd_array4* apz,
+                                                const ocfd_array4* const* fc, const ocfd_array4* bcent,
+                                                ocfd_box bx, const double dxinv[3], unsigned flags,
+                                                void* stream) {
+    using namespace ocfd;
+    (void)fc;
+    (void)bcent;
+    if (flags & ~(unsigned)OCFD_VISC) return fail(OCFD_BAD_ARG, "ocfd_rhs_chem_eb_box_f64: unsupported flags");
+    if (!covers_flag(flag, bx, 1)) return fail(OCFD_BAD_ARG, "ocfd_rhs_chem_eb_box_f64: flag must cover grow(bx,1)");
+    if (!covers(vfrac, bx, 0, 1)) return fail(OCFD_BAD_ARG, "ocfd_rhs_chem_eb_box_f64: vfrac must cover bx");
+    const ocfd_array4* ap[3] = {apx, apy, apz};
+    for (int d = 0; d < 3; ++d)
+        if (!covers(ap[d], bx, 0, 1, d)) return fail(OCFD_BAD_ARG, "ocfd_rhs_chem_eb_box_f64: area fractions");
+    ChemBoxArgs B{};
+    ocfd_status s = chem_box_setup(ctx, S, spec, dSdt, dSdt_spec, flux, flux_spec, bx, dxinv, flags, 2,
+                                   "ocfd_rhs_chem_eb_box_f64", B);
+    if (s != OCFD_OK) return s;
+    B.eb = 1;
+    B.flag = view_of_flag(flag);
+    B.vfrac = view_of<const double>(vfrac);
+    for (int d = 0; d < 3; ++d) B.ap[d] = view_of<const double>(ap[d]);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int sms = ctx->num_sms;
+    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
+    const long long qcells = (long long)(n[0] + 2 * B.qg) * (n[1] + 2 * B.qg) * (n[2] + 2 * B.qg);
+    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    k_chem_prims<<<chem_blocks(qcells, 128, sms), 128, 0, st>>>(B, ctx->parm);
+    if (B.visc) k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
+    k_chem_eb_faces<0><<<chem_blocks((long long)(n[0] + 1) * n[1] * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
+    k_chem_eb_faces<1><<<chem_blocks((long long)n[0] * (n[1] + 1) * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
+    k_chem_eb_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, ctx->parm);
+    k_chem_eb_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
+    return check_launch("ocfd_rhs_chem_eb_box_f64");
 }

@@ -66,6 +66,20 @@ _SIGS = {
                                            ctypes.POINTER(Array4), ctypes.POINTER(Array4), ctypes.POINTER(Array4),
                                            ctypes.c_void_p, ctypes.POINTER(Array4), Box,
                                            ctypes.POINTER(ctypes.c_double), ctypes.c_uint, ctypes.c_void_p]),
+    "ocfd_chem_advance_box_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                                 Box, ctypes.c_double, ctypes.c_void_p]),
+    "ocfd_spec_renorm_box_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                                Box, ctypes.c_void_p]),
+    "ocfd_rhs_chem_box_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                             ctypes.POINTER(Array4), ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                             ctypes.POINTER(Array4), Box, ctypes.POINTER(ctypes.c_double),
+                                             ctypes.c_uint, ctypes.c_void_p]),
+    "ocfd_rhs_chem_eb_box_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                                ctypes.POINTER(Array4), ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                                ctypes.POINTER(Array4), ctypes.POINTER(Flag4), ctypes.POINTER(Array4),
+                                                ctypes.POINTER(Array4), ctypes.POINTER(Array4), ctypes.POINTER(Array4),
+                                                ctypes.c_void_p, ctypes.POINTER(Array4), Box,
+                                                ctypes.POINTER(ctypes.c_double), ctypes.c_uint, ctypes.c_void_p]),
     "ocfd_measure_fma_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 

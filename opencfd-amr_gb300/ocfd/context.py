@@ -87,3 +87,52 @@ class Context:
                                           ctypes.byref(ap[1]), ctypes.byref(ap[2]), None, None,
                                           box(lo, hi), dx, flags, _stream_ptr(stream))
         check(st, "ocfd_rhs_eb_box_f64")
+
+    # ---- chemistry ---------------------------------------------------------
+    def chem_advance_box(self, S, spec, lo, hi, dt, S_begin=None, spec_begin=None, stream=None):
+        """One chemistry substep in place on (5, nz, ny, nx) / (9, nz, ny, nx)
+        tensors (or larger arrays described by *_begin)."""
+        aS = array4(S, S_begin if S_begin is not None else lo)
+        aR = array4(spec, spec_begin if spec_begin is not None else lo)
+        check(self.lib.ocfd_chem_advance_box_f64(self.h, ctypes.byref(aS), ctypes.byref(aR),
+                                                  box(lo, hi), dt, _stream_ptr(stream)),
+              "ocfd_chem_advance_box_f64")
+
+    def spec_renorm_box(self, S, spec, lo, hi, S_begin=None, spec_begin=None, stream=None):
+        aS = array4(S, S_begin if S_begin is not None else lo)
+        aR = array4(spec, spec_begin if spec_begin is not None else lo)
+        check(self.lib.ocfd_spec_renorm_box_f64(self.h, ctypes.byref(aS), ctypes.byref(aR),
+                                                 box(lo, hi), _stream_ptr(stream)),
+              "ocfd_spec_renorm_box_f64")
+
+    def rhs_chem_box(self, S, spec, dSdt, dSdt_spec, lo, hi, dxinv, flags=0, flux=None,
+                     flux_spec=None, stream=None):
+        """Regular multispecies box; S (5) and spec (9) grown by 4 around lo..hi."""
+        g4 = tuple(l - 4 for l in lo)
+        aS, aR = array4(S, g4), array4(spec, g4)
+        aD, aDs = array4(dSdt, lo), array4(dSdt_spec, lo)
+        fl = (Array4 * 3)(*[array4(f, lo) for f in flux]) if flux is not None else None
+        fs = (Array4 * 3)(*[array4(f, lo) for f in flux_spec]) if flux_spec is not None else None
+        dx = (ctypes.c_double * 3)(*dxinv)
+        check(self.lib.ocfd_rhs_chem_box_f64(self.h, ctypes.byref(aS), ctypes.byref(aR),
+                                              ctypes.byref(aD), ctypes.byref(aDs), fl, fs,
+                                              box(lo, hi), dx, flags, _stream_ptr(stream)),
+              "ocfd_rhs_chem_box_f64")
+
+    def rhs_chem_eb_box(self, S, spec, dSdt, dSdt_spec, geom, lo, hi, dxinv, flags=0, flux=None,
+                        flux_spec=None, stream=None):
+        """Cut multispecies box; S, spec and geom flag/vfrac grown by 4 around lo..hi."""
+        g4 = tuple(l - 4 for l in lo)
+        aS, aR = array4(S, g4), array4(spec, g4)
+        aD, aDs = array4(dSdt, lo), array4(dSdt_spec, lo)
+        fl = (Array4 * 3)(*[array4(f, lo) for f in flux]) if flux is not None else None
+        fs = (Array4 * 3)(*[array4(f, lo) for f in flux_spec]) if flux_spec is not None else None
+        af, av = flag4(geom["flag"], g4), array4(geom["vfrac"], g4)
+        ap = [array4(geom[k], lo) for k in ("apx", "apy", "apz")]
+        dx = (ctypes.c_double * 3)(*dxinv)
+        check(self.lib.ocfd_rhs_chem_eb_box_f64(self.h, ctypes.byref(aS), ctypes.byref(aR),
+                                                 ctypes.byref(aD), ctypes.byref(aDs), fl, fs,
+                                                 ctypes.byref(af), ctypes.byref(av), ctypes.byref(ap[0]),
+                                                 ctypes.byref(ap[1]), ctypes.byref(ap[2]), None, None,
+                                                 box(lo, hi), dx, flags, _stream_ptr(stream)),
+              "ocfd_rhs_chem_eb_box_f64")
