@@ -154,6 +154,24 @@ ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S, const o
                                 const ocfd_array4* const* fc, const ocfd_array4* bcent,
                                 ocfd_box bx, const double dxinv[3], unsigned flags, void* stream);
 
+/* Same computation as ocfd_rhs_eb_box_f64, for callers that cannot let a
+ * library allocate device memory (applications that own all device memory
+ * through their own pool, or code where a cudaMalloc/cudaFree, which can
+ * synchronise the device, must not happen).  It has no counterpart in the
+ * reference.  Its scratch is a fixed 16 MiB array compiled into the library
+ * (2^21 doubles), held by every GPU that loads the library until exit; a box
+ * needing more (7 (nx+4)(ny+4)(nz+4) doubles, plus 5 per face of the three face
+ * boxes when flux is NULL) is rejected with OCFD_BAD_ARG.  It allocates nothing.
+ * The first call on a device looks up the array's device address (the
+ * context's device must be current); make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller. */
+ocfd_status ocfd_rhs_eb_box_f64_static_scratch(
+    ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* dSdt, const ocfd_array4* flux,
+    const ocfd_flag4* flag, const ocfd_array4* vfrac, const ocfd_array4* apx,
+    const ocfd_array4* apy, const ocfd_array4* apz, const ocfd_array4* const* fc,
+    const ocfd_array4* bcent, ocfd_box bx, const double dxinv[3], unsigned flags, void* stream);
+
 /* Regular box, multispecies (9-species Li-Dryer gas): real-gas primitives (T by
  * Newton on NASA-7, p from the species, gamma = 1 + p/e), Steger-Warming split of
  * the flow with the local gamma and of the species densities, WENO-Z of all
