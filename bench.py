@@ -255,6 +255,11 @@ def run_ours(args, world, rank, local):
     e2e_ms = allreduce_max(e0.elapsed_time(e1) / e2e_steps, world)
     e2e_value = cells * world / (e2e_ms * 1e-3)
 
+    # matched error: the other form from the same initial state to the same time
+    l1err = None
+    if rank == 0:
+        l1err = matched_l1(ctx, c, boxes, flags)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu_steps = 2
@@ -269,6 +274,7 @@ def run_ours(args, world, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.form == "fp64" else "f32-flux/f64-state", "data": "synthetic",
             "config": {"workload": c["name"], "form": args.form, "cells": cells, "boxes": len(boxes),
+                       "l1_vs_other_form": l1err,
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -285,6 +291,34 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
     lev.close()
     ctx.close()
+
+
+def matched_l1(ctx, c, boxes, flags, steps=40):
+    """L1 (sum|a-b| / sum|b|, as fcompare) of density and pressure between this
+    form and the other one after `steps` CFL steps of the FP64 form, both
+    stopped at the same time."""
+    import numpy as np
+    import ocfd
+    from ocfd.level import Level
+    out = {}
+    t_end = None
+    for f in (0, ocfd.FLUX_FP32):
+        lev = Level(ctx, boxes, tuple(n - 1 for n in c["n"]), c["lo_bc"], c["hi_bc"], c["dx"],
+                    c["prob_lo"], c["bc_case"], c["case_params"])
+        lev.set_global(c["G"])
+        if t_end is None:
+            lev.advance(steps, CFL, f)
+            t_end = lev.time()[0]
+        else:
+            lev.set_stop_time(t_end)
+            lev.advance(4 * steps, CFL, f)
+        out[f] = lev.get_global()
+        lev.close()
+    a, b = out[ocfd.FLUX_FP32], out[0]
+    pr = lambda U: 0.4 * (U[4] - 0.5 * (U[1] ** 2 + U[2] ** 2 + U[3] ** 2) / U[0])
+    l1 = lambda x, y: float(np.abs(x - y).sum() / np.abs(y).sum())
+    return {"rho": l1(a[0], b[0]), "p": l1(pr(a), pr(b)), "t": t_end, "steps_fp64": steps,
+            "forms": "fp32-flux vs fp64"}
 
 
 def main():

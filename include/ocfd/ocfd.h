@@ -282,6 +282,11 @@ ocfd_status ocfd_level_time(ocfd_level* level, double* time, double* last_dt, vo
 /* Set the level time and forget the previous dt (the next step is not limited). */
 ocfd_status ocfd_level_set_time(ocfd_level* level, double time, void* stream);
 
+/* Steps that would pass `stop_time` are shortened to end on it, and later steps
+ * have dt = 0 (stop-time limit of EBR::computeNewDt, Source/EBR.cpp:277-286).
+ * Default: no stop time. */
+ocfd_status ocfd_level_set_stop_time(ocfd_level* level, double stop_time, void* stream);
+
 /* Cells of the level (valid cells of all boxes). */
 int64_t ocfd_level_cells(const ocfd_level* level);
 /* Kernels one ocfd_level_advance step launches with `flags`. */

@@ -35,26 +35,28 @@ __device__ __forceinline__ void c2prim_ideal(const DevParm& P, double u0, double
 
 // Steger-Warming split along D (Source/kernel/FluxSplit.H:11-193), given the
 // split constants t1 = 1/(2g), t2 = 2(g-1), t3 = (3-g)/(2(g-1)), gm1 = g-1.
-template <int D>
-__device__ __forceinline__ void sw_split(double d, double u, double v, double w, double c,
-                                         double t1, double t2, double t3, double gm1,
-                                         double* fp, double* fm) {
-    const double vel[3] = {u, v, w};
-    const double un = vel[D];
-    const double uc1 = un - c, uc2 = un + c;
-    double a0 = u, a1 = v, a2 = w, b0 = u, b1 = v, b2 = w;
+// T = double keeps the reference's expressions; T = float serves the
+// mixed-precision form.
+template <int D, class T = double>
+__device__ __forceinline__ void sw_split(T d, T u, T v, T w, T c, T t1, T t2, T t3, T gm1, T* fp,
+                                         T* fm) {
+    const T vel[3] = {u, v, w};
+    const T un = vel[D];
+    const T uc1 = un - c, uc2 = un + c;
+    T a0 = u, a1 = v, a2 = w, b0 = u, b1 = v, b2 = w;
     if (D == 0) { a0 = uc1; b0 = uc2; }
     if (D == 1) { a1 = uc1; b1 = uc2; }
     if (D == 2) { a2 = uc1; b2 = uc2; }
-    const double vvc1 = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
-    const double vvc2 = 0.5 * (b0 * b0 + b1 * b1 + b2 * b2);
-    const double v2 = gm1 * (u * u + v * v + w * w);
-    const double w2 = t3 * c * c;
-    const double E1 = un, E2 = un - c, E3 = un + c;
-    const double E1P = (E1 + fabs(E1)) * 0.5, E2P = (E2 + fabs(E2)) * 0.5, E3P = (E3 + fabs(E3)) * 0.5;
-    const double E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
-    const double t0 = d * t1;
-    const double sp = t2 * E1P + E2P + E3P, sm = t2 * E1M + E2M + E3M;
+    const T half = T(0.5);
+    const T vvc1 = half * (a0 * a0 + a1 * a1 + a2 * a2);
+    const T vvc2 = half * (b0 * b0 + b1 * b1 + b2 * b2);
+    const T v2 = gm1 * (u * u + v * v + w * w);
+    const T w2 = t3 * c * c;
+    const T E1 = un, E2 = un - c, E3 = un + c;
+    const T E1P = (E1 + fabs(E1)) * half, E2P = (E2 + fabs(E2)) * half, E3P = (E3 + fabs(E3)) * half;
+    const T E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
+    const T t0 = d * t1;
+    const T sp = t2 * E1P + E2P + E3P, sm = t2 * E1M + E2M + E3M;
     fp[URHO] = t0 * sp;
     fm[URHO] = t0 * sm;
 #pragma unroll

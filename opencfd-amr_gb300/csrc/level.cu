@@ -53,6 +53,7 @@ struct BcTag {
 struct StepState {
     double time, dt, dt_prev, cfl;
     unsigned long long cfl_min;
+    double stop_time;  // the last step is shortened to land on it (Source/EBR.cpp:279-286)
 };
 
 struct BcInfo {
@@ -193,6 +194,9 @@ __global__ void k_step_begin(StepState* st) {
     const double est = __longlong_as_double((long long)st->cfl_min);
     double dt = st->cfl * est;
     if (st->dt_prev > 0 && dt > 1.1 * st->dt_prev) dt = 1.1 * st->dt_prev;
+    // stop-time limit of EBR::computeNewDt (Source/EBR.cpp:277-286): eps = 0.001 dt
+    if (st->time + dt > st->stop_time - 0.001 * dt) dt = st->stop_time - st->time;
+    if (dt < 0) dt = 0;
     st->dt = dt;
     st->cfl_min = 0x7FF0000000000000ULL;
 }
@@ -203,6 +207,8 @@ __global__ void k_step_end(StepState* st) {
 }
 
 __global__ void k_reset_cfl(StepState* st) { st->cfl_min = 0x7FF0000000000000ULL; }
+
+__global__ void k_set_stop(StepState* st, double t) { st->stop_time = t; }
 
 __global__ void k_set_time(StepState* st, double t) {
     st->time = t;
@@ -559,6 +565,7 @@ ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, oc
     if (s == OCFD_OK) s = upload(&L->d_tile_start, tile_start);
     if (s == OCFD_OK) {
         k_set_time<<<1, 1>>>(L->d_step, 0.0);
+        k_set_stop<<<1, 1>>>(L->d_step, __builtin_huge_val());
         s = check_launch("ocfd_level_create");
         if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = fail(OCFD_LAUNCH_FAIL, "level setup");
     }
@@ -693,6 +700,12 @@ ocfd_status ocfd_level_time(ocfd_level* L, double* time, double* last_dt, void* 
 }
 
 int64_t ocfd_level_cells(const ocfd_level* L) { return L ? L->ncells : 0; }
+
+ocfd_status ocfd_level_set_stop_time(ocfd_level* L, double stop_time, void* stream) {
+    if (!L) return fail(OCFD_BAD_ARG, "ocfd_level_set_stop_time");
+    k_set_stop<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(L->d_step, stop_time);
+    return check_launch("ocfd_level_set_stop_time");
+}
 
 int ocfd_level_launches_per_step(const ocfd_level* L, unsigned flags) {
     if (!L) return 0;

@@ -1,0 +1,417 @@
+// Fused regular-box right-hand side, templated on the precision of the flux
+// evaluation FT:
+//   FT = double  the plain FP64 form (reference operation order; parity 1e-12)
+//   FT = float   the mixed-precision form: primitives, Steger-Warming split,
+//                WENO-Z (stencils normalised by a power of two, the smoothness
+//                epsilon rescaled into the normalised units), viscous flux and
+//                divergence in FP32; the RK accumulation and the CFL bound stay
+//                FP64.
+// Included by rhs_regular.cu (double) and rhs_regular_f32.cu (float).
+//
+// One CTA owns a TX x TY x TZ tile.  Per direction D:
+//   1. the tile's pencil along D (tile + 3 cells each side) is read from the
+//      state, turned into primitives and split into F+ / F- (10 values per
+//      cell) in shared memory,
+//   2. WENO-Z face fluxes of the tile's T_D+1 faces x 5 components are formed
+//      in shared memory (work items = face x component),
+//   3. with OCFD_VISC the viscous stress / heat flux is added per face from a
+//      primitive ring (tile grown by 1) staged once per tile,
+//   4. each cell thread accumulates dxinv_D (F_f - F_f+1) in registers in the
+//      reference's summation order x, y, z (Source/kernel/Kernels.H:94-96);
+//      face fluxes are written out when the caller asked for them (reflux).
+// Only U (read) and the output touch HBM.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device_physics.cuh"
+#include "ocfd_internal.h"
+#include "rhs_regular.h"
+
+namespace ocfd {
+
+constexpr size_t kMaxSmem = 227 * 1024;  // opt-in dynamic shared memory per CTA
+
+template <int D, int TX, int TY, int TZ>
+struct Pencil {
+    static constexpr int PX = TX + (D == 0 ? 6 : 0);
+    static constexpr int PY = TY + (D == 1 ? 6 : 0);
+    static constexpr int PZ = TZ + (D == 2 ? 6 : 0);
+    static constexpr int N = PX * PY * PZ;
+    static constexpr int FX = TX + (D == 0);
+    static constexpr int FY = TY + (D == 1);
+    static constexpr int FZ = TZ + (D == 2);
+    static constexpr int NF = FX * FY * FZ;
+    static constexpr int PST = D == 0 ? 1 : (D == 1 ? PX : PX * PY);  // pencil stride along D
+    static constexpr int FST = D == 0 ? 1 : (D == 1 ? FX : FX * FY);  // face stride along D
+    static constexpr int SMEM = 10 * N + 5 * NF;                       // elements
+};
+
+template <int TX, int TY, int TZ>
+struct Ring {
+    static constexpr int RX = TX + 2, RY = TY + 2, RZ = TZ + 2;
+    static constexpr int N = RX * RY * RZ;
+};
+
+template <int TX, int TY, int TZ>
+__host__ __device__ constexpr int pencil_elems() {
+    constexpr int a = Pencil<0, TX, TY, TZ>::SMEM;
+    constexpr int b = Pencil<1, TX, TY, TZ>::SMEM;
+    constexpr int c = Pencil<2, TX, TY, TZ>::SMEM;
+    return a > b ? (a > c ? a : c) : (b > c ? b : c);
+}
+
+template <class FT, int TX, int TY, int TZ, bool VISC>
+__host__ __device__ constexpr size_t regular_smem_bytes() {
+    return sizeof(FT) * (pencil_elems<TX, TY, TZ>() + (VISC ? 4 * Ring<TX, TY, TZ>::N : 0));
+}
+
+// ------------------------------------------------------------ precision traits
+template <class FT>
+struct Prec;
+
+// FP64: the reference's expressions
+template <>
+struct Prec<double> {
+    // q = rho, u, v, w, p, T, c
+    static __device__ __forceinline__ void prims(const DevParm& P, const View<const double>& S, int i,
+                                                 int j, int k, double* q) {
+        c2prim_ideal(P, S(i, j, k, 0), S(i, j, k, 1), S(i, j, k, 2), S(i, j, k, 3), S(i, j, k, 4), q);
+    }
+    template <int D>
+    static __device__ __forceinline__ void split(const DevParm& P, const double* q, double* fp, double* fm) {
+        sw_split<D>(q[QRHO], q[QU], q[QV], q[QW], q[QC], P.sw_tmp1, P.sw_tmp2, P.sw_tmp3, P.sw_gm1, fp, fm);
+    }
+    static __device__ __forceinline__ double weno(const double* a, const double* b, int s) {
+        return wenoz_plus(a[0], a[s], a[2 * s], a[3 * s], a[4 * s]) +
+               wenoz_minus(b[s], b[2 * s], b[3 * s], b[4 * s], b[5 * s]);
+    }
+    static __device__ __forceinline__ double mu(const DevParm& P, double T) { return sutherland(P, T); }
+};
+
+// WENO-Z in FP32.  The stencil values are normalised by the power of two s
+// nearest above their largest magnitude (an exact scaling), and the reference's
+// absolute smoothness epsilon (1e-6, Reconstruction.H:83) is rescaled to the
+// local state as eps / s^2 in the normalised units.  The scheme is therefore
+// the FP64 scheme up to FP32 rounding, and no smoothness indicator can overflow
+// whatever the magnitude of the flux.
+__device__ __forceinline__ float wenoz_side_f(float V1, float V2, float V3, float V4, float V5, float eps) {
+    float s11 = (13.0f / 12.0f) * (V1 - 2.0f * V2 + V3) * (V1 - 2.0f * V2 + V3) +
+                0.25f * (V1 - 4.0f * V2 + 3.0f * V3) * (V1 - 4.0f * V2 + 3.0f * V3);
+    float s22 = (13.0f / 12.0f) * (V2 - 2.0f * V3 + V4) * (V2 - 2.0f * V3 + V4) + 0.25f * (V2 - V4) * (V2 - V4);
+    float s33 = (13.0f / 12.0f) * (V3 - 2.0f * V4 + V5) * (V3 - 2.0f * V4 + V5) +
+                0.25f * (3.0f * V3 - 4.0f * V4 + V5) * (3.0f * V3 - 4.0f * V4 + V5);
+    const float s55 = fabsf(s11 - s33);
+    const float r1 = __fdividef(s55, eps + s11), r2 = __fdividef(s55, eps + s22), r3 = __fdividef(s55, eps + s33);
+    const float a1 = 1.0f + r1 * r1, a2 = 6.0f * (1.0f + r2 * r2), a3 = 3.0f * (1.0f + r3 * r3);
+    const float v1 = 2.0f * V1 - 7.0f * V2 + 11.0f * V3;
+    const float v2 = -V2 + 5.0f * V3 + 2.0f * V4;
+    const float v3 = 2.0f * V3 + 5.0f * V4 - V5;
+    return __fdividef(a1 * v1 + a2 * v2 + a3 * v3, 6.0f * (a1 + a2 + a3));
+}
+
+// f+ at cells i-3..i+1, or f- at i+2..i-2 (the mirrored stencil): normalise,
+// reconstruct, scale back
+__device__ __forceinline__ float wenoz_norm_f(float V1, float V2, float V3, float V4, float V5) {
+    const float m = fmaxf(fmaxf(fmaxf(fabsf(V1), fabsf(V2)), fmaxf(fabsf(V3), fabsf(V4))), fabsf(V5));
+    const int ex = (__float_as_int(m) >> 23) & 0xff;
+    // zero / subnormal stencils, and inf / NaN, are reconstructed as they are
+    if (ex == 0 || ex > 250) return wenoz_side_f(V1, V2, V3, V4, V5, 1e-6f);
+    const float sc = __int_as_float((254 - ex) << 23);      // 2^-(ex-127)
+    const float inv = __int_as_float(ex << 23);             // 2^(ex-127)
+    // 1e-6 absolute, in normalised units; kept > 0 so that 0/0 cannot occur
+    const float eps = fmaxf(1e-6f * sc * sc, 1e-37f);
+    return wenoz_side_f(V1 * sc, V2 * sc, V3 * sc, V4 * sc, V5 * sc, eps) * inv;
+}
+
+template <>
+struct Prec<float> {
+    static __device__ __forceinline__ void prims(const DevParm& P, const View<const double>& S, int i,
+                                                 int j, int k, float* q) {
+        const float g = (float)P.gamma;
+        const float rho = fmaxf((float)S(i, j, k, 0), (float)P.smallr);
+        const float rhoinv = __frcp_rn(rho);
+        const float ux = (float)S(i, j, k, 1) * rhoinv, uy = (float)S(i, j, k, 2) * rhoinv,
+                    uz = (float)S(i, j, k, 3) * rhoinv;
+        const float ei = (float)(S(i, j, k, 4) - 0.5 * S(i, j, k, 0) * ((double)ux * ux + (double)uy * uy + (double)uz * uz));
+        const float p = fmaxf((g - 1.0f) * ei, (float)P.smallp);
+        q[QRHO] = rho;
+        q[QU] = ux;
+        q[QV] = uy;
+        q[QW] = uz;
+        q[QPRES] = p;
+        q[QT] = p * rhoinv * (float)(1.0 / P.Rg);
+        q[QC] = sqrtf(g * p * rhoinv);
+    }
+    template <int D>
+    static __device__ __forceinline__ void split(const DevParm& P, const float* q, float* fp, float* fm) {
+        sw_split<D, float>(q[QRHO], q[QU], q[QV], q[QW], q[QC], (float)P.sw_tmp1, (float)P.sw_tmp2,
+                           (float)P.sw_tmp3, (float)P.sw_gm1, fp, fm);
+    }
+    static __device__ __forceinline__ float weno(const float* a, const float* b, int s) {
+        return wenoz_norm_f(a[0], a[s], a[2 * s], a[3 * s], a[4 * s]) +
+               wenoz_norm_f(b[5 * s], b[4 * s], b[3 * s], b[2 * s], b[s]);
+    }
+    static __device__ __forceinline__ float mu(const DevParm& P, float T) {
+        return (float)P.C_s * T * sqrtf(T) / (T + (float)P.T_s);
+    }
+};
+
+// Viscous stress and heat flux of the D-face between ring cells (r - e_D) and r,
+// Source/kernel/Diffusion.H:7-131.  ring holds u, v, w, T (4 planes of RN).
+template <class FT, int D, int TX, int TY, int TZ>
+__device__ __forceinline__ void visc_face(const DevParm& P, const FT* ring, int rx, int ry, int rz,
+                                          const double* dxinv_d, FT* f /*stride fs*/, int fs) {
+    using R = Ring<TX, TY, TZ>;
+    constexpr int S[3] = {1, R::RX, R::RX * R::RY};
+    const FT dxinv[3] = {(FT)dxinv_d[0], (FT)dxinv_d[1], (FT)dxinv_d[2]};
+    const FT kOverMu = (FT)P.kOverMu, twoThirds = (FT)P.twoThirds;
+    const int c = rx + ry * R::RX + rz * R::RX * R::RY;
+    const int l = c - S[D];
+    const FT* qu = ring;
+    const FT* qT = ring + 3 * R::N;
+    const FT Tr = qT[c], Tl = qT[l];
+    const FT mutl = Prec<FT>::mu(P, Tl), mutr = Prec<FT>::mu(P, Tr);
+    const FT ktl = mutl * kOverMu, ktr = mutr * kOverMu;
+    const FT dT = (Tr - Tl) * dxinv[D];
+    FT g[3][3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) g[m][D] = (qu[m * R::N + c] - qu[m * R::N + l]) * dxinv[D];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        if (t == D) continue;
+        const int st = S[t];
+        // d(u_D)/dx_t and d(u_t)/dx_t averaged over the two cells of the face
+        g[D][t] = (qu[D * R::N + c + st] + qu[D * R::N + l + st] - qu[D * R::N + c - st] -
+                   qu[D * R::N + l - st]) * (FT(0.25) * dxinv[t]);
+        g[t][t] = (qu[t * R::N + c + st] + qu[t * R::N + l + st] - qu[t * R::N + c - st] -
+                   qu[t * R::N + l - st]) * (FT(0.25) * dxinv[t]);
+    }
+    const FT divu = g[0][0] + g[1][1] + g[2][2];
+    const FT muf = FT(0.5) * (mutl + mutr);
+    FT tau[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+        tau[m] = (m == D) ? muf * (FT(2.0) * g[D][D] - twoThirds * divu) : muf * (g[m][D] + g[D][m]);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) f[(1 + m) * fs] += -tau[m];
+    f[4 * fs] += FT(-0.5) * ((qu[c] + qu[l]) * tau[0] + (qu[R::N + c] + qu[R::N + l]) * tau[1] +
+                             (qu[2 * R::N + c] + qu[2 * R::N + l]) * tau[2] + (ktl + ktr) * dT);
+}
+
+template <class FT, int D, int TX, int TY, int TZ, bool VISC>
+__device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int i0, int j0, int k0,
+                                      FT* F, FT* FF, const FT* ring, FT* acc) {
+    using PC = Pencil<D, TX, TY, TZ>;
+    constexpr int NT = TX * TY * TZ;
+    const int tid = threadIdx.x;
+    // ---- 1. primitives and Steger-Warming split over the pencil
+    for (int c = tid; c < PC::N; c += NT) {
+        const int px = c % PC::PX, py = (c / PC::PX) % PC::PY, pz = c / (PC::PX * PC::PY);
+        const int gi = i0 + px - (D == 0 ? 3 : 0);
+        const int gj = j0 + py - (D == 1 ? 3 : 0);
+        const int gk = k0 + pz - (D == 2 ? 3 : 0);
+        FT fp[5] = {0, 0, 0, 0, 0}, fm[5] = {0, 0, 0, 0, 0};
+        if (gi <= B.hi[0] + (D == 0 ? 3 : 0) && gj <= B.hi[1] + (D == 1 ? 3 : 0) &&
+            gk <= B.hi[2] + (D == 2 ? 3 : 0)) {
+            FT q[7];
+            Prec<FT>::prims(P, B.S, gi, gj, gk, q);
+            Prec<FT>::template split<D>(P, q, fp, fm);
+        }
+#pragma unroll
+        for (int n = 0; n < 5; ++n) {
+            F[n * PC::N + c] = fp[n];
+            F[(5 + n) * PC::N + c] = fm[n];
+        }
+    }
+    __syncthreads();
+    // ---- 2. WENO-Z face fluxes
+    for (int it = tid; it < 5 * PC::NF; it += NT) {
+        const int n = it / PC::NF, f = it - n * PC::NF;
+        const int fx = f % PC::FX, fy = (f / PC::FX) % PC::FY, fz = f / (PC::FX * PC::FY);
+        const int base = fx + fy * PC::PX + fz * PC::PX * PC::PY;
+        FF[n * PC::NF + f] = Prec<FT>::weno(F + n * PC::N + base, F + (5 + n) * PC::N + base, PC::PST);
+    }
+    __syncthreads();
+    // ---- 3. viscous part of the face flux
+    if (VISC) {
+        for (int f = tid; f < PC::NF; f += NT) {
+            const int fx = f % PC::FX, fy = (f / PC::FX) % PC::FY, fz = f / (PC::FX * PC::FY);
+            // ring coordinates of the cell on the high side of the face
+            visc_face<FT, D, TX, TY, TZ>(P, ring, fx + 1, fy + 1, fz + 1, B.dxinv, FF + f, PC::NF);
+        }
+        __syncthreads();
+    }
+    // ---- 4. divergence contribution and optional face-flux output
+    {
+        const int ti = tid % TX, tj = (tid / TX) % TY, tk = tid / (TX * TY);
+        const int f = ti + tj * PC::FX + tk * PC::FX * PC::FY;
+        const FT dxi = (FT)B.dxinv[D];
+#pragma unroll
+        for (int n = 0; n < 5; ++n) {
+            FT v = dxi * (FF[n * PC::NF + f] - FF[n * PC::NF + f + PC::FST]);
+            acc[n] = (D == 0) ? v : acc[n] + v;
+        }
+    }
+    if (B.has_flux) {
+        const View<double>& out = B.flux[D];
+        for (int f = tid; f < PC::NF; f += NT) {
+            const int fx = f % PC::FX, fy = (f / PC::FX) % PC::FY, fz = f / (PC::FX * PC::FY);
+            const int fc[3] = {fx, fy, fz};
+            const int gi = i0 + fx, gj = j0 + fy, gk = k0 + fz;
+            const int g[3] = {gi, gj, gk};
+            bool ok = true;
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                const int lim = B.hi[t] + (t == D ? 1 : 0);
+                const int tdim = t == 0 ? TX : (t == 1 ? TY : TZ);
+                ok = ok && g[t] <= lim;
+                // the tile owns faces 0..T_D-1, plus face T_D at the box's high end
+                if (t == D) ok = ok && (fc[t] < tdim || g[t] == B.hi[t] + 1);
+            }
+            if (ok) {
+#pragma unroll
+                for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) = (double)FF[n * PC::NF + f];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <class FT, int TX, int TY, int TZ, bool VISC>
+__global__ void __launch_bounds__(TX* TY* TZ)
+    k_rhs_regular(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
+                  int nbox, RegBoxArgs single, DevParm P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FT* smem = reinterpret_cast<FT*>(smem_raw);
+    constexpr int NT = TX * TY * TZ;
+    // locate the box of this CTA: a single box, or a prefix table over a box list
+    int b = 0;
+    int t = blockIdx.x;
+    if (boxes) {
+        int lo = 0, hi = nbox - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (tile_start[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        b = lo;
+        t -= tile_start[b];
+    }
+    const RegBoxArgs& B = boxes ? boxes[b] : single;
+    const int ntx = B.ntile[0], nty = B.ntile[1];
+    const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
+    const int i0 = B.lo[0] + tx * TX, j0 = B.lo[1] + ty * TY, k0 = B.lo[2] + tz * TZ;
+
+    constexpr int PMAX = pencil_elems<TX, TY, TZ>();
+    FT* F = smem;
+    FT* ring = smem + PMAX;
+    if (VISC) {
+        using R = Ring<TX, TY, TZ>;
+        for (int c = threadIdx.x; c < R::N; c += NT) {
+            const int rx = c % R::RX, ry = (c / R::RX) % R::RY, rz = c / (R::RX * R::RY);
+            const int gi = i0 + rx - 1, gj = j0 + ry - 1, gk = k0 + rz - 1;
+            FT q[7] = {0, 0, 0, 0, 0, 1, 0};
+            if (gi <= B.hi[0] + 1 && gj <= B.hi[1] + 1 && gk <= B.hi[2] + 1) Prec<FT>::prims(P, B.S, gi, gj, gk, q);
+            ring[c] = q[QU];
+            ring[R::N + c] = q[QV];
+            ring[2 * R::N + c] = q[QW];
+            ring[3 * R::N + c] = q[QT];
+        }
+        __syncthreads();
+    }
+    FT acc[5];
+    sweep<FT, 0, TX, TY, TZ, VISC>(B, P, i0, j0, k0, F, F + 10 * Pencil<0, TX, TY, TZ>::N, ring, acc);
+    sweep<FT, 1, TX, TY, TZ, VISC>(B, P, i0, j0, k0, F, F + 10 * Pencil<1, TX, TY, TZ>::N, ring, acc);
+    sweep<FT, 2, TX, TY, TZ, VISC>(B, P, i0, j0, k0, F, F + 10 * Pencil<2, TX, TY, TZ>::N, ring, acc);
+
+    const int ti = threadIdx.x % TX, tj = (threadIdx.x / TX) % TY, tk = threadIdx.x / (TX * TY);
+    const int ci = i0 + ti, cj = j0 + tj, ck = k0 + tk;
+    const bool valid = ci <= B.hi[0] && cj <= B.hi[1] && ck <= B.hi[2];
+    double local_dt = __longlong_as_double(0x7FF0000000000000LL);
+    if (valid) {
+        if (B.mode == RHS_WRITE_DSDT) {
+#pragma unroll
+            for (int n = 0; n < 5; ++n) B.dsdt(ci, cj, ck, n) = (double)acc[n];
+        } else {
+            // fused Shu-Osher stage in FP64: U_out = a U0 + b (U_s + dt L(U_s))
+            const double dt = B.dt_ptr ? *B.dt_ptr : B.dt;
+            double un[5];
+#pragma unroll
+            for (int n = 0; n < 5; ++n) {
+                double us = B.S(ci, cj, ck, n);
+                double u0 = B.U0(ci, cj, ck, n);
+                un[n] = B.rk_a * u0 + B.rk_b * (us + dt * (double)acc[n]);
+                B.Uout(ci, cj, ck, n) = un[n];
+            }
+            if (B.cfl_min) local_dt = cfl_bound(P, un, B.dx);
+        }
+    }
+    if (B.cfl_min) block_min_atomic(local_dt, B.cfl_min);
+}
+
+template <class FT, int TX, int TY, int TZ, bool VISC>
+static ocfd_status launch_t(const RegBoxArgs* d_boxes, const int* d_tile_start, int nbox,
+                            const RegBoxArgs& single, int ntiles, const DevParm& P,
+                            cudaStream_t st) {
+    constexpr int NT = TX * TY * TZ;
+    constexpr size_t smem = regular_smem_bytes<FT, TX, TY, TZ, VISC>();
+    auto kern = k_rhs_regular<FT, TX, TY, TZ, VISC>;
+    if (smem > kMaxSmem) return fail(OCFD_BAD_ARG, "regular RHS tile does not fit shared memory in this mode");
+    if (ntiles <= 0) return OCFD_OK;
+    kern<<<ntiles, NT, smem, st>>>(d_boxes, d_tile_start, nbox, single, P);
+    return check_launch("k_rhs_regular");
+}
+
+template <class FT, int TX, int TY, int TZ, bool VISC>
+static bool configure_one() {
+    const size_t smem = regular_smem_bytes<FT, TX, TY, TZ, VISC>();
+    if (smem > kMaxSmem) return true;  // shape not offered in this mode
+    return cudaFuncSetAttribute(k_rhs_regular<FT, TX, TY, TZ, VISC>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+}
+
+// Every compiled tile shape (index = position in kRegularTiles)
+#define OCFD_REGULAR_TILES(X) X(0, 8, 8, 8) X(1, 8, 8, 4) X(2, 16, 8, 4) X(3, 16, 16, 2) X(4, 32, 8, 2) X(5, 16, 8, 2)
+
+template <class FT>
+static ocfd_status configure_all() {
+    bool ok = true;
+#define OCFD_CONF(I, X, Y, Z) ok = ok && configure_one<FT, X, Y, Z, false>() && configure_one<FT, X, Y, Z, true>();
+    OCFD_REGULAR_TILES(OCFD_CONF)
+#undef OCFD_CONF
+    if (!ok) return check_launch("configure regular RHS kernels");
+    return OCFD_OK;
+}
+
+template <class FT>
+static bool tile_fits(int tile, bool visc) {
+    size_t b = 0;
+    switch (tile) {
+#define OCFD_FIT(I, X, Y, Z)                                                                                \
+    case I:                                                                                                 \
+        b = visc ? regular_smem_bytes<FT, X, Y, Z, true>() : regular_smem_bytes<FT, X, Y, Z, false>(); \
+        break;
+        OCFD_REGULAR_TILES(OCFD_FIT)
+#undef OCFD_FIT
+        default:
+            return false;
+    }
+    return b <= kMaxSmem;
+}
+
+template <class FT>
+static ocfd_status launch_any(int tile, bool visc, const RegBoxArgs* d_boxes, const int* d_tile_start,
+                              int nbox, const RegBoxArgs& single, int ntiles, const DevParm& P,
+                              cudaStream_t st) {
+    switch (tile) {
+#define OCFD_CASE(I, X, Y, Z)                                                                           \
+    case I:                                                                                             \
+        return visc ? launch_t<FT, X, Y, Z, true>(d_boxes, d_tile_start, nbox, single, ntiles, P, st) \
+                    : launch_t<FT, X, Y, Z, false>(d_boxes, d_tile_start, nbox, single, ntiles, P, st);
+        OCFD_REGULAR_TILES(OCFD_CASE)
+#undef OCFD_CASE
+    }
+    return fail(OCFD_BAD_ARG, "regular RHS: bad tile index");
+}
+
+}  // namespace ocfd

@@ -33,6 +33,7 @@ declare("ocfd_level_time", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double), _vp])
 declare("ocfd_level_set_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
 declare("ocfd_level_cells", ctypes.c_int64, [_vp])
+declare("ocfd_level_set_stop_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
 declare("ocfd_level_launches_per_step", ctypes.c_int, [_vp, ctypes.c_uint])
 declare("ocfd_level_profile_stage", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int,
                                                    ctypes.POINTER(ctypes.c_double), _vp])
@@ -168,6 +169,9 @@ class Level:
 
     def set_time(self, t, stream=None):
         check(self.lib.ocfd_level_set_time(self.h, t, _stream_ptr(stream)), "set_time")
+
+    def set_stop_time(self, t, stream=None):
+        check(self.lib.ocfd_level_set_stop_time(self.h, t, _stream_ptr(stream)), "set_stop_time")
 
     def cells(self):
         return int(self.lib.ocfd_level_cells(self.h))
