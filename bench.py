@@ -6,7 +6,10 @@
 A step is one SSP-RK3 time step of every box of the workload (3 ghost fills +
 3 fused RHS/update stages + the CFL reduction), i.e. one CUDA-graph launch.
 value  = cells x steps / device time of the K timed steps (state resident in
-         HBM; L2 flushed between steps, untimed)
+         HBM; L2 flushed between steps, untimed), for the headline form (default
+         the mixed-precision form, FP32 flux / FP64 state); the plain FP64 form is
+         timed the same way and reported in config, with the L1 error in density
+         and pressure between the two forms at the same time
 e2e    = the same through the C ABI from pinned host buffers: every step uploads
          the state, advances, downloads the state
 --impl reference times the reference algorithm on the host CPU cores (the
@@ -211,23 +214,31 @@ def run_ours(args, world, rank, local):
     lev.copy_in(flat)
     l2flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    lev.advance(args.warmup, CFL, flags)
-    torch.cuda.synchronize()
-    barrier(world)
-    torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
+    def timed(fl):
+        """K steps of form `fl`, each step timed with CUDA events, L2 flushed between
+        steps outside the events; returns the summed device time in ms."""
+        lev.copy_in(flat)
+        lev.advance(args.warmup, CFL, fl)
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
         for e0, e1 in ev:
             l2flush.fill_(1.0)            # untimed: evicts the state from L2
             e0.record(stream)
-            lev.advance(1, CFL, flags)
+            lev.advance(1, CFL, fl)
             e1.record(stream)
         torch.cuda.synchronize()
-    barrier(world)
-    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
-    ms_max = allreduce_max(ms, world)
+        barrier(world)
+        return allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
+
+    other = 0 if flags else ocfd.FLUX_FP32
+    ms_other = timed(other)
+    with ClockSampler(local) as clk:
+        ms_max = timed(flags)
     value = cells * args.steps * world / (ms_max * 1e-3)
+    value_other = cells * args.steps * world / (ms_other * 1e-3)
 
     # dominant kernel, timed live: the fused RK-stage kernel (stage 2)
     stage_ms = lev.profile_stage(flags, reps=10)
@@ -275,6 +286,8 @@ def run_ours(args, world, rank, local):
             "dtype": "f64" if args.form == "fp64" else "f32-flux/f64-state", "data": "synthetic",
             "config": {"workload": c["name"], "form": args.form, "cells": cells, "boxes": len(boxes),
                        "l1_vs_other_form": l1err,
+                       "forms_cell_steps_per_s": {args.form: value, ("fp64" if flags else "fp32"): value_other},
+                       "speedup_fp32_over_fp64": (value / value_other) if flags else (value_other / value),
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -328,7 +341,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="sod", choices=["sod", "dmr", "cube"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
+                    help="headline form (the other form is timed too and reported in config)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -4,8 +4,9 @@
 //   FT = float   the mixed-precision form: primitives, Steger-Warming split,
 //                WENO-Z (stencils normalised by a power of two, the smoothness
 //                epsilon rescaled into the normalised units), viscous flux and
-//                divergence in FP32; the RK accumulation and the CFL bound stay
-//                FP64.
+//                divergence in FP32, state narrowed / divergence widened on the
+//                integer pipes; the RK accumulation stays FP64 (the CFL bound
+//                of the new state is evaluated in FP32).
 // Included by rhs_regular.cu (double) and rhs_regular_f32.cu (float).
 //
 // One CTA owns a TX x TY x TZ tile.  Per direction D:
@@ -124,16 +125,51 @@ __device__ __forceinline__ float wenoz_norm_f(float V1, float V2, float V3, floa
     return wenoz_side_f(V1 * sc, V2 * sc, V3 * sc, V4 * sc, V5 * sc, eps) * inv;
 }
 
+// Conversions between FP64 and FP32 on the integer pipes.  GB300 runs FP64
+// (and its conversions) at 2 instructions / cycle / SM, so in the mixed form the
+// state is narrowed and the FP32 divergence widened with bit operations:
+// double -> float truncates the mantissa (error < 1 ulp of float; values below
+// 2^-126 flush to zero), float -> double is exact.
+__device__ __forceinline__ float d2f_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int ed = (int)((hi >> 20) & 0x7ffu);
+    const int e = ed - 896;  // rebias 1023 -> 127
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned f;
+    if (e <= 0) f = sign;
+    else if (ed == 0x7ff) f = sign | 0x7f800000u | ((((hi & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u);
+    else if (e >= 255) f = sign | 0x7f800000u;
+    else f = sign | ((unsigned)e << 23) | m;
+    return __uint_as_float(f);
+}
+
+__device__ __forceinline__ double f2d_bits(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned hi, lo = 0u;
+    if (e == 0u) hi = sign;
+    else if (e == 0xffu) hi = sign | 0x7ff00000u | (m ? 0x80000u : 0u);
+    else {
+        hi = sign | ((e + 896u) << 20) | (m >> 3);
+        lo = m << 29;
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 template <>
 struct Prec<float> {
+    // c2prim in FP32 from the narrowed conserved state
     static __device__ __forceinline__ void prims(const DevParm& P, const View<const double>& S, int i,
                                                  int j, int k, float* q) {
         const float g = (float)P.gamma;
-        const float rho = fmaxf((float)S(i, j, k, 0), (float)P.smallr);
+        const float u0 = d2f_bits(S(i, j, k, 0)), u1 = d2f_bits(S(i, j, k, 1)), u2 = d2f_bits(S(i, j, k, 2)),
+                    u3 = d2f_bits(S(i, j, k, 3)), u4 = d2f_bits(S(i, j, k, 4));
+        const float rho = fmaxf(u0, (float)P.smallr);
         const float rhoinv = __frcp_rn(rho);
-        const float ux = (float)S(i, j, k, 1) * rhoinv, uy = (float)S(i, j, k, 2) * rhoinv,
-                    uz = (float)S(i, j, k, 3) * rhoinv;
-        const float ei = (float)(S(i, j, k, 4) - 0.5 * S(i, j, k, 0) * ((double)ux * ux + (double)uy * uy + (double)uz * uz));
+        const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
+        const float ei = u4 - rho * (0.5f * (ux * ux + uy * uy + uz * uz));
         const float p = fmaxf((g - 1.0f) * ei, (float)P.smallp);
         q[QRHO] = rho;
         q[QU] = ux;
@@ -159,6 +195,31 @@ struct Prec<float> {
 
 // Viscous stress and heat flux of the D-face between ring cells (r - e_D) and r,
 // Source/kernel/Diffusion.H:7-131.  ring holds u, v, w, T (4 planes of RN).
+// CFL bound of the new state (Source/Advance.cpp:26-49): FP64 in the plain form,
+// FP32 (from the narrowed state) in the mixed form
+template <class FT>
+__device__ __forceinline__ double stage_cfl_bound(const DevParm& P, const double* un, const double* dx) {
+    return cfl_bound(P, un, dx);
+}
+template <>
+__device__ __forceinline__ double stage_cfl_bound<float>(const DevParm& P, const double* un, const double* dx) {
+    const float g = (float)P.gamma;
+    const float rho = d2f_bits(un[0]);
+    const float rhoinv = __frcp_rn(fmaxf(rho, (float)P.smallr));
+    const float vx = d2f_bits(un[1]) * rhoinv, vy = d2f_bits(un[2]) * rhoinv, vz = d2f_bits(un[3]) * rhoinv;
+    const float p = fmaxf((g - 1.0f) * (d2f_bits(un[4]) - 0.5f * rho * (vx * vx + vy * vy + vz * vz)), (float)P.smallp);
+    const float cs = sqrtf(g * p * rhoinv);
+    const float dtx = __fdividef((float)dx[0], fabsf(vx) + cs);
+    const float dty = __fdividef((float)dx[1], fabsf(vy) + cs);
+    const float dtz = __fdividef((float)dx[2], fabsf(vz) + cs);
+    return f2d_bits(fminf(dtx, fminf(dty, dtz)));
+}
+
+template <class FT>
+__device__ __forceinline__ double widen(FT x) { return (double)x; }
+template <>
+__device__ __forceinline__ double widen<float>(float x) { return f2d_bits(x); }
+
 template <class FT, int D, int TX, int TY, int TZ>
 __device__ __forceinline__ void visc_face(const DevParm& P, const FT* ring, int rx, int ry, int rz,
                                           const double* dxinv_d, FT* f /*stride fs*/, int fs) {
@@ -271,7 +332,7 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
             }
             if (ok) {
 #pragma unroll
-                for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) = (double)FF[n * PC::NF + f];
+                for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) = widen<FT>(FF[n * PC::NF + f]);
             }
         }
     }
@@ -331,7 +392,7 @@ __global__ void __launch_bounds__(TX* TY* TZ)
     if (valid) {
         if (B.mode == RHS_WRITE_DSDT) {
 #pragma unroll
-            for (int n = 0; n < 5; ++n) B.dsdt(ci, cj, ck, n) = (double)acc[n];
+            for (int n = 0; n < 5; ++n) B.dsdt(ci, cj, ck, n) = widen<FT>(acc[n]);
         } else {
             // fused Shu-Osher stage in FP64: U_out = a U0 + b (U_s + dt L(U_s))
             const double dt = B.dt_ptr ? *B.dt_ptr : B.dt;
@@ -340,10 +401,10 @@ __global__ void __launch_bounds__(TX* TY* TZ)
             for (int n = 0; n < 5; ++n) {
                 double us = B.S(ci, cj, ck, n);
                 double u0 = B.U0(ci, cj, ck, n);
-                un[n] = B.rk_a * u0 + B.rk_b * (us + dt * (double)acc[n]);
+                un[n] = B.rk_a * u0 + B.rk_b * (us + dt * widen<FT>(acc[n]));
                 B.Uout(ci, cj, ck, n) = un[n];
             }
-            if (B.cfl_min) local_dt = cfl_bound(P, un, B.dx);
+            if (B.cfl_min) local_dt = stage_cfl_bound<FT>(P, un, B.dx);
         }
     }
     if (B.cfl_min) block_min_atomic(local_dt, B.cfl_min);
