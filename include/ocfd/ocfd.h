@@ -297,6 +297,79 @@ int ocfd_level_launches_per_step(const ocfd_level* level, unsigned flags);
 ocfd_status ocfd_level_profile_stage(ocfd_level* level, unsigned flags, int reps, double* ms,
                                      void* stream);
 
+/* ---------------------------------------------------- AMR hierarchy (GPU)
+ * The per-level path of EBR::advance / EBR::post_timestep run over a whole
+ * refined hierarchy with subcycling in time (AMReX Amr::timeStep, ratio 2):
+ *   - coarse-fine ghost cells of a finer level are interpolated from the coarser
+ *     level with MC-limited conservative linear slopes, in time from the coarse
+ *     SSP-RK3 stage states (the role of FillPatch / FillPatcher::fillRK under
+ *     AmrLevel::RK, Source/Advance.cpp:141-148; Source/Setup.cpp:194-196),
+ *   - flux registers collect the RK3-weighted face fluxes on both sides of each
+ *     coarse-fine face and reflux the uncovered coarse cells
+ *     (EBFluxRegister CrseAdd / FineAdd / Reflux, Source/Advance.cpp:344-360,
+ *     Source/EBR.cpp:322-330),
+ *   - covered coarse cells are replaced by the average of their fine cells
+ *     (EB_average_down with unit volume fractions, Source/EBR.cpp:535-559),
+ *   - the time step is the CFL bound over all levels (EBR::estTimeStep per
+ *     level, dt_0 = min over levels of dt_l * 2^l, Source/EBR.cpp:240-305),
+ *   - regridding tags cells with |d rho| >= refine_dengrad
+ *     (Source/Tagging.H:11-36), buffers them by n_error_buf, clusters the
+ *     tagged blocking_factor blocks into boxes no larger than max_grid_size and
+ *     keeps every level properly nested in the one below.
+ * Regular (non-EB) ideal-gas boxes; one CUDA graph launch per coarse step.     */
+#define OCFD_AMR_MAX_LEVELS 6
+
+typedef struct ocfd_amr ocfd_amr;
+
+typedef struct ocfd_amr_desc {
+    int32_t nbox0;               /* level-0 boxes (disjoint, covering the domain) */
+    const ocfd_box* boxes0;
+    ocfd_box domain;             /* level-0 domain */
+    int32_t lo_bc[3], hi_bc[3];  /* ebr.lo_bc / ebr.hi_bc */
+    double dx[3];                /* level-0 cell size */
+    double prob_lo[3];
+    int32_t bc_case;             /* OCFD_CASE_* */
+    double case_params[16];
+    int32_t max_level;           /* amr.max_level: finest level index allowed */
+    int32_t blocking_factor[3];  /* amr.blocking_factor, in cells of the level built */
+    int32_t max_grid_size[3];    /* amr.max_grid_size */
+    int32_t n_error_buf;         /* amr.n_error_buf */
+    int32_t regrid_int;          /* amr.regrid_int (coarse steps), 0 = never inside ocfd_amr_advance */
+    double refine_dengrad;       /* ebr.refine_dengrad */
+} ocfd_amr_desc;
+
+ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_amr** amr);
+ocfd_status ocfd_amr_destroy(ocfd_amr* amr);
+int ocfd_amr_nlevels(const ocfd_amr* amr);
+/* The level object of level `lev` (state access through ocfd_level_state /
+ * copy_in / copy_out); owned by the hierarchy, valid until the next regrid. */
+ocfd_level* ocfd_amr_level(ocfd_amr* amr, int lev);
+/* Boxes of level `lev`: writes min(cap, n) boxes and returns n (-1 on error). */
+int ocfd_amr_get_grids(const ocfd_amr* amr, int lev, ocfd_box* out, int cap);
+/* Tag levels lbase.. and rebuild the grids of levels lbase+1..max_level (data of
+ * new cells interpolated from the level below, of old cells copied). Called with
+ * lbase = finest level it adds one level (hierarchy construction at t = 0). */
+ocfd_status ocfd_amr_regrid(ocfd_amr* amr, int lbase, void* stream);
+/* Replace levels 1..nlev-1 by the given boxes (a recorded regrid replayed);
+ * nbox[l] boxes of level l follow each other in `boxes`, level 1 first. */
+ocfd_status ocfd_amr_set_grids(ocfd_amr* amr, int nlev, const int32_t* nbox, const ocfd_box* boxes,
+                               void* stream);
+/* Covered coarse cells := average of their fine cells, finest level first. */
+ocfd_status ocfd_amr_average_down(ocfd_amr* amr, void* stream);
+/* Ghost cells of every level at the current time (exchange, coarse-fine
+ * interpolation, physical BCs). */
+ocfd_status ocfd_amr_fill_ghosts(ocfd_amr* amr, void* stream);
+/* nsteps coarse steps (regridding every regrid_int steps). */
+ocfd_status ocfd_amr_advance(ocfd_amr* amr, int nsteps, double cfl, unsigned flags, void* stream);
+ocfd_status ocfd_amr_time(ocfd_amr* amr, double* time, double* last_dt0, void* stream);
+ocfd_status ocfd_amr_set_time(ocfd_amr* amr, double time, void* stream);
+ocfd_status ocfd_amr_set_stop_time(ocfd_amr* amr, double stop_time, void* stream);
+/* Cell-steps of one coarse step: leaf = cells not covered by a finer level,
+ * all = every cell advanced; each weighted by the level's 2^lev substeps. */
+ocfd_status ocfd_amr_cell_steps(const ocfd_amr* amr, int64_t* leaf, int64_t* all);
+/* Kernel and copy nodes of one coarse step (the captured graph). */
+int ocfd_amr_launches_per_step(const ocfd_amr* amr);
+
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops
  * per FMA), from register-only FMA chains over all SMs. */

@@ -1,0 +1,1532 @@
+// AMR hierarchy on the GPU: subcycled SSP-RK3 over levels of ratio 2 with
+// coarse-fine ghost interpolation (space and time), flux registers + reflux,
+// average-down, CFL over all levels, density-gradient regridding.
+//
+// One coarse step (AMReX Amr::timeStep recursion, EBR::advance,
+// EBR::post_timestep; Source/EBR.cpp:312-360) is captured as one CUDA graph:
+//
+//   k_amr_begin: dt_0 = cfl * min_l(est_l * 2^l) (1.1 dt_prev, stop time),
+//                dt_l = dt_0 / 2^l
+//   advance(0, 1)
+//   estdt of every level (for the next step), k_amr_end: t += dt_0
+//
+//   advance(l, it):                        (it = 1..2 for l >= 1)
+//     zero the coarse side of level l's flux register and the fine side of l+1's
+//     stage s = 1..3:  ghosts of the stage input:
+//                        coarse-fine cells interpolated from level l-1's RK3 stage
+//                        states at the matching time (below), exchange, physical BCs
+//                      fused RHS + Shu-Osher stage; RK3-weighted face fluxes
+//                      accumulated into the flux registers
+//     if level l+1 exists:
+//        stage 3 writes buffer D (U^n stays in A), D's ghosts filled at t + dt_l
+//        advance(l+1, 1); advance(l+1, 2)
+//        reflux of the uncovered cells next to level l+1, average-down of the
+//        covered cells, D -> A
+//
+// Time interpolation of coarse-fine ghosts.  From the coarse stage states
+// u0 = A, U1 = B, U2 = C, U3 = D the scaled stage derivatives are
+//   K1 = U1 - u0,  K2 = 4 U2 - 3 u0 - U1,  K3 = (3 U3 - u0 - 2 U2) / 2
+// and the SSP-RK3 dense output at theta in [0, 1] of the coarse step is
+//   P(theta) = u0 + (theta - 5/6 theta^2) K1 + theta^2/6 K2 + 2/3 theta^2 K3.
+// A fine substep from theta to theta + r (r = 1/2) fills its three stages with
+// the Taylor expansion of the fine stage states (u, u + h u', u + h/2 u' +
+// h^2/4 u'' for SSP-RK3) evaluated on P, following McCorquodale & Colella,
+// "A high-order finite-volume method for conservation laws on locally refined
+// grids", CAMCoS 6 (2011), sec. 3.  Every value is a fixed linear combination
+// a_A A + a_B B + a_C C + a_D D with sum(a) = 1, so the interpolation kernel
+// mixes the four buffers and then applies MC-limited conservative linear
+// slopes (van Leer) in space.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "level.h"
+
+namespace ocfd {
+
+// ================================================================ box algebra
+struct IBox {
+    int lo[3], hi[3];
+};
+
+static bool ib_empty(const IBox& b) {
+    return b.lo[0] > b.hi[0] || b.lo[1] > b.hi[1] || b.lo[2] > b.hi[2];
+}
+static IBox ib_of(const ocfd_box& b) {
+    IBox r;
+    for (int d = 0; d < 3; ++d) { r.lo[d] = b.lo[d]; r.hi[d] = b.hi[d]; }
+    return r;
+}
+static ocfd_box ob_of(const IBox& b) {
+    ocfd_box r;
+    for (int d = 0; d < 3; ++d) { r.lo[d] = b.lo[d]; r.hi[d] = b.hi[d]; }
+    return r;
+}
+static bool ib_isect(const IBox& a, const IBox& b, IBox& o) {
+    for (int d = 0; d < 3; ++d) {
+        o.lo[d] = std::max(a.lo[d], b.lo[d]);
+        o.hi[d] = std::min(a.hi[d], b.hi[d]);
+        if (o.lo[d] > o.hi[d]) return false;
+    }
+    return true;
+}
+static IBox ib_grow(const IBox& b, int g) {
+    IBox r = b;
+    for (int d = 0; d < 3; ++d) { r.lo[d] -= g; r.hi[d] += g; }
+    return r;
+}
+static int floordiv2(int x) { return x >= 0 ? x / 2 : -((1 - x) / 2); }
+static IBox ib_coarsen(const IBox& b) {
+    IBox r;
+    for (int d = 0; d < 3; ++d) { r.lo[d] = floordiv2(b.lo[d]); r.hi[d] = floordiv2(b.hi[d]); }
+    return r;
+}
+static IBox ib_refine(const IBox& b) {
+    IBox r;
+    for (int d = 0; d < 3; ++d) { r.lo[d] = 2 * b.lo[d]; r.hi[d] = 2 * b.hi[d] + 1; }
+    return r;
+}
+static IBox ib_shift(const IBox& b, const int* s) {
+    IBox r;
+    for (int d = 0; d < 3; ++d) { r.lo[d] = b.lo[d] + s[d]; r.hi[d] = b.hi[d] + s[d]; }
+    return r;
+}
+static long long ib_cells(const IBox& b) {
+    return ib_empty(b) ? 0 : (long long)(b.hi[0] - b.lo[0] + 1) * (b.hi[1] - b.lo[1] + 1) * (b.hi[2] - b.lo[2] + 1);
+}
+static bool ib_same(const IBox& a, const IBox& b) {
+    for (int d = 0; d < 3; ++d)
+        if (a.lo[d] != b.lo[d] || a.hi[d] != b.hi[d]) return false;
+    return true;
+}
+// a minus b as up to 6 disjoint boxes
+static void ib_subtract(const IBox& a, const IBox& b, std::vector<IBox>& out) {
+    IBox i;
+    if (!ib_isect(a, b, i)) {
+        out.push_back(a);
+        return;
+    }
+    IBox r = a;
+    for (int d = 0; d < 3; ++d) {
+        if (r.lo[d] < i.lo[d]) {
+            IBox p = r;
+            p.hi[d] = i.lo[d] - 1;
+            out.push_back(p);
+            r.lo[d] = i.lo[d];
+        }
+        if (r.hi[d] > i.hi[d]) {
+            IBox p = r;
+            p.lo[d] = i.hi[d] + 1;
+            out.push_back(p);
+            r.hi[d] = i.hi[d];
+        }
+    }
+}
+static void list_subtract(std::vector<IBox>& list, const IBox& b) {
+    std::vector<IBox> out;
+    for (const IBox& a : list) ib_subtract(a, b, out);
+    list.swap(out);
+}
+
+// Bucketed lookup of the boxes of one level (buckets of 16^3 cells over the domain).
+struct BoxIndex {
+    static constexpr int BS = 16;
+    std::vector<IBox> boxes;
+    IBox dom{};
+    int nb[3] = {0, 0, 0};
+    std::vector<std::vector<int>> bucket;
+    void build(const std::vector<IBox>& bx, const IBox& d) {
+        boxes = bx;
+        dom = d;
+        for (int e = 0; e < 3; ++e) nb[e] = (d.hi[e] - d.lo[e] + BS) / BS;
+        bucket.assign((size_t)nb[0] * nb[1] * nb[2], {});
+        for (int b = 0; b < (int)bx.size(); ++b) {
+            IBox c;
+            if (!ib_isect(bx[b], dom, c)) continue;
+            int lo[3], hi[3];
+            for (int e = 0; e < 3; ++e) {
+                lo[e] = (c.lo[e] - dom.lo[e]) / BS;
+                hi[e] = (c.hi[e] - dom.lo[e]) / BS;
+            }
+            for (int k = lo[2]; k <= hi[2]; ++k)
+                for (int j = lo[1]; j <= hi[1]; ++j)
+                    for (int i = lo[0]; i <= hi[0]; ++i) bucket[(size_t)i + nb[0] * ((size_t)j + (size_t)nb[1] * k)].push_back(b);
+        }
+    }
+    int find(const int* c) const {
+        for (int e = 0; e < 3; ++e)
+            if (c[e] < dom.lo[e] || c[e] > dom.hi[e]) return -1;
+        const size_t q = (size_t)((c[0] - dom.lo[0]) / BS) +
+                         nb[0] * ((size_t)((c[1] - dom.lo[1]) / BS) + (size_t)nb[1] * ((c[2] - dom.lo[2]) / BS));
+        for (int b : bucket[q]) {
+            const IBox& B = boxes[b];
+            if (c[0] >= B.lo[0] && c[0] <= B.hi[0] && c[1] >= B.lo[1] && c[1] <= B.hi[1] && c[2] >= B.lo[2] &&
+                c[2] <= B.hi[2])
+                return b;
+        }
+        return -1;
+    }
+    // boxes intersecting r (r clipped to the domain), ascending
+    std::vector<int> query(const IBox& r) const {
+        std::vector<int> out;
+        IBox c;
+        if (!ib_isect(r, dom, c)) return out;
+        int lo[3], hi[3];
+        for (int e = 0; e < 3; ++e) {
+            lo[e] = (c.lo[e] - dom.lo[e]) / BS;
+            hi[e] = (c.hi[e] - dom.lo[e]) / BS;
+        }
+        for (int k = lo[2]; k <= hi[2]; ++k)
+            for (int j = lo[1]; j <= hi[1]; ++j)
+                for (int i = lo[0]; i <= hi[0]; ++i)
+                    for (int b : bucket[(size_t)i + nb[0] * ((size_t)j + (size_t)nb[1] * k)]) {
+                        IBox t;
+                        if (ib_isect(boxes[b], c, t)) out.push_back(b);
+                    }
+        std::sort(out.begin(), out.end());
+        out.erase(std::unique(out.begin(), out.end()), out.end());
+        return out;
+    }
+};
+
+// ================================================================ device tags
+struct CfTag {  // fine cells (fine box index space) interpolated from one coarse box
+    int fbox, cbox;
+    int lo[3], hi[3];
+    int shift[3];  // fine cell + shift = its image inside the domain (periodic)
+};
+struct AvgTag {  // coarse cells averaged from one fine box
+    int cbox, fbox;
+    int lo[3], hi[3];
+};
+struct CopyTag {  // regrid: new box dst <- old box src
+    int dst, src;
+    int lo[3], hi[3];
+};
+struct RefluxCell {
+    long long u, uns;  // element of component 0 in the coarse state buffer, component stride
+    int first, count;  // faces
+};
+struct RefluxFace {
+    int d;
+    double sgn;      // +1: the coarse cell is on the low side of the face
+    long long c, cns;  // coarse register element (component 0), component stride
+    long long f[4];    // the four fine register elements (component 0)
+    long long fns;
+};
+struct TimeMix {
+    const double* src[4];
+    double a[4];
+};
+struct TagGeom {
+    int dom_lo[3], dom_hi[3];
+    int bs[3], nb[3];  // block size in this level's cells, blocks per direction
+    int nbuf;
+    double thr;
+};
+struct AmrStates {
+    StepState* s[OCFD_AMR_MAX_LEVELS];
+    int n;
+};
+
+__device__ __forceinline__ double mc_slope(double m, double c, double p) {
+    const double dl = c - m, dr = p - c;
+    if (dl * dr <= 0.0) return 0.0;
+    const double dc = 0.5 * (dl + dr);
+    const double a = fmin(fabs(dc), 2.0 * fmin(fabs(dl), fabs(dr)));
+    return dc > 0.0 ? a : -a;
+}
+
+__device__ __forceinline__ double mixed(const TimeMix& m, long long q) {
+    double v = 0.0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+        if (m.a[s] != 0.0) v += m.a[s] * m.src[s][q];
+    return v;
+}
+
+__global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __restrict__ start, int ntag,
+                            long long total, const FabGeom* __restrict__ ffabs, double* dst,
+                            const FabGeom* __restrict__ cfabs, TimeMix mix, int ncomp) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<CfTag>(start, ntag, idx);
+        const CfTag& T = tags[t];
+        int i, j, k;
+        region_cell(T.lo, T.hi, idx - start[t], i, j, k);
+        const int fi = i + T.shift[0], fj = j + T.shift[1], fk = k + T.shift[2];
+        const double ox = (fi & 1) ? 0.25 : -0.25, oy = (fj & 1) ? 0.25 : -0.25, oz = (fk & 1) ? 0.25 : -0.25;
+        const FabGeom& cf = cfabs[T.cbox];
+        const FabGeom& ff = ffabs[T.fbox];
+        const long long c = fab_index(cf, fi >> 1, fj >> 1, fk >> 1);
+        const long long sy = cf.g[0], sz = (long long)cf.g[0] * cf.g[1];
+        const long long o = fab_index(ff, i, j, k);
+        for (int n = 0; n < ncomp; ++n) {
+            const long long q = c + n * cf.ns;
+            const double v0 = mixed(mix, q);
+            const double sx_ = mc_slope(mixed(mix, q - 1), v0, mixed(mix, q + 1));
+            const double sy_ = mc_slope(mixed(mix, q - sy), v0, mixed(mix, q + sy));
+            const double sz_ = mc_slope(mixed(mix, q - sz), v0, mixed(mix, q + sz));
+            dst[o + n * ff.ns] = v0 + ox * sx_ + oy * sy_ + oz * sz_;
+        }
+    }
+}
+
+__global__ void k_avg_down(const AvgTag* __restrict__ tags, const long long* __restrict__ start, int ntag,
+                           long long total, const FabGeom* __restrict__ cfabs, double* cdst,
+                           const FabGeom* __restrict__ ffabs, const double* __restrict__ fsrc, int ncomp) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<AvgTag>(start, ntag, idx);
+        const AvgTag& T = tags[t];
+        int i, j, k;
+        region_cell(T.lo, T.hi, idx - start[t], i, j, k);
+        const FabGeom& cf = cfabs[T.cbox];
+        const FabGeom& ff = ffabs[T.fbox];
+        const long long o = fab_index(cf, i, j, k);
+        const long long f0 = fab_index(ff, 2 * i, 2 * j, 2 * k);
+        const long long sy = ff.g[0], sz = (long long)ff.g[0] * ff.g[1];
+        for (int n = 0; n < ncomp; ++n) {
+            const double* p = fsrc + f0 + n * ff.ns;
+            double s = 0.0;
+            for (int kk = 0; kk < 2; ++kk)
+                for (int jj = 0; jj < 2; ++jj)
+                    for (int ii = 0; ii < 2; ++ii) s += p[ii + jj * sy + kk * sz];
+            cdst[o + n * cf.ns] = 0.125 * s;
+        }
+    }
+}
+
+__global__ void k_reflux(const RefluxCell* __restrict__ cells, int ncell, const RefluxFace* __restrict__ faces,
+                         const double* __restrict__ creg, const double* __restrict__ freg, double* U,
+                         double dxi0, double dxi1, double dxi2) {
+    const double dxinv[3] = {dxi0, dxi1, dxi2};
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        const RefluxCell& C = cells[c];
+        for (int n = 0; n < 5; ++n) {
+            double acc = 0.0;
+            for (int q = C.first; q < C.first + C.count; ++q) {
+                const RefluxFace& F = faces[q];
+                const double fc = creg[F.c + n * F.cns];
+                const double ff = 0.25 * (freg[F.f[0] + n * F.fns] + freg[F.f[1] + n * F.fns] +
+                                          freg[F.f[2] + n * F.fns] + freg[F.f[3] + n * F.fns]);
+                acc += F.sgn * dxinv[F.d] * (fc - ff);
+            }
+            U[C.u + n * C.uns] += acc;
+        }
+    }
+}
+
+__global__ void k_copy_tags(const CopyTag* __restrict__ tags, const long long* __restrict__ start, int ntag,
+                            long long total, const FabGeom* __restrict__ dfabs, double* dst,
+                            const FabGeom* __restrict__ sfabs, const double* __restrict__ src, int ncomp) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<CopyTag>(start, ntag, idx);
+        const CopyTag& T = tags[t];
+        int i, j, k;
+        region_cell(T.lo, T.hi, idx - start[t], i, j, k);
+        const FabGeom& fd = dfabs[T.dst];
+        const FabGeom& fs = sfabs[T.src];
+        const long long d = fab_index(fd, i, j, k), s = fab_index(fs, i, j, k);
+        for (int n = 0; n < ncomp; ++n) dst[d + n * fd.ns] = src[s + n * fs.ns];
+    }
+}
+
+// tag_dengrad, Source/Tagging.H:11-36, marking the blocks of the next level that
+// hold a tagged cell or one within n_error_buf cells of it
+__global__ void k_tag_dengrad(const FabGeom* __restrict__ lfabs, const long long* __restrict__ cstart, int nbox,
+                              long long total, const double* __restrict__ U, TagGeom g, unsigned char* blk) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = find_tag<FabGeom>(cstart, nbox, idx);
+        const FabGeom& f = lfabs[b];
+        int c3[3];
+        region_cell(f.lo, f.hi, idx - cstart[b], c3[0], c3[1], c3[2]);
+        const long long c = fab_index(f, c3[0], c3[1], c3[2]);
+        const long long sy = f.g[0], sz = (long long)f.g[0] * f.g[1];
+        const double r = U[c];
+        double ax = fabs(U[c + 1] - r), ay = fabs(U[c + sy] - r), az = fabs(U[c + sz] - r);
+        ax = fmax(ax, fabs(r - U[c - 1]));
+        ay = fmax(ay, fabs(r - U[c - sy]));
+        az = fmax(az, fabs(r - U[c - sz]));
+        if (fmax(ax, fmax(ay, az)) >= g.thr) {
+            int lo[3], hi[3];
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = (max(c3[d] - g.nbuf, g.dom_lo[d]) - g.dom_lo[d]) / g.bs[d];
+                hi[d] = (min(c3[d] + g.nbuf, g.dom_hi[d]) - g.dom_lo[d]) / g.bs[d];
+            }
+            for (int kb = lo[2]; kb <= hi[2]; ++kb)
+                for (int jb = lo[1]; jb <= hi[1]; ++jb)
+                    for (int ib = lo[0]; ib <= hi[0]; ++ib)
+                        blk[ib + (long long)g.nb[0] * (jb + (long long)g.nb[1] * kb)] = 1;
+        }
+    }
+}
+
+__global__ void k_amr_begin(AmrStates S) {
+    StepState* s0 = S.s[0];
+    double est = __longlong_as_double(0x7FF0000000000000LL);
+    for (int l = 0; l < S.n; ++l) {
+        const double e = __longlong_as_double((long long)S.s[l]->cfl_min) * (double)(1 << l);
+        est = e < est ? e : est;
+    }
+    double dt = s0->cfl * est;
+    if (s0->dt_prev > 0 && dt > 1.1 * s0->dt_prev) dt = 1.1 * s0->dt_prev;
+    if (s0->time + dt > s0->stop_time - 0.001 * dt) dt = s0->stop_time - s0->time;
+    if (dt < 0) dt = 0;
+    for (int l = 0; l < S.n; ++l) {
+        S.s[l]->dt = dt / (double)(1 << l);
+        S.s[l]->time = s0->time;
+        S.s[l]->cfl_min = 0x7FF0000000000000ULL;
+    }
+}
+
+__global__ void k_sub_end(StepState* s) { s->time += s->dt; }
+
+__global__ void k_amr_end(AmrStates S) {
+    StepState* s0 = S.s[0];
+    s0->time += s0->dt;
+    s0->dt_prev = s0->dt;
+    for (int l = 1; l < S.n; ++l) S.s[l]->time = s0->time;
+}
+
+__global__ void k_amr_sync(AmrStates S, double t, int reset) {
+    for (int l = 0; l < S.n; ++l) {
+        S.s[l]->time = t;
+        S.s[l]->stop_time = S.s[0]->stop_time;
+        if (reset) {
+            S.s[l]->dt = 0;
+            S.s[l]->dt_prev = -1.0;
+        }
+    }
+}
+
+__global__ void k_amr_stop(AmrStates S, double t) {
+    for (int l = 0; l < S.n; ++l) S.s[l]->stop_time = t;
+}
+
+__global__ void k_copy_step(StepState* dst, const StepState* src) {
+    *dst = *src;
+    dst->cfl_min = 0x7FF0000000000000ULL;
+}
+
+__global__ void k_reset_cfl_all(AmrStates S) {
+    for (int l = 0; l < S.n; ++l) S.s[l]->cfl_min = 0x7FF0000000000000ULL;
+}
+
+__global__ void k_estdt_into(const FabGeom* __restrict__ fabs, const long long* __restrict__ start, int nbox,
+                             long long total, const double* __restrict__ U, DevParm P, double dx0, double dx1,
+                             double dx2, unsigned long long* out) {
+    const double dx[3] = {dx0, dx1, dx2};
+    double m = __longlong_as_double(0x7FF0000000000000LL);
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = find_tag<FabGeom>(start, nbox, idx);
+        const FabGeom& f = fabs[b];
+        int i, j, k;
+        region_cell(f.lo, f.hi, idx - start[b], i, j, k);
+        const long long c = fab_index(f, i, j, k);
+        double u[5];
+        for (int n = 0; n < 5; ++n) u[n] = U[c + n * f.ns];
+        const double v = cfl_bound(P, u, dx);
+        m = v < m ? v : m;
+    }
+    block_min_atomic(m, out);
+}
+
+// ================================================================ hierarchy
+template <class Tag>
+struct DevTags {
+    Tag* d = nullptr;
+    long long* start = nullptr;
+    int n = 0;
+    long long total = 0;
+    void release() {
+        cudaFree(d);
+        cudaFree(start);
+        d = nullptr;
+        start = nullptr;
+        n = 0;
+        total = 0;
+    }
+    ocfd_status set(const std::vector<Tag>& v) {
+        release();
+        n = (int)v.size();
+        return upload_tags(v, &d, &start, &total);
+    }
+};
+
+struct AmrLev {
+    ocfd_level* L = nullptr;
+    std::vector<IBox> boxes;
+    IBox dom{};
+    double dx[3] = {0, 0, 0};
+    int bf[3] = {1, 1, 1};           // blocking factor of this level's boxes (lev >= 1)
+    DevTags<CfTag> cf;               // coarse-fine ghost cells (lev >= 1)
+    DevTags<AvgTag> avg;             // average-down into lev - 1
+    RefluxCell* d_rc = nullptr;      // reflux of lev - 1 around this level
+    RefluxFace* d_rf = nullptr;
+    int nrc = 0;
+    double* freg = nullptr;          // fine side of the register with lev - 1: boundary planes
+    long long freg_elems = 0;
+    double* creg = nullptr;          // coarse side of the register with lev + 1: face arrays
+    long long creg_elems = 0;
+    long long leaf = 0;
+    unsigned char* d_blk = nullptr;  // tag blocks of lev + 1
+    long long nblk_cap = 0;
+    void release_tables() {
+        cf.release();
+        avg.release();
+        cudaFree(d_rc);
+        cudaFree(d_rf);
+        cudaFree(freg);
+        cudaFree(creg);
+        d_rc = nullptr;
+        d_rf = nullptr;
+        nrc = 0;
+        freg = creg = nullptr;
+        freg_elems = creg_elems = 0;
+    }
+};
+
+}  // namespace ocfd
+
+struct ocfd_amr {
+    ocfd_context* ctx = nullptr;
+    ocfd_amr_desc desc{};
+    std::vector<ocfd_box> boxes0;
+    int nlev = 0;
+    ocfd::AmrLev lev[OCFD_AMR_MAX_LEVELS];
+    bool periodic[3] = {false, false, false};
+    cudaGraphExec_t graph = nullptr;
+    unsigned graph_flags = ~0u;
+    bool graph_ok = false;
+    bool need_estdt = true;
+    long long steps = 0;
+    int launches = 0;
+};
+
+namespace ocfd {
+
+static const int kNest = 2;  // proper nesting: coarse cells around a fine box's coarsening
+
+static IBox level_domain(const ocfd_amr* H, int l) {
+    IBox d = ib_of(H->desc.domain);
+    for (int e = 0; e < 3; ++e) {
+        d.lo[e] = d.lo[e] << l;
+        d.hi[e] = ((d.hi[e] + 1) << l) - 1;
+    }
+    return d;
+}
+
+static long long fab_index_h(const FabGeom& f, int i, int j, int k) {
+    return f.off + (long long)(i - f.lo[0] + NGR) + (long long)(j - f.lo[1] + NGR) * f.g[0] +
+           (long long)(k - f.lo[2] + NGR) * f.g[0] * f.g[1];
+}
+
+static AmrStates states(const ocfd_amr* H) {
+    AmrStates S{};
+    S.n = H->nlev;
+    for (int l = 0; l < H->nlev; ++l) S.s[l] = H->lev[l].L->d_step;
+    return S;
+}
+
+static ocfd_status ensure_d(ocfd_level* L) {
+    if (L->nbuf >= 4) return OCFD_OK;
+    if (cudaMalloc(&L->buf[3], sizeof(double) * L->elems) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(OCFD_OUT_OF_MEMORY, "AMR: fourth state buffer");
+    }
+    cudaMemset(L->buf[3], 0, sizeof(double) * L->elems);
+    L->nbuf = 4;
+    return OCFD_OK;
+}
+
+static ocfd_status make_level(ocfd_amr* H, int l, const std::vector<IBox>& boxes, int nbuf, ocfd_level** out) {
+    std::vector<ocfd_box> ob;
+    for (const IBox& b : boxes) ob.push_back(ob_of(b));
+    ocfd_level_desc d{};
+    d.nbox = (int)ob.size();
+    d.boxes = ob.data();
+    d.domain = ob_of(level_domain(H, l));
+    for (int e = 0; e < 3; ++e) {
+        d.lo_bc[e] = H->desc.lo_bc[e];
+        d.hi_bc[e] = H->desc.hi_bc[e];
+        d.dx[e] = H->desc.dx[e] / (double)(1 << l);
+        d.prob_lo[e] = H->desc.prob_lo[e];
+    }
+    d.bc_case = H->desc.bc_case;
+    std::memcpy(d.case_params, H->desc.case_params, sizeof(d.case_params));
+    d.tile = -1;
+    return level_alloc(H->ctx, &d, nbuf, out);
+}
+
+// periodic images (shift vectors) of a region that meet the domain
+static void periodic_shifts(const ocfd_amr* H, const IBox& dom, std::vector<std::array<int, 3>>& out) {
+    out.clear();
+    int period[3];
+    for (int e = 0; e < 3; ++e) period[e] = dom.hi[e] - dom.lo[e] + 1;
+    for (int sx = -1; sx <= 1; ++sx)
+        for (int sy = -1; sy <= 1; ++sy)
+            for (int sz = -1; sz <= 1; ++sz) {
+                const int s[3] = {sx, sy, sz};
+                bool ok = true;
+                for (int e = 0; e < 3; ++e)
+                    if (s[e] != 0 && !H->periodic[e]) ok = false;
+                if (ok) out.push_back({sx * period[0], sy * period[1], sz * period[2]});
+            }
+}
+
+// Fine cells of `regions` (per fine box) that take their value from level f-1:
+// split by the coarse box holding their parent, periodic images resolved.
+static ocfd_status build_cf_tags(const ocfd_amr* H, int f, const std::vector<std::vector<IBox>>& regions,
+                                 std::vector<CfTag>& out) {
+    const AmrLev& C = H->lev[f - 1];
+    const IBox fdom = level_domain(H, f);
+    BoxIndex cidx;
+    cidx.build(C.boxes, C.dom);
+    std::vector<std::array<int, 3>> shifts;
+    periodic_shifts(H, fdom, shifts);
+    for (int b = 0; b < (int)regions.size(); ++b) {
+        for (const IBox& P : regions[b]) {
+            long long need = ib_cells(P), got = 0;
+            for (const auto& sh : shifts) {
+                // cells g of P with g + sh inside the domain
+                IBox Qs;
+                if (!ib_isect(ib_shift(P, sh.data()), fdom, Qs)) continue;
+                const IBox Qc = ib_coarsen(Qs);
+                for (int cb : cidx.query(Qc)) {
+                    IBox I;
+                    if (!ib_isect(Qc, C.boxes[cb], I)) continue;
+                    IBox Fr;
+                    if (!ib_isect(ib_refine(I), Qs, Fr)) continue;
+                    const int back[3] = {-sh[0], -sh[1], -sh[2]};
+                    const IBox R = ib_shift(Fr, back);
+                    CfTag t{};
+                    t.fbox = b;
+                    t.cbox = cb;
+                    for (int e = 0; e < 3; ++e) {
+                        t.lo[e] = R.lo[e];
+                        t.hi[e] = R.hi[e];
+                        t.shift[e] = sh[e];
+                    }
+                    out.push_back(t);
+                    got += ib_cells(R);
+                }
+            }
+            if (got != need) return fail(OCFD_BAD_ARG, "AMR: a fine level is not properly nested in the level below");
+        }
+    }
+    return OCFD_OK;
+}
+
+// in-domain ghost cells of each fine box not covered by the level's valid boxes
+static void ghost_regions(const ocfd_amr* H, int f, std::vector<std::vector<IBox>>& regions) {
+    const AmrLev& F = H->lev[f];
+    const IBox fdom = level_domain(H, f);
+    std::vector<std::array<int, 3>> shifts;
+    periodic_shifts(H, fdom, shifts);
+    regions.assign(F.boxes.size(), {});
+    for (size_t b = 0; b < F.boxes.size(); ++b) {
+        IBox R = ib_grow(F.boxes[b], NGR);
+        for (int e = 0; e < 3; ++e)
+            if (!H->periodic[e]) {
+                R.lo[e] = std::max(R.lo[e], fdom.lo[e]);
+                R.hi[e] = std::min(R.hi[e], fdom.hi[e]);
+            }
+        std::vector<IBox> list{R};
+        for (const auto& sh : shifts)
+            for (const IBox& Q : F.boxes) {
+                IBox t;
+                const IBox Qs = ib_shift(Q, sh.data());
+                if (ib_isect(R, Qs, t)) list_subtract(list, Qs);
+            }
+        regions[b] = list;
+    }
+}
+
+static long long region_offset_plane(const IBox& pl, int i, int j, int k) {
+    const long long ex = pl.hi[0] - pl.lo[0] + 1, ey = pl.hi[1] - pl.lo[1] + 1;
+    return (long long)(i - pl.lo[0]) + (long long)(j - pl.lo[1]) * ex + (long long)(k - pl.lo[2]) * ex * ey;
+}
+
+// Tables between level c = f-1 and level f: ghost interpolation, average-down,
+// reflux cells and the two sides of the flux register.
+static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf) {
+    AmrLev& C = H->lev[f - 1];
+    AmrLev& F = H->lev[f];
+    ocfd_status s;
+    {
+        std::vector<std::vector<IBox>> regions;
+        ghost_regions(H, f, regions);
+        std::vector<CfTag> tags;
+        s = build_cf_tags(H, f, regions, tags);
+        if (s != OCFD_OK) return s;
+        s = F.cf.set(tags);
+        if (s != OCFD_OK) return s;
+    }
+    BoxIndex cidx;
+    cidx.build(C.boxes, C.dom);
+    std::vector<IBox> fcoarse;
+    for (const IBox& b : F.boxes) fcoarse.push_back(ib_coarsen(b));
+    BoxIndex fcidx;
+    fcidx.build(fcoarse, C.dom);
+    {
+        std::vector<AvgTag> tags;
+        long long covered = 0;
+        for (int fb = 0; fb < (int)F.boxes.size(); ++fb)
+            for (int cb : cidx.query(fcoarse[fb])) {
+                IBox I;
+                if (!ib_isect(fcoarse[fb], C.boxes[cb], I)) continue;
+                AvgTag t{};
+                t.cbox = cb;
+                t.fbox = fb;
+                for (int e = 0; e < 3; ++e) { t.lo[e] = I.lo[e]; t.hi[e] = I.hi[e]; }
+                tags.push_back(t);
+                covered += ib_cells(I);
+            }
+        s = F.avg.set(tags);
+        if (s != OCFD_OK) return s;
+        C.leaf = C.L->ncells - covered;
+    }
+    // ---- flux register layout: fine planes of every fine box
+    const int nfb = (int)F.boxes.size(), ncb = (int)C.boxes.size();
+    std::vector<long long> plane_off((size_t)nfb * 6);
+    std::vector<IBox> plane_box((size_t)nfb * 6);
+    long long fe = 0;
+    for (int fb = 0; fb < nfb; ++fb)
+        for (int d = 0; d < 3; ++d)
+            for (int sd = 0; sd < 2; ++sd) {
+                IBox pl = F.boxes[fb];
+                pl.lo[d] = pl.hi[d] = (sd == 0) ? F.boxes[fb].lo[d] : F.boxes[fb].hi[d] + 1;
+                plane_off[fb * 6 + 2 * d + sd] = fe;
+                plane_box[fb * 6 + 2 * d + sd] = pl;
+                fe += ib_cells(pl) * 5;
+            }
+    // ---- reflux faces grouped by uncovered coarse cell
+    struct Face {
+        int d, side, cb, fb;
+        int cf[3];  // coarse face index
+        int c[3];   // unwrapped coarse cell (transverse coordinates pick the fine faces)
+    };
+    std::map<std::pair<int, long long>, std::vector<Face>> cells;
+    const IBox& cd = C.dom;
+    for (int fb = 0; fb < nfb; ++fb) {
+        const IBox& Fc = fcoarse[fb];
+        for (int d = 0; d < 3; ++d)
+            for (int sd = 0; sd < 2; ++sd) {
+                IBox pl = Fc;
+                pl.lo[d] = pl.hi[d] = (sd == 0) ? Fc.lo[d] - 1 : Fc.hi[d] + 1;
+                for (int k = pl.lo[2]; k <= pl.hi[2]; ++k)
+                    for (int j = pl.lo[1]; j <= pl.hi[1]; ++j)
+                        for (int i = pl.lo[0]; i <= pl.hi[0]; ++i) {
+                            int c[3] = {i, j, k}, w[3] = {i, j, k};
+                            bool inside = true;
+                            for (int e = 0; e < 3; ++e) {
+                                const int per = cd.hi[e] - cd.lo[e] + 1;
+                                if (w[e] < cd.lo[e] || w[e] > cd.hi[e]) {
+                                    if (!H->periodic[e]) inside = false;
+                                    else w[e] = cd.lo[e] + (((w[e] - cd.lo[e]) % per) + per) % per;
+                                }
+                            }
+                            if (!inside) continue;
+                            if (fcidx.find(w) >= 0) continue;  // covered: fine-fine face
+                            const int cb = cidx.find(w);
+                            if (cb < 0) return fail(OCFD_BAD_ARG, "AMR: reflux cell outside the coarse level");
+                            Face fc{};
+                            fc.d = d;
+                            fc.side = sd;
+                            fc.cb = cb;
+                            fc.fb = fb;
+                            for (int e = 0; e < 3; ++e) { fc.cf[e] = w[e]; fc.c[e] = c[e]; }
+                            if (sd == 0) fc.cf[d] = w[d] + 1;
+                            const FabGeom& g = C.L->fabs[cb];
+                            cells[{cb, fab_index_h(g, w[0], w[1], w[2])}].push_back(fc);
+                        }
+            }
+    }
+    // coarse register: face arrays of the coarse boxes that own a reflux cell
+    std::vector<long long> creg_off((size_t)ncb, -1);
+    long long ce = 0;
+    for (const auto& kv : cells) {
+        const int cb = kv.first.first;
+        if (creg_off[cb] >= 0) continue;
+        creg_off[cb] = ce;
+        const IBox& B = C.boxes[cb];
+        for (int d = 0; d < 3; ++d) {
+            IBox fa = B;
+            fa.hi[d] += 1;
+            ce += ib_cells(fa) * 5;
+        }
+    }
+    auto creg_face = [&](int cb, int d, const int* fc, long long* cns) {
+        const IBox& B = C.boxes[cb];
+        long long off = creg_off[cb];
+        for (int e = 0; e < d; ++e) {
+            IBox fa = B;
+            fa.hi[e] += 1;
+            off += ib_cells(fa) * 5;
+        }
+        IBox fa = B;
+        fa.hi[d] += 1;
+        *cns = ib_cells(fa);
+        return off + region_offset_plane(fa, fc[0], fc[1], fc[2]);
+    };
+    std::vector<RefluxCell> rc_h;
+    std::vector<RefluxFace> rf_h;
+    for (const auto& kv : cells) {
+        RefluxCell cell{};
+        cell.u = kv.first.second;
+        cell.uns = C.L->fabs[kv.first.first].ns;
+        cell.first = (int)rf_h.size();
+        cell.count = (int)kv.second.size();
+        for (const Face& fc : kv.second) {
+            RefluxFace q{};
+            q.d = fc.d;
+            q.sgn = fc.side == 0 ? 1.0 : -1.0;
+            q.c = creg_face(fc.cb, fc.d, fc.cf, &q.cns);
+            const int pidx = fc.fb * 6 + 2 * fc.d + fc.side;
+            const IBox& pl = plane_box[pidx];
+            q.fns = ib_cells(pl);
+            const int t1 = fc.d == 0 ? 1 : 0, t2 = fc.d == 2 ? 1 : 2;
+            int m = 0;
+            for (int b2 = 0; b2 < 2; ++b2)
+                for (int b1 = 0; b1 < 2; ++b1) {
+                    int g[3];
+                    g[fc.d] = pl.lo[fc.d];
+                    g[t1] = 2 * fc.c[t1] + b1;
+                    g[t2] = 2 * fc.c[t2] + b2;
+                    q.f[m++] = plane_off[pidx] + region_offset_plane(pl, g[0], g[1], g[2]);
+                }
+            rf_h.push_back(q);
+        }
+        rc_h.push_back(cell);
+    }
+    F.nrc = (int)rc_h.size();
+    s = upload(&F.d_rc, rc_h);
+    if (s == OCFD_OK) s = upload(&F.d_rf, rf_h);
+    if (s != OCFD_OK) return s;
+    F.freg_elems = fe;
+    C.creg_elems = ce;
+    if (cudaMalloc(&F.freg, sizeof(double) * std::max<long long>(1, fe)) != cudaSuccess ||
+        cudaMalloc(&C.creg, sizeof(double) * std::max<long long>(1, ce)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(OCFD_OUT_OF_MEMORY, "AMR: flux registers");
+    }
+    // stage roles: register views
+    rf.flux_bits.resize(nfb, 0);
+    rf.fplane.resize((size_t)nfb * 6);
+    for (int fb = 0; fb < nfb; ++fb) {
+        rf.flux_bits[fb] |= FLUX_ACC_PLANES;
+        for (int q = 0; q < 6; ++q) {
+            const IBox& pl = plane_box[fb * 6 + q];
+            const long long ex = pl.hi[0] - pl.lo[0] + 1, ey = pl.hi[1] - pl.lo[1] + 1;
+            rf.fplane[fb * 6 + q] = View<double>{F.freg + plane_off[fb * 6 + q], ex, ex * ey, ib_cells(pl),
+                                                 pl.lo[0], pl.lo[1], pl.lo[2]};
+        }
+    }
+    rc.flux_bits.resize(ncb, 0);
+    rc.creg.resize((size_t)ncb * 3);
+    for (int cb = 0; cb < ncb; ++cb) {
+        if (creg_off[cb] < 0) continue;
+        rc.flux_bits[cb] |= FLUX_ACC_ALL;
+        long long off = creg_off[cb];
+        for (int d = 0; d < 3; ++d) {
+            IBox fa = C.boxes[cb];
+            fa.hi[d] += 1;
+            const long long ex = fa.hi[0] - fa.lo[0] + 1, ey = fa.hi[1] - fa.lo[1] + 1;
+            rc.creg[cb * 3 + d] = View<double>{C.creg + off, ex, ex * ey, ib_cells(fa), fa.lo[0], fa.lo[1], fa.lo[2]};
+            off += ib_cells(fa) * 5;
+        }
+    }
+    return OCFD_OK;
+}
+
+static ocfd_status rebuild_tables(ocfd_amr* H) {
+    std::vector<StageRoles> roles(H->nlev);
+    for (int l = 0; l < H->nlev; ++l) {
+        H->lev[l].release_tables();
+        H->lev[l].leaf = H->lev[l].L->ncells;
+        roles[l].cfl = false;
+        roles[l].out3 = (l < H->nlev - 1) ? 3 : 0;
+        if (l < H->nlev - 1) {
+            ocfd_status s = ensure_d(H->lev[l].L);
+            if (s != OCFD_OK) return s;
+        }
+    }
+    for (int f = 1; f < H->nlev; ++f) {
+        ocfd_status s = build_pair(H, f, roles[f - 1], roles[f]);
+        if (s != OCFD_OK) return s;
+    }
+    for (int l = 0; l < H->nlev; ++l) {
+        StageRoles& r = roles[l];
+        const int nb = (int)H->lev[l].boxes.size();
+        if (!r.flux_bits.empty()) {
+            r.flux_bits.resize(nb, 0);
+            r.creg.resize((size_t)nb * 3);
+            r.fplane.resize((size_t)nb * 6);
+        }
+        ocfd_status s = build_stage_tables(H->lev[l].L, r);
+        if (s != OCFD_OK) return s;
+    }
+    H->graph_ok = false;
+    H->need_estdt = true;
+    return OCFD_OK;
+}
+
+// ---------------------------------------------------------------- launches
+static int launches_counter = 0;
+
+static void mix_coefs(int kind, double theta, double r, double* a) {
+    // kind 0..2: fine stage 1..3 of the substep starting at theta; kind 3: end (theta + r)
+    double w1, w2, w3;
+    auto P = [&](double th) {
+        w1 = th - 5.0 / 6.0 * th * th;
+        w2 = th * th / 6.0;
+        w3 = 2.0 / 3.0 * th * th;
+    };
+    if (kind == 3) {
+        P(theta + r);
+    } else {
+        P(theta);
+        const double d1 = 1.0 - 5.0 / 3.0 * theta, d2 = theta / 3.0, d3 = 4.0 / 3.0 * theta;  // P' dt
+        const double e1 = -5.0 / 3.0, e2 = 1.0 / 3.0, e3 = 4.0 / 3.0;                         // P'' dt^2
+        if (kind == 1) {
+            w1 += r * d1;
+            w2 += r * d2;
+            w3 += r * d3;
+        } else if (kind == 2) {
+            w1 += 0.5 * r * d1 + 0.25 * r * r * e1;
+            w2 += 0.5 * r * d2 + 0.25 * r * r * e2;
+            w3 += 0.5 * r * d3 + 0.25 * r * r * e3;
+        }
+    }
+    a[0] = 1.0 - w1 - 3.0 * w2 - 0.5 * w3;
+    a[1] = w1 - w2;
+    a[2] = 4.0 * w2 - w3;
+    a[3] = 1.5 * w3;
+}
+
+static ocfd_status launch_cf(ocfd_amr* H, int f, double* dst, const double* a, cudaStream_t st) {
+    AmrLev& F = H->lev[f];
+    AmrLev& C = H->lev[f - 1];
+    if (F.cf.total == 0) return OCFD_OK;
+    TimeMix m{};
+    for (int q = 0; q < 4; ++q) {
+        m.a[q] = a[q];
+        m.src[q] = (a[q] != 0.0) ? C.L->buf[q] : nullptr;
+        if (a[q] != 0.0 && q >= C.L->nbuf) return fail(OCFD_BAD_ARG, "AMR: time interpolation needs a missing buffer");
+    }
+    k_cf_interp<<<grid_for(F.cf.total, 128, H->ctx->num_sms), 128, 0, st>>>(
+        F.cf.d, F.cf.start, F.cf.n, F.cf.total, F.L->d_fabs, dst, C.L->d_fabs, m, F.L->ncomp);
+    ++launches_counter;
+    return check_launch("AMR coarse-fine interpolation");
+}
+
+static ocfd_status fill_level(ocfd_amr* H, int l, double* U, const double* a, double tfrac, cudaStream_t st) {
+    ocfd_status s = OCFD_OK;
+    if (l > 0) s = launch_cf(H, l, U, a, st);
+    if (s == OCFD_OK) s = fill_exchange(H->lev[l].L, U, st);
+    if (s == OCFD_OK) s = fill_physbc(H->lev[l].L, U, tfrac, st);
+    ocfd_level* L = H->lev[l].L;
+    launches_counter += (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0);
+    return s;
+}
+
+static ocfd_status launch_avg(ocfd_amr* H, int f, const double* fsrc, double* cdst, cudaStream_t st) {
+    AmrLev& F = H->lev[f];
+    AmrLev& C = H->lev[f - 1];
+    if (F.avg.total == 0) return OCFD_OK;
+    k_avg_down<<<grid_for(F.avg.total, 256, H->ctx->num_sms), 256, 0, st>>>(
+        F.avg.d, F.avg.start, F.avg.n, F.avg.total, C.L->d_fabs, cdst, F.L->d_fabs, fsrc, F.L->ncomp);
+    ++launches_counter;
+    return check_launch("AMR average-down");
+}
+
+static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cudaStream_t st) {
+    AmrLev& A = H->lev[l];
+    ocfd_level* L = A.L;
+    const bool has_child = l < H->nlev - 1;
+    const double theta = 0.5 * (it - 1), r = 0.5;
+    const double tfrac[3] = {0.0, 1.0, 0.5};
+    ocfd_status s = OCFD_OK;
+    if (has_child) {
+        cudaMemsetAsync(A.creg, 0, sizeof(double) * std::max<long long>(1, A.creg_elems), st);
+        cudaMemsetAsync(H->lev[l + 1].freg, 0, sizeof(double) * std::max<long long>(1, H->lev[l + 1].freg_elems), st);
+        launches_counter += 2;
+    }
+    for (int k = 0; k < 3 && s == OCFD_OK; ++k) {
+        double a[4];
+        mix_coefs(k, theta, r, a);
+        s = fill_level(H, l, L->buf[k], a, tfrac[k], st);
+        if (s == OCFD_OK) s = launch_stage(L, k, flags, st);
+        ++launches_counter;
+    }
+    if (s != OCFD_OK) return s;
+    if (has_child) {
+        double a[4];
+        mix_coefs(3, theta, r, a);
+        s = fill_level(H, l, L->buf[3], a, 1.0, st);
+        for (int i = 1; i <= 2 && s == OCFD_OK; ++i) s = advance_level(H, l + 1, i, flags, st);
+        if (s != OCFD_OK) return s;
+        AmrLev& F = H->lev[l + 1];
+        if (F.nrc > 0) {
+            k_reflux<<<(F.nrc + 127) / 128, 128, 0, st>>>(F.d_rc, F.nrc, F.d_rf, A.creg, F.freg, L->buf[3],
+                                                         1.0 / A.dx[0], 1.0 / A.dx[1], 1.0 / A.dx[2]);
+            ++launches_counter;
+        }
+        s = launch_avg(H, l + 1, F.L->buf[0], L->buf[3], st);
+        if (s != OCFD_OK) return s;
+        if (cudaMemcpyAsync(L->buf[0], L->buf[3], sizeof(double) * L->elems, cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess)
+            return check_launch("AMR D -> A");
+        ++launches_counter;
+    }
+    if (l > 0) {
+        k_sub_end<<<1, 1, 0, st>>>(L->d_step);
+        ++launches_counter;
+    }
+    return check_launch("AMR level advance");
+}
+
+static ocfd_status launch_estdt_all(ocfd_amr* H, cudaStream_t st) {
+    for (int l = 0; l < H->nlev; ++l) {
+        ocfd_level* L = H->lev[l].L;
+        k_estdt_into<<<grid_for(L->ncells, 256, H->ctx->num_sms), 256, 0, st>>>(
+            L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->buf[0], H->ctx->parm, L->desc.dx[0],
+            L->desc.dx[1], L->desc.dx[2], &L->d_step->cfl_min);
+        ++launches_counter;
+    }
+    return check_launch("AMR estdt");
+}
+
+static ocfd_status record_amr_step(ocfd_amr* H, unsigned flags, cudaStream_t st) {
+    launches_counter = 0;
+    k_amr_begin<<<1, 1, 0, st>>>(states(H));
+    ocfd_status s = advance_level(H, 0, 1, flags, st);
+    if (s == OCFD_OK) s = launch_estdt_all(H, st);
+    k_amr_end<<<1, 1, 0, st>>>(states(H));
+    launches_counter += 2;
+    H->launches = launches_counter;
+    if (s != OCFD_OK) return s;
+    return check_launch("AMR step");
+}
+
+// all levels' ghosts from their current state A, bottom-up
+static ocfd_status fill_all_sync(ocfd_amr* H, cudaStream_t st) {
+    const double a[4] = {1.0, 0.0, 0.0, 0.0};
+    for (int l = 0; l < H->nlev; ++l) {
+        ocfd_status s = fill_level(H, l, H->lev[l].L->buf[0], a, 0.0, st);
+        if (s != OCFD_OK) return s;
+    }
+    return OCFD_OK;
+}
+
+// ---------------------------------------------------------------- regridding
+struct BlockGrid {
+    IBox dom;      // level domain (cells of the level)
+    int bf[3];     // block size in cells of the level
+    int nb[3];
+    std::vector<unsigned char> v;
+    size_t at(int i, int j, int k) const { return (size_t)i + (size_t)nb[0] * ((size_t)j + (size_t)nb[1] * k); }
+};
+
+static void block_geometry(const ocfd_amr* H, int f, BlockGrid& g) {
+    g.dom = level_domain(H, f);
+    for (int e = 0; e < 3; ++e) {
+        const int ext = g.dom.hi[e] - g.dom.lo[e] + 1;
+        g.bf[e] = std::min(H->desc.blocking_factor[e], ext);
+        g.nb[e] = ext / g.bf[e];
+    }
+    g.v.assign((size_t)g.nb[0] * g.nb[1] * g.nb[2], 0);
+}
+
+static IBox block_box(const BlockGrid& g, int i, int j, int k) {
+    const int b[3] = {i, j, k};
+    IBox r;
+    for (int e = 0; e < 3; ++e) {
+        r.lo[e] = g.dom.lo[e] + b[e] * g.bf[e];
+        r.hi[e] = r.lo[e] + g.bf[e] - 1;
+    }
+    return r;
+}
+
+// mark the blocks of g that meet region r (level cells; periodic images wrapped,
+// non-periodic parts outside the domain dropped)
+static void mark_region(const ocfd_amr* H, BlockGrid& g, const IBox& r) {
+    std::vector<std::array<int, 3>> shifts;
+    periodic_shifts(H, g.dom, shifts);
+    for (const auto& sh : shifts) {
+        IBox q;
+        if (!ib_isect(ib_shift(r, sh.data()), g.dom, q)) continue;
+        int lo[3], hi[3];
+        for (int e = 0; e < 3; ++e) {
+            lo[e] = (q.lo[e] - g.dom.lo[e]) / g.bf[e];
+            hi[e] = (q.hi[e] - g.dom.lo[e]) / g.bf[e];
+        }
+        for (int k = lo[2]; k <= hi[2]; ++k)
+            for (int j = lo[1]; j <= hi[1]; ++j)
+                for (int i = lo[0]; i <= hi[0]; ++i) g.v[g.at(i, j, k)] = 1;
+    }
+}
+
+// is region r (level cells) inside the boxes of `idx` wherever it is inside the domain?
+static bool region_covered(const ocfd_amr* H, const BoxIndex& idx, const IBox& r) {
+    std::vector<std::array<int, 3>> shifts;
+    periodic_shifts(H, idx.dom, shifts);
+    for (const auto& sh : shifts) {
+        IBox q;
+        if (!ib_isect(ib_shift(r, sh.data()), idx.dom, q)) continue;
+        std::vector<IBox> rest{q};
+        for (int b : idx.query(q)) {
+            list_subtract(rest, idx.boxes[b]);
+            if (rest.empty()) break;
+        }
+        if (!rest.empty()) return false;
+    }
+    return true;
+}
+
+static std::vector<IBox> cluster_blocks(const ocfd_amr* H, const BlockGrid& g) {
+    std::vector<IBox> out;
+    std::vector<unsigned char> used(g.v.size(), 0);
+    int mg[3];
+    for (int e = 0; e < 3; ++e) mg[e] = std::max(1, H->desc.max_grid_size[e] / g.bf[e]);
+    auto ok = [&](int i, int j, int k) { return g.v[g.at(i, j, k)] && !used[g.at(i, j, k)]; };
+    for (int k = 0; k < g.nb[2]; ++k)
+        for (int j = 0; j < g.nb[1]; ++j)
+            for (int i = 0; i < g.nb[0]; ++i) {
+                if (!ok(i, j, k)) continue;
+                int ex = 1, ey = 1, ez = 1;
+                while (i + ex < g.nb[0] && ex < mg[0] && ok(i + ex, j, k)) ++ex;
+                while (j + ey < g.nb[1] && ey < mg[1]) {
+                    bool row = true;
+                    for (int a = 0; a < ex && row; ++a) row = ok(i + a, j + ey, k);
+                    if (!row) break;
+                    ++ey;
+                }
+                while (k + ez < g.nb[2] && ez < mg[2]) {
+                    bool pl = true;
+                    for (int b = 0; b < ey && pl; ++b)
+                        for (int a = 0; a < ex && pl; ++a) pl = ok(i + a, j + b, k + ez);
+                    if (!pl) break;
+                    ++ez;
+                }
+                for (int c = 0; c < ez; ++c)
+                    for (int b = 0; b < ey; ++b)
+                        for (int a = 0; a < ex; ++a) used[g.at(i + a, j + b, k + c)] = 1;
+                IBox lo = block_box(g, i, j, k), hi = block_box(g, i + ex - 1, j + ey - 1, k + ez - 1);
+                IBox r;
+                for (int e = 0; e < 3; ++e) { r.lo[e] = lo.lo[e]; r.hi[e] = hi.hi[e]; }
+                out.push_back(r);
+            }
+    return out;
+}
+
+static bool same_boxes(const std::vector<IBox>& a, const std::vector<IBox>& b) {
+    if (a.size() != b.size()) return false;
+    for (size_t i = 0; i < a.size(); ++i)
+        if (!ib_same(a[i], b[i])) return false;
+    return true;
+}
+
+static ocfd_status launch_copy(ocfd_amr* H, ocfd_level* dst, const std::vector<IBox>& dboxes, ocfd_level* src,
+                               const std::vector<IBox>& sboxes, cudaStream_t st) {
+    std::vector<CopyTag> tags;
+    for (int d = 0; d < (int)dboxes.size(); ++d)
+        for (int s = 0; s < (int)sboxes.size(); ++s) {
+            IBox I;
+            if (!ib_isect(dboxes[d], sboxes[s], I)) continue;
+            CopyTag t{};
+            t.dst = d;
+            t.src = s;
+            for (int e = 0; e < 3; ++e) { t.lo[e] = I.lo[e]; t.hi[e] = I.hi[e]; }
+            tags.push_back(t);
+        }
+    if (tags.empty()) return OCFD_OK;
+    DevTags<CopyTag> dt;
+    ocfd_status s = dt.set(tags);
+    if (s == OCFD_OK) {
+        k_copy_tags<<<grid_for(dt.total, 256, H->ctx->num_sms), 256, 0, st>>>(
+            dt.d, dt.start, dt.n, dt.total, dst->d_fabs, dst->buf[0], src->d_fabs, src->buf[0], dst->ncomp);
+        s = check_launch("AMR regrid copy");
+    }
+    cudaStreamSynchronize(st);
+    dt.release();
+    return s;
+}
+
+// Install new grids for levels lbase+1 .. lbase+grids.size() (empty list ends the
+// hierarchy); ghosts of levels <= lbase must hold the current state.
+static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::vector<IBox>>& grids, cudaStream_t st) {
+    int newfinest = lbase;
+    for (size_t q = 0; q < grids.size(); ++q) {
+        if (grids[q].empty()) break;
+        newfinest = lbase + 1 + (int)q;
+    }
+    if (newfinest >= OCFD_AMR_MAX_LEVELS || newfinest > H->desc.max_level)
+        return fail(OCFD_BAD_ARG, "AMR: more levels than max_level");
+    const double a[4] = {1.0, 0.0, 0.0, 0.0};
+    for (int f = lbase + 1; f <= newfinest; ++f) {
+        const std::vector<IBox>& nb = grids[f - lbase - 1];
+        const bool exists = f < H->nlev;
+        if (exists && same_boxes(nb, H->lev[f].boxes)) continue;
+        ocfd_level* NL = nullptr;
+        ocfd_status s = make_level(H, f, nb, f < newfinest ? 4 : 3, &NL);
+        if (s != OCFD_OK) return s;
+        AmrLev& A = H->lev[f];
+        ocfd_level* old = exists ? A.L : nullptr;
+        std::vector<IBox> oldboxes = exists ? A.boxes : std::vector<IBox>();
+        A.release_tables();
+        A.L = NL;
+        A.boxes = nb;
+        A.dom = level_domain(H, f);
+        for (int e = 0; e < 3; ++e) A.dx[e] = H->desc.dx[e] / (double)(1 << f);
+        if (H->nlev < f + 1) H->nlev = f + 1;
+        k_copy_step<<<1, 1, 0, st>>>(NL->d_step, H->lev[0].L->d_step);
+        // every valid cell from the level below, then the old level where it overlaps
+        {
+            std::vector<std::vector<IBox>> regions(nb.size());
+            for (size_t b = 0; b < nb.size(); ++b) regions[b] = {nb[b]};
+            std::vector<CfTag> tags;
+            s = build_cf_tags(H, f, regions, tags);
+            if (s == OCFD_OK) s = A.cf.set(tags);
+            if (s == OCFD_OK) s = launch_cf(H, f, NL->buf[0], a, st);
+        }
+        if (s == OCFD_OK && old) s = launch_copy(H, NL, nb, old, oldboxes, st);
+        if (old) {
+            cudaStreamSynchronize(st);
+            ocfd_level_destroy(old);
+        }
+        if (s != OCFD_OK) return s;
+        // ghosts of the new level (its finer neighbour interpolates from them)
+        {
+            std::vector<std::vector<IBox>> regions;
+            ghost_regions(H, f, regions);
+            std::vector<CfTag> tags;
+            s = build_cf_tags(H, f, regions, tags);
+            if (s == OCFD_OK) s = A.cf.set(tags);
+            if (s == OCFD_OK) s = fill_level(H, f, NL->buf[0], a, 0.0, st);
+            if (s != OCFD_OK) return s;
+        }
+    }
+    for (int f = newfinest + 1; f < H->nlev; ++f) {
+        cudaStreamSynchronize(st);
+        H->lev[f].release_tables();
+        ocfd_level_destroy(H->lev[f].L);
+        H->lev[f].L = nullptr;
+        H->lev[f].boxes.clear();
+    }
+    H->nlev = newfinest + 1;
+    // every level's clock follows level 0
+    {
+        AmrStates S = states(H);
+        StepState h{};
+        cudaStreamSynchronize(st);
+        if (cudaMemcpy(&h, S.s[0], sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return check_launch("AMR time");
+        for (int l = 1; l < H->nlev; ++l) {
+            StepState q = h;
+            q.cfl_min = 0x7FF0000000000000ULL;
+            if (cudaMemcpy(S.s[l], &q, sizeof(q), cudaMemcpyHostToDevice) != cudaSuccess) return check_launch("AMR time");
+        }
+    }
+    return rebuild_tables(H);
+}
+
+static ocfd_status regrid(ocfd_amr* H, int lbase, cudaStream_t st) {
+    if (lbase < 0 || lbase >= H->nlev) return fail(OCFD_BAD_ARG, "ocfd_amr_regrid: lbase");
+    if (lbase >= H->desc.max_level) return OCFD_OK;
+    ocfd_status s = fill_all_sync(H, st);
+    if (s != OCFD_OK) return s;
+    const int top = std::min(H->nlev - 1, H->desc.max_level - 1);
+    std::vector<BlockGrid> T(top + 2);
+    for (int l = lbase; l <= top; ++l) {
+        BlockGrid& g = T[l + 1];
+        block_geometry(H, l + 1, g);
+        AmrLev& A = H->lev[l];
+        const long long nblk = (long long)g.v.size();
+        if (A.nblk_cap < nblk) {
+            cudaFree(A.d_blk);
+            if (cudaMalloc(&A.d_blk, nblk) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(OCFD_OUT_OF_MEMORY, "AMR tag blocks");
+            }
+            A.nblk_cap = nblk;
+        }
+        cudaMemsetAsync(A.d_blk, 0, nblk, st);
+        TagGeom tg{};
+        for (int e = 0; e < 3; ++e) {
+            tg.dom_lo[e] = A.dom.lo[e];
+            tg.dom_hi[e] = A.dom.hi[e];
+            tg.bs[e] = g.bf[e] / 2;
+            tg.nb[e] = g.nb[e];
+        }
+        tg.nbuf = H->desc.n_error_buf;
+        tg.thr = H->desc.refine_dengrad;
+        ocfd_level* L = A.L;
+        k_tag_dengrad<<<grid_for(L->ncells, 256, H->ctx->num_sms), 256, 0, st>>>(
+            L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->buf[0], tg, A.d_blk);
+        s = check_launch("AMR tagging");
+        if (s != OCFD_OK) return s;
+        if (cudaMemcpyAsync(g.v.data(), A.d_blk, nblk, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            return check_launch("AMR tag download");
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("AMR tagging");
+    // top-down: a level also covers the neighbourhood of the new level above it
+    for (int f = top + 1; f >= lbase + 2; --f) {
+        BlockGrid& fine = T[f];
+        BlockGrid& crse = T[f - 1];
+        for (int k = 0; k < fine.nb[2]; ++k)
+            for (int j = 0; j < fine.nb[1]; ++j)
+                for (int i = 0; i < fine.nb[0]; ++i)
+                    if (fine.v[fine.at(i, j, k)]) mark_region(H, crse, ib_grow(ib_coarsen(block_box(fine, i, j, k)), kNest));
+    }
+    // bottom-up: drop blocks not properly nested, cluster
+    std::vector<std::vector<IBox>> grids;
+    BoxIndex below;
+    below.build(H->lev[lbase].boxes, H->lev[lbase].dom);
+    for (int f = lbase + 1; f <= top + 1; ++f) {
+        BlockGrid& g = T[f];
+        for (int k = 0; k < g.nb[2]; ++k)
+            for (int j = 0; j < g.nb[1]; ++j)
+                for (int i = 0; i < g.nb[0]; ++i) {
+                    unsigned char& v = g.v[g.at(i, j, k)];
+                    if (v && !region_covered(H, below, ib_grow(ib_coarsen(block_box(g, i, j, k)), kNest))) v = 0;
+                }
+        std::vector<IBox> boxes = cluster_blocks(H, g);
+        grids.push_back(boxes);
+        if (boxes.empty()) break;
+        below.build(boxes, g.dom);
+    }
+    return apply_grids(H, lbase, grids, st);
+}
+
+static ocfd_status ensure_graph(ocfd_amr* H, unsigned flags) {
+    if (H->graph_ok && H->graph && H->graph_flags == flags) return OCFD_OK;
+    if (H->graph) {
+        cudaGraphExecDestroy(H->graph);
+        H->graph = nullptr;
+    }
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return check_launch("capture stream");
+    cudaGraph_t g;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaStreamDestroy(cap);
+        return check_launch("begin capture");
+    }
+    ocfd_status s = record_amr_step(H, flags, cap);
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (s != OCFD_OK) return s;
+    if (e != cudaSuccess) return fail(OCFD_LAUNCH_FAIL, std::string("AMR end capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&H->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(OCFD_LAUNCH_FAIL, std::string("AMR graph instantiate: ") + cudaGetErrorString(e));
+    H->graph_flags = flags;
+    H->graph_ok = true;
+    return OCFD_OK;
+}
+
+}  // namespace ocfd
+
+using namespace ocfd;
+
+extern "C" {
+
+ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_amr** out) {
+    if (!ctx || !desc || !out || desc->nbox0 <= 0 || !desc->boxes0) return fail(OCFD_BAD_ARG, "ocfd_amr_create: bad arguments");
+    *out = nullptr;
+    if (desc->max_level < 0 || desc->max_level >= OCFD_AMR_MAX_LEVELS)
+        return fail(OCFD_BAD_ARG, "ocfd_amr_create: max_level out of range");
+    for (int e = 0; e < 3; ++e) {
+        const int ext = desc->domain.hi[e] - desc->domain.lo[e] + 1;
+        if (ext <= 0 || desc->max_grid_size[e] <= 0 || desc->blocking_factor[e] <= 0)
+            return fail(OCFD_BAD_ARG, "ocfd_amr_create: domain, blocking_factor and max_grid_size must be positive");
+        for (int l = 1; l <= desc->max_level; ++l) {
+            const int el = ext << l;
+            const int bf = std::min(desc->blocking_factor[e], el);
+            if (bf % 2 != 0 || el % bf != 0)
+                return fail(OCFD_BAD_ARG, "ocfd_amr_create: blocking_factor must be even and divide every level's domain");
+        }
+    }
+    if (desc->n_error_buf < 0) return fail(OCFD_BAD_ARG, "ocfd_amr_create: n_error_buf");
+    ocfd_amr* H = new ocfd_amr();
+    H->ctx = ctx;
+    H->desc = *desc;
+    H->boxes0.assign(desc->boxes0, desc->boxes0 + desc->nbox0);
+    H->desc.boxes0 = nullptr;
+    for (int e = 0; e < 3; ++e) H->periodic[e] = desc->lo_bc[e] == OCFD_BC_INTERIOR;
+    std::vector<IBox> b0;
+    long long cells = 0;
+    for (const ocfd_box& b : H->boxes0) {
+        b0.push_back(ib_of(b));
+        cells += ib_cells(ib_of(b));
+    }
+    if (cells != ib_cells(ib_of(desc->domain))) {
+        delete H;
+        return fail(OCFD_BAD_ARG, "ocfd_amr_create: level-0 boxes must cover the domain");
+    }
+    ocfd_level* L0 = nullptr;
+    ocfd_status s = make_level(H, 0, b0, 3, &L0);
+    if (s != OCFD_OK) {
+        delete H;
+        return s;
+    }
+    H->lev[0].L = L0;
+    H->lev[0].boxes = b0;
+    H->lev[0].dom = level_domain(H, 0);
+    for (int e = 0; e < 3; ++e) H->lev[0].dx[e] = desc->dx[e];
+    H->nlev = 1;
+    s = rebuild_tables(H);
+    if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = check_launch("ocfd_amr_create");
+    if (s != OCFD_OK) {
+        ocfd_amr_destroy(H);
+        return s;
+    }
+    *out = H;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_amr_destroy(ocfd_amr* H) {
+    if (!H) return OCFD_OK;
+    cudaDeviceSynchronize();
+    if (H->graph) cudaGraphExecDestroy(H->graph);
+    for (int l = 0; l < OCFD_AMR_MAX_LEVELS; ++l) {
+        H->lev[l].release_tables();
+        cudaFree(H->lev[l].d_blk);
+        if (H->lev[l].L) ocfd_level_destroy(H->lev[l].L);
+    }
+    delete H;
+    return OCFD_OK;
+}
+
+int ocfd_amr_nlevels(const ocfd_amr* H) { return H ? H->nlev : 0; }
+
+ocfd_level* ocfd_amr_level(ocfd_amr* H, int lev) {
+    if (!H || lev < 0 || lev >= H->nlev) return nullptr;
+    return H->lev[lev].L;
+}
+
+int ocfd_amr_get_grids(const ocfd_amr* H, int lev, ocfd_box* out, int cap) {
+    if (!H || lev < 0 || lev >= H->nlev) return -1;
+    const std::vector<IBox>& b = H->lev[lev].boxes;
+    for (int i = 0; i < (int)b.size() && i < cap; ++i) out[i] = ob_of(b[i]);
+    return (int)b.size();
+}
+
+ocfd_status ocfd_amr_regrid(ocfd_amr* H, int lbase, void* stream) {
+    if (!H) return fail(OCFD_BAD_ARG, "ocfd_amr_regrid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    ocfd_status s = regrid(H, lbase, st);
+    if (s == OCFD_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_launch("ocfd_amr_regrid");
+    return s;
+}
+
+ocfd_status ocfd_amr_set_grids(ocfd_amr* H, int nlev, const int32_t* nbox, const ocfd_box* boxes, void* stream) {
+    if (!H || nlev < 1 || nlev - 1 > H->desc.max_level || (nlev > 1 && (!nbox || !boxes)))
+        return fail(OCFD_BAD_ARG, "ocfd_amr_set_grids");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::vector<std::vector<IBox>> grids;
+    long long q = 0;
+    for (int l = 1; l < nlev; ++l) {
+        if (nbox[l] <= 0) return fail(OCFD_BAD_ARG, "ocfd_amr_set_grids: empty level");
+        std::vector<IBox> g;
+        const IBox dom = level_domain(H, l);
+        for (int i = 0; i < nbox[l]; ++i) {
+            IBox b = ib_of(boxes[q++]), t;
+            if (!ib_isect(b, dom, t) || !ib_same(b, t)) return fail(OCFD_BAD_ARG, "ocfd_amr_set_grids: box outside the domain");
+            for (int e = 0; e < 3; ++e)
+                if (b.lo[e] % 2 != 0 || (b.hi[e] + 1) % 2 != 0)
+                    return fail(OCFD_BAD_ARG, "ocfd_amr_set_grids: fine boxes must coarsen by 2");
+            g.push_back(b);
+        }
+        grids.push_back(g);
+    }
+    grids.push_back({});
+    ocfd_status s = fill_all_sync(H, st);
+    if (s == OCFD_OK) s = apply_grids(H, 0, grids, st);
+    if (s == OCFD_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_launch("ocfd_amr_set_grids");
+    return s;
+}
+
+ocfd_status ocfd_amr_average_down(ocfd_amr* H, void* stream) {
+    if (!H) return fail(OCFD_BAD_ARG, "ocfd_amr_average_down");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int f = H->nlev - 1; f >= 1; --f) {
+        ocfd_status s = launch_avg(H, f, H->lev[f].L->buf[0], H->lev[f - 1].L->buf[0], st);
+        if (s != OCFD_OK) return s;
+    }
+    H->need_estdt = true;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_amr_fill_ghosts(ocfd_amr* H, void* stream) {
+    if (!H) return fail(OCFD_BAD_ARG, "ocfd_amr_fill_ghosts");
+    return fill_all_sync(H, static_cast<cudaStream_t>(stream));
+}
+
+ocfd_status ocfd_amr_advance(ocfd_amr* H, int nsteps, double cfl, unsigned flags, void* stream) {
+    if (!H || nsteps < 0 || !(cfl > 0)) return fail(OCFD_BAD_ARG, "ocfd_amr_advance");
+    if (flags & ~(unsigned)OCFD_FLUX_FP32) return fail(OCFD_BAD_ARG, "ocfd_amr_advance: flags (inviscid ideal gas only)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int i = 0; i < nsteps; ++i) {
+        if (H->desc.regrid_int > 0 && H->steps > 0 && H->steps % H->desc.regrid_int == 0) {
+            ocfd_status s = regrid(H, 0, st);
+            if (s != OCFD_OK) return s;
+        }
+        if (cudaMemcpyAsync(&H->lev[0].L->d_step->cfl, &cfl, sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return check_launch("ocfd_amr_advance");
+        if (H->need_estdt) {
+            k_reset_cfl_all<<<1, 1, 0, st>>>(states(H));
+            ocfd_status s = launch_estdt_all(H, st);
+            if (s != OCFD_OK) return s;
+            H->need_estdt = false;
+        }
+        ocfd_status s = ensure_graph(H, flags);
+        if (s != OCFD_OK) return s;
+        if (cudaGraphLaunch(H->graph, st) != cudaSuccess) return check_launch("AMR graph launch");
+        ++H->steps;
+    }
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_amr_time(ocfd_amr* H, double* time, double* last_dt0, void* stream) {
+    if (!H) return fail(OCFD_BAD_ARG, "ocfd_amr_time");
+    return ocfd_level_time(H->lev[0].L, time, last_dt0, stream);
+}
+
+ocfd_status ocfd_amr_set_time(ocfd_amr* H, double time, void* stream) {
+    if (!H) return fail(OCFD_BAD_ARG, "ocfd_amr_set_time");
+    k_amr_sync<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(states(H), time, 1);
+    H->need_estdt = true;
+    H->steps = 0;
+    return check_launch("ocfd_amr_set_time");
+}
+
+ocfd_status ocfd_amr_set_stop_time(ocfd_amr* H, double stop_time, void* stream) {
+    if (!H) return fail(OCFD_BAD_ARG, "ocfd_amr_set_stop_time");
+    k_amr_stop<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(states(H), stop_time);
+    return check_launch("ocfd_amr_set_stop_time");
+}
+
+ocfd_status ocfd_amr_cell_steps(const ocfd_amr* H, int64_t* leaf, int64_t* all) {
+    if (!H) return fail(OCFD_BAD_ARG, "ocfd_amr_cell_steps");
+    int64_t a = 0, b = 0;
+    for (int l = 0; l < H->nlev; ++l) {
+        a += (int64_t)H->lev[l].leaf << l;
+        b += (int64_t)H->lev[l].L->ncells << l;
+    }
+    if (leaf) *leaf = a;
+    if (all) *all = b;
+    return OCFD_OK;
+}
+
+int ocfd_amr_launches_per_step(const ocfd_amr* H) { return H ? H->launches : 0; }
+
+}  // extern "C"

@@ -25,67 +25,9 @@
 #include <string>
 #include <vector>
 
-#include "ocfd_internal.h"
-#include "rhs_regular.h"
+#include "level.h"
 
 namespace ocfd {
-
-constexpr int NGR = OCFD_NUM_GROW;
-
-struct FabGeom {
-    int lo[3], hi[3];  // valid box
-    long long off;     // element offset of the FAB in a state buffer
-    int g[3];          // grown extents
-    long long ns;      // component stride
-};
-
-struct ExTag {
-    int dst, src;
-    int lo[3], hi[3];  // region, absolute cell indices of the destination
-    int shift[3];      // src cell = dst cell + shift
-};
-
-struct BcTag {
-    int box, side;
-    int lo[3], hi[3];
-};
-
-struct StepState {
-    double time, dt, dt_prev, cfl;
-    unsigned long long cfl_min;
-    double stop_time;  // the last step is shortened to land on it (Source/EBR.cpp:279-286)
-};
-
-struct BcInfo {
-    int lo_bc[3], hi_bc[3];
-    int dom_lo[3], dom_hi[3];
-    double dx[3], prob_lo[3];
-    int bc_case;
-    double params[16];
-};
-
-__device__ __forceinline__ long long fab_index(const FabGeom& f, int i, int j, int k) {
-    return f.off + (long long)(i - f.lo[0] + NGR) + (long long)(j - f.lo[1] + NGR) * f.g[0] +
-           (long long)(k - f.lo[2] + NGR) * f.g[0] * f.g[1];
-}
-
-template <class Tag>
-__device__ __forceinline__ int find_tag(const long long* start, int ntag, long long idx) {
-    int lo = 0, hi = ntag - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (start[mid] <= idx) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-__device__ __forceinline__ void region_cell(const int* lo, const int* hi, long long local, int& i,
-                                            int& j, int& k) {
-    const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
-    i = lo[0] + (int)(local % nx);
-    j = lo[1] + (int)((local / nx) % ny);
-    k = lo[2] + (int)(local / (nx * ny));
-}
 
 __global__ void k_exchange(const ExTag* __restrict__ tags, const long long* __restrict__ start,
                            int ntag, long long total, const FabGeom* __restrict__ fabs, double* U,
@@ -217,7 +159,7 @@ __global__ void k_set_time(StepState* st, double t) {
     st->cfl_min = 0x7FF0000000000000ULL;
 }
 
-static int grid_for(long long total, int threads, int sms) {
+int grid_for(long long total, int threads, int sms) {
     long long b = (total + threads - 1) / threads;
     long long cap = (long long)sms * 16;
     return (int)std::max<long long>(1, std::min(b, cap));
@@ -227,53 +169,9 @@ static int grid_for(long long total, int threads, int sms) {
 
 using namespace ocfd;
 
-struct ocfd_level {
-    ocfd_context* ctx = nullptr;
-    ocfd_level_desc desc{};
-    std::vector<ocfd_box> boxes;
-    std::vector<FabGeom> fabs;
-    long long elems = 0;      // per state buffer
-    int ncomp = 5;
-    double* buf[3] = {nullptr, nullptr, nullptr};
-    FabGeom* d_fabs = nullptr;
-    long long* d_cell_start = nullptr;
-    long long ncells = 0;
-    // exchange
-    ExTag* d_ex = nullptr;
-    long long* d_ex_start = nullptr;
-    int nex = 0;
-    long long ex_total = 0;
-    // physical BC passes
-    BcTag* d_bc[3] = {nullptr, nullptr, nullptr};
-    long long* d_bc_start[3] = {nullptr, nullptr, nullptr};
-    int nbc[3] = {0, 0, 0};
-    long long bc_total[3] = {0, 0, 0};
-    BcInfo bcinfo{};
-    // RHS stage tables (3 stages)
-    int tile = 0;
-    RegBoxArgs* d_stage[3] = {nullptr, nullptr, nullptr};
-    int* d_tile_start = nullptr;
-    int ntiles = 0;
-    StepState* d_step = nullptr;
-    bool need_estdt = true;
-    // graph
-    cudaGraphExec_t graph = nullptr;
-    unsigned graph_flags = ~0u;
-    double graph_cfl = -1;
-};
-
 namespace ocfd {
 
-template <class T>
-static ocfd_status upload(T** dptr, const std::vector<T>& v) {
-    size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
-    if (cudaMalloc(dptr, bytes) != cudaSuccess) return fail(OCFD_OUT_OF_MEMORY, "level table allocation");
-    if (!v.empty() && cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
-        return fail(OCFD_LAUNCH_FAIL, "level table upload");
-    return OCFD_OK;
-}
-
-static bool intersect(const int* alo, const int* ahi, const int* blo, const int* bhi, int* lo, int* hi) {
+bool intersect(const int* alo, const int* ahi, const int* blo, const int* bhi, int* lo, int* hi) {
     for (int d = 0; d < 3; ++d) {
         lo[d] = std::max(alo[d], blo[d]);
         hi[d] = std::min(ahi[d], bhi[d]);
@@ -282,7 +180,7 @@ static bool intersect(const int* alo, const int* ahi, const int* blo, const int*
     return true;
 }
 
-static long long region_cells(const int* lo, const int* hi) {
+long long region_cells(const int* lo, const int* hi) {
     return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
 }
 
@@ -370,27 +268,15 @@ static void build_physbc(ocfd_level* L, int d, std::vector<BcTag>& tags) {
     }
 }
 
-template <class Tag>
-static ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** d_start,
-                               long long* total) {
-    std::vector<long long> start(tags.size());
-    long long acc = 0;
-    for (size_t i = 0; i < tags.size(); ++i) {
-        start[i] = acc;
-        acc += region_cells(tags[i].lo, tags[i].hi);
-    }
-    *total = acc;
-    ocfd_status s = upload(d_tags, tags);
-    if (s != OCFD_OK) return s;
-    return upload(d_start, start);
+ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st) {
+    if (L->ex_total > 0)
+        k_exchange<<<grid_for(L->ex_total, 256, L->ctx->num_sms), 256, 0, st>>>(
+            L->d_ex, L->d_ex_start, L->nex, L->ex_total, L->d_fabs, U, L->ncomp);
+    return check_launch("level exchange");
 }
 
-static ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st) {
+ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st) {
     const int sms = L->ctx->num_sms;
-    if (L->ex_total > 0) {
-        k_exchange<<<grid_for(L->ex_total, 256, sms), 256, 0, st>>>(L->d_ex, L->d_ex_start, L->nex,
-                                                                    L->ex_total, L->d_fabs, U, L->ncomp);
-    }
     if (L->bc_total[0] > 0)
         k_physbc<0><<<grid_for(L->bc_total[0], 256, sms), 256, 0, st>>>(
             L->d_bc[0], L->d_bc_start[0], L->nbc[0], L->bc_total[0], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
@@ -400,10 +286,16 @@ static ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStrea
     if (L->bc_total[2] > 0)
         k_physbc<2><<<grid_for(L->bc_total[2], 256, sms), 256, 0, st>>>(
             L->d_bc[2], L->d_bc_start[2], L->nbc[2], L->bc_total[2], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
-    return check_launch("level ghost fill");
+    return check_launch("level physical BC");
 }
 
-static ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st) {
+ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st) {
+    ocfd_status s = fill_exchange(L, U, st);
+    if (s != OCFD_OK) return s;
+    return fill_physbc(L, U, tfrac, st);
+}
+
+ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st) {
     const int sms = L->ctx->num_sms;
     k_reset_cfl<<<1, 1, 0, st>>>(L->d_step);
     k_estdt<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(
@@ -412,32 +304,103 @@ static ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st) {
     return check_launch("level estdt");
 }
 
-static ocfd_status record_step(ocfd_level* L, unsigned flags, cudaStream_t st) {
+ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st) {
     const bool visc = flags & OCFD_VISC;
+    RegBoxArgs dummy{};
+    return (flags & OCFD_FLUX_FP32)
+               ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[s], L->d_tile_start,
+                                        (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st)
+               : launch_rhs_regular(L->tile, visc, L->d_stage[s], L->d_tile_start,
+                                    (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st);
+}
+
+static ocfd_status record_step(ocfd_level* L, unsigned flags, cudaStream_t st) {
     k_step_begin<<<1, 1, 0, st>>>(L->d_step);
     const double tfrac[3] = {0.0, 1.0, 0.5};
     const int src[3] = {0, 1, 2};
     for (int s = 0; s < 3; ++s) {
         ocfd_status r = fill_ghosts(L, L->buf[src[s]], tfrac[s], st);
         if (r != OCFD_OK) return r;
-        RegBoxArgs dummy{};
-        r = (flags & OCFD_FLUX_FP32)
-                ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[s], L->d_tile_start,
-                                         (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st)
-                : launch_rhs_regular(L->tile, visc, L->d_stage[s], L->d_tile_start,
-                                     (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st);
+        r = launch_stage(L, s, flags, st);
         if (r != OCFD_OK) return r;
     }
     k_step_end<<<1, 1, 0, st>>>(L->d_step);
     return check_launch("level step");
 }
 
-}  // namespace ocfd
+static ocfd_array4 fab_array(const ocfd_level* L, int b, int i) {
+    const FabGeom& f = L->fabs[b];
+    ocfd_array4 a{};
+    a.p = L->buf[i] + f.off;
+    a.jstride = f.g[0];
+    a.kstride = (long long)f.g[0] * f.g[1];
+    a.nstride = f.ns;
+    for (int d = 0; d < 3; ++d) {
+        a.begin[d] = f.lo[d] - NGR;
+        a.end[d] = f.hi[d] + NGR + 1;
+    }
+    a.ncomp = L->ncomp;
+    return a;
+}
 
-extern "C" {
+// Stage tables: stage 1 A -> B, stage 2 (A, B) -> C, stage 3 (A, C) -> A (or D)
+ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
+    const ocfd_level_desc* desc = &L->desc;
+    const double dxinv[3] = {1.0 / desc->dx[0], 1.0 / desc->dx[1], 1.0 / desc->dx[2]};
+    std::vector<int> tile_start;
+    int nt = 0;
+    std::vector<RegBoxArgs> st[3];
+    const int S_of[3] = {0, 1, 2}, O_of[3] = {1, 2, roles.out3};
+    const double ra[3] = {0.0, 0.75, 1.0 / 3.0}, rb[3] = {1.0, 0.25, 2.0 / 3.0};
+    // stage weights of the SSP-RK3 update U^{n+1} = U^n + dt (L0 + L1 + 4 L2) / 6
+    const double wflux[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
+    for (size_t b = 0; b < L->boxes.size(); ++b) {
+        ocfd_array4 a[4];
+        for (int i = 0; i < L->nbuf; ++i) a[i] = fab_array(L, (int)b, i);
+        for (int k = 0; k < 3; ++k) {
+            RegBoxArgs r{};
+            fill_regular_args(r, &a[S_of[k]], nullptr, nullptr, L->boxes[b], dxinv, L->tile);
+            r.mode = RHS_FUSED_STAGE;
+            r.U0 = view_of<const double>(&a[0]);
+            r.Uout = view_of<double>(&a[O_of[k]]);
+            r.rk_a = ra[k];
+            r.rk_b = rb[k];
+            r.dt_ptr = &L->d_step->dt;
+            r.cfl_min = (k == 2 && roles.cfl) ? &L->d_step->cfl_min : nullptr;
+            for (int d = 0; d < 3; ++d) r.dx[d] = desc->dx[d];
+            if (!roles.flux_bits.empty() && roles.flux_bits[b]) {
+                r.has_flux = roles.flux_bits[b];
+                r.flux_w = wflux[k];
+                if (r.has_flux & FLUX_ACC_ALL)
+                    for (int d = 0; d < 3; ++d) r.flux[d] = roles.creg[3 * b + d];
+                if (r.has_flux & FLUX_ACC_PLANES)
+                    for (int d = 0; d < 3; ++d)
+                        for (int sd = 0; sd < 2; ++sd) r.fplane[d][sd] = roles.fplane[6 * b + 2 * d + sd];
+            }
+            st[k].push_back(r);
+            if (k == 0) {
+                tile_start.push_back(nt);
+                nt += r.ntile[0] * r.ntile[1] * r.ntile[2];
+            }
+        }
+    }
+    L->ntiles = nt;
+    ocfd_status s = OCFD_OK;
+    for (int k = 0; k < 3 && s == OCFD_OK; ++k) {
+        cudaFree(L->d_stage[k]);
+        L->d_stage[k] = nullptr;
+        s = upload(&L->d_stage[k], st[k]);
+    }
+    cudaFree(L->d_tile_start);
+    L->d_tile_start = nullptr;
+    if (s == OCFD_OK) s = upload(&L->d_tile_start, tile_start);
+    return s;
+}
 
-ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, ocfd_level** out) {
-    if (!ctx || !desc || !out || desc->nbox <= 0 || !desc->boxes)
+// Everything of a level but its stage tables: FABs, state buffers, exchange and
+// physical-BC tags, RHS tile choice, step state.
+ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out) {
+    if (!ctx || !desc || !out || desc->nbox <= 0 || !desc->boxes || nbuf < 3 || nbuf > 4)
         return fail(OCFD_BAD_ARG, "ocfd_level_create: bad arguments");
     *out = nullptr;
     for (int d = 0; d < 3; ++d) {
@@ -450,6 +413,7 @@ ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, oc
     ocfd_level* L = new ocfd_level();
     L->ctx = ctx;
     L->desc = *desc;
+    L->nbuf = nbuf;
     L->boxes.assign(desc->boxes, desc->boxes + desc->nbox);
     L->desc.boxes = nullptr;
     long long off = 0;
@@ -473,7 +437,7 @@ ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, oc
         L->fabs.push_back(f);
     }
     L->elems = off;
-    for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < nbuf; ++i) {
         if (cudaMalloc(&L->buf[i], sizeof(double) * L->elems) != cudaSuccess) {
             cudaGetLastError();
             ocfd_level_destroy(L);
@@ -520,55 +484,33 @@ ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, oc
             if (cost < best * 0.999) { best = cost; L->tile = t; }
         }
     }
-    // stage tables: stage 1 A -> B, stage 2 (A, B) -> C, stage 3 (A, C) -> A
-    const double dxinv[3] = {1.0 / desc->dx[0], 1.0 / desc->dx[1], 1.0 / desc->dx[2]};
-    std::vector<int> tile_start;
-    int nt = 0;
-    std::vector<RegBoxArgs> st[3];
-    if (s == OCFD_OK && cudaMalloc(&L->d_step, sizeof(StepState)) != cudaSuccess) s = fail(OCFD_OUT_OF_MEMORY, "step state");
-    for (size_t b = 0; b < L->boxes.size() && s == OCFD_OK; ++b) {
-        const FabGeom& f = L->fabs[b];
-        ocfd_array4 a[3];
-        for (int i = 0; i < 3; ++i) {
-            a[i].p = L->buf[i] + f.off;
-            a[i].jstride = f.g[0];
-            a[i].kstride = (long long)f.g[0] * f.g[1];
-            a[i].nstride = f.ns;
-            for (int d = 0; d < 3; ++d) {
-                a[i].begin[d] = f.lo[d] - NGR;
-                a[i].end[d] = f.hi[d] + NGR + 1;
-            }
-            a[i].ncomp = L->ncomp;
-        }
-        const int S_of[3] = {0, 1, 2}, O_of[3] = {1, 2, 0};
-        const double ra[3] = {0.0, 0.75, 1.0 / 3.0}, rb[3] = {1.0, 0.25, 2.0 / 3.0};
-        for (int k = 0; k < 3; ++k) {
-            RegBoxArgs r{};
-            fill_regular_args(r, &a[S_of[k]], nullptr, nullptr, L->boxes[b], dxinv, L->tile);
-            r.mode = RHS_FUSED_STAGE;
-            r.U0 = view_of<const double>(&a[0]);
-            r.Uout = view_of<double>(&a[O_of[k]]);
-            r.rk_a = ra[k];
-            r.rk_b = rb[k];
-            r.dt_ptr = &L->d_step->dt;
-            r.cfl_min = k == 2 ? &L->d_step->cfl_min : nullptr;
-            for (int d = 0; d < 3; ++d) r.dx[d] = desc->dx[d];
-            st[k].push_back(r);
-            if (k == 0) {
-                tile_start.push_back(nt);
-                nt += r.ntile[0] * r.ntile[1] * r.ntile[2];
-            }
-        }
+    if (s == OCFD_OK && cudaMalloc(&L->d_step, sizeof(StepState)) != cudaSuccess) {
+        cudaGetLastError();
+        s = fail(OCFD_OUT_OF_MEMORY, "step state");
     }
-    L->ntiles = nt;
-    for (int k = 0; k < 3 && s == OCFD_OK; ++k) s = upload(&L->d_stage[k], st[k]);
-    if (s == OCFD_OK) s = upload(&L->d_tile_start, tile_start);
     if (s == OCFD_OK) {
         k_set_time<<<1, 1>>>(L->d_step, 0.0);
         k_set_stop<<<1, 1>>>(L->d_step, __builtin_huge_val());
         s = check_launch("ocfd_level_create");
-        if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = fail(OCFD_LAUNCH_FAIL, "level setup");
     }
+    if (s != OCFD_OK) {
+        ocfd_level_destroy(L);
+        return s;
+    }
+    *out = L;
+    return OCFD_OK;
+}
+
+}  // namespace ocfd
+
+extern "C" {
+
+ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, ocfd_level** out) {
+    ocfd_level* L = nullptr;
+    ocfd_status s = level_alloc(ctx, desc, 3, &L);
+    if (s != OCFD_OK) return s;
+    s = build_stage_tables(L, StageRoles{});
+    if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = fail(OCFD_LAUNCH_FAIL, "level setup");
     if (s != OCFD_OK) {
         ocfd_level_destroy(L);
         return s;
@@ -580,8 +522,8 @@ ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, oc
 ocfd_status ocfd_level_destroy(ocfd_level* L) {
     if (!L) return OCFD_OK;
     if (L->graph) cudaGraphExecDestroy(L->graph);
+    for (int i = 0; i < 4; ++i) cudaFree(L->buf[i]);
     for (int i = 0; i < 3; ++i) {
-        cudaFree(L->buf[i]);
         cudaFree(L->d_stage[i]);
         cudaFree(L->d_bc[i]);
         cudaFree(L->d_bc_start[i]);
@@ -717,15 +659,7 @@ int ocfd_level_launches_per_step(const ocfd_level* L, unsigned flags) {
 ocfd_status ocfd_level_profile_stage(ocfd_level* L, unsigned flags, int reps, double* ms, void* stream) {
     if (!L || reps <= 0 || !ms) return fail(OCFD_BAD_ARG, "ocfd_level_profile_stage");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const bool visc = flags & OCFD_VISC;
-    RegBoxArgs dummy{};
-    auto launch = [&]() {
-        return (flags & OCFD_FLUX_FP32)
-                   ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[1], L->d_tile_start,
-                                            (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st)
-                   : launch_rhs_regular(L->tile, visc, L->d_stage[1], L->d_tile_start,
-                                        (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st);
-    };
+    auto launch = [&]() { return launch_stage(L, 1, flags, st); };
     ocfd_status s = launch();  // warm-up
     if (s != OCFD_OK) return s;
     cudaEvent_t e0, e1;

@@ -1,0 +1,165 @@
+// Level internals shared by the single-level driver (level.cu) and the AMR
+// hierarchy (amr.cu): FAB geometry, copy / boundary tags, the step state and
+// the level object itself.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ocfd_internal.h"
+#include "rhs_regular.h"
+
+namespace ocfd {
+
+constexpr int NGR = OCFD_NUM_GROW;
+
+struct FabGeom {
+    int lo[3], hi[3];  // valid box
+    long long off;     // element offset of the FAB in a state buffer
+    int g[3];          // grown extents
+    long long ns;      // component stride
+};
+
+struct ExTag {
+    int dst, src;
+    int lo[3], hi[3];  // region, absolute cell indices of the destination
+    int shift[3];      // src cell = dst cell + shift
+};
+
+struct BcTag {
+    int box, side;
+    int lo[3], hi[3];
+};
+
+struct StepState {
+    double time, dt, dt_prev, cfl;
+    unsigned long long cfl_min;
+    double stop_time;  // the last step is shortened to land on it (Source/EBR.cpp:279-286)
+};
+
+struct BcInfo {
+    int lo_bc[3], hi_bc[3];
+    int dom_lo[3], dom_hi[3];
+    double dx[3], prob_lo[3];
+    int bc_case;
+    double params[16];
+};
+
+__device__ __forceinline__ long long fab_index(const FabGeom& f, int i, int j, int k) {
+    return f.off + (long long)(i - f.lo[0] + NGR) + (long long)(j - f.lo[1] + NGR) * f.g[0] +
+           (long long)(k - f.lo[2] + NGR) * f.g[0] * f.g[1];
+}
+
+template <class Tag>
+__device__ __forceinline__ int find_tag(const long long* start, int ntag, long long idx) {
+    int lo = 0, hi = ntag - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= idx) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void region_cell(const int* lo, const int* hi, long long local, int& i,
+                                            int& j, int& k) {
+    const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
+    i = lo[0] + (int)(local % nx);
+    j = lo[1] + (int)((local / nx) % ny);
+    k = lo[2] + (int)(local / (nx * ny));
+}
+
+// ---- host helpers (level.cu)
+template <class T>
+ocfd_status upload(T** dptr, const std::vector<T>& v) {
+    size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
+    if (cudaMalloc(dptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(OCFD_OUT_OF_MEMORY, "level table allocation");
+    }
+    if (!v.empty() && cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(OCFD_LAUNCH_FAIL, "level table upload");
+    return OCFD_OK;
+}
+
+bool intersect(const int* alo, const int* ahi, const int* blo, const int* bhi, int* lo, int* hi);
+long long region_cells(const int* lo, const int* hi);
+int grid_for(long long total, int threads, int sms);
+
+template <class Tag>
+ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** d_start, long long* total) {
+    std::vector<long long> start(tags.size());
+    long long acc = 0;
+    for (size_t i = 0; i < tags.size(); ++i) {
+        start[i] = acc;
+        acc += region_cells(tags[i].lo, tags[i].hi);
+    }
+    *total = acc;
+    ocfd_status s = upload(d_tags, tags);
+    if (s != OCFD_OK) return s;
+    return upload(d_start, start);
+}
+
+}  // namespace ocfd
+
+struct ocfd_level {
+    ocfd_context* ctx = nullptr;
+    ocfd_level_desc desc{};
+    std::vector<ocfd_box> boxes;
+    std::vector<ocfd::FabGeom> fabs;
+    long long elems = 0;      // per state buffer
+    int ncomp = 5;
+    // A (U^n), B, C: RK3 stage states; D: end-of-step state of a level that has
+    // a finer level (U^n stays in A while the finer level interpolates in time)
+    int nbuf = 3;
+    double* buf[4] = {nullptr, nullptr, nullptr, nullptr};
+    ocfd::FabGeom* d_fabs = nullptr;
+    long long* d_cell_start = nullptr;
+    long long ncells = 0;
+    // exchange
+    ocfd::ExTag* d_ex = nullptr;
+    long long* d_ex_start = nullptr;
+    int nex = 0;
+    long long ex_total = 0;
+    // physical BC passes
+    ocfd::BcTag* d_bc[3] = {nullptr, nullptr, nullptr};
+    long long* d_bc_start[3] = {nullptr, nullptr, nullptr};
+    int nbc[3] = {0, 0, 0};
+    long long bc_total[3] = {0, 0, 0};
+    ocfd::BcInfo bcinfo{};
+    // RHS stage tables (3 stages)
+    int tile = 0;
+    ocfd::RegBoxArgs* d_stage[3] = {nullptr, nullptr, nullptr};
+    int* d_tile_start = nullptr;
+    int ntiles = 0;
+    ocfd::StepState* d_step = nullptr;
+    bool need_estdt = true;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    unsigned graph_flags = ~0u;
+    double graph_cfl = -1;
+};
+
+namespace ocfd {
+
+// Per-stage roles of a level inside an AMR hierarchy (defaults: single level).
+struct StageRoles {
+    int out3 = 0;              // buffer stage 3 writes: 0 (in place over U^n) or 3
+    bool cfl = true;           // fused CFL bound in stage 3
+    // per box: flux-register accumulation flags and views (empty: none)
+    std::vector<int> flux_bits;
+    std::vector<View<double>> creg;   // 3 per box (FLUX_ACC_ALL)
+    std::vector<View<double>> fplane; // 6 per box (FLUX_ACC_PLANES), [d][side]
+};
+
+ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles);
+ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st);
+ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st);
+ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st);
+ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st);
+ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st);
+ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out);
+__global__ void k_set_time(StepState* st, double t);
+
+}  // namespace ocfd

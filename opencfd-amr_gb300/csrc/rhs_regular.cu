@@ -49,7 +49,8 @@ void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* d
                        int tile) {
     a.S = view_of<const double>(S);
     if (dSdt) a.dsdt = view_of<double>(dSdt);
-    a.has_flux = flux != nullptr;
+    a.has_flux = flux != nullptr ? FLUX_WRITE : 0;
+    a.flux_w = 0.0;
     for (int d = 0; d < 3; ++d) {
         if (flux) a.flux[d] = view_of<double>(&flux[d]);
         a.lo[d] = bx.lo[d];

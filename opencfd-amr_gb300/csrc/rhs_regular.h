@@ -9,6 +9,7 @@
 namespace ocfd {
 
 enum RhsMode { RHS_WRITE_DSDT = 0, RHS_FUSED_STAGE = 1 };
+enum FluxBits { FLUX_WRITE = 1, FLUX_ACC_ALL = 2, FLUX_ACC_PLANES = 4 };
 
 struct TileShape {
     int x, y, z;
@@ -21,7 +22,15 @@ struct RegBoxArgs {
     View<const double> S;      // state with ghosts (stage input U_s)
     View<double> dsdt;         // RHS_WRITE_DSDT: output over the box
     View<double> flux[3];      // optional face-flux output
+    // face-flux output, bit flags:
+    //   FLUX_WRITE       flux[d] = F on every face of the box (per-box entry points)
+    //   FLUX_ACC_ALL     flux[d] += flux_w * dt * F on every face (coarse side of a
+    //                    flux register: time-weighted stage fluxes summed over RK3)
+    //   FLUX_ACC_PLANES  fplane[d][side] += flux_w * dt * F on the box's own lo / hi
+    //                    faces in d (fine side of a flux register)
     int has_flux;
+    double flux_w;
+    View<double> fplane[3][2];
     int lo[3], hi[3];
     double dxinv[3];
     int ntile[3];

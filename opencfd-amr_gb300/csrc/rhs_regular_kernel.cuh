@@ -316,6 +316,8 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
     }
     if (B.has_flux) {
         const View<double>& out = B.flux[D];
+        const int fl = B.has_flux;
+        const double wdt = (fl & (FLUX_ACC_ALL | FLUX_ACC_PLANES)) ? B.flux_w * (B.dt_ptr ? *B.dt_ptr : B.dt) : 0.0;
         for (int f = tid; f < PC::NF; f += NT) {
             const int fx = f % PC::FX, fy = (f / PC::FX) % PC::FY, fz = f / (PC::FX * PC::FY);
             const int fc[3] = {fx, fy, fz};
@@ -331,8 +333,18 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
                 if (t == D) ok = ok && (fc[t] < tdim || g[t] == B.hi[t] + 1);
             }
             if (ok) {
+                if (fl & FLUX_WRITE) {
 #pragma unroll
-                for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) = widen<FT>(FF[n * PC::NF + f]);
+                    for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) = widen<FT>(FF[n * PC::NF + f]);
+                } else if (fl & FLUX_ACC_ALL) {
+#pragma unroll
+                    for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) += wdt * widen<FT>(FF[n * PC::NF + f]);
+                }
+                if ((fl & FLUX_ACC_PLANES) && (g[D] == B.lo[D] || g[D] == B.hi[D] + 1)) {
+                    const View<double>& pl = B.fplane[D][g[D] == B.lo[D] ? 0 : 1];
+#pragma unroll
+                    for (int n = 0; n < 5; ++n) pl(gi, gj, gk, n) += wdt * widen<FT>(FF[n * PC::NF + f]);
+                }
             }
         }
     }

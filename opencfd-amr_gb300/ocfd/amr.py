@@ -1,0 +1,202 @@
+"""AMR hierarchy binding (ocfd_amr_* in include/ocfd/ocfd.h): levels of ratio
+2 advanced with subcycling, coarse-fine interpolation, reflux, average-down and
+density-gradient regridding on the device."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._abi import Box, check, declare, load
+from .context import _stream_ptr
+from .level import NG, Level
+
+MAX_LEVELS = 6
+
+
+class AmrDesc(ctypes.Structure):
+    _fields_ = [("nbox0", ctypes.c_int32), ("boxes0", ctypes.POINTER(Box)), ("domain", Box),
+                ("lo_bc", ctypes.c_int32 * 3), ("hi_bc", ctypes.c_int32 * 3),
+                ("dx", ctypes.c_double * 3), ("prob_lo", ctypes.c_double * 3),
+                ("bc_case", ctypes.c_int32), ("case_params", ctypes.c_double * 16),
+                ("max_level", ctypes.c_int32), ("blocking_factor", ctypes.c_int32 * 3),
+                ("max_grid_size", ctypes.c_int32 * 3), ("n_error_buf", ctypes.c_int32),
+                ("regrid_int", ctypes.c_int32), ("refine_dengrad", ctypes.c_double)]
+
+
+_vp = ctypes.c_void_p
+declare("ocfd_amr_create", ctypes.c_int, [_vp, ctypes.POINTER(AmrDesc), ctypes.POINTER(_vp)])
+declare("ocfd_amr_destroy", ctypes.c_int, [_vp])
+declare("ocfd_amr_nlevels", ctypes.c_int, [_vp])
+declare("ocfd_amr_level", _vp, [_vp, ctypes.c_int])
+declare("ocfd_amr_get_grids", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Box), ctypes.c_int])
+declare("ocfd_amr_regrid", ctypes.c_int, [_vp, ctypes.c_int, _vp])
+declare("ocfd_amr_set_grids", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int32),
+                                             ctypes.POINTER(Box), _vp])
+declare("ocfd_amr_average_down", ctypes.c_int, [_vp, _vp])
+declare("ocfd_amr_fill_ghosts", ctypes.c_int, [_vp, _vp])
+declare("ocfd_amr_advance", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _vp])
+declare("ocfd_amr_time", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _vp])
+declare("ocfd_amr_set_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
+declare("ocfd_amr_set_stop_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
+declare("ocfd_amr_cell_steps", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)])
+declare("ocfd_amr_launches_per_step", ctypes.c_int, [_vp])
+
+
+def _boxes_array(boxes):
+    bx = (Box * max(1, len(boxes)))()
+    for i, (lo, hi) in enumerate(boxes):
+        bx[i].lo[:] = list(lo)
+        bx[i].hi[:] = list(hi)
+    return bx
+
+
+class Hierarchy:
+    """A refined hierarchy over the level-0 `boxes0` of the domain 0..n0-1."""
+
+    def __init__(self, ctx, boxes0, n0, lo_bc, hi_bc, dx, prob_lo=(0.0, 0.0, 0.0), bc_case=0,
+                 case_params=(), max_level=2, blocking_factor=(32, 32, 32), max_grid_size=(128, 128, 128),
+                 n_error_buf=1, regrid_int=2, refine_dengrad=0.05):
+        self.ctx = ctx
+        self.lib = load()
+        self.n0 = tuple(n0)
+        self.dx0 = tuple(dx)
+        d = AmrDesc()
+        bx = _boxes_array(boxes0)
+        d.nbox0 = len(boxes0)
+        d.boxes0 = bx
+        d.domain.lo[:] = [0, 0, 0]
+        d.domain.hi[:] = [n - 1 for n in n0]
+        d.lo_bc[:] = list(lo_bc)
+        d.hi_bc[:] = list(hi_bc)
+        d.dx[:] = list(dx)
+        d.prob_lo[:] = list(prob_lo)
+        d.bc_case = bc_case
+        for i, v in enumerate(case_params):
+            d.case_params[i] = v
+        d.max_level = max_level
+        d.blocking_factor[:] = list(blocking_factor)
+        d.max_grid_size[:] = list(max_grid_size)
+        d.n_error_buf = n_error_buf
+        d.regrid_int = regrid_int
+        d.refine_dengrad = refine_dengrad
+        self.desc = d
+        h = ctypes.c_void_p()
+        check(self.lib.ocfd_amr_create(ctx.h, ctypes.byref(d), ctypes.byref(h)), "ocfd_amr_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.ocfd_amr_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- structure --------------------------------------------------------
+    def nlevels(self):
+        return int(self.lib.ocfd_amr_nlevels(self.h))
+
+    def domain(self, lev):
+        return (0, 0, 0), tuple((n << lev) - 1 for n in self.n0)
+
+    def dx(self, lev):
+        return tuple(x / (1 << lev) for x in self.dx0)
+
+    def grids(self, lev):
+        n = self.lib.ocfd_amr_get_grids(self.h, lev, None, 0)
+        if n < 0:
+            raise IndexError(lev)
+        bx = (Box * max(1, n))()
+        self.lib.ocfd_amr_get_grids(self.h, lev, bx, n)
+        return [(tuple(bx[i].lo), tuple(bx[i].hi)) for i in range(n)]
+
+    def all_grids(self):
+        return [self.grids(l) for l in range(self.nlevels())]
+
+    def level(self, lev):
+        h = self.lib.ocfd_amr_level(self.h, lev)
+        if not h:
+            raise IndexError(lev)
+        lo, hi = self.domain(lev)
+        return Level.wrap(self.ctx, h, self.grids(lev), lo, hi)
+
+    # ---- regridding ---------------------------------------------------------
+    def regrid(self, lbase=0, stream=None):
+        check(self.lib.ocfd_amr_regrid(self.h, lbase, _stream_ptr(stream)), "ocfd_amr_regrid")
+
+    def set_grids(self, grids, stream=None):
+        """grids: box lists of levels 1.. (level 0 is fixed)."""
+        nlev = 1 + len(grids)
+        nbox = (ctypes.c_int32 * nlev)(*([0] + [len(g) for g in grids]))
+        flat = [b for g in grids for b in g]
+        bx = _boxes_array(flat)
+        check(self.lib.ocfd_amr_set_grids(self.h, nlev, nbox, bx, _stream_ptr(stream)), "ocfd_amr_set_grids")
+
+    def build(self, fab_of_box, stream=None):
+        """Hierarchy at t = 0 (AMReX bldFineLevels): level 0 from the initial
+        condition, then per level: tag, make the next level, set its initial
+        condition; finally average down.  fab_of_box(lev, lo, hi, dx) returns the
+        grown FAB of a box."""
+        L0 = self.level(0)
+        L0.copy_in(L0.pack_fabs(lambda lo, hi: fab_of_box(0, lo, hi, self.dx(0))), stream)
+        for lev in range(self.desc.max_level):
+            if self.nlevels() != lev + 1:
+                break
+            self.regrid(lev, stream)
+            if self.nlevels() == lev + 2:
+                L = self.level(lev + 1)
+                L.copy_in(L.pack_fabs(lambda lo, hi, l=lev + 1: fab_of_box(l, lo, hi, self.dx(l))), stream)
+        self.average_down(stream)
+        self.set_time(0.0, stream)
+
+    # ---- stepping -------------------------------------------------------------
+    def average_down(self, stream=None):
+        check(self.lib.ocfd_amr_average_down(self.h, _stream_ptr(stream)), "average_down")
+
+    def fill_ghosts(self, stream=None):
+        check(self.lib.ocfd_amr_fill_ghosts(self.h, _stream_ptr(stream)), "fill_ghosts")
+
+    def advance(self, nsteps, cfl, flags=0, stream=None):
+        check(self.lib.ocfd_amr_advance(self.h, nsteps, cfl, flags, _stream_ptr(stream)), "ocfd_amr_advance")
+
+    def time(self, stream=None):
+        t = ctypes.c_double()
+        dt = ctypes.c_double()
+        check(self.lib.ocfd_amr_time(self.h, ctypes.byref(t), ctypes.byref(dt), _stream_ptr(stream)), "time")
+        return t.value, dt.value
+
+    def set_time(self, t, stream=None):
+        check(self.lib.ocfd_amr_set_time(self.h, t, _stream_ptr(stream)), "set_time")
+
+    def set_stop_time(self, t, stream=None):
+        check(self.lib.ocfd_amr_set_stop_time(self.h, t, _stream_ptr(stream)), "set_stop_time")
+
+    def cell_steps(self):
+        a = ctypes.c_int64()
+        b = ctypes.c_int64()
+        check(self.lib.ocfd_amr_cell_steps(self.h, ctypes.byref(a), ctypes.byref(b)), "cell_steps")
+        return a.value, b.value
+
+    def launches_per_step(self):
+        return int(self.lib.ocfd_amr_launches_per_step(self.h))
+
+    # ---- data -----------------------------------------------------------------
+    def level_global(self, lev, stream=None):
+        """(valid data (5, Nz, Ny, Nx) of the whole level domain, mask of valid cells)"""
+        L = self.level(lev)
+        lo, hi = self.domain(lev)
+        n = [hi[d] + 1 for d in range(3)]
+        out = np.full((5, n[2], n[1], n[0]), np.nan)
+        L.unpack_valid(L.copy_out(stream=stream), out)
+        mask = np.zeros((n[2], n[1], n[0]), bool)
+        for blo, bhi in L.boxes:
+            mask[blo[2]:bhi[2] + 1, blo[1]:bhi[1] + 1, blo[0]:bhi[0] + 1] = True
+        return out, mask
+
+    def state(self, stream=None):
+        """Snapshot of every level's state FABs (host), for restore()."""
+        return [self.level(l).copy_out(stream=stream) for l in range(self.nlevels())]

@@ -71,3 +71,32 @@ def blast3d(nx=256, ny=256, nz=64, gamma=GAMMA):
     G[4] = np.where(inside, 1.0, 0.1) / (gamma - 1.0)
     return dict(G=G, n=n, dx=(dx, dx, dx), prob_lo=(0.0, 0.0, 0.0),
                 lo_bc=(0, 0, 0), hi_bc=(0, 0, 0), bc_case=0, case_params=())
+
+
+def dmr_fab(lo, hi, dx, gamma=GAMMA):
+    """Grown FAB (5, nz+8, ny+8, nx+8) of the DMR initial condition over the box
+    lo..hi at cell size dx (Exec/1_DMR/prob.H:11-46)."""
+    x = (np.arange(lo[0] - NG, hi[0] + NG + 1) + 0.5) * dx[0]
+    y = (np.arange(lo[1] - NG, hi[1] + NG + 1) + 0.5) * dx[1]
+    nz = hi[2] - lo[2] + 1 + 2 * NG
+    left, right = dmr_states(gamma)
+    X, Y = np.meshgrid(x, y, indexing="xy")
+    post = X < 1.0 / 6.0 + math.sqrt(1 / 3.0) * Y
+    F = np.empty((5, nz, len(y), len(x)))
+    for c in range(5):
+        F[c] = np.where(post, left[c], right[c])[None]
+    return F
+
+
+def dmr_amr(nx=1024, ny=256, nz=2, max_level=2, blocking_factor=32, max_grid=128, n_error_buf=1,
+            refine_dengrad=0.05, regrid_int=2, gamma=GAMMA, Lx=4.0):
+    """Double Mach reflection with refinement: base nx x ny x nz, ratio 2,
+    |d rho| >= refine_dengrad tagging (Exec/1_DMR/inputs:48-49), blocking factor
+    and max grid size in cells of each level (z blocks span the thin slab)."""
+    dx = Lx / nx
+    left, right = dmr_states(gamma)
+    return dict(n=(nx, ny, nz), dx=(dx, dx, dx), prob_lo=(0.0, 0.0, 0.0), lo_bc=(1, 4, 2), hi_bc=(2, 1, 2),
+                bc_case=1, case_params=tuple(left) + tuple(right), max_level=max_level,
+                blocking_factor=(blocking_factor,) * 3, max_grid_size=(max_grid,) * 3,
+                n_error_buf=n_error_buf, refine_dengrad=refine_dengrad, regrid_int=regrid_int,
+                fab=lambda lev, lo, hi, d: dmr_fab(lo, hi, d, gamma))

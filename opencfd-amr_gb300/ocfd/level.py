@@ -88,10 +88,25 @@ class Level:
         self.domain_lo = tuple(domain_lo)
         self.domain_hi = tuple(domain_hi)
 
+    @classmethod
+    def wrap(cls, ctx, handle, boxes, domain_lo, domain_hi, ncomp=5):
+        """A view of a level owned elsewhere (an AMR hierarchy); never destroyed here."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.lib = load()
+        self.boxes = [(tuple(lo), tuple(hi)) for lo, hi in boxes]
+        self.ncomp = ncomp
+        self.h = ctypes.c_void_p(handle)
+        self.owned = False
+        self.elems = self.lib.ocfd_level_state_elems(self.h)
+        self.domain_lo = tuple(domain_lo)
+        self.domain_hi = tuple(domain_hi)
+        return self
+
     def close(self):
-        if self.h:
+        if self.h and getattr(self, "owned", True):
             self.lib.ocfd_level_destroy(self.h)
-            self.h = ctypes.c_void_p()
+        self.h = ctypes.c_void_p()
 
     def __del__(self):
         try:
@@ -152,6 +167,12 @@ class Level:
 
     def set_global(self, G, stream=None):
         self.copy_in(self.pack(G), stream)
+
+    def pack_fabs(self, fab_of_box):
+        """Concatenate fab_of_box(lo, hi) over the boxes: each returns the grown
+        FAB (ncomp, nz+8, ny+8, nx+8) of the valid box lo..hi."""
+        return np.concatenate([np.ascontiguousarray(fab_of_box(lo, hi), dtype=np.float64).ravel()
+                               for lo, hi in self.boxes])
 
     def get_global(self, stream=None):
         n = [self.domain_hi[d] - self.domain_lo[d] + 1 for d in range(3)]
