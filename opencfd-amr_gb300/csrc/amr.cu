@@ -40,6 +40,9 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -447,18 +450,18 @@ struct DevTags {
     long long* start = nullptr;
     int n = 0;
     long long total = 0;
-    void release() {
-        cudaFree(d);
-        cudaFree(start);
+    void release(DevPool* pool) {
+        dev_free(d, pool);
+        dev_free(start, pool);
         d = nullptr;
         start = nullptr;
         n = 0;
         total = 0;
     }
-    ocfd_status set(const std::vector<Tag>& v) {
-        release();
+    ocfd_status set(const std::vector<Tag>& v, DevPool* pool) {
+        release(pool);
         n = (int)v.size();
-        return upload_tags(v, &d, &start, &total);
+        return upload_tags(v, &d, &start, &total, pool);
     }
 };
 
@@ -480,13 +483,13 @@ struct AmrLev {
     long long leaf = 0;
     unsigned char* d_blk = nullptr;  // tag blocks of lev + 1
     long long nblk_cap = 0;
-    void release_tables() {
-        cf.release();
-        avg.release();
-        cudaFree(d_rc);
-        cudaFree(d_rf);
-        cudaFree(freg);
-        cudaFree(creg);
+    void release_tables(DevPool* pool) {
+        cf.release(pool);
+        avg.release(pool);
+        dev_free(d_rc, pool);
+        dev_free(d_rf, pool);
+        dev_free(freg, pool);
+        dev_free(creg, pool);
         d_rc = nullptr;
         d_rf = nullptr;
         nrc = 0;
@@ -498,6 +501,7 @@ struct AmrLev {
 }  // namespace ocfd
 
 struct ocfd_amr {
+    ocfd::DevPool pool;   // destroyed last: every level and table returns its blocks here
     ocfd_context* ctx = nullptr;
     ocfd_amr_desc desc{};
     std::vector<ocfd_box> boxes0;
@@ -515,6 +519,19 @@ struct ocfd_amr {
 namespace ocfd {
 
 static const int kNest = 2;  // proper nesting: coarse cells around a fine box's coarsening
+
+// host-side phase timing of regridding, printed to stderr when OCFD_AMR_PROFILE is set
+struct PhaseTimer {
+    bool on = std::getenv("OCFD_AMR_PROFILE") != nullptr;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void mark(const char* what, cudaStream_t st) {
+        if (!on) return;
+        cudaStreamSynchronize(st);
+        const auto n = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[amr] %-28s %8.3f ms\n", what, std::chrono::duration<double, std::milli>(n - t).count());
+        t = n;
+    }
+};
 
 static IBox level_domain(const ocfd_amr* H, int l) {
     IBox d = ib_of(H->desc.domain);
@@ -539,11 +556,8 @@ static AmrStates states(const ocfd_amr* H) {
 
 static ocfd_status ensure_d(ocfd_level* L) {
     if (L->nbuf >= 4) return OCFD_OK;
-    if (cudaMalloc(&L->buf[3], sizeof(double) * L->elems) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(OCFD_OUT_OF_MEMORY, "AMR: fourth state buffer");
-    }
-    cudaMemset(L->buf[3], 0, sizeof(double) * L->elems);
+    L->buf[3] = static_cast<double*>(dev_alloc(sizeof(double) * L->elems, L->pool));
+    if (!L->buf[3]) return fail(OCFD_OUT_OF_MEMORY, "AMR: fourth state buffer");
     L->nbuf = 4;
     return OCFD_OK;
 }
@@ -564,7 +578,7 @@ static ocfd_status make_level(ocfd_amr* H, int l, const std::vector<IBox>& boxes
     d.bc_case = H->desc.bc_case;
     std::memcpy(d.case_params, H->desc.case_params, sizeof(d.case_params));
     d.tile = -1;
-    return level_alloc(H->ctx, &d, nbuf, out);
+    return level_alloc(H->ctx, &d, nbuf, out, &H->pool);
 }
 
 // periodic images (shift vectors) of a region that meet the domain
@@ -662,15 +676,17 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     AmrLev& C = H->lev[f - 1];
     AmrLev& F = H->lev[f];
     ocfd_status s;
+    PhaseTimer pt;
     {
         std::vector<std::vector<IBox>> regions;
         ghost_regions(H, f, regions);
         std::vector<CfTag> tags;
         s = build_cf_tags(H, f, regions, tags);
         if (s != OCFD_OK) return s;
-        s = F.cf.set(tags);
+        s = F.cf.set(tags, &H->pool);
         if (s != OCFD_OK) return s;
     }
+    pt.mark("      ghost cf tags", 0);
     BoxIndex cidx;
     cidx.build(C.boxes, C.dom);
     std::vector<IBox> fcoarse;
@@ -691,10 +707,11 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
                 tags.push_back(t);
                 covered += ib_cells(I);
             }
-        s = F.avg.set(tags);
+        s = F.avg.set(tags, &H->pool);
         if (s != OCFD_OK) return s;
         C.leaf = C.L->ncells - covered;
     }
+    pt.mark("      avg tags", 0);
     // ---- flux register layout: fine planes of every fine box
     const int nfb = (int)F.boxes.size(), ncb = (int)C.boxes.size();
     std::vector<long long> plane_off((size_t)nfb * 6);
@@ -715,7 +732,12 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
         int cf[3];  // coarse face index
         int c[3];   // unwrapped coarse cell (transverse coordinates pick the fine faces)
     };
-    std::map<std::pair<int, long long>, std::vector<Face>> cells;
+    struct Keyed {
+        int cb;
+        long long u;  // coarse cell: box and element index
+        Face f;
+    };
+    std::vector<Keyed> faces_k;
     const IBox& cd = C.dom;
     for (int fb = 0; fb < nfb; ++fb) {
         const IBox& Fc = fcoarse[fb];
@@ -723,6 +745,7 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
             for (int sd = 0; sd < 2; ++sd) {
                 IBox pl = Fc;
                 pl.lo[d] = pl.hi[d] = (sd == 0) ? Fc.lo[d] - 1 : Fc.hi[d] + 1;
+                if (!H->periodic[d] && (pl.lo[d] < cd.lo[d] || pl.lo[d] > cd.hi[d])) continue;  // physical boundary
                 for (int k = pl.lo[2]; k <= pl.hi[2]; ++k)
                     for (int j = pl.lo[1]; j <= pl.hi[1]; ++j)
                         for (int i = pl.lo[0]; i <= pl.hi[0]; ++i) {
@@ -746,16 +769,20 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
                             fc.fb = fb;
                             for (int e = 0; e < 3; ++e) { fc.cf[e] = w[e]; fc.c[e] = c[e]; }
                             if (sd == 0) fc.cf[d] = w[d] + 1;
-                            const FabGeom& g = C.L->fabs[cb];
-                            cells[{cb, fab_index_h(g, w[0], w[1], w[2])}].push_back(fc);
+                            faces_k.push_back({cb, fab_index_h(C.L->fabs[cb], w[0], w[1], w[2]), fc});
                         }
             }
     }
+    pt.mark("      reflux scan", 0);
     // coarse register: face arrays of the coarse boxes that own a reflux cell
+    // group by coarse cell, faces of a cell in discovery order
+    std::stable_sort(faces_k.begin(), faces_k.end(), [](const Keyed& x, const Keyed& y) {
+        return x.cb != y.cb ? x.cb < y.cb : x.u < y.u;
+    });
     std::vector<long long> creg_off((size_t)ncb, -1);
     long long ce = 0;
-    for (const auto& kv : cells) {
-        const int cb = kv.first.first;
+    for (const Keyed& kf : faces_k) {
+        const int cb = kf.cb;
         if (creg_off[cb] >= 0) continue;
         creg_off[cb] = ce;
         const IBox& B = C.boxes[cb];
@@ -780,13 +807,16 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     };
     std::vector<RefluxCell> rc_h;
     std::vector<RefluxFace> rf_h;
-    for (const auto& kv : cells) {
+    for (size_t q0 = 0; q0 < faces_k.size();) {
+        size_t q1 = q0;
+        while (q1 < faces_k.size() && faces_k[q1].cb == faces_k[q0].cb && faces_k[q1].u == faces_k[q0].u) ++q1;
         RefluxCell cell{};
-        cell.u = kv.first.second;
-        cell.uns = C.L->fabs[kv.first.first].ns;
+        cell.u = faces_k[q0].u;
+        cell.uns = C.L->fabs[faces_k[q0].cb].ns;
         cell.first = (int)rf_h.size();
-        cell.count = (int)kv.second.size();
-        for (const Face& fc : kv.second) {
+        cell.count = (int)(q1 - q0);
+        for (size_t qi = q0; qi < q1; ++qi) {
+            const Face& fc = faces_k[qi].f;
             RefluxFace q{};
             q.d = fc.d;
             q.sgn = fc.side == 0 ? 1.0 : -1.0;
@@ -807,18 +837,19 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
             rf_h.push_back(q);
         }
         rc_h.push_back(cell);
+        q0 = q1;
     }
+    pt.mark("      reflux tables", 0);
     F.nrc = (int)rc_h.size();
-    s = upload(&F.d_rc, rc_h);
-    if (s == OCFD_OK) s = upload(&F.d_rf, rf_h);
+    s = upload(&F.d_rc, rc_h, &H->pool);
+    if (s == OCFD_OK) s = upload(&F.d_rf, rf_h, &H->pool);
     if (s != OCFD_OK) return s;
     F.freg_elems = fe;
     C.creg_elems = ce;
-    if (cudaMalloc(&F.freg, sizeof(double) * std::max<long long>(1, fe)) != cudaSuccess ||
-        cudaMalloc(&C.creg, sizeof(double) * std::max<long long>(1, ce)) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(OCFD_OUT_OF_MEMORY, "AMR: flux registers");
-    }
+    F.freg = static_cast<double*>(dev_alloc(sizeof(double) * std::max<long long>(1, fe), &H->pool));
+    C.creg = static_cast<double*>(dev_alloc(sizeof(double) * std::max<long long>(1, ce), &H->pool));
+    if (!F.freg || !C.creg) return fail(OCFD_OUT_OF_MEMORY, "AMR: flux registers");
+    pt.mark("      uploads", 0);
     // stage roles: register views
     rf.flux_bits.resize(nfb, 0);
     rf.fplane.resize((size_t)nfb * 6);
@@ -849,9 +880,11 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
 }
 
 static ocfd_status rebuild_tables(ocfd_amr* H) {
+    // blocks of the old tables go back to the pool: nothing may still read them
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("AMR table rebuild");
     std::vector<StageRoles> roles(H->nlev);
     for (int l = 0; l < H->nlev; ++l) {
-        H->lev[l].release_tables();
+        H->lev[l].release_tables(&H->pool);
         H->lev[l].leaf = H->lev[l].L->ncells;
         roles[l].cfl = false;
         roles[l].out3 = (l < H->nlev - 1) ? 3 : 0;
@@ -860,9 +893,11 @@ static ocfd_status rebuild_tables(ocfd_amr* H) {
             if (s != OCFD_OK) return s;
         }
     }
+    PhaseTimer pt;
     for (int f = 1; f < H->nlev; ++f) {
         ocfd_status s = build_pair(H, f, roles[f - 1], roles[f]);
         if (s != OCFD_OK) return s;
+        pt.mark("    pair tables", 0);
     }
     for (int l = 0; l < H->nlev; ++l) {
         StageRoles& r = roles[l];
@@ -875,6 +910,7 @@ static ocfd_status rebuild_tables(ocfd_amr* H) {
         ocfd_status s = build_stage_tables(H->lev[l].L, r);
         if (s != OCFD_OK) return s;
     }
+    pt.mark("    stage tables", 0);
     H->graph_ok = false;
     H->need_estdt = true;
     return OCFD_OK;
@@ -1151,14 +1187,14 @@ static ocfd_status launch_copy(ocfd_amr* H, ocfd_level* dst, const std::vector<I
         }
     if (tags.empty()) return OCFD_OK;
     DevTags<CopyTag> dt;
-    ocfd_status s = dt.set(tags);
+    ocfd_status s = dt.set(tags, &H->pool);
     if (s == OCFD_OK) {
         k_copy_tags<<<grid_for(dt.total, 256, H->ctx->num_sms), 256, 0, st>>>(
             dt.d, dt.start, dt.n, dt.total, dst->d_fabs, dst->buf[0], src->d_fabs, src->buf[0], dst->ncomp);
         s = check_launch("AMR regrid copy");
     }
     cudaStreamSynchronize(st);
-    dt.release();
+    dt.release(&H->pool);
     return s;
 }
 
@@ -1172,6 +1208,12 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
     }
     if (newfinest >= OCFD_AMR_MAX_LEVELS || newfinest > H->desc.max_level)
         return fail(OCFD_BAD_ARG, "AMR: more levels than max_level");
+    // unchanged hierarchy: tables and graph stay valid
+    bool changed = newfinest != H->nlev - 1;
+    for (int f = lbase + 1; f <= newfinest && !changed; ++f)
+        changed = !(f < H->nlev && same_boxes(grids[f - lbase - 1], H->lev[f].boxes));
+    if (!changed) return OCFD_OK;
+    PhaseTimer pt;
     const double a[4] = {1.0, 0.0, 0.0, 0.0};
     for (int f = lbase + 1; f <= newfinest; ++f) {
         const std::vector<IBox>& nb = grids[f - lbase - 1];
@@ -1180,26 +1222,35 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
         ocfd_level* NL = nullptr;
         ocfd_status s = make_level(H, f, nb, f < newfinest ? 4 : 3, &NL);
         if (s != OCFD_OK) return s;
+        pt.mark("  make level", st);
         AmrLev& A = H->lev[f];
         ocfd_level* old = exists ? A.L : nullptr;
         std::vector<IBox> oldboxes = exists ? A.boxes : std::vector<IBox>();
-        A.release_tables();
+        A.release_tables(&H->pool);
         A.L = NL;
         A.boxes = nb;
         A.dom = level_domain(H, f);
         for (int e = 0; e < 3; ++e) A.dx[e] = H->desc.dx[e] / (double)(1 << f);
         if (H->nlev < f + 1) H->nlev = f + 1;
         k_copy_step<<<1, 1, 0, st>>>(NL->d_step, H->lev[0].L->d_step);
-        // every valid cell from the level below, then the old level where it overlaps
+        // cells the old level did not cover from the level below, the rest copied
         {
             std::vector<std::vector<IBox>> regions(nb.size());
-            for (size_t b = 0; b < nb.size(); ++b) regions[b] = {nb[b]};
+            for (size_t b = 0; b < nb.size(); ++b) {
+                regions[b] = {nb[b]};
+                for (const IBox& ob : oldboxes) {
+                    IBox t;
+                    if (ib_isect(nb[b], ob, t)) list_subtract(regions[b], ob);
+                }
+            }
             std::vector<CfTag> tags;
             s = build_cf_tags(H, f, regions, tags);
-            if (s == OCFD_OK) s = A.cf.set(tags);
+            if (s == OCFD_OK) s = A.cf.set(tags, &H->pool);
             if (s == OCFD_OK) s = launch_cf(H, f, NL->buf[0], a, st);
         }
+        pt.mark("  interpolate new level", st);
         if (s == OCFD_OK && old) s = launch_copy(H, NL, nb, old, oldboxes, st);
+        pt.mark("  copy old level", st);
         if (old) {
             cudaStreamSynchronize(st);
             ocfd_level_destroy(old);
@@ -1211,14 +1262,16 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
             ghost_regions(H, f, regions);
             std::vector<CfTag> tags;
             s = build_cf_tags(H, f, regions, tags);
-            if (s == OCFD_OK) s = A.cf.set(tags);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("AMR regrid");
+            if (s == OCFD_OK) s = A.cf.set(tags, &H->pool);
             if (s == OCFD_OK) s = fill_level(H, f, NL->buf[0], a, 0.0, st);
             if (s != OCFD_OK) return s;
         }
+        pt.mark("  destroy old + ghosts", st);
     }
     for (int f = newfinest + 1; f < H->nlev; ++f) {
         cudaStreamSynchronize(st);
-        H->lev[f].release_tables();
+        H->lev[f].release_tables(&H->pool);
         ocfd_level_destroy(H->lev[f].L);
         H->lev[f].L = nullptr;
         H->lev[f].boxes.clear();
@@ -1236,14 +1289,19 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
             if (cudaMemcpy(S.s[l], &q, sizeof(q), cudaMemcpyHostToDevice) != cudaSuccess) return check_launch("AMR time");
         }
     }
-    return rebuild_tables(H);
+    pt.mark("  clocks", st);
+    ocfd_status r = rebuild_tables(H);
+    pt.mark("  rebuild tables", st);
+    return r;
 }
 
 static ocfd_status regrid(ocfd_amr* H, int lbase, cudaStream_t st) {
     if (lbase < 0 || lbase >= H->nlev) return fail(OCFD_BAD_ARG, "ocfd_amr_regrid: lbase");
     if (lbase >= H->desc.max_level) return OCFD_OK;
+    PhaseTimer pt;
     ocfd_status s = fill_all_sync(H, st);
     if (s != OCFD_OK) return s;
+    pt.mark("sync fill", st);
     const int top = std::min(H->nlev - 1, H->desc.max_level - 1);
     std::vector<BlockGrid> T(top + 2);
     for (int l = lbase; l <= top; ++l) {
@@ -1278,6 +1336,7 @@ static ocfd_status regrid(ocfd_amr* H, int lbase, cudaStream_t st) {
             return check_launch("AMR tag download");
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("AMR tagging");
+    pt.mark("tag + download", st);
     // top-down: a level also covers the neighbourhood of the new level above it
     for (int f = top + 1; f >= lbase + 2; --f) {
         BlockGrid& fine = T[f];
@@ -1304,7 +1363,10 @@ static ocfd_status regrid(ocfd_amr* H, int lbase, cudaStream_t st) {
         if (boxes.empty()) break;
         below.build(boxes, g.dom);
     }
-    return apply_grids(H, lbase, grids, st);
+    pt.mark("cluster", st);
+    s = apply_grids(H, lbase, grids, st);
+    pt.mark("apply grids", st);
+    return s;
 }
 
 static ocfd_status ensure_graph(ocfd_amr* H, unsigned flags) {
@@ -1398,7 +1460,7 @@ ocfd_status ocfd_amr_destroy(ocfd_amr* H) {
     cudaDeviceSynchronize();
     if (H->graph) cudaGraphExecDestroy(H->graph);
     for (int l = 0; l < OCFD_AMR_MAX_LEVELS; ++l) {
-        H->lev[l].release_tables();
+        H->lev[l].release_tables(&H->pool);
         cudaFree(H->lev[l].d_blk);
         if (H->lev[l].L) ocfd_level_destroy(H->lev[l].L);
     }

@@ -387,19 +387,20 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     L->ntiles = nt;
     ocfd_status s = OCFD_OK;
     for (int k = 0; k < 3 && s == OCFD_OK; ++k) {
-        cudaFree(L->d_stage[k]);
+        dev_free(L->d_stage[k], L->pool);
         L->d_stage[k] = nullptr;
-        s = upload(&L->d_stage[k], st[k]);
+        s = upload(&L->d_stage[k], st[k], L->pool);
     }
-    cudaFree(L->d_tile_start);
+    dev_free(L->d_tile_start, L->pool);
     L->d_tile_start = nullptr;
-    if (s == OCFD_OK) s = upload(&L->d_tile_start, tile_start);
+    if (s == OCFD_OK) s = upload(&L->d_tile_start, tile_start, L->pool);
     return s;
 }
 
 // Everything of a level but its stage tables: FABs, state buffers, exchange and
 // physical-BC tags, RHS tile choice, step state.
-ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out) {
+ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
+                        DevPool* pool) {
     if (!ctx || !desc || !out || desc->nbox <= 0 || !desc->boxes || nbuf < 3 || nbuf > 4)
         return fail(OCFD_BAD_ARG, "ocfd_level_create: bad arguments");
     *out = nullptr;
@@ -414,6 +415,7 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
     L->ctx = ctx;
     L->desc = *desc;
     L->nbuf = nbuf;
+    L->pool = pool;
     L->boxes.assign(desc->boxes, desc->boxes + desc->nbox);
     L->desc.boxes = nullptr;
     long long off = 0;
@@ -438,24 +440,24 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
     }
     L->elems = off;
     for (int i = 0; i < nbuf; ++i) {
-        if (cudaMalloc(&L->buf[i], sizeof(double) * L->elems) != cudaSuccess) {
-            cudaGetLastError();
+        L->buf[i] = static_cast<double*>(dev_alloc(sizeof(double) * L->elems, pool));
+        if (!L->buf[i]) {
             ocfd_level_destroy(L);
             return fail(OCFD_OUT_OF_MEMORY, "ocfd_level_create: state buffers");
         }
-        cudaMemset(L->buf[i], 0, sizeof(double) * L->elems);
+        if (!pool) cudaMemset(L->buf[i], 0, sizeof(double) * L->elems);
     }
-    ocfd_status s = upload(&L->d_fabs, L->fabs);
-    if (s == OCFD_OK) s = upload(&L->d_cell_start, cell_start);
+    ocfd_status s = upload(&L->d_fabs, L->fabs, pool);
+    if (s == OCFD_OK) s = upload(&L->d_cell_start, cell_start, pool);
     std::vector<ExTag> ex;
     build_exchange(L, ex);
     L->nex = (int)ex.size();
-    if (s == OCFD_OK) s = upload_tags(ex, &L->d_ex, &L->d_ex_start, &L->ex_total);
+    if (s == OCFD_OK) s = upload_tags(ex, &L->d_ex, &L->d_ex_start, &L->ex_total, pool);
     for (int d = 0; d < 3 && s == OCFD_OK; ++d) {
         std::vector<BcTag> bt;
         build_physbc(L, d, bt);
         L->nbc[d] = (int)bt.size();
-        s = upload_tags(bt, &L->d_bc[d], &L->d_bc_start[d], &L->bc_total[d]);
+        s = upload_tags(bt, &L->d_bc[d], &L->d_bc_start[d], &L->bc_total[d], pool);
     }
     for (int d = 0; d < 3; ++d) {
         L->bcinfo.lo_bc[d] = desc->lo_bc[d];
@@ -484,9 +486,9 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
             if (cost < best * 0.999) { best = cost; L->tile = t; }
         }
     }
-    if (s == OCFD_OK && cudaMalloc(&L->d_step, sizeof(StepState)) != cudaSuccess) {
-        cudaGetLastError();
-        s = fail(OCFD_OUT_OF_MEMORY, "step state");
+    if (s == OCFD_OK) {
+        L->d_step = static_cast<StepState*>(dev_alloc(sizeof(StepState), pool));
+        if (!L->d_step) s = fail(OCFD_OUT_OF_MEMORY, "step state");
     }
     if (s == OCFD_OK) {
         k_set_time<<<1, 1>>>(L->d_step, 0.0);
@@ -522,18 +524,19 @@ ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, oc
 ocfd_status ocfd_level_destroy(ocfd_level* L) {
     if (!L) return OCFD_OK;
     if (L->graph) cudaGraphExecDestroy(L->graph);
-    for (int i = 0; i < 4; ++i) cudaFree(L->buf[i]);
+    DevPool* pool = L->pool;
+    for (int i = 0; i < 4; ++i) dev_free(L->buf[i], pool);
     for (int i = 0; i < 3; ++i) {
-        cudaFree(L->d_stage[i]);
-        cudaFree(L->d_bc[i]);
-        cudaFree(L->d_bc_start[i]);
+        dev_free(L->d_stage[i], pool);
+        dev_free(L->d_bc[i], pool);
+        dev_free(L->d_bc_start[i], pool);
     }
-    cudaFree(L->d_fabs);
-    cudaFree(L->d_cell_start);
-    cudaFree(L->d_ex);
-    cudaFree(L->d_ex_start);
-    cudaFree(L->d_tile_start);
-    cudaFree(L->d_step);
+    dev_free(L->d_fabs, pool);
+    dev_free(L->d_cell_start, pool);
+    dev_free(L->d_ex, pool);
+    dev_free(L->d_ex_start, pool);
+    dev_free(L->d_tile_start, pool);
+    dev_free(L->d_step, pool);
     delete L;
     return OCFD_OK;
 }

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <vector>
 
 #include "ocfd_internal.h"
@@ -70,14 +71,76 @@ __device__ __forceinline__ void region_cell(const int* lo, const int* hi, long l
     k = lo[2] + (int)(local / (nx * ny));
 }
 
+// Device memory of an AMR hierarchy: released blocks are kept and handed out
+// again by capacity, so regridding neither allocates nor frees in steady state
+// (cudaMalloc / cudaFree synchronize the device).  Blocks are reused only after
+// the caller has synchronized the work that used them.
+struct DevPool {
+    struct Blk {
+        void* p;
+        size_t cap;
+    };
+    std::vector<Blk> free_list;
+    std::map<void*, size_t> live;
+    ~DevPool() { release_all(); }
+    void* get(size_t bytes) {
+        bytes = std::max<size_t>(256, (bytes + 255) & ~size_t(255));
+        int best = -1;
+        for (int i = 0; i < (int)free_list.size(); ++i) {
+            const size_t c = free_list[i].cap;
+            if (c >= bytes && c <= 2 * bytes + 65536 && (best < 0 || c < free_list[best].cap)) best = i;
+        }
+        void* p = nullptr;
+        size_t cap = bytes;
+        if (best >= 0) {
+            p = free_list[best].p;
+            cap = free_list[best].cap;
+            free_list.erase(free_list.begin() + best);
+        } else {
+            if (bytes >= (size_t(1) << 20)) cap = bytes + bytes / 8;  // room for a slightly larger level
+            if (cudaMalloc(&p, cap) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+        }
+        live[p] = cap;
+        return p;
+    }
+    void put(void* p) {
+        if (!p) return;
+        auto it = live.find(p);
+        if (it == live.end()) return;
+        free_list.push_back({p, it->second});
+        live.erase(it);
+    }
+    void release_all() {
+        for (auto& b : free_list) cudaFree(b.p);
+        for (auto& kv : live) cudaFree(kv.first);
+        free_list.clear();
+        live.clear();
+    }
+};
+
+inline void* dev_alloc(size_t bytes, DevPool* pool) {
+    if (pool) return pool->get(bytes);
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(1, bytes)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+inline void dev_free(void* p, DevPool* pool) {
+    if (pool) pool->put(p);
+    else cudaFree(p);
+}
+
 // ---- host helpers (level.cu)
 template <class T>
-ocfd_status upload(T** dptr, const std::vector<T>& v) {
+ocfd_status upload(T** dptr, const std::vector<T>& v, DevPool* pool = nullptr) {
     size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
-    if (cudaMalloc(dptr, bytes) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(OCFD_OUT_OF_MEMORY, "level table allocation");
-    }
+    *dptr = static_cast<T*>(dev_alloc(bytes, pool));
+    if (!*dptr) return fail(OCFD_OUT_OF_MEMORY, "level table allocation");
     if (!v.empty() && cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(OCFD_LAUNCH_FAIL, "level table upload");
     return OCFD_OK;
@@ -88,7 +151,8 @@ long long region_cells(const int* lo, const int* hi);
 int grid_for(long long total, int threads, int sms);
 
 template <class Tag>
-ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** d_start, long long* total) {
+ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** d_start, long long* total,
+                        DevPool* pool = nullptr) {
     std::vector<long long> start(tags.size());
     long long acc = 0;
     for (size_t i = 0; i < tags.size(); ++i) {
@@ -96,9 +160,9 @@ ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** 
         acc += region_cells(tags[i].lo, tags[i].hi);
     }
     *total = acc;
-    ocfd_status s = upload(d_tags, tags);
+    ocfd_status s = upload(d_tags, tags, pool);
     if (s != OCFD_OK) return s;
-    return upload(d_start, start);
+    return upload(d_start, start, pool);
 }
 
 }  // namespace ocfd
@@ -135,6 +199,9 @@ struct ocfd_level {
     int ntiles = 0;
     ocfd::StepState* d_step = nullptr;
     bool need_estdt = true;
+    // device memory source: nullptr = cudaMalloc / cudaFree (standalone level),
+    // else the owning hierarchy's pool (state buffers are then not zeroed)
+    ocfd::DevPool* pool = nullptr;
     // graph
     cudaGraphExec_t graph = nullptr;
     unsigned graph_flags = ~0u;
@@ -159,7 +226,8 @@ ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st);
 ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st);
 ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st);
 ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st);
-ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out);
+ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
+                        DevPool* pool = nullptr);
 __global__ void k_set_time(StepState* st, double t);
 
 }  // namespace ocfd
