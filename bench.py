@@ -1,19 +1,28 @@
 """Benchmark: cell-steps/s of the OpenCFD-AMR RHS + RK3 update path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config sod|dmr] [--form fp64|fp32]
+                    [--config dmr-amr|sod|dmr|cube] [--form fp32|fp64]
 
-A step is one SSP-RK3 time step of every box of the workload (3 ghost fills +
-3 fused RHS/update stages + the CFL reduction), i.e. one CUDA-graph launch.
-value  = cells x steps / device time of the K timed steps (state resident in
-         HBM; L2 flushed between steps, untimed), for the headline form (default
-         the mixed-precision form, FP32 flux / FP64 state); the plain FP64 form is
-         timed the same way and reported in config, with the L1 error in density
-         and pressure between the two forms at the same time
+Default workload (dmr-amr): double Mach reflection on a 1024x256x2 base grid
+with two refined levels (ratio 2, |d rho| >= 0.05 tagging, regrid every 2 coarse
+steps, blocking factor 32, max grid 128), subcycled SSP-RK3 at CFL 0.5.  The
+hierarchy is first developed to t = 0.05 (untimed, mixed form), then both forms
+are timed for K coarse steps from that same state.
+A step is one coarse step: regridding when due (host clustering included), then
+one CUDA-graph launch that advances every level with its substeps (ghost fills,
+coarse-fine interpolation, fused RHS/RK stages, reflux, average-down, CFL).
+value  = leaf cell-steps (cells not covered by a finer level, times the
+         substeps of their level) / device time of the K timed steps, state
+         resident in HBM, L2 flushed between steps (untimed), for the headline
+         form (default: FP32 flux / FP64 state); the plain FP64 form is timed the
+         same way and reported in config, with the L1 error in density and
+         pressure between the forms after 20 coarse steps on identical grids
+         (the FP64 run's regrids replayed in the FP32 run)
 e2e    = the same through the C ABI from pinned host buffers: every step uploads
-         the state, advances, downloads the state
+         every level's state, advances, downloads every level's state
 --impl reference times the reference algorithm on the host CPU cores (the
-         oracle port, OpenMP, all threads) on the same workload.
+         oracle port, OpenMP, all threads): RK3 steps of the base grid.
+The single-level configs (sod, dmr, cube) time one level of boxes.
 Multi-GPU: independent replicas (the workload does not shard over GPUs here);
 value is summed over ranks with the max time.
 """
@@ -34,6 +43,20 @@ for p in (os.path.join(ROOT, "opencfd-amr_gb300"), os.path.join(ROOT, "oracle"))
 
 METRIC = "cell-steps/s on 1 GB300, plain FP64 vs mixed/batched form at matched L1 error"
 CFL = 0.5
+
+
+T_DEV = 0.05
+L1_STEPS = 20
+
+
+def amr_workload():
+    from ocfd import cases
+    c = cases.dmr_amr(1024, 256, 2, max_level=2, blocking_factor=32, max_grid=128, n_error_buf=1,
+                      refine_dengrad=0.05, regrid_int=2)
+    c["name"] = ("Double Mach reflection 1024x256x2 base + 2 levels (ratio 2, |drho|>=0.05 tagging, "
+                 "regrid every 2 coarse steps, blocking 32, max grid 128), subcycled SSP-RK3, CFL 0.5, "
+                 "timed from t=%.2f" % T_DEV)
+    return c
 
 
 def workload(name):
@@ -173,10 +196,23 @@ def cpu_time_steps(c, steps, threads=None):
     return dt, cells
 
 
+def cpu_sample_workload(config):
+    """The CPU sample: the workload itself for single-level configs, the base
+    grid of the DMR hierarchy (one level, the same boxes' arithmetic) for dmr-amr."""
+    if config == "dmr-amr":
+        c = workload("dmr")
+        c["name"] = amr_workload()["name"]
+        c["sample_note"] = "base grid 1024x256x2 only (no refined levels)"
+        return c
+    c = workload(config)
+    c["sample_note"] = "full workload"
+    return c
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    c = workload(args.config)
+    c = cpu_sample_workload(args.config)
     threads = os.cpu_count() or 1
     # bounded: warm-up steps then K timed steps, each a full-domain RK3 step
     cpu_time_steps(c, max(1, min(args.warmup, 2)), threads)
@@ -188,12 +224,202 @@ def run_reference(args, world, rank):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": c["name"], "form": "fp64", "cells": cells},
             "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-                             "sample": "%d full-domain RK3 steps of the oracle restatement (OpenMP)" % args.steps},
+                             "sample": "%d RK3 steps of the oracle restatement (OpenMP), %s" % (
+                                 args.steps, c["sample_note"])},
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- GPU (ours)
+def make_hierarchy(ctx, c, regrid_int):
+    from ocfd.amr import Hierarchy
+    from ocfd.level import chop_domain
+    return Hierarchy(ctx, chop_domain(c["n"], c["max_grid_size"]), c["n"], c["lo_bc"], c["hi_bc"], c["dx"],
+                     c["prob_lo"], c["bc_case"], c["case_params"], c["max_level"], c["blocking_factor"],
+                     c["max_grid_size"], c["n_error_buf"], regrid_int, c["refine_dengrad"])
+
+
+def amr_matched_l1(ctx, c, snap, steps=L1_STEPS):
+    """L1 (sum|a-b| / sum|b| over valid cells, as fcompare) of density and
+    pressure between the FP32 and FP64 forms after `steps` coarse steps from the
+    same state: the FP64 run regrids every 2 steps and the FP32 run replays its
+    grids, so every level compares on identical grids."""
+    import numpy as np
+    import ocfd
+    Hd = make_hierarchy(ctx, c, 0)
+    Hd.restore(snap)
+    grids_at = {}
+    for i in range(steps):
+        if i > 0 and i % c["regrid_int"] == 0:
+            Hd.regrid(0)
+            grids_at[i] = Hd.all_grids()[1:]
+        Hd.advance(1, CFL, 0)
+    t_end = Hd.time()[0]
+    ref = [Hd.level_global(l) for l in range(Hd.nlevels())]
+    Hd.close()
+    Hf = make_hierarchy(ctx, c, 0)
+    Hf.restore(snap)
+    Hf.set_stop_time(t_end)
+    for i in range(steps):
+        if i in grids_at:
+            Hf.set_grids(grids_at[i])
+        Hf.advance(1, CFL, ocfd.FLUX_FP32)
+    t_f = Hf.time()[0]
+    got = [Hf.level_global(l) for l in range(Hf.nlevels())]
+    Hf.close()
+    pr = lambda U: 0.4 * (U[4] - 0.5 * (U[1] ** 2 + U[2] ** 2 + U[3] ** 2) / U[0])
+    l1 = lambda x, y: float(np.abs(x - y).sum() / np.abs(y).sum())
+    out = {"t0": snap["time"], "t": t_end, "t_fp32": t_f, "coarse_steps": steps, "forms": "fp32-flux vs fp64",
+           "grids": "fp64 regrids replayed"}
+    per = []
+    for l, ((a, m), (b, _)) in enumerate(zip(got, ref)):
+        A, B = a[:, m], b[:, m]
+        per.append({"level": l, "rho": l1(A[0], B[0]), "p": l1(pr(A), pr(B))})
+    out["rho"] = per[0]["rho"]            # level 0 after average-down: the composite solution
+    out["p"] = per[0]["p"]
+    out["per_level"] = per
+    out["linf_rho_rel"] = max(float(np.abs(a[0][m] - b[0][m]).max() / np.abs(b[0][m]).max())
+                              for (a, m), (b, _) in zip(got, ref))
+    return out
+
+
+def run_ours_amr(args, world, rank, local):
+    import numpy as np
+    import torch
+    import ocfd
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    flags = ocfd.FLUX_FP32 if args.form == "fp32" else 0
+    c = amr_workload()
+    ctx = ocfd.Context(device=local)
+    H = make_hierarchy(ctx, c, c["regrid_int"])
+    H.build(c["fab"])
+    while H.time()[0] < T_DEV:                       # untimed: develop the flow
+        H.advance(10, CFL, ocfd.FLUX_FP32)
+    snap = H.snapshot()
+    stream = torch.cuda.current_stream(dev)
+    l2flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(fl):
+        """K coarse steps of form `fl` from the snapshot, each timed with CUDA
+        events (regridding inside the events), L2 flushed between steps
+        outside them; returns (ms, leaf cell-steps, all cell-steps, kernels)."""
+        H.restore(snap)
+        H.advance(args.warmup, CFL, fl)
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        leaf = allc = 0
+        k0 = H.kernels_launched()
+        for e0, e1 in ev:
+            l2flush.fill_(1.0)
+            e0.record(stream)
+            H.advance(1, CFL, fl)
+            e1.record(stream)
+            a, b = H.cell_steps()
+            leaf += a
+            allc += b
+        torch.cuda.synchronize()
+        barrier(world)
+        ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
+        return ms, leaf, allc, H.kernels_launched() - k0
+
+    other = 0 if flags else ocfd.FLUX_FP32
+    ms_o, leaf_o, all_o, _ = timed(other)
+    with ClockSampler(local) as clk:
+        ms, leaf, allc, kernels = timed(flags)
+    value = leaf * world / (ms * 1e-3)
+    value_other = leaf_o * world / (ms_o * 1e-3)
+    levels = [{"level": l, "boxes": len(H.grids(l)), "cells": H.level(l).cells()} for l in range(H.nlevels())]
+
+    # dominant kernel, timed live: the fused RK-stage kernel on the finest level
+    fin = H.level(H.nlevels() - 1)
+    stage_ms = fin.profile_stage(flags, reps=10)
+    fcells = fin.cells()
+    alg_bytes = 120.0 * fcells
+    hbm_peak, peak_src = peaks()
+    achieved = alg_bytes / (stage_ms * 1e-3) / 1e9
+    fp64 = ctypes.c_double(); fp32 = ctypes.c_double()
+    ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
+
+    # end to end through the C ABI with host buffers: upload every level,
+    # advance one coarse step, download every level
+    H.restore(snap)
+    H.advance(1, CFL, flags)
+    torch.cuda.synchronize()
+    pins = {}
+
+    def pin(l, n):
+        if l not in pins or pins[l].numel() < n:
+            pins[l] = torch.empty(int(n * 1.5) + 1, dtype=torch.float64).pin_memory()
+        return pins[l]
+    for l in range(H.nlevels()):
+        H.copy_out(l, pin(l, H.state_elems(l)), stream)
+    torch.cuda.synchronize()
+    e2e_steps = max(2, min(args.steps, 10))
+    h2d = d2h = 0
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e2e_leaf = 0
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        for l in range(H.nlevels()):
+            n = H.state_elems(l)
+            H.copy_in(l, pins[l], stream)
+            h2d += 8 * n
+        H.advance(1, CFL, flags, stream)
+        e2e_leaf += H.cell_steps()[0]
+        for l in range(H.nlevels()):
+            n = H.state_elems(l)
+            H.copy_out(l, pin(l, n), stream)
+            d2h += 8 * n
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = allreduce_max(e0.elapsed_time(e1), world)
+    e2e_value = e2e_leaf * world / (e2e_ms * 1e-3)
+
+    l1err = amr_matched_l1(ctx, c, snap) if rank == 0 else None
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cs = cpu_sample_workload("dmr-amr")
+        cpu_steps = 2
+        dt, ccells = cpu_time_steps(cs, cpu_steps, os.cpu_count())
+        cpu = {"value": ccells * cpu_steps / dt, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "%d RK3 steps of the oracle restatement (OpenMP), %s" % (cpu_steps, cs["sample_note"])}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.form == "fp64" else "f32-flux/f64-state", "data": "synthetic",
+            "config": {"workload": c["name"], "form": args.form, "levels": levels,
+                       "leaf_cell_steps_per_coarse_step": leaf / args.steps,
+                       "all_cell_steps_per_coarse_step": allc / args.steps,
+                       "l1_vs_other_form": l1err,
+                       "forms_cell_steps_per_s": {args.form: value, ("fp64" if flags else "fp32"): value_other},
+                       "speedup_fp32_over_fp64": (value / value_other) if flags else (value_other / value),
+                       "l2": "flushed between timed steps (512 MB write, untimed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "k_rhs_regular fused RK stage, finest level (%d cells)" % fcells,
+                         "ms_per_launch": stage_ms, "alg_bytes_per_cell": 120,
+                         "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s",
+                    "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps)},
+            "clocks": clk.summary(),
+            "gpu_launches": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    H.close()
+    ctx.close()
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -340,7 +566,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="sod", choices=["sod", "dmr", "cube"])
+    ap.add_argument("--config", default="dmr-amr", choices=["dmr-amr", "sod", "dmr", "cube"])
     ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
                     help="headline form (the other form is timed too and reported in config)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -350,6 +576,8 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.config == "dmr-amr":
+        run_ours_amr(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

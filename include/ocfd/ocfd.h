@@ -367,8 +367,18 @@ ocfd_status ocfd_amr_set_stop_time(ocfd_amr* amr, double stop_time, void* stream
 /* Cell-steps of one coarse step: leaf = cells not covered by a finer level,
  * all = every cell advanced; each weighted by the level's 2^lev substeps. */
 ocfd_status ocfd_amr_cell_steps(const ocfd_amr* amr, int64_t* leaf, int64_t* all);
-/* Kernel and copy nodes of one coarse step (the captured graph). */
+/* State FABs of level `lev` (grown boxes back to back, layout of
+ * ocfd_level_copy_in) to / from host or device memory; the hierarchy's clock is
+ * left alone.  ocfd_amr_state_elems gives the number of doubles. */
+size_t ocfd_amr_state_elems(const ocfd_amr* amr, int lev);
+ocfd_status ocfd_amr_copy_in(ocfd_amr* amr, int lev, const double* buf, void* stream);
+ocfd_status ocfd_amr_copy_out(ocfd_amr* amr, int lev, double* buf, void* stream);
+/* Kernel launches of one coarse step (the captured graph; memset / copy nodes
+ * not counted). */
 int ocfd_amr_launches_per_step(const ocfd_amr* amr);
+/* Kernels launched by the hierarchy since its creation: graph launches times
+ * their kernels, plus regridding, ghost filling and time-step estimation. */
+int64_t ocfd_amr_kernels_launched(const ocfd_amr* amr);
 
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops

@@ -513,7 +513,8 @@ struct ocfd_amr {
     bool graph_ok = false;
     bool need_estdt = true;
     long long steps = 0;
-    int launches = 0;
+    int launches = 0;          // kernels of the captured coarse step
+    long long kernel_total = 0;  // kernels launched by this hierarchy so far
 };
 
 namespace ocfd {
@@ -995,7 +996,6 @@ static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cud
     if (has_child) {
         cudaMemsetAsync(A.creg, 0, sizeof(double) * std::max<long long>(1, A.creg_elems), st);
         cudaMemsetAsync(H->lev[l + 1].freg, 0, sizeof(double) * std::max<long long>(1, H->lev[l + 1].freg_elems), st);
-        launches_counter += 2;
     }
     for (int k = 0; k < 3 && s == OCFD_OK; ++k) {
         double a[4];
@@ -1022,7 +1022,6 @@ static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cud
         if (cudaMemcpyAsync(L->buf[0], L->buf[3], sizeof(double) * L->elems, cudaMemcpyDeviceToDevice, st) !=
             cudaSuccess)
             return check_launch("AMR D -> A");
-        ++launches_counter;
     }
     if (l > 0) {
         k_sub_end<<<1, 1, 0, st>>>(L->d_step);
@@ -1191,6 +1190,7 @@ static ocfd_status launch_copy(ocfd_amr* H, ocfd_level* dst, const std::vector<I
     if (s == OCFD_OK) {
         k_copy_tags<<<grid_for(dt.total, 256, H->ctx->num_sms), 256, 0, st>>>(
             dt.d, dt.start, dt.n, dt.total, dst->d_fabs, dst->buf[0], src->d_fabs, src->buf[0], dst->ncomp);
+        ++launches_counter;
         s = check_launch("AMR regrid copy");
     }
     cudaStreamSynchronize(st);
@@ -1233,6 +1233,7 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
         for (int e = 0; e < 3; ++e) A.dx[e] = H->desc.dx[e] / (double)(1 << f);
         if (H->nlev < f + 1) H->nlev = f + 1;
         k_copy_step<<<1, 1, 0, st>>>(NL->d_step, H->lev[0].L->d_step);
+        ++launches_counter;
         // cells the old level did not cover from the level below, the rest copied
         {
             std::vector<std::vector<IBox>> regions(nb.size());
@@ -1295,7 +1296,16 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
     return r;
 }
 
+static ocfd_status regrid_impl(ocfd_amr* H, int lbase, cudaStream_t st);
+
 static ocfd_status regrid(ocfd_amr* H, int lbase, cudaStream_t st) {
+    const int c0 = launches_counter;
+    ocfd_status s = regrid_impl(H, lbase, st);
+    H->kernel_total += launches_counter - c0;
+    return s;
+}
+
+static ocfd_status regrid_impl(ocfd_amr* H, int lbase, cudaStream_t st) {
     if (lbase < 0 || lbase >= H->nlev) return fail(OCFD_BAD_ARG, "ocfd_amr_regrid: lbase");
     if (lbase >= H->desc.max_level) return OCFD_OK;
     PhaseTimer pt;
@@ -1330,6 +1340,7 @@ static ocfd_status regrid(ocfd_amr* H, int lbase, cudaStream_t st) {
         ocfd_level* L = A.L;
         k_tag_dengrad<<<grid_for(L->ncells, 256, H->ctx->num_sms), 256, 0, st>>>(
             L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->buf[0], tg, A.d_blk);
+        ++launches_counter;
         s = check_launch("AMR tagging");
         if (s != OCFD_OK) return s;
         if (cudaMemcpyAsync(g.v.data(), A.d_blk, nblk, cudaMemcpyDeviceToHost, st) != cudaSuccess)
@@ -1545,14 +1556,18 @@ ocfd_status ocfd_amr_advance(ocfd_amr* H, int nsteps, double cfl, unsigned flags
         if (cudaMemcpyAsync(&H->lev[0].L->d_step->cfl, &cfl, sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
             return check_launch("ocfd_amr_advance");
         if (H->need_estdt) {
+            const int c0 = launches_counter;
             k_reset_cfl_all<<<1, 1, 0, st>>>(states(H));
+            ++launches_counter;
             ocfd_status s = launch_estdt_all(H, st);
             if (s != OCFD_OK) return s;
+            H->kernel_total += launches_counter - c0;
             H->need_estdt = false;
         }
         ocfd_status s = ensure_graph(H, flags);
         if (s != OCFD_OK) return s;
         if (cudaGraphLaunch(H->graph, st) != cudaSuccess) return check_launch("AMR graph launch");
+        H->kernel_total += H->launches;
         ++H->steps;
     }
     return OCFD_OK;
@@ -1590,5 +1605,31 @@ ocfd_status ocfd_amr_cell_steps(const ocfd_amr* H, int64_t* leaf, int64_t* all) 
 }
 
 int ocfd_amr_launches_per_step(const ocfd_amr* H) { return H ? H->launches : 0; }
+
+size_t ocfd_amr_state_elems(const ocfd_amr* H, int lev) {
+    if (!H || lev < 0 || lev >= H->nlev) return 0;
+    return (size_t)H->lev[lev].L->elems;
+}
+
+ocfd_status ocfd_amr_copy_in(ocfd_amr* H, int lev, const double* buf, void* stream) {
+    if (!H || lev < 0 || lev >= H->nlev || !buf) return fail(OCFD_BAD_ARG, "ocfd_amr_copy_in");
+    ocfd_level* L = H->lev[lev].L;
+    if (cudaMemcpyAsync(L->buf[0], buf, sizeof(double) * L->elems, cudaMemcpyDefault,
+                        static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        return check_launch("ocfd_amr_copy_in");
+    H->need_estdt = true;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_amr_copy_out(ocfd_amr* H, int lev, double* buf, void* stream) {
+    if (!H || lev < 0 || lev >= H->nlev || !buf) return fail(OCFD_BAD_ARG, "ocfd_amr_copy_out");
+    ocfd_level* L = H->lev[lev].L;
+    if (cudaMemcpyAsync(buf, L->buf[0], sizeof(double) * L->elems, cudaMemcpyDefault,
+                        static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        return check_launch("ocfd_amr_copy_out");
+    return OCFD_OK;
+}
+
+int64_t ocfd_amr_kernels_launched(const ocfd_amr* H) { return H ? H->kernel_total : 0; }
 
 }  // extern "C"

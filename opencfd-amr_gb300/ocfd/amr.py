@@ -41,6 +41,10 @@ declare("ocfd_amr_set_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
 declare("ocfd_amr_set_stop_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
 declare("ocfd_amr_cell_steps", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)])
 declare("ocfd_amr_launches_per_step", ctypes.c_int, [_vp])
+declare("ocfd_amr_kernels_launched", ctypes.c_int64, [_vp])
+declare("ocfd_amr_state_elems", ctypes.c_size_t, [_vp, ctypes.c_int])
+declare("ocfd_amr_copy_in", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
+declare("ocfd_amr_copy_out", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
 
 
 def _boxes_array(boxes):
@@ -184,6 +188,9 @@ class Hierarchy:
     def launches_per_step(self):
         return int(self.lib.ocfd_amr_launches_per_step(self.h))
 
+    def kernels_launched(self):
+        return int(self.lib.ocfd_amr_kernels_launched(self.h))
+
     # ---- data -----------------------------------------------------------------
     def level_global(self, lev, stream=None):
         """(valid data (5, Nz, Ny, Nx) of the whole level domain, mask of valid cells)"""
@@ -197,6 +204,32 @@ class Hierarchy:
             mask[blo[2]:bhi[2] + 1, blo[1]:bhi[1] + 1, blo[0]:bhi[0] + 1] = True
         return out, mask
 
-    def state(self, stream=None):
-        """Snapshot of every level's state FABs (host), for restore()."""
-        return [self.level(l).copy_out(stream=stream) for l in range(self.nlevels())]
+    def state_elems(self, lev):
+        return int(self.lib.ocfd_amr_state_elems(self.h, lev))
+
+    def copy_in(self, lev, buf, stream=None):
+        """buf: host numpy array or CUDA tensor of state_elems(lev) doubles."""
+        ptr = buf.ctypes.data if isinstance(buf, np.ndarray) else buf.data_ptr()
+        check(self.lib.ocfd_amr_copy_in(self.h, lev, ctypes.c_void_p(ptr), _stream_ptr(stream)), "amr copy_in")
+
+    def copy_out(self, lev, buf=None, stream=None):
+        if buf is None:
+            buf = np.empty(self.state_elems(lev))
+        ptr = buf.ctypes.data if isinstance(buf, np.ndarray) else buf.data_ptr()
+        check(self.lib.ocfd_amr_copy_out(self.h, lev, ctypes.c_void_p(ptr), _stream_ptr(stream)), "amr copy_out")
+        return buf
+
+    def snapshot(self):
+        """Grids, state and time of every level (host), for restore()."""
+        import torch
+        data = [self.copy_out(l) for l in range(self.nlevels())]
+        torch.cuda.synchronize()
+        return dict(grids=self.all_grids(), data=data, time=self.time()[0])
+
+    def restore(self, snap, stream=None):
+        import torch
+        self.set_grids(snap["grids"][1:], stream)
+        for l, d in enumerate(snap["data"]):
+            self.copy_in(l, d, stream)
+        torch.cuda.synchronize()
+        self.set_time(snap["time"], stream)
