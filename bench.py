@@ -314,6 +314,7 @@ def run_ours_amr(args, world, rank, local):
               for _ in range(args.steps)]
         leaf = allc = 0
         k0 = H.kernels_launched()
+        torch.cuda.nvtx.range_push("bench_timed_" + ("fp32" if fl else "fp64"))
         for e0, e1 in ev:
             l2flush.fill_(1.0)
             e0.record(stream)
@@ -323,6 +324,7 @@ def run_ours_amr(args, world, rank, local):
             leaf += a
             allc += b
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         barrier(world)
         ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
         return ms, leaf, allc, H.kernels_launched() - k0

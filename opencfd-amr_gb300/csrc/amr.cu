@@ -198,10 +198,11 @@ struct BoxIndex {
 };
 
 // ================================================================ device tags
-struct CfTag {  // fine cells (fine box index space) interpolated from one coarse box
+struct CfTag {  // fine cells interpolated from one coarse box, by parent cell
     int fbox, cbox;
-    int lo[3], hi[3];
-    int shift[3];  // fine cell + shift = its image inside the domain (periodic)
+    int lo[3], hi[3];    // parent cells (coarse, inside the domain)
+    int flo[3], fhi[3];  // the children to fill (fine, inside the domain)
+    int shift[3];        // fine cell in the fine box's index space = domain cell - shift
 };
 struct AvgTag {  // coarse cells averaged from one fine box
     int cbox, fbox;
@@ -260,22 +261,37 @@ __global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __r
          idx += (long long)gridDim.x * blockDim.x) {
         const int t = find_tag<CfTag>(start, ntag, idx);
         const CfTag& T = tags[t];
-        int i, j, k;
-        region_cell(T.lo, T.hi, idx - start[t], i, j, k);
-        const int fi = i + T.shift[0], fj = j + T.shift[1], fk = k + T.shift[2];
-        const double ox = (fi & 1) ? 0.25 : -0.25, oy = (fj & 1) ? 0.25 : -0.25, oz = (fk & 1) ? 0.25 : -0.25;
+        int pi, pj, pk;
+        region_cell(T.lo, T.hi, idx - start[t], pi, pj, pk);
         const FabGeom& cf = cfabs[T.cbox];
         const FabGeom& ff = ffabs[T.fbox];
-        const long long c = fab_index(cf, fi >> 1, fj >> 1, fk >> 1);
+        const long long c = fab_index(cf, pi, pj, pk);
         const long long sy = cf.g[0], sz = (long long)cf.g[0] * cf.g[1];
-        const long long o = fab_index(ff, i, j, k);
+        const long long o = fab_index(ff, 2 * pi - T.shift[0], 2 * pj - T.shift[1], 2 * pk - T.shift[2]);
+        const long long fy = ff.g[0], fz = (long long)ff.g[0] * ff.g[1];
+        // children of this parent inside the region (bit ii + 2 jj + 4 kk)
+        unsigned inside = 0;
+#pragma unroll
+        for (int q8 = 0; q8 < 8; ++q8) {
+            const int ci = 2 * pi + (q8 & 1), cj = 2 * pj + ((q8 >> 1) & 1), ck = 2 * pk + (q8 >> 2);
+            if (ci >= T.flo[0] && ci <= T.fhi[0] && cj >= T.flo[1] && cj <= T.fhi[1] && ck >= T.flo[2] &&
+                ck <= T.fhi[2])
+                inside |= 1u << q8;
+        }
         for (int n = 0; n < ncomp; ++n) {
             const long long q = c + n * cf.ns;
             const double v0 = mixed(mix, q);
             const double sx_ = mc_slope(mixed(mix, q - 1), v0, mixed(mix, q + 1));
             const double sy_ = mc_slope(mixed(mix, q - sy), v0, mixed(mix, q + sy));
             const double sz_ = mc_slope(mixed(mix, q - sz), v0, mixed(mix, q + sz));
-            dst[o + n * ff.ns] = v0 + ox * sx_ + oy * sy_ + oz * sz_;
+            double* d = dst + o + n * ff.ns;
+#pragma unroll
+            for (int q8 = 0; q8 < 8; ++q8) {
+                const int ii = q8 & 1, jj = (q8 >> 1) & 1, kk = q8 >> 2;
+                if (inside & (1u << q8))
+                    d[ii + jj * fy + kk * fz] = v0 + (ii ? 0.25 : -0.25) * sx_ + (jj ? 0.25 : -0.25) * sy_ +
+                                               (kk ? 0.25 : -0.25) * sz_;
+            }
         }
     }
 }
@@ -414,9 +430,9 @@ __global__ void k_amr_stop(AmrStates S, double t) {
     for (int l = 0; l < S.n; ++l) S.s[l]->stop_time = t;
 }
 
-__global__ void k_copy_step(StepState* dst, const StepState* src) {
+__global__ void k_copy_step(StepState* dst, const StepState* src, const StepState* est) {
     *dst = *src;
-    dst->cfl_min = 0x7FF0000000000000ULL;
+    dst->cfl_min = est ? est->cfl_min : 0x7FF0000000000000ULL;
 }
 
 __global__ void k_reset_cfl_all(AmrStates S) {
@@ -621,18 +637,19 @@ static ocfd_status build_cf_tags(const ocfd_amr* H, int f, const std::vector<std
                     if (!ib_isect(Qc, C.boxes[cb], I)) continue;
                     IBox Fr;
                     if (!ib_isect(ib_refine(I), Qs, Fr)) continue;
-                    const int back[3] = {-sh[0], -sh[1], -sh[2]};
-                    const IBox R = ib_shift(Fr, back);
+                    const IBox Pc = ib_coarsen(Fr);
                     CfTag t{};
                     t.fbox = b;
                     t.cbox = cb;
                     for (int e = 0; e < 3; ++e) {
-                        t.lo[e] = R.lo[e];
-                        t.hi[e] = R.hi[e];
+                        t.lo[e] = Pc.lo[e];
+                        t.hi[e] = Pc.hi[e];
+                        t.flo[e] = Fr.lo[e];
+                        t.fhi[e] = Fr.hi[e];
                         t.shift[e] = sh[e];
                     }
                     out.push_back(t);
-                    got += ib_cells(R);
+                    got += ib_cells(Fr);
                 }
             }
             if (got != need) return fail(OCFD_BAD_ARG, "AMR: a fine level is not properly nested in the level below");
@@ -649,7 +666,7 @@ static void ghost_regions(const ocfd_amr* H, int f, std::vector<std::vector<IBox
     periodic_shifts(H, fdom, shifts);
     regions.assign(F.boxes.size(), {});
     for (size_t b = 0; b < F.boxes.size(); ++b) {
-        IBox R = ib_grow(F.boxes[b], NGR);
+        IBox R = ib_grow(F.boxes[b], NFILL);
         for (int e = 0; e < 3; ++e)
             if (!H->periodic[e]) {
                 R.lo[e] = std::max(R.lo[e], fdom.lo[e]);
@@ -913,7 +930,6 @@ static ocfd_status rebuild_tables(ocfd_amr* H) {
     }
     pt.mark("    stage tables", 0);
     H->graph_ok = false;
-    H->need_estdt = true;
     return OCFD_OK;
 }
 
@@ -1232,7 +1248,9 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
         A.dom = level_domain(H, f);
         for (int e = 0; e < 3; ++e) A.dx[e] = H->desc.dx[e] / (double)(1 << f);
         if (H->nlev < f + 1) H->nlev = f + 1;
-        k_copy_step<<<1, 1, 0, st>>>(NL->d_step, H->lev[0].L->d_step);
+        // clock of level 0; the CFL estimate of the level it replaces (the step's dt
+        // comes from the estimates made at the end of the previous step)
+        k_copy_step<<<1, 1, 0, st>>>(NL->d_step, H->lev[0].L->d_step, old ? old->d_step : nullptr);
         ++launches_counter;
         // cells the old level did not cover from the level below, the rest copied
         {
@@ -1285,8 +1303,11 @@ static ocfd_status apply_grids(ocfd_amr* H, int lbase, const std::vector<std::ve
         cudaStreamSynchronize(st);
         if (cudaMemcpy(&h, S.s[0], sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return check_launch("AMR time");
         for (int l = 1; l < H->nlev; ++l) {
-            StepState q = h;
-            q.cfl_min = 0x7FF0000000000000ULL;
+            StepState q{};
+            if (cudaMemcpy(&q, S.s[l], sizeof(q), cudaMemcpyDeviceToHost) != cudaSuccess) return check_launch("AMR time");
+            const unsigned long long est = q.cfl_min;
+            q = h;
+            q.cfl_min = est;
             if (cudaMemcpy(S.s[l], &q, sizeof(q), cudaMemcpyHostToDevice) != cudaSuccess) return check_launch("AMR time");
         }
     }

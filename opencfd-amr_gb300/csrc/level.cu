@@ -194,7 +194,7 @@ static void build_exchange(ocfd_level* L, std::vector<ExTag>& tags) {
     for (int b = 0; b < nb; ++b) {
         const ocfd_box& B = L->boxes[b];
         int glo[3], ghi[3];
-        for (int d = 0; d < 3; ++d) { glo[d] = B.lo[d] - NGR; ghi[d] = B.hi[d] + NGR; }
+        for (int d = 0; d < 3; ++d) { glo[d] = B.lo[d] - NFILL; ghi[d] = B.hi[d] + NFILL; }
         for (int sx = -1; sx <= 1; ++sx)
             for (int sy = -1; sy <= 1; ++sy)
                 for (int sz = -1; sz <= 1; ++sz) {
@@ -252,8 +252,8 @@ static void build_physbc(ocfd_level* L, int d, std::vector<BcTag>& tags) {
             t.box = b;
             t.side = side;
             for (int e = 0; e < 3; ++e) {
-                t.lo[e] = B.lo[e] - NGR;
-                t.hi[e] = B.hi[e] + NGR;
+                t.lo[e] = B.lo[e] - NFILL;
+                t.hi[e] = B.hi[e] + NFILL;
                 if (e > d && L->desc.lo_bc[e] != OCFD_BC_INTERIOR) {
                     t.lo[e] = std::max(t.lo[e], dom.lo[e]);
                     t.hi[e] = std::min(t.hi[e], dom.hi[e]);

@@ -15,6 +15,10 @@
 namespace ocfd {
 
 constexpr int NGR = OCFD_NUM_GROW;
+// Ghost layers the level and hierarchy fill: the regular stencils read 3 (WENO-Z
+// +-3, the viscous ring +-1, coarse-fine interpolation and tagging +-1); the 4th
+// layer of the NUM_GROW-wide FABs is left untouched.
+constexpr int NFILL = 3;
 
 struct FabGeom {
     int lo[3], hi[3];  // valid box

@@ -505,7 +505,10 @@ class AmrOracle:
                 V[:, keep] = old["U"][:, NG:-NG, NG:-NG, NG:-NG][:, keep]
             self.fill(f, new["U"])
         del self.levels[newfinest + 1:]
-        self.est = None
+        # the next step's dt comes from the estimates made at the end of the
+        # previous step: a rebuilt level keeps its level's estimate, a new one has none
+        if self.est is not None:
+            self.est = (self.est + [math.inf] * len(self.levels))[:len(self.levels)]
 
     def grids(self):
         return [list(L["boxes"]) for L in self.levels]
