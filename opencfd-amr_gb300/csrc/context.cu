@@ -76,6 +76,18 @@ DevParm make_dev_parm(const ocfd_parm& p) {
     d.sw_tmp2 = 2.0 * (g - 1.0);
     d.sw_tmp3 = (3.0 - g) / (2.0 * (g - 1.0));
     d.sw_gm1 = g - 1;
+    d.f_gamma = (float)d.gamma;
+    d.f_smallr = (float)d.smallr;
+    d.f_smallp = (float)d.smallp;
+    d.f_invRg = (float)(1.0 / d.Rg);
+    d.f_C_s = (float)d.C_s;
+    d.f_T_s = (float)d.T_s;
+    d.f_kOverMu = (float)d.kOverMu;
+    d.f_twoThirds = (float)d.twoThirds;
+    d.f_sw_tmp1 = (float)d.sw_tmp1;
+    d.f_sw_tmp2 = (float)d.sw_tmp2;
+    d.f_sw_tmp3 = (float)d.sw_tmp3;
+    d.f_sw_gm1 = (float)d.sw_gm1;
     return d;
 }
 

@@ -367,7 +367,10 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
             r.rk_b = rb[k];
             r.dt_ptr = &L->d_step->dt;
             r.cfl_min = (k == 2 && roles.cfl) ? &L->d_step->cfl_min : nullptr;
-            for (int d = 0; d < 3; ++d) r.dx[d] = desc->dx[d];
+            for (int d = 0; d < 3; ++d) {
+                r.dx[d] = desc->dx[d];
+                r.dx_f[d] = (float)desc->dx[d];
+            }
             if (!roles.flux_bits.empty() && roles.flux_bits[b]) {
                 r.has_flux = roles.flux_bits[b];
                 r.flux_w = wflux[k];

@@ -56,6 +56,7 @@ void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* d
         a.lo[d] = bx.lo[d];
         a.hi[d] = bx.hi[d];
         a.dxinv[d] = dxinv[d];
+        a.dxinv_f[d] = (float)dxinv[d];
     }
     const TileShape& s = kRegularTiles[tile];
     const int T[3] = {s.x, s.y, s.z};

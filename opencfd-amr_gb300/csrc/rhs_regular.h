@@ -33,6 +33,7 @@ struct RegBoxArgs {
     View<double> fplane[3][2];
     int lo[3], hi[3];
     double dxinv[3];
+    float dxinv_f[3], dx_f[3];  // FP32 copies for the mixed form
     int ntile[3];
     int mode;
     // RHS_FUSED_STAGE: Uout = rk_a * U0 + rk_b * (S + dt * L(S)) over the box,

@@ -163,33 +163,33 @@ struct Prec<float> {
     // c2prim in FP32 from the narrowed conserved state
     static __device__ __forceinline__ void prims(const DevParm& P, const View<const double>& S, int i,
                                                  int j, int k, float* q) {
-        const float g = (float)P.gamma;
+        const float g = P.f_gamma;
         const float u0 = d2f_bits(S(i, j, k, 0)), u1 = d2f_bits(S(i, j, k, 1)), u2 = d2f_bits(S(i, j, k, 2)),
                     u3 = d2f_bits(S(i, j, k, 3)), u4 = d2f_bits(S(i, j, k, 4));
-        const float rho = fmaxf(u0, (float)P.smallr);
+        const float rho = fmaxf(u0, P.f_smallr);
         const float rhoinv = __frcp_rn(rho);
         const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
         const float ei = u4 - rho * (0.5f * (ux * ux + uy * uy + uz * uz));
-        const float p = fmaxf((g - 1.0f) * ei, (float)P.smallp);
+        const float p = fmaxf((g - 1.0f) * ei, P.f_smallp);
         q[QRHO] = rho;
         q[QU] = ux;
         q[QV] = uy;
         q[QW] = uz;
         q[QPRES] = p;
-        q[QT] = p * rhoinv * (float)(1.0 / P.Rg);
+        q[QT] = p * rhoinv * P.f_invRg;
         q[QC] = sqrtf(g * p * rhoinv);
     }
     template <int D>
     static __device__ __forceinline__ void split(const DevParm& P, const float* q, float* fp, float* fm) {
-        sw_split<D, float>(q[QRHO], q[QU], q[QV], q[QW], q[QC], (float)P.sw_tmp1, (float)P.sw_tmp2,
-                           (float)P.sw_tmp3, (float)P.sw_gm1, fp, fm);
+        sw_split<D, float>(q[QRHO], q[QU], q[QV], q[QW], q[QC], P.f_sw_tmp1, P.f_sw_tmp2, P.f_sw_tmp3,
+                           P.f_sw_gm1, fp, fm);
     }
     static __device__ __forceinline__ float weno(const float* a, const float* b, int s) {
         return wenoz_norm_f(a[0], a[s], a[2 * s], a[3 * s], a[4 * s]) +
                wenoz_norm_f(b[5 * s], b[4 * s], b[3 * s], b[2 * s], b[s]);
     }
     static __device__ __forceinline__ float mu(const DevParm& P, float T) {
-        return (float)P.C_s * T * sqrtf(T) / (T + (float)P.T_s);
+        return P.f_C_s * T * sqrtf(T) / (T + P.f_T_s);
     }
 };
 
@@ -198,22 +198,36 @@ struct Prec<float> {
 // CFL bound of the new state (Source/Advance.cpp:26-49): FP64 in the plain form,
 // FP32 (from the narrowed state) in the mixed form
 template <class FT>
-__device__ __forceinline__ double stage_cfl_bound(const DevParm& P, const double* un, const double* dx) {
-    return cfl_bound(P, un, dx);
+__device__ __forceinline__ double stage_cfl_bound(const DevParm& P, const double* un, const RegBoxArgs& B) {
+    return cfl_bound(P, un, B.dx);
 }
 template <>
-__device__ __forceinline__ double stage_cfl_bound<float>(const DevParm& P, const double* un, const double* dx) {
-    const float g = (float)P.gamma;
+__device__ __forceinline__ double stage_cfl_bound<float>(const DevParm& P, const double* un, const RegBoxArgs& B) {
+    const float g = P.f_gamma;
     const float rho = d2f_bits(un[0]);
-    const float rhoinv = __frcp_rn(fmaxf(rho, (float)P.smallr));
+    const float rhoinv = __frcp_rn(fmaxf(rho, P.f_smallr));
     const float vx = d2f_bits(un[1]) * rhoinv, vy = d2f_bits(un[2]) * rhoinv, vz = d2f_bits(un[3]) * rhoinv;
-    const float p = fmaxf((g - 1.0f) * (d2f_bits(un[4]) - 0.5f * rho * (vx * vx + vy * vy + vz * vz)), (float)P.smallp);
+    const float p = fmaxf((g - 1.0f) * (d2f_bits(un[4]) - 0.5f * rho * (vx * vx + vy * vy + vz * vz)), P.f_smallp);
     const float cs = sqrtf(g * p * rhoinv);
-    const float dtx = __fdividef((float)dx[0], fabsf(vx) + cs);
-    const float dty = __fdividef((float)dx[1], fabsf(vy) + cs);
-    const float dtz = __fdividef((float)dx[2], fabsf(vz) + cs);
+    const float dtx = __fdividef(B.dx_f[0], fabsf(vx) + cs);
+    const float dty = __fdividef(B.dx_f[1], fabsf(vy) + cs);
+    const float dtz = __fdividef(B.dx_f[2], fabsf(vz) + cs);
     return f2d_bits(fminf(dtx, fminf(dty, dtz)));
 }
+
+// box geometry and Parm constants in the flux precision
+template <class FT>
+__device__ __forceinline__ FT dxinv_of(const RegBoxArgs& B, int d) { return B.dxinv[d]; }
+template <>
+__device__ __forceinline__ float dxinv_of<float>(const RegBoxArgs& B, int d) { return B.dxinv_f[d]; }
+template <class FT>
+__device__ __forceinline__ FT kovermu_of(const DevParm& P) { return P.kOverMu; }
+template <>
+__device__ __forceinline__ float kovermu_of<float>(const DevParm& P) { return P.f_kOverMu; }
+template <class FT>
+__device__ __forceinline__ FT twothirds_of(const DevParm& P) { return P.twoThirds; }
+template <>
+__device__ __forceinline__ float twothirds_of<float>(const DevParm& P) { return P.f_twoThirds; }
 
 template <class FT>
 __device__ __forceinline__ double widen(FT x) { return (double)x; }
@@ -222,11 +236,10 @@ __device__ __forceinline__ double widen<float>(float x) { return f2d_bits(x); }
 
 template <class FT, int D, int TX, int TY, int TZ>
 __device__ __forceinline__ void visc_face(const DevParm& P, const FT* ring, int rx, int ry, int rz,
-                                          const double* dxinv_d, FT* f /*stride fs*/, int fs) {
+                                          const FT* dxinv, FT* f /*stride fs*/, int fs) {
     using R = Ring<TX, TY, TZ>;
     constexpr int S[3] = {1, R::RX, R::RX * R::RY};
-    const FT dxinv[3] = {(FT)dxinv_d[0], (FT)dxinv_d[1], (FT)dxinv_d[2]};
-    const FT kOverMu = (FT)P.kOverMu, twoThirds = (FT)P.twoThirds;
+    const FT kOverMu = kovermu_of<FT>(P), twoThirds = twothirds_of<FT>(P);
     const int c = rx + ry * R::RX + rz * R::RX * R::RY;
     const int l = c - S[D];
     const FT* qu = ring;
@@ -296,10 +309,11 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
     __syncthreads();
     // ---- 3. viscous part of the face flux
     if (VISC) {
+        const FT dxinvT[3] = {dxinv_of<FT>(B, 0), dxinv_of<FT>(B, 1), dxinv_of<FT>(B, 2)};
         for (int f = tid; f < PC::NF; f += NT) {
             const int fx = f % PC::FX, fy = (f / PC::FX) % PC::FY, fz = f / (PC::FX * PC::FY);
             // ring coordinates of the cell on the high side of the face
-            visc_face<FT, D, TX, TY, TZ>(P, ring, fx + 1, fy + 1, fz + 1, B.dxinv, FF + f, PC::NF);
+            visc_face<FT, D, TX, TY, TZ>(P, ring, fx + 1, fy + 1, fz + 1, dxinvT, FF + f, PC::NF);
         }
         __syncthreads();
     }
@@ -307,7 +321,7 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
     {
         const int ti = tid % TX, tj = (tid / TX) % TY, tk = tid / (TX * TY);
         const int f = ti + tj * PC::FX + tk * PC::FX * PC::FY;
-        const FT dxi = (FT)B.dxinv[D];
+        const FT dxi = dxinv_of<FT>(B, D);
 #pragma unroll
         for (int n = 0; n < 5; ++n) {
             FT v = dxi * (FF[n * PC::NF + f] - FF[n * PC::NF + f + PC::FST]);
@@ -416,7 +430,7 @@ __global__ void __launch_bounds__(TX* TY* TZ)
                 un[n] = B.rk_a * u0 + B.rk_b * (us + dt * widen<FT>(acc[n]));
                 B.Uout(ci, cj, ck, n) = un[n];
             }
-            if (B.cfl_min) local_dt = stage_cfl_bound<FT>(P, un, B.dx);
+            if (B.cfl_min) local_dt = stage_cfl_bound<FT>(P, un, B);
         }
     }
     if (B.cfl_min) block_min_atomic(local_dt, B.cfl_min);
