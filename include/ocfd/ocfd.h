@@ -373,12 +373,42 @@ ocfd_status ocfd_amr_cell_steps(const ocfd_amr* amr, int64_t* leaf, int64_t* all
 size_t ocfd_amr_state_elems(const ocfd_amr* amr, int lev);
 ocfd_status ocfd_amr_copy_in(ocfd_amr* amr, int lev, const double* buf, void* stream);
 ocfd_status ocfd_amr_copy_out(ocfd_amr* amr, int lev, double* buf, void* stream);
+/* Plotfile of the hierarchy's current state: rho, xmom, ymom, zmom, Eden (the
+ * state names of Source/Setup.cpp:202-206) and the derived ux, uy, uz and
+ * pressure (Source/Setup.cpp:95-110, 164-178); level steps step * 2^lev. */
+ocfd_status ocfd_amr_write_plotfile(ocfd_amr* amr, const char* dir, int32_t step, void* stream);
 /* Kernel launches of one coarse step (the captured graph; memset / copy nodes
  * not counted). */
 int ocfd_amr_launches_per_step(const ocfd_amr* amr);
 /* Kernels launched by the hierarchy since its creation: graph launches times
  * their kernels, plus regridding, ghost filling and time-step estimation. */
 int64_t ocfd_amr_kernels_launched(const ocfd_amr* amr);
+
+/* ------------------------------------------------ plotfiles and comparison
+ * AMReX plotfile layout (HyperCLaw-V1.1: Header, Level_<l>/Cell_H, Cell_D_00000
+ * with one little-endian double FAB per box), the files AmrLevel::writePlotFile
+ * writes for the reference (Source/IO.cpp:32-35), and the comparison of
+ * Util/Plotfile/fcompare.cpp:150-290.  Host code; needs no device.            */
+typedef struct ocfd_plot_level {
+    int32_t nbox;
+    const ocfd_box* boxes;       /* valid boxes of the level */
+    const double* const* fabs;   /* per box: ncomp components over the box, i fastest, component slowest */
+    double dx[3];
+    int32_t step;                /* steps taken by the level */
+} ocfd_plot_level;
+
+ocfd_status ocfd_plotfile_write(const char* dir, int32_t nlev, const ocfd_plot_level* levels, int32_t ncomp,
+                                const char* const* names, const ocfd_box* domain0, const double prob_lo[3],
+                                const double prob_hi[3], int32_t ref_ratio, double time);
+/* Levels and variables of a plotfile. */
+ocfd_status ocfd_plotfile_info(const char* file, int32_t* nlev, int32_t* ncomp);
+/* fcompare: per level l and variable n (index l * ncomp + n, up to cap entries)
+ * the absolute error ||b - a|| (norm 0: max; 1 / 2: discrete L1 / L2 times
+ * dV^(1/norm)) and the relative error ||b - a|| / ||a||; nan_flags bit 0 / 1 =
+ * NaN in a / b.  allow_diff_grids compares over a's boxes. */
+ocfd_status ocfd_plotfile_compare(const char* file_a, const char* file_b, int32_t norm, int32_t allow_diff_grids,
+                                  int32_t cap, double* abs_err, double* rel_err, int32_t* nan_flags,
+                                  int32_t* nlev, int32_t* ncomp);
 
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops

@@ -1627,6 +1627,59 @@ ocfd_status ocfd_amr_cell_steps(const ocfd_amr* H, int64_t* leaf, int64_t* all) 
 
 int ocfd_amr_launches_per_step(const ocfd_amr* H) { return H ? H->launches : 0; }
 
+ocfd_status ocfd_amr_write_plotfile(ocfd_amr* H, const char* dir, int32_t step, void* stream) {
+    if (!H || !dir) return fail(OCFD_BAD_ARG, "ocfd_amr_write_plotfile");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("ocfd_amr_write_plotfile");
+    StepState s0{};
+    if (cudaMemcpy(&s0, H->lev[0].L->d_step, sizeof(s0), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return check_launch("ocfd_amr_write_plotfile");
+    const double gm1 = H->ctx->host_parm.eos_gamma - 1.;
+    const int ncomp = 9;
+    static const char* names[ncomp] = {"rho", "xmom", "ymom", "zmom", "Eden", "ux", "uy", "uz", "pressure"};
+    std::vector<std::vector<std::vector<double>>> data(H->nlev);
+    std::vector<std::vector<const double*>> ptrs(H->nlev);
+    std::vector<std::vector<ocfd_box>> boxes(H->nlev);
+    std::vector<ocfd_plot_level> lv(H->nlev);
+    for (int l = 0; l < H->nlev; ++l) {
+        ocfd_level* L = H->lev[l].L;
+        std::vector<double> host((size_t)L->elems);
+        if (cudaMemcpy(host.data(), L->buf[0], sizeof(double) * L->elems, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return check_launch("ocfd_amr_write_plotfile");
+        for (size_t b = 0; b < L->boxes.size(); ++b) {
+            const FabGeom& f = L->fabs[b];
+            const long long nc = (long long)(f.hi[0] - f.lo[0] + 1) * (f.hi[1] - f.lo[1] + 1) * (f.hi[2] - f.lo[2] + 1);
+            std::vector<double> v((size_t)nc * ncomp);
+            long long c = 0;
+            for (int k = f.lo[2]; k <= f.hi[2]; ++k)
+                for (int j = f.lo[1]; j <= f.hi[1]; ++j)
+                    for (int i = f.lo[0]; i <= f.hi[0]; ++i, ++c) {
+                        const long long q = fab_index_h(f, i, j, k);
+                        double u[5];
+                        for (int n = 0; n < 5; ++n) u[n] = host[q + n * f.ns];
+                        for (int n = 0; n < 5; ++n) v[n * nc + c] = u[n];
+                        v[5 * nc + c] = u[1] / u[0];
+                        v[6 * nc + c] = u[2] / u[0];
+                        v[7 * nc + c] = u[3] / u[0];
+                        v[8 * nc + c] = gm1 * (u[4] - 0.5 / u[0] * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]));
+                    }
+            data[l].push_back(std::move(v));
+            boxes[l].push_back(L->boxes[b]);
+        }
+        for (auto& v : data[l]) ptrs[l].push_back(v.data());
+        lv[l].nbox = (int32_t)boxes[l].size();
+        lv[l].boxes = boxes[l].data();
+        lv[l].fabs = ptrs[l].data();
+        for (int e = 0; e < 3; ++e) lv[l].dx[e] = H->lev[l].dx[e];
+        lv[l].step = step << l;
+    }
+    double phi[3];
+    for (int e = 0; e < 3; ++e)
+        phi[e] = H->desc.prob_lo[e] + H->desc.dx[e] * (H->desc.domain.hi[e] - H->desc.domain.lo[e] + 1);
+    return ocfd_plotfile_write(dir, H->nlev, lv.data(), ncomp, names, &H->desc.domain, H->desc.prob_lo, phi, 2,
+                               s0.time);
+}
+
 size_t ocfd_amr_state_elems(const ocfd_amr* H, int lev) {
     if (!H || lev < 0 || lev >= H->nlev) return 0;
     return (size_t)H->lev[lev].L->elems;

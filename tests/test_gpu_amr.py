@@ -247,3 +247,38 @@ def test_mixed_form_close_on_hierarchy(ctx):
     assert t0 == pytest.approx(0.01, abs=1e-15) and t1 == pytest.approx(0.01, abs=1e-15)
     l1 = np.abs(a[0] - b[0]).sum() / np.abs(a[0]).sum()
     assert l1 < 1e-4, l1
+
+
+def test_plotfile_of_hierarchy(ctx, tmp_path):
+    """the hierarchy's plotfile holds every level's valid state and the derived
+    ux, uy, uz, pressure; fcompare of the FP32 and FP64 runs on the same grids
+    gives the L1 norm computed from the device data"""
+    import ocfd
+    from ocfd import plotfile
+    from test_plotfile import parse
+    case = small_dmr()
+    runs = {}
+    for flags in (0, ocfd.FLUX_FP32):
+        H = make_hierarchy(ctx, case, regrid_int=0)
+        H.build(case["fab"])
+        H.advance(3, 0.5, flags)
+        p = str(tmp_path / ("plt_%d" % flags))
+        plotfile.write_hierarchy(H, p, step=3)
+        runs[flags] = (p, [H.level_global(l) for l in range(H.nlevels())], H.time()[0])
+    p, glob, t = runs[0]
+    d = parse(p)
+    assert d["names"] == ["rho", "xmom", "ymom", "zmom", "Eden", "ux", "uy", "uz", "pressure"]
+    assert d["finest"] == len(glob) - 1 and d["time"] == t and d["steps"] == [3, 6, 12][:len(glob)]
+    for l, (g, m) in enumerate(glob):
+        for lo, hi, arr in d["data"][l]:
+            sl = (slice(None), slice(lo[2], hi[2] + 1), slice(lo[1], hi[1] + 1), slice(lo[0], hi[0] + 1))
+            U = g[sl]
+            assert np.array_equal(arr[:5], U)
+            assert np.array_equal(arr[5], U[1] / U[0])
+            pres = 0.4 * (U[4] - 0.5 / U[0] * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]))
+            assert np.allclose(arr[8], pres, rtol=1e-15, atol=0)
+    r = plotfile.compare(runs[0][0], runs[ocfd.FLUX_FP32][0], norm=1)
+    for l, ((a, m), (b, _)) in enumerate(zip(runs[0][1], runs[ocfd.FLUX_FP32][1])):
+        l1 = np.abs(b[0][m] - a[0][m]).sum() / np.abs(a[0][m]).sum()
+        assert r["rel"][l, 0] == pytest.approx(l1, rel=1e-9)
+        assert r["rel"][l, 0] < 1e-4
