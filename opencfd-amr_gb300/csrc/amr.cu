@@ -226,12 +226,15 @@ struct RefluxFace {
 struct TimeMix {
     const double* src[4];
     double a[4];
+    // z faces of the coarse level whose outside ghosts are not filled
+    int zvirt, zlo, zhi, zsign[2];
 };
 struct TagGeom {
     int dom_lo[3], dom_hi[3];
     int bs[3], nb[3];  // block size in this level's cells, blocks per direction
     int nbuf;
     double thr;
+    int zvirt;         // z ghosts outside the domain unfilled: rho there equals the boundary cell's
 };
 struct AmrStates {
     StepState* s[OCFD_AMR_MAX_LEVELS];
@@ -278,12 +281,19 @@ __global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __r
                 ck <= T.fhi[2])
                 inside |= 1u << q8;
         }
+        // a z neighbour outside a z face with unfilled ghosts is the parent itself
+        // (the boundary cell and the first mirror cell coincide), signs per BC
+        const bool zl = mix.zvirt && pk - 1 < mix.zlo, zh = mix.zvirt && pk + 1 > mix.zhi;
         for (int n = 0; n < ncomp; ++n) {
             const long long q = c + n * cf.ns;
             const double v0 = mixed(mix, q);
+            const bool flip_l = zl && n >= 1 && n <= 3 && ((mix.zsign[0] >> (n - 1)) & 1);
+            const bool flip_h = zh && n >= 1 && n <= 3 && ((mix.zsign[1] >> (n - 1)) & 1);
+            const double vzm = zl ? (flip_l ? -v0 : v0) : mixed(mix, q - sz);
+            const double vzp = zh ? (flip_h ? -v0 : v0) : mixed(mix, q + sz);
             const double sx_ = mc_slope(mixed(mix, q - 1), v0, mixed(mix, q + 1));
             const double sy_ = mc_slope(mixed(mix, q - sy), v0, mixed(mix, q + sy));
-            const double sz_ = mc_slope(mixed(mix, q - sz), v0, mixed(mix, q + sz));
+            const double sz_ = mc_slope(vzm, v0, vzp);
             double* d = dst + o + n * ff.ns;
 #pragma unroll
             for (int q8 = 0; q8 < 8; ++q8) {
@@ -370,10 +380,12 @@ __global__ void k_tag_dengrad(const FabGeom* __restrict__ lfabs, const long long
         const long long c = fab_index(f, c3[0], c3[1], c3[2]);
         const long long sy = f.g[0], sz = (long long)f.g[0] * f.g[1];
         const double r = U[c];
-        double ax = fabs(U[c + 1] - r), ay = fabs(U[c + sy] - r), az = fabs(U[c + sz] - r);
+        const double rzp = (g.zvirt && c3[2] + 1 > g.dom_hi[2]) ? r : U[c + sz];
+        const double rzm = (g.zvirt && c3[2] - 1 < g.dom_lo[2]) ? r : U[c - sz];
+        double ax = fabs(U[c + 1] - r), ay = fabs(U[c + sy] - r), az = fabs(rzp - r);
         ax = fmax(ax, fabs(r - U[c - 1]));
         ay = fmax(ay, fabs(r - U[c - sy]));
-        az = fmax(az, fabs(r - U[c - sz]));
+        az = fmax(az, fabs(r - rzm));
         if (fmax(ax, fmax(ay, az)) >= g.thr) {
             int lo[3], hi[3];
             for (int d = 0; d < 3; ++d) {
@@ -976,6 +988,11 @@ static ocfd_status launch_cf(ocfd_amr* H, int f, double* dst, const double* a, c
         m.src[q] = (a[q] != 0.0) ? C.L->buf[q] : nullptr;
         if (a[q] != 0.0 && q >= C.L->nbuf) return fail(OCFD_BAD_ARG, "AMR: time interpolation needs a missing buffer");
     }
+    m.zvirt = C.L->zvirt ? 1 : 0;
+    m.zlo = C.dom.lo[2];
+    m.zhi = C.dom.hi[2];
+    m.zsign[0] = C.L->zsign[0];
+    m.zsign[1] = C.L->zsign[1];
     k_cf_interp<<<grid_for(F.cf.total, 128, H->ctx->num_sms), 128, 0, st>>>(
         F.cf.d, F.cf.start, F.cf.n, F.cf.total, F.L->d_fabs, dst, C.L->d_fabs, m, F.L->ncomp);
     ++launches_counter;
@@ -1358,6 +1375,7 @@ static ocfd_status regrid_impl(ocfd_amr* H, int lbase, cudaStream_t st) {
         }
         tg.nbuf = H->desc.n_error_buf;
         tg.thr = H->desc.refine_dengrad;
+        tg.zvirt = A.L->zvirt ? 1 : 0;
         ocfd_level* L = A.L;
         k_tag_dengrad<<<grid_for(L->ncells, 256, H->ctx->num_sms), 256, 0, st>>>(
             L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->buf[0], tg, A.d_blk);

@@ -275,7 +275,7 @@ ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st) {
     return check_launch("level exchange");
 }
 
-ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st) {
+ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st, bool all) {
     const int sms = L->ctx->num_sms;
     if (L->bc_total[0] > 0)
         k_physbc<0><<<grid_for(L->bc_total[0], 256, sms), 256, 0, st>>>(
@@ -283,16 +283,16 @@ ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st)
     if (L->bc_total[1] > 0)
         k_physbc<1><<<grid_for(L->bc_total[1], 256, sms), 256, 0, st>>>(
             L->d_bc[1], L->d_bc_start[1], L->nbc[1], L->bc_total[1], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
-    if (L->bc_total[2] > 0)
+    if (L->bc_total[2] > 0 && (all || !L->zvirt))
         k_physbc<2><<<grid_for(L->bc_total[2], 256, sms), 256, 0, st>>>(
             L->d_bc[2], L->d_bc_start[2], L->nbc[2], L->bc_total[2], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
     return check_launch("level physical BC");
 }
 
-ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st) {
+ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st, bool all) {
     ocfd_status s = fill_exchange(L, U, st);
     if (s != OCFD_OK) return s;
-    return fill_physbc(L, U, tfrac, st);
+    return fill_physbc(L, U, tfrac, st, all);
 }
 
 ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st) {
@@ -366,6 +366,13 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
             r.rk_a = ra[k];
             r.rk_b = rb[k];
             r.dt_ptr = &L->d_step->dt;
+            r.zvirt = L->zvirt ? 1 : 0;
+            r.zdom[0] = desc->domain.lo[2];
+            r.zdom[1] = desc->domain.hi[2];
+            for (int sd = 0; sd < 2; ++sd) {
+                r.zmirror[sd] = L->zmirror[sd];
+                r.zsign[sd] = L->zsign[sd];
+            }
             r.cfl_min = (k == 2 && roles.cfl) ? &L->d_step->cfl_min : nullptr;
             for (int d = 0; d < 3; ++d) {
                 r.dx[d] = desc->dx[d];
@@ -471,6 +478,19 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
         L->bcinfo.prob_lo[d] = desc->prob_lo[d];
     }
     L->bcinfo.bc_case = desc->bc_case;
+    // outflow (foextrap), symmetry / slip wall (reflect, w odd) and no-slip wall
+    // (reflect, u v w odd) take z ghosts from inside the domain, Source/Setup.cpp:22-35;
+    // no case functor writes z faces
+    {
+        const int zb[2] = {desc->lo_bc[2], desc->hi_bc[2]};
+        bool simple = true;
+        for (int sd = 0; sd < 2; ++sd) {
+            simple = simple && zb[sd] >= 2 && zb[sd] <= 5;
+            L->zmirror[sd] = zb[sd] >= 3 ? 1 : 0;
+            L->zsign[sd] = zb[sd] == 5 ? 7 : (zb[sd] >= 3 ? 4 : 0);
+        }
+        L->zvirt = simple;
+    }
     std::memcpy(L->bcinfo.params, desc->case_params, sizeof(L->bcinfo.params));
     // RHS tile: the shape with the least padded work summed over the boxes
     if (desc->tile >= 0 && desc->tile < kNumRegularTiles) {
@@ -583,7 +603,7 @@ ocfd_status ocfd_level_fill_ghosts(ocfd_level* L, double time, void* stream) {
     if (!L) return fail(OCFD_BAD_ARG, "ocfd_level_fill_ghosts");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     k_set_time<<<1, 1, 0, st>>>(L->d_step, time);
-    ocfd_status s = fill_ghosts(L, L->buf[0], 0.0, st);
+    ocfd_status s = fill_ghosts(L, L->buf[0], 0.0, st, true);
     L->need_estdt = true;
     return s;
 }
@@ -658,7 +678,7 @@ ocfd_status ocfd_level_set_stop_time(ocfd_level* L, double stop_time, void* stre
 int ocfd_level_launches_per_step(const ocfd_level* L, unsigned flags) {
     if (!L) return 0;
     (void)flags;
-    int fill = (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0);
+    int fill = (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0 && !L->zvirt);
     return 2 + 3 * (fill + 1);
 }
 

@@ -203,6 +203,10 @@ struct ocfd_level {
     int ntiles = 0;
     ocfd::StepState* d_step = nullptr;
     bool need_estdt = true;
+    // z faces with source-cell BCs on both sides: stepping leaves their outside
+    // ghosts unfilled and the stencils map the loads (RegBoxArgs::zvirt)
+    bool zvirt = false;
+    int zmirror[2] = {0, 0}, zsign[2] = {0, 0};
     // device memory source: nullptr = cudaMalloc / cudaFree (standalone level),
     // else the owning hierarchy's pool (state buffers are then not zeroed)
     ocfd::DevPool* pool = nullptr;
@@ -225,9 +229,10 @@ struct StageRoles {
 };
 
 ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles);
-ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st);
+// fill_physbc skips the z pass of a level with zvirt unless `all`
+ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st, bool all = false);
 ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st);
-ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st);
+ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st, bool all = false);
 ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st);
 ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st);
 ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,

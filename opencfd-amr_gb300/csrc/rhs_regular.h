@@ -46,7 +46,30 @@ struct RegBoxArgs {
     // atomicMin of min(dx_d / (|u_d| + c)) as ordered double bits
     unsigned long long* cfl_min;
     double dx[3];
+    // z faces whose outside ghost cells are not filled (their BC takes values from
+    // inside the domain): stencil loads read the source cell instead - the
+    // boundary cell (foextrap) or the mirror cell (reflect) with the velocity
+    // components of zsign (bit 0/1/2 = u/v/w) negated
+    int zvirt;
+    int zdom[2];
+    int zmirror[2];
+    int zsign[2];
 };
+
+// the cell a load at z index gk reads, and the velocity signs to flip
+__host__ __device__ __forceinline__ int zmap(const RegBoxArgs& B, int gk, int& sign) {
+    sign = 0;
+    if (!B.zvirt) return gk;
+    if (gk < B.zdom[0]) {
+        sign = B.zsign[0];
+        return B.zmirror[0] ? 2 * B.zdom[0] - 1 - gk : B.zdom[0];
+    }
+    if (gk > B.zdom[1]) {
+        sign = B.zsign[1];
+        return B.zmirror[1] ? 2 * B.zdom[1] + 1 - gk : B.zdom[1];
+    }
+    return gk;
+}
 
 // CFL bound dx/(|u|+c) of one conserved state, Source/Advance.cpp:26-49
 __device__ __forceinline__ double cfl_bound(const DevParm& P, const double* u, const double* dx) {

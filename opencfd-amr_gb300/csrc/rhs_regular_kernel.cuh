@@ -289,7 +289,12 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
         if (gi <= B.hi[0] + (D == 0 ? 3 : 0) && gj <= B.hi[1] + (D == 1 ? 3 : 0) &&
             gk <= B.hi[2] + (D == 2 ? 3 : 0)) {
             FT q[7];
-            Prec<FT>::prims(P, B.S, gi, gj, gk, q);
+            int sg;
+            const int gks = D == 2 ? zmap(B, gk, sg) : (sg = 0, gk);
+            Prec<FT>::prims(P, B.S, gi, gj, gks, q);
+            if (sg & 1) q[QU] = -q[QU];
+            if (sg & 2) q[QV] = -q[QV];
+            if (sg & 4) q[QW] = -q[QW];
             Prec<FT>::template split<D>(P, q, fp, fm);
         }
 #pragma unroll
@@ -398,7 +403,13 @@ __global__ void __launch_bounds__(TX* TY* TZ)
             const int rx = c % R::RX, ry = (c / R::RX) % R::RY, rz = c / (R::RX * R::RY);
             const int gi = i0 + rx - 1, gj = j0 + ry - 1, gk = k0 + rz - 1;
             FT q[7] = {0, 0, 0, 0, 0, 1, 0};
-            if (gi <= B.hi[0] + 1 && gj <= B.hi[1] + 1 && gk <= B.hi[2] + 1) Prec<FT>::prims(P, B.S, gi, gj, gk, q);
+            if (gi <= B.hi[0] + 1 && gj <= B.hi[1] + 1 && gk <= B.hi[2] + 1) {
+                int sg;
+                Prec<FT>::prims(P, B.S, gi, gj, zmap(B, gk, sg), q);
+                if (sg & 1) q[QU] = -q[QU];
+                if (sg & 2) q[QV] = -q[QV];
+                if (sg & 4) q[QW] = -q[QW];
+            }
             ring[c] = q[QU];
             ring[R::N + c] = q[QV];
             ring[2 * R::N + c] = q[QW];
