@@ -297,6 +297,40 @@ int ocfd_level_launches_per_step(const ocfd_level* level, unsigned flags);
 ocfd_status ocfd_level_profile_stage(ocfd_level* level, unsigned flags, int reps, double* ms,
                                      void* stream);
 
+/* ------------------------------------------------------- reacting level (GPU)
+ * A level of the multispecies flow with operator-split chemistry, one CUDA graph
+ * per step: n chemistry substeps of dt/(2n), the flow step (RK2 as
+ * Source/CHEM/FlowAdvance.cpp:95-122, or SSP-RK3) with the multispecies RHS of
+ * every box, n substeps of dt/(2n), species renormalisation (EBR::advance CHEM
+ * branch, Source/Advance.cpp:152-177; EBR::post_timestep, Source/EBR.cpp:333-357).
+ * The level's FABs hold 14 components: the 5 conserved then the 9 partial
+ * densities.  dt is fixed (the reference's CHEM time step, Source/Advance.cpp:54-57,
+ * times its CFL number).                                                        */
+typedef struct ocfd_react ocfd_react;
+
+typedef struct ocfd_react_desc {
+    ocfd_level_desc level;
+    int32_t rk_order;        /* 2 (the reference) or 3 */
+    int32_t chem_substeps;   /* per half step; 4 on level 0 (Source/Advance.cpp:159-161) */
+    double dt;
+    uint32_t flags;          /* OCFD_VISC: mixture-averaged viscous and species transport */
+    int32_t binned_chem;     /* 1: chemistry as one launch over all cells ordered by a temperature key */
+} ocfd_react_desc;
+
+ocfd_status ocfd_react_create(ocfd_context* ctx, const ocfd_react_desc* desc, ocfd_react** react);
+ocfd_status ocfd_react_destroy(ocfd_react* react);
+/* The 14-component level: ocfd_level_copy_in / copy_out / time / cells. */
+ocfd_level* ocfd_react_level(ocfd_react* react);
+ocfd_status ocfd_react_advance(ocfd_react* react, int nsteps, void* stream);
+/* Kernels of one step (the captured graph). */
+int ocfd_react_launches_per_step(const ocfd_react* react);
+/* Conserved state of resting mixtures from temperature, pressure and mole
+ * fractions (CKXTY, CKRHOY, CKUBMS as Exec/7_JET/prob.H:46-60 uses them), n
+ * cells, device arrays: T[n], p[n], X[9][n] -> U[5][n] (rho, 0, 0, 0, rho e),
+ * rhoY[9][n]. */
+ocfd_status ocfd_chem_state_tpx(ocfd_context* ctx, int64_t n, const double* T, const double* p, const double* X,
+                                double* U, double* rhoY, void* stream);
+
 /* ---------------------------------------------------- AMR hierarchy (GPU)
  * The per-level path of EBR::advance / EBR::post_timestep run over a whole
  * refined hierarchy with subcycling in time (AMReX Amr::timeStep, ratio 2):

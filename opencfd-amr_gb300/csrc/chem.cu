@@ -6,6 +6,7 @@
 #include <cstring>
 #include <string>
 
+#include "chem_internal.h"
 #include "chem_physics.cuh"
 #include "eb_physics.cuh"
 #include "mechanism.h"
@@ -39,47 +40,20 @@ ocfd_status mech_upload(const ocfd_parm& p) {
     return OCFD_OK;
 }
 
-// Per-thread 9x10 matrix in shared memory, element-major so that the threads
-// of a warp touch consecutive words.
-struct SmemMat {
-    double* base;
-    int stride;
-    __device__ __forceinline__ double& operator()(int r, int c) const { return base[(r * 10 + c) * stride]; }
-};
-
-struct CellBox {
-    int lo[3], n[3];
-    __device__ __forceinline__ long long count() const { return (long long)n[0] * n[1] * n[2]; }
-    __device__ __forceinline__ void cell(long long c, int& i, int& j, int& k) const {
-        i = lo[0] + (int)(c % n[0]);
-        j = lo[1] + (int)((c / n[0]) % n[1]);
-        k = lo[2] + (int)(c / ((long long)n[0] * n[1]));
-    }
-};
-
-constexpr int kChemThreads = 128;
-
-// One semi-implicit chemistry substep per cell, in place: the lambda of
-// EBR::chemical_advance, Source/CHEM/ChemAdvance.cpp:27-82.
-__global__ void __launch_bounds__(kChemThreads) k_chem_advance(View<double> S, View<double> sp, CellBox B,
-                                                               double dt, DevParm P) {
-    extern __shared__ double smem[];
-    const SmemMat U{smem + threadIdx.x, (int)blockDim.x};
-    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (c >= B.count()) return;
-    int i, j, k;
-    B.cell(c, i, j, k);
-    const double rho = dmax(S(i, j, k, 0), P.smallr);
+// One semi-implicit chemistry substep of one cell, in place: the lambda of
+// EBR::chemical_advance, Source/CHEM/ChemAdvance.cpp:27-82.  u = rho, mx, my,
+// mz, E (E updated), r = the 9 partial densities (updated).
+__device__ __forceinline__ void chem_cell(const double* u, double& E, double* r, double dt, const DevParm& P,
+                                          const SmemMat& U) {
+    const double rho = dmax(u[0], P.smallr);
     const double rhoinv = 1.0 / rho;
-    const double ux = S(i, j, k, 1) * rhoinv, uy = S(i, j, k, 2) * rhoinv, uz = S(i, j, k, 3) * rhoinv;
+    const double ux = u[1] * rhoinv, uy = u[2] * rhoinv, uz = u[3] * rhoinv;
     const double kineng = 0.5 * (ux * ux + uy * uy + uz * uz);
-    const double ei = S(i, j, k, 4) - rho * kineng;
-    double r0[NSP], cc[NSP], wdot[NSP], drho[NSP];
+    const double ei = E - rho * kineng;
+    double cc[NSP], wdot[NSP], drho[NSP];
+    const double T = get_t_given_ey(ei, r, P.Ru);
 #pragma unroll
-    for (int n = 0; n < NSP; ++n) r0[n] = sp(i, j, k, n);
-    const double T = get_t_given_ey(ei, r0, P.Ru);
-#pragma unroll
-    for (int n = 0; n < NSP; n++) cc[n] = r0[n] / c_mech.mw[n] * 1e-6;
+    for (int n = 0; n < NSP; n++) cc[n] = r[n] / c_mech.mw[n] * 1e-6;
     for (int a = 0; a < NSP; ++a)
         for (int b = 0; b < NSP; ++b) U(a, b) = 0.0;
     production_rate(wdot, U, cc, T, P.Ru, P.Patm);
@@ -96,13 +70,58 @@ __global__ void __launch_bounds__(kChemThreads) k_chem_advance(View<double> S, V
     double dei = 0;
 #pragma unroll
     for (int n = 0; n < NSP; ++n) {
-        double v = r0[n] + drho[n];
+        double v = r[n] + drho[n];
         if (v < 0) v = 0.0;
-        sp(i, j, k, n) = v;
+        r[n] = v;
     }
 #pragma unroll
     for (int n = 0; n < NSP; ++n) dei += -c_mech.HP[n] * P.Ru / c_mech.mw[n] * drho[n];
-    S(i, j, k, 4) += dei;
+    E += dei;
+}
+
+__global__ void __launch_bounds__(kChemThreads) k_chem_advance(View<double> S, View<double> sp, CellBox B,
+                                                               double dt, DevParm P) {
+    extern __shared__ double smem[];
+    const SmemMat U{smem + threadIdx.x, (int)blockDim.x};
+    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= B.count()) return;
+    int i, j, k;
+    B.cell(c, i, j, k);
+    double u[5], r[NSP];
+#pragma unroll
+    for (int n = 0; n < 5; ++n) u[n] = S(i, j, k, n);
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) r[n] = sp(i, j, k, n);
+    double E = u[4];
+    chem_cell(u, E, r, dt, P, U);
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) sp(i, j, k, n) = r[n];
+    S(i, j, k, 4) = E;
+}
+
+// The same substep over a list of cells of a level (element offset of component
+// 0 and the component stride of each cell's FAB; state then species
+// components): one launch for every box, in the list's order.
+__global__ void __launch_bounds__(kChemThreads) k_chem_advance_list(const long long* __restrict__ off,
+                                                                    const long long* __restrict__ stride,
+                                                                    long long ncell, double* Ubuf, double dt,
+                                                                    DevParm P) {
+    extern __shared__ double smem[];
+    const SmemMat U{smem + threadIdx.x, (int)blockDim.x};
+    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    double* x = Ubuf + off[c];
+    const long long ns = stride[c];
+    double u[5], r[NSP];
+#pragma unroll
+    for (int n = 0; n < 5; ++n) u[n] = x[n * ns];
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) r[n] = x[(5 + n) * ns];
+    double E = u[4];
+    chem_cell(u, E, r, dt, P, U);
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) x[(5 + n) * ns] = r[n];
+    x[4 * ns] = E;
 }
 
 // Species clip and rescale to the mixture density, Source/EBR.cpp:341-355
@@ -126,9 +145,68 @@ __global__ void k_spec_renorm(View<const double> S, View<double> sp, CellBox B) 
 
 ocfd_status configure_chem() {
     if (cudaFuncSetAttribute(k_chem_advance, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(double) * 90 * kChemThreads)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_chem_advance_list, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(double) * 90 * kChemThreads)) != cudaSuccess)
         return check_launch("configure_chem");
     return OCFD_OK;
+}
+
+ocfd_status launch_chem_advance(View<double> S, View<double> sp, const CellBox& B, double dt, const DevParm& P,
+                                cudaStream_t st) {
+    const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+    const int blocks = (int)((n + kChemThreads - 1) / kChemThreads);
+    k_chem_advance<<<blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, st>>>(S, sp, B, dt, P);
+    return check_launch("chemistry substep");
+}
+
+ocfd_status launch_chem_advance_list(const long long* off, const long long* stride, long long ncell, double* U,
+                                     double dt, const DevParm& P, cudaStream_t st) {
+    if (ncell <= 0) return OCFD_OK;
+    const long long blocks = (ncell + kChemThreads - 1) / kChemThreads;
+    k_chem_advance_list<<<(unsigned)blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, st>>>(off, stride, ncell,
+                                                                                                 U, dt, P);
+    return check_launch("chemistry substep (cell list)");
+}
+
+ocfd_status launch_spec_renorm(View<const double> S, View<double> sp, const CellBox& B, int sms, cudaStream_t st) {
+    const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+    long long blocks = (n + 255) / 256;
+    if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+    k_spec_renorm<<<(int)blocks, 256, 0, st>>>(S, sp, B);
+    return check_launch("species renormalisation");
+}
+
+// Conserved state of a resting mixture at (T, p, X): CKXTY, CKRHOY, CKUBMS as
+// the reference's initial conditions use them (Exec/7_JET/prob.H:46-60).
+__global__ void k_chem_state_tpx(long long n, const double* T, const double* p, const double* X, double* U,
+                                 double* rhoY, double Ru) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        double x[NSP], y[NSP], r[NSP];
+#pragma unroll
+        for (int i = 0; i < NSP; ++i) x[i] = X[i * n + c];
+        double XW = 0.0;
+#pragma unroll
+        for (int i = 0; i < NSP; ++i) XW += x[i] * c_mech.mw[i];
+#pragma unroll
+        for (int i = 0; i < NSP; ++i) y[i] = x[i] * c_mech.mw[i] / XW;
+        double YOW = 0, tmp[NSP];
+#pragma unroll
+        for (int i = 0; i < NSP; ++i) tmp[i] = y[i] / c_mech.mw[i];
+#pragma unroll
+        for (int i = 0; i < NSP; ++i) YOW += tmp[i];
+        const double rho = p[c] / (Ru * T[c] * YOW);
+#pragma unroll
+        for (int i = 0; i < NSP; ++i) r[i] = rho * y[i];
+        U[c] = rho;
+        U[n + c] = 0.0;
+        U[2 * n + c] = 0.0;
+        U[3 * n + c] = 0.0;
+        U[4 * n + c] = ckubms(T[c], r, Ru);
+#pragma unroll
+        for (int i = 0; i < NSP; ++i) rhoY[i * n + c] = r[i];
+    }
 }
 
 static CellBox cellbox(const ocfd_box& bx) {
@@ -153,12 +231,8 @@ extern "C" ocfd_status ocfd_chem_advance_box_f64(ocfd_context* ctx, const ocfd_a
     if (!covers(S, bx, 0, 5) || !covers(spec, bx, 0, NSP))
         return fail(OCFD_BAD_ARG, "ocfd_chem_advance_box_f64: S (5 comps) and spec (9 comps) must cover bx");
     if (!(dt >= 0)) return fail(OCFD_BAD_ARG, "ocfd_chem_advance_box_f64: dt must be >= 0");
-    const CellBox B = cellbox(bx);
-    const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
-    const int blocks = (int)((n + kChemThreads - 1) / kChemThreads);
-    k_chem_advance<<<blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, static_cast<cudaStream_t>(stream)>>>(
-        view_of<double>(S), view_of<double>(spec), B, dt, ctx->parm);
-    return check_launch("ocfd_chem_advance_box_f64");
+    return launch_chem_advance(view_of<double>(S), view_of<double>(spec), cellbox(bx), dt, ctx->parm,
+                               static_cast<cudaStream_t>(stream));
 }
 
 extern "C" ocfd_status ocfd_spec_renorm_box_f64(ocfd_context* ctx, const ocfd_array4* S,
@@ -168,13 +242,8 @@ extern "C" ocfd_status ocfd_spec_renorm_box_f64(ocfd_context* ctx, const ocfd_ar
         if (bx.hi[d] < bx.lo[d]) return fail(OCFD_BAD_ARG, "ocfd_spec_renorm_box_f64: empty box");
     if (!covers(S, bx, 0, 1) || !covers(spec, bx, 0, NSP))
         return fail(OCFD_BAD_ARG, "ocfd_spec_renorm_box_f64: S and spec must cover bx");
-    const CellBox B = cellbox(bx);
-    const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
-    long long blocks = (n + 255) / 256;
-    if (blocks > (long long)ctx->num_sms * 16) blocks = (long long)ctx->num_sms * 16;
-    k_spec_renorm<<<(int)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        view_of<const double>(S), view_of<double>(spec), B);
-    return check_launch("ocfd_spec_renorm_box_f64");
+    return launch_spec_renorm(view_of<const double>(S), view_of<double>(spec), cellbox(bx), ctx->num_sms,
+                              static_cast<cudaStream_t>(stream));
 }
 
 // =====================================================================
@@ -191,23 +260,6 @@ extern "C" ocfd_status ocfd_spec_renorm_box_f64(ocfd_context* ctx, const ocfd_ar
 //   k_chem_div      divop for the 5 + 9 components       (Kernels.H:84-97)
 // =====================================================================
 namespace ocfd {
-
-struct ChemBoxArgs {
-    View<const double> S, sp;
-    View<double> dsdt, dsdts;
-    View<double> flux[3], fluxs[3];
-    View<double> q;    // 8 primitives over grow(bx, qg)
-    int qg;            // primitive halo: 3 (WENO, regular boxes) or 2 (MUSCL, cut boxes)
-    View<double> tr;   // mu, lambda, D[9] over grow(bx, 1)
-    int lo[3], hi[3];
-    double dxinv[3];
-    int visc;
-    // cut-cell variant
-    int eb;
-    View<const uint32_t> flag;
-    View<const double> vfrac;
-    View<const double> ap[3];
-};
 
 // c2prim_rgas, Source/kernel/Kernels.H:42-81
 __device__ __forceinline__ void c2prim_real(const DevParm& P, const double* u, const double* rhoi, double* q) {
@@ -546,6 +598,63 @@ static int chem_blocks(long long n, int threads, int sms) {
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
+size_t chem_rhs_scratch_doubles(const ocfd_box& bx) {
+    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
+    const long long qcells = (long long)(n[0] + 6) * (n[1] + 6) * (n[2] + 6);
+    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    long long f = 0;
+    for (int d = 0; d < 3; ++d) f += (long long)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
+    return (size_t)(8 * qcells + 11 * tcells + (5 + NSP) * f);
+}
+
+void chem_rhs_args(ChemBoxArgs& B, View<const double> S, View<const double> sp, View<double> dsdt,
+                   View<double> dsdts, const ocfd_box& bx, const double dxinv[3], bool visc, double* scr) {
+    B = ChemBoxArgs{};
+    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
+    const int g = 3;
+    const long long qcells = (long long)(n[0] + 2 * g) * (n[1] + 2 * g) * (n[2] + 2 * g);
+    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    B.S = S;
+    B.sp = sp;
+    B.dsdt = dsdt;
+    B.dsdts = dsdts;
+    for (int d = 0; d < 3; ++d) {
+        B.lo[d] = bx.lo[d];
+        B.hi[d] = bx.hi[d];
+        B.dxinv[d] = dxinv[d];
+    }
+    B.q = View<double>{scr, n[0] + 2 * g, (long long)(n[0] + 2 * g) * (n[1] + 2 * g), qcells, bx.lo[0] - g,
+                       bx.lo[1] - g, bx.lo[2] - g};
+    B.qg = g;
+    scr += 8 * qcells;
+    B.tr = View<double>{scr, n[0] + 2, (long long)(n[0] + 2) * (n[1] + 2), tcells, bx.lo[0] - 1, bx.lo[1] - 1,
+                        bx.lo[2] - 1};
+    scr += 11 * tcells;
+    for (int d = 0; d < 3; ++d) {
+        const int sx = n[0] + (d == 0), sy = n[1] + (d == 1);
+        const long long fc = (long long)sx * sy * (n[2] + (d == 2));
+        B.flux[d] = View<double>{scr, sx, (long long)sx * sy, fc, bx.lo[0], bx.lo[1], bx.lo[2]};
+        scr += 5 * fc;
+        B.fluxs[d] = View<double>{scr, sx, (long long)sx * sy, fc, bx.lo[0], bx.lo[1], bx.lo[2]};
+        scr += NSP * fc;
+    }
+    B.visc = visc ? 1 : 0;
+}
+
+// the kernel chain of one regular box (regular branch of compute_dSdt_multi)
+ocfd_status launch_chem_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cudaStream_t st) {
+    const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
+    const long long qcells = (long long)(n[0] + 2 * B.qg) * (n[1] + 2 * B.qg) * (n[2] + 2 * B.qg);
+    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    k_chem_prims<<<chem_blocks(qcells, 128, sms), 128, 0, st>>>(B, P);
+    if (B.visc) k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
+    k_chem_faces<0><<<chem_blocks((long long)(n[0] + 1) * n[1] * n[2], 128, sms), 128, 0, st>>>(B, P);
+    k_chem_faces<1><<<chem_blocks((long long)n[0] * (n[1] + 1) * n[2], 128, sms), 128, 0, st>>>(B, P);
+    k_chem_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, P);
+    k_chem_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
+    return check_launch("multispecies RHS");
+}
+
 // Shared set-up of the regular and cut-cell multispecies box calls.
 static ocfd_status chem_box_setup(ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* spec,
                                   const ocfd_array4* dSdt, const ocfd_array4* dSdt_spec,
@@ -624,18 +733,19 @@ extern "C" ocfd_status ocfd_rhs_chem_box_f64(ocfd_context* ctx, const ocfd_array
     ocfd_status s = chem_box_setup(ctx, S, spec, dSdt, dSdt_spec, flux, flux_spec, bx, dxinv, flags, 3,
                                    "ocfd_rhs_chem_box_f64", B);
     if (s != OCFD_OK) return s;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int sms = ctx->num_sms;
-    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
-    const long long qcells = (long long)(n[0] + 2 * B.qg) * (n[1] + 2 * B.qg) * (n[2] + 2 * B.qg);
-    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
-    k_chem_prims<<<chem_blocks(qcells, 128, sms), 128, 0, st>>>(B, ctx->parm);
-    if (B.visc) k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
-    k_chem_faces<0><<<chem_blocks((long long)(n[0] + 1) * n[1] * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
-    k_chem_faces<1><<<chem_blocks((long long)n[0] * (n[1] + 1) * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
-    k_chem_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, ctx->parm);
-    k_chem_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
-    return check_launch("ocfd_rhs_chem_box_f64");
+    return launch_chem_rhs(B, ctx->parm, ctx->num_sms, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" ocfd_status ocfd_chem_state_tpx(ocfd_context* ctx, int64_t n, const double* T, const double* p,
+                                           const double* X, double* U, double* rhoY, void* stream) {
+    using namespace ocfd;
+    if (!ctx || n < 0 || (n > 0 && (!T || !p || !X || !U || !rhoY)))
+        return fail(OCFD_BAD_ARG, "ocfd_chem_state_tpx: bad arguments");
+    if (n == 0) return OCFD_OK;
+    long long blocks = (n + 255) / 256;
+    if (blocks > (long long)ctx->num_sms * 16) blocks = (long long)ctx->num_sms * 16;
+    k_chem_state_tpx<<<(int)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(n, T, p, X, U, rhoY, ctx->parm.Ru);
+    return check_launch("ocfd_chem_state_tpx");
 }
 
 extern "C" ocfd_status ocfd_rhs_chem_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S,

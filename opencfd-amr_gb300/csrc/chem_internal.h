@@ -1,0 +1,61 @@
+// Multispecies internals shared by chem.cu (kernels) and react.cu (the
+// reacting level driver).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mechanism.h"
+#include "ocfd_internal.h"
+
+namespace ocfd {
+
+constexpr int kChemThreads = 128;
+
+// Per-thread 9x10 matrix in shared memory, element-major so that the threads
+// of a warp touch consecutive words.
+struct SmemMat {
+    double* base;
+    int stride;
+    __device__ __forceinline__ double& operator()(int r, int c) const { return base[(r * 10 + c) * stride]; }
+};
+
+struct CellBox {
+    int lo[3], n[3];
+    __host__ __device__ __forceinline__ long long count() const { return (long long)n[0] * n[1] * n[2]; }
+    __device__ __forceinline__ void cell(long long c, int& i, int& j, int& k) const {
+        i = lo[0] + (int)(c % n[0]);
+        j = lo[1] + (int)((c / n[0]) % n[1]);
+        k = lo[2] + (int)(c / ((long long)n[0] * n[1]));
+    }
+};
+
+struct ChemBoxArgs {
+    View<const double> S, sp;
+    View<double> dsdt, dsdts;
+    View<double> flux[3], fluxs[3];
+    View<double> q;    // 8 primitives over grow(bx, qg)
+    int qg;            // primitive halo: 3 (WENO, regular boxes) or 2 (MUSCL, cut boxes)
+    View<double> tr;   // mu, lambda, D[9] over grow(bx, 1)
+    int lo[3], hi[3];
+    double dxinv[3];
+    int visc;
+    // cut-cell variant
+    int eb;
+    View<const uint32_t> flag;
+    View<const double> vfrac;
+    View<const double> ap[3];
+};
+
+// Scratch (doubles) of one regular box's multispecies RHS without external
+// face arrays, and the argument block carving it.
+size_t chem_rhs_scratch_doubles(const ocfd_box& bx);
+void chem_rhs_args(ChemBoxArgs& B, View<const double> S, View<const double> sp, View<double> dsdt,
+                   View<double> dsdts, const ocfd_box& bx, const double dxinv[3], bool visc, double* scr);
+ocfd_status launch_chem_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cudaStream_t st);
+ocfd_status launch_chem_advance(View<double> S, View<double> sp, const CellBox& B, double dt, const DevParm& P,
+                                cudaStream_t st);
+ocfd_status launch_chem_advance_list(const long long* off, const long long* stride, long long ncell, double* U,
+                                     double dt, const DevParm& P, cudaStream_t st);
+ocfd_status launch_spec_renorm(View<const double> S, View<double> sp, const CellBox& B, int sms, cudaStream_t st);
+
+}  // namespace ocfd

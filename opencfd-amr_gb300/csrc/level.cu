@@ -410,7 +410,7 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
 // Everything of a level but its stage tables: FABs, state buffers, exchange and
 // physical-BC tags, RHS tile choice, step state.
 ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
-                        DevPool* pool) {
+                        DevPool* pool, int ncomp) {
     if (!ctx || !desc || !out || desc->nbox <= 0 || !desc->boxes || nbuf < 3 || nbuf > 4)
         return fail(OCFD_BAD_ARG, "ocfd_level_create: bad arguments");
     *out = nullptr;
@@ -426,6 +426,7 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
     L->desc = *desc;
     L->nbuf = nbuf;
     L->pool = pool;
+    L->ncomp = ncomp;
     L->boxes.assign(desc->boxes, desc->boxes + desc->nbox);
     L->desc.boxes = nullptr;
     long long off = 0;

@@ -236,7 +236,7 @@ ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st,
 ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st);
 ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st);
 ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
-                        DevPool* pool = nullptr);
+                        DevPool* pool = nullptr, int ncomp = 5);
 __global__ void k_set_time(StepState* st, double t);
 
 }  // namespace ocfd

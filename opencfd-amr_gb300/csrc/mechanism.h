@@ -19,6 +19,8 @@ struct MechTables {
     double diff[45 * 5];
 };
 
+// The built-in tables (Source/Constants.cpp:15-150).
+void mech_builtin(MechTables* t);
 // Points the CHEM table members of `p` at the library's host copies of the
 // reference's Source/Constants.cpp:15-150 data.
 void mech_host_tables(ocfd_parm* p);

@@ -1,0 +1,345 @@
+// Reacting level: the multispecies flow of Source/CHEM with operator-split
+// chemistry, on the device, one CUDA graph per step (EBR::advance, CHEM branch,
+// Source/Advance.cpp:152-177, and EBR::post_timestep, Source/EBR.cpp:333-357):
+//
+//   chemistry half step : n substeps of dt / (2 n)   (EBR::chemical_advance)
+//   flow step           : RK2 (Source/CHEM/FlowAdvance.cpp:95-122) or SSP-RK3,
+//                         each stage = ghost fill of 5 + 9 components, the
+//                         multispecies RHS chain per box, one combine kernel
+//                         U_out = a U^n + b (U_s + dt L(U_s)) over the level
+//   chemistry half step
+//   species renormalisation
+//
+// State FABs hold 14 components: rho, rho u, rho v, rho w, rho E, then the 9
+// partial densities (the Spec MultiFab of the reference) in the same FAB.
+// Chemistry either runs per box, or (binned) as one launch over a list of all
+// the level's cells ordered by a temperature key, so that the warps' Newton
+// iterations for T(e) see similar states (the per-cell arithmetic is the same
+// function, so results do not depend on the order).
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "chem_internal.h"
+#include "level.h"
+
+namespace ocfd {
+
+constexpr int NCOMP_REACT = 5 + NSP;
+constexpr int NBIN = 32;
+
+__global__ void k_react_combine(const FabGeom* __restrict__ fabs, const long long* __restrict__ start, int nbox,
+                                long long total, double* out, const double* __restrict__ U0,
+                                const double* __restrict__ S, const double* __restrict__ R, double a, double b,
+                                const StepState* st) {
+    const double dt = st->dt;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int bx = find_tag<FabGeom>(start, nbox, idx);
+        const FabGeom& f = fabs[bx];
+        int i, j, k;
+        region_cell(f.lo, f.hi, idx - start[bx], i, j, k);
+        const long long c = fab_index(f, i, j, k);
+        for (int n = 0; n < NCOMP_REACT; ++n) {
+            const long long q = c + n * f.ns;
+            out[q] = a * U0[q] + b * (S[q] + dt * R[q]);
+        }
+    }
+}
+
+// temperature key: the linear estimate e / sum((a0 - 1) R / W_i rho_i) that
+// starts the Newton iteration for T(e) (LiDryer.H:833-888), in 100 K bins
+__global__ void k_react_keys(const FabGeom* __restrict__ fabs, const long long* __restrict__ start, int nbox,
+                             long long total, const double* __restrict__ U, const double* __restrict__ a0w,
+                             unsigned char* key, unsigned* count) {
+    __shared__ unsigned hist[NBIN];
+    for (int q = threadIdx.x; q < NBIN; q += blockDim.x) hist[q] = 0;
+    __syncthreads();
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int bx = find_tag<FabGeom>(start, nbox, idx);
+        const FabGeom& f = fabs[bx];
+        int i, j, k;
+        region_cell(f.lo, f.hi, idx - start[bx], i, j, k);
+        const long long c = fab_index(f, i, j, k);
+        const double rho = U[c];
+        const double ke = 0.5 * (U[c + f.ns] * U[c + f.ns] + U[c + 2 * f.ns] * U[c + 2 * f.ns] +
+                                 U[c + 3 * f.ns] * U[c + 3 * f.ns]) / rho;
+        double As = 0.0;
+        for (int n = 0; n < NSP; ++n) As += a0w[n] * U[c + (5 + n) * f.ns];
+        const double T = (U[c + 4 * f.ns] - ke) / As;
+        int b = (int)(T * 0.01);
+        b = b < 0 ? 0 : (b >= NBIN ? NBIN - 1 : b);
+        key[idx] = (unsigned char)b;
+        atomicAdd(&hist[b], 1u);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < NBIN; q += blockDim.x)
+        if (hist[q]) atomicAdd(&count[q], hist[q]);
+}
+
+__global__ void k_react_scan(unsigned* count) {
+    unsigned acc = 0;
+    for (int q = 0; q < NBIN; ++q) {
+        const unsigned c = count[q];
+        count[q] = acc;  // becomes the cursor of bin q
+        acc += c;
+    }
+}
+
+__global__ void k_react_scatter(const FabGeom* __restrict__ fabs, const long long* __restrict__ start, int nbox,
+                                long long total, const unsigned char* __restrict__ key, unsigned* cursor,
+                                long long* off, long long* stride) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int bx = find_tag<FabGeom>(start, nbox, idx);
+        const FabGeom& f = fabs[bx];
+        int i, j, k;
+        region_cell(f.lo, f.hi, idx - start[bx], i, j, k);
+        const unsigned pos = atomicAdd(&cursor[key[idx]], 1u);
+        off[pos] = fab_index(f, i, j, k);
+        stride[pos] = f.ns;
+    }
+}
+
+__global__ void k_react_begin(StepState* st, double dt) {
+    st->dt = dt;
+}
+
+__global__ void k_react_end(StepState* st) {
+    st->time += st->dt;
+    st->dt_prev = st->dt;
+}
+
+}  // namespace ocfd
+
+struct ocfd_react {
+    ocfd_context* ctx = nullptr;
+    ocfd_react_desc desc{};
+    ocfd_level* L = nullptr;     // 14-component FABs: A (U^n), B, C
+    double* rhs = nullptr;       // L(U_s), same FAB layout
+    double* scr = nullptr;       // multispecies RHS scratch of the largest box
+    std::vector<ocfd::ChemBoxArgs> args[3];  // RHS chain of each box, per stage input buffer
+    // binned chemistry
+    unsigned char* key = nullptr;
+    unsigned* count = nullptr;
+    long long* off = nullptr;
+    long long* stride = nullptr;
+    double* a0w = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    unsigned graph_flags = ~0u;
+    int launches = 0;
+};
+
+namespace ocfd {
+
+static ocfd_array4 fab_view(const ocfd_level* L, double* base, int b, int comp0, int ncomp) {
+    const FabGeom& f = L->fabs[b];
+    ocfd_array4 a{};
+    a.p = base + f.off + comp0 * f.ns;
+    a.jstride = f.g[0];
+    a.kstride = (long long)f.g[0] * f.g[1];
+    a.nstride = f.ns;
+    for (int d = 0; d < 3; ++d) {
+        a.begin[d] = f.lo[d] - NGR;
+        a.end[d] = f.hi[d] + NGR + 1;
+    }
+    a.ncomp = ncomp;
+    return a;
+}
+
+static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
+    ocfd_level* L = R->L;
+    const double dt2 = 0.5 * R->desc.dt / R->desc.chem_substeps;
+    const int sms = R->ctx->num_sms;
+    if (R->desc.binned_chem) {
+        cudaMemsetAsync(R->count, 0, sizeof(unsigned) * NBIN, st);
+        k_react_keys<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(L->d_fabs, L->d_cell_start, (int)L->boxes.size(),
+                                                                   L->ncells, L->buf[0], R->a0w, R->key, R->count);
+        k_react_scan<<<1, 1, 0, st>>>(R->count);
+        k_react_scatter<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(
+            L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, R->key, R->count, R->off, R->stride);
+        launches += 3;
+        for (int s = 0; s < R->desc.chem_substeps; ++s) {
+            ocfd_status r = launch_chem_advance_list(R->off, R->stride, L->ncells, L->buf[0], dt2, R->ctx->parm, st);
+            if (r != OCFD_OK) return r;
+            ++launches;
+        }
+        return OCFD_OK;
+    }
+    for (int s = 0; s < R->desc.chem_substeps; ++s)
+        for (size_t b = 0; b < L->boxes.size(); ++b) {
+            ocfd_array4 S = fab_view(L, L->buf[0], (int)b, 0, 5), sp = fab_view(L, L->buf[0], (int)b, 5, NSP);
+            CellBox cb{};
+            for (int d = 0; d < 3; ++d) {
+                cb.lo[d] = L->boxes[b].lo[d];
+                cb.n[d] = L->boxes[b].hi[d] - L->boxes[b].lo[d] + 1;
+            }
+            ocfd_status r = launch_chem_advance(view_of<double>(&S), view_of<double>(&sp), cb, dt2, R->ctx->parm, st);
+            if (r != OCFD_OK) return r;
+            ++launches;
+        }
+    return OCFD_OK;
+}
+
+static ocfd_status record_react_step(ocfd_react* R, unsigned flags, cudaStream_t st) {
+    (void)flags;
+    ocfd_level* L = R->L;
+    int launches = 0;
+    k_react_begin<<<1, 1, 0, st>>>(L->d_step, R->desc.dt);
+    ++launches;
+    ocfd_status s = chem_half(R, st, launches);
+    if (s != OCFD_OK) return s;
+    // flow: stage k reads buffer in[k], writes out[k] = a U^n + b (in + dt L(in))
+    const bool rk3 = R->desc.rk_order == 3;
+    const int nst = rk3 ? 3 : 2;
+    const int in3[3] = {0, 1, 2}, out3[3] = {1, 2, 0};
+    const int in2[2] = {0, 1}, out2[2] = {1, 0};
+    const double a3[3] = {0.0, 0.75, 1.0 / 3.0}, b3[3] = {1.0, 0.25, 2.0 / 3.0};
+    const double a2[2] = {0.0, 0.5}, b2[2] = {1.0, 0.5};
+    const double tf3[3] = {0.0, 1.0, 0.5}, tf2[2] = {0.0, 1.0};
+    const int sms = R->ctx->num_sms;
+    for (int k = 0; k < nst && s == OCFD_OK; ++k) {
+        const int in = rk3 ? in3[k] : in2[k], out = rk3 ? out3[k] : out2[k];
+        s = fill_ghosts(L, L->buf[in], rk3 ? tf3[k] : tf2[k], st, true);
+        launches += (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0);
+        for (size_t b = 0; b < L->boxes.size() && s == OCFD_OK; ++b) {
+            s = launch_chem_rhs(R->args[in][b], R->ctx->parm, sms, st);
+            launches += R->args[in][b].visc ? 6 : 5;
+        }
+        if (s != OCFD_OK) break;
+        k_react_combine<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(
+            L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->buf[out], L->buf[0], L->buf[in], R->rhs,
+            rk3 ? a3[k] : a2[k], rk3 ? b3[k] : b2[k], L->d_step);
+        ++launches;
+        s = check_launch("reacting flow stage");
+    }
+    if (s != OCFD_OK) return s;
+    s = chem_half(R, st, launches);
+    if (s != OCFD_OK) return s;
+    for (size_t b = 0; b < L->boxes.size(); ++b) {
+        ocfd_array4 S = fab_view(L, L->buf[0], (int)b, 0, 5), sp = fab_view(L, L->buf[0], (int)b, 5, NSP);
+        CellBox cb{};
+        for (int d = 0; d < 3; ++d) {
+            cb.lo[d] = L->boxes[b].lo[d];
+            cb.n[d] = L->boxes[b].hi[d] - L->boxes[b].lo[d] + 1;
+        }
+        s = launch_spec_renorm(view_of<const double>(&S), view_of<double>(&sp), cb, sms, st);
+        if (s != OCFD_OK) return s;
+        ++launches;
+    }
+    k_react_end<<<1, 1, 0, st>>>(L->d_step);
+    ++launches;
+    R->launches = launches;
+    return check_launch("reacting step");
+}
+
+}  // namespace ocfd
+
+using namespace ocfd;
+
+extern "C" {
+
+ocfd_status ocfd_react_create(ocfd_context* ctx, const ocfd_react_desc* desc, ocfd_react** out) {
+    if (!ctx || !desc || !out) return fail(OCFD_BAD_ARG, "ocfd_react_create: bad arguments");
+    *out = nullptr;
+    if (desc->rk_order != 2 && desc->rk_order != 3) return fail(OCFD_BAD_ARG, "ocfd_react_create: rk_order is 2 or 3");
+    if (desc->chem_substeps < 0 || !(desc->dt > 0)) return fail(OCFD_BAD_ARG, "ocfd_react_create: substeps / dt");
+    ocfd_react* R = new ocfd_react();
+    R->ctx = ctx;
+    R->desc = *desc;
+    R->desc.level.boxes = nullptr;
+    ocfd_status s = level_alloc(ctx, &desc->level, 3, &R->L, nullptr, NCOMP_REACT);
+    if (s != OCFD_OK) {
+        delete R;
+        return s;
+    }
+    ocfd_level* L = R->L;
+    size_t scr = 0;
+    for (const ocfd_box& b : L->boxes) scr = std::max(scr, chem_rhs_scratch_doubles(b));
+    if (cudaMalloc(&R->rhs, sizeof(double) * L->elems) != cudaSuccess ||
+        cudaMalloc(&R->scr, sizeof(double) * scr) != cudaSuccess ||
+        cudaMalloc(&R->key, std::max<long long>(1, L->ncells)) != cudaSuccess ||
+        cudaMalloc(&R->count, sizeof(unsigned) * NBIN) != cudaSuccess ||
+        cudaMalloc(&R->off, sizeof(long long) * std::max<long long>(1, L->ncells)) != cudaSuccess ||
+        cudaMalloc(&R->stride, sizeof(long long) * std::max<long long>(1, L->ncells)) != cudaSuccess ||
+        cudaMalloc(&R->a0w, sizeof(double) * NSP) != cudaSuccess) {
+        cudaGetLastError();
+        ocfd_react_destroy(R);
+        return fail(OCFD_OUT_OF_MEMORY, "ocfd_react_create: buffers");
+    }
+    cudaMemset(R->rhs, 0, sizeof(double) * L->elems);
+    // (a0 - 1) Ru / W_i of the Newton start (LiDryer.H:833-888)
+    {
+        MechTables t;
+        mech_builtin(&t);
+        ocfd_parm hp = ctx->host_parm;
+        double a0w[NSP];
+        for (int n = 0; n < NSP; ++n) a0w[n] = t.A0[n] * hp.Ru / t.mw[n];
+        cudaMemcpy(R->a0w, a0w, sizeof(a0w), cudaMemcpyHostToDevice);
+    }
+    const double dxinv[3] = {1.0 / desc->level.dx[0], 1.0 / desc->level.dx[1], 1.0 / desc->level.dx[2]};
+    for (int in = 0; in < 3; ++in)
+        for (size_t b = 0; b < L->boxes.size(); ++b) {
+            ocfd_array4 S = fab_view(L, L->buf[in], (int)b, 0, 5), sp = fab_view(L, L->buf[in], (int)b, 5, NSP);
+            ocfd_array4 d = fab_view(L, R->rhs, (int)b, 0, 5), ds = fab_view(L, R->rhs, (int)b, 5, NSP);
+            ChemBoxArgs A{};
+            chem_rhs_args(A, view_of<const double>(&S), view_of<const double>(&sp), view_of<double>(&d),
+                          view_of<double>(&ds), L->boxes[b], dxinv, (desc->flags & OCFD_VISC) != 0, R->scr);
+            R->args[in].push_back(A);
+        }
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        ocfd_react_destroy(R);
+        return check_launch("ocfd_react_create");
+    }
+    *out = R;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_react_destroy(ocfd_react* R) {
+    if (!R) return OCFD_OK;
+    if (R->graph) cudaGraphExecDestroy(R->graph);
+    cudaFree(R->rhs);
+    cudaFree(R->scr);
+    cudaFree(R->key);
+    cudaFree(R->count);
+    cudaFree(R->off);
+    cudaFree(R->stride);
+    cudaFree(R->a0w);
+    if (R->L) ocfd_level_destroy(R->L);
+    delete R;
+    return OCFD_OK;
+}
+
+ocfd_level* ocfd_react_level(ocfd_react* R) { return R ? R->L : nullptr; }
+
+ocfd_status ocfd_react_advance(ocfd_react* R, int nsteps, void* stream) {
+    if (!R || nsteps < 0) return fail(OCFD_BAD_ARG, "ocfd_react_advance");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (nsteps == 0) return OCFD_OK;
+    if (!R->graph) {
+        cudaStream_t cap;
+        if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return check_launch("capture stream");
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            return check_launch("begin capture");
+        }
+        ocfd_status s = record_react_step(R, 0, cap);
+        cudaError_t e = cudaStreamEndCapture(cap, &g);
+        cudaStreamDestroy(cap);
+        if (s != OCFD_OK) return s;
+        if (e != cudaSuccess) return fail(OCFD_LAUNCH_FAIL, std::string("end capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&R->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(OCFD_LAUNCH_FAIL, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    for (int i = 0; i < nsteps; ++i)
+        if (cudaGraphLaunch(R->graph, st) != cudaSuccess) return check_launch("reacting graph launch");
+    return OCFD_OK;
+}
+
+int ocfd_react_launches_per_step(const ocfd_react* R) { return R ? R->launches : 0; }
+
+}  // extern "C"

@@ -100,3 +100,38 @@ def dmr_amr(nx=1024, ny=256, nz=2, max_level=2, blocking_factor=32, max_grid=128
                 blocking_factor=(blocking_factor,) * 3, max_grid_size=(max_grid,) * 3,
                 n_error_buf=n_error_buf, refine_dengrad=refine_dengrad, regrid_int=regrid_int,
                 fab=lambda lev, lo, hi, d: dmr_fab(lo, hi, d, gamma))
+
+
+# Species order of the mechanism: H2, O2, H2O, H, O, OH, HO2, H2O2, N2
+PHI1_AIR_X = (0.2958, 0.1479, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.5563)
+
+
+def hot_spot_temperature(n=128, length=0.01, seed=20261203, nspots=8, t0=1200.0, dT=600.0, radius_cells=6.0):
+    """Temperature over the grown periodic box (nz+8, ny+8, nx+8): t0 plus 8
+    Gaussian hot spots dT * exp(-(r / (6 dx))^2) at centres drawn from
+    MT19937(seed), periodic minimum-image distances."""
+    dx = length / n
+    rng = np.random.Generator(np.random.MT19937(seed))
+    centres = rng.uniform(0.0, length, size=(nspots, 3))
+    x = (np.arange(-NG, n + NG) + 0.5) * dx
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    T = np.full(Z.shape, t0)
+    for cx, cy, cz in centres:
+        d2 = 0.0
+        for coord, c in ((X, cx), (Y, cy), (Z, cz)):
+            d = np.abs(coord - c)
+            d = np.minimum(d, length - d)
+            d2 = d2 + d * d
+        T += dT * np.exp(-d2 / (radius_cells * dx) ** 2)
+    return T, dx, centres
+
+
+def react_cube(ctx, n=128, length=0.01, seed=20261203, p=101325.0):
+    """configs[2]: premixed phi = 1 H2/air at 1 atm, 1200 K with 8 seeded hot
+    spots, periodic cube of n^3 cells and edge `length`; the grown global state
+    (14, n+8, n+8, n+8): conserved variables then partial densities."""
+    from .react import state_tpx
+    T, dx, centres = hot_spot_temperature(n, length, seed)
+    X = np.array(PHI1_AIR_X)[:, None, None, None] * np.ones((1,) + T.shape)
+    G = state_tpx(ctx, T, p, X)
+    return dict(G=G, n=(n, n, n), dx=(dx, dx, dx), T=T, centres=centres, seed=seed, length=length)
