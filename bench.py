@@ -212,8 +212,21 @@ def cpu_sample_workload(config):
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    c = cpu_sample_workload(args.config)
     threads = os.cpu_count() or 1
+    if args.config == "react":
+        dt, ncs = react_cpu_sample(64, 1, threads)
+        v = ncs / dt
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": args.gpus,
+            "steps": 1, "warmup": 0, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3D H2/air reacting box (sample 64^3 of the 128^3 workload)", "form": "fp64"},
+            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": "1 Strang step of a periodic 64^3 sample, oracle restatement (OpenMP)"},
+            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+            flush=True)
+        return
+    c = cpu_sample_workload(args.config)
     # bounded: warm-up steps then K timed steps, each a full-domain RK3 step
     cpu_time_steps(c, max(1, min(args.warmup, 2)), threads)
     dt, cells = cpu_time_steps(c, args.steps, threads)
@@ -422,6 +435,188 @@ def run_ours_amr(args, world, rank, local):
     ctx.close()
 
 
+REACT_N = 128
+REACT_DT = 1e-8
+
+
+def react_cpu_sample(n=64, steps=1, threads=None):
+    """CPU leg of the reacting workload: the oracle port (OpenMP) of one Strang
+    step (4 + 4 chemistry substeps, RK2 with the multispecies RHS, species
+    renormalisation) on a periodic n^3 sample with the workload's cell size.
+    Returns (seconds, cells x steps)."""
+    import numpy as np
+    from oracle import BCStruct, Oracle
+    from ocfd.cases import PHI1_AIR_X, hot_spot_temperature
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = Oracle(openmp=True)
+    NG = 4
+    T, dxs, _ = hot_spot_temperature(n, 0.01 * n / REACT_N)
+    dx = (dxs, dxs, dxs)
+    y = o.ckxty(np.array(PHI1_AIR_X))
+    S = np.zeros((5,) + T.shape)
+    sp = np.zeros((9,) + T.shape)
+    flatT = T.ravel()
+    for c in range(flatT.size):
+        rho = o.ckrhoy(101325.0, flatT[c], y)
+        r = rho * y
+        idx = np.unravel_index(c, T.shape)
+        S[(0,) + idx] = rho
+        S[(4,) + idx] = o.ckubms(flatT[c], r)
+        sp[(slice(None),) + idx] = r
+    bc = BCStruct()
+    bc.dx[:] = list(dx)
+    bc.dom_hi[:] = [n - 1] * 3
+    inner = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
+    dt = REACT_DT
+
+    def chem_half(S, sp):
+        for _ in range(4):
+            a = np.ascontiguousarray(S[inner].reshape(5, -1))
+            b = np.ascontiguousarray(sp[inner].reshape(9, -1))
+            o.chem_advance(a, b, 0.5 * dt / 4)
+            S[inner] = a.reshape(S[inner].shape)
+            sp[inner] = b.reshape(sp[inner].shape)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        chem_half(S, sp)
+        U0, V0 = S.copy(), sp.copy()
+        Us, Vs = S, sp
+        for a, b in ((0.0, 1.0), (0.5, 0.5)):
+            o.fill_ghosts(bc, Us)
+            o.fill_ghosts(bc, Vs)
+            dS, dSs, *_ = o.rhs_chem(Us, Vs, tuple(1.0 / x for x in dx), do_visc=True)
+            Un, Vn = Us.copy(), Vs.copy()
+            Un[inner] = a * U0[inner] + b * (Us[inner] + dt * dS)
+            Vn[inner] = a * V0[inner] + b * (Vs[inner] + dt * dSs)
+            Us, Vs = Un, Vn
+        S, sp = Us, Vs
+        chem_half(S, sp)
+        a = np.ascontiguousarray(S[inner].reshape(5, -1))
+        b = np.ascontiguousarray(sp[inner].reshape(9, -1))
+        o.spec_renorm(a, b)
+        sp[inner] = b.reshape(sp[inner].shape)
+    return time.perf_counter() - t0, n ** 3 * steps
+
+
+def run_ours_react(args, world, rank, local):
+    """configs[2]: 128^3 periodic H2/air with 8 hot spots, Strang chemistry around
+    the RK2 multispecies flow step, dt = 1e-8 s."""
+    import numpy as np
+    import torch
+    import ocfd
+    from ocfd.cases import react_cube
+    from ocfd.level import chop_domain
+    from ocfd.react import Reactor
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = ocfd.Context(device=local)
+    case = react_cube(ctx, n=REACT_N)
+    n = case["n"]
+    boxes = chop_domain(n, 64)
+    cells = n[0] * n[1] * n[2]
+    stream = torch.cuda.current_stream(dev)
+    l2flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def make(binned, rk=2):
+        R = Reactor(ctx, boxes, tuple(x - 1 for x in n), case["dx"], dt=REACT_DT, rk_order=rk, chem_substeps=4,
+                    visc=True, binned=binned)
+        R.level.set_global(case["G"])
+        return R
+
+    def timed(binned):
+        R = make(binned)
+        R.advance(args.warmup)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for e0, e1 in ev:
+            l2flush.fill_(1.0)
+            e0.record(stream)
+            R.advance(1)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
+        return ms, R
+
+    ms_plain, Rp = timed(False)
+    with ClockSampler(local) as clk:
+        ms_bin, Rb = timed(True)
+    value = cells * args.steps * world / (ms_bin * 1e-3)
+    value_plain = cells * args.steps * world / (ms_plain * 1e-3)
+    same_steps = args.warmup + args.steps
+    a = Rp.level.get_global()
+    b = Rb.level.get_global()
+    identical = bool(np.array_equal(a, b))
+    chem_ms = Rb.profile_chem(reps=3)
+    launches = Rb.launches_per_step()
+    Rp.close()
+    # RK3 beside the reference's RK2 after the same number of steps
+    R3 = make(False, rk=3)
+    R3.advance(same_steps)
+    c3 = R3.level.get_global()
+    R3.close()
+    y = lambda U, s: U[5 + s] / U[0]
+    l1 = lambda x, y_: float(np.abs(x - y_).sum() / np.abs(y_).sum())
+    rk3_vs_rk2 = {"rho": l1(c3[0], a[0]), "Y_OH": l1(y(c3, 5), y(a, 5)), "Y_H2O": l1(y(c3, 2), y(a, 2)),
+                  "steps": same_steps}
+
+    # end to end: upload the state, one step, download, per step
+    flat = Rb.level.copy_out()
+    pin = torch.from_numpy(flat).pin_memory()
+    out = torch.empty_like(pin).pin_memory()
+    e2e_steps = max(2, min(args.steps, 5))
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        Rb.level.lib.ocfd_level_copy_in(Rb.level.h, ctypes.c_void_p(pin.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        Rb.advance(1, stream)
+        Rb.level.lib.ocfd_level_copy_out(Rb.level.h, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_value = cells * e2e_steps * world / (allreduce_max(e0.elapsed_time(e1), world) * 1e-3)
+    Rb.close()
+
+    hbm_peak, peak_src = peaks()
+    fp64 = ctypes.c_double(); fp32 = ctypes.c_double()
+    ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
+    achieved = 192.0 * cells / (chem_ms * 1e-3) / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        dt_cpu, ncs = react_cpu_sample(64, 1, os.cpu_count())
+        cpu = {"value": ncs / dt_cpu, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "1 Strang step (4+4 chemistry substeps, RK2 multispecies flow, renormalisation) of a "
+                         "periodic 64^3 sample with the workload's cell size, oracle restatement (OpenMP)"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_bin / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3D H2/air reacting box 128^3 periodic, 9 species / 19 reactions, phi=1, 1 atm, "
+                                   "1200 K + 8 hot spots (seed %d, edge 1 cm), mixture-averaged transport, "
+                                   "Strang chemistry (4+4 substeps), RK2, dt=1e-8 s" % case["seed"],
+                       "form": "binned batched chemistry",
+                       "forms_cell_steps_per_s": {"binned": value, "plain": value_plain},
+                       "speedup_binned_over_plain": value / value_plain,
+                       "forms_identical": identical,
+                       "mixed_precision_flux": "not available for the multispecies RHS (FP64)",
+                       "rk3_vs_rk2_l1": rk3_vs_rk2, "boxes": len(boxes), "cells": cells,
+                       "l2": "flushed between timed steps (512 MB write, untimed)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "k_chem_advance_list (one chemistry substep)", "ms_per_launch": chem_ms,
+                         "alg_bytes_per_cell": 192, "fp64_fma_peak_gflops": fp64.value},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": int(flat.nbytes),
+                    "d2h_bytes_per_step": int(flat.nbytes)},
+            "clocks": clk.summary(),
+            "gpu_launches": launches * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -568,7 +763,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="dmr-amr", choices=["dmr-amr", "sod", "dmr", "cube"])
+    ap.add_argument("--config", default="dmr-amr", choices=["dmr-amr", "react", "sod", "dmr", "cube"])
     ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
                     help="headline form (the other form is timed too and reported in config)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -580,6 +775,8 @@ def main():
         run_reference(args, world, rank)
     elif args.config == "dmr-amr":
         run_ours_amr(args, world, rank, local)
+    elif args.config == "react":
+        run_ours_react(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

@@ -324,6 +324,9 @@ ocfd_level* ocfd_react_level(ocfd_react* react);
 ocfd_status ocfd_react_advance(ocfd_react* react, int nsteps, void* stream);
 /* Kernels of one step (the captured graph). */
 int ocfd_react_launches_per_step(const ocfd_react* react);
+/* Mean device time of one chemistry substep over the level (the configured
+ * form), `reps` substeps of dt/(2 n) applied to the current state. */
+ocfd_status ocfd_react_profile_chem(ocfd_react* react, int reps, double* ms, void* stream);
 /* Conserved state of resting mixtures from temperature, pressure and mole
  * fractions (CKXTY, CKRHOY, CKUBMS as Exec/7_JET/prob.H:46-60 uses them), n
  * cells, device arrays: T[n], p[n], X[9][n] -> U[5][n] (rho, 0, 0, 0, rho e),

@@ -342,4 +342,27 @@ ocfd_status ocfd_react_advance(ocfd_react* R, int nsteps, void* stream) {
 
 int ocfd_react_launches_per_step(const ocfd_react* R) { return R ? R->launches : 0; }
 
+ocfd_status ocfd_react_profile_chem(ocfd_react* R, int reps, double* ms, void* stream) {
+    if (!R || reps <= 0 || !ms) return fail(OCFD_BAD_ARG, "ocfd_react_profile_chem");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    ocfd_react_desc d = R->desc;
+    R->desc.chem_substeps = 1;
+    int launches = 0;
+    ocfd_status s = chem_half(R, st, launches);  // warm-up
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < reps && s == OCFD_OK; ++r) s = chem_half(R, st, launches);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    R->desc = d;
+    *ms = t / reps;
+    return s;
+}
+
 }  // extern "C"

@@ -24,6 +24,7 @@ declare("ocfd_react_destroy", ctypes.c_int, [_vp])
 declare("ocfd_react_level", _vp, [_vp])
 declare("ocfd_react_advance", ctypes.c_int, [_vp, ctypes.c_int, _vp])
 declare("ocfd_react_launches_per_step", ctypes.c_int, [_vp])
+declare("ocfd_react_profile_chem", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double), _vp])
 declare("ocfd_chem_state_tpx", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp])
 
 
@@ -73,6 +74,11 @@ class Reactor:
 
     def launches_per_step(self):
         return int(self.lib.ocfd_react_launches_per_step(self.h))
+
+    def profile_chem(self, reps=5, stream=None):
+        ms = ctypes.c_double()
+        check(self.lib.ocfd_react_profile_chem(self.h, reps, ctypes.byref(ms), _stream_ptr(stream)), "profile_chem")
+        return ms.value
 
 
 def state_tpx(ctx, T, p, X):

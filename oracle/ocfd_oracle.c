@@ -1081,6 +1081,9 @@ void ocfdo_c2prim(const ocfdo_parm* p, int chem, const double* S, const double* 
 static void transport_q(const ocfdo_parm* p, const box_t* b, const double* q, const double* spec,
                         double* mu, double* lam, double* D) {
     long long N = gN(b);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
     for (long long c = 0; c < N; ++c) {
         double Yt[NS], Xt[NS], Dc[NS];
         double T = q[QT * N + c], pr = q[QPRES * N + c];
@@ -1176,6 +1179,9 @@ void ocfdo_rhs_chem(const ocfdo_parm* p, const double* S, const double* spec, in
     if (do_visc) transport_q(p, &b, q, spec, mu, lam, D);
     for (int d = 0; d < 3; ++d) {
         long long FN = fN(&b, d);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
         for (long long c = 0; c < N; ++c) {
             double qc[8], a[5], m[5], tp, tm, tmp1;
             for (int n = 0; n < 8; ++n) qc[n] = q[n * N + c];
@@ -1188,6 +1194,9 @@ void ocfdo_rhs_chem(const ocfdo_parm* p, const double* S, const double* spec, in
                 fms[n * N + c] = tmp0 * tm;
             }
         }
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
         for (int k = 0; k < nz + (d == 2); ++k)
             for (int j = 0; j < ny + (d == 1); ++j)
                 for (int i = 0; i < nx + (d == 0); ++i) {
@@ -1198,12 +1207,18 @@ void ocfdo_rhs_chem(const ocfdo_parm* p, const double* S, const double* spec, in
                         fls[d][n * FN + fi] = weno_face(&b, fps + n * N, fms + n * N, d, i, j, k);
                 }
         if (do_visc) {
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
             for (int k = 0; k < nz + (d == 2); ++k)
                 for (int j = 0; j < ny + (d == 1); ++j)
                     for (int i = 0; i < nx + (d == 0); ++i) {
                         long long fi = fI(&b, d, i, j, k);
                         diffusion_face(&b, q, spec, D, d, i, j, k, dxinv, fls[d] + fi, fld[d] + fi, FN);
                     }
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
             for (int k = 0; k < nz + (d == 2); ++k)
                 for (int j = 0; j < ny + (d == 1); ++j)
                     for (int i = 0; i < nx + (d == 0); ++i) {
@@ -1215,6 +1230,9 @@ void ocfdo_rhs_chem(const ocfdo_parm* p, const double* S, const double* spec, in
         }
     }
     long long F0 = fN(&b, 0), F1 = fN(&b, 1), F2 = fN(&b, 2);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
     for (int k = 0; k < nz; ++k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
