@@ -447,6 +447,15 @@ ocfd_status ocfd_plotfile_compare(const char* file_a, const char* file_b, int32_
                                   int32_t cap, double* abs_err, double* rel_err, int32_t* nan_flags,
                                   int32_t* nlev, int32_t* ncomp);
 
+/* ------------------------------------------- 5th-generation tensor cores
+ * C[128 x N] = A[128 x K] * B[N x K]^T with row-major BF16 A and B (device),
+ * FP32 C, on tcgen05.mma with the accumulator in tensor memory: the building
+ * block of the chemistry surrogate's kernels, exposed for testing.  N and K in
+ * [16, 256], multiples of 16.  Synchronises `stream`; OCFD_TIMEOUT if the
+ * bounded wait for the MMA ran out. */
+ocfd_status ocfd_tc_gemm_bf16(ocfd_context* ctx, const uint16_t* A, const uint16_t* B, float* C, int N, int K,
+                              void* stream);
+
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops
  * per FMA), from register-only FMA chains over all SMs. */
