@@ -456,6 +456,36 @@ ocfd_status ocfd_plotfile_compare(const char* file_a, const char* file_b, int32_
 ocfd_status ocfd_tc_gemm_bf16(ocfd_context* ctx, const uint16_t* A, const uint16_t* B, float* C, int N, int K,
                               void* stream);
 
+/* ------------------------------------------------ chemistry surrogate network
+ * MLP 12 -> 128 x 4 (GELU) -> 10 on the tensor cores: BF16 weights and
+ * activations, FP32 accumulation (tcgen05.mma into tensor memory).  Inputs
+ * (T, p, 9 Y, log10 dt) and outputs (increments of T and of the 9 Y) are used
+ * normalised: x_n = (x - in_mu) * in_isd, y = y_n * out_sd + out_mu.
+ * Weights: five row-major (out x in) blocks W1 128x16 (inputs padded from 12),
+ * W2..W4 128x128, W5 16x128 (outputs padded from 10), 53248 floats; biases
+ * 128 x 4 + 16 = 528 floats.                                                    */
+typedef struct ocfd_mlp ocfd_mlp;
+#define OCFD_MLP_WEIGHTS 53248
+#define OCFD_MLP_BIASES 528
+
+/* He-normal initial weights from `seed`; training batches up to max_batch rows
+ * (a multiple of 256). */
+ocfd_status ocfd_mlp_create(ocfd_context* ctx, int32_t max_batch, uint64_t seed, ocfd_mlp** mlp);
+ocfd_status ocfd_mlp_destroy(ocfd_mlp* mlp);
+ocfd_status ocfd_mlp_set_norm(ocfd_mlp* mlp, const float in_mu[12], const float in_isd[12], const float out_mu[10],
+                              const float out_sd[10]);
+/* FP32 master parameters (host arrays of OCFD_MLP_WEIGHTS / OCFD_MLP_BIASES). */
+ocfd_status ocfd_mlp_get_params(ocfd_mlp* mlp, float* W, float* b);
+ocfd_status ocfd_mlp_set_params(ocfd_mlp* mlp, const float* W, const float* b);
+/* Y [M x 10] = network(X [M x 12]), normalised units, device arrays, M a
+ * multiple of 128 up to max_batch. */
+ocfd_status ocfd_mlp_forward(ocfd_mlp* mlp, const float* X, float* Y, int64_t M, void* stream);
+/* One step on normalised device batches X [M x 12], T [M x 10]: forward, mean
+ * squared error, backward, and with `update` an Adam step of rate lr; the loss
+ * and (optional, host) gradients gW [OCFD_MLP_WEIGHTS], gb [OCFD_MLP_BIASES]. */
+ocfd_status ocfd_mlp_train_step(ocfd_mlp* mlp, const float* X, const float* T, int64_t M, float lr, int32_t update,
+                                float* loss, float* gW, float* gb, void* stream);
+
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops
  * per FMA), from register-only FMA chains over all SMs. */

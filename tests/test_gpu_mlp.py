@@ -47,3 +47,71 @@ def test_tc_gemm(ctx, N, K):
     # FP32 accumulation of K exact BF16 products
     tol = 1e-6 * np.abs(bf16_value(A)) @ np.abs(bf16_value(B)).T + 1e-30
     assert (np.abs(got - want) <= 8 * tol).all(), np.abs(got - want).max()
+
+
+def make_mlp(ctx, max_batch=1024, seed=11):
+    import ctypes as C
+    import ocfd
+    from ocfd import mlp
+    return mlp.Mlp(ctx, max_batch, seed)
+
+
+def test_mlp_forward_vs_oracle(ctx):
+    import torch
+    import mlp_oracle as mo
+    net = make_mlp(ctx)
+    W, b = net.get_params()
+    rng = np.random.default_rng(1)
+    b = (0.1 * rng.standard_normal(b.shape)).astype(np.float32)
+    b[mo.BOFF[4] + 10:] = 0
+    net.set_params(W, b)
+    X = rng.standard_normal((512, 12)).astype(np.float32)
+    Y = net.forward(torch.from_numpy(X).cuda()).cpu().numpy()
+    want, _ = mo.forward(W, b, X)
+    err = np.abs(Y - want[:, :10]).max() / np.abs(want[:, :10]).max()
+    assert err < 2e-3, err
+
+
+def test_mlp_gradients_vs_oracle(ctx):
+    import torch
+    import mlp_oracle as mo
+    net = make_mlp(ctx)
+    W, b = net.get_params()
+    rng = np.random.default_rng(2)
+    b = (0.1 * rng.standard_normal(b.shape)).astype(np.float32)
+    b[mo.BOFF[4] + 10:] = 0
+    net.set_params(W, b)
+    X = rng.standard_normal((512, 12)).astype(np.float32)
+    T = rng.standard_normal((512, 10)).astype(np.float32)
+    loss, gW, gb = net.train_step(torch.from_numpy(X).cuda(), torch.from_numpy(T).cuda(), lr=0.0, update=False,
+                                  grads=True)
+    wl, wW, wb = mo.train_grads(W, b, X, T)
+    assert loss == pytest.approx(wl, rel=1e-4)
+    for l in range(5):
+        sl = slice(mo.WOFF[l], mo.WOFF[l] + mo.LN[l] * mo.LK[l])
+        e = np.linalg.norm(gW[sl] - wW[sl]) / np.linalg.norm(wW[sl])
+        assert e < 5e-3, (l, e)
+        sb = slice(mo.BOFF[l], mo.BOFF[l] + mo.LN[l])
+        e = np.linalg.norm(gb[sb] - wb[sb]) / max(np.linalg.norm(wb[sb]), 1e-30)
+        assert e < 5e-3, (l, e)
+    # padding rows / columns of the layout receive no gradient
+    assert np.all(gW[mo.WOFF[4] + 10 * 128:mo.WOFF[4] + 16 * 128] == 0)
+    assert np.all(mo.layer(gW, 0)[:, 12:] == 0)
+
+
+def test_mlp_learns_smooth_map(ctx):
+    """Adam on a smooth 12 -> 10 regression lowers the loss by 10x"""
+    import torch
+    net = make_mlp(ctx, max_batch=1024, seed=3)
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((12, 10)) / 4
+    X = rng.standard_normal((8192, 12)).astype(np.float32)
+    T = np.tanh(X @ A).astype(np.float32)
+    Xd = torch.from_numpy(X).cuda()
+    Td = torch.from_numpy(T).cuda()
+    first = None
+    for it in range(300):
+        s = (it * 1024) % 8192
+        loss, _, _ = net.train_step(Xd[s:s + 1024], Td[s:s + 1024], lr=2e-3)
+        first = loss if first is None else first
+    assert loss < first / 10, (first, loss)
