@@ -486,6 +486,33 @@ ocfd_status ocfd_mlp_forward(ocfd_mlp* mlp, const float* X, float* Y, int64_t M,
 ocfd_status ocfd_mlp_train_step(ocfd_mlp* mlp, const float* X, const float* T, int64_t M, float lr, int32_t update,
                                 float* loss, float* gW, float* gb, void* stream);
 
+/* Guard of the surrogate chemistry substep: a cell takes the network's increments
+ * only when its inputs lie in the training range and the increments keep every
+ * Y in [-y_tol, 1 + y_tol] and the H, O, N element contents within elem_tol
+ * (relative); otherwise the FP64 implicit substep is applied to it. */
+typedef struct ocfd_surrogate_guard {
+    double T_min, T_max, p_min, p_max, dt_min, dt_max;
+    double y_tol, elem_tol;
+} ocfd_surrogate_guard;
+
+/* Chemistry of a reacting level by the network (NULL: back to the FP64
+ * substep): every substep runs the network over the level's cells and the FP64
+ * substep over the cells its guard rejected.  ocfd_react_fallbacks: cells sent
+ * to the FP64 substep so far. */
+ocfd_status ocfd_react_set_surrogate(ocfd_react* react, ocfd_mlp* mlp, const ocfd_surrogate_guard* guard);
+ocfd_status ocfd_react_fallbacks(ocfd_react* react, int64_t* fallbacks, void* stream);
+
+/* 0D cells: n states of 14 components (component stride n, device memory). */
+/* one FP64 implicit substep per cell, step dt_cells[i] (or dt when NULL) */
+ocfd_status ocfd_chem_cells_advance(ocfd_context* ctx, int64_t n, double* U, const double* dt_cells, double dt,
+                                    void* stream);
+/* T, p, Y[9] of each cell into out [11][n] */
+ocfd_status ocfd_chem_cells_props(ocfd_context* ctx, int64_t n, const double* U, double* out, void* stream);
+/* one surrogate substep of dt per cell (with the FP64 fallback); *fallbacks
+ * receives the number of cells the guard sent to the FP64 substep */
+ocfd_status ocfd_chem_cells_surrogate(ocfd_context* ctx, ocfd_mlp* mlp, const ocfd_surrogate_guard* guard,
+                                      int64_t n, double* U, double dt, int64_t* fallbacks, void* stream);
+
 /* ----------------------------------------------------------- measurement */
 /* Sustained FP64 and FP32 FMA rates of the current device in GFLOP/s (2 flops
  * per FMA), from register-only FMA chains over all SMs. */

@@ -6,8 +6,11 @@
 #include <cstring>
 #include <string>
 
+#include <algorithm>
+
 #include "chem_internal.h"
 #include "chem_physics.cuh"
+#include "mlp_kernel.cuh"
 #include "eb_physics.cuh"
 #include "mechanism.h"
 #include "ocfd_internal.h"
@@ -102,14 +105,19 @@ __global__ void __launch_bounds__(kChemThreads) k_chem_advance(View<double> S, V
 // The same substep over a list of cells of a level (element offset of component
 // 0 and the component stride of each cell's FAB; state then species
 // components): one launch for every box, in the list's order.
+// ncell is bounded by *count when given (a list filled on the device); dtc gives
+// a step per cell when given.
 __global__ void __launch_bounds__(kChemThreads) k_chem_advance_list(const long long* __restrict__ off,
                                                                     const long long* __restrict__ stride,
-                                                                    long long ncell, double* Ubuf, double dt,
-                                                                    DevParm P) {
+                                                                    long long ncell, const unsigned* count,
+                                                                    const double* __restrict__ dtc, double* Ubuf,
+                                                                    double dt, DevParm P) {
     extern __shared__ double smem[];
     const SmemMat U{smem + threadIdx.x, (int)blockDim.x};
     const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (count && c >= (long long)*count) return;
     if (c >= ncell) return;
+    if (dtc) dt = dtc[c];
     double* x = Ubuf + off[c];
     const long long ns = stride[c];
     double u[5], r[NSP];
@@ -161,12 +169,156 @@ ocfd_status launch_chem_advance(View<double> S, View<double> sp, const CellBox& 
 }
 
 ocfd_status launch_chem_advance_list(const long long* off, const long long* stride, long long ncell, double* U,
-                                     double dt, const DevParm& P, cudaStream_t st) {
+                                     double dt, const DevParm& P, cudaStream_t st, const unsigned* count,
+                                     const double* dtc) {
     if (ncell <= 0) return OCFD_OK;
     const long long blocks = (ncell + kChemThreads - 1) / kChemThreads;
-    k_chem_advance_list<<<(unsigned)blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, st>>>(off, stride, ncell,
-                                                                                                 U, dt, P);
+    k_chem_advance_list<<<(unsigned)blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, st>>>(
+        off, stride, ncell, count, dtc, U, dt, P);
     return check_launch("chemistry substep (cell list)");
+}
+
+// ------------------------------------------------------------ surrogate substep
+// Temperature, pressure and mass fractions of cells of a list: T from e by the
+// Newton of LiDryer.H:833-888, p = CKPY (LiDryer.H:10-18)
+__device__ __forceinline__ void cell_props(const double* x, long long ns, const DevParm& P, double* T, double* p,
+                                           double* Y, double* rho_out, double* r) {
+    const double rho = dmax(x[0], P.smallr);
+    const double rhoinv = 1.0 / rho;
+    const double ux = x[ns] * rhoinv, uy = x[2 * ns] * rhoinv, uz = x[3 * ns] * rhoinv;
+    const double ei = x[4 * ns] - rho * (0.5 * (ux * ux + uy * uy + uz * uz));
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) r[n] = x[(5 + n) * ns];
+    *T = get_t_given_ey(ei, r, P.Ru);
+    *p = ckpy(r, *T, P.Ru);
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) Y[n] = r[n] * rhoinv;
+    *rho_out = rho;
+}
+
+__global__ void k_chem_props(const long long* __restrict__ off, const long long* __restrict__ stride, long long ncell,
+                             const double* __restrict__ Ubuf, double* out, DevParm P) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        double T, p, Y[NSP], rho, r[NSP];
+        cell_props(Ubuf + off[c], stride[c], P, &T, &p, Y, &rho, r);
+        out[c] = T;
+        out[ncell + c] = p;
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) out[(2 + n) * ncell + c] = Y[n];
+    }
+}
+
+// element content per unit mass (mol / kg): H, O, N atoms of
+// H2, O2, H2O, H, O, OH, HO2, H2O2, N2
+__constant__ float c_elem[3][NSP] = {{2, 0, 2, 1, 0, 1, 1, 2, 0}, {0, 2, 1, 0, 1, 1, 2, 2, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 2}};
+
+// One chemistry substep by the network for the cells of a list, 128 cells per
+// tile (thread = cell): inputs (T, p, Y, log10 dt) -> increments of T and Y.
+// Cells whose inputs leave the training range, or whose increments break the
+// species bounds or the H / O / N element balance beyond the guard's
+// tolerances, are appended to the fallback list for the FP64 substep.
+__global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long long* __restrict__ off,
+                                                        const long long* __restrict__ stride, long long ncell,
+                                                        double* Ubuf, double dt, DevParm P, ocfd_surrogate_guard g,
+                                                        long long* fb_off, long long* fb_stride, unsigned* fb_count,
+                                                        unsigned long long* fb_total, unsigned* err) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S_BAR);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S_BAR + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    mlp_stage_weights(net, sm);
+    if (tid == 0) mbar_init(bar, 1);
+    if (warp == 0) {
+        tmem_alloc(tslot, 128);
+        tmem_relinquish();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tbase = *tslot;
+    uint32_t phase = 0;
+    bool ok = true;
+    const long long ntile = (ncell + 127) / 128;
+    const float ldt = (float)log10(dt);
+    const bool dt_in = dt >= g.dt_min && dt <= g.dt_max;
+    for (long long t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
+        const long long c = t * 128 + tid;
+        const bool valid = c < ncell;
+        double T = 0, p = 0, Y[NSP] = {}, rho = 1, r[NSP] = {};
+        double* x = nullptr;
+        long long ns = 0;
+        if (valid) {
+            x = Ubuf + off[c];
+            ns = stride[c];
+            cell_props(x, ns, P, &T, &p, Y, &rho, r);
+        }
+        float f[16];
+        f[0] = ((float)T - net.in_mu[0]) * net.in_isd[0];
+        f[1] = ((float)p - net.in_mu[1]) * net.in_isd[1];
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) f[2 + n] = ((float)Y[n] - net.in_mu[2 + n]) * net.in_isd[2 + n];
+        f[11] = (ldt - net.in_mu[11]) * net.in_isd[11];
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            *reinterpret_cast<uint16_t*>(sm + S_A0 + kmajor_offset(tid, k, 128)) = k < MLP_IN ? bf16_bits(f[k]) : 0;
+        float out[16];
+        ok = mlp_tile(sm, tbase, bar, phase, out, nullptr, nullptr, 0);
+        if (!ok || !valid) continue;
+        double dY[NSP];
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) dY[n] = (double)(out[1 + n] * net.out_sd[1 + n] + net.out_mu[1 + n]);
+        bool pass = dt_in && T >= g.T_min && T <= g.T_max && p >= g.p_min && p <= g.p_max;
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) pass = pass && Y[n] + dY[n] >= -g.y_tol && Y[n] + dY[n] <= 1.0 + g.y_tol;
+        for (int e = 0; e < 3 && pass; ++e) {
+            double have = 0, d = 0;
+#pragma unroll
+            for (int n = 0; n < NSP; ++n) {
+                have += c_elem[e][n] * Y[n] / c_mech.mw[n];
+                d += c_elem[e][n] * dY[n] / c_mech.mw[n];
+            }
+            pass = fabs(d) <= g.elem_tol * have;
+        }
+        if (pass) {
+            double dei = 0;
+#pragma unroll
+            for (int n = 0; n < NSP; ++n) {
+                const double drho = rho * dY[n];
+                double v = r[n] + drho;
+                if (v < 0) v = 0.0;
+                x[(5 + n) * ns] = v;
+                dei += -c_mech.HP[n] * P.Ru / c_mech.mw[n] * drho;
+            }
+            x[4 * ns] += dei;
+        } else {
+            const unsigned q = atomicAdd(fb_count, 1u);
+            fb_off[q] = off[c];
+            fb_stride[q] = ns;
+            atomicAdd(fb_total, 1ull);
+        }
+    }
+    if (!ok && tid == 0) atomicOr(err, 1u);
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tbase, 128);
+}
+
+ocfd_status launch_chem_surrogate(const ocfd_mlp* mlp, const long long* off, const long long* stride, long long ncell,
+                                  double* U, double dt, const DevParm& P, const ocfd_surrogate_guard& g,
+                                  long long* fb_off, long long* fb_stride, unsigned* fb_count,
+                                  unsigned long long* fb_total, unsigned* err, int sms, cudaStream_t st) {
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(k_chem_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, S_TOT) != cudaSuccess)
+            return check_launch("surrogate attribute");
+        configured = true;
+    }
+    if (ncell <= 0) return OCFD_OK;
+    const long long ntile = (ncell + 127) / 128;
+    k_chem_surrogate<<<(unsigned)std::min<long long>(ntile, sms), 128, S_TOT, st>>>(
+        mlp_net(mlp), off, stride, ncell, U, dt, P, g, fb_off, fb_stride, fb_count, fb_total, err);
+    return check_launch("surrogate chemistry substep");
 }
 
 ocfd_status launch_spec_renorm(View<const double> S, View<double> sp, const CellBox& B, int sms, cudaStream_t st) {
@@ -786,4 +938,95 @@ extern "C" ocfd_status ocfd_rhs_chem_eb_box_f64(ocfd_context* ctx, const ocfd_ar
     k_chem_eb_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, ctx->parm);
     k_chem_eb_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
     return check_launch("ocfd_rhs_chem_eb_box_f64");
+}
+
+// ------------------------------------------------------------ 0D cells
+namespace ocfd {
+__global__ void k_iota_cells(long long* off, long long* stride, long long n) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        off[c] = c;
+        stride[c] = n;
+    }
+}
+
+struct CellList {
+    long long* off = nullptr;
+    long long* stride = nullptr;
+    ~CellList() {
+        cudaFree(off);
+        cudaFree(stride);
+    }
+    bool make(long long n, int sms, cudaStream_t st) {
+        if (cudaMalloc(&off, sizeof(long long) * n) != cudaSuccess ||
+            cudaMalloc(&stride, sizeof(long long) * n) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        long long b = (n + 255) / 256;
+        if (b > (long long)sms * 16) b = (long long)sms * 16;
+        k_iota_cells<<<(int)b, 256, 0, st>>>(off, stride, n);
+        return true;
+    }
+};
+}  // namespace ocfd
+
+extern "C" ocfd_status ocfd_chem_cells_advance(ocfd_context* ctx, int64_t n, double* U, const double* dt_cells,
+                                               double dt, void* stream) {
+    using namespace ocfd;
+    if (!ctx || n <= 0 || !U) return fail(OCFD_BAD_ARG, "ocfd_chem_cells_advance");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CellList L;
+    if (!L.make(n, ctx->num_sms, st)) return fail(OCFD_OUT_OF_MEMORY, "ocfd_chem_cells_advance");
+    ocfd_status s = launch_chem_advance_list(L.off, L.stride, n, U, dt, ctx->parm, st, nullptr, dt_cells);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("ocfd_chem_cells_advance");
+    return s;
+}
+
+extern "C" ocfd_status ocfd_chem_cells_props(ocfd_context* ctx, int64_t n, const double* U, double* out,
+                                             void* stream) {
+    using namespace ocfd;
+    if (!ctx || n <= 0 || !U || !out) return fail(OCFD_BAD_ARG, "ocfd_chem_cells_props");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CellList L;
+    if (!L.make(n, ctx->num_sms, st)) return fail(OCFD_OUT_OF_MEMORY, "ocfd_chem_cells_props");
+    long long b = (n + 127) / 128;
+    if (b > (long long)ctx->num_sms * 32) b = (long long)ctx->num_sms * 32;
+    k_chem_props<<<(int)b, 128, 0, st>>>(L.off, L.stride, n, U, out, ctx->parm);
+    ocfd_status s = check_launch("ocfd_chem_cells_props");
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("ocfd_chem_cells_props");
+    return s;
+}
+
+extern "C" ocfd_status ocfd_chem_cells_surrogate(ocfd_context* ctx, ocfd_mlp* mlp, const ocfd_surrogate_guard* g,
+                                                 int64_t n, double* U, double dt, int64_t* fallbacks,
+                                                 void* stream) {
+    using namespace ocfd;
+    if (!ctx || !mlp || !g || n <= 0 || !U) return fail(OCFD_BAD_ARG, "ocfd_chem_cells_surrogate");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CellList L, F;
+    unsigned* cnt = nullptr;
+    unsigned long long* tot = nullptr;
+    if (!L.make(n, ctx->num_sms, st) || !F.make(n, ctx->num_sms, st) || cudaMalloc(&cnt, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&tot, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(cnt);
+        return fail(OCFD_OUT_OF_MEMORY, "ocfd_chem_cells_surrogate");
+    }
+    cudaMemsetAsync(cnt, 0, sizeof(unsigned), st);
+    cudaMemsetAsync(tot, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(ctx->d_error, 0, sizeof(uint32_t), st);
+    ocfd_status s = launch_chem_surrogate(mlp, L.off, L.stride, n, U, dt, ctx->parm, *g, F.off, F.stride, cnt, tot,
+                                          ctx->d_error, ctx->num_sms, st);
+    if (s == OCFD_OK) s = launch_chem_advance_list(F.off, F.stride, n, U, dt, ctx->parm, st, cnt, nullptr);
+    unsigned long long h = 0;
+    uint32_t e = 0;
+    if (cudaMemcpyAsync(&h, tot, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&e, ctx->d_error, sizeof(e), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        s = check_launch("ocfd_chem_cells_surrogate");
+    cudaFree(cnt);
+    cudaFree(tot);
+    if (s == OCFD_OK && e) s = fail(OCFD_TIMEOUT, "ocfd_chem_cells_surrogate: a tensor-core completion wait ran out");
+    if (fallbacks) *fallbacks = (int64_t)h;
+    return s;
 }

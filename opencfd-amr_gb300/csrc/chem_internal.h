@@ -55,7 +55,12 @@ ocfd_status launch_chem_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cud
 ocfd_status launch_chem_advance(View<double> S, View<double> sp, const CellBox& B, double dt, const DevParm& P,
                                 cudaStream_t st);
 ocfd_status launch_chem_advance_list(const long long* off, const long long* stride, long long ncell, double* U,
-                                     double dt, const DevParm& P, cudaStream_t st);
+                                     double dt, const DevParm& P, cudaStream_t st, const unsigned* count = nullptr,
+                                     const double* dtc = nullptr);
+ocfd_status launch_chem_surrogate(const ocfd_mlp* mlp, const long long* off, const long long* stride, long long ncell,
+                                  double* U, double dt, const DevParm& P, const ocfd_surrogate_guard& g,
+                                  long long* fb_off, long long* fb_stride, unsigned* fb_count,
+                                  unsigned long long* fb_total, unsigned* err, int sms, cudaStream_t st);
 ocfd_status launch_spec_renorm(View<const double> S, View<double> sp, const CellBox& B, int sms, cudaStream_t st);
 
 }  // namespace ocfd

@@ -103,6 +103,19 @@ __global__ void k_react_scatter(const FabGeom* __restrict__ fabs, const long lon
     }
 }
 
+__global__ void k_react_identity(const FabGeom* __restrict__ fabs, const long long* __restrict__ start, int nbox,
+                                 long long total, long long* off, long long* stride) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int bx = find_tag<FabGeom>(start, nbox, idx);
+        const FabGeom& f = fabs[bx];
+        int i, j, k;
+        region_cell(f.lo, f.hi, idx - start[bx], i, j, k);
+        off[idx] = fab_index(f, i, j, k);
+        stride[idx] = f.ns;
+    }
+}
+
 __global__ void k_react_begin(StepState* st, double dt) {
     st->dt = dt;
 }
@@ -127,6 +140,13 @@ struct ocfd_react {
     long long* off = nullptr;
     long long* stride = nullptr;
     double* a0w = nullptr;
+    // surrogate chemistry: network, guard, fallback list and counters
+    ocfd_mlp* mlp = nullptr;
+    ocfd_surrogate_guard guard{};
+    long long* fb_off = nullptr;
+    long long* fb_stride = nullptr;
+    unsigned* fb_count = nullptr;
+    unsigned long long* fb_total = nullptr;
     cudaGraphExec_t graph = nullptr;
     unsigned graph_flags = ~0u;
     int launches = 0;
@@ -153,6 +173,22 @@ static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
     ocfd_level* L = R->L;
     const double dt2 = 0.5 * R->desc.dt / R->desc.chem_substeps;
     const int sms = R->ctx->num_sms;
+    if (R->mlp) {
+        // network substep over the level's cells, then the FP64 substep for the
+        // cells the guard rejected
+        for (int s = 0; s < R->desc.chem_substeps; ++s) {
+            cudaMemsetAsync(R->fb_count, 0, sizeof(unsigned), st);
+            ocfd_status r = launch_chem_surrogate(R->mlp, R->off, R->stride, L->ncells, L->buf[0], dt2, R->ctx->parm,
+                                                  R->guard, R->fb_off, R->fb_stride, R->fb_count, R->fb_total,
+                                                  R->ctx->d_error, sms, st);
+            if (r == OCFD_OK)
+                r = launch_chem_advance_list(R->fb_off, R->fb_stride, L->ncells, L->buf[0], dt2, R->ctx->parm, st,
+                                             R->fb_count, nullptr);
+            if (r != OCFD_OK) return r;
+            launches += 2;
+        }
+        return OCFD_OK;
+    }
     if (R->desc.binned_chem) {
         cudaMemsetAsync(R->count, 0, sizeof(unsigned) * NBIN, st);
         k_react_keys<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(L->d_fabs, L->d_cell_start, (int)L->boxes.size(),
@@ -270,6 +306,19 @@ ocfd_status ocfd_react_create(ocfd_context* ctx, const ocfd_react_desc* desc, oc
         return fail(OCFD_OUT_OF_MEMORY, "ocfd_react_create: buffers");
     }
     cudaMemset(R->rhs, 0, sizeof(double) * L->elems);
+    if (cudaMalloc(&R->fb_off, sizeof(long long) * std::max<long long>(1, L->ncells)) != cudaSuccess ||
+        cudaMalloc(&R->fb_stride, sizeof(long long) * std::max<long long>(1, L->ncells)) != cudaSuccess ||
+        cudaMalloc(&R->fb_count, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&R->fb_total, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        ocfd_react_destroy(R);
+        return fail(OCFD_OUT_OF_MEMORY, "ocfd_react_create: fallback list");
+    }
+    cudaMemset(R->fb_total, 0, sizeof(unsigned long long));
+    // the level's cells in box order (re-ordered by the binned form every half step)
+    k_react_identity<<<grid_for(L->ncells, 256, ctx->num_sms), 256>>>(L->d_fabs, L->d_cell_start,
+                                                                       (int)L->boxes.size(), L->ncells, R->off,
+                                                                       R->stride);
     // (a0 - 1) Ru / W_i of the Newton start (LiDryer.H:833-888)
     {
         MechTables t;
@@ -307,6 +356,10 @@ ocfd_status ocfd_react_destroy(ocfd_react* R) {
     cudaFree(R->off);
     cudaFree(R->stride);
     cudaFree(R->a0w);
+    cudaFree(R->fb_off);
+    cudaFree(R->fb_stride);
+    cudaFree(R->fb_count);
+    cudaFree(R->fb_total);
     if (R->L) ocfd_level_destroy(R->L);
     delete R;
     return OCFD_OK;
@@ -341,6 +394,28 @@ ocfd_status ocfd_react_advance(ocfd_react* R, int nsteps, void* stream) {
 }
 
 int ocfd_react_launches_per_step(const ocfd_react* R) { return R ? R->launches : 0; }
+
+ocfd_status ocfd_react_set_surrogate(ocfd_react* R, ocfd_mlp* mlp, const ocfd_surrogate_guard* guard) {
+    if (!R || (mlp && !guard)) return fail(OCFD_BAD_ARG, "ocfd_react_set_surrogate");
+    R->mlp = mlp;
+    if (guard) R->guard = *guard;
+    if (R->graph) {
+        cudaGraphExecDestroy(R->graph);
+        R->graph = nullptr;
+    }
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_react_fallbacks(ocfd_react* R, int64_t* fallbacks, void* stream) {
+    if (!R || !fallbacks) return fail(OCFD_BAD_ARG, "ocfd_react_fallbacks");
+    unsigned long long h = 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(&h, R->fb_total, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return check_launch("ocfd_react_fallbacks");
+    *fallbacks = (int64_t)h;
+    return OCFD_OK;
+}
 
 ocfd_status ocfd_react_profile_chem(ocfd_react* R, int reps, double* ms, void* stream) {
     if (!R || reps <= 0 || !ms) return fail(OCFD_BAD_ARG, "ocfd_react_profile_chem");

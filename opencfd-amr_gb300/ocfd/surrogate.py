@@ -1,0 +1,193 @@
+"""Chemistry surrogate: data from the FP64 implicit substep, training on the
+tensor-core kernels, the guard, and evaluation against the FP64 substep.
+
+Data: 0D constant-volume trajectories (the operator the surrogate replaces is
+the constant-volume substep of EBR::chemical_advance,
+Source/CHEM/ChemAdvance.cpp:27-82) of H2/O2/N2 mixtures with T0 in
+[1000, 2500] K, equivalence ratio in [0.5, 2] and p0 in [1, 10] atm, advanced by
+the FP64 substep with a per-trajectory step; at every snapshot each state takes
+one FP64 substep of a step drawn log-uniformly in [1e-9, 1e-6] s, and the pair
+(T, p, Y, log10 dt) -> (dT, dY) is a training sample.  The lower end extends
+the configured [1e-8, 1e-6] s so that the substeps of the reacting box
+(dt / 8 = 1.25e-9 s) lie inside the training range.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+
+import numpy as np
+
+from ._abi import check, declare, load
+from .context import _stream_ptr
+
+_vp = ctypes.c_void_p
+ATM = 101325.0
+# species order: H2, O2, H2O, H, O, OH, HO2, H2O2, N2
+SPECIES = ("H2", "O2", "H2O", "H", "O", "OH", "HO2", "H2O2", "N2")
+
+
+class Guard(ctypes.Structure):
+    _fields_ = [("T_min", ctypes.c_double), ("T_max", ctypes.c_double), ("p_min", ctypes.c_double),
+                ("p_max", ctypes.c_double), ("dt_min", ctypes.c_double), ("dt_max", ctypes.c_double),
+                ("y_tol", ctypes.c_double), ("elem_tol", ctypes.c_double)]
+
+
+declare("ocfd_chem_cells_advance", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, ctypes.c_double, _vp])
+declare("ocfd_chem_cells_props", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, _vp])
+declare("ocfd_chem_cells_surrogate", ctypes.c_int, [_vp, _vp, ctypes.POINTER(Guard), ctypes.c_int64, _vp,
+                                                    ctypes.c_double, ctypes.POINTER(ctypes.c_int64), _vp])
+declare("ocfd_react_set_surrogate", ctypes.c_int, [_vp, _vp, ctypes.POINTER(Guard)])
+declare("ocfd_react_fallbacks", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64), _vp])
+
+# H, O, N atoms per species
+ELEM = np.array([[2, 0, 2, 1, 0, 1, 1, 2, 0], [0, 2, 1, 0, 1, 1, 2, 2, 0], [0, 0, 0, 0, 0, 0, 0, 0, 2]], float)
+
+
+def cells_advance(ctx, U, dt=None, dt_cells=None):
+    """one FP64 substep of every 0D cell of U (CUDA float64 [14, n])"""
+    check(load().ocfd_chem_cells_advance(ctx.h, U.shape[1], U.data_ptr(),
+                                         None if dt_cells is None else dt_cells.data_ptr(),
+                                         0.0 if dt is None else dt, _stream_ptr(None)), "ocfd_chem_cells_advance")
+
+
+def cells_props(ctx, U):
+    """T, p, Y [11, n] of 0D cells"""
+    import torch
+    out = torch.empty((11, U.shape[1]), dtype=torch.float64, device=U.device)
+    check(load().ocfd_chem_cells_props(ctx.h, U.shape[1], U.data_ptr(), out.data_ptr(), _stream_ptr(None)),
+          "ocfd_chem_cells_props")
+    return out
+
+
+def cells_surrogate(ctx, net, guard, U, dt):
+    fb = ctypes.c_int64()
+    check(load().ocfd_chem_cells_surrogate(ctx.h, net.h, ctypes.byref(guard), U.shape[1], U.data_ptr(), dt,
+                                           ctypes.byref(fb), _stream_ptr(None)), "ocfd_chem_cells_surrogate")
+    return fb.value
+
+
+def mixtures(rng, n):
+    """T0, p0 and mole fractions of H2/air mixtures (O2:N2 = 1:3.76) at random
+    equivalence ratios"""
+    T = rng.uniform(1000.0, 2500.0, n)
+    phi = rng.uniform(0.5, 2.0, n)
+    p = rng.uniform(1.0, 10.0, n) * ATM
+    X = np.zeros((9, n))
+    tot = 2 * phi + 1.0 + 3.76
+    X[0] = 2 * phi / tot
+    X[1] = 1.0 / tot
+    X[8] = 3.76 / tot
+    return T, p, X
+
+
+def generate(ctx, n_traj=32768, n_snap=300, seed=20261203, dt_lo=1e-9, dt_hi=1e-6, log=None):
+    """Training samples (features [N x 12], targets [N x 10]) as CUDA float32."""
+    import torch
+    from .react import state_tpx
+    rng = np.random.default_rng(seed)
+    T, p, X = mixtures(rng, n_traj)
+    U = torch.as_tensor(state_tpx(ctx, T, p, X), device="cuda").contiguous()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    # per-trajectory integration step, log-uniform in [1e-8, 5e-7] s
+    dt_traj = torch.pow(10.0, torch.empty(n_traj, dtype=torch.float64, device="cuda").uniform_(-8.0, math.log10(5e-7),
+                                                                                               generator=gen))
+    feats, targs = [], []
+    t0 = time.time()
+    for s in range(n_snap):
+        dts = torch.pow(10.0, torch.empty(n_traj, dtype=torch.float64, device="cuda").uniform_(
+            math.log10(dt_lo), math.log10(dt_hi), generator=gen))
+        before = cells_props(ctx, U)
+        V = U.clone()
+        cells_advance(ctx, V, dt_cells=dts)
+        after = cells_props(ctx, V)
+        f = torch.cat([before, torch.log10(dts)[None]], 0)            # T, p, Y[9], log10 dt
+        t = torch.cat([after[0:1] - before[0:1], after[2:] - before[2:]], 0)   # dT, dY[9]
+        feats.append(f.T.float())
+        targs.append(t.T.float())
+        cells_advance(ctx, U, dt_cells=dt_traj)
+    Xs = torch.cat(feats, 0)
+    Ts = torch.cat(targs, 0)
+    ok = torch.isfinite(Xs).all(1) & torch.isfinite(Ts).all(1)
+    if log:
+        log("generated %d samples in %.1f s (%d non-finite dropped)" % (Xs.shape[0], time.time() - t0,
+                                                                         int((~ok).sum())))
+    return Xs[ok].contiguous(), Ts[ok].contiguous()
+
+
+class Surrogate:
+    """A trained network with its normalisation and guard."""
+
+    def __init__(self, ctx, net, stats, guard):
+        self.ctx = ctx
+        self.net = net
+        self.stats = stats
+        self.guard = guard
+
+
+def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, log=None):
+    """Normalise, train with Adam on the tensor-core kernels (cosine schedule),
+    calibrate the guard on held-out samples.  Returns (Surrogate, report)."""
+    import torch
+    from .mlp import Mlp
+    n = X.shape[0]
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    perm = torch.randperm(n, generator=gen, device="cuda")
+    nval = max(batch, int(n * val_frac) // 256 * 256)
+    val, tr = perm[:nval], perm[nval:]
+    Xd, Td = X.double(), T.double()
+    in_mu = Xd[tr].mean(0)
+    in_sd = Xd[tr].std(0).clamp_min(1e-30)
+    out_mu = Td[tr].mean(0)
+    out_sd = Td[tr].std(0).clamp_min(1e-30)
+    Xn = ((Xd - in_mu) / in_sd).float()
+    Tn = ((Td - out_mu) / out_sd).float()
+    net = Mlp(ctx, batch, seed)
+    net.set_norm(in_mu.float().cpu().numpy(), (1.0 / in_sd).float().cpu().numpy(), out_mu.float().cpu().numpy(),
+                 out_sd.float().cpu().numpy())
+    steps_per_epoch = tr.numel() // batch
+    total = epochs * steps_per_epoch
+    t0 = time.time()
+    it = 0
+    losses = []
+    for ep in range(epochs):
+        order = tr[torch.randperm(tr.numel(), generator=gen, device="cuda")]
+        ep_loss = 0.0
+        for b in range(steps_per_epoch):
+            idx = order[b * batch:(b + 1) * batch]
+            rate = 1e-5 + 0.5 * (lr - 1e-5) * (1 + math.cos(math.pi * it / total))
+            loss, _, _ = net.train_step(Xn[idx].contiguous(), Tn[idx].contiguous(), lr=rate)
+            ep_loss += loss
+            it += 1
+        losses.append(ep_loss / steps_per_epoch)
+        if log:
+            log("epoch %d: loss %.4g (%.1f s)" % (ep, losses[-1], time.time() - t0))
+    train_s = time.time() - t0
+    # validation in physical units
+    Yv = []
+    for b in range(0, nval, batch):
+        Yv.append(net.forward(Xn[val[b:b + batch]].contiguous()))
+    Yv = torch.cat(Yv).double() * out_sd + out_mu
+    Tv = Td[val]
+    Xv = Xd[val]
+    val_loss = float((((Yv - Tv) / out_sd) ** 2).mean())
+    # element balance of the predicted increments (relative to the content)
+    W = np.array([2.016e-3, 31.998e-3, 18.015e-3, 1.008e-3, 15.999e-3, 17.007e-3, 33.006e-3, 34.014e-3, 28.014e-3])
+    E = torch.as_tensor(ELEM / W[None], device="cuda")
+    have = Xv[:, 2:11] @ E.T
+    dbal = (Yv[:, 1:] @ E.T).abs() / have.clamp_min(1e-300)
+    elem_err = dbal.max(1).values
+    elem_tol = float(torch.quantile(elem_err.float(), 0.99))
+    guard = Guard(T_min=float(Xd[tr, 0].min()), T_max=float(Xd[tr, 0].max()), p_min=float(Xd[tr, 1].min()),
+                  p_max=float(Xd[tr, 1].max()), dt_min=float(10 ** Xd[tr, 11].min()),
+                  dt_max=float(10 ** Xd[tr, 11].max()), y_tol=1e-3, elem_tol=elem_tol)
+    rel = lambda k: float(((Yv[:, k] - Tv[:, k]).abs().mean() / Tv[:, k].abs().mean()))
+    report = {"samples": int(n), "train_samples": int(tr.numel()), "val_samples": int(nval), "epochs": epochs,
+              "batch": batch, "train_seconds": train_s, "final_train_loss": losses[-1], "val_loss": val_loss,
+              "first_epoch_loss": losses[0], "val_rel_l1_dT": rel(0), "val_rel_l1_dY_OH": rel(1 + 5),
+              "val_rel_l1_dY_H2O": rel(1 + 2), "guard_elem_tol": elem_tol}
+    stats = dict(in_mu=in_mu, in_sd=in_sd, out_mu=out_mu, out_sd=out_sd)
+    return Surrogate(ctx, net, stats, guard), report

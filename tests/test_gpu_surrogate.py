@@ -1,0 +1,97 @@
+"""Chemistry surrogate pipeline on the GPU, at a small scale: samples from the
+FP64 implicit substep, training on the tensor-core kernels, the guard with its
+FP64 fallback, and the network embedded in the reacting level."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import ocfd
+    return ocfd.Context()
+
+
+@pytest.fixture(scope="module")
+def trained(ctx):
+    from ocfd import surrogate
+    X, T = surrogate.generate(ctx, n_traj=4096, n_snap=48, seed=5)
+    sur, rep = surrogate.train(ctx, X, T, epochs=4, batch=4096, lr=2e-3, seed=2)
+    return X, T, sur, rep
+
+
+def test_samples_are_physical(trained):
+    import torch
+    X, T, _, _ = trained
+    assert X.shape[1] == 12 and T.shape[1] == 10 and X.shape[0] > 150000
+    Y = X[:, 2:11]
+    assert float(Y.min()) >= 0.0 and torch.allclose(Y.sum(1), torch.ones_like(Y[:, 0]), atol=1e-5)
+    assert float(X[:, 0].min()) > 900.0 and float(X[:, 0].max()) < 3600.0
+    # mass is conserved by the FP64 substep: the increments of Y sum to ~0
+    assert float(T[:, 1:].sum(1).abs().max()) < 1e-5
+
+
+def test_training_lowers_the_loss(trained):
+    _, _, _, rep = trained
+    assert rep["final_train_loss"] < 0.5 * rep["first_epoch_loss"]
+    assert rep["val_loss"] < 1.5 * rep["final_train_loss"] + 1e-3
+
+
+def test_surrogate_substep_vs_fp64(ctx, trained):
+    """one network substep of 0D states against the FP64 substep: the guard's
+    fallback keeps every state physical and the temperature error small"""
+    import torch
+    from ocfd import surrogate
+    from ocfd.react import state_tpx
+    _, _, sur, _ = trained
+    rng = np.random.default_rng(9)
+    Tm, p, X = surrogate.mixtures(rng, 8192)
+    U0 = torch.as_tensor(state_tpx(ctx, Tm, p, X), device="cuda").contiguous()
+    # advance a little so that radicals exist
+    surrogate.cells_advance(ctx, U0, dt=2e-7)
+    surrogate.cells_advance(ctx, U0, dt=2e-7)
+    a, b = U0.clone(), U0.clone()
+    dt = 1e-7
+    surrogate.cells_advance(ctx, a, dt=dt)
+    fb = surrogate.cells_surrogate(ctx, sur.net, sur.guard, b, dt)
+    pa = surrogate.cells_props(ctx, a)
+    pb = surrogate.cells_props(ctx, b)
+    p0 = surrogate.cells_props(ctx, U0)
+    assert 0 <= fb < 8192
+    assert torch.isfinite(b).all() and float(b[5:].min()) >= 0.0
+    dT_true = (pa[0] - p0[0]).abs().mean()
+    err = (pb[0] - pa[0]).abs().mean()
+    assert float(err) < float(dT_true), (float(err), float(dT_true))
+
+
+def test_reacting_level_with_surrogate(ctx, trained):
+    from ocfd.cases import react_cube
+    from ocfd.level import chop_domain
+    from ocfd.react import Reactor
+    from ocfd import surrogate
+    import ctypes
+    _, _, sur, _ = trained
+    case = react_cube(ctx, n=32, length=0.01 * 32 / 128, seed=7)
+    boxes = chop_domain(case["n"], 16)
+    out = {}
+    for mode in ("plain", "surrogate"):
+        R = Reactor(ctx, boxes, (31, 31, 31), case["dx"], dt=1e-8, rk_order=2, chem_substeps=4)
+        R.level.set_global(case["G"])
+        if mode == "surrogate":
+            from ocfd._abi import check, load
+            check(load().ocfd_react_set_surrogate(R.h, sur.net.h, ctypes.byref(sur.guard)), "set_surrogate")
+        R.advance(3)
+        out[mode] = R.level.get_global()
+        if mode == "surrogate":
+            fb = ctypes.c_int64()
+            check(load().ocfd_react_fallbacks(R.h, ctypes.byref(fb), None), "fallbacks")
+            out["fb"] = fb.value
+        R.close()
+    a, b = out["plain"], out["surrogate"]
+    assert np.isfinite(b).all() and b[5:].min() >= 0.0
+    assert 0 <= out["fb"] <= 3 * 8 * 32 ** 3
+    # density is untouched by chemistry; the species stay close to the FP64 run
+    assert np.abs(b[0] - a[0]).max() / a[0].max() < 1e-4
+    l1 = lambda x, y: np.abs(x - y).sum() / np.abs(y).sum()
+    assert l1(b[5 + 2], a[5 + 2]) < 0.5     # water, a product of a 30 ns run
