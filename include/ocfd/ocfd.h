@@ -459,8 +459,8 @@ ocfd_status ocfd_tc_gemm_bf16(ocfd_context* ctx, const uint16_t* A, const uint16
 /* ------------------------------------------------ chemistry surrogate network
  * MLP 12 -> 128 x 4 (GELU) -> 10 on the tensor cores: BF16 weights and
  * activations, FP32 accumulation (tcgen05.mma into tensor memory).  Inputs
- * (T, p, 9 Y, log10 dt) and outputs (increments of T and of the 9 Y) are used
- * normalised: x_n = (x - in_mu) * in_isd, y = y_n * out_sd + out_mu.
+ * (T, ln p, sqrt of the 9 Y, log10 dt) and outputs (rates of T and of the 9 Y)
+ * are used normalised: x_n = (x - in_mu) * in_isd, y = y_n * out_sd + out_mu.
  * Weights: five row-major (out x in) blocks W1 128x16 (inputs padded from 12),
  * W2..W4 128x128, W5 16x128 (outputs padded from 10), 53248 floats; biases
  * 128 x 4 + 16 = 528 floats.                                                    */
@@ -474,6 +474,10 @@ ocfd_status ocfd_mlp_create(ocfd_context* ctx, int32_t max_batch, uint64_t seed,
 ocfd_status ocfd_mlp_destroy(ocfd_mlp* mlp);
 ocfd_status ocfd_mlp_set_norm(ocfd_mlp* mlp, const float in_mu[12], const float in_isd[12], const float out_mu[10],
                               const float out_sd[10]);
+/* Outputs as signed logarithms of rates: with scale[k] > 0 the network's output
+ * y_k (after out_mu / out_sd) stands for the rate sign(y) scale[k] expm1(|y|),
+ * and an increment over dt is rate * dt (0: y is the rate itself). */
+ocfd_status ocfd_mlp_set_target_scale(ocfd_mlp* mlp, const float scale[10]);
 /* FP32 master parameters (host arrays of OCFD_MLP_WEIGHTS / OCFD_MLP_BIASES). */
 ocfd_status ocfd_mlp_get_params(ocfd_mlp* mlp, float* W, float* b);
 ocfd_status ocfd_mlp_set_params(ocfd_mlp* mlp, const float* W, const float* b);

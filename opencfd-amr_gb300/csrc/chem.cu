@@ -214,7 +214,8 @@ __global__ void k_chem_props(const long long* __restrict__ off, const long long*
 __constant__ float c_elem[3][NSP] = {{2, 0, 2, 1, 0, 1, 1, 2, 0}, {0, 2, 1, 0, 1, 1, 2, 2, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 2}};
 
 // One chemistry substep by the network for the cells of a list, 128 cells per
-// tile (thread = cell): inputs (T, p, Y, log10 dt) -> increments of T and Y.
+// tile (thread = cell): inputs (T, p, Y, log10 dt) -> rates of T and Y (the
+// increments over the substep divided by dt).
 // Cells whose inputs leave the training range, or whose increments break the
 // species bounds or the H / O / N element balance beyond the guard's
 // tolerances, are appended to the fallback list for the FP64 substep.
@@ -253,11 +254,12 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
             ns = stride[c];
             cell_props(x, ns, P, &T, &p, Y, &rho, r);
         }
+        // features: T, ln p, sqrt(Y), log10 dt, normalised
         float f[16];
         f[0] = ((float)T - net.in_mu[0]) * net.in_isd[0];
-        f[1] = ((float)p - net.in_mu[1]) * net.in_isd[1];
+        f[1] = ((valid ? (float)log(p) : 0.0f) - net.in_mu[1]) * net.in_isd[1];
 #pragma unroll
-        for (int n = 0; n < NSP; ++n) f[2 + n] = ((float)Y[n] - net.in_mu[2 + n]) * net.in_isd[2 + n];
+        for (int n = 0; n < NSP; ++n) f[2 + n] = ((float)sqrt(Y[n] > 0 ? Y[n] : 0.0) - net.in_mu[2 + n]) * net.in_isd[2 + n];
         f[11] = (ldt - net.in_mu[11]) * net.in_isd[11];
 #pragma unroll
         for (int k = 0; k < 16; ++k)
@@ -267,7 +269,12 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
         if (!ok || !valid) continue;
         double dY[NSP];
 #pragma unroll
-        for (int n = 0; n < NSP; ++n) dY[n] = (double)(out[1 + n] * net.out_sd[1 + n] + net.out_mu[1 + n]);
+        for (int n = 0; n < NSP; ++n) {
+            const float y = out[1 + n] * net.out_sd[1 + n] + net.out_mu[1 + n];
+            const float sc = net.out_scale[1 + n];
+            const float rate = sc > 0.0f ? copysignf(sc * expm1f(fabsf(y)), y) : y;
+            dY[n] = (double)rate * dt;
+        }
         bool pass = dt_in && T >= g.T_min && T <= g.T_max && p >= g.p_min && p <= g.p_max;
 #pragma unroll
         for (int n = 0; n < NSP; ++n) pass = pass && Y[n] + dY[n] >= -g.y_tol && Y[n] + dY[n] <= 1.0 + g.y_tol;

@@ -327,7 +327,7 @@ struct ocfd_mlp {
     int max_batch = 0;
     float *W32 = nullptr, *b32 = nullptr, *mW = nullptr, *vW = nullptr, *mb = nullptr, *vb = nullptr;
     uint16_t* Wb = nullptr;
-    float norm[2 * ocfd::MLP_IN + 2 * ocfd::MLP_OUT] = {};
+    float norm[2 * ocfd::MLP_IN + 3 * ocfd::MLP_OUT] = {};
     long long steps = 0;
     // training scratch (max_batch rows)
     uint16_t* Xb = nullptr;
@@ -359,6 +359,7 @@ MlpNet mlp_net(const ocfd_mlp* n) {
     for (int i = 0; i < MLP_OUT; ++i) {
         d.out_mu[i] = n->norm[2 * MLP_IN + i];
         d.out_sd[i] = n->norm[2 * MLP_IN + MLP_OUT + i];
+        d.out_scale[i] = n->norm[2 * MLP_IN + 2 * MLP_OUT + i];
     }
     return d;
 }
@@ -504,6 +505,12 @@ ocfd_status ocfd_mlp_set_norm(ocfd_mlp* n, const float* in_mu, const float* in_i
         n->norm[2 * MLP_IN + i] = out_mu[i];
         n->norm[2 * MLP_IN + MLP_OUT + i] = out_sd[i];
     }
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_mlp_set_target_scale(ocfd_mlp* n, const float* scale) {
+    if (!n || !scale) return fail(OCFD_BAD_ARG, "ocfd_mlp_set_target_scale");
+    for (int i = 0; i < MLP_OUT; ++i) n->norm[2 * MLP_IN + 2 * MLP_OUT + i] = scale[i];
     return OCFD_OK;
 }
 

@@ -51,6 +51,7 @@ struct MlpNet {
     const float* b;     // FP32 biases, BTOT
     float in_mu[MLP_IN], in_isd[MLP_IN];     // feature normalisation: (x - mu) * isd
     float out_mu[MLP_OUT], out_sd[MLP_OUT];  // target scaling: y * sd + mu
+    float out_scale[MLP_OUT];                // > 0: y is sign(r) log1p(|r| / scale) of the rate r
 };
 
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }

@@ -16,6 +16,7 @@ declare("ocfd_mlp_create", ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_uint64, 
 declare("ocfd_mlp_destroy", ctypes.c_int, [_vp])
 declare("ocfd_mlp_set_norm", ctypes.c_int, [_vp, _fp, _fp, _fp, _fp])
 declare("ocfd_mlp_get_params", ctypes.c_int, [_vp, _vp, _vp])
+declare("ocfd_mlp_set_target_scale", ctypes.c_int, [_vp, _fp])
 declare("ocfd_mlp_set_params", ctypes.c_int, [_vp, _vp, _vp])
 declare("ocfd_mlp_forward", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, _vp])
 declare("ocfd_mlp_train_step", ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, ctypes.c_float, ctypes.c_int32,
@@ -50,6 +51,10 @@ class Mlp:
     def set_norm(self, in_mu, in_isd, out_mu, out_sd):
         a = [_f(x) for x in (in_mu, in_isd, out_mu, out_sd)]
         check(self.lib.ocfd_mlp_set_norm(self.h, *[p for _, p in a]), "ocfd_mlp_set_norm")
+
+    def set_target_scale(self, scale):
+        a, p = _f(scale)
+        check(self.lib.ocfd_mlp_set_target_scale(self.h, p), "ocfd_mlp_set_target_scale")
 
     def get_params(self):
         W = np.zeros(WTOT, np.float32)

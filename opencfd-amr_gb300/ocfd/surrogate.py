@@ -91,8 +91,8 @@ def generate(ctx, n_traj=32768, n_snap=300, seed=20261203, dt_lo=1e-9, dt_hi=1e-
     U = torch.as_tensor(state_tpx(ctx, T, p, X), device="cuda").contiguous()
     gen = torch.Generator(device="cuda")
     gen.manual_seed(seed)
-    # per-trajectory integration step, log-uniform in [1e-8, 5e-7] s
-    dt_traj = torch.pow(10.0, torch.empty(n_traj, dtype=torch.float64, device="cuda").uniform_(-8.0, math.log10(5e-7),
+    # per-trajectory integration step, log-uniform in [1e-8, 1e-7] s
+    dt_traj = torch.pow(10.0, torch.empty(n_traj, dtype=torch.float64, device="cuda").uniform_(-8.0, -7.0,
                                                                                                generator=gen))
     feats, targs = [], []
     t0 = time.time()
@@ -108,12 +108,20 @@ def generate(ctx, n_traj=32768, n_snap=300, seed=20261203, dt_lo=1e-9, dt_hi=1e-
         feats.append(f.T.float())
         targs.append(t.T.float())
         cells_advance(ctx, U, dt_cells=dt_traj)
+        # species clip and rescale to the density, as the solver does after each
+        # step (Source/EBR.cpp:333-357)
+        r = U[5:].clamp_min(0.0)
+        U[5:] = r * (U[0] / r.sum(0))
     Xs = torch.cat(feats, 0)
     Ts = torch.cat(targs, 0)
-    ok = torch.isfinite(Xs).all(1) & torch.isfinite(Ts).all(1)
+    # keep states inside the NASA-7 fit range (250-3500 K) before and after the
+    # substep: large linearised steps can leave it
+    Ta = Xs[:, 0] + Ts[:, 0]
+    ok = torch.isfinite(Xs).all(1) & torch.isfinite(Ts).all(1) & (Xs[:, 0] >= 250.0) & (Xs[:, 0] <= 3500.0) & \
+        (Ta >= 250.0) & (Ta <= 3500.0)
     if log:
-        log("generated %d samples in %.1f s (%d non-finite dropped)" % (Xs.shape[0], time.time() - t0,
-                                                                         int((~ok).sum())))
+        log("generated %d samples in %.1f s (%d outside the fit range or non-finite dropped)" % (
+            Xs.shape[0], time.time() - t0, int((~ok).sum())))
     return Xs[ok].contiguous(), Ts[ok].contiguous()
 
 
@@ -138,7 +146,18 @@ def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, log=
     perm = torch.randperm(n, generator=gen, device="cuda")
     nval = max(batch, int(n * val_frac) // 256 * 256)
     val, tr = perm[:nval], perm[nval:]
-    Xd, Td = X.double(), T.double()
+    # the network predicts signed logarithms of the rates (increment / dt),
+    # sign(r) log1p(|r| / s) with s the median |rate| of each output, from
+    # T, ln p, sqrt(Y), log10 dt
+    Xraw = X.double()
+    dtv = torch.pow(10.0, Xraw[:, 11])
+    Rt = T.double() / dtv[:, None]
+    scale = Rt[tr].abs().median(0).values
+    scale = torch.where(scale > 0, scale, torch.ones_like(scale))
+    Td = torch.sign(Rt) * torch.log1p(Rt.abs() / scale)
+    Xd = Xraw.clone()
+    Xd[:, 1] = torch.log(Xraw[:, 1])
+    Xd[:, 2:11] = torch.sqrt(Xraw[:, 2:11].clamp_min(0.0))
     in_mu = Xd[tr].mean(0)
     in_sd = Xd[tr].std(0).clamp_min(1e-30)
     out_mu = Td[tr].mean(0)
@@ -148,6 +167,7 @@ def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, log=
     net = Mlp(ctx, batch, seed)
     net.set_norm(in_mu.float().cpu().numpy(), (1.0 / in_sd).float().cpu().numpy(), out_mu.float().cpu().numpy(),
                  out_sd.float().cpu().numpy())
+    net.set_target_scale(scale.float().cpu().numpy())
     steps_per_epoch = tr.numel() // batch
     total = epochs * steps_per_epoch
     t0 = time.time()
@@ -170,10 +190,12 @@ def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, log=
     Yv = []
     for b in range(0, nval, batch):
         Yv.append(net.forward(Xn[val[b:b + batch]].contiguous()))
-    Yv = torch.cat(Yv).double() * out_sd + out_mu
-    Tv = Td[val]
-    Xv = Xd[val]
-    val_loss = float((((Yv - Tv) / out_sd) ** 2).mean())
+    yv = torch.cat(Yv).double()
+    val_loss = float(((yv - Tn[val].double()) ** 2).mean())
+    yv = yv * out_sd + out_mu
+    Yv = torch.sign(yv) * scale * torch.expm1(yv.abs()) * dtv[val, None]
+    Tv = T.double()[val]
+    Xv = Xraw[val]
     # element balance of the predicted increments (relative to the content)
     W = np.array([2.016e-3, 31.998e-3, 18.015e-3, 1.008e-3, 15.999e-3, 17.007e-3, 33.006e-3, 34.014e-3, 28.014e-3])
     E = torch.as_tensor(ELEM / W[None], device="cuda")
@@ -181,13 +203,13 @@ def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, log=
     dbal = (Yv[:, 1:] @ E.T).abs() / have.clamp_min(1e-300)
     elem_err = dbal.max(1).values
     elem_tol = float(torch.quantile(elem_err.float(), 0.99))
-    guard = Guard(T_min=float(Xd[tr, 0].min()), T_max=float(Xd[tr, 0].max()), p_min=float(Xd[tr, 1].min()),
-                  p_max=float(Xd[tr, 1].max()), dt_min=float(10 ** Xd[tr, 11].min()),
-                  dt_max=float(10 ** Xd[tr, 11].max()), y_tol=1e-3, elem_tol=elem_tol)
+    guard = Guard(T_min=float(Xraw[tr, 0].min()), T_max=float(Xraw[tr, 0].max()), p_min=float(Xraw[tr, 1].min()),
+                  p_max=float(Xraw[tr, 1].max()), dt_min=float(10 ** Xraw[tr, 11].min()),
+                  dt_max=float(10 ** Xraw[tr, 11].max()), y_tol=1e-3, elem_tol=elem_tol)
     rel = lambda k: float(((Yv[:, k] - Tv[:, k]).abs().mean() / Tv[:, k].abs().mean()))
     report = {"samples": int(n), "train_samples": int(tr.numel()), "val_samples": int(nval), "epochs": epochs,
               "batch": batch, "train_seconds": train_s, "final_train_loss": losses[-1], "val_loss": val_loss,
               "first_epoch_loss": losses[0], "val_rel_l1_dT": rel(0), "val_rel_l1_dY_OH": rel(1 + 5),
               "val_rel_l1_dY_H2O": rel(1 + 2), "guard_elem_tol": elem_tol}
-    stats = dict(in_mu=in_mu, in_sd=in_sd, out_mu=out_mu, out_sd=out_sd)
+    stats = dict(in_mu=in_mu, in_sd=in_sd, out_mu=out_mu, out_sd=out_sd, scale=scale)
     return Surrogate(ctx, net, stats, guard), report
