@@ -209,9 +209,70 @@ __global__ void k_chem_props(const long long* __restrict__ off, const long long*
     }
 }
 
-// element content per unit mass (mol / kg): H, O, N atoms of
-// H2, O2, H2O, H, O, OH, HO2, H2O2, N2
+// H, O, N atoms of H2, O2, H2O, H, O, OH, HO2, H2O2, N2
 __constant__ float c_elem[3][NSP] = {{2, 0, 2, 1, 0, 1, 1, 2, 0}, {0, 2, 1, 0, 1, 1, 2, 2, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 2}};
+
+// FP32 thermochemistry of the surrogate substep, per unit mass, built once per
+// CTA from the NASA-7 tables: the network's inputs are BF16-rounded, so T and p
+// only need FP32 accuracy, and the FP64 Newton of the plain substep (divisions
+// by the molar masses and by 3 and 5 in every evaluation) would cost more than
+// the network itself.
+struct SurThermo {
+    float ce[2][NSP][6];  // e_n(T) = c5 + T (c0 + T (c1 + T (c2 + T (c3 + T c4)))) [J/kg], T < 1000 K | >= 1000 K
+    float iw[NSP];        // 1 / W_n
+    float elem[3][NSP];   // atoms per unit mass (mol/kg) of each element
+    double hw[NSP];       // d(rho e)/d(rho_n) of the chemistry update, -HP_n Ru / W_n (ChemAdvance.cpp:70-75)
+};
+constexpr int S_THERMO = (S_TOT + 15) / 16 * 16;
+constexpr int S_SUR_TOT = S_THERMO + (int)sizeof(SurThermo);
+
+__device__ __forceinline__ void sur_thermo_build(SurThermo& th, double Ru) {
+    const int n = threadIdx.x;
+    if (n >= NSP) return;
+    const double rw = Ru / c_mech.mw[n];
+    for (int h = 0; h < 2; ++h) {
+        const double* a = h ? c_mech.hi[n] : c_mech.lo[n];
+        // e/(RT) of speciesInternalEnergy (LiDryer.H:531-614) times R T / W
+        th.ce[h][n][0] = (float)(rw * (a[0] - 1.0));
+        th.ce[h][n][1] = (float)(rw * a[1] / 2.0);
+        th.ce[h][n][2] = (float)(rw * a[2] / 3.0);
+        th.ce[h][n][3] = (float)(rw * a[3] / 4.0);
+        th.ce[h][n][4] = (float)(rw * a[4] / 5.0);
+        th.ce[h][n][5] = (float)(h ? rw * (a[5] - c_mech.lo[n][5]) : 0.0);
+    }
+    th.iw[n] = (float)(1.0 / c_mech.mw[n]);
+    for (int e = 0; e < 3; ++e) th.elem[e][n] = (float)(c_elem[e][n] / c_mech.mw[n]);
+    th.hw[n] = -c_mech.HP[n] * Ru / c_mech.mw[n];
+}
+
+// T from the internal energy per unit mass: Newton on the mixture polynomial
+// (its coefficients summed once), a fixed five iterations from 1500 K (the
+// energy is close to linear in T, so the error after five is at FP32 rounding
+// for 250-3500 K); T is kept inside [200, 5000] K on the way.
+__device__ __forceinline__ float sur_temperature(const SurThermo& th, const float* Y, float e) {
+    float lo[6], hi[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) lo[k] = hi[k] = 0.0f;
+#pragma unroll
+    for (int n = 0; n < NSP; ++n)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            lo[k] = fmaf(Y[n], th.ce[0][n][k], lo[k]);
+            hi[k] = fmaf(Y[n], th.ce[1][n][k], hi[k]);
+        }
+    float T = 1500.0f;
+#pragma unroll
+    for (int it = 0; it < 5; ++it) {
+        const bool h = T >= 1000.0f;
+        float c[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) c[k] = h ? hi[k] : lo[k];
+        const float ev = fmaf(T, fmaf(T, fmaf(T, fmaf(T, fmaf(T, c[4], c[3]), c[2]), c[1]), c[0]), c[5]);
+        const float cv = fmaf(T, fmaf(T, fmaf(T, fmaf(T, 5.0f * c[4], 4.0f * c[3]), 3.0f * c[2]), 2.0f * c[1]), c[0]);
+        T = fminf(fmaxf(T + (e - ev) / cv, 200.0f), 5000.0f);
+    }
+    return T;
+}
 
 // One chemistry substep by the network for the cells of a list, 128 cells per
 // tile (thread = cell): inputs (T, p, Y, log10 dt) -> rates of T and Y (the
@@ -219,6 +280,8 @@ __constant__ float c_elem[3][NSP] = {{2, 0, 2, 1, 0, 1, 1, 2, 0}, {0, 2, 1, 0, 1
 // Cells whose inputs leave the training range, or whose increments break the
 // species bounds or the H / O / N element balance beyond the guard's
 // tolerances, are appended to the fallback list for the FP64 substep.
+// Accepted cells update rho Y_n (clipped at 0) and rho E as the FP64 substep
+// does (ChemAdvance.cpp:62-80).
 __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long long* __restrict__ off,
                                                         const long long* __restrict__ stride, long long ncell,
                                                         double* Ubuf, double dt, DevParm P, ocfd_surrogate_guard g,
@@ -227,8 +290,10 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S_BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S_BAR + 8);
+    SurThermo& th = *reinterpret_cast<SurThermo*>(sm + S_THERMO);
     const int tid = threadIdx.x, warp = tid >> 5;
     mlp_stage_weights(net, sm);
+    sur_thermo_build(th, P.Ru);
     if (tid == 0) mbar_init(bar, 1);
     if (warp == 0) {
         tmem_alloc(tslot, 128);
@@ -243,23 +308,42 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
     const long long ntile = (ncell + 127) / 128;
     const float ldt = (float)log10(dt);
     const bool dt_in = dt >= g.dt_min && dt <= g.dt_max;
+    const float Ru = (float)P.Ru, fdt = (float)dt;
+    const float T_min = (float)g.T_min, T_max = (float)g.T_max, p_min = (float)g.p_min, p_max = (float)g.p_max;
+    const float y_tol = (float)g.y_tol, elem_tol = (float)g.elem_tol;
     for (long long t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
         const long long c = t * 128 + tid;
         const bool valid = c < ncell;
-        double T = 0, p = 0, Y[NSP] = {}, rho = 1, r[NSP] = {};
         double* x = nullptr;
         long long ns = 0;
+        double rho = 1.0, r[NSP];
+        float Y[NSP], T = 0.0f, p = 1.0f;
         if (valid) {
             x = Ubuf + off[c];
             ns = stride[c];
-            cell_props(x, ns, P, &T, &p, Y, &rho, r);
+            rho = dmax(x[0], P.smallr);
+            const double rhoinv = 1.0 / rho;
+            const double ux = x[ns] * rhoinv, uy = x[2 * ns] * rhoinv, uz = x[3 * ns] * rhoinv;
+            const float em = (float)(x[4 * ns] * rhoinv - 0.5 * (ux * ux + uy * uy + uz * uz));
+            float wsum = 0.0f;
+#pragma unroll
+            for (int n = 0; n < NSP; ++n) {
+                r[n] = x[(5 + n) * ns];
+                Y[n] = (float)(r[n] * rhoinv);
+                wsum = fmaf(Y[n], th.iw[n], wsum);
+            }
+            T = sur_temperature(th, Y, em);
+            p = (float)rho * Ru * T * wsum;
+        } else {
+#pragma unroll
+            for (int n = 0; n < NSP; ++n) r[n] = 0.0, Y[n] = 0.0f;
         }
         // features: T, ln p, sqrt(Y), log10 dt, normalised
         float f[16];
-        f[0] = ((float)T - net.in_mu[0]) * net.in_isd[0];
-        f[1] = ((valid ? (float)log(p) : 0.0f) - net.in_mu[1]) * net.in_isd[1];
+        f[0] = (T - net.in_mu[0]) * net.in_isd[0];
+        f[1] = ((valid ? logf(p) : 0.0f) - net.in_mu[1]) * net.in_isd[1];
 #pragma unroll
-        for (int n = 0; n < NSP; ++n) f[2 + n] = ((float)sqrt(Y[n] > 0 ? Y[n] : 0.0) - net.in_mu[2 + n]) * net.in_isd[2 + n];
+        for (int n = 0; n < NSP; ++n) f[2 + n] = (sqrtf(fmaxf(Y[n], 0.0f)) - net.in_mu[2 + n]) * net.in_isd[2 + n];
         f[11] = (ldt - net.in_mu[11]) * net.in_isd[11];
 #pragma unroll
         for (int k = 0; k < 16; ++k)
@@ -267,35 +351,68 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
         float out[16];
         ok = mlp_tile(sm, tbase, bar, phase, out, nullptr, nullptr, 0);
         if (!ok || !valid) continue;
-        double dY[NSP];
+        float dY[NSP];
 #pragma unroll
         for (int n = 0; n < NSP; ++n) {
             const float y = out[1 + n] * net.out_sd[1 + n] + net.out_mu[1 + n];
             const float sc = net.out_scale[1 + n];
-            const float rate = sc > 0.0f ? copysignf(sc * expm1f(fabsf(y)), y) : y;
-            dY[n] = (double)rate * dt;
+            dY[n] = (sc > 0.0f ? copysignf(sc * expm1f(fabsf(y)), y) : y) * fdt;
         }
-        bool pass = dt_in && T >= g.T_min && T <= g.T_max && p >= g.p_min && p <= g.p_max;
+        bool pass = dt_in && T >= T_min && T <= T_max && p >= p_min && p <= p_max;
 #pragma unroll
-        for (int n = 0; n < NSP; ++n) pass = pass && Y[n] + dY[n] >= -g.y_tol && Y[n] + dY[n] <= 1.0 + g.y_tol;
-        for (int e = 0; e < 3 && pass; ++e) {
-            double have = 0, d = 0;
+        for (int n = 0; n < NSP; ++n) pass = pass && Y[n] + dY[n] >= -y_tol && Y[n] + dY[n] <= 1.0f + y_tol;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            float have = 0.0f, d = 0.0f;
 #pragma unroll
             for (int n = 0; n < NSP; ++n) {
-                have += c_elem[e][n] * Y[n] / c_mech.mw[n];
-                d += c_elem[e][n] * dY[n] / c_mech.mw[n];
+                have = fmaf(th.elem[e][n], Y[n], have);
+                d = fmaf(th.elem[e][n], dY[n], d);
             }
-            pass = fabs(d) <= g.elem_tol * have;
+            pass = pass && fabsf(d) <= elem_tol * have;
+        }
+        // accepted increments are made element-conserving: N2 is inert, and the
+        // H and O imbalance is removed by the correction of least weighted norm
+        // with weights |dY_n| (each increment absorbs a share of the imbalance in
+        // proportion to its own size), on the increments scaled by their sum
+        if (pass) {
+            dY[NSP - 1] = 0.0f;
+            float S = 0.0f;
+#pragma unroll
+            for (int n = 0; n < NSP - 1; ++n) S += fabsf(dY[n]);
+            if (S > 0.0f) {
+                const float iS = 1.0f / S;
+                float w[NSP - 1], m00 = 0, m01 = 0, m11 = 0, r0 = 0, r1 = 0;
+#pragma unroll
+                for (int n = 0; n < NSP - 1; ++n) {
+                    const float u = dY[n] * iS, aH = th.elem[0][n], aO = th.elem[1][n];
+                    w[n] = fabsf(u) + 1e-6f;
+                    m00 = fmaf(w[n] * aH, aH, m00);
+                    m01 = fmaf(w[n] * aH, aO, m01);
+                    m11 = fmaf(w[n] * aO, aO, m11);
+                    r0 = fmaf(aH, u, r0);
+                    r1 = fmaf(aO, u, r1);
+                }
+                const float det = m00 * m11 - m01 * m01;
+                if (det > 1e-6f * m00 * m11) {
+                    const float l0 = (m11 * r0 - m01 * r1) / det, l1 = (m00 * r1 - m01 * r0) / det;
+#pragma unroll
+                    for (int n = 0; n < NSP - 1; ++n)
+                        dY[n] = S * (dY[n] * iS - w[n] * (th.elem[0][n] * l0 + th.elem[1][n] * l1));
+                } else {
+                    pass = false;
+                }
+            }
         }
         if (pass) {
             double dei = 0;
 #pragma unroll
             for (int n = 0; n < NSP; ++n) {
-                const double drho = rho * dY[n];
+                const double drho = rho * (double)dY[n];
                 double v = r[n] + drho;
                 if (v < 0) v = 0.0;
                 x[(5 + n) * ns] = v;
-                dei += -c_mech.HP[n] * P.Ru / c_mech.mw[n] * drho;
+                dei += th.hw[n] * drho;
             }
             x[4 * ns] += dei;
         } else {
@@ -317,13 +434,13 @@ ocfd_status launch_chem_surrogate(const ocfd_mlp* mlp, const long long* off, con
                                   unsigned long long* fb_total, unsigned* err, int sms, cudaStream_t st) {
     static bool configured = false;
     if (!configured) {
-        if (cudaFuncSetAttribute(k_chem_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, S_TOT) != cudaSuccess)
+        if (cudaFuncSetAttribute(k_chem_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, S_SUR_TOT) != cudaSuccess)
             return check_launch("surrogate attribute");
         configured = true;
     }
     if (ncell <= 0) return OCFD_OK;
     const long long ntile = (ncell + 127) / 128;
-    k_chem_surrogate<<<(unsigned)std::min<long long>(ntile, sms), 128, S_TOT, st>>>(
+    k_chem_surrogate<<<(unsigned)std::min<long long>(ntile, sms), 128, S_SUR_TOT, st>>>(
         mlp_net(mlp), off, stride, ncell, U, dt, P, g, fb_off, fb_stride, fb_count, fb_total, err);
     return check_launch("surrogate chemistry substep");
 }

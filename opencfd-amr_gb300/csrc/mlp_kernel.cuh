@@ -62,8 +62,13 @@ __device__ __forceinline__ void mlp_stage_weights(const MlpNet& net, unsigned ch
         const int N = LN(l), K = LK(l);
         unsigned char* dst = sm + S_W + WOFF(l) * 2;
         const uint16_t* src = net.W + WOFF(l);
-        for (int e = threadIdx.x; e < N * K; e += blockDim.x)
-            *reinterpret_cast<uint16_t*>(dst + kmajor_offset(e / K, e % K, N)) = src[e];
+        // 8 consecutive k of a row are one 16-byte core-matrix row in both layouts
+        // (W and every WOFF(l) * 2 are 16-byte aligned)
+        for (int q = threadIdx.x; q < N * K / 8; q += blockDim.x) {
+            const int n = q / (K / 8), k = (q % (K / 8)) * 8;
+            *reinterpret_cast<uint4*>(dst + kmajor_offset(n, k, N)) =
+                __ldg(reinterpret_cast<const uint4*>(src + (long long)n * K + k));
+        }
     }
     float* sb = reinterpret_cast<float*>(sm + S_B);
     for (int e = threadIdx.x; e < BTOT; e += blockDim.x) sb[e] = net.b[e];

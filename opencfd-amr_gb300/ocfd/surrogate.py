@@ -135,7 +135,7 @@ class Surrogate:
         self.guard = guard
 
 
-def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, log=None):
+def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, rate_scale=100.0, log=None):
     """Normalise, train with Adam on the tensor-core kernels (cosine schedule),
     calibrate the guard on held-out samples.  Returns (Surrogate, report)."""
     import torch
@@ -147,12 +147,12 @@ def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, log=
     nval = max(batch, int(n * val_frac) // 256 * 256)
     val, tr = perm[:nval], perm[nval:]
     # the network predicts signed logarithms of the rates (increment / dt),
-    # sign(r) log1p(|r| / s) with s the median |rate| of each output, from
-    # T, ln p, sqrt(Y), log10 dt
+    # sign(r) log1p(|r| / s) with s = rate_scale x the median |rate| of each
+    # output (linear below s, logarithmic above), from T, ln p, sqrt(Y), log10 dt
     Xraw = X.double()
     dtv = torch.pow(10.0, Xraw[:, 11])
     Rt = T.double() / dtv[:, None]
-    scale = Rt[tr].abs().median(0).values
+    scale = Rt[tr].abs().median(0).values * rate_scale
     scale = torch.where(scale > 0, scale, torch.ones_like(scale))
     Td = torch.sign(Rt) * torch.log1p(Rt.abs() / scale)
     Xd = Xraw.clone()

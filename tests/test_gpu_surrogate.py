@@ -16,15 +16,15 @@ def ctx():
 @pytest.fixture(scope="module")
 def trained(ctx):
     from ocfd import surrogate
-    X, T = surrogate.generate(ctx, n_traj=4096, n_snap=48, seed=5)
-    sur, rep = surrogate.train(ctx, X, T, epochs=12, batch=4096, lr=2e-3, seed=2)
+    X, T = surrogate.generate(ctx, n_traj=8192, n_snap=96, seed=5)
+    sur, rep = surrogate.train(ctx, X, T, epochs=30, batch=8192, lr=2e-3, seed=2)
     return X, T, sur, rep
 
 
 def test_samples_are_physical(trained):
     import torch
     X, T, _, _ = trained
-    assert X.shape[1] == 12 and T.shape[1] == 10 and X.shape[0] > 150000
+    assert X.shape[1] == 12 and T.shape[1] == 10 and X.shape[0] > 700000
     Y = X[:, 2:11]
     assert float(Y.min()) >= 0.0 and torch.allclose(Y.sum(1), torch.ones_like(Y[:, 0]), atol=1e-6)
     assert float(X[:, 0].min()) >= 250.0 and float(X[:, 0].max()) <= 3500.0
@@ -39,31 +39,64 @@ def test_training_lowers_the_loss(trained):
     assert rep["val_loss"] < 1.5 * rep["final_train_loss"] + 1e-3
 
 
+def _timed(fn, reps=5):
+    import torch
+    fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def test_surrogate_substep_vs_fp64(ctx, trained):
-    """one network substep of 0D states against the FP64 substep: the guard's
-    fallback keeps every state physical and the temperature error small"""
+    """What the network gains over the FP64 implicit substep it stands in for:
+    the same substep of 1M 0D states (the reacting box's substep, 1.25 ns) at
+    several times the cell rate, the guard's FP64 fallback keeping every state
+    physical, and the temperature error within a small multiple of the
+    temperature change itself (a broken network, wrong sign or scale, is off by
+    orders of magnitude)."""
     import torch
     from ocfd import surrogate
     from ocfd.react import state_tpx
     _, _, sur, _ = trained
     rng = np.random.default_rng(9)
-    Tm, p, X = surrogate.mixtures(rng, 8192)
+    n = 1 << 20
+    Tm, p, X = surrogate.mixtures(rng, n)
     U0 = torch.as_tensor(state_tpx(ctx, Tm, p, X), device="cuda").contiguous()
-    # advance a little so that radicals exist
-    surrogate.cells_advance(ctx, U0, dt=2e-7)
-    surrogate.cells_advance(ctx, U0, dt=2e-7)
+    # advance so that radicals exist (0.4 us in steps of 10 ns: the linearised
+    # implicit substep leaves the physical range on steps of 100 ns in a few
+    # cells), keep the cells inside the tables' 250-3500 K
+    for _ in range(40):
+        surrogate.cells_advance(ctx, U0, dt=1e-8)
+    T0 = surrogate.cells_props(ctx, U0)[0]
+    keep = torch.isfinite(U0).all(0) & (T0 >= 250.0) & (T0 <= 3500.0)
+    assert int(keep.sum()) > 0.99 * n
+    U0 = U0[:, keep].contiguous()
+    n = U0.shape[1]
+    dt = 1.25e-9
     a, b = U0.clone(), U0.clone()
-    dt = 1e-7
     surrogate.cells_advance(ctx, a, dt=dt)
     fb = surrogate.cells_surrogate(ctx, sur.net, sur.guard, b, dt)
-    pa = surrogate.cells_props(ctx, a)
-    pb = surrogate.cells_props(ctx, b)
-    p0 = surrogate.cells_props(ctx, U0)
-    assert 0 <= fb < 8192
+    pa, pb, p0 = surrogate.cells_props(ctx, a), surrogate.cells_props(ctx, b), surrogate.cells_props(ctx, U0)
+    assert 0 <= fb < n // 20
     assert torch.isfinite(b).all() and float(b[5:].min()) >= 0.0
-    dT_true = (pa[0] - p0[0]).abs().mean()
-    err = (pb[0] - pa[0]).abs().mean()
-    assert float(err) < float(dT_true), (float(err), float(dT_true))
+    dT_true = float((pa[0] - p0[0]).abs().mean())
+    err = float((pb[0] - pa[0]).abs().mean())
+    assert err < 3.0 * dT_true, (err, dT_true)
+    # density and momentum are untouched; accepted increments conserve the
+    # elements, so the species mass is unchanged but for the clip of partial
+    # densities driven below zero (the guard admits Y + dY >= -y_tol)
+    assert torch.equal(b[:4], U0[:4])
+    dm = (b[5:].sum(0) - U0[5:].sum(0)).abs() / b[0]
+    assert float(dm.median()) < 1e-6 and float(dm.max()) < 2e-3
+    Ua, Ub = U0.clone(), U0.clone()
+    t_fp64 = _timed(lambda: surrogate.cells_advance(ctx, Ua, dt=dt))
+    t_sur = _timed(lambda: surrogate.cells_surrogate(ctx, sur.net, sur.guard, Ub, dt))
+    assert t_sur * 3.0 < t_fp64, (t_sur, t_fp64)
 
 
 def test_reacting_level_with_surrogate(ctx, trained):
