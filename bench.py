@@ -188,6 +188,8 @@ def cpu_time_steps(c, steps, threads=None):
     bc.dom_lo[:] = [0, 0, 0]; bc.dom_hi[:] = [n - 1 for n in c["n"]]
     if c["bc_case"] == 1:
         bc.dmr_left[:] = list(c["case_params"][:5]); bc.dmr_right[:] = list(c["case_params"][5:10])
+    if c["bc_case"] == 3:
+        bc.jet[:] = list(c["case_params"][:8])
     S = np.ascontiguousarray(c["G"].copy())
     t0 = time.perf_counter()
     o.advance_rk3(bc, S, CFL, steps, form=1)
@@ -203,6 +205,13 @@ def cpu_sample_workload(config):
         c = workload("dmr")
         c["name"] = amr_workload()["name"]
         c["sample_note"] = "base grid 1024x256x2 only (no refined levels)"
+        return c
+    if config == "jet-eb-amr":
+        from ocfd import cases
+        c = cases.jet_eb(*JET_N)
+        c["name"] = jet_workload()["name"]
+        c["sample_note"] = ("base grid %dx%dx%d only, regular scheme everywhere (no refined levels, the cylinder's "
+                            "cut cells not included)" % JET_N)
         return c
     c = workload(config)
     c["sample_note"] = "full workload"
@@ -252,14 +261,15 @@ def make_hierarchy(ctx, c, regrid_int):
                      c["max_grid_size"], c["n_error_buf"], regrid_int, c["refine_dengrad"])
 
 
-def amr_matched_l1(ctx, c, snap, steps=L1_STEPS):
+def amr_matched_l1(ctx, c, snap, steps=L1_STEPS, mk=None):
     """L1 (sum|a-b| / sum|b| over valid cells, as fcompare) of density and
     pressure between the FP32 and FP64 forms after `steps` coarse steps from the
     same state: the FP64 run regrids every 2 steps and the FP32 run replays its
     grids, so every level compares on identical grids."""
     import numpy as np
     import ocfd
-    Hd = make_hierarchy(ctx, c, 0)
+    mk = mk or (lambda ri: make_hierarchy(ctx, c, ri))
+    Hd = mk(0)
     Hd.restore(snap)
     grids_at = {}
     for i in range(steps):
@@ -270,7 +280,7 @@ def amr_matched_l1(ctx, c, snap, steps=L1_STEPS):
     t_end = Hd.time()[0]
     ref = [Hd.level_global(l) for l in range(Hd.nlevels())]
     Hd.close()
-    Hf = make_hierarchy(ctx, c, 0)
+    Hf = mk(0)
     Hf.restore(snap)
     Hf.set_stop_time(t_end)
     for i in range(steps):
@@ -294,6 +304,167 @@ def amr_matched_l1(ctx, c, snap, steps=L1_STEPS):
     out["linf_rho_rel"] = max(float(np.abs(a[0][m] - b[0][m]).max() / np.abs(b[0][m]).max())
                               for (a, m), (b, _) in zip(got, ref))
     return out
+
+
+JET_N = (256, 128, 128)
+JET_DEV_STEPS = 20
+
+
+def jet_workload():
+    from ocfd import cases
+    c = cases.jet_eb_amr(*JET_N, max_level=2, blocking_factor=8, max_grid=32, n_error_buf=1, refine_dengrad=0.1,
+                         regrid_int=2)
+    c["name"] = ("Mach 2 planar jet past a z-cylinder EB (r=0.1) in 2x1x1, base %dx%dx%d + 2 levels (ratio 2, "
+                 "|drho|>=0.1 tagging, regrid every 2 coarse steps, blocking 8, max grid 32), KH perturbation "
+                 "1e-2 (seed %d), inflow jet / outflow / periodic z, subcycled SSP-RK3, CFL 0.5, cut cells with "
+                 "the small-cell rescale, timed after %d coarse steps" % (JET_N + (c["seed"], JET_DEV_STEPS)))
+    return c
+
+
+def run_ours_jet(args, world, rank, local):
+    """configs[3]: the multi-level EB jet.  Forms timed from the same developed
+    state: the batched graph (one launch per level per RK stage for the regular
+    boxes + three for the cut / covered boxes, autotuned tile shape and
+    schedule) in FP32-flux and FP64, and the reference's execution model in
+    FP64 (per-box launches issued from the host, no graph)."""
+    import numpy as np
+    import torch
+    import ocfd
+    from ocfd.level import eb_desc
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    c = jet_workload()
+    ctx = ocfd.Context(device=local)
+    eb = eb_desc(center=c["eb"]["center"], radius=c["eb"]["radius"], redistribute=c["eb"]["redistribute"])
+
+    def mk(regrid_int):
+        h = make_hierarchy(ctx, c, regrid_int)
+        h.set_eb(eb)
+        return h
+    H = mk(c["regrid_int"])
+    H.build(c["fab"])
+    H.advance(JET_DEV_STEPS, CFL, ocfd.FLUX_FP32)            # untimed: bow shock, shear layers
+    snap = H.snapshot()
+    stream = torch.cuda.current_stream(dev)
+    l2flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tuned = {}
+
+    def timed(fl, tune=True):
+        H.restore(snap)
+        if tune and not (fl & ocfd.PER_BOX):
+            H.autotune(fl, reps=3)
+            tuned[fl] = [H.tuned(l) for l in range(H.nlevels())]
+        H.advance(args.warmup, CFL, fl)
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        leaf = allc = 0
+        k0 = H.kernels_launched()
+        for e0, e1 in ev:
+            l2flush.fill_(1.0)
+            e0.record(stream)
+            H.advance(1, CFL, fl)
+            e1.record(stream)
+            a, b = H.cell_steps()
+            leaf += a
+            allc += b
+        torch.cuda.synchronize()
+        barrier(world)
+        ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
+        return ms, leaf, allc, H.kernels_launched() - k0
+
+    ms_d, leaf_d, _, k_d = timed(0)
+    ms_p, leaf_p, _, k_p = timed(ocfd.PER_BOX)
+    with ClockSampler(local) as clk:
+        ms, leaf, allc, kernels = timed(ocfd.FLUX_FP32)
+    value = leaf * world / (ms * 1e-3)
+    v64 = leaf_d * world / (ms_d * 1e-3)
+    vpb = leaf_p * world / (ms_p * 1e-3)
+    levels = [{"level": l, "boxes": len(H.grids(l)), "cells": H.level(l).cells(),
+               "boxes_regular_cut_covered": [H.box_classes(l).count(k) for k in (0, 1, 2)]}
+              for l in range(H.nlevels())]
+    nbox = sum(x["boxes"] for x in levels)
+    fin = H.level(H.nlevels() - 1)
+    stage_ms = fin.profile_stage(ocfd.FLUX_FP32, reps=10)
+    fcells = fin.cells()
+    hbm_peak, peak_src = peaks()
+    achieved = 120.0 * fcells / (stage_ms * 1e-3) / 1e9
+    fp64 = ctypes.c_double(); fp32 = ctypes.c_double()
+    ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
+
+    # end to end: every level uploaded from pinned host memory, one coarse step, every level downloaded
+    H.restore(snap)
+    H.advance(1, CFL, ocfd.FLUX_FP32)
+    torch.cuda.synchronize()
+    pins = {}
+
+    def pin(l, n):
+        if l not in pins or pins[l].numel() < n:
+            pins[l] = torch.empty(int(n * 1.5) + 1, dtype=torch.float64).pin_memory()
+        return pins[l]
+    for l in range(H.nlevels()):
+        H.copy_out(l, pin(l, H.state_elems(l)), stream)
+    torch.cuda.synchronize()
+    e2e_steps = max(2, min(args.steps, 5))
+    h2d = d2h = 0
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e2e_leaf = 0
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        for l in range(H.nlevels()):
+            H.copy_in(l, pins[l], stream)
+            h2d += 8 * H.state_elems(l)
+        H.advance(1, CFL, ocfd.FLUX_FP32, stream)
+        e2e_leaf += H.cell_steps()[0]
+        for l in range(H.nlevels()):
+            n = H.state_elems(l)
+            H.copy_out(l, pin(l, n), stream)
+            d2h += 8 * n
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_value = e2e_leaf * world / (allreduce_max(e0.elapsed_time(e1), world) * 1e-3)
+
+    l1err = amr_matched_l1(ctx, c, snap, mk=mk) if rank == 0 else None
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cs = cpu_sample_workload("jet-eb-amr")
+        dt, ccells = cpu_time_steps(cs, 1, os.cpu_count())
+        cpu = {"value": ccells / dt, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "1 RK3 step of the oracle restatement (OpenMP), %s" % cs["sample_note"]}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-flux/f64-state", "data": "synthetic",
+            "config": {"workload": c["name"], "form": "fp32 batched graph, autotuned", "levels": levels,
+                       "boxes": nbox, "leaf_cell_steps_per_coarse_step": leaf / args.steps,
+                       "forms_cell_steps_per_s": {"fp32_batched": value, "fp64_batched": v64,
+                                                  "fp64_per_box_launches": vpb},
+                       "speedup_fp32_batched_over_fp64_batched": value / v64,
+                       "speedup_fp32_batched_over_fp64_per_box": value / vpb,
+                       "speedup_batched_over_per_box_fp64": v64 / vpb,
+                       "kernels_per_coarse_step": {"fp32_batched": kernels / args.steps,
+                                                   "fp64_per_box": k_p / args.steps},
+                       "autotuned_tile_sched_per_level": {("fp32" if k else "fp64"): v for k, v in tuned.items()},
+                       "l1_vs_other_form": l1err,
+                       "l2": "flushed between timed steps (512 MB write, untimed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "k_rhs_regular fused RK stage (FP32 flux), finest level (%d cells)" % fcells,
+                         "ms_per_launch": stage_ms, "alg_bytes_per_cell": 120,
+                         "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
+                    "d2h_bytes_per_step": int(d2h / e2e_steps)},
+            "clocks": clk.summary(),
+            "gpu_launches": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    H.close()
+    ctx.close()
 
 
 def run_ours_amr(args, world, rank, local):
@@ -499,6 +670,62 @@ def react_cpu_sample(n=64, steps=1, threads=None):
     return time.perf_counter() - t0, n ** 3 * steps
 
 
+def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, same_steps):
+    """The learned chemistry form of the reacting workload: the MLP surrogate
+    (12 -> 128 x4 GELU -> 10, BF16 on tcgen05) trained here on ~1e7 samples of
+    the FP64 implicit substep (0D trajectories, T0 1000-2500 K, phi 0.5-2,
+    p 1-10 atm), then embedded in the reacting level with the guard's FP64
+    fallback.  Reports the data / training cost, the fallback rate, the
+    cell-steps/s beside the FP64 forms and the L1 error in T, Y_OH, Y_H2O
+    against the binned FP64 run after the same steps."""
+    import numpy as np
+    import torch
+    from ocfd import surrogate
+    from ocfd._abi import check, load
+
+    t0 = time.time()
+    X, T = surrogate.generate(ctx, n_traj=32768, n_snap=300, seed=20261203)
+    gen_s = time.time() - t0
+    sur, rep = surrogate.train(ctx, X, T, epochs=args.sur_epochs, batch=8192, lr=2e-3, seed=2)
+    del X, T
+    torch.cuda.empty_cache()
+
+    R = make(True)
+    check(load().ocfd_react_set_surrogate(R.h, sur.net.h, ctypes.byref(sur.guard)), "set_surrogate")
+    R.advance(args.warmup)
+    fb0 = ctypes.c_int64()
+    check(load().ocfd_react_fallbacks(R.h, ctypes.byref(fb0), None), "fallbacks")
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for e0, e1 in ev:
+        l2flush.fill_(1.0)
+        e0.record(stream)
+        R.advance(1)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
+    fb = ctypes.c_int64()
+    check(load().ocfd_react_fallbacks(R.h, ctypes.byref(fb), None), "fallbacks")
+    got = R.level.get_global()
+    R.close()
+    substeps = 8 * same_steps
+    props = lambda U: surrogate.cells_props(ctx, torch.as_tensor(U.reshape(14, -1), device="cuda").contiguous())
+    pa, pb = props(ref), props(got)
+    l1 = lambda x, y: float((x - y).abs().sum() / y.abs().sum())
+    return {
+        "form": "binned chemistry with the MLP surrogate, FP64 fallback on guard failure",
+        "cell_steps_per_s": cells * args.steps * world / (ms * 1e-3),
+        "fallback_rate": fb.value / float(cells * substeps),
+        "fallback_cells": int(fb.value), "cell_substeps": int(cells * substeps),
+        "l1_vs_fp64_after_steps": {"steps": same_steps, "T": l1(pb[0], pa[0]), "Y_OH": l1(pb[2 + 5], pa[2 + 5]),
+                                   "Y_H2O": l1(pb[2 + 2], pa[2 + 2]), "p": l1(pb[1], pa[1]),
+                                   "rho": float(np.abs(got[0] - ref[0]).sum() / np.abs(ref[0]).sum())},
+        "training": {"samples": rep["samples"], "generate_seconds": gen_s, "train_seconds": rep["train_seconds"],
+                     "epochs": rep["epochs"], "val_loss": rep["val_loss"], "val_rel_l1_dT": rep["val_rel_l1_dT"],
+                     "val_rel_l1_dY_OH": rep["val_rel_l1_dY_OH"]},
+    }
+
+
 def run_ours_react(args, world, rank, local):
     """configs[2]: 128^3 periodic H2/air with 8 hot spots, Strang chemistry around
     the RK2 multispecies flow step, dt = 1e-8 s."""
@@ -561,6 +788,9 @@ def run_ours_react(args, world, rank, local):
     rk3_vs_rk2 = {"rho": l1(c3[0], a[0]), "Y_OH": l1(y(c3, 5), y(a, 5)), "Y_H2O": l1(y(c3, 2), y(a, 2)),
                   "steps": same_steps}
 
+    sur_rep = react_surrogate_form(args, world, ctx, make, stream, l2flush, b, cells, same_steps) \
+        if not args.no_surrogate else None
+
     # end to end: upload the state, one step, download, per step
     flat = Rb.level.copy_out()
     pin = torch.from_numpy(flat).pin_memory()
@@ -601,7 +831,7 @@ def run_ours_react(args, world, rank, local):
                        "speedup_binned_over_plain": value / value_plain,
                        "forms_identical": identical,
                        "mixed_precision_flux": "not available for the multispecies RHS (FP64)",
-                       "rk3_vs_rk2_l1": rk3_vs_rk2, "boxes": len(boxes), "cells": cells,
+                       "rk3_vs_rk2_l1": rk3_vs_rk2, "surrogate": sur_rep, "boxes": len(boxes), "cells": cells,
                        "l2": "flushed between timed steps (512 MB write, untimed)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
@@ -763,10 +993,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="dmr-amr", choices=["dmr-amr", "react", "sod", "dmr", "cube"])
+    ap.add_argument("--config", default="dmr-amr", choices=["dmr-amr", "jet-eb-amr", "react", "sod", "dmr", "cube"])
     ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
                     help="headline form (the other form is timed too and reported in config)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-surrogate", action="store_true", help="react: skip the surrogate form")
+    ap.add_argument("--sur-epochs", type=int, default=6, help="react: surrogate training epochs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -777,6 +1009,8 @@ def main():
         run_ours_amr(args, world, rank, local)
     elif args.config == "react":
         run_ours_react(args, world, rank, local)
+    elif args.config == "jet-eb-amr":
+        run_ours_jet(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

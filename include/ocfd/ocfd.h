@@ -93,6 +93,9 @@ typedef struct ocfd_parm {
 #define OCFD_VISC 1u           /* EBR::do_visc (Source/EBR.cpp:25) */
 #define OCFD_REDISTRIBUTE 2u   /* EBR::do_redistribute (Source/EBR.cpp:27), cut boxes only */
 #define OCFD_FLUX_FP32 4u      /* mixed precision: split + WENO-Z in FP32, FP64 divergence */
+#define OCFD_PER_BOX 8u        /* level / hierarchy steps: the reference's execution model - every
+                                  box's RHS stage as its own launches, issued from the host each
+                                  step (no graph); for comparison with the batched graph form */
 
 typedef struct ocfd_context ocfd_context;
 
@@ -249,6 +252,11 @@ typedef struct ocfd_level ocfd_level;
 #define OCFD_CASE_NONE 0
 #define OCFD_CASE_DMR 1    /* Exec/1_DMR/prob_bcfill.cpp:9-59; params = left state (5), right state (5) */
 #define OCFD_CASE_INFLOW 2 /* constant inflow state on ext_dir faces; params = state (5) */
+/* planar jet entering through an ext_dir x-lo face: with s(y) = (1 + tanh((w -
+ * |y - yc|) / delta)) / 2, u = u_co + (u_jet - u_co) s, rho = rho_co + (rho_jet -
+ * rho_co) s, v = w = 0, uniform pressure; params = rho_jet, u_jet, u_co, yc, w,
+ * delta, rho e (internal energy per volume), rho_co */
+#define OCFD_CASE_JET 3
 
 typedef struct ocfd_level_desc {
     int32_t nbox;
@@ -296,6 +304,66 @@ int ocfd_level_launches_per_step(const ocfd_level* level, unsigned flags);
  * events on `stream`.  Overwrites the level's stage scratch buffer only. */
 ocfd_status ocfd_level_profile_stage(ocfd_level* level, unsigned flags, int reps, double* ms,
                                      void* stream);
+
+/* Autotuner of the batched stage kernel: times every tile shape that fits x
+ * every tile schedule (0: one CTA per tile; 1: persistent CTAs striding over
+ * the tiles; 2: persistent CTAs taking tiles from a work queue) over the
+ * level's own boxes - `reps` launches each after a warm-up, CUDA events on
+ * `stream` - and keeps the fastest.  Results do not depend on the choice
+ * (bit-identical).  Overwrites the level's stage scratch buffer; synchronous.
+ * tile / sched (may be NULL) receive the choice. */
+ocfd_status ocfd_level_autotune(ocfd_level* level, unsigned flags, int reps, int32_t* tile, int32_t* sched,
+                                void* stream);
+/* Set the tile shape (index, -1 keeps it) and schedule (0-2) explicitly. */
+ocfd_status ocfd_level_set_schedule(ocfd_level* level, int32_t tile, int32_t sched);
+
+/* ------------------------------------------- embedded boundary on a level
+ * The box loop of EBR::compute_dSdt (Source/Advance.cpp:201-342) over a level
+ * that an embedded body cuts: a box whose cells are all covered gets a zero
+ * right-hand side (:213-214), a box whose grow(bx, 4) holds no cut or covered
+ * cell takes the fused regular path (:231), every other box the cut-cell scheme
+ * of eb_compute_dSdt_box (Source/EB/AdvanceBox.cpp:16-228: MUSCL-minmod, Van
+ * Leer, cut-cell divergence with the wall flux).  The cut and covered boxes of
+ * a level are batched: three launches per RK stage (primitives, faces of all
+ * three directions, divergence fused with the RK stage update and the CFL
+ * bound) beside the regular boxes' launch, inside the same step graph.  The
+ * cut-cell scheme runs in FP64 in every form.
+ *
+ * AMReX's EB2 (Source/Geometry.cpp:9-29) is absent: the geometry is built on
+ * the device from an implicit function by sub-sampling - flags with the
+ * 27-neighbour connectivity (fluid neighbour, open shared face), volume
+ * fractions, area fractions - for bodies extruded along z, stored per box as
+ * z-invariant arrays (kstride 0) over grow(bx, 5) in x and y. */
+#define OCFD_EB_NONE 0
+#define OCFD_EB_CYLINDER_Z 1 /* fluid where (x-cx)^2 + (y-cy)^2 > r^2 */
+
+typedef struct ocfd_eb_desc {
+    int32_t kind;            /* OCFD_EB_* */
+    int32_t nsub;            /* sub-samples per cell edge (0: 16) */
+    double center[2];        /* axis position (x, y) */
+    double radius;
+    int32_t redistribute;    /* ebr.do_redistribute (Source/EBR.cpp:27; default 0) */
+} ocfd_eb_desc;
+
+#define OCFD_BOX_REGULAR 0
+#define OCFD_BOX_CUT 1
+#define OCFD_BOX_COVERED 2
+
+/* Build the geometry of every box of the level, classify the boxes and rebuild
+ * the stage tables (kind OCFD_EB_NONE removes the body).  Synchronous. */
+ocfd_status ocfd_level_set_eb(ocfd_level* level, const ocfd_eb_desc* eb);
+/* Class (OCFD_BOX_*) of every box, in box order. */
+ocfd_status ocfd_level_box_classes(const ocfd_level* level, int32_t* classes);
+/* Device views of the geometry of box `ibox` (a cut box; z-invariant, kstride
+ * 0): flags and volume fractions over grow(bx, 5) in x, y; area fractions
+ * ap[0..2] on the faces of grow(bx, 5) (ap[2], the z faces of an extruded body,
+ * is the volume fraction). */
+ocfd_status ocfd_level_eb_geometry(const ocfd_level* level, int ibox, ocfd_flag4* flag,
+                                   ocfd_array4* vfrac, ocfd_array4* ap);
+/* The same geometry copied to host arrays, rows of x: flag and vfrac (gy, gx),
+ * apx (gy, gx + 1), apy (gy + 1, gx), gx = nx + 10, gy = ny + 10. */
+ocfd_status ocfd_level_eb_geometry_copy(const ocfd_level* level, int ibox, uint32_t* flag, double* vfrac,
+                                        double* apx, double* apy);
 
 /* ------------------------------------------------------- reacting level (GPU)
  * A level of the multispecies flow with operator-split chemistry, one CUDA graph
@@ -353,7 +421,8 @@ ocfd_status ocfd_chem_state_tpx(ocfd_context* ctx, int64_t n, const double* T, c
  *     (Source/Tagging.H:11-36), buffers them by n_error_buf, clusters the
  *     tagged blocking_factor blocks into boxes no larger than max_grid_size and
  *     keeps every level properly nested in the one below.
- * Regular (non-EB) ideal-gas boxes; one CUDA graph launch per coarse step.     */
+ * Ideal-gas boxes, optionally cut by an embedded body (ocfd_amr_set_eb); one
+ * CUDA graph launch per coarse step.                                          */
 #define OCFD_AMR_MAX_LEVELS 6
 
 typedef struct ocfd_amr ocfd_amr;
@@ -376,6 +445,21 @@ typedef struct ocfd_amr_desc {
 } ocfd_amr_desc;
 
 ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_amr** amr);
+/* Cut every level, present and future, with an embedded body (see
+ * ocfd_level_set_eb): per box the regular, cut-cell or covered scheme of
+ * EBR::compute_dSdt; cut-cell fluxes enter the flux registers weighted by their
+ * area fractions and the reflux of a cut coarse cell is divided by its volume
+ * fraction (EBFluxRegister with areafrac / volfrac, Source/Advance.cpp:344-360,
+ * Source/EBR.cpp:322-330); average-down weights the fine cells by their volume
+ * fractions (EB_average_down, Source/EBR.cpp:549-557); coarse-fine ghost cells
+ * whose parent or a face neighbour of it is cut or covered are interpolated
+ * piecewise-constant.  kind OCFD_EB_NONE removes the body.  Synchronous. */
+ocfd_status ocfd_amr_set_eb(ocfd_amr* amr, const ocfd_eb_desc* eb);
+/* ocfd_level_autotune for every level; the choice per level index is kept for
+ * the levels later regrids build.  ocfd_amr_tuned reads a level's tile shape and
+ * schedule (0 on success, -1 for a bad level). */
+ocfd_status ocfd_amr_autotune(ocfd_amr* amr, unsigned flags, int reps, void* stream);
+int ocfd_amr_tuned(const ocfd_amr* amr, int lev, int32_t* tile, int32_t* sched);
 ocfd_status ocfd_amr_destroy(ocfd_amr* amr);
 int ocfd_amr_nlevels(const ocfd_amr* amr);
 /* The level object of level `lev` (state access through ocfd_level_state /

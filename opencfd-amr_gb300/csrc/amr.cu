@@ -49,6 +49,7 @@
 #include <vector>
 
 #include "level.h"
+#include "eb_level.h"
 
 namespace ocfd {
 
@@ -198,15 +199,25 @@ struct BoxIndex {
 };
 
 // ================================================================ device tags
+// Cut-cell data of one box for the coarse-fine operators: kind OCFD_BOX_* and,
+// for a cut box, its z-invariant flags / volume fractions over grow(bx, 5) in x, y
+struct EbRef {
+    const uint32_t* flag;
+    const double* vf;
+    int gx, x0, y0;
+    int kind;
+};
 struct CfTag {  // fine cells interpolated from one coarse box, by parent cell
     int fbox, cbox;
     int lo[3], hi[3];    // parent cells (coarse, inside the domain)
     int flo[3], fhi[3];  // the children to fill (fine, inside the domain)
     int shift[3];        // fine cell in the fine box's index space = domain cell - shift
+    EbRef ceb;           // the coarse box's cut-cell data
 };
 struct AvgTag {  // coarse cells averaged from one fine box
     int cbox, fbox;
     int lo[3], hi[3];
+    EbRef feb;           // the fine box's cut-cell data (volume-fraction weights)
 };
 struct CopyTag {  // regrid: new box dst <- old box src
     int dst, src;
@@ -215,6 +226,7 @@ struct CopyTag {  // regrid: new box dst <- old box src
 struct RefluxCell {
     long long u, uns;  // element of component 0 in the coarse state buffer, component stride
     int first, count;  // faces
+    const double* vf;  // volume fraction of a cut coarse cell (nullptr: 1)
 };
 struct RefluxFace {
     int d;
@@ -281,6 +293,13 @@ __global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __r
                 ck <= T.fhi[2])
                 inside |= 1u << q8;
         }
+        // piecewise-constant interpolation where the parent or one of its face
+        // neighbours is cut or covered (z neighbours share the parent's column)
+        bool flat = T.ceb.kind == OCFD_BOX_COVERED;
+        if (T.ceb.kind == OCFD_BOX_CUT) {
+            const uint32_t* fl = T.ceb.flag + (pi - T.ceb.x0) + (long long)(pj - T.ceb.y0) * T.ceb.gx;
+            flat = ((fl[0] | fl[-1] | fl[1] | fl[-T.ceb.gx] | fl[T.ceb.gx]) & 3u) != 0u;
+        }
         // a z neighbour outside a z face with unfilled ghosts is the parent itself
         // (the boundary cell and the first mirror cell coincide), signs per BC
         const bool zl = mix.zvirt && pk - 1 < mix.zlo, zh = mix.zvirt && pk + 1 > mix.zhi;
@@ -291,9 +310,9 @@ __global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __r
             const bool flip_h = zh && n >= 1 && n <= 3 && ((mix.zsign[1] >> (n - 1)) & 1);
             const double vzm = zl ? (flip_l ? -v0 : v0) : mixed(mix, q - sz);
             const double vzp = zh ? (flip_h ? -v0 : v0) : mixed(mix, q + sz);
-            const double sx_ = mc_slope(mixed(mix, q - 1), v0, mixed(mix, q + 1));
-            const double sy_ = mc_slope(mixed(mix, q - sy), v0, mixed(mix, q + sy));
-            const double sz_ = mc_slope(vzm, v0, vzp);
+            const double sx_ = flat ? 0.0 : mc_slope(mixed(mix, q - 1), v0, mixed(mix, q + 1));
+            const double sy_ = flat ? 0.0 : mc_slope(mixed(mix, q - sy), v0, mixed(mix, q + sy));
+            const double sz_ = flat ? 0.0 : mc_slope(vzm, v0, vzp);
             double* d = dst + o + n * ff.ns;
 #pragma unroll
             for (int q8 = 0; q8 < 8; ++q8) {
@@ -320,13 +339,36 @@ __global__ void k_avg_down(const AvgTag* __restrict__ tags, const long long* __r
         const long long o = fab_index(cf, i, j, k);
         const long long f0 = fab_index(ff, 2 * i, 2 * j, 2 * k);
         const long long sy = ff.g[0], sz = (long long)ff.g[0] * ff.g[1];
-        for (int n = 0; n < ncomp; ++n) {
-            const double* p = fsrc + f0 + n * ff.ns;
-            double s = 0.0;
-            for (int kk = 0; kk < 2; ++kk)
-                for (int jj = 0; jj < 2; ++jj)
-                    for (int ii = 0; ii < 2; ++ii) s += p[ii + jj * sy + kk * sz];
-            cdst[o + n * cf.ns] = 0.125 * s;
+        if (T.feb.kind == OCFD_BOX_REGULAR) {
+            for (int n = 0; n < ncomp; ++n) {
+                const double* p = fsrc + f0 + n * ff.ns;
+                double s = 0.0;
+                for (int kk = 0; kk < 2; ++kk)
+                    for (int jj = 0; jj < 2; ++jj)
+                        for (int ii = 0; ii < 2; ++ii) s += p[ii + jj * sy + kk * sz];
+                cdst[o + n * cf.ns] = 0.125 * s;
+            }
+        } else {
+            // EB_average_down (Source/EBR.cpp:549-557): fine cells weighted by
+            // their volume fractions; a coarse cell whose children are all
+            // covered takes its first child
+            double w[8], wt = 0.0;
+            for (int q8 = 0; q8 < 8; ++q8) {
+                const int ii = q8 & 1, jj = (q8 >> 1) & 1;
+                w[q8] = T.feb.kind == OCFD_BOX_COVERED
+                            ? 0.0
+                            : T.feb.vf[(2 * i + ii - T.feb.x0) + (long long)(2 * j + jj - T.feb.y0) * T.feb.gx];
+                wt += w[q8];
+            }
+            for (int n = 0; n < ncomp; ++n) {
+                const double* p = fsrc + f0 + n * ff.ns;
+                double s = 0.0;
+                for (int q8 = 0; q8 < 8; ++q8) {
+                    const int ii = q8 & 1, jj = (q8 >> 1) & 1, kk = q8 >> 2;
+                    s += w[q8] * p[ii + jj * sy + kk * sz];
+                }
+                cdst[o + n * cf.ns] = wt > 0.0 ? s / wt : p[0];
+            }
         }
     }
 }
@@ -337,6 +379,8 @@ __global__ void k_reflux(const RefluxCell* __restrict__ cells, int ncell, const 
     const double dxinv[3] = {dxi0, dxi1, dxi2};
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
         const RefluxCell& C = cells[c];
+        const double vf = C.vf ? *C.vf : 1.0;
+        if (!(vf > 0.0)) continue;
         for (int n = 0; n < 5; ++n) {
             double acc = 0.0;
             for (int q = C.first; q < C.first + C.count; ++q) {
@@ -346,7 +390,7 @@ __global__ void k_reflux(const RefluxCell* __restrict__ cells, int ncell, const 
                                           freg[F.f[2] + n * F.fns] + freg[F.f[3] + n * F.fns]);
                 acc += F.sgn * dxinv[F.d] * (fc - ff);
             }
-            U[C.u + n * C.uns] += acc;
+            U[C.u + n * C.uns] += C.vf ? acc / vf : acc;
         }
     }
 }
@@ -542,6 +586,11 @@ struct ocfd_amr {
     bool need_estdt = true;
     long long steps = 0;
     int launches = 0;          // kernels of the captured coarse step
+    bool has_eb = false;       // embedded body cutting every level
+    ocfd_eb_desc eb{};
+    // autotuned tile shape and schedule per level index (-1: not tuned)
+    int tuned_tile[OCFD_AMR_MAX_LEVELS] = {-1, -1, -1, -1, -1, -1};
+    int tuned_sched[OCFD_AMR_MAX_LEVELS] = {0, 0, 0, 0, 0, 0};
     long long kernel_total = 0;  // kernels launched by this hierarchy so far
 };
 
@@ -606,8 +655,23 @@ static ocfd_status make_level(ocfd_amr* H, int l, const std::vector<IBox>& boxes
     }
     d.bc_case = H->desc.bc_case;
     std::memcpy(d.case_params, H->desc.case_params, sizeof(d.case_params));
-    d.tile = -1;
-    return level_alloc(H->ctx, &d, nbuf, out, &H->pool);
+    d.tile = H->tuned_tile[l];
+    ocfd_status s = level_alloc(H->ctx, &d, nbuf, out, &H->pool);
+    if (s == OCFD_OK) (*out)->sched = H->tuned_sched[l];
+    if (s == OCFD_OK && H->has_eb) s = eb_setup(*out, H->eb);
+    return s;
+}
+
+static EbRef eb_ref(const ocfd_level* L, int b) {
+    EbRef r{};
+    r.kind = eb_box_class(L, b);
+    if (r.kind == OCFD_BOX_CUT) {
+        r.vf = eb_box_vfrac(L, b, &r.gx);
+        r.flag = eb_box_flag(L, b);
+        r.x0 = L->boxes[b].lo[0] - EB_GEOM_GROW;
+        r.y0 = L->boxes[b].lo[1] - EB_GEOM_GROW;
+    }
+    return r;
 }
 
 // periodic images (shift vectors) of a region that meet the domain
@@ -653,6 +717,7 @@ static ocfd_status build_cf_tags(const ocfd_amr* H, int f, const std::vector<std
                     CfTag t{};
                     t.fbox = b;
                     t.cbox = cb;
+                    t.ceb = eb_ref(C.L, cb);
                     for (int e = 0; e < 3; ++e) {
                         t.lo[e] = Pc.lo[e];
                         t.hi[e] = Pc.hi[e];
@@ -733,6 +798,7 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
                 AvgTag t{};
                 t.cbox = cb;
                 t.fbox = fb;
+                t.feb = eb_ref(F.L, fb);
                 for (int e = 0; e < 3; ++e) { t.lo[e] = I.lo[e]; t.hi[e] = I.hi[e]; }
                 tags.push_back(t);
                 covered += ib_cells(I);
@@ -840,9 +906,20 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     for (size_t q0 = 0; q0 < faces_k.size();) {
         size_t q1 = q0;
         while (q1 < faces_k.size() && faces_k[q1].cb == faces_k[q0].cb && faces_k[q1].u == faces_k[q0].u) ++q1;
+        const EbRef ce = eb_ref(C.L, faces_k[q0].cb);
+        if (ce.kind == OCFD_BOX_COVERED) {  // covered coarse cells take no reflux
+            q0 = q1;
+            continue;
+        }
         RefluxCell cell{};
         cell.u = faces_k[q0].u;
         cell.uns = C.L->fabs[faces_k[q0].cb].ns;
+        if (ce.kind == OCFD_BOX_CUT) {
+            const Face& f0 = faces_k[q0].f;
+            int w[3] = {f0.cf[0], f0.cf[1], f0.cf[2]};
+            if (f0.side == 0) w[f0.d] -= 1;
+            cell.vf = ce.vf + (w[0] - ce.x0) + (long long)(w[1] - ce.y0) * ce.gx;
+        }
         cell.first = (int)rf_h.size();
         cell.count = (int)(q1 - q0);
         for (size_t qi = q0; qi < q1; ++qi) {
@@ -1035,7 +1112,7 @@ static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cud
         mix_coefs(k, theta, r, a);
         s = fill_level(H, l, L->buf[k], a, tfrac[k], st);
         if (s == OCFD_OK) s = launch_stage(L, k, flags, st);
-        ++launches_counter;
+        launches_counter += stage_launches(L, flags);
     }
     if (s != OCFD_OK) return s;
     if (has_child) {
@@ -1451,6 +1528,40 @@ using namespace ocfd;
 
 extern "C" {
 
+ocfd_status ocfd_amr_autotune(ocfd_amr* H, unsigned flags, int reps, void* stream) {
+    if (!H || reps <= 0) return fail(OCFD_BAD_ARG, "ocfd_amr_autotune");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int l = 0; l < H->nlev; ++l) {
+        ocfd_status s = level_autotune(H->lev[l].L, flags & ~(unsigned)OCFD_PER_BOX, reps, st);
+        if (s != OCFD_OK) return s;
+        H->tuned_tile[l] = H->lev[l].L->tile;
+        H->tuned_sched[l] = H->lev[l].L->sched;
+    }
+    H->graph_ok = false;
+    return OCFD_OK;
+}
+
+int ocfd_amr_tuned(const ocfd_amr* H, int lev, int32_t* tile, int32_t* sched) {
+    if (!H || lev < 0 || lev >= H->nlev) return -1;
+    if (tile) *tile = H->lev[lev].L->tile;
+    if (sched) *sched = H->lev[lev].L->sched;
+    return 0;
+}
+
+ocfd_status ocfd_amr_set_eb(ocfd_amr* H, const ocfd_eb_desc* eb) {
+    if (!H || !eb) return fail(OCFD_BAD_ARG, "ocfd_amr_set_eb: null argument");
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_amr_set_eb");
+    H->has_eb = eb->kind != OCFD_EB_NONE;
+    H->eb = *eb;
+    for (int l = 0; l < H->nlev; ++l) {
+        ocfd_status s = eb_setup(H->lev[l].L, *eb);
+        if (s != OCFD_OK) return s;
+    }
+    ocfd_status s = rebuild_tables(H);
+    H->need_estdt = true;
+    return s;
+}
+
 ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_amr** out) {
     if (!ctx || !desc || !out || desc->nbox0 <= 0 || !desc->boxes0) return fail(OCFD_BAD_ARG, "ocfd_amr_create: bad arguments");
     *out = nullptr;
@@ -1585,7 +1696,8 @@ ocfd_status ocfd_amr_fill_ghosts(ocfd_amr* H, void* stream) {
 
 ocfd_status ocfd_amr_advance(ocfd_amr* H, int nsteps, double cfl, unsigned flags, void* stream) {
     if (!H || nsteps < 0 || !(cfl > 0)) return fail(OCFD_BAD_ARG, "ocfd_amr_advance");
-    if (flags & ~(unsigned)OCFD_FLUX_FP32) return fail(OCFD_BAD_ARG, "ocfd_amr_advance: flags (inviscid ideal gas only)");
+    if (flags & ~(unsigned)(OCFD_FLUX_FP32 | OCFD_PER_BOX))
+        return fail(OCFD_BAD_ARG, "ocfd_amr_advance: flags (inviscid ideal gas only)");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     for (int i = 0; i < nsteps; ++i) {
         if (H->desc.regrid_int > 0 && H->steps > 0 && H->steps % H->desc.regrid_int == 0) {
@@ -1603,10 +1715,18 @@ ocfd_status ocfd_amr_advance(ocfd_amr* H, int nsteps, double cfl, unsigned flags
             H->kernel_total += launches_counter - c0;
             H->need_estdt = false;
         }
-        ocfd_status s = ensure_graph(H, flags);
-        if (s != OCFD_OK) return s;
-        if (cudaGraphLaunch(H->graph, st) != cudaSuccess) return check_launch("AMR graph launch");
-        H->kernel_total += H->launches;
+        if (flags & OCFD_PER_BOX) {  // host-issued launches (the reference's execution model)
+            const int graph_launches = H->launches;
+            ocfd_status s = record_amr_step(H, flags, st);
+            H->kernel_total += H->launches;
+            H->launches = graph_launches;
+            if (s != OCFD_OK) return s;
+        } else {
+            ocfd_status s = ensure_graph(H, flags);
+            if (s != OCFD_OK) return s;
+            if (cudaGraphLaunch(H->graph, st) != cudaSuccess) return check_launch("AMR graph launch");
+            H->kernel_total += H->launches;
+        }
         ++H->steps;
     }
     return OCFD_OK;

@@ -1,0 +1,803 @@
+// Embedded boundary over a level of boxes (ideal gas).
+//
+// The box loop of EBR::compute_dSdt (Source/Advance.cpp:201-342) picks a scheme
+// per box: all cells covered -> dSdt = 0 (:213-214); grow(bx, NUM_GROW) free of
+// cut and covered cells -> the regular WENO-Z chain (:231); otherwise the
+// cut-cell scheme eb_compute_dSdt_box (Source/EB/AdvanceBox.cpp:16-228).  Here
+// the regular boxes stay in the fused tile kernel, and all cut and covered boxes
+// of the level run as one batch per RK stage:
+//   k_ebl_prims       primitives over grow(bx, 2) of every cut box     (c2prim)
+//   k_ebl_faces       every face of every cut box in x, y and z: MUSCL-minmod
+//                     states, Van Leer flux, EB viscous flux; RK3-weighted
+//                     area-fraction fluxes into the flux registers (AMR)
+//   k_ebl_div_stage   per cell: cut-cell divergence with the wall flux, negated
+//                     (zero in covered boxes), fused with the Shu-Osher stage
+//                     update and the CFL bound of the new state
+// Work items of a batch are addressed through prefix sums over the boxes.
+//
+// Geometry.  AMReX EB2 (Source/Geometry.cpp:9-29) is absent.  For a body
+// extruded along z the cut-cell data do not depend on z, so each box keeps 2D
+// arrays over grow(bx, 5) in x and y, read through views with kstride 0:
+//   vfrac  volume fraction: fraction of nsub x nsub sub-cell centres in the fluid
+//   apx    x-face area fraction: fraction of nsub points along the face
+//   apy    y-face area fraction
+//   apz    z faces: the column's volume fraction
+//   flag   EBCellFlag word: bits 0-1 type (0 regular, 1 cut, 3 covered), bits
+//          4 + (i+1) + 3(j+1) + 9(k+1) connectivity to neighbour (i, j, k): a
+//          cut cell is connected to a neighbour that is not covered, through an
+//          open face (area fraction > 0) for face neighbours; regular cells
+//          carry all 27 bits; neighbours outside the stored region count as
+//          covered.  A cell is regular when its volume fraction and the area
+//          fractions of its six faces are 1.
+// The sample points, their arithmetic (IEEE round-to-nearest, no contraction)
+// and the reductions are those of the fixture generator the tests compare with,
+// so the geometry is identical to it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "eb_level.h"
+#include "eb_physics.cuh"
+
+namespace ocfd {
+
+constexpr int EB_GG = EB_GEOM_GROW;
+
+struct GeoTag {
+    int lo[2];         // first cell (x, y) of the stored region, grow(bx, 5)
+    int gx, gy;        // stored cells
+    long long off_vf, off_ax, off_ay, off_fl;
+};
+
+struct EbShape {
+    int kind, nsub;
+    double cx, cy, r;
+    double plo[2], dx[2];
+};
+
+__device__ __forceinline__ double phi_of(const EbShape& s, double x, double y) {
+    const double a = __dsub_rn(x, s.cx), b = __dsub_rn(y, s.cy);
+    return __dsub_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(s.r, s.r));
+}
+// sample coordinate prob_lo + (i + (m + 1/2) / nsub) dx, and the face coordinate prob_lo + i dx
+__device__ __forceinline__ double sample_at(const EbShape& s, int d, int i, int m) {
+    const double sm = __ddiv_rn(__dadd_rn((double)m, 0.5), (double)s.nsub);
+    return __dadd_rn(s.plo[d], __dmul_rn(__dadd_rn((double)i, sm), s.dx[d]));
+}
+__device__ __forceinline__ double face_at(const EbShape& s, int d, int i) {
+    return __dadd_rn(s.plo[d], __dmul_rn((double)i, s.dx[d]));
+}
+
+// volume and area fractions of every stored cell / face
+__global__ void k_geom_frac(const GeoTag* __restrict__ tags, const long long* __restrict__ start, int ntag,
+                            long long total, EbShape sh, double* geo) {
+    const int ns = sh.nsub;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<GeoTag>(start, ntag, idx);
+        const GeoTag& T = tags[t];
+        const long long loc = idx - start[t];
+        const int W = T.gx + 1;
+        const int li = (int)(loc % W), lj = (int)(loc / W);
+        const int i = T.lo[0] + li, j = T.lo[1] + lj;
+        if (li < T.gx && lj < T.gy) {
+            int cnt = 0;
+            for (int b = 0; b < ns; ++b) {
+                const double y = sample_at(sh, 1, j, b);
+                for (int a = 0; a < ns; ++a) cnt += phi_of(sh, sample_at(sh, 0, i, a), y) > 0.0;
+            }
+            geo[T.off_vf + li + (long long)lj * T.gx] = __ddiv_rn((double)cnt, (double)(ns * ns));
+        }
+        if (lj < T.gy) {
+            const double xf = face_at(sh, 0, i);
+            int cnt = 0;
+            for (int b = 0; b < ns; ++b) cnt += phi_of(sh, xf, sample_at(sh, 1, j, b)) > 0.0;
+            geo[T.off_ax + li + (long long)lj * (T.gx + 1)] = __ddiv_rn((double)cnt, (double)ns);
+        }
+        if (li < T.gx) {
+            const double yf = face_at(sh, 1, j);
+            int cnt = 0;
+            for (int a = 0; a < ns; ++a) cnt += phi_of(sh, sample_at(sh, 0, i, a), yf) > 0.0;
+            geo[T.off_ay + li + (long long)lj * T.gx] = __ddiv_rn((double)cnt, (double)ns);
+        }
+    }
+}
+
+__host__ __device__ constexpr int conn_bit(int i, int j, int k) { return 4 + (i + 1) + 3 * (j + 1) + 9 * (k + 1); }
+
+// flag words of every stored cell; per box the count of cells that are not
+// regular inside grow(bx, 4) and of covered cells inside bx (class test)
+__global__ void k_geom_flag(const GeoTag* __restrict__ tags, const long long* __restrict__ start, int ntag,
+                            long long total, const double* __restrict__ geo, uint32_t* flag,
+                            unsigned long long* counts) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<GeoTag>(start, ntag, idx);
+        const GeoTag& T = tags[t];
+        const long long loc = idx - start[t];
+        const int li = (int)(loc % T.gx), lj = (int)(loc / T.gx);
+        const double* vf = geo + T.off_vf;
+        const double* ax = geo + T.off_ax;
+        const double* ay = geo + T.off_ay;
+        auto VF = [&](int a, int b) { return vf[a + (long long)b * T.gx]; };
+        auto AX = [&](int a, int b) { return ax[a + (long long)b * (T.gx + 1)]; };
+        auto AY = [&](int a, int b) { return ay[a + (long long)b * T.gx]; };
+        const double v = VF(li, lj);
+        const bool covered = v <= 0.0;
+        const bool full = v >= 1.0;
+        const bool open = AX(li, lj) >= 1.0 && AX(li + 1, lj) >= 1.0 && AY(li, lj) >= 1.0 && AY(li, lj + 1) >= 1.0;
+        uint32_t w;
+        if (full && open) {
+            w = 0u;
+            for (int b = 0; b < 27; ++b) w |= 1u << (4 + b);
+        } else if (covered) {
+            w = 3u;
+        } else {
+            w = 1u;
+            for (int dk = -1; dk <= 1; ++dk)
+                for (int dj = -1; dj <= 1; ++dj)
+                    for (int di = -1; di <= 1; ++di) {
+                        const int ni = li + di, nj = lj + dj;
+                        const bool inside = ni >= 0 && ni < T.gx && nj >= 0 && nj < T.gy;
+                        bool ok = inside && !(VF(ni, nj) <= 0.0);
+                        const int nface = (di != 0) + (dj != 0) + (dk != 0);
+                        if (ok && nface == 1) {
+                            double a;
+                            if (di) a = di > 0 ? AX(li + 1, lj) : AX(li, lj);
+                            else if (dj) a = dj > 0 ? AY(li, lj + 1) : AY(li, lj);
+                            else a = v;
+                            ok = a > 0.0;
+                        }
+                        if (ok) w |= 1u << conn_bit(di, dj, dk);
+                    }
+        }
+        flag[T.off_fl + loc] = w;
+        // class counts: grow(bx, 4) is the stored region less its outer ring
+        if (li >= 1 && li < T.gx - 1 && lj >= 1 && lj < T.gy - 1 && (w & 3u) != 0u)
+            atomicAdd(&counts[2 * t], 1ull);
+        if (li >= EB_GG && li < T.gx - EB_GG && lj >= EB_GG && lj < T.gy - EB_GG && covered)
+            atomicAdd(&counts[2 * t + 1], 1ull);
+    }
+}
+
+// ------------------------------------------------------------------ stages
+struct EbStageBox {
+    View<const double> S, U0;
+    View<double> Uout;
+    View<const uint32_t> flag;
+    View<const double> vfrac, ap[3];
+    View<double> q, flux[3];
+    int lo[3], hi[3];
+    double rk_a, rk_b;
+    int covered;
+    int has_flux;  // FLUX_ACC_ALL / FLUX_ACC_PLANES
+    double flux_w;
+    View<double> creg[3];
+    View<double> fplane[3][2];
+};
+
+struct EbStageArgs {
+    const EbStageBox* boxes;
+    int nbox;
+    const long long* pstart;  // grow(bx, 2) cells of each box (0 for covered boxes)
+    long long ptotal;
+    const long long* fstart;  // faces, tag 3 b + d (0 for covered boxes)
+    long long ftotal;
+    const long long* cstart;  // valid cells of each box
+    long long ctotal;
+    double dxinv[3], dx[3];
+    const double* dt_ptr;
+    unsigned long long* cfl_min;
+    int visc, redist;
+};
+
+__global__ void k_ebl_prims(EbStageArgs A, DevParm P) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ptotal;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = find_tag<EbStageBox>(A.pstart, A.nbox, idx);
+        const EbStageBox& B = A.boxes[b];
+        const long long loc = idx - A.pstart[b];
+        const int gx = B.hi[0] - B.lo[0] + 5, gy = B.hi[1] - B.lo[1] + 5;
+        const int i = B.lo[0] - 2 + (int)(loc % gx), j = B.lo[1] - 2 + (int)((loc / gx) % gy),
+                  k = B.lo[2] - 2 + (int)(loc / ((long long)gx * gy));
+        double q[7];
+        c2prim_ideal(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3), B.S(i, j, k, 4), q);
+#pragma unroll
+        for (int m = 0; m < 7; ++m) B.q(i, j, k, m) = q[m];
+    }
+}
+
+__global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ftotal;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int t = find_tag<EbStageBox>(A.fstart, 3 * A.nbox, idx);
+        const int b = t / 3, D = t % 3;
+        const EbStageBox& B = A.boxes[b];
+        const long long loc = idx - A.fstart[t];
+        const int fx = B.hi[0] - B.lo[0] + 1 + (D == 0), fy = B.hi[1] - B.lo[1] + 1 + (D == 1);
+        const int i = B.lo[0] + (int)(loc % fx), j = B.lo[1] + (int)((loc / fx) % fy),
+                  k = B.lo[2] + (int)(loc / ((long long)fx * fy));
+        const int di = D == 0, dj = D == 1, dk = D == 2;
+        const View<const double> q{B.q.p, B.q.js, B.q.ks, B.q.ns, B.q.b0, B.q.b1, B.q.b2};
+        const uint32_t f = B.flag(i, j, k);
+        double ql[7], qr[7];
+#pragma unroll
+        for (int m = 0; m < 7; ++m)
+            eb_recon(f, D, q(i - 2 * di, j - 2 * dj, k - 2 * dk, m), q(i - di, j - dj, k - dk, m), q(i, j, k, m),
+                     q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
+        double flx[5];
+        vanleer(P, P.gamma, ql, qr, D, flx);
+        if (A.visc) eb_visc_face(P, q, B.flag, D, i, j, k, A.dxinv, flx, 1, false, 0, 0, 0);
+#pragma unroll
+        for (int m = 0; m < 5; ++m) B.flux[D](i, j, k, m) = flx[m];
+        if (B.has_flux) {
+            const double w = B.flux_w * *A.dt_ptr * B.ap[D](i, j, k);
+            if (B.has_flux & FLUX_ACC_ALL) {
+#pragma unroll
+                for (int m = 0; m < 5; ++m) B.creg[D](i, j, k, m) += w * flx[m];
+            }
+            const int g = D == 0 ? i : (D == 1 ? j : k);
+            if ((B.has_flux & FLUX_ACC_PLANES) && (g == B.lo[D] || g == B.hi[D] + 1)) {
+                const View<double>& pl = B.fplane[D][g == B.lo[D] ? 0 : 1];
+#pragma unroll
+                for (int m = 0; m < 5; ++m) pl(i, j, k, m) += w * flx[m];
+            }
+        }
+    }
+}
+
+// cut-cell divergence of one cell (Source/EB/EBkernels.H:216-338, negated and
+// optionally rescaled as flux_redist, :341-377) + the Shu-Osher stage
+__global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
+    const double dt = *A.dt_ptr;
+    double local_dt = __longlong_as_double(0x7FF0000000000000LL);
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ctotal;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = find_tag<EbStageBox>(A.cstart, A.nbox, idx);
+        const EbStageBox& B = A.boxes[b];
+        const long long loc = idx - A.cstart[b];
+        const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1;
+        const int i = B.lo[0] + (int)(loc % nx), j = B.lo[1] + (int)((loc / nx) % ny),
+                  k = B.lo[2] + (int)(loc / ((long long)nx * ny));
+        double L[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (!B.covered) {
+            const uint32_t f = B.flag(i, j, k);
+            const double vf = B.vfrac(i, j, k);
+            double out[5];
+            if (eb_covered(f)) {
+#pragma unroll
+                for (int m = 0; m < 5; ++m) out[m] = 0.0;
+            } else if (eb_regular(f)) {
+#pragma unroll
+                for (int m = 0; m < 5; ++m)
+                    out[m] = A.dxinv[0] * (B.flux[0](i + 1, j, k, m) - B.flux[0](i, j, k, m)) +
+                             A.dxinv[1] * (B.flux[1](i, j + 1, k, m) - B.flux[1](i, j, k, m)) +
+                             A.dxinv[2] * (B.flux[2](i, j, k + 1, m) - B.flux[2](i, j, k, m));
+            } else {
+                const double tmp = A.dxinv[0] / vf;
+                const double axm = B.ap[0](i, j, k), axp = B.ap[0](i + 1, j, k);
+                const double aym = B.ap[1](i, j, k), ayp = B.ap[1](i, j + 1, k);
+                const double azm = B.ap[2](i, j, k), azp = B.ap[2](i, j, k + 1);
+#pragma unroll
+                for (int m = 0; m < 5; ++m)
+                    out[m] = tmp * (axp * B.flux[0](i + 1, j, k, m) - axm * B.flux[0](i, j, k, m) +
+                                    ayp * B.flux[1](i, j + 1, k, m) - aym * B.flux[1](i, j, k, m) +
+                                    azp * B.flux[2](i, j, k + 1, m) - azm * B.flux[2](i, j, k, m));
+                double fw[5];
+                const double pr = B.q(i, j, k, QPRES);
+                if (!A.visc) {
+                    // slip-wall pressure flux, EBkernels.H:305-311
+                    fw[0] = 0.0;
+                    fw[1] = (axm - axp) * pr;
+                    fw[2] = (aym - ayp) * pr;
+                    fw[3] = (azm - azp) * pr;
+                    fw[4] = 0.0;
+                } else {
+                    // eb_wallflux, EBkernels.H:173-214
+                    const double d = B.q(i, j, k, QRHO), u = B.q(i, j, k, QU), v = B.q(i, j, k, QV),
+                                 w = B.q(i, j, k, QW), cs = B.q(i, j, k, QC);
+                    const double apnorm = sqrt((axm - axp) * (axm - axp) + (aym - ayp) * (aym - ayp) +
+                                               (azm - azp) * (azm - azp));
+                    const double un = u * (axm - axp) + v * (aym - ayp) + w * (azm - azp);
+                    const double lambda0 = fabs(un) + cs * apnorm;
+                    const double gamma = P.gamma;
+                    const double E0 = pr / (gamma - 1) + 0.50 * d * (u * u + v * v + w * w);
+                    double fpw[5], fmw[5];
+                    fpw[0] = 0.5 * (d * un + lambda0 * d);
+                    fpw[1] = 0.5 * (d * u * un + (axm - axp) * pr + lambda0 * d * u);
+                    fpw[2] = 0.5 * (d * v * un + (aym - ayp) * pr + lambda0 * d * v);
+                    fpw[3] = 0.5 * (d * w * un + (azm - azp) * pr + lambda0 * d * w);
+                    fpw[4] = 0.5 * ((E0 + pr) * un + lambda0 * E0);
+                    fmw[0] = 0.5 * (d * (-un) - lambda0 * d);
+                    fmw[1] = fpw[1];
+                    fmw[2] = fpw[2];
+                    fmw[3] = fpw[3];
+                    fmw[4] = 0.5 * (-(E0 + pr) * un - lambda0 * E0);
+#pragma unroll
+                    for (int m = 0; m < 5; ++m) fw[m] = fpw[m] + fmw[m];
+                }
+#pragma unroll
+                for (int m = 0; m < 5; ++m) out[m] += fw[m] * tmp;
+            }
+            const bool rescale = A.redist && vf < 0.5 && vf > 0.0;
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                const double divc = out[m] * -1.0;
+                L[m] = rescale ? vf * divc : divc;
+            }
+        }
+        double un[5];
+#pragma unroll
+        for (int n = 0; n < 5; ++n) {
+            const double us = B.S(i, j, k, n);
+            const double u0 = B.U0(i, j, k, n);
+            un[n] = B.rk_a * u0 + B.rk_b * (us + dt * L[n]);
+            B.Uout(i, j, k, n) = un[n];
+        }
+        if (A.cfl_min) {
+            const double v = cfl_bound(P, un, A.dx);
+            local_dt = v < local_dt ? v : local_dt;
+        }
+    }
+    if (A.cfl_min) block_min_atomic(local_dt, A.cfl_min);
+}
+
+}  // namespace ocfd
+
+// ------------------------------------------------------------------ host side
+struct ocfd::EbLevel {
+    ocfd_eb_desc desc{};
+    std::vector<int> cls;       // per box
+    std::vector<int> geo_of;    // per box: geometry tag, or -1
+    std::vector<GeoTag> geo;    // host copies of the geometry tags
+    double* d_geo = nullptr;
+    uint32_t* d_flag = nullptr;
+    // cut and covered boxes (level box indices) and their scratch
+    std::vector<int> ebox;
+    std::vector<long long> q_off, f_off[3];
+    double* d_scratch = nullptr;
+    EbStageBox* d_stage[3] = {nullptr, nullptr, nullptr};
+    long long *d_pstart = nullptr, *d_fstart = nullptr, *d_cstart = nullptr;
+    long long ptotal = 0, ftotal = 0, ctotal = 0;
+    bool cfl3 = true;
+    // per-box launches: work of each box and its local prefix tables
+    std::vector<long long> pcount, fcount, ccount;
+    long long* d_floc = nullptr;  // (0, F0, F0 + F1) per box
+    long long* d_zero = nullptr;
+};
+
+namespace ocfd {
+
+static void eb_free_tables(ocfd_level* L) {
+    EbLevel* E = L->eb;
+    for (int s = 0; s < 3; ++s) {
+        dev_free(E->d_stage[s], L->pool);
+        E->d_stage[s] = nullptr;
+    }
+    dev_free(E->d_pstart, L->pool);
+    dev_free(E->d_fstart, L->pool);
+    dev_free(E->d_cstart, L->pool);
+    dev_free(E->d_floc, L->pool);
+    dev_free(E->d_zero, L->pool);
+    E->d_pstart = E->d_fstart = E->d_cstart = E->d_floc = E->d_zero = nullptr;
+}
+
+void eb_free(ocfd_level* L) {
+    if (!L || !L->eb) return;
+    EbLevel* E = L->eb;
+    eb_free_tables(L);
+    dev_free(E->d_geo, L->pool);
+    dev_free(E->d_flag, L->pool);
+    dev_free(E->d_scratch, L->pool);
+    delete E;
+    L->eb = nullptr;
+}
+
+bool eb_box_regular(const ocfd_level* L, int b) { return !L->eb || L->eb->cls[b] == OCFD_BOX_REGULAR; }
+int eb_box_class(const ocfd_level* L, int b) { return L->eb ? L->eb->cls[b] : OCFD_BOX_REGULAR; }
+
+const uint32_t* eb_box_flag(const ocfd_level* L, int b) {
+    if (!L->eb || L->eb->geo_of[b] < 0 || L->eb->cls[b] != OCFD_BOX_CUT) return nullptr;
+    return L->eb->d_flag + L->eb->geo[L->eb->geo_of[b]].off_fl;
+}
+
+const double* eb_box_vfrac(const ocfd_level* L, int b, int* gx) {
+    if (!L->eb || L->eb->geo_of[b] < 0 || L->eb->cls[b] != OCFD_BOX_CUT) return nullptr;
+    const GeoTag& g = L->eb->geo[L->eb->geo_of[b]];
+    if (gx) *gx = g.gx;
+    return L->eb->d_geo + g.off_vf;
+}
+
+// squared distance bounds from (cx, cy) to the rectangle [x0, x1] x [y0, y1]
+static void rect_dist2(double cx, double cy, double x0, double x1, double y0, double y1, double& dmin2,
+                       double& dmax2) {
+    const double ex = cx < x0 ? x0 - cx : (cx > x1 ? cx - x1 : 0.0);
+    const double ey = cy < y0 ? y0 - cy : (cy > y1 ? cy - y1 : 0.0);
+    dmin2 = ex * ex + ey * ey;
+    const double fx = std::max(std::fabs(cx - x0), std::fabs(cx - x1));
+    const double fy = std::max(std::fabs(cy - y0), std::fabs(cy - y1));
+    dmax2 = fx * fx + fy * fy;
+}
+
+ocfd_status eb_setup(ocfd_level* L, const ocfd_eb_desc& eb) {
+    eb_free(L);
+    if (eb.kind == OCFD_EB_NONE) return OCFD_OK;
+    if (eb.kind != OCFD_EB_CYLINDER_Z) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: unknown body kind");
+    if (!(eb.radius > 0) || eb.nsub < 0 || eb.nsub > 256) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: radius / nsub");
+    EbLevel* E = new EbLevel();
+    L->eb = E;
+    E->desc = eb;
+    if (E->desc.nsub == 0) E->desc.nsub = 16;
+    const int nb = (int)L->boxes.size();
+    E->cls.assign(nb, OCFD_BOX_REGULAR);
+    E->geo_of.assign(nb, -1);
+    const double* plo = L->desc.prob_lo;
+    const double* dx = L->desc.dx;
+    const double r = eb.radius, r2 = r * r;
+    // analytic screening: every sample point of grow(bx, 5) outside the circle ->
+    // regular; every sample of bx inside -> covered; otherwise build the geometry
+    std::map<std::tuple<int, int, int, int>, int> geo_index;
+    long long nvf = 0, nfl = 0;
+    for (int b = 0; b < nb; ++b) {
+        const ocfd_box& B = L->boxes[b];
+        double dmin2, dmax2;
+        rect_dist2(eb.center[0], eb.center[1], plo[0] + (B.lo[0] - EB_GG) * dx[0], plo[0] + (B.hi[0] + 1 + EB_GG) * dx[0],
+                   plo[1] + (B.lo[1] - EB_GG) * dx[1], plo[1] + (B.hi[1] + 1 + EB_GG) * dx[1], dmin2, dmax2);
+        if (dmin2 > r2 * (1.0 + 1e-9) + 1e-300) continue;  // regular
+        rect_dist2(eb.center[0], eb.center[1], plo[0] + B.lo[0] * dx[0], plo[0] + (B.hi[0] + 1) * dx[0],
+                   plo[1] + B.lo[1] * dx[1], plo[1] + (B.hi[1] + 1) * dx[1], dmin2, dmax2);
+        if (dmax2 < r2 * (1.0 - 1e-9)) {
+            E->cls[b] = OCFD_BOX_COVERED;
+            continue;
+        }
+        auto key = std::make_tuple(B.lo[0], B.lo[1], B.hi[0], B.hi[1]);
+        auto it = geo_index.find(key);
+        if (it != geo_index.end()) {
+            E->geo_of[b] = it->second;
+            continue;
+        }
+        GeoTag g{};
+        g.lo[0] = B.lo[0] - EB_GG;
+        g.lo[1] = B.lo[1] - EB_GG;
+        g.gx = B.hi[0] - B.lo[0] + 1 + 2 * EB_GG;
+        g.gy = B.hi[1] - B.lo[1] + 1 + 2 * EB_GG;
+        g.off_vf = nvf;
+        g.off_ax = g.off_vf + (long long)g.gx * g.gy;
+        g.off_ay = g.off_ax + (long long)(g.gx + 1) * g.gy;
+        nvf = g.off_ay + (long long)g.gx * (g.gy + 1);
+        g.off_fl = nfl;
+        nfl += (long long)g.gx * g.gy;
+        const int id = (int)E->geo.size();
+        E->geo.push_back(g);
+        geo_index[key] = id;
+        E->geo_of[b] = id;
+    }
+    const int ng = (int)E->geo.size();
+    ocfd_status s = OCFD_OK;
+    std::vector<unsigned long long> counts(2 * (size_t)std::max(ng, 1), 0ull);
+    if (ng > 0) {
+        E->d_geo = static_cast<double*>(dev_alloc(sizeof(double) * nvf, L->pool));
+        E->d_flag = static_cast<uint32_t*>(dev_alloc(sizeof(uint32_t) * nfl, L->pool));
+        if (!E->d_geo || !E->d_flag) return fail(OCFD_OUT_OF_MEMORY, "ocfd_level_set_eb: geometry");
+        std::vector<long long> fstart(ng), cstart(ng);
+        long long ftot = 0, ctot = 0;
+        for (int g = 0; g < ng; ++g) {
+            fstart[g] = ftot;
+            ftot += (long long)(E->geo[g].gx + 1) * (E->geo[g].gy + 1);
+            cstart[g] = ctot;
+            ctot += (long long)E->geo[g].gx * E->geo[g].gy;
+        }
+        GeoTag* d_tags = nullptr;
+        long long *d_fs = nullptr, *d_cs = nullptr;
+        unsigned long long* d_counts = nullptr;
+        s = upload(&d_tags, E->geo);
+        if (s == OCFD_OK) s = upload(&d_fs, fstart);
+        if (s == OCFD_OK) s = upload(&d_cs, cstart);
+        if (s == OCFD_OK) s = upload(&d_counts, counts);
+        if (s == OCFD_OK) {
+            EbShape sh{};
+            sh.kind = eb.kind;
+            sh.nsub = E->desc.nsub;
+            sh.cx = eb.center[0];
+            sh.cy = eb.center[1];
+            sh.r = eb.radius;
+            for (int d = 0; d < 2; ++d) {
+                sh.plo[d] = plo[d];
+                sh.dx[d] = dx[d];
+            }
+            const int sms = L->ctx->num_sms;
+            k_geom_frac<<<grid_for(ftot, 128, sms), 128>>>(d_tags, d_fs, ng, ftot, sh, E->d_geo);
+            k_geom_flag<<<grid_for(ctot, 256, sms), 256>>>(d_tags, d_cs, ng, ctot, E->d_geo, E->d_flag, d_counts);
+            s = check_launch("ocfd_level_set_eb geometry");
+        }
+        if (s == OCFD_OK && cudaMemcpy(counts.data(), d_counts, sizeof(unsigned long long) * 2 * ng,
+                                       cudaMemcpyDeviceToHost) != cudaSuccess)
+            s = fail(OCFD_LAUNCH_FAIL, "ocfd_level_set_eb: class counts");
+        cudaFree(d_tags);
+        cudaFree(d_fs);
+        cudaFree(d_cs);
+        cudaFree(d_counts);
+        if (s != OCFD_OK) return s;
+    }
+    for (int b = 0; b < nb; ++b) {
+        const int g = E->geo_of[b];
+        if (g < 0) continue;
+        const ocfd_box& B = L->boxes[b];
+        const long long ncell_xy = (long long)(B.hi[0] - B.lo[0] + 1) * (B.hi[1] - B.lo[1] + 1);
+        if (counts[2 * g + 1] == (unsigned long long)ncell_xy) E->cls[b] = OCFD_BOX_COVERED;
+        else if (counts[2 * g] == 0) E->cls[b] = OCFD_BOX_REGULAR;
+        else E->cls[b] = OCFD_BOX_CUT;
+    }
+    // scratch of the cut boxes: primitives over grow(bx, 2), face fluxes
+    long long off = 0;
+    bool any_cut = false;
+    for (int b = 0; b < nb; ++b) {
+        if (E->cls[b] == OCFD_BOX_REGULAR) continue;
+        E->ebox.push_back(b);
+        const ocfd_box& B = L->boxes[b];
+        const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
+        if (E->cls[b] == OCFD_BOX_CUT) {
+            any_cut = true;
+            E->q_off.push_back(off);
+            off += 7LL * (n[0] + 4) * (n[1] + 4) * (n[2] + 4);
+            for (int d = 0; d < 3; ++d) {
+                E->f_off[d].push_back(off);
+                off += 5LL * (n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
+            }
+        } else {
+            E->q_off.push_back(-1);
+            for (int d = 0; d < 3; ++d) E->f_off[d].push_back(-1);
+        }
+    }
+    if (off > 0) {
+        E->d_scratch = static_cast<double*>(dev_alloc(sizeof(double) * off, L->pool));
+        if (!E->d_scratch) return fail(OCFD_OUT_OF_MEMORY, "ocfd_level_set_eb: scratch");
+    }
+    // the cut-cell stencils read z ghost cells from the state: fill them
+    if (any_cut) L->zvirt = false;
+    return OCFD_OK;
+}
+
+static ocfd_array4 fab_view(const ocfd_level* L, int b, int i) {
+    const FabGeom& f = L->fabs[b];
+    ocfd_array4 a{};
+    a.p = L->buf[i] + f.off;
+    a.jstride = f.g[0];
+    a.kstride = (long long)f.g[0] * f.g[1];
+    a.nstride = f.ns;
+    for (int d = 0; d < 3; ++d) {
+        a.begin[d] = f.lo[d] - NGR;
+        a.end[d] = f.hi[d] + NGR + 1;
+    }
+    a.ncomp = L->ncomp;
+    return a;
+}
+
+ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
+    EbLevel* E = L->eb;
+    if (!E) return OCFD_OK;
+    eb_free_tables(L);
+    const int ne = (int)E->ebox.size();
+    if (ne == 0) return OCFD_OK;
+    E->cfl3 = roles.cfl;
+    const int S_of[3] = {0, 1, 2}, O_of[3] = {1, 2, roles.out3};
+    const double ra[3] = {0.0, 0.75, 1.0 / 3.0}, rb[3] = {1.0, 0.25, 2.0 / 3.0};
+    const double wflux[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
+    std::vector<EbStageBox> st[3];
+    std::vector<long long> ps(ne), fs(3 * ne), cs(ne), floc(3 * ne);
+    long long pt = 0, ft = 0, ct = 0;
+    E->pcount.assign(ne, 0);
+    E->fcount.assign(ne, 0);
+    E->ccount.assign(ne, 0);
+    for (int e = 0; e < ne; ++e) {
+        const int b = E->ebox[e];
+        const ocfd_box& B = L->boxes[b];
+        const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
+        const bool cut = E->cls[b] == OCFD_BOX_CUT;
+        ps[e] = pt;
+        if (cut) pt += (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
+        E->pcount[e] = pt - ps[e];
+        for (int d = 0; d < 3; ++d) {
+            fs[3 * e + d] = ft;
+            floc[3 * e + d] = ft - fs[3 * e];
+            if (cut) ft += (long long)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
+        }
+        E->fcount[e] = ft - fs[3 * e];
+        cs[e] = ct;
+        ct += (long long)n[0] * n[1] * n[2];
+        E->ccount[e] = ct - cs[e];
+        EbStageBox base{};
+        for (int d = 0; d < 3; ++d) {
+            base.lo[d] = B.lo[d];
+            base.hi[d] = B.hi[d];
+        }
+        base.covered = cut ? 0 : 1;
+        if (cut) {
+            const GeoTag& g = E->geo[E->geo_of[b]];
+            const int b0 = g.lo[0], b1 = g.lo[1];
+            base.flag = View<const uint32_t>{E->d_flag + g.off_fl, g.gx, 0, 0, b0, b1, 0};
+            base.vfrac = View<const double>{E->d_geo + g.off_vf, g.gx, 0, 0, b0, b1, 0};
+            base.ap[0] = View<const double>{E->d_geo + g.off_ax, g.gx + 1, 0, 0, b0, b1, 0};
+            base.ap[1] = View<const double>{E->d_geo + g.off_ay, g.gx, 0, 0, b0, b1, 0};
+            base.ap[2] = base.vfrac;
+            const long long gq = (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
+            base.q = View<double>{E->d_scratch + E->q_off[e], n[0] + 4, (long long)(n[0] + 4) * (n[1] + 4), gq,
+                                  B.lo[0] - 2, B.lo[1] - 2, B.lo[2] - 2};
+            for (int d = 0; d < 3; ++d) {
+                const int sx = n[0] + (d == 0), sy = n[1] + (d == 1), sz = n[2] + (d == 2);
+                base.flux[d] = View<double>{E->d_scratch + E->f_off[d][e], sx, (long long)sx * sy,
+                                            (long long)sx * sy * sz, B.lo[0], B.lo[1], B.lo[2]};
+            }
+        }
+        if (!roles.flux_bits.empty() && roles.flux_bits[b] && cut) {
+            base.has_flux = roles.flux_bits[b] & (FLUX_ACC_ALL | FLUX_ACC_PLANES);
+            if (base.has_flux & FLUX_ACC_ALL)
+                for (int d = 0; d < 3; ++d) base.creg[d] = roles.creg[3 * b + d];
+            if (base.has_flux & FLUX_ACC_PLANES)
+                for (int d = 0; d < 3; ++d)
+                    for (int sd = 0; sd < 2; ++sd) base.fplane[d][sd] = roles.fplane[6 * b + 2 * d + sd];
+        }
+        ocfd_array4 a[4];
+        for (int i = 0; i < L->nbuf; ++i) a[i] = fab_view(L, b, i);
+        for (int k = 0; k < 3; ++k) {
+            EbStageBox x = base;
+            x.S = view_of<const double>(&a[S_of[k]]);
+            x.U0 = view_of<const double>(&a[0]);
+            x.Uout = view_of<double>(&a[O_of[k]]);
+            x.rk_a = ra[k];
+            x.rk_b = rb[k];
+            x.flux_w = wflux[k];
+            st[k].push_back(x);
+        }
+    }
+    E->ptotal = pt;
+    E->ftotal = ft;
+    E->ctotal = ct;
+    ocfd_status s = OCFD_OK;
+    for (int k = 0; k < 3 && s == OCFD_OK; ++k) s = upload(&E->d_stage[k], st[k], L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_pstart, ps, L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_fstart, fs, L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_cstart, cs, L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_floc, floc, L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_zero, std::vector<long long>(1, 0), L->pool);
+    return s;
+}
+
+ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st) {
+    EbLevel* E = L->eb;
+    if (!E || E->ebox.empty()) return OCFD_OK;
+    EbStageArgs A{};
+    A.boxes = E->d_stage[s];
+    A.nbox = (int)E->ebox.size();
+    A.pstart = E->d_pstart;
+    A.ptotal = E->ptotal;
+    A.fstart = E->d_fstart;
+    A.ftotal = E->ftotal;
+    A.cstart = E->d_cstart;
+    A.ctotal = E->ctotal;
+    for (int d = 0; d < 3; ++d) {
+        A.dxinv[d] = 1.0 / L->desc.dx[d];
+        A.dx[d] = L->desc.dx[d];
+    }
+    A.dt_ptr = &L->d_step->dt;
+    A.cfl_min = (s == 2 && E->cfl3) ? &L->d_step->cfl_min : nullptr;
+    A.visc = (flags & OCFD_VISC) ? 1 : 0;
+    A.redist = E->desc.redistribute ? 1 : 0;
+    const int sms = L->ctx->num_sms;
+    if (flags & OCFD_PER_BOX) {
+        // one box at a time (the reference's per-box kernel chain)
+        const EbStageBox* base = E->d_stage[s];
+        for (int e = 0; e < (int)E->ebox.size(); ++e) {
+            EbStageArgs B = A;
+            B.boxes = base + e;
+            B.nbox = 1;
+            B.pstart = E->d_zero;
+            B.ptotal = E->pcount[e];
+            B.fstart = E->d_floc + 3 * e;
+            B.ftotal = E->fcount[e];
+            B.cstart = E->d_zero;
+            B.ctotal = E->ccount[e];
+            if (B.ptotal > 0) k_ebl_prims<<<grid_for(B.ptotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+            if (B.ftotal > 0) k_ebl_faces<<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
+            k_ebl_div_stage<<<grid_for(B.ctotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+        }
+        return check_launch("level cut-cell stage (per box)");
+    }
+    if (A.ptotal > 0) k_ebl_prims<<<grid_for(A.ptotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+    if (A.ftotal > 0) k_ebl_faces<<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
+    k_ebl_div_stage<<<grid_for(A.ctotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+    return check_launch("level cut-cell stage");
+}
+
+int eb_launches_per_stage(const ocfd_level* L, unsigned flags) {
+    const EbLevel* E = L->eb;
+    if (!E || E->ebox.empty()) return 0;
+    if (flags & OCFD_PER_BOX) {
+        int n = 0;
+        for (int b : E->ebox) n += E->cls[b] == OCFD_BOX_CUT ? 3 : 1;
+        return n;
+    }
+    return (E->ptotal > 0) + (E->ftotal > 0) + 1;
+}
+
+}  // namespace ocfd
+
+using namespace ocfd;
+
+extern "C" {
+
+ocfd_status ocfd_level_set_eb(ocfd_level* L, const ocfd_eb_desc* eb) {
+    if (!L || !eb) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: null argument");
+    if (L->ncomp != 5) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: the cut-cell level path is the ideal-gas one");
+    ocfd_status s = eb_setup(L, *eb);
+    if (s == OCFD_OK) s = build_stage_tables(L, StageRoles{});
+    if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = fail(OCFD_LAUNCH_FAIL, "ocfd_level_set_eb");
+    if (L->graph) {
+        cudaGraphExecDestroy(L->graph);
+        L->graph = nullptr;
+    }
+    return s;
+}
+
+ocfd_status ocfd_level_box_classes(const ocfd_level* L, int32_t* classes) {
+    if (!L || !classes) return fail(OCFD_BAD_ARG, "ocfd_level_box_classes");
+    for (int b = 0; b < (int)L->boxes.size(); ++b) classes[b] = eb_box_class(L, b);
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_level_eb_geometry(const ocfd_level* L, int ibox, ocfd_flag4* flag, ocfd_array4* vfrac,
+                                   ocfd_array4* ap) {
+    if (!L || ibox < 0 || ibox >= (int)L->boxes.size() || !flag || !vfrac || !ap)
+        return fail(OCFD_BAD_ARG, "ocfd_level_eb_geometry");
+    const EbLevel* E = L->eb;
+    if (!E || E->geo_of[ibox] < 0) return fail(OCFD_BAD_ARG, "ocfd_level_eb_geometry: box has no cut-cell data");
+    const GeoTag& g = E->geo[E->geo_of[ibox]];
+    const ocfd_box& B = L->boxes[ibox];
+    auto fill = [&](int64_t js, int nxe, int nye, int32_t* begin, int32_t* end) {
+        begin[0] = g.lo[0];
+        begin[1] = g.lo[1];
+        begin[2] = B.lo[2] - EB_GG;
+        end[0] = g.lo[0] + nxe;
+        end[1] = g.lo[1] + nye;
+        end[2] = B.hi[2] + EB_GG + 1;
+        (void)js;
+    };
+    flag->p = E->d_flag + g.off_fl;
+    flag->jstride = g.gx;
+    flag->kstride = 0;
+    flag->nstride = 0;
+    flag->ncomp = 1;
+    fill(g.gx, g.gx, g.gy, flag->begin, flag->end);
+    *vfrac = ocfd_array4{E->d_geo + g.off_vf, g.gx, 0, 0, {0, 0, 0}, {0, 0, 0}, 1};
+    fill(g.gx, g.gx, g.gy, vfrac->begin, vfrac->end);
+    ap[0] = ocfd_array4{E->d_geo + g.off_ax, g.gx + 1, 0, 0, {0, 0, 0}, {0, 0, 0}, 1};
+    fill(g.gx + 1, g.gx + 1, g.gy, ap[0].begin, ap[0].end);
+    ap[1] = ocfd_array4{E->d_geo + g.off_ay, g.gx, 0, 0, {0, 0, 0}, {0, 0, 0}, 1};
+    fill(g.gx, g.gx, g.gy + 1, ap[1].begin, ap[1].end);
+    ap[2] = *vfrac;
+    ap[2].end[2] += 1;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_level_eb_geometry_copy(const ocfd_level* L, int ibox, uint32_t* flag, double* vfrac,
+                                        double* apx, double* apy) {
+    if (!L || ibox < 0 || ibox >= (int)L->boxes.size() || !flag || !vfrac || !apx || !apy)
+        return fail(OCFD_BAD_ARG, "ocfd_level_eb_geometry_copy");
+    const EbLevel* E = L->eb;
+    if (!E || E->geo_of[ibox] < 0) return fail(OCFD_BAD_ARG, "ocfd_level_eb_geometry_copy: box has no cut-cell data");
+    const GeoTag& g = E->geo[E->geo_of[ibox]];
+    const size_t nc = (size_t)g.gx * g.gy;
+    bool ok = cudaMemcpy(flag, E->d_flag + g.off_fl, sizeof(uint32_t) * nc, cudaMemcpyDeviceToHost) == cudaSuccess &&
+              cudaMemcpy(vfrac, E->d_geo + g.off_vf, sizeof(double) * nc, cudaMemcpyDeviceToHost) == cudaSuccess &&
+              cudaMemcpy(apx, E->d_geo + g.off_ax, sizeof(double) * (g.gx + 1) * g.gy, cudaMemcpyDeviceToHost) ==
+                  cudaSuccess &&
+              cudaMemcpy(apy, E->d_geo + g.off_ay, sizeof(double) * g.gx * (g.gy + 1), cudaMemcpyDeviceToHost) ==
+                  cudaSuccess;
+    return ok ? OCFD_OK : fail(OCFD_LAUNCH_FAIL, "ocfd_level_eb_geometry_copy");
+}
+
+}  // extern "C"

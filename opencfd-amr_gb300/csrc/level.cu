@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "level.h"
+#include "eb_level.h"
 
 namespace ocfd {
 
@@ -75,6 +76,20 @@ __device__ void dmr_functor(const BcInfo& bc, double* U, const FabGeom& f, long 
         for (int n = 0; n < ncomp && n < 5; ++n) U[c + n * f.ns] = left[n];
 }
 
+// Planar jet inflow on the x-lo face: with s(y) = (1 + tanh((w - |y - yc|) /
+// delta)) / 2, u = u_co + (u_jet - u_co) s and rho = rho_co + (rho_jet - rho_co) s
+// at uniform pressure (internal energy rho e); params = rho_jet, u_jet, u_co, yc,
+// w, delta, rho e, rho_co
+__device__ void jet_inflow(const BcInfo& bc, double* U, const FabGeom& f, long long c, int j, int ncomp) {
+    const double* pr = bc.params;
+    const double y = bc.prob_lo[1] + (j + 0.5) * bc.dx[1];
+    const double s = 0.5 * (1.0 + tanh((pr[4] - fabs(y - pr[3])) / pr[5]));
+    const double u = pr[2] + (pr[1] - pr[2]) * s;
+    const double r = pr[7] + (pr[0] - pr[7]) * s;
+    const double st[5] = {r, r * u, 0.0, 0.0, pr[6] + 0.5 * r * u * u};
+    for (int n = 0; n < ncomp && n < 5; ++n) U[c + n * f.ns] = st[n];
+}
+
 template <int D>
 __global__ void k_physbc(const BcTag* __restrict__ tags, const long long* __restrict__ start,
                          int ntag, long long total, const FabGeom* __restrict__ fabs, double* U,
@@ -108,6 +123,8 @@ __global__ void k_physbc(const BcTag* __restrict__ tags, const long long* __rest
         } else if (bc.bc_case == OCFD_CASE_INFLOW) {
             if ((T.side == 0 ? bc.lo_bc[D] : bc.hi_bc[D]) == OCFD_BC_INFLOW)
                 for (int n = 0; n < ncomp && n < 5; ++n) U[c + n * f.ns] = bc.params[n];
+        } else if (bc.bc_case == OCFD_CASE_JET) {
+            if (D == 0 && T.side == 0 && bc.lo_bc[0] == OCFD_BC_INFLOW) jet_inflow(bc, U, f, c, c3[1], ncomp);
         }
     }
 }
@@ -306,12 +323,79 @@ ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st) {
 
 ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st) {
     const bool visc = flags & OCFD_VISC;
-    RegBoxArgs dummy{};
-    return (flags & OCFD_FLUX_FP32)
-               ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[s], L->d_tile_start,
-                                        (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st)
-               : launch_rhs_regular(L->tile, visc, L->d_stage[s], L->d_tile_start,
-                                    (int)L->boxes.size(), dummy, L->ntiles, L->ctx->parm, st);
+    const bool f32 = flags & OCFD_FLUX_FP32;
+    ocfd_status r = OCFD_OK;
+    if (flags & OCFD_PER_BOX) {
+        // one launch per regular box (its tiles), then the cut boxes one by one
+        for (int b = 0; b < L->nreg && r == OCFD_OK; ++b)
+            r = f32 ? launch_rhs_regular_f32(L->tile, visc, nullptr, nullptr, 1, L->h_stage[s][b], L->h_ntiles[b],
+                                             L->ctx->parm, st)
+                    : launch_rhs_regular(L->tile, visc, nullptr, nullptr, 1, L->h_stage[s][b], L->h_ntiles[b],
+                                         L->ctx->parm, st);
+    } else if (L->ntiles > 0) {
+        RegBoxArgs dummy{};
+        r = f32 ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[s], L->d_tile_start, L->nreg, dummy, L->ntiles,
+                                         L->ctx->parm, st, L->sched, L->d_queue)
+                : launch_rhs_regular(L->tile, visc, L->d_stage[s], L->d_tile_start, L->nreg, dummy, L->ntiles,
+                                     L->ctx->parm, st, L->sched, L->d_queue);
+    }
+    if (r == OCFD_OK) r = eb_launch_stage(L, s, flags, st);
+    return r;
+}
+
+ocfd_status level_autotune(ocfd_level* L, unsigned flags, int reps, cudaStream_t st) {
+    if (L->nreg == 0 || reps <= 0) return OCFD_OK;
+    const bool visc = flags & OCFD_VISC, f32 = flags & OCFD_FLUX_FP32;
+    const StageRoles roles = L->roles ? *L->roles : StageRoles{};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bt = L->tile, bs = L->sched;
+    ocfd_status s = OCFD_OK;
+    for (int t = 0; t < kNumRegularTiles && s == OCFD_OK; ++t) {
+        if (!regular_tile_fits(t, visc)) continue;
+        L->tile = t;
+        s = build_stage_tables(L, roles);
+        for (int sc = 0; sc < NUM_SCHED && s == OCFD_OK; ++sc) {
+            L->sched = sc;
+            RegBoxArgs dummy{};
+            auto go = [&]() {
+                return f32 ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[1], L->d_tile_start, L->nreg, dummy,
+                                                    L->ntiles, L->ctx->parm, st, L->sched, L->d_queue)
+                           : launch_rhs_regular(L->tile, visc, L->d_stage[1], L->d_tile_start, L->nreg, dummy,
+                                                L->ntiles, L->ctx->parm, st, L->sched, L->d_queue);
+            };
+            s = go();  // warm-up
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && s == OCFD_OK; ++r) s = go();
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (s == OCFD_OK && ms < best) {
+                best = ms;
+                bt = t;
+                bs = sc;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != OCFD_OK) return s;
+    L->tile = bt;
+    L->sched = bs;
+    s = build_stage_tables(L, roles);
+    if (L->graph) {
+        cudaGraphExecDestroy(L->graph);
+        L->graph = nullptr;
+    }
+    if (s == OCFD_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_launch("level autotune");
+    return s;
+}
+
+int stage_launches(const ocfd_level* L, unsigned flags) {
+    return ((flags & OCFD_PER_BOX) ? L->nreg : (L->ntiles > 0 ? 1 : 0)) + eb_launches_per_stage(L, flags);
 }
 
 static ocfd_status record_step(ocfd_level* L, unsigned flags, cudaStream_t st) {
@@ -345,6 +429,10 @@ static ocfd_array4 fab_array(const ocfd_level* L, int b, int i) {
 
 // Stage tables: stage 1 A -> B, stage 2 (A, B) -> C, stage 3 (A, C) -> A (or D)
 ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
+    if (L->roles != &roles) {
+        delete L->roles;
+        L->roles = new StageRoles(roles);
+    }
     const ocfd_level_desc* desc = &L->desc;
     const double dxinv[3] = {1.0 / desc->dx[0], 1.0 / desc->dx[1], 1.0 / desc->dx[2]};
     std::vector<int> tile_start;
@@ -355,6 +443,7 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     // stage weights of the SSP-RK3 update U^{n+1} = U^n + dt (L0 + L1 + 4 L2) / 6
     const double wflux[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
     for (size_t b = 0; b < L->boxes.size(); ++b) {
+        if (!eb_box_regular(L, (int)b)) continue;  // cut / covered: eb_level.cu
         ocfd_array4 a[4];
         for (int i = 0; i < L->nbuf; ++i) a[i] = fab_array(L, (int)b, i);
         for (int k = 0; k < 3; ++k) {
@@ -395,6 +484,10 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
         }
     }
     L->ntiles = nt;
+    L->nreg = (int)tile_start.size();
+    L->h_ntiles.clear();
+    for (int b = 0; b < L->nreg; ++b) L->h_ntiles.push_back((b + 1 < L->nreg ? tile_start[b + 1] : nt) - tile_start[b]);
+    for (int k = 0; k < 3; ++k) L->h_stage[k] = st[k];
     ocfd_status s = OCFD_OK;
     for (int k = 0; k < 3 && s == OCFD_OK; ++k) {
         dev_free(L->d_stage[k], L->pool);
@@ -404,6 +497,7 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     dev_free(L->d_tile_start, L->pool);
     L->d_tile_start = nullptr;
     if (s == OCFD_OK) s = upload(&L->d_tile_start, tile_start, L->pool);
+    if (s == OCFD_OK) s = eb_build_stage_tables(L, roles);
     return s;
 }
 
@@ -512,7 +606,9 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
     }
     if (s == OCFD_OK) {
         L->d_step = static_cast<StepState*>(dev_alloc(sizeof(StepState), pool));
-        if (!L->d_step) s = fail(OCFD_OUT_OF_MEMORY, "step state");
+        L->d_queue = static_cast<unsigned*>(dev_alloc(2 * sizeof(unsigned), pool));
+        if (!L->d_step || !L->d_queue) s = fail(OCFD_OUT_OF_MEMORY, "step state");
+        else if (cudaMemset(L->d_queue, 0, 2 * sizeof(unsigned)) != cudaSuccess) s = check_launch("work queue");
     }
     if (s == OCFD_OK) {
         k_set_time<<<1, 1>>>(L->d_step, 0.0);
@@ -548,6 +644,8 @@ ocfd_status ocfd_level_create(ocfd_context* ctx, const ocfd_level_desc* desc, oc
 ocfd_status ocfd_level_destroy(ocfd_level* L) {
     if (!L) return OCFD_OK;
     if (L->graph) cudaGraphExecDestroy(L->graph);
+    eb_free(L);
+    delete L->roles;
     DevPool* pool = L->pool;
     for (int i = 0; i < 4; ++i) dev_free(L->buf[i], pool);
     for (int i = 0; i < 3; ++i) {
@@ -561,6 +659,7 @@ ocfd_status ocfd_level_destroy(ocfd_level* L) {
     dev_free(L->d_ex_start, pool);
     dev_free(L->d_tile_start, pool);
     dev_free(L->d_step, pool);
+    dev_free(L->d_queue, pool);
     delete L;
     return OCFD_OK;
 }
@@ -581,6 +680,33 @@ ocfd_status ocfd_level_state(ocfd_level* L, int ibox, ocfd_array4* out) {
 }
 
 size_t ocfd_level_state_elems(const ocfd_level* L) { return L ? (size_t)L->elems : 0; }
+
+ocfd_status ocfd_level_set_schedule(ocfd_level* L, int32_t tile, int32_t sched) {
+    if (!L || sched < 0 || sched >= NUM_SCHED || tile < -1 || tile >= kNumRegularTiles ||
+        (tile >= 0 && !regular_tile_fits(tile, true)))
+        return fail(OCFD_BAD_ARG, "ocfd_level_set_schedule");
+    L->sched = sched;
+    ocfd_status s = OCFD_OK;
+    if (tile >= 0 && tile != L->tile) {
+        L->tile = tile;
+        const StageRoles roles = L->roles ? *L->roles : StageRoles{};
+        s = build_stage_tables(L, roles);
+    }
+    if (L->graph) {
+        cudaGraphExecDestroy(L->graph);
+        L->graph = nullptr;
+    }
+    return s;
+}
+
+ocfd_status ocfd_level_autotune(ocfd_level* L, unsigned flags, int reps, int32_t* tile, int32_t* sched,
+                                void* stream) {
+    if (!L || reps <= 0) return fail(OCFD_BAD_ARG, "ocfd_level_autotune");
+    ocfd_status s = level_autotune(L, flags, reps, static_cast<cudaStream_t>(stream));
+    if (tile) *tile = L->tile;
+    if (sched) *sched = L->sched;
+    return s;
+}
 
 ocfd_status ocfd_level_copy_in(ocfd_level* L, const double* buf, void* stream) {
     if (!L || !buf) return fail(OCFD_BAD_ARG, "ocfd_level_copy_in");
@@ -618,7 +744,8 @@ ocfd_status ocfd_level_set_time(ocfd_level* L, double time, void* stream) {
 
 ocfd_status ocfd_level_advance(ocfd_level* L, int nsteps, double cfl, unsigned flags, void* stream) {
     if (!L || nsteps < 0 || !(cfl > 0)) return fail(OCFD_BAD_ARG, "ocfd_level_advance");
-    if (flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32)) return fail(OCFD_BAD_ARG, "ocfd_level_advance: flags");
+    if (flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32 | OCFD_PER_BOX))
+        return fail(OCFD_BAD_ARG, "ocfd_level_advance: flags");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (nsteps == 0) return OCFD_OK;
     if (cudaMemcpyAsync(&L->d_step->cfl, &cfl, sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -627,6 +754,13 @@ ocfd_status ocfd_level_advance(ocfd_level* L, int nsteps, double cfl, unsigned f
         ocfd_status s = launch_estdt(L, st);
         if (s != OCFD_OK) return s;
         L->need_estdt = false;
+    }
+    if (flags & OCFD_PER_BOX) {  // host-issued launches, step after step
+        for (int i = 0; i < nsteps; ++i) {
+            ocfd_status s = record_step(L, flags, st);
+            if (s != OCFD_OK) return s;
+        }
+        return OCFD_OK;
     }
     if (!L->graph || L->graph_flags != flags) {
         if (L->graph) {
@@ -680,7 +814,7 @@ int ocfd_level_launches_per_step(const ocfd_level* L, unsigned flags) {
     if (!L) return 0;
     (void)flags;
     int fill = (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0 && !L->zvirt);
-    return 2 + 3 * (fill + 1);
+    return 2 + 3 * (fill + stage_launches(L, flags));
 }
 
 ocfd_status ocfd_level_profile_stage(ocfd_level* L, unsigned flags, int reps, double* ms, void* stream) {

@@ -169,6 +169,9 @@ ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** 
     return upload(d_start, start, pool);
 }
 
+struct EbLevel;
+struct StageRoles;
+
 }  // namespace ocfd
 
 struct ocfd_level {
@@ -201,6 +204,15 @@ struct ocfd_level {
     ocfd::RegBoxArgs* d_stage[3] = {nullptr, nullptr, nullptr};
     int* d_tile_start = nullptr;
     int ntiles = 0;
+    int nreg = 0;  // boxes in the regular stage tables
+    // host copies of the regular stage tables and tiles per box (per-box launches)
+    std::vector<ocfd::RegBoxArgs> h_stage[3];
+    std::vector<int> h_ntiles;
+    // tile schedule of the batched launch (TileSched) and its work-queue words
+    int sched = ocfd::SCHED_GRID;
+    unsigned* d_queue = nullptr;
+    // the stage roles the tables were last built with (the autotuner rebuilds them)
+    ocfd::StageRoles* roles = nullptr;
     ocfd::StepState* d_step = nullptr;
     bool need_estdt = true;
     // z faces with source-cell BCs on both sides: stepping leaves their outside
@@ -210,6 +222,9 @@ struct ocfd_level {
     // device memory source: nullptr = cudaMalloc / cudaFree (standalone level),
     // else the owning hierarchy's pool (state buffers are then not zeroed)
     ocfd::DevPool* pool = nullptr;
+    // embedded body: geometry, box classes, cut-cell stage tables (eb_level.cu);
+    // nullptr: every box regular
+    ocfd::EbLevel* eb = nullptr;
     // graph
     cudaGraphExec_t graph = nullptr;
     unsigned graph_flags = ~0u;
@@ -229,11 +244,16 @@ struct StageRoles {
 };
 
 ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles);
+// time every tile shape x schedule of the level's batched stage kernel, keep the
+// fastest (stage tables rebuilt with the level's last roles); synchronous
+ocfd_status level_autotune(ocfd_level* L, unsigned flags, int reps, cudaStream_t st);
 // fill_physbc skips the z pass of a level with zvirt unless `all`
 ocfd_status fill_ghosts(ocfd_level* L, double* U, double tfrac, cudaStream_t st, bool all = false);
 ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st);
 ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st, bool all = false);
 ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st);
+// kernels one launch_stage call issues
+int stage_launches(const ocfd_level* L, unsigned flags);
 ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st);
 ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
                         DevPool* pool = nullptr, int ncomp = 5);

@@ -19,8 +19,8 @@ const int kNumRegularTiles = sizeof(kRegularTiles) / sizeof(kRegularTiles[0]);
 
 ocfd_status launch_rhs_regular(int tile, bool visc, const RegBoxArgs* d_boxes,
                                const int* d_tile_start, int nbox, const RegBoxArgs& single,
-                               int ntiles, const DevParm& P, cudaStream_t st) {
-    return launch_any<double>(tile, visc, d_boxes, d_tile_start, nbox, single, ntiles, P, st);
+                               int ntiles, const DevParm& P, cudaStream_t st, int sched, unsigned* queue) {
+    return launch_any<double>(tile, visc, d_boxes, d_tile_start, nbox, single, ntiles, P, st, sched, queue);
 }
 
 // Default tile for a box: the shape with the least padded work.

@@ -9,6 +9,8 @@
 namespace ocfd {
 
 enum RhsMode { RHS_WRITE_DSDT = 0, RHS_FUSED_STAGE = 1 };
+// tile schedules of the batched launch (k_rhs_regular)
+enum TileSched { SCHED_GRID = 0, SCHED_STRIDE = 1, SCHED_QUEUE = 2, NUM_SCHED = 3 };
 enum FluxBits { FLUX_WRITE = 1, FLUX_ACC_ALL = 2, FLUX_ACC_PLANES = 4 };
 
 struct TileShape {
@@ -117,12 +119,15 @@ void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* d
 
 // d_boxes == nullptr: one box given by `single`, ntiles CTAs.
 // otherwise: nbox boxes, d_tile_start[b] = first CTA of box b, ntiles in total.
+// sched / queue: TileSched and, for SCHED_QUEUE, two zeroed device words
 ocfd_status launch_rhs_regular(int tile, bool visc, const RegBoxArgs* d_boxes,
                                const int* d_tile_start, int nbox, const RegBoxArgs& single,
-                               int ntiles, const DevParm& P, cudaStream_t st);
+                               int ntiles, const DevParm& P, cudaStream_t st, int sched = SCHED_GRID,
+                               unsigned* queue = nullptr);
 ocfd_status launch_rhs_regular_f32(int tile, bool visc, const RegBoxArgs* d_boxes,
                                    const int* d_tile_start, int nbox, const RegBoxArgs& single,
-                                   int ntiles, const DevParm& P, cudaStream_t st);
+                                   int ntiles, const DevParm& P, cudaStream_t st, int sched = SCHED_GRID,
+                                   unsigned* queue = nullptr);
 
 ocfd_status rhs_regular_box_f32(ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* dSdt,
                                 const ocfd_array4* flux, const ocfd_box& bx,

@@ -10,9 +10,9 @@ namespace ocfd {
 ocfd_status configure_rhs_regular_f32() { return configure_all<float>(); }
 
 ocfd_status launch_rhs_regular_f32(int tile, bool visc, const RegBoxArgs* d_boxes,
-                                   const int* d_tile_start, int nbox, const RegBoxArgs& single,
-                                   int ntiles, const DevParm& P, cudaStream_t st) {
-    return launch_any<float>(tile, visc, d_boxes, d_tile_start, nbox, single, ntiles, P, st);
+                               const int* d_tile_start, int nbox, const RegBoxArgs& single,
+                               int ntiles, const DevParm& P, cudaStream_t st, int sched, unsigned* queue) {
+    return launch_any<float>(tile, visc, d_boxes, d_tile_start, nbox, single, ntiles, P, st, sched, queue);
 }
 
 ocfd_status rhs_regular_box_f32(ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* dSdt,

@@ -25,6 +25,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "device_physics.cuh"
 #include "ocfd_internal.h"
 #include "rhs_regular.h"
@@ -370,16 +372,15 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
     __syncthreads();
 }
 
+// One tile (index t over the box list, or over the single box) of the fused
+// RHS / stage; the CFL bound of its cells is folded into local_dt.
 template <class FT, int TX, int TY, int TZ, bool VISC>
-__global__ void __launch_bounds__(TX* TY* TZ)
-    k_rhs_regular(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
-                  int nbox, RegBoxArgs single, DevParm P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    FT* smem = reinterpret_cast<FT*>(smem_raw);
+__device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
+                                         int nbox, const RegBoxArgs& single, const DevParm& P, int t, FT* smem,
+                                         double& local_dt) {
     constexpr int NT = TX * TY * TZ;
-    // locate the box of this CTA: a single box, or a prefix table over a box list
+    // locate the box of this tile: a single box, or a prefix table over a box list
     int b = 0;
-    int t = blockIdx.x;
     if (boxes) {
         int lo = 0, hi = nbox - 1;
         while (lo < hi) {
@@ -425,7 +426,6 @@ __global__ void __launch_bounds__(TX* TY* TZ)
     const int ti = threadIdx.x % TX, tj = (threadIdx.x / TX) % TY, tk = threadIdx.x / (TX * TY);
     const int ci = i0 + ti, cj = j0 + tj, ck = k0 + tk;
     const bool valid = ci <= B.hi[0] && cj <= B.hi[1] && ck <= B.hi[2];
-    double local_dt = __longlong_as_double(0x7FF0000000000000LL);
     if (valid) {
         if (B.mode == RHS_WRITE_DSDT) {
 #pragma unroll
@@ -441,22 +441,82 @@ __global__ void __launch_bounds__(TX* TY* TZ)
                 un[n] = B.rk_a * u0 + B.rk_b * (us + dt * widen<FT>(acc[n]));
                 B.Uout(ci, cj, ck, n) = un[n];
             }
-            if (B.cfl_min) local_dt = stage_cfl_bound<FT>(P, un, B);
+            if (B.cfl_min) {
+                const double v = stage_cfl_bound<FT>(P, un, B);
+                local_dt = v < local_dt ? v : local_dt;
+            }
         }
     }
-    if (B.cfl_min) block_min_atomic(local_dt, B.cfl_min);
+}
+
+// Tile schedules of one launch over a box list:
+//   SCHED_GRID    one CTA per tile (grid = tiles)
+//   SCHED_STRIDE  persistent: grid = resident CTAs, CTA c takes tiles c, c + grid, ...
+//   SCHED_QUEUE   persistent: CTAs take the next tile from a counter in `queue`
+//                 (queue[0] next tile, queue[1] CTAs done); the last CTA to finish
+//                 resets both, so every launch starts from zero (graph replays too)
+template <class FT, int TX, int TY, int TZ, bool VISC>
+__global__ void __launch_bounds__(TX* TY* TZ)
+    k_rhs_regular(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
+                  int nbox, RegBoxArgs single, DevParm P, int ntiles, int sched, unsigned* queue) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FT* smem = reinterpret_cast<FT*>(smem_raw);
+    double local_dt = __longlong_as_double(0x7FF0000000000000LL);
+    unsigned long long* cfl = boxes ? boxes[0].cfl_min : single.cfl_min;  // one target per stage
+    if (sched == SCHED_GRID) {
+        rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, blockIdx.x, smem, local_dt);
+    } else if (sched == SCHED_STRIDE) {
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, smem, local_dt);
+            __syncthreads();
+        }
+    } else {
+        __shared__ int next;
+        for (;;) {
+            if (threadIdx.x == 0) next = (int)atomicAdd(&queue[0], 1u);
+            __syncthreads();
+            const int t = next;
+            __syncthreads();
+            if (t >= ntiles) break;
+            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, smem, local_dt);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&queue[1], 1u) == gridDim.x - 1) {
+                queue[0] = 0u;
+                queue[1] = 0u;
+                __threadfence();
+            }
+        }
+    }
+    if (cfl) block_min_atomic(local_dt, cfl);
 }
 
 template <class FT, int TX, int TY, int TZ, bool VISC>
 static ocfd_status launch_t(const RegBoxArgs* d_boxes, const int* d_tile_start, int nbox,
                             const RegBoxArgs& single, int ntiles, const DevParm& P,
-                            cudaStream_t st) {
+                            cudaStream_t st, int sched, unsigned* queue) {
     constexpr int NT = TX * TY * TZ;
     constexpr size_t smem = regular_smem_bytes<FT, TX, TY, TZ, VISC>();
     auto kern = k_rhs_regular<FT, TX, TY, TZ, VISC>;
     if (smem > kMaxSmem) return fail(OCFD_BAD_ARG, "regular RHS tile does not fit shared memory in this mode");
     if (ntiles <= 0) return OCFD_OK;
-    kern<<<ntiles, NT, smem, st>>>(d_boxes, d_tile_start, nbox, single, P);
+    if (sched == SCHED_QUEUE && !queue) return fail(OCFD_BAD_ARG, "regular RHS: work-queue schedule without a queue");
+    int grid = ntiles;
+    if (sched != SCHED_GRID) {
+        // resident CTAs of this shape over the whole GPU (cached per instantiation)
+        static int resident = 0;
+        if (resident == 0) {
+            int per_sm = 0, dev = 0, sms = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) != cudaSuccess) per_sm = 1;
+            resident = std::max(1, per_sm) * std::max(1, sms);
+        }
+        grid = std::min(ntiles, resident);
+    }
+    kern<<<grid, NT, smem, st>>>(d_boxes, d_tile_start, nbox, single, P, ntiles, sched, queue);
     return check_launch("k_rhs_regular");
 }
 
@@ -500,12 +560,14 @@ static bool tile_fits(int tile, bool visc) {
 template <class FT>
 static ocfd_status launch_any(int tile, bool visc, const RegBoxArgs* d_boxes, const int* d_tile_start,
                               int nbox, const RegBoxArgs& single, int ntiles, const DevParm& P,
-                              cudaStream_t st) {
+                              cudaStream_t st, int sched = SCHED_GRID, unsigned* queue = nullptr) {
     switch (tile) {
-#define OCFD_CASE(I, X, Y, Z)                                                                           \
-    case I:                                                                                             \
-        return visc ? launch_t<FT, X, Y, Z, true>(d_boxes, d_tile_start, nbox, single, ntiles, P, st) \
-                    : launch_t<FT, X, Y, Z, false>(d_boxes, d_tile_start, nbox, single, ntiles, P, st);
+#define OCFD_CASE(I, X, Y, Z)                                                                             \
+    case I:                                                                                               \
+        return visc ? launch_t<FT, X, Y, Z, true>(d_boxes, d_tile_start, nbox, single, ntiles, P, st, sched, \
+                                                  queue)                                                  \
+                    : launch_t<FT, X, Y, Z, false>(d_boxes, d_tile_start, nbox, single, ntiles, P, st, sched, \
+                                                   queue);
         OCFD_REGULAR_TILES(OCFD_CASE)
 #undef OCFD_CASE
     }

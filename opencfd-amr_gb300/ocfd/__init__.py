@@ -18,3 +18,4 @@ NSPEC = 9
 VISC = 1
 REDISTRIBUTE = 2
 FLUX_FP32 = 4
+PER_BOX = 8

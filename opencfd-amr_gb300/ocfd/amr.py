@@ -9,7 +9,7 @@ import numpy as np
 
 from ._abi import Box, check, declare, load
 from .context import _stream_ptr
-from .level import NG, Level
+from .level import NG, EbDesc, Level
 
 MAX_LEVELS = 6
 
@@ -45,6 +45,9 @@ declare("ocfd_amr_kernels_launched", ctypes.c_int64, [_vp])
 declare("ocfd_amr_state_elems", ctypes.c_size_t, [_vp, ctypes.c_int])
 declare("ocfd_amr_copy_in", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
 declare("ocfd_amr_copy_out", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
+declare("ocfd_amr_set_eb", ctypes.c_int, [_vp, ctypes.POINTER(EbDesc)])
+declare("ocfd_amr_autotune", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int, _vp])
+declare("ocfd_amr_tuned", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)])
 
 
 def _boxes_array(boxes):
@@ -127,6 +130,23 @@ class Hierarchy:
             raise IndexError(lev)
         lo, hi = self.domain(lev)
         return Level.wrap(self.ctx, h, self.grids(lev), lo, hi)
+
+    def set_eb(self, desc):
+        """Cut every level with an embedded body (ocfd.level.eb_desc(...))."""
+        check(self.lib.ocfd_amr_set_eb(self.h, ctypes.byref(desc)), "ocfd_amr_set_eb")
+
+    def box_classes(self, lev):
+        return self.level(lev).box_classes()
+
+    def autotune(self, flags=0, reps=5, stream=None):
+        """Autotune every level's batched stage kernel (kept for later regrids)."""
+        check(self.lib.ocfd_amr_autotune(self.h, flags, reps, _stream_ptr(stream)), "ocfd_amr_autotune")
+
+    def tuned(self, lev):
+        t, s = ctypes.c_int32(), ctypes.c_int32()
+        if self.lib.ocfd_amr_tuned(self.h, lev, ctypes.byref(t), ctypes.byref(s)) != 0:
+            raise IndexError(lev)
+        return t.value, s.value
 
     # ---- regridding ---------------------------------------------------------
     def regrid(self, lbase=0, stream=None):

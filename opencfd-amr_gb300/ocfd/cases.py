@@ -102,6 +102,86 @@ def dmr_amr(nx=1024, ny=256, nz=2, max_level=2, blocking_factor=32, max_grid=128
                 fab=lambda lev, lo, hi, d: dmr_fab(lo, hi, d, gamma))
 
 
+JET_SEED = 20261203
+
+
+def jet_params(gamma=GAMMA, rho=1.4, p=1.0, mach=2.0, u_co=0.5, yc=0.5, half_width=0.25, delta=0.02,
+               rho_co=1.0):
+    """Inflow parameters of the planar jet (OCFD_CASE_JET): rho_jet, u_jet, u_co,
+    yc, w, delta, rho e, rho_co.  rho = 1.4, p = 1 gives c = 1 in the jet, so
+    u_jet = Mach number; the co-flow is lighter (rho_co) and slower (u_co c)."""
+    c = math.sqrt(gamma * p / rho)
+    return (rho, mach * c, u_co * c, yc, half_width, delta, p / (gamma - 1.0), rho_co)
+
+
+def jet_kh_modes(seed=JET_SEED, nx_modes=4, nz_modes=3):
+    """Random phases of the Kelvin-Helmholtz perturbation modes (x mode m =
+    1..nx_modes, z mode l = 0..nz_modes-1), numpy PCG64 seeded with `seed`."""
+    rng = np.random.default_rng(seed)
+    return rng.uniform(0.0, 2.0 * math.pi, size=(nx_modes, nz_modes))
+
+
+def jet_fab(lo, hi, dx, prob_lo=(0.0, 0.0, 0.0), L=(2.0, 1.0, 1.0), params=None, amp=1e-2, seed=JET_SEED,
+            gamma=GAMMA, thickness=None):
+    """Grown FAB (5, nz+8, ny+8, nx+8) of the jet initial condition over lo..hi:
+    the inflow profile everywhere plus a transverse velocity perturbation
+    v' = amp u_jet sum_{m,l} sin(2 pi (m x / Lx + l z / Lz) + phi_ml) g(y) / (M L)
+    concentrated on the two shear layers, g(y) = sum_+- exp(-((y - yc -+ w) / (4 delta))^2)."""
+    rho_j, uj, uc, yc, w, delta, rhoe, rho_c = params if params is not None else jet_params(gamma)
+    x = prob_lo[0] + (np.arange(lo[0] - NG, hi[0] + NG + 1) + 0.5) * dx[0]
+    y = prob_lo[1] + (np.arange(lo[1] - NG, hi[1] + NG + 1) + 0.5) * dx[1]
+    z = prob_lo[2] + (np.arange(lo[2] - NG, hi[2] + NG + 1) + 0.5) * dx[2]
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    sh = 0.5 * (1.0 + np.tanh((w - np.abs(Y - yc)) / delta))
+    u = uc + (uj - uc) * sh
+    rho = rho_c + (rho_j - rho_c) * sh
+    th = 4.0 * delta if thickness is None else thickness
+    g = np.exp(-((Y - yc - w) / th) ** 2) + np.exp(-((Y - yc + w) / th) ** 2)
+    ph = jet_kh_modes(seed)
+    M, Lm = ph.shape
+    v = np.zeros_like(X)
+    for m in range(M):
+        for l in range(Lm):
+            v += np.sin(2 * math.pi * ((m + 1) * X / L[0] + l * Z / L[2]) + ph[m, l])
+    v *= amp * uj * g / (M * Lm)
+    F = np.empty((5,) + X.shape)
+    F[0] = rho
+    F[1] = rho * u
+    F[2] = rho * v
+    F[3] = 0.0
+    F[4] = rhoe + 0.5 * rho * (u * u + v * v)
+    return F
+
+
+def jet_eb_amr(nx=256, ny=128, nz=128, max_level=2, blocking_factor=8, max_grid=64, n_error_buf=1,
+               refine_dengrad=0.1, regrid_int=2, gamma=GAMMA, center=(0.5, 0.5), radius=0.1, redistribute=True):
+    """Mach 2 planar jet past a z-aligned cylinder (radius 0.1 at (0.5, 0.5)) in
+    [0,2] x [0,1] x [0,1]: x-lo jet inflow (OCFD_CASE_JET), x-hi and y outflow,
+    z periodic; Kelvin-Helmholtz perturbations of amplitude 1e-2 with seeded
+    random phases on the shear layers; ratio-2 levels tagged by |d rho|.  The
+    cut cells use the reference's small-cell rescale (ebr.do_redistribute = 1,
+    Source/EB/EBkernels.H:341-377): without it the unscaled 1/vfrac update of
+    cells with small volume fractions is unstable at CFL 0.5."""
+    dx = 2.0 / nx
+    params = jet_params(gamma)
+    return dict(n=(nx, ny, nz), dx=(dx, dx, dx), prob_lo=(0.0, 0.0, 0.0), lo_bc=(1, 2, 0), hi_bc=(2, 2, 0),
+                bc_case=3, case_params=params, max_level=max_level, blocking_factor=(blocking_factor,) * 3,
+                max_grid_size=(max_grid,) * 3, n_error_buf=n_error_buf, refine_dengrad=refine_dengrad,
+                regrid_int=regrid_int, eb=dict(center=center, radius=radius, redistribute=redistribute), seed=JET_SEED,
+                fab=lambda lev, lo, hi, d: jet_fab(lo, hi, d, L=(nx * dx, ny * dx, nz * dx), params=params,
+                                                   gamma=gamma))
+
+
+def jet_eb(nx=256, ny=128, nz=128, gamma=GAMMA, center=(0.5, 0.5), radius=0.1, redistribute=True):
+    """Single-level form of jet_eb_amr on a global grown array."""
+    c = jet_eb_amr(nx, ny, nz, gamma=gamma, center=center, radius=radius, redistribute=redistribute)
+    n = c["n"]
+    G = jet_fab((0, 0, 0), (n[0] - 1, n[1] - 1, n[2] - 1), c["dx"], L=tuple(m * c["dx"][0] for m in n),
+                params=c["case_params"], gamma=gamma)
+    return dict(G=G, n=n, dx=c["dx"], prob_lo=c["prob_lo"], lo_bc=c["lo_bc"], hi_bc=c["hi_bc"], bc_case=3,
+                case_params=c["case_params"], eb=c["eb"])
+
+
 # Species order of the mechanism: H2, O2, H2O, H, O, OH, HO2, H2O2, N2
 PHI1_AIR_X = (0.2958, 0.1479, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.5563)
 

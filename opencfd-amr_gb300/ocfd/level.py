@@ -6,7 +6,7 @@ import ctypes
 
 import numpy as np
 
-from ._abi import Array4, Box, check, declare, load
+from ._abi import Array4, Box, Flag4, check, declare, load
 from .context import _stream_ptr
 
 NG = 4
@@ -39,6 +39,33 @@ declare("ocfd_level_profile_stage", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_
                                                    ctypes.POINTER(ctypes.c_double), _vp])
 
 CASE_NONE, CASE_DMR, CASE_INFLOW = 0, 1, 2
+EB_NONE, EB_CYLINDER_Z = 0, 1
+BOX_REGULAR, BOX_CUT, BOX_COVERED = 0, 1, 2
+
+
+class EbDesc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("nsub", ctypes.c_int32), ("center", ctypes.c_double * 2),
+                ("radius", ctypes.c_double), ("redistribute", ctypes.c_int32)]
+
+
+def eb_desc(kind=EB_CYLINDER_Z, center=(0.5, 0.5), radius=0.1, nsub=16, redistribute=False):
+    d = EbDesc()
+    d.kind = kind
+    d.nsub = nsub
+    d.center[:] = list(center)
+    d.radius = radius
+    d.redistribute = 1 if redistribute else 0
+    return d
+
+
+declare("ocfd_level_set_eb", ctypes.c_int, [_vp, ctypes.POINTER(EbDesc)])
+declare("ocfd_level_set_schedule", ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32])
+declare("ocfd_level_autotune", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int, ctypes.POINTER(ctypes.c_int32),
+                                              ctypes.POINTER(ctypes.c_int32), _vp])
+declare("ocfd_level_box_classes", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32)])
+declare("ocfd_level_eb_geometry_copy", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _vp])
+declare("ocfd_level_eb_geometry", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Flag4), ctypes.POINTER(Array4),
+                                                 ctypes.POINTER(Array4)])
 
 
 def chop_domain(n, max_grid):
@@ -206,5 +233,43 @@ class Level:
               "profile_stage")
         return ms.value
 
+    def autotune(self, flags=0, reps=5, stream=None):
+        """Pick the fastest tile shape x schedule of the batched stage kernel;
+        returns (tile, sched)."""
+        t, s = ctypes.c_int32(), ctypes.c_int32()
+        check(self.lib.ocfd_level_autotune(self.h, flags, reps, ctypes.byref(t), ctypes.byref(s), _stream_ptr(stream)),
+              "ocfd_level_autotune")
+        return t.value, s.value
+
+    # ---- embedded body ---------------------------------------------------------
+    def set_eb(self, desc):
+        """Cut the level with an embedded body (EbDesc); classifies the boxes."""
+        check(self.lib.ocfd_level_set_eb(self.h, ctypes.byref(desc)), "ocfd_level_set_eb")
+
+    def box_classes(self):
+        out = (ctypes.c_int32 * len(self.boxes))()
+        check(self.lib.ocfd_level_box_classes(self.h, out), "ocfd_level_box_classes")
+        return list(out)
+
+    def eb_geometry(self, ibox):
+        """(flag, vfrac, apx, apy) of a box with cut-cell data as 2D numpy arrays
+        (y, x) over grow(bx, 5) (apx one column wider, apy one row taller), and
+        the (x, y) cell index of their first element."""
+        fl, vf = Flag4(), Array4()
+        ap = (Array4 * 3)()
+        check(self.lib.ocfd_level_eb_geometry(self.h, ibox, ctypes.byref(fl), ctypes.byref(vf), ap),
+              "ocfd_level_eb_geometry")
+        gx, gy = fl.end[0] - fl.begin[0], fl.end[1] - fl.begin[1]
+        flag = np.empty((gy, gx), np.uint32)
+        vfrac = np.empty((gy, gx))
+        apx = np.empty((gy, gx + 1))
+        apy = np.empty((gy + 1, gx))
+        check(self.lib.ocfd_level_eb_geometry_copy(self.h, ibox, flag.ctypes.data_as(ctypes.c_void_p),
+                                                   vfrac.ctypes.data_as(ctypes.c_void_p),
+                                                   apx.ctypes.data_as(ctypes.c_void_p),
+                                                   apy.ctypes.data_as(ctypes.c_void_p)), "eb_geometry_copy")
+        return flag, vfrac, apx, apy, (fl.begin[0], fl.begin[1])
+
     def fill_ghosts(self, time, stream=None):
         check(self.lib.ocfd_level_fill_ghosts(self.h, time, _stream_ptr(stream)), "fill_ghosts")
+

@@ -4,7 +4,8 @@ tensor-core kernels, the guard, and evaluation against the FP64 substep.
 Data: 0D constant-volume trajectories (the operator the surrogate replaces is
 the constant-volume substep of EBR::chemical_advance,
 Source/CHEM/ChemAdvance.cpp:27-82) of H2/O2/N2 mixtures with T0 in
-[1000, 2500] K, equivalence ratio in [0.5, 2] and p0 in [1, 10] atm, advanced by
+[1000, 2500] K, equivalence ratio in [0.5, 2] and p0 in [0.8, 10] atm (the
+configured [1, 10] atm extended below 1 atm, where the reacting box lies), advanced by
 the FP64 substep with a per-trajectory step; at every snapshot each state takes
 one FP64 substep of a step drawn log-uniformly in [1e-9, 1e-6] s, and the pair
 (T, p, Y, log10 dt) -> (dT, dY) is a training sample.  The lower end extends
@@ -24,6 +25,10 @@ from .context import _stream_ptr
 
 _vp = ctypes.c_void_p
 ATM = 101325.0
+# lower end of the initial pressures: the configured 1-10 atm extended to 0.8 atm
+# so that the guard's pressure range (the extremes of the training states)
+# contains the reacting box at 1 atm and its expansion regions
+P_LO_ATM = 0.8
 # species order: H2, O2, H2O, H, O, OH, HO2, H2O2, N2
 SPECIES = ("H2", "O2", "H2O", "H", "O", "OH", "HO2", "H2O2", "N2")
 
@@ -68,12 +73,12 @@ def cells_surrogate(ctx, net, guard, U, dt):
     return fb.value
 
 
-def mixtures(rng, n):
+def mixtures(rng, n, p_atm=(P_LO_ATM, 10.0)):
     """T0, p0 and mole fractions of H2/air mixtures (O2:N2 = 1:3.76) at random
     equivalence ratios"""
     T = rng.uniform(1000.0, 2500.0, n)
     phi = rng.uniform(0.5, 2.0, n)
-    p = rng.uniform(1.0, 10.0, n) * ATM
+    p = rng.uniform(p_atm[0], p_atm[1], n) * ATM
     X = np.zeros((9, n))
     tot = 2 * phi + 1.0 + 3.76
     X[0] = 2 * phi / tot

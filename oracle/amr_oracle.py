@@ -17,7 +17,14 @@ tables, what one coarse step of the GPU hierarchy does:
 * flux registers with the SSP-RK3 stage weights 1/6, 1/6, 2/3 and reflux of
   the uncovered coarse cells (EBFluxRegister CrseAdd / FineAdd / Reflux,
   Source/Advance.cpp:344-360, Source/EBR.cpp:322-330);
-* average-down with unit volume fractions (EB_average_down, Source/EBR.cpp:535-559);
+* average-down weighted by the fine volume fractions (EB_average_down,
+  Source/EBR.cpp:535-559; unit fractions without a body);
+* an optional embedded body (a z-aligned cylinder): per box the regular,
+  cut-cell (ocfdo_rhs_eb, Source/EB/AdvanceBox.cpp:16-228) or covered scheme of
+  the EBR::compute_dSdt box loop (Source/Advance.cpp:201-342), area-fraction
+  weighted cut-cell fluxes in the registers and reflux divided by the coarse
+  volume fraction (EBFluxRegister with areafrac / volfrac), piecewise-constant
+  coarse-fine interpolation next to cut or covered parents;
 * dt_0 = cfl * min over levels of est_l * 2^l, limited to 1.1 dt_prev and the
   stop time (EBR::computeNewDt, Source/EBR.cpp:240-305);
 * regridding: |d rho| >= refine_dengrad (Source/Tagging.H:11-36) buffered by
@@ -37,6 +44,9 @@ import math
 import numpy as np
 
 from oracle import NG, BCStruct
+
+T_REGULAR, T_CUT, T_COVERED = 0, 1, 3
+BOX_REGULAR, BOX_CUT, BOX_COVERED = 0, 1, 2
 
 W_RK3 = (1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0)
 RK_A = (0.0, 0.75, 1.0 / 3.0)
@@ -77,6 +87,24 @@ def mc_slope(m, c, p):
     return np.where(dl * dr <= 0.0, 0.0, s)
 
 
+def box_classes(geom, boxes):
+    """Class of each box (Source/Advance.cpp:213, 231) from the geometry of its
+    level (arrays over the level domain grown by NG): covered when all its cells
+    are covered, regular when grow(bx, NG) holds no cut or covered cell."""
+    typ = geom["flag"][0] & 3
+    out = []
+    for lo, hi in boxes:
+        valid = typ[NG + lo[2]:NG + hi[2] + 1, NG + lo[1]:NG + hi[1] + 1, NG + lo[0]:NG + hi[0] + 1]
+        grown = typ[lo[2]:hi[2] + 2 * NG + 1, lo[1]:hi[1] + 2 * NG + 1, lo[0]:hi[0] + 2 * NG + 1]
+        if np.all(valid == T_COVERED):
+            out.append(BOX_COVERED)
+        elif np.all(grown == T_REGULAR):
+            out.append(BOX_REGULAR)
+        else:
+            out.append(BOX_CUT)
+    return out
+
+
 def _sl(lo, hi, g=0):
     """numpy slices (z, y, x) of the cells lo..hi of an array offset by g."""
     return tuple(slice(lo[d] + g, hi[d] + g + 1) for d in (2, 1, 0))
@@ -85,8 +113,10 @@ def _sl(lo, hi, g=0):
 class AmrOracle:
     def __init__(self, orc, n0, dx0, lo_bc, hi_bc, boxes0, prob_lo=(0.0, 0.0, 0.0), bc_case=0,
                  case_params=(), max_level=1, blocking_factor=(8, 8, 8), max_grid_size=(32, 32, 32),
-                 n_error_buf=1, refine_dengrad=0.05):
+                 n_error_buf=1, refine_dengrad=0.05, eb=None):
         self.orc = orc
+        self.eb = eb          # None or dict(center=(cx, cy), radius=r, nsub=16, redistribute=False)
+        self._geoms = {}
         self.n0 = tuple(n0)
         self.dx0 = tuple(dx0)
         self.lo_bc = tuple(lo_bc)
@@ -113,6 +143,22 @@ class AmrOracle:
     def dx(self, l):
         return tuple(x / (1 << l) for x in self.dx0)
 
+    def geom(self, l):
+        """cut-cell geometry of level l over the whole level (None: no body)"""
+        if self.eb is None:
+            return None
+        if l not in self._geoms:
+            from ocfd import geometry
+            phi = geometry.cylinder_phi(self.eb["center"][0], self.eb["center"][1], self.eb["radius"])
+            self._geoms[l] = geometry.box_geometry(phi, (0, 0, 0), self.n(l), self.dx(l), self.prob_lo,
+                                                   nsub=self.eb.get("nsub", 16))
+        return self._geoms[l]
+
+    def classes(self, l):
+        g = self.geom(l)
+        boxes = self.levels[l]["boxes"]
+        return [BOX_REGULAR] * len(boxes) if g is None else box_classes(g, boxes)
+
     def _new_level(self, l, boxes):
         n = self.n(l)
         U = np.full((5, n[2] + 2 * NG, n[1] + 2 * NG, n[0] + 2 * NG), np.nan)
@@ -137,7 +183,9 @@ class AmrOracle:
         n = self.n(l)
         bc.lo_bc[:] = list(self.lo_bc)
         bc.hi_bc[:] = list(self.hi_bc)
-        bc.dirichlet_case = 1 if self.bc_case == 1 else 0
+        bc.dirichlet_case = self.bc_case if self.bc_case in (1, 3) else 0
+        if self.bc_case == 3:
+            bc.jet[:] = list(self.case_params[:8])
         bc.prob_lo[:] = list(self.prob_lo)
         bc.dx[:] = list(self.dx(l))
         bc.dom_lo[:] = [0, 0, 0]
@@ -188,6 +236,15 @@ class AmrOracle:
         sx = mc_slope(at(-1, 0, 0), v0, at(1, 0, 0))
         sy = mc_slope(at(0, -1, 0), v0, at(0, 1, 0))
         sz = mc_slope(at(0, 0, -1), v0, at(0, 0, 1))
+        g = self.geom(l - 1)
+        if g is not None:
+            # piecewise constant where the parent or a face neighbour is cut or covered
+            t = g["flag"][0, NG] & 3          # z-invariant: one plane over the grown level
+            nonreg = (t[pj + NG, pi + NG] | t[pj + NG, pi + NG - 1] | t[pj + NG, pi + NG + 1] |
+                      t[pj + NG - 1, pi + NG] | t[pj + NG + 1, pi + NG]) != 0
+            sx = np.where(nonreg, 0.0, sx)
+            sy = np.where(nonreg, 0.0, sy)
+            sz = np.where(nonreg, 0.0, sz)
         U[:, kk + NG, jj + NG, ii + NG] = v0 + ox * sx + oy * sy + oz * sz
 
     def fill(self, l, U, a=(1.0, 0.0, 0.0, 0.0), tfrac=0.0, srcs=None):
@@ -222,10 +279,28 @@ class AmrOracle:
         F = None
         if with_flux:
             F = [np.zeros((5, n[2] + (d == 2), n[1] + (d == 1), n[0] + (d == 0))) for d in range(3)]
-        for lo, hi in L["boxes"]:
+        g = self.geom(l)
+        cls = self.classes(l)
+        for b, (lo, hi) in enumerate(L["boxes"]):
+            if cls[b] == BOX_COVERED:
+                dS[(slice(None),) + _sl(lo, hi)] = 0.0
+                continue
             Sb = np.ascontiguousarray(S[(slice(None),) + _sl((lo[0] - NG, lo[1] - NG, lo[2] - NG),
                                                              (hi[0] + NG, hi[1] + NG, hi[2] + NG), NG)])
-            d_, f = self.orc.rhs_regular(Sb, dxinv)
+            if cls[b] == BOX_REGULAR:
+                d_, f = self.orc.rhs_regular(Sb, dxinv)
+            else:
+                gsl = (slice(None), slice(lo[2], hi[2] + 2 * NG + 1), slice(lo[1], hi[1] + 2 * NG + 1),
+                       slice(lo[0], hi[0] + 2 * NG + 1))
+                gb = dict(flag=np.ascontiguousarray(g["flag"][gsl]), vfrac=np.ascontiguousarray(g["vfrac"][gsl]))
+                ap = []
+                for d, key in enumerate(("apx", "apy", "apz")):
+                    h = list(hi)
+                    h[d] += 1
+                    gb[key] = np.ascontiguousarray(g[key][(slice(None),) + _sl(lo, h)])
+                    ap.append(gb[key])
+                d_, f = self.orc.rhs_eb(Sb, gb, dxinv, do_redistribute=self.eb.get("redistribute", False))
+                f = [ap[d] * f[d] for d in range(3)]
             dS[(slice(None),) + _sl(lo, hi)] = d_
             if with_flux:
                 for d in range(3):
@@ -302,12 +377,26 @@ class AmrOracle:
 
     def _avg_down(self, c, D):
         F = self.levels[c + 1]["U"][:, NG:-NG, NG:-NG, NG:-NG]
+        g = self.geom(c + 1)
         s = 0.0
-        for kk in range(2):
-            for jj in range(2):
-                for ii in range(2):
-                    s = s + F[:, kk::2, jj::2, ii::2]
-        avg = 0.125 * s
+        if g is None:
+            for kk in range(2):
+                for jj in range(2):
+                    for ii in range(2):
+                        s = s + F[:, kk::2, jj::2, ii::2]
+            avg = 0.125 * s
+        else:
+            # volume-fraction weights; all children covered: the first child
+            vf = g["vfrac"][:, NG:-NG, NG:-NG, NG:-NG]
+            wt = 0.0
+            for kk in range(2):
+                for jj in range(2):
+                    for ii in range(2):
+                        w = vf[:, kk::2, jj::2, ii::2]
+                        s = s + w * F[:, kk::2, jj::2, ii::2]
+                        wt = wt + w
+            with np.errstate(all="ignore"):
+                avg = np.where(wt > 0.0, s / wt, F[:, 0::2, 0::2, 0::2])
         cov = self._covered(c)
         D[:, NG:-NG, NG:-NG, NG:-NG][:, cov] = avg[:, cov]
 
@@ -344,7 +433,7 @@ class AmrOracle:
                     cell[ax] = pos[ax] + 1
                 fidx = (slice(None),) + tuple(face)
                 val = dxinv[d] * (creg[fidx] - favg[fidx])
-                V[(slice(None),) + tuple(cell)] += val if low_uncovered else -val
+                self._add_reflux(c, V, tuple(cell), val if low_uncovered else -val)
             if self.periodic[d]:
                 c0 = np.take(cov, 0, axis=ax)
                 cn = np.take(cov, n - 1, axis=ax)
@@ -360,7 +449,31 @@ class AmrOracle:
                         q.insert(ax, np.full(len(pos[0]), v, dtype=np.intp))
                         return (slice(None),) + tuple(q)
                     val = dxinv[d] * (creg[full(fc)] - favg[full(ff)])
-                    V[full(cidx)] += val if low_uncovered else -val
+                    self._add_reflux(c, V, full(cidx)[1:], val if low_uncovered else -val)
+
+    def _add_reflux(self, c, V, cell, val):
+        """V[cell] += val, divided by the volume fraction of cut cells, none for
+        covered cells"""
+        g = self.geom(c)
+        if g is None:
+            V[(slice(None),) + cell] += val
+            return
+        vf = g["vfrac"][0, NG:-NG, NG:-NG, NG:-NG][cell]
+        cut = self._cut_mask(c)[cell]
+        keep = vf > 0.0
+        with np.errstate(all="ignore"):
+            val = np.where(cut[None], val / vf[None], val)
+        sel = tuple(a[keep] for a in cell)
+        V[(slice(None),) + sel] += val[:, keep]
+
+    def _cut_mask(self, c):
+        """cells of level c in cut boxes"""
+        n = self.n(c)
+        m = np.zeros((n[2], n[1], n[0]), bool)
+        for cl, (lo, hi) in zip(self.classes(c), self.levels[c]["boxes"]):
+            if cl == BOX_CUT:
+                m[_sl(lo, hi)] = True
+        return m
 
     def average_down_all(self):
         for c in range(len(self.levels) - 2, -1, -1):

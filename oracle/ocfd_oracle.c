@@ -1452,6 +1452,22 @@ static void dmr_fill(const ocfdo_bc* bc, double* S, long long N, const box_t* b,
         for (int n = 0; n < ncomp; ++n) S[n * N + c] = bc->dmr_left[n];
 }
 
+/* Planar jet inflow on the x-lo face (the multi-level EB workload): with s(y) =
+ * (1 + tanh((w - |y - yc|) / delta)) / 2, u = u_co + (u_jet - u_co) s, rho =
+ * rho_co + (rho_jet - rho_co) s, v = w = 0, uniform pressure */
+static void jet_fill(const ocfdo_bc* bc, double* S, long long N, const box_t* b, int i, int j, int k,
+                     int ncomp) {
+    const double* pr = bc->jet;
+    int aj = j + bc->dom_lo[1];
+    double y = bc->prob_lo[1] + (aj + 0.5) * bc->dx[1];
+    double s = 0.5 * (1.0 + tanh((pr[4] - fabs(y - pr[3])) / pr[5]));
+    double u = pr[2] + (pr[1] - pr[2]) * s;
+    double r = pr[7] + (pr[0] - pr[7]) * s;
+    double st[5] = {r, r * u, 0.0, 0.0, pr[6] + 0.5 * r * u * u};
+    long long c = gI(b, i, j, k);
+    for (int n = 0; n < ncomp && n < 5; ++n) S[n * N + c] = st[n];
+}
+
 void ocfdo_fill_ghosts(const ocfdo_bc* bc, double* S, int ncomp, int nx, int ny, int nz,
                        double time) {
     box_t b = mkbox(nx, ny, nz);
@@ -1494,6 +1510,11 @@ void ocfdo_fill_ghosts(const ocfdo_bc* bc, double* S, int ncomp, int nx, int ny,
                         }
                 }
             }
+        }
+        if (bc->dirichlet_case == 3 && d == 0 && bc->lo_bc[0] == 1) {
+            for (int gcell = 0; gcell < NG; ++gcell)
+                for (int a = lo[1]; a < hi[1]; ++a)
+                    for (int bb = lo[2]; bb < hi[2]; ++bb) jet_fill(bc, S, N, &b, -1 - gcell, a, bb, ncomp);
         }
         if (bc->dirichlet_case == 1) {
             for (int side = 0; side < 2; ++side)

@@ -108,11 +108,12 @@ double ocfdo_estdt(const ocfdo_parm* p, const double* S, int nx, int ny, int nz,
  * 5 no-slip wall), mapped to AMReX BC types by Source/Setup.cpp:17-92. */
 typedef struct {
     int lo_bc[3], hi_bc[3];
-    int dirichlet_case; /* 0 none, 1 double Mach reflection functor */
+    int dirichlet_case; /* 0 none, 1 double Mach reflection functor, 3 planar jet inflow */
     double prob_lo[3], dx[3];
     int dom_lo[3];      /* absolute index of the box's first interior cell */
     int dom_hi[3];      /* absolute index of the domain's last cell */
     double dmr_left[5], dmr_right[5];
+    double jet[8];      /* rho_jet, u_jet, u_co, yc, w, delta, rho e, rho_co */
 } ocfdo_bc;
 
 void ocfdo_fill_ghosts(const ocfdo_bc* bc, double* S, int ncomp, int nx, int ny, int nz,

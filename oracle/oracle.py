@@ -52,7 +52,8 @@ class BCStruct(ctypes.Structure):
                 ("dirichlet_case", ctypes.c_int),
                 ("prob_lo", ctypes.c_double * 3), ("dx", ctypes.c_double * 3),
                 ("dom_lo", ctypes.c_int * 3), ("dom_hi", ctypes.c_int * 3),
-                ("dmr_left", ctypes.c_double * 5), ("dmr_right", ctypes.c_double * 5)]
+                ("dmr_left", ctypes.c_double * 5), ("dmr_right", ctypes.c_double * 5),
+                ("jet", ctypes.c_double * 8)]
 
 
 def build_oracle(quiet=True):
