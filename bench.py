@@ -362,6 +362,7 @@ def run_ours_jet(args, world, rank, local):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         leaf = allc = 0
         k0 = H.kernels_launched()
+        torch.cuda.nvtx.range_push("bench_timed_jet_%d" % fl)
         for e0, e1 in ev:
             l2flush.fill_(1.0)
             e0.record(stream)
@@ -371,12 +372,17 @@ def run_ours_jet(args, world, rank, local):
             leaf += a
             allc += b
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         barrier(world)
         ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
         return ms, leaf, allc, H.kernels_launched() - k0
 
-    ms_d, leaf_d, _, k_d = timed(0)
-    ms_p, leaf_p, _, k_p = timed(ocfd.PER_BOX)
+    if args.headline_only:
+        ms_d = ms_p = 1.0
+        leaf_d = leaf_p = k_p = 0
+    else:
+        ms_d, leaf_d, _, k_d = timed(0)
+        ms_p, leaf_p, _, k_p = timed(ocfd.PER_BOX)
     with ClockSampler(local) as clk:
         ms, leaf, allc, kernels = timed(ocfd.FLUX_FP32)
     value = leaf * world / (ms * 1e-3)
@@ -426,7 +432,7 @@ def run_ours_jet(args, world, rank, local):
     torch.cuda.synchronize()
     e2e_value = e2e_leaf * world / (allreduce_max(e0.elapsed_time(e1), world) * 1e-3)
 
-    l1err = amr_matched_l1(ctx, c, snap, mk=mk) if rank == 0 else None
+    l1err = amr_matched_l1(ctx, c, snap, mk=mk) if rank == 0 and not args.headline_only else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cs = cpu_sample_workload("jet-eb-amr")
@@ -442,9 +448,9 @@ def run_ours_jet(args, world, rank, local):
                        "boxes": nbox, "leaf_cell_steps_per_coarse_step": leaf / args.steps,
                        "forms_cell_steps_per_s": {"fp32_batched": value, "fp64_batched": v64,
                                                   "fp64_per_box_launches": vpb},
-                       "speedup_fp32_batched_over_fp64_batched": value / v64,
-                       "speedup_fp32_batched_over_fp64_per_box": value / vpb,
-                       "speedup_batched_over_per_box_fp64": v64 / vpb,
+                       "speedup_fp32_batched_over_fp64_batched": (value / v64) if v64 else None,
+                       "speedup_fp32_batched_over_fp64_per_box": (value / vpb) if vpb else None,
+                       "speedup_batched_over_per_box_fp64": (v64 / vpb) if vpb else None,
                        "kernels_per_coarse_step": {"fp32_batched": kernels / args.steps,
                                                    "fp64_per_box": k_p / args.steps},
                        "autotuned_tile_sched_per_level": {("fp32" if k else "fp64"): v for k, v in tuned.items()},
@@ -674,10 +680,10 @@ def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, sa
     """The learned chemistry form of the reacting workload: the MLP surrogate
     (12 -> 128 x4 GELU -> 10, BF16 on tcgen05) trained here on ~1e7 samples of
     the FP64 implicit substep (0D trajectories, T0 1000-2500 K, phi 0.5-2,
-    p 1-10 atm), then embedded in the reacting level with the guard's FP64
+    p 0.8-10 atm), then embedded in the reacting level with the guard's FP64
     fallback.  Reports the data / training cost, the fallback rate, the
     cell-steps/s beside the FP64 forms and the L1 error in T, Y_OH, Y_H2O
-    against the binned FP64 run after the same steps."""
+    against the plain FP64 run after the same steps."""
     import numpy as np
     import torch
     from ocfd import surrogate
@@ -690,7 +696,7 @@ def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, sa
     del X, T
     torch.cuda.empty_cache()
 
-    R = make(True)
+    R = make(True, f32=True)
     check(load().ocfd_react_set_surrogate(R.h, sur.net.h, ctypes.byref(sur.guard)), "set_surrogate")
     R.advance(args.warmup)
     fb0 = ctypes.c_int64()
@@ -713,7 +719,7 @@ def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, sa
     pa, pb = props(ref), props(got)
     l1 = lambda x, y: float((x - y).abs().sum() / y.abs().sum())
     return {
-        "form": "binned chemistry with the MLP surrogate, FP64 fallback on guard failure",
+        "form": "mixed FP32 faces + MLP surrogate chemistry (FP64 fallback on guard failure)",
         "cell_steps_per_s": cells * args.steps * world / (ms * 1e-3),
         "fallback_rate": fb.value / float(cells * substeps),
         "fallback_cells": int(fb.value), "cell_substeps": int(cells * substeps),
@@ -746,35 +752,48 @@ def run_ours_react(args, world, rank, local):
     stream = torch.cuda.current_stream(dev)
     l2flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def make(binned, rk=2):
+    def make(binned, rk=2, f32=False):
         R = Reactor(ctx, boxes, tuple(x - 1 for x in n), case["dx"], dt=REACT_DT, rk_order=rk, chem_substeps=4,
-                    visc=True, binned=binned)
+                    visc=True, binned=binned, flux_fp32=f32)
         R.level.set_global(case["G"])
         return R
 
-    def timed(binned):
-        R = make(binned)
+    def timed(binned, f32=False):
+        R = make(binned, f32=f32)
         R.advance(args.warmup)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.nvtx.range_push("bench_timed_react_%s%s" % ("binned" if binned else "plain", "_f32" if f32 else ""))
         for e0, e1 in ev:
             l2flush.fill_(1.0)
             e0.record(stream)
             R.advance(1)
             e1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
         return ms, R
 
     ms_plain, Rp = timed(False)
+    ms_bin, Rb = timed(True)
     with ClockSampler(local) as clk:
-        ms_bin, Rb = timed(True)
-    value = cells * args.steps * world / (ms_bin * 1e-3)
+        ms_mix, Rm = timed(True, f32=True)
+    value = cells * args.steps * world / (ms_mix * 1e-3)
+    value_bin = cells * args.steps * world / (ms_bin * 1e-3)
     value_plain = cells * args.steps * world / (ms_plain * 1e-3)
     same_steps = args.warmup + args.steps
     a = Rp.level.get_global()
     b = Rb.level.get_global()
+    mix = Rm.level.get_global()
+    Rm.close()
     identical = bool(np.array_equal(a, b))
+    from ocfd import surrogate as _sur
+    props = lambda U: _sur.cells_props(ctx, torch.as_tensor(U.reshape(14, -1), device="cuda").contiguous())
+    pa, pm = props(a), props(mix)
+    l1t = lambda x, y: float((x - y).abs().sum() / y.abs().sum())
+    mixed_err = {"steps": same_steps, "rho": float(np.abs(mix[0] - a[0]).sum() / np.abs(a[0]).sum()),
+                 "p": l1t(pm[1], pa[1]), "T": l1t(pm[0], pa[0]), "Y_OH": l1t(pm[7], pa[7]),
+                 "Y_H2O": l1t(pm[4], pa[4])}
     chem_ms = Rb.profile_chem(reps=3)
     launches = Rb.launches_per_step()
     Rp.close()
@@ -788,7 +807,7 @@ def run_ours_react(args, world, rank, local):
     rk3_vs_rk2 = {"rho": l1(c3[0], a[0]), "Y_OH": l1(y(c3, 5), y(a, 5)), "Y_H2O": l1(y(c3, 2), y(a, 2)),
                   "steps": same_steps}
 
-    sur_rep = react_surrogate_form(args, world, ctx, make, stream, l2flush, b, cells, same_steps) \
+    sur_rep = react_surrogate_form(args, world, ctx, make, stream, l2flush, a, cells, same_steps) \
         if not args.no_surrogate else None
 
     # end to end: upload the state, one step, download, per step
@@ -821,16 +840,18 @@ def run_ours_react(args, world, rank, local):
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_bin / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "warmup": args.warmup, "ms_per_step": ms_mix / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-flux/f64-state", "data": "synthetic",
             "config": {"workload": "3D H2/air reacting box 128^3 periodic, 9 species / 19 reactions, phi=1, 1 atm, "
                                    "1200 K + 8 hot spots (seed %d, edge 1 cm), mixture-averaged transport, "
                                    "Strang chemistry (4+4 substeps), RK2, dt=1e-8 s" % case["seed"],
-                       "form": "binned batched chemistry",
-                       "forms_cell_steps_per_s": {"binned": value, "plain": value_plain},
-                       "speedup_binned_over_plain": value / value_plain,
-                       "forms_identical": identical,
-                       "mixed_precision_flux": "not available for the multispecies RHS (FP64)",
+                       "form": "mixed: FP32 split + WENO-Z faces, binned batched FP64 chemistry",
+                       "forms_cell_steps_per_s": {"mixed_binned": value, "fp64_binned": value_bin,
+                                                  "fp64_plain": value_plain},
+                       "speedup_mixed_over_fp64_plain": value / value_plain,
+                       "speedup_binned_over_plain_fp64": value_bin / value_plain,
+                       "binned_identical_to_plain": identical,
+                       "l1_mixed_vs_fp64": mixed_err,
                        "rk3_vs_rk2_l1": rk3_vs_rk2, "surrogate": sur_rep, "boxes": len(boxes), "cells": cells,
                        "l2": "flushed between timed steps (512 MB write, untimed)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -998,6 +1019,8 @@ def main():
                     help="headline form (the other form is timed too and reported in config)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-surrogate", action="store_true", help="react: skip the surrogate form")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="jet-eb-amr: time the headline form only (no other forms, no L1 run); for profiling")
     ap.add_argument("--sur-epochs", type=int, default=6, help="react: surrogate training epochs")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -381,7 +381,11 @@ typedef struct ocfd_react_desc {
     int32_t rk_order;        /* 2 (the reference) or 3 */
     int32_t chem_substeps;   /* per half step; 4 on level 0 (Source/Advance.cpp:159-161) */
     double dt;
-    uint32_t flags;          /* OCFD_VISC: mixture-averaged viscous and species transport */
+    uint32_t flags;          /* OCFD_VISC: mixture-averaged viscous and species transport;
+                                OCFD_FLUX_FP32: the mixed form - Steger-Warming split and WENO-Z of
+                                the flow and species face fluxes in FP32 (primitives with the Newton
+                                temperature, transport, viscous / diffusive fluxes, RK and chemistry
+                                stay FP64) */
     int32_t binned_chem;     /* 1: chemistry as one launch over all cells ordered by a temperature key */
 } ocfd_react_desc;
 

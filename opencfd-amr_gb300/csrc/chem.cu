@@ -3,12 +3,14 @@
 // implicit chemistry substep).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <string>
 
 #include <algorithm>
 
 #include "chem_internal.h"
+#include "weno_f32.cuh"
 #include "chem_physics.cuh"
 #include "mlp_kernel.cuh"
 #include "eb_physics.cuh"
@@ -39,6 +41,24 @@ ocfd_status mech_upload(const ocfd_parm& p) {
     if (cudaMemcpyToSymbol(c_mech, &t, sizeof(t)) != cudaSuccess) {
         cudaError_t e = cudaGetLastError();
         return fail(OCFD_LAUNCH_FAIL, std::string("mechanism upload: ") + cudaGetErrorString(e));
+    }
+    TransF tf{};
+    for (int i = 0; i < NSP * 5; ++i) {
+        tf.visc[i] = (float)t.visc[i];
+        tf.cond[i] = (float)t.cond[i];
+    }
+    for (int i = 0; i < 45 * 5; ++i) tf.diff[i] = (float)t.diff[i];
+    for (int k = 0; k < NSP; ++k) {
+        tf.mw[k] = (float)t.mw[k];
+        for (int j = 0; j < NSP; ++j) {
+            tf.wr14[k][j] = (float)std::sqrt(std::sqrt(t.mw[j] / t.mw[k]));
+            tf.den[k][j] = (float)(1.0 / std::sqrt(8.0 + 8.0 * t.mw[k] / t.mw[j]));
+            tf.wratio[k][j] = (float)(t.mw[j] / t.mw[k]);
+        }
+    }
+    if (cudaMemcpyToSymbol(c_trf, &tf, sizeof(tf)) != cudaSuccess) {
+        cudaError_t e = cudaGetLastError();
+        return fail(OCFD_LAUNCH_FAIL, std::string("transport upload: ") + cudaGetErrorString(e));
     }
     return OCFD_OK;
 }
@@ -577,6 +597,27 @@ __global__ void k_chem_prims(ChemBoxArgs B, DevParm P) {
     }
 }
 
+// mixed form: transport in FP32 (transport_f32), widened into the FP64 array
+__global__ void k_chem_trans_f32(ChemBoxArgs B) {
+    const int gx = B.hi[0] - B.lo[0] + 3, gy = B.hi[1] - B.lo[1] + 3, gz = B.hi[2] - B.lo[2] + 3;
+    const long long n = (long long)gx * gy * gz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = B.lo[0] - 1 + (int)(c % gx), j = B.lo[1] - 1 + (int)((c / gx) % gy),
+                  k = B.lo[2] - 1 + (int)(c / ((long long)gx * gy));
+        const float T = d2f_bits(B.q(i, j, k, QT)), p = d2f_bits(B.q(i, j, k, QPRES));
+        const float rinv = __frcp_rn(d2f_bits(B.q(i, j, k, QRHO)));
+        float Y[NSP], D[NSP], mu, lam;
+#pragma unroll
+        for (int m = 0; m < NSP; ++m) Y[m] = d2f_bits(B.sp(i, j, k, m)) * rinv;
+        transport_f32(T, p, Y, mu, lam, D);
+        B.tr(i, j, k, 0) = f2d_bits(mu);
+        B.tr(i, j, k, 1) = f2d_bits(lam);
+#pragma unroll
+        for (int m = 0; m < NSP; ++m) B.tr(i, j, k, 2 + m) = f2d_bits(D[m]);
+    }
+}
+
 __global__ void k_chem_trans(ChemBoxArgs B) {
     const int gx = B.hi[0] - B.lo[0] + 3, gy = B.hi[1] - B.lo[1] + 3, gz = B.hi[2] - B.lo[2] + 3;
     const long long n = (long long)gx * gy * gz;
@@ -668,7 +709,49 @@ __device__ __forceinline__ void visc_multi_face(const DevParm& P, const ChemBoxA
             lamf * dT - hflux;
 }
 
+// Convective face fluxes in FP32 (the mixed form): the stencil's primitives and
+// partial densities narrowed on the integer pipes, Steger-Warming split and the
+// split factors of the species in FP32, WENO-Z on normalised stencils
+// (weno_f32.cuh), widened back to FP64.
 template <int D>
+__device__ __forceinline__ void chem_conv_f32(const ChemBoxArgs& B, int i, int j, int k, double* f, double* fs) {
+    const int di = D == 0, dj = D == 1, dk = D == 2;
+    float fp[6][5], fm[6][5], t1[6], tp[6], tm[6];
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        const int ci = i + (s - 3) * di, cj = j + (s - 3) * dj, ck = k + (s - 3) * dk;
+        const float d = d2f_bits(B.q(ci, cj, ck, QRHO)), u = d2f_bits(B.q(ci, cj, ck, QU)),
+                    v = d2f_bits(B.q(ci, cj, ck, QV)), w = d2f_bits(B.q(ci, cj, ck, QW)),
+                    cs = d2f_bits(B.q(ci, cj, ck, QC)), gamma = d2f_bits(B.q(ci, cj, ck, QGAMA));
+        const float tmp1 = __frcp_rn(2.0f * gamma);
+        const float tmp2 = 2.0f * (gamma - 1.0f);
+        const float tmp3 = __fdividef(3.0f - gamma, 2.0f * (gamma - 1.0f));
+        sw_split<D, float>(d, u, v, w, cs, tmp1, tmp2, tmp3, gamma - 1.0f, fp[s], fm[s]);
+        const float un = D == 0 ? u : (D == 1 ? v : w);
+        const float E1 = un, E2 = un - cs, E3 = un + cs;
+        const float E1P = (E1 + fabsf(E1)) * 0.5f, E2P = (E2 + fabsf(E2)) * 0.5f, E3P = (E3 + fabsf(E3)) * 0.5f;
+        t1[s] = tmp1;
+        tp[s] = tmp2 * E1P + E2P + E3P;
+        tm[s] = tmp2 * (E1 - E1P) + (E2 - E2P) + (E3 - E3P);
+    }
+#pragma unroll
+    for (int n = 0; n < 5; ++n)
+        f[n] = f2d_bits(wenoz_norm_f(fp[0][n], fp[1][n], fp[2][n], fp[3][n], fp[4][n]) +
+                        wenoz_norm_f(fm[5][n], fm[4][n], fm[3][n], fm[2][n], fm[1][n]));
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) {
+        float a[6], b[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+            const float tmp0 = d2f_bits(B.sp(i + (s - 3) * di, j + (s - 3) * dj, k + (s - 3) * dk, n)) * t1[s];
+            a[s] = tmp0 * tp[s];
+            b[s] = tmp0 * tm[s];
+        }
+        fs[n] = f2d_bits(wenoz_norm_f(a[0], a[1], a[2], a[3], a[4]) + wenoz_norm_f(b[5], b[4], b[3], b[2], b[1]));
+    }
+}
+
+template <int D, bool F32>
 __global__ void __launch_bounds__(128) k_chem_faces(ChemBoxArgs B, DevParm P) {
     const int fx = B.hi[0] - B.lo[0] + 1 + (D == 0), fy = B.hi[1] - B.lo[1] + 1 + (D == 1),
               fz = B.hi[2] - B.lo[2] + 1 + (D == 2);
@@ -679,6 +762,9 @@ __global__ void __launch_bounds__(128) k_chem_faces(ChemBoxArgs B, DevParm P) {
         const int i = B.lo[0] + (int)(c % fx), j = B.lo[1] + (int)((c / fx) % fy),
                   k = B.lo[2] + (int)(c / ((long long)fx * fy));
         double f[5], fs[NSP];
+        if (F32) {
+            chem_conv_f32<D>(B, i, j, k, f, fs);
+        } else {
         // split of the stencil cells i-3 .. i+2 along D; s = 0..5
         double fp[6][5], fm[6][5], t1[6], tp[6], tm[6];
 #pragma unroll
@@ -712,6 +798,7 @@ __global__ void __launch_bounds__(128) k_chem_faces(ChemBoxArgs B, DevParm P) {
                 b[s] = tmp0 * tm[s];
             }
             fs[n] = wenoz_plus(a[0], a[1], a[2], a[3], a[4]) + wenoz_minus(b[1], b[2], b[3], b[4], b[5]);
+        }
         }
         if (B.visc) {
             double fd[NSP], muf, lamf, hflux;
@@ -800,7 +887,7 @@ __global__ void __launch_bounds__(128) k_chem_eb_faces(ChemBoxArgs B, DevParm P)
         for (int m = 0; m < NSP; ++m)
             eb_recon(f, D, B.sp(i - 2 * di, j - 2 * dj, k - 2 * dk, m), B.sp(i - di, j - dj, k - dk, m),
                      B.sp(i, j, k, m), B.sp(i + di, j + dj, k + dk, m), rl[m], rr[m]);
-        vanleer(P, 0.5 * (ql[QGAMA] + qr[QGAMA]), ql, qr, D, flx);
+        vanleer<double>(P.smallp, 0.5 * (ql[QGAMA] + qr[QGAMA]), ql, qr, D, flx);
         vanleer_spec(ql, qr, rl, rr, D, fs);
         if (B.visc) {
             double fd[NSP], muf, lamf, hflux;
@@ -923,10 +1010,21 @@ ocfd_status launch_chem_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cud
     const long long qcells = (long long)(n[0] + 2 * B.qg) * (n[1] + 2 * B.qg) * (n[2] + 2 * B.qg);
     const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
     k_chem_prims<<<chem_blocks(qcells, 128, sms), 128, 0, st>>>(B, P);
-    if (B.visc) k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
-    k_chem_faces<0><<<chem_blocks((long long)(n[0] + 1) * n[1] * n[2], 128, sms), 128, 0, st>>>(B, P);
-    k_chem_faces<1><<<chem_blocks((long long)n[0] * (n[1] + 1) * n[2], 128, sms), 128, 0, st>>>(B, P);
-    k_chem_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, P);
+    if (B.visc) {
+        if (B.f32) k_chem_trans_f32<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
+        else k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
+    }
+    const long long nfx = (long long)(n[0] + 1) * n[1] * n[2], nfy = (long long)n[0] * (n[1] + 1) * n[2],
+                    nfz = (long long)n[0] * n[1] * (n[2] + 1);
+    if (B.f32) {
+        k_chem_faces<0, true><<<chem_blocks(nfx, 128, sms), 128, 0, st>>>(B, P);
+        k_chem_faces<1, true><<<chem_blocks(nfy, 128, sms), 128, 0, st>>>(B, P);
+        k_chem_faces<2, true><<<chem_blocks(nfz, 128, sms), 128, 0, st>>>(B, P);
+    } else {
+        k_chem_faces<0, false><<<chem_blocks(nfx, 128, sms), 128, 0, st>>>(B, P);
+        k_chem_faces<1, false><<<chem_blocks(nfy, 128, sms), 128, 0, st>>>(B, P);
+        k_chem_faces<2, false><<<chem_blocks(nfz, 128, sms), 128, 0, st>>>(B, P);
+    }
     k_chem_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
     return check_launch("multispecies RHS");
 }

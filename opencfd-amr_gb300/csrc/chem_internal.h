@@ -39,6 +39,9 @@ struct ChemBoxArgs {
     int lo[3], hi[3];
     double dxinv[3];
     int visc;
+    // mixed precision: split and WENO-Z of the faces in FP32 (the viscous,
+    // diffusive and enthalpy fluxes, the primitives and the transport stay FP64)
+    int f32;
     // cut-cell variant
     int eb;
     View<const uint32_t> flag;

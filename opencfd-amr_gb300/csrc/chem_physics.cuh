@@ -428,6 +428,90 @@ __device__ __forceinline__ void mixture_properties(double T, const double* X, do
     mu = m;
 }
 
+// ---- FP32 transport of the mixed form: the same fits and mixing rules with the
+// species-pair constants of the Wilke rule precomputed in FP64 and rounded once
+struct TransF {
+    float visc[NSP * 5], cond[NSP * 5], diff[45 * 5];
+    float mw[NSP];
+    float wr14[NSP][NSP];   // (W_j / W_k)^(1/4)
+    float den[NSP][NSP];    // 1 / sqrt(8 + 8 W_k / W_j)
+    float wratio[NSP][NSP]; // W_j / W_k
+};
+__constant__ TransF c_trf;
+
+__device__ __forceinline__ float dot5f(const float* x, const float* y) {
+    return x[0] * y[0] + x[1] * y[1] + x[2] * y[2] + x[3] * y[3] + x[4] * y[4];
+}
+
+// mixtureProperties (ChemViscous.H:16-64) and getMixDiffCoeffsMass
+// (ChemViscous.H:66-106) in FP32: mole fractions from the mass fractions,
+// Wilke viscosity, averaged conductivity, mixture-averaged diffusivities
+__device__ __forceinline__ void transport_f32(float T, float p, const float* Y, float& mu, float& lambda, float* D) {
+    float X[NSP], tmp[NSP], yow = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NSP; ++i) {
+        tmp[i] = __fdividef(Y[i], c_trf.mw[i]);
+        yow += tmp[i];
+    }
+    const float yowinv = __frcp_rn(yow);
+#pragma unroll
+    for (int i = 0; i < NSP; ++i) X[i] = tmp[i] * yowinv;
+    const float sqT = sqrtf(T), logT = __logf(T), sqsqT = sqrtf(sqT);
+    const float poly[5] = {1.0f, logT, logT * logT, logT * logT * logT, logT * logT * logT * logT};
+    float mui[NSP], sqmui[NSP], lami[NSP];
+    float s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) {
+        sqmui[k] = sqsqT * dot5f(poly, &c_trf.visc[k * 5]);
+        lami[k] = sqT * dot5f(poly, &c_trf.cond[k * 5]);
+        mui[k] = sqmui[k] * sqmui[k];
+        s1 += X[k] * lami[k];
+        s2 += __fdividef(X[k], lami[k]);
+    }
+    lambda = 0.5f * (s1 + __frcp_rn(s2));
+    float phi[NSP][NSP];
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) {
+#pragma unroll
+        for (int j = 0; j < k; ++j) {
+            const float f1 = 1.0f + __fdividef(sqmui[k], sqmui[j]) * c_trf.wr14[k][j];
+            const float t = f1 * f1 * c_trf.den[k][j];
+            phi[k][j] = t;
+            phi[j][k] = __fdividef(t, __fdividef(mui[k], mui[j]) * c_trf.wratio[k][j]);
+        }
+        phi[k][k] = 1.0f;
+    }
+    float m = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NSP; ++k) {
+        float t = 0.0f;
+#pragma unroll
+        for (int j = 0; j < NSP; ++j) t += X[j] * phi[k][j];
+        m += __fdividef(X[k] * mui[k], t);
+    }
+    mu = m;
+    const float t32 = T * sqT;
+    float mmw = 0.0f;
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) mmw += X[n] * c_trf.mw[n];
+#pragma unroll
+    for (int n = 0; n < NSP; n++) {
+        float a1 = 0.0f, a2 = 0.0f;
+#pragma unroll
+        for (int nn = 0; nn < NSP; nn++) {
+            if (nn == n) continue;
+            const int a = n < nn ? n : nn, b = n < nn ? nn : n;
+            const int ic = a * NSP - (a * (a - 1)) / 2 + (b - a);
+            const float bdinv = __frcp_rn(t32 * dot5f(poly, &c_trf.diff[ic * 5]));
+            a1 += X[nn] * bdinv;
+            a2 += X[nn] * c_trf.mw[nn] * bdinv;
+        }
+        a1 *= p;
+        a2 *= __fdividef(p * X[n], mmw - c_trf.mw[n] * X[n]);
+        D[n] = __frcp_rn(a1 + a2);
+    }
+}
+
 // getMixDiffCoeffsMass, ChemViscous.H:66-106
 __device__ __forceinline__ void mix_diff_coeffs(double T, double p, const double* X, double* D) {
     const double logT = log(T);

@@ -64,7 +64,7 @@ __global__ void k_eb_faces(EbBoxArgs B, DevParm P) {
             eb_recon(f, D, q(i - 2 * di, j - 2 * dj, k - 2 * dk, m), q(i - di, j - dj, k - dk, m),
                      q(i, j, k, m), q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
         double flx[5];
-        vanleer(P, P.gamma, ql, qr, D, flx);
+        vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
         if (B.visc) eb_visc_face(P, q, B.flag, D, i, j, k, B.dxinv, flx, 1, false, 0, 0, 0);
 #pragma unroll
         for (int m = 0; m < 5; ++m) B.flux[D](i, j, k, m) = flx[m];

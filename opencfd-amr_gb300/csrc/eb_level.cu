@@ -13,6 +13,8 @@
 //   k_ebl_div_stage   per cell: cut-cell divergence with the wall flux, negated
 //                     (zero in covered boxes), fused with the Shu-Osher stage
 //                     update and the CFL bound of the new state
+// In the mixed form (OCFD_FLUX_FP32, inviscid) the face states and the Van Leer
+// flux are FP32; primitives, divergence, wall flux and RK stay FP64.
 // Work items of a batch are addressed through prefix sums over the boxes.
 //
 // Geometry.  AMReX EB2 (Source/Geometry.cpp:9-29) is absent.  For a body
@@ -42,6 +44,7 @@
 
 #include "eb_level.h"
 #include "eb_physics.cuh"
+#include "weno_f32.cuh"
 
 namespace ocfd {
 
@@ -180,9 +183,22 @@ struct EbStageBox {
     View<double> fplane[3][2];
 };
 
+// Work items of a batch are found through the prefix sums over the boxes; a
+// chunk table (the tag holding item 128 c, for every c) replaces the binary
+// search by one load and a short forward scan.
+constexpr int EB_CHUNK_LOG2 = 7;
+
+__device__ __forceinline__ int tag_of(const long long* start, const int* chunk, int ntag, long long idx) {
+    if (!chunk) return find_tag<int>(start, ntag, idx);
+    int t = chunk[idx >> EB_CHUNK_LOG2];
+    while (t + 1 < ntag && start[t + 1] <= idx) ++t;
+    return t;
+}
+
 struct EbStageArgs {
     const EbStageBox* boxes;
     int nbox;
+    const int *pchunk, *fchunk, *cchunk;  // chunk tables (nullptr: binary search)
     const long long* pstart;  // grow(bx, 2) cells of each box (0 for covered boxes)
     long long ptotal;
     const long long* fstart;  // faces, tag 3 b + d (0 for covered boxes)
@@ -198,7 +214,7 @@ struct EbStageArgs {
 __global__ void k_ebl_prims(EbStageArgs A, DevParm P) {
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ptotal;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int b = find_tag<EbStageBox>(A.pstart, A.nbox, idx);
+        const int b = tag_of(A.pstart, A.pchunk, A.nbox, idx);
         const EbStageBox& B = A.boxes[b];
         const long long loc = idx - A.pstart[b];
         const int gx = B.hi[0] - B.lo[0] + 5, gy = B.hi[1] - B.lo[1] + 5;
@@ -211,10 +227,14 @@ __global__ void k_ebl_prims(EbStageArgs A, DevParm P) {
     }
 }
 
+// F32: the mixed form - primitives narrowed on the integer pipes, MUSCL-minmod
+// states and the Van Leer flux in FP32, the flux widened back (inviscid only;
+// the EB viscous flux and everything after the face flux stay FP64)
+template <bool F32>
 __global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ftotal;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int t = find_tag<EbStageBox>(A.fstart, 3 * A.nbox, idx);
+        const int t = tag_of(A.fstart, A.fchunk, 3 * A.nbox, idx);
         const int b = t / 3, D = t % 3;
         const EbStageBox& B = A.boxes[b];
         const long long loc = idx - A.fstart[t];
@@ -224,14 +244,26 @@ __global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
         const int di = D == 0, dj = D == 1, dk = D == 2;
         const View<const double> q{B.q.p, B.q.js, B.q.ks, B.q.ns, B.q.b0, B.q.b1, B.q.b2};
         const uint32_t f = B.flag(i, j, k);
-        double ql[7], qr[7];
-#pragma unroll
-        for (int m = 0; m < 7; ++m)
-            eb_recon(f, D, q(i - 2 * di, j - 2 * dj, k - 2 * dk, m), q(i - di, j - dj, k - dk, m), q(i, j, k, m),
-                     q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
         double flx[5];
-        vanleer(P, P.gamma, ql, qr, D, flx);
-        if (A.visc) eb_visc_face(P, q, B.flag, D, i, j, k, A.dxinv, flx, 1, false, 0, 0, 0);
+        if (F32) {
+            float ql[7], qr[7], ff[5];
+#pragma unroll
+            for (int m = 0; m < 7; ++m)
+                eb_recon<float>(f, D, d2f_bits(q(i - 2 * di, j - 2 * dj, k - 2 * dk, m)),
+                                d2f_bits(q(i - di, j - dj, k - dk, m)), d2f_bits(q(i, j, k, m)),
+                                d2f_bits(q(i + di, j + dj, k + dk, m)), ql[m], qr[m]);
+            vanleer<float>(P.f_smallp, P.f_gamma, ql, qr, D, ff);
+#pragma unroll
+            for (int m = 0; m < 5; ++m) flx[m] = f2d_bits(ff[m]);
+        } else {
+            double ql[7], qr[7];
+#pragma unroll
+            for (int m = 0; m < 7; ++m)
+                eb_recon(f, D, q(i - 2 * di, j - 2 * dj, k - 2 * dk, m), q(i - di, j - dj, k - dk, m), q(i, j, k, m),
+                         q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
+            vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
+            if (A.visc) eb_visc_face(P, q, B.flag, D, i, j, k, A.dxinv, flx, 1, false, 0, 0, 0);
+        }
 #pragma unroll
         for (int m = 0; m < 5; ++m) B.flux[D](i, j, k, m) = flx[m];
         if (B.has_flux) {
@@ -257,7 +289,7 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
     double local_dt = __longlong_as_double(0x7FF0000000000000LL);
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ctotal;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int b = find_tag<EbStageBox>(A.cstart, A.nbox, idx);
+        const int b = tag_of(A.cstart, A.cchunk, A.nbox, idx);
         const EbStageBox& B = A.boxes[b];
         const long long loc = idx - A.cstart[b];
         const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1;
@@ -368,6 +400,7 @@ struct ocfd::EbLevel {
     std::vector<long long> pcount, fcount, ccount;
     long long* d_floc = nullptr;  // (0, F0, F0 + F1) per box
     long long* d_zero = nullptr;
+    int *d_pchunk = nullptr, *d_fchunk = nullptr, *d_cchunk = nullptr;
 };
 
 namespace ocfd {
@@ -383,7 +416,11 @@ static void eb_free_tables(ocfd_level* L) {
     dev_free(E->d_cstart, L->pool);
     dev_free(E->d_floc, L->pool);
     dev_free(E->d_zero, L->pool);
+    dev_free(E->d_pchunk, L->pool);
+    dev_free(E->d_fchunk, L->pool);
+    dev_free(E->d_cchunk, L->pool);
     E->d_pstart = E->d_fstart = E->d_cstart = E->d_floc = E->d_zero = nullptr;
+    E->d_pchunk = E->d_fchunk = E->d_cchunk = nullptr;
 }
 
 void eb_free(ocfd_level* L) {
@@ -664,6 +701,20 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     if (s == OCFD_OK) s = upload(&E->d_cstart, cs, L->pool);
     if (s == OCFD_OK) s = upload(&E->d_floc, floc, L->pool);
     if (s == OCFD_OK) s = upload(&E->d_zero, std::vector<long long>(1, 0), L->pool);
+    // chunk tables: the tag holding item (c << EB_CHUNK_LOG2)
+    auto chunks = [](const std::vector<long long>& start, long long total) {
+        std::vector<int> out((size_t)((total >> EB_CHUNK_LOG2) + 1), 0);
+        int t = 0;
+        for (size_t c = 0; c < out.size(); ++c) {
+            const long long idx = (long long)c << EB_CHUNK_LOG2;
+            while (t + 1 < (int)start.size() && start[t + 1] <= idx) ++t;
+            out[c] = t;
+        }
+        return out;
+    };
+    if (s == OCFD_OK) s = upload(&E->d_pchunk, chunks(ps, pt), L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_fchunk, chunks(fs, ft), L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_cchunk, chunks(cs, ct), L->pool);
     return s;
 }
 
@@ -679,6 +730,9 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
     A.ftotal = E->ftotal;
     A.cstart = E->d_cstart;
     A.ctotal = E->ctotal;
+    A.pchunk = E->d_pchunk;
+    A.fchunk = E->d_fchunk;
+    A.cchunk = E->d_cchunk;
     for (int d = 0; d < 3; ++d) {
         A.dxinv[d] = 1.0 / L->desc.dx[d];
         A.dx[d] = L->desc.dx[d];
@@ -687,6 +741,7 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
     A.cfl_min = (s == 2 && E->cfl3) ? &L->d_step->cfl_min : nullptr;
     A.visc = (flags & OCFD_VISC) ? 1 : 0;
     A.redist = E->desc.redistribute ? 1 : 0;
+    const bool f32 = (flags & OCFD_FLUX_FP32) && !A.visc;
     const int sms = L->ctx->num_sms;
     if (flags & OCFD_PER_BOX) {
         // one box at a time (the reference's per-box kernel chain)
@@ -701,14 +756,21 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
             B.ftotal = E->fcount[e];
             B.cstart = E->d_zero;
             B.ctotal = E->ccount[e];
+            B.pchunk = B.fchunk = B.cchunk = nullptr;
             if (B.ptotal > 0) k_ebl_prims<<<grid_for(B.ptotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
-            if (B.ftotal > 0) k_ebl_faces<<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
+            if (B.ftotal > 0) {
+                if (f32) k_ebl_faces<true><<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
+                else k_ebl_faces<false><<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
+            }
             k_ebl_div_stage<<<grid_for(B.ctotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
         }
         return check_launch("level cut-cell stage (per box)");
     }
     if (A.ptotal > 0) k_ebl_prims<<<grid_for(A.ptotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
-    if (A.ftotal > 0) k_ebl_faces<<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
+    if (A.ftotal > 0) {
+        if (f32) k_ebl_faces<true><<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
+        else k_ebl_faces<false><<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
+    }
     k_ebl_div_stage<<<grid_for(A.ctotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
     return check_launch("level cut-cell stage");
 }

@@ -16,64 +16,66 @@ __device__ __forceinline__ bool eb_conn(uint32_t f, int i, int j, int k) {
 __device__ __forceinline__ bool eb_covered(uint32_t f) { return (f & 3u) == 3u; }
 __device__ __forceinline__ bool eb_regular(uint32_t f) { return (f & 3u) == 0u; }
 
-// minmod, Source/kernel/Reconstruction.H:8-19
-__device__ __forceinline__ double minmod(double a, double b) {
+// minmod, Source/kernel/Reconstruction.H:8-19 (T = double: the reference's
+// arithmetic; T = float: the mixed form's cut-cell faces)
+template <class T>
+__device__ __forceinline__ T minmod(T a, T b) {
     if (a * b > 0) return fabs(a) > fabs(b) ? b : a;
-    return 0.0;
+    return T(0);
 }
 
 // eb_recon_x/y/z for one component: left/right states at the D-face of cell c
 // given the values at c-2e, c-e, c, c+e and the flag of c.
-__device__ __forceinline__ void eb_recon(uint32_t f, int D, double vm2, double vm1, double v0,
-                                         double vp1, double& l, double& r) {
+template <class T>
+__device__ __forceinline__ void eb_recon(uint32_t f, int D, T vm2, T vm1, T v0, T vp1, T& l, T& r) {
     const int di = D == 0, dj = D == 1, dk = D == 2;
     l = vm1;
     r = v0;
     if (eb_conn(f, -di, -dj, -dk)) {
-        if (eb_conn(f, -2 * di, -2 * dj, -2 * dk)) l = vm1 + 0.5 * minmod(v0 - vm1, vm1 - vm2);
-        if (eb_conn(f, di, dj, dk)) r = v0 - 0.5 * minmod(vp1 - v0, v0 - vm1);
+        if (eb_conn(f, -2 * di, -2 * dj, -2 * dk)) l = vm1 + T(0.5) * minmod<T>(v0 - vm1, vm1 - vm2);
+        if (eb_conn(f, di, dj, dk)) r = v0 - T(0.5) * minmod<T>(vp1 - v0, v0 - vm1);
     }
 }
 
 // Van Leer flux vector splitting, Source/EB/EBkernels.H:73-171
-__device__ __forceinline__ void vanleer(const DevParm& P, double gamma, const double* ql,
-                                        const double* qr, int D, double* flx) {
-    double fp[5] = {0, 0, 0, 0, 0}, fm[5] = {0, 0, 0, 0, 0};
-    const double dl = ql[QRHO], ul = ql[QU], vl = ql[QV], wl = ql[QW], pl = dmax(ql[QPRES], P.smallp);
-    const double dr = qr[QRHO], ur = qr[QU], vr = qr[QV], wr = qr[QW], pr = dmax(qr[QPRES], P.smallp);
-    const double cL = ql[QC], cR = qr[QC];
+template <class T>
+__device__ __forceinline__ void vanleer(T smallp, T gamma, const T* ql, const T* qr, int D, T* flx) {
+    T fp[5] = {0, 0, 0, 0, 0}, fm[5] = {0, 0, 0, 0, 0};
+    const T dl = ql[QRHO], ul = ql[QU], vl = ql[QV], wl = ql[QW], pl = ql[QPRES] > smallp ? ql[QPRES] : smallp;
+    const T dr = qr[QRHO], ur = qr[QU], vr = qr[QV], wr = qr[QW], pr = qr[QPRES] > smallp ? qr[QPRES] : smallp;
+    const T cL = ql[QC], cR = qr[QC];
     const int nn[3] = {D == 0, D == 1, D == 2};
-    const double UL = D == 0 ? ul : (D == 1 ? vl : wl);
-    const double UR = D == 0 ? ur : (D == 1 ? vr : wr);
-    const double ML = UL / cL, MR = UR / cR;
-    const double lv[3] = {ul, vl, wl}, rv[3] = {ur, vr, wr};
-    if (ML >= 1.0) {
+    const T UL = D == 0 ? ul : (D == 1 ? vl : wl);
+    const T UR = D == 0 ? ur : (D == 1 ? vr : wr);
+    const T ML = UL / cL, MR = UR / cR;
+    const T lv[3] = {ul, vl, wl}, rv[3] = {ur, vr, wr};
+    if (ML >= T(1)) {
         fp[0] = dl * UL;
 #pragma unroll
-        for (int m = 0; m < 3; ++m) fp[1 + m] = dl * UL * lv[m] + nn[m] * pl;
-        fp[4] = UL * (gamma * pl / (gamma - 1.0) + 0.5 * dl * (ul * ul + vl * vl + wl * wl));
-    } else if (fabs(ML) < 1.0) {
-        const double Mp = 0.250 * (1.0 + ML) * (1.0 + ML);
-        const double t0 = dl * cL * Mp;
+        for (int m = 0; m < 3; ++m) fp[1 + m] = dl * UL * lv[m] + T(nn[m]) * pl;
+        fp[4] = UL * (gamma * pl / (gamma - T(1)) + T(0.5) * dl * (ul * ul + vl * vl + wl * wl));
+    } else if (fabs(ML) < T(1)) {
+        const T Mp = T(0.25) * (T(1) + ML) * (T(1) + ML);
+        const T t0 = dl * cL * Mp;
         fp[0] = t0;
 #pragma unroll
-        for (int m = 0; m < 3; ++m) fp[1 + m] = t0 * (nn[m] * (-UL + 2.0 * cL) / gamma + lv[m]);
+        for (int m = 0; m < 3; ++m) fp[1 + m] = t0 * (T(nn[m]) * (-UL + T(2) * cL) / gamma + lv[m]);
         fp[4] = t0 * (((gamma - 1) * UL + 2 * cL) * ((gamma - 1) * UL + 2 * cL) / (2 * (gamma * gamma - 1)) +
                       (ul * ul + vl * vl + wl * wl - UL * UL) / 2);
     }
-    if (fabs(MR) < 1.0) {
-        const double Mm = -0.250 * (MR - 1.0) * (MR - 1.0);
-        const double t0 = dr * cR * Mm;
+    if (fabs(MR) < T(1)) {
+        const T Mm = T(-0.25) * (MR - T(1)) * (MR - T(1));
+        const T t0 = dr * cR * Mm;
         fm[0] = t0;
 #pragma unroll
-        for (int m = 0; m < 3; ++m) fm[1 + m] = t0 * (nn[m] * (-UR - 2.0 * cR) / gamma + rv[m]);
+        for (int m = 0; m < 3; ++m) fm[1 + m] = t0 * (T(nn[m]) * (-UR - T(2) * cR) / gamma + rv[m]);
         fm[4] = t0 * (((gamma - 1) * UR - 2 * cR) * ((gamma - 1) * UR - 2 * cR) / (2 * (gamma * gamma - 1)) +
                       (ur * ur + vr * vr + wr * wr - UR * UR) / 2);
-    } else if (MR <= -1.0) {
+    } else if (MR <= T(-1)) {
         fm[0] = dr * UR;
 #pragma unroll
-        for (int m = 0; m < 3; ++m) fm[1 + m] = dr * UR * rv[m] + nn[m] * pr;
-        fm[4] = UR * (gamma * pr / (gamma - 1.0) + 0.5 * dr * (ur * ur + vr * vr + wr * wr));
+        for (int m = 0; m < 3; ++m) fm[1 + m] = dr * UR * rv[m] + T(nn[m]) * pr;
+        fm[4] = UR * (gamma * pr / (gamma - T(1)) + T(0.5) * dr * (ur * ur + vr * vr + wr * wr));
     }
 #pragma unroll
     for (int n = 0; n < 5; ++n) flx[n] = fp[n] + fm[n];

@@ -336,6 +336,7 @@ ocfd_status ocfd_react_create(ocfd_context* ctx, const ocfd_react_desc* desc, oc
             ChemBoxArgs A{};
             chem_rhs_args(A, view_of<const double>(&S), view_of<const double>(&sp), view_of<double>(&d),
                           view_of<double>(&ds), L->boxes[b], dxinv, (desc->flags & OCFD_VISC) != 0, R->scr);
+            A.f32 = (desc->flags & OCFD_FLUX_FP32) ? 1 : 0;
             R->args[in].push_back(A);
         }
     if (cudaDeviceSynchronize() != cudaSuccess) {

@@ -30,7 +30,7 @@ declare("ocfd_chem_state_tpx", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, _vp
 
 class Reactor:
     def __init__(self, ctx, boxes, domain_hi, dx, lo_bc=(0, 0, 0), hi_bc=(0, 0, 0), dt=1e-8, rk_order=2,
-                 chem_substeps=4, visc=True, binned=False, prob_lo=(0.0, 0.0, 0.0)):
+                 chem_substeps=4, visc=True, binned=False, prob_lo=(0.0, 0.0, 0.0), flux_fp32=False):
         self.ctx = ctx
         self.lib = load()
         d = ReactDesc()
@@ -50,7 +50,7 @@ class Reactor:
         d.rk_order = rk_order
         d.chem_substeps = chem_substeps
         d.dt = dt
-        d.flags = 1 if visc else 0
+        d.flags = (1 if visc else 0) | (4 if flux_fp32 else 0)
         d.binned_chem = 1 if binned else 0
         self._keep = bx
         h = ctypes.c_void_p()

@@ -196,3 +196,22 @@ def test_schedules_and_per_box_launches_are_bit_identical(ctx):
         lev.close()
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+def test_mixed_form_close_to_fp64(ctx):
+    """the mixed form on a cut level (FP32 WENO-Z in regular boxes, FP32 MUSCL
+    states + Van Leer flux in cut boxes) stays within 1e-6 L1 of the FP64 form"""
+    import ocfd
+    from ocfd.cases import jet_eb
+    c = jet_eb(64, 32, 8)
+    case = dict(c, center=c["eb"]["center"], radius=c["eb"]["radius"])
+    out = []
+    for flags in (0, ocfd.FLUX_FP32):
+        lev, boxes = make(ctx, case, (16, 16, 8), redist=True)
+        lev.advance(10, 0.5, flags)
+        out.append(lev.get_global())
+        lev.close()
+    a, b = out
+    assert np.isfinite(b).all() and not np.array_equal(a, b)
+    l1 = lambda x, y: float(np.abs(x - y).sum() / np.abs(y).sum())
+    assert l1(b[0], a[0]) < 1e-6 and l1(b[4], a[4]) < 1e-6
