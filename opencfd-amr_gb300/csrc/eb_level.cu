@@ -13,8 +13,9 @@
 //   k_ebl_div_stage   per cell: cut-cell divergence with the wall flux, negated
 //                     (zero in covered boxes), fused with the Shu-Osher stage
 //                     update and the CFL bound of the new state
-// In the mixed form (OCFD_FLUX_FP32, inviscid) the face states and the Van Leer
-// flux are FP32; primitives, divergence, wall flux and RK stay FP64.
+// In the mixed form (OCFD_FLUX_FP32, inviscid) the primitives (from the narrowed
+// state), the face states and the Van Leer flux are FP32 and kept in FP32
+// scratch; divergence, wall flux and RK stay FP64.
 // Work items of a batch are addressed through prefix sums over the boxes.
 //
 // Geometry.  AMReX EB2 (Source/Geometry.cpp:9-29) is absent.  For a body
@@ -174,6 +175,8 @@ struct EbStageBox {
     View<const uint32_t> flag;
     View<const double> vfrac, ap[3];
     View<double> q, flux[3];
+    // the same scratch read as FP32 arrays (same element strides) in the mixed form
+    View<float> qf, fluxf[3];
     int lo[3], hi[3];
     double rk_a, rk_b;
     int covered;
@@ -211,19 +214,39 @@ struct EbStageArgs {
     int visc, redist;
 };
 
+// F32 (mixed form): c2prim in FP32 from the state narrowed on the integer
+// pipes, stored as FP32 primitives for the FP32 faces
+template <bool F32>
 __global__ void k_ebl_prims(EbStageArgs A, DevParm P) {
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ptotal;
          idx += (long long)gridDim.x * blockDim.x) {
         const int b = tag_of(A.pstart, A.pchunk, A.nbox, idx);
         const EbStageBox& B = A.boxes[b];
-        const long long loc = idx - A.pstart[b];
+        const int loc = (int)(idx - A.pstart[b]);
         const int gx = B.hi[0] - B.lo[0] + 5, gy = B.hi[1] - B.lo[1] + 5;
-        const int i = B.lo[0] - 2 + (int)(loc % gx), j = B.lo[1] - 2 + (int)((loc / gx) % gy),
-                  k = B.lo[2] - 2 + (int)(loc / ((long long)gx * gy));
-        double q[7];
-        c2prim_ideal(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3), B.S(i, j, k, 4), q);
+        const int r = loc / gx;
+        const int i = B.lo[0] - 2 + (loc - r * gx), j = B.lo[1] - 2 + r % gy, k = B.lo[2] - 2 + r / gy;
+        if (F32) {
+            const float g = P.f_gamma;
+            const float u0 = d2f_bits(B.S(i, j, k, 0)), u1 = d2f_bits(B.S(i, j, k, 1)), u2 = d2f_bits(B.S(i, j, k, 2)),
+                        u3 = d2f_bits(B.S(i, j, k, 3)), u4 = d2f_bits(B.S(i, j, k, 4));
+            const float rho = fmaxf(u0, P.f_smallr);
+            const float rhoinv = __frcp_rn(rho);
+            const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
+            const float p = fmaxf((g - 1.0f) * (u4 - rho * (0.5f * (ux * ux + uy * uy + uz * uz))), P.f_smallp);
+            B.qf(i, j, k, QRHO) = rho;
+            B.qf(i, j, k, QU) = ux;
+            B.qf(i, j, k, QV) = uy;
+            B.qf(i, j, k, QW) = uz;
+            B.qf(i, j, k, QPRES) = p;
+            B.qf(i, j, k, QT) = p * rhoinv * P.f_invRg;
+            B.qf(i, j, k, QC) = sqrtf(g * p * rhoinv);
+        } else {
+            double q[7];
+            c2prim_ideal(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3), B.S(i, j, k, 4), q);
 #pragma unroll
-        for (int m = 0; m < 7; ++m) B.q(i, j, k, m) = q[m];
+            for (int m = 0; m < 7; ++m) B.q(i, j, k, m) = q[m];
+        }
     }
 }
 
@@ -237,24 +260,27 @@ __global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
         const int t = tag_of(A.fstart, A.fchunk, 3 * A.nbox, idx);
         const int b = t / 3, D = t % 3;
         const EbStageBox& B = A.boxes[b];
-        const long long loc = idx - A.fstart[t];
+        const int loc = (int)(idx - A.fstart[t]);
         const int fx = B.hi[0] - B.lo[0] + 1 + (D == 0), fy = B.hi[1] - B.lo[1] + 1 + (D == 1);
-        const int i = B.lo[0] + (int)(loc % fx), j = B.lo[1] + (int)((loc / fx) % fy),
-                  k = B.lo[2] + (int)(loc / ((long long)fx * fy));
+        const int r = loc / fx;
+        const int i = B.lo[0] + (loc - r * fx), j = B.lo[1] + r % fy, k = B.lo[2] + r / fy;
         const int di = D == 0, dj = D == 1, dk = D == 2;
         const View<const double> q{B.q.p, B.q.js, B.q.ks, B.q.ns, B.q.b0, B.q.b1, B.q.b2};
         const uint32_t f = B.flag(i, j, k);
         double flx[5];
         if (F32) {
+            const View<float>& qf = B.qf;
             float ql[7], qr[7], ff[5];
 #pragma unroll
             for (int m = 0; m < 7; ++m)
-                eb_recon<float>(f, D, d2f_bits(q(i - 2 * di, j - 2 * dj, k - 2 * dk, m)),
-                                d2f_bits(q(i - di, j - dj, k - dk, m)), d2f_bits(q(i, j, k, m)),
-                                d2f_bits(q(i + di, j + dj, k + dk, m)), ql[m], qr[m]);
+                eb_recon<float>(f, D, qf(i - 2 * di, j - 2 * dj, k - 2 * dk, m), qf(i - di, j - dj, k - dk, m),
+                                qf(i, j, k, m), qf(i + di, j + dj, k + dk, m), ql[m], qr[m]);
             vanleer<float>(P.f_smallp, P.f_gamma, ql, qr, D, ff);
 #pragma unroll
-            for (int m = 0; m < 5; ++m) flx[m] = f2d_bits(ff[m]);
+            for (int m = 0; m < 5; ++m) {
+                B.fluxf[D](i, j, k, m) = ff[m];
+                flx[m] = f2d_bits(ff[m]);
+            }
         } else {
             double ql[7], qr[7];
 #pragma unroll
@@ -263,9 +289,9 @@ __global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
                          q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
             vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
             if (A.visc) eb_visc_face(P, q, B.flag, D, i, j, k, A.dxinv, flx, 1, false, 0, 0, 0);
-        }
 #pragma unroll
-        for (int m = 0; m < 5; ++m) B.flux[D](i, j, k, m) = flx[m];
+            for (int m = 0; m < 5; ++m) B.flux[D](i, j, k, m) = flx[m];
+        }
         if (B.has_flux) {
             const double w = B.flux_w * *A.dt_ptr * B.ap[D](i, j, k);
             if (B.has_flux & FLUX_ACC_ALL) {
@@ -283,7 +309,19 @@ __global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
 }
 
 // cut-cell divergence of one cell (Source/EB/EBkernels.H:216-338, negated and
-// optionally rescaled as flux_redist, :341-377) + the Shu-Osher stage
+// optionally rescaled as flux_redist, :341-377) + the Shu-Osher stage.  F32: the
+// face fluxes and primitives come from the FP32 scratch (widened; the divergence,
+// wall flux and stage stay FP64)
+template <bool F32>
+__device__ __forceinline__ double eb_fx(const EbStageBox& B, int D, int i, int j, int k, int m) {
+    return F32 ? f2d_bits(B.fluxf[D](i, j, k, m)) : B.flux[D](i, j, k, m);
+}
+template <bool F32>
+__device__ __forceinline__ double eb_q(const EbStageBox& B, int i, int j, int k, int m) {
+    return F32 ? f2d_bits(B.qf(i, j, k, m)) : B.q(i, j, k, m);
+}
+
+template <bool F32>
 __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
     const double dt = *A.dt_ptr;
     double local_dt = __longlong_as_double(0x7FF0000000000000LL);
@@ -291,10 +329,10 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
          idx += (long long)gridDim.x * blockDim.x) {
         const int b = tag_of(A.cstart, A.cchunk, A.nbox, idx);
         const EbStageBox& B = A.boxes[b];
-        const long long loc = idx - A.cstart[b];
+        const int loc = (int)(idx - A.cstart[b]);
         const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1;
-        const int i = B.lo[0] + (int)(loc % nx), j = B.lo[1] + (int)((loc / nx) % ny),
-                  k = B.lo[2] + (int)(loc / ((long long)nx * ny));
+        const int r = loc / nx;
+        const int i = B.lo[0] + (loc - r * nx), j = B.lo[1] + r % ny, k = B.lo[2] + r / ny;
         double L[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         if (!B.covered) {
             const uint32_t f = B.flag(i, j, k);
@@ -306,9 +344,9 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
             } else if (eb_regular(f)) {
 #pragma unroll
                 for (int m = 0; m < 5; ++m)
-                    out[m] = A.dxinv[0] * (B.flux[0](i + 1, j, k, m) - B.flux[0](i, j, k, m)) +
-                             A.dxinv[1] * (B.flux[1](i, j + 1, k, m) - B.flux[1](i, j, k, m)) +
-                             A.dxinv[2] * (B.flux[2](i, j, k + 1, m) - B.flux[2](i, j, k, m));
+                    out[m] = A.dxinv[0] * (eb_fx<F32>(B, 0, i + 1, j, k, m) - eb_fx<F32>(B, 0, i, j, k, m)) +
+                             A.dxinv[1] * (eb_fx<F32>(B, 1, i, j + 1, k, m) - eb_fx<F32>(B, 1, i, j, k, m)) +
+                             A.dxinv[2] * (eb_fx<F32>(B, 2, i, j, k + 1, m) - eb_fx<F32>(B, 2, i, j, k, m));
             } else {
                 const double tmp = A.dxinv[0] / vf;
                 const double axm = B.ap[0](i, j, k), axp = B.ap[0](i + 1, j, k);
@@ -316,11 +354,11 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
                 const double azm = B.ap[2](i, j, k), azp = B.ap[2](i, j, k + 1);
 #pragma unroll
                 for (int m = 0; m < 5; ++m)
-                    out[m] = tmp * (axp * B.flux[0](i + 1, j, k, m) - axm * B.flux[0](i, j, k, m) +
-                                    ayp * B.flux[1](i, j + 1, k, m) - aym * B.flux[1](i, j, k, m) +
-                                    azp * B.flux[2](i, j, k + 1, m) - azm * B.flux[2](i, j, k, m));
+                    out[m] = tmp * (axp * eb_fx<F32>(B, 0, i + 1, j, k, m) - axm * eb_fx<F32>(B, 0, i, j, k, m) +
+                                    ayp * eb_fx<F32>(B, 1, i, j + 1, k, m) - aym * eb_fx<F32>(B, 1, i, j, k, m) +
+                                    azp * eb_fx<F32>(B, 2, i, j, k + 1, m) - azm * eb_fx<F32>(B, 2, i, j, k, m));
                 double fw[5];
-                const double pr = B.q(i, j, k, QPRES);
+                const double pr = eb_q<F32>(B, i, j, k, QPRES);
                 if (!A.visc) {
                     // slip-wall pressure flux, EBkernels.H:305-311
                     fw[0] = 0.0;
@@ -330,8 +368,9 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
                     fw[4] = 0.0;
                 } else {
                     // eb_wallflux, EBkernels.H:173-214
-                    const double d = B.q(i, j, k, QRHO), u = B.q(i, j, k, QU), v = B.q(i, j, k, QV),
-                                 w = B.q(i, j, k, QW), cs = B.q(i, j, k, QC);
+                    const double d = eb_q<F32>(B, i, j, k, QRHO), u = eb_q<F32>(B, i, j, k, QU),
+                                 v = eb_q<F32>(B, i, j, k, QV), w = eb_q<F32>(B, i, j, k, QW),
+                                 cs = eb_q<F32>(B, i, j, k, QC);
                     const double apnorm = sqrt((axm - axp) * (axm - axp) + (aym - ayp) * (aym - ayp) +
                                                (azm - azp) * (azm - azp));
                     const double un = u * (axm - axp) + v * (aym - ayp) + w * (azm - azp);
@@ -664,10 +703,14 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
             const long long gq = (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
             base.q = View<double>{E->d_scratch + E->q_off[e], n[0] + 4, (long long)(n[0] + 4) * (n[1] + 4), gq,
                                   B.lo[0] - 2, B.lo[1] - 2, B.lo[2] - 2};
+            base.qf = View<float>{reinterpret_cast<float*>(base.q.p), base.q.js, base.q.ks, base.q.ns,
+                                  base.q.b0, base.q.b1, base.q.b2};
             for (int d = 0; d < 3; ++d) {
                 const int sx = n[0] + (d == 0), sy = n[1] + (d == 1), sz = n[2] + (d == 2);
                 base.flux[d] = View<double>{E->d_scratch + E->f_off[d][e], sx, (long long)sx * sy,
                                             (long long)sx * sy * sz, B.lo[0], B.lo[1], B.lo[2]};
+                base.fluxf[d] = View<float>{reinterpret_cast<float*>(base.flux[d].p), base.flux[d].js,
+                                            base.flux[d].ks, base.flux[d].ns, B.lo[0], B.lo[1], B.lo[2]};
             }
         }
         if (!roles.flux_bits.empty() && roles.flux_bits[b] && cut) {
@@ -757,21 +800,29 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
             B.cstart = E->d_zero;
             B.ctotal = E->ccount[e];
             B.pchunk = B.fchunk = B.cchunk = nullptr;
-            if (B.ptotal > 0) k_ebl_prims<<<grid_for(B.ptotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+            if (B.ptotal > 0) {
+                if (f32) k_ebl_prims<true><<<grid_for(B.ptotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+                else k_ebl_prims<false><<<grid_for(B.ptotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+            }
             if (B.ftotal > 0) {
                 if (f32) k_ebl_faces<true><<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
                 else k_ebl_faces<false><<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
             }
-            k_ebl_div_stage<<<grid_for(B.ctotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+            if (f32) k_ebl_div_stage<true><<<grid_for(B.ctotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+            else k_ebl_div_stage<false><<<grid_for(B.ctotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
         }
         return check_launch("level cut-cell stage (per box)");
     }
-    if (A.ptotal > 0) k_ebl_prims<<<grid_for(A.ptotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+    if (A.ptotal > 0) {
+        if (f32) k_ebl_prims<true><<<grid_for(A.ptotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+        else k_ebl_prims<false><<<grid_for(A.ptotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+    }
     if (A.ftotal > 0) {
         if (f32) k_ebl_faces<true><<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
         else k_ebl_faces<false><<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
     }
-    k_ebl_div_stage<<<grid_for(A.ctotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+    if (f32) k_ebl_div_stage<true><<<grid_for(A.ctotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+    else k_ebl_div_stage<false><<<grid_for(A.ctotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
     return check_launch("level cut-cell stage");
 }
 
