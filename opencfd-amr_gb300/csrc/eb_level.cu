@@ -14,8 +14,9 @@
 //                     (zero in covered boxes), fused with the Shu-Osher stage
 //                     update and the CFL bound of the new state
 // In the mixed form (OCFD_FLUX_FP32, inviscid) the primitives (from the narrowed
-// state), the face states and the Van Leer flux are FP32 and kept in FP32
-// scratch; divergence, wall flux and RK stay FP64.
+// state), the face states, the Van Leer flux, the cut-cell divergence with the
+// slip-wall pressure flux and the CFL bound are FP32 (FP32 scratch); the RK
+// stage update stays FP64.
 // Work items of a batch are addressed through prefix sums over the boxes.
 //
 // Geometry.  AMReX EB2 (Source/Geometry.cpp:9-29) is absent.  For a body
@@ -209,6 +210,7 @@ struct EbStageArgs {
     const long long* cstart;  // valid cells of each box
     long long ctotal;
     double dxinv[3], dx[3];
+    float dxinv_f[3], dx_f[3];  // FP32 copies for the mixed form
     const double* dt_ptr;
     unsigned long long* cfl_min;
     int visc, redist;
@@ -334,7 +336,37 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
         const int r = loc / nx;
         const int i = B.lo[0] + (loc - r * nx), j = B.lo[1] + r % ny, k = B.lo[2] + r / ny;
         double L[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        if (!B.covered) {
+        if (F32 && !B.covered) {
+            // mixed form (inviscid): the divergence and the slip-wall pressure flux
+            // in FP32 from the FP32 face fluxes, widened once per component
+            const uint32_t f = B.flag(i, j, k);
+            float out[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            const float vf = d2f_bits(B.vfrac(i, j, k));
+            if (eb_regular(f)) {
+#pragma unroll
+                for (int m = 0; m < 5; ++m)
+                    out[m] = A.dxinv_f[0] * (B.fluxf[0](i + 1, j, k, m) - B.fluxf[0](i, j, k, m)) +
+                             A.dxinv_f[1] * (B.fluxf[1](i, j + 1, k, m) - B.fluxf[1](i, j, k, m)) +
+                             A.dxinv_f[2] * (B.fluxf[2](i, j, k + 1, m) - B.fluxf[2](i, j, k, m));
+            } else if (!eb_covered(f)) {
+                const float tmp = __fdividef(A.dxinv_f[0], vf);
+                const float axm = d2f_bits(B.ap[0](i, j, k)), axp = d2f_bits(B.ap[0](i + 1, j, k));
+                const float aym = d2f_bits(B.ap[1](i, j, k)), ayp = d2f_bits(B.ap[1](i, j + 1, k));
+                const float azm = d2f_bits(B.ap[2](i, j, k)), azp = d2f_bits(B.ap[2](i, j, k + 1));
+#pragma unroll
+                for (int m = 0; m < 5; ++m)
+                    out[m] = tmp * (axp * B.fluxf[0](i + 1, j, k, m) - axm * B.fluxf[0](i, j, k, m) +
+                                    ayp * B.fluxf[1](i, j + 1, k, m) - aym * B.fluxf[1](i, j, k, m) +
+                                    azp * B.fluxf[2](i, j, k + 1, m) - azm * B.fluxf[2](i, j, k, m));
+                const float pr = B.qf(i, j, k, QPRES);
+                out[1] += (axm - axp) * pr * tmp;
+                out[2] += (aym - ayp) * pr * tmp;
+                out[3] += (azm - azp) * pr * tmp;
+            }
+            const bool rescale = A.redist && vf < 0.5f && vf > 0.0f;
+#pragma unroll
+            for (int m = 0; m < 5; ++m) L[m] = f2d_bits(rescale ? -(vf * out[m]) : -out[m]);
+        } else if (!B.covered) {
             const uint32_t f = B.flag(i, j, k);
             const double vf = B.vfrac(i, j, k);
             double out[5];
@@ -410,7 +442,23 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
             B.Uout(i, j, k, n) = un[n];
         }
         if (A.cfl_min) {
-            const double v = cfl_bound(P, un, A.dx);
+            double v;
+            if (F32) {
+                // CFL bound of the new state in FP32 (as the mixed regular kernel)
+                const float g = P.f_gamma;
+                const float rho = d2f_bits(un[0]);
+                const float rhoinv = __frcp_rn(fmaxf(rho, P.f_smallr));
+                const float vx = d2f_bits(un[1]) * rhoinv, vy = d2f_bits(un[2]) * rhoinv, vz = d2f_bits(un[3]) * rhoinv;
+                const float p = fmaxf((g - 1.0f) * (d2f_bits(un[4]) - 0.5f * rho * (vx * vx + vy * vy + vz * vz)),
+                                      P.f_smallp);
+                const float cs = sqrtf(g * p * rhoinv);
+                const float dtx = __fdividef(A.dx_f[0], fabsf(vx) + cs);
+                const float dty = __fdividef(A.dx_f[1], fabsf(vy) + cs);
+                const float dtz = __fdividef(A.dx_f[2], fabsf(vz) + cs);
+                v = f2d_bits(fminf(dtx, fminf(dty, dtz)));
+            } else {
+                v = cfl_bound(P, un, A.dx);
+            }
             local_dt = v < local_dt ? v : local_dt;
         }
     }
@@ -779,6 +827,8 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
     for (int d = 0; d < 3; ++d) {
         A.dxinv[d] = 1.0 / L->desc.dx[d];
         A.dx[d] = L->desc.dx[d];
+        A.dxinv_f[d] = (float)A.dxinv[d];
+        A.dx_f[d] = (float)L->desc.dx[d];
     }
     A.dt_ptr = &L->d_step->dt;
     A.cfl_min = (s == 2 && E->cfl3) ? &L->d_step->cfl_min : nullptr;
