@@ -20,7 +20,12 @@ __device__ __forceinline__ float wenoz_side_f(float V1, float V2, float V3, floa
     float s33 = (13.0f / 12.0f) * (V3 - 2.0f * V4 + V5) * (V3 - 2.0f * V4 + V5) +
                 0.25f * (3.0f * V3 - 4.0f * V4 + V5) * (3.0f * V3 - 4.0f * V4 + V5);
     const float s55 = fabsf(s11 - s33);
-    const float r1 = __fdividef(s55, eps + s11), r2 = __fdividef(s55, eps + s22), r3 = __fdividef(s55, eps + s33);
+    // tau / (eps + beta), capped at 1e18: a stencil side that is exactly flat
+    // (beta = 0) next to a jump gives tau / eps, which for |V| above ~1e5 in
+    // normalised units of a small eps would overflow (1 + r^2) in FP32; at the cap
+    // that side's weight already dominates the others by > 1e30
+    const float r1 = fminf(__fdividef(s55, eps + s11), 1e18f), r2 = fminf(__fdividef(s55, eps + s22), 1e18f),
+                r3 = fminf(__fdividef(s55, eps + s33), 1e18f);
     const float a1 = 1.0f + r1 * r1, a2 = 6.0f * (1.0f + r2 * r2), a3 = 3.0f * (1.0f + r3 * r3);
     const float v1 = 2.0f * V1 - 7.0f * V2 + 11.0f * V3;
     const float v2 = -V2 + 5.0f * V3 + 2.0f * V4;

@@ -73,3 +73,35 @@ def test_jet_eb_steps_match_oracle(ctx, oracle):
         # bounded: the jet's density lies between 1.0 and 1.4, the bow shock
         # compresses it a few times, the wake expands it
         assert np.isfinite(g[:, m]).all() and 0.0 < g[0][m].min() and g[0][m].max() < 10.0
+
+
+def test_jet_eb_forms_and_schedules(ctx):
+    """On the cut hierarchy: the autotuned schedules give the same state as the
+    default ones bit for bit, the reference's per-box execution model too, and
+    the mixed form stays within 1e-6 L1 of the FP64 form in density and energy
+    after coarse steps on identical grids."""
+    import ocfd
+    from ocfd.level import eb_desc
+    case = small_jet()
+
+    def run(flags, tune=False, steps=3):
+        H = make_hierarchy(ctx, case, regrid_int=0)
+        H.set_eb(eb_desc(center=case["eb"]["center"], radius=case["eb"]["radius"],
+                         redistribute=case["eb"]["redistribute"]))
+        H.build(case["fab"])
+        if tune:
+            H.autotune(flags & ocfd.FLUX_FP32, reps=2)
+        H.advance(steps, 0.5, flags)
+        out = [H.level_global(l) for l in range(H.nlevels())]
+        H.close()
+        return out
+
+    base = run(0)
+    for other in (run(0, tune=True), run(ocfd.PER_BOX)):
+        for (a, m), (b, _) in zip(base, other):
+            assert np.array_equal(a[:, m], b[:, m])
+    mixed = run(ocfd.FLUX_FP32)
+    l1 = lambda x, y: float(np.abs(x - y).sum() / np.abs(y).sum())
+    for (a, m), (b, _) in zip(base, mixed):
+        assert not np.array_equal(a[:, m], b[:, m])
+        assert l1(b[0][m], a[0][m]) < 1e-6 and l1(b[4][m], a[4][m]) < 1e-6
