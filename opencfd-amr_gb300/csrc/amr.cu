@@ -269,12 +269,13 @@ __device__ __forceinline__ double mixed(const TimeMix& m, long long q) {
     return v;
 }
 
-__global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __restrict__ start, int ntag,
-                            long long total, const FabGeom* __restrict__ ffabs, double* dst,
-                            const FabGeom* __restrict__ cfabs, TimeMix mix, int ncomp) {
+__global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __restrict__ start,
+                            const int* __restrict__ chunk, int ntag, long long total,
+                            const FabGeom* __restrict__ ffabs, double* dst, const FabGeom* __restrict__ cfabs,
+                            TimeMix mix, int ncomp) {
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int t = find_tag<CfTag>(start, ntag, idx);
+        const int t = find_tag_chunked(start, chunk, ntag, idx);
         const CfTag& T = tags[t];
         int pi, pj, pk;
         region_cell(T.lo, T.hi, idx - start[t], pi, pj, pk);
@@ -520,20 +521,23 @@ template <class Tag>
 struct DevTags {
     Tag* d = nullptr;
     long long* start = nullptr;
+    int* chunk = nullptr;  // find_tag_chunked table
     int n = 0;
     long long total = 0;
     void release(DevPool* pool) {
         dev_free(d, pool);
         dev_free(start, pool);
+        dev_free(chunk, pool);
         d = nullptr;
         start = nullptr;
+        chunk = nullptr;
         n = 0;
         total = 0;
     }
     ocfd_status set(const std::vector<Tag>& v, DevPool* pool) {
         release(pool);
         n = (int)v.size();
-        return upload_tags(v, &d, &start, &total, pool);
+        return upload_tags(v, &d, &start, &total, pool, &chunk);
     }
 };
 
@@ -1071,7 +1075,7 @@ static ocfd_status launch_cf(ocfd_amr* H, int f, double* dst, const double* a, c
     m.zsign[0] = C.L->zsign[0];
     m.zsign[1] = C.L->zsign[1];
     k_cf_interp<<<grid_for(F.cf.total, 128, H->ctx->num_sms), 128, 0, st>>>(
-        F.cf.d, F.cf.start, F.cf.n, F.cf.total, F.L->d_fabs, dst, C.L->d_fabs, m, F.L->ncomp);
+        F.cf.d, F.cf.start, F.cf.chunk, F.cf.n, F.cf.total, F.L->d_fabs, dst, C.L->d_fabs, m, F.L->ncomp);
     ++launches_counter;
     return check_launch("AMR coarse-fine interpolation");
 }

@@ -31,11 +31,11 @@
 namespace ocfd {
 
 __global__ void k_exchange(const ExTag* __restrict__ tags, const long long* __restrict__ start,
-                           int ntag, long long total, const FabGeom* __restrict__ fabs, double* U,
-                           int ncomp) {
+                           const int* __restrict__ chunk, int ntag, long long total,
+                           const FabGeom* __restrict__ fabs, double* U, int ncomp) {
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int t = find_tag<ExTag>(start, ntag, idx);
+        const int t = find_tag_chunked(start, chunk, ntag, idx);
         const ExTag& T = tags[t];
         int i, j, k;
         region_cell(T.lo, T.hi, idx - start[t], i, j, k);
@@ -92,11 +92,12 @@ __device__ void jet_inflow(const BcInfo& bc, double* U, const FabGeom& f, long l
 
 template <int D>
 __global__ void k_physbc(const BcTag* __restrict__ tags, const long long* __restrict__ start,
-                         int ntag, long long total, const FabGeom* __restrict__ fabs, double* U,
-                         int ncomp, BcInfo bc, const StepState* st, double tfrac) {
+                         const int* __restrict__ chunk, int ntag, long long total,
+                         const FabGeom* __restrict__ fabs, double* U, int ncomp, BcInfo bc,
+                         const StepState* st, double tfrac) {
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        const int t = find_tag<BcTag>(start, ntag, idx);
+        const int t = find_tag_chunked(start, chunk, ntag, idx);
         const BcTag& T = tags[t];
         int c3[3];
         region_cell(T.lo, T.hi, idx - start[t], c3[0], c3[1], c3[2]);
@@ -288,7 +289,7 @@ static void build_physbc(ocfd_level* L, int d, std::vector<BcTag>& tags) {
 ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st) {
     if (L->ex_total > 0)
         k_exchange<<<grid_for(L->ex_total, 256, L->ctx->num_sms), 256, 0, st>>>(
-            L->d_ex, L->d_ex_start, L->nex, L->ex_total, L->d_fabs, U, L->ncomp);
+            L->d_ex, L->d_ex_start, L->d_ex_chunk, L->nex, L->ex_total, L->d_fabs, U, L->ncomp);
     return check_launch("level exchange");
 }
 
@@ -296,13 +297,16 @@ ocfd_status fill_physbc(ocfd_level* L, double* U, double tfrac, cudaStream_t st,
     const int sms = L->ctx->num_sms;
     if (L->bc_total[0] > 0)
         k_physbc<0><<<grid_for(L->bc_total[0], 256, sms), 256, 0, st>>>(
-            L->d_bc[0], L->d_bc_start[0], L->nbc[0], L->bc_total[0], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
+            L->d_bc[0], L->d_bc_start[0], L->d_bc_chunk[0], L->nbc[0], L->bc_total[0], L->d_fabs, U, L->ncomp,
+            L->bcinfo, L->d_step, tfrac);
     if (L->bc_total[1] > 0)
         k_physbc<1><<<grid_for(L->bc_total[1], 256, sms), 256, 0, st>>>(
-            L->d_bc[1], L->d_bc_start[1], L->nbc[1], L->bc_total[1], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
+            L->d_bc[1], L->d_bc_start[1], L->d_bc_chunk[1], L->nbc[1], L->bc_total[1], L->d_fabs, U, L->ncomp,
+            L->bcinfo, L->d_step, tfrac);
     if (L->bc_total[2] > 0 && (all || !L->zvirt))
         k_physbc<2><<<grid_for(L->bc_total[2], 256, sms), 256, 0, st>>>(
-            L->d_bc[2], L->d_bc_start[2], L->nbc[2], L->bc_total[2], L->d_fabs, U, L->ncomp, L->bcinfo, L->d_step, tfrac);
+            L->d_bc[2], L->d_bc_start[2], L->d_bc_chunk[2], L->nbc[2], L->bc_total[2], L->d_fabs, U, L->ncomp,
+            L->bcinfo, L->d_step, tfrac);
     return check_launch("level physical BC");
 }
 
@@ -557,12 +561,12 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
     std::vector<ExTag> ex;
     build_exchange(L, ex);
     L->nex = (int)ex.size();
-    if (s == OCFD_OK) s = upload_tags(ex, &L->d_ex, &L->d_ex_start, &L->ex_total, pool);
+    if (s == OCFD_OK) s = upload_tags(ex, &L->d_ex, &L->d_ex_start, &L->ex_total, pool, &L->d_ex_chunk);
     for (int d = 0; d < 3 && s == OCFD_OK; ++d) {
         std::vector<BcTag> bt;
         build_physbc(L, d, bt);
         L->nbc[d] = (int)bt.size();
-        s = upload_tags(bt, &L->d_bc[d], &L->d_bc_start[d], &L->bc_total[d], pool);
+        s = upload_tags(bt, &L->d_bc[d], &L->d_bc_start[d], &L->bc_total[d], pool, &L->d_bc_chunk[d]);
     }
     for (int d = 0; d < 3; ++d) {
         L->bcinfo.lo_bc[d] = desc->lo_bc[d];
@@ -652,11 +656,13 @@ ocfd_status ocfd_level_destroy(ocfd_level* L) {
         dev_free(L->d_stage[i], pool);
         dev_free(L->d_bc[i], pool);
         dev_free(L->d_bc_start[i], pool);
+        dev_free(L->d_bc_chunk[i], pool);
     }
     dev_free(L->d_fabs, pool);
     dev_free(L->d_cell_start, pool);
     dev_free(L->d_ex, pool);
     dev_free(L->d_ex_start, pool);
+    dev_free(L->d_ex_chunk, pool);
     dev_free(L->d_tile_start, pool);
     dev_free(L->d_step, pool);
     dev_free(L->d_queue, pool);

@@ -67,6 +67,16 @@ __device__ __forceinline__ int find_tag(const long long* start, int ntag, long l
     return lo;
 }
 
+// The same through a chunk table: chunk[c] = the tag holding item c << TAG_CHUNK_LOG2,
+// then a short forward scan (nullptr: the binary search)
+constexpr int TAG_CHUNK_LOG2 = 7;
+__device__ __forceinline__ int find_tag_chunked(const long long* start, const int* chunk, int ntag, long long idx) {
+    if (!chunk) return find_tag<int>(start, ntag, idx);
+    int t = chunk[idx >> TAG_CHUNK_LOG2];
+    while (t + 1 < ntag && start[t + 1] <= idx) ++t;
+    return t;
+}
+
 __device__ __forceinline__ void region_cell(const int* lo, const int* hi, long long local, int& i,
                                             int& j, int& k) {
     const long long nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
@@ -156,7 +166,7 @@ int grid_for(long long total, int threads, int sms);
 
 template <class Tag>
 ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** d_start, long long* total,
-                        DevPool* pool = nullptr) {
+                        DevPool* pool = nullptr, int** d_chunk = nullptr) {
     std::vector<long long> start(tags.size());
     long long acc = 0;
     for (size_t i = 0; i < tags.size(); ++i) {
@@ -166,7 +176,17 @@ ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** 
     *total = acc;
     ocfd_status s = upload(d_tags, tags, pool);
     if (s != OCFD_OK) return s;
-    return upload(d_start, start, pool);
+    s = upload(d_start, start, pool);
+    if (s != OCFD_OK || !d_chunk) return s;
+    // chunk table of find_tag_chunked
+    std::vector<int> chunk((size_t)((acc >> TAG_CHUNK_LOG2) + 1), 0);
+    int t = 0;
+    for (size_t c = 0; c < chunk.size(); ++c) {
+        const long long idx = (long long)c << TAG_CHUNK_LOG2;
+        while (t + 1 < (int)start.size() && start[t + 1] <= idx) ++t;
+        chunk[c] = t;
+    }
+    return upload(d_chunk, chunk, pool);
 }
 
 struct EbLevel;
@@ -191,11 +211,13 @@ struct ocfd_level {
     // exchange
     ocfd::ExTag* d_ex = nullptr;
     long long* d_ex_start = nullptr;
+    int* d_ex_chunk = nullptr;
     int nex = 0;
     long long ex_total = 0;
     // physical BC passes
     ocfd::BcTag* d_bc[3] = {nullptr, nullptr, nullptr};
     long long* d_bc_start[3] = {nullptr, nullptr, nullptr};
+    int* d_bc_chunk[3] = {nullptr, nullptr, nullptr};
     int nbc[3] = {0, 0, 0};
     long long bc_total[3] = {0, 0, 0};
     ocfd::BcInfo bcinfo{};
