@@ -271,16 +271,33 @@ __global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
         const uint32_t f = B.flag(i, j, k);
         double flx[5];
         if (F32) {
+            // eb_recon with the connectivity tests and the addressing hoisted out of
+            // the component loop: one base pointer, the stride along D, the
+            // component stride
             const View<float>& qf = B.qf;
+            const float* p0 = &qf(i, j, k, 0);
+            const long long sd = D == 0 ? 1 : (D == 1 ? qf.js : qf.ks), ns = qf.ns;
+            const bool cm1 = eb_conn(f, -di, -dj, -dk), cm2 = eb_conn(f, -2 * di, -2 * dj, -2 * dk),
+                       cp1 = eb_conn(f, di, dj, dk);
             float ql[7], qr[7], ff[5];
 #pragma unroll
-            for (int m = 0; m < 7; ++m)
-                eb_recon<float>(f, D, qf(i - 2 * di, j - 2 * dj, k - 2 * dk, m), qf(i - di, j - dj, k - dk, m),
-                                qf(i, j, k, m), qf(i + di, j + dj, k + dk, m), ql[m], qr[m]);
+            for (int m = 0; m < 7; ++m) {
+                const float* pm = p0 + m * ns;
+                const float vm2 = pm[-2 * sd], vm1 = pm[-sd], v0 = pm[0], vp1 = pm[sd];
+                float l = vm1, r = v0;
+                if (cm1) {
+                    if (cm2) l = vm1 + 0.5f * minmod<float>(v0 - vm1, vm1 - vm2);
+                    if (cp1) r = v0 - 0.5f * minmod<float>(vp1 - v0, v0 - vm1);
+                }
+                ql[m] = l;
+                qr[m] = r;
+            }
             vanleer<float>(P.f_smallp, P.f_gamma, ql, qr, D, ff);
+            float* fo = &B.fluxf[D](i, j, k, 0);
+            const long long fns = B.fluxf[D].ns;
 #pragma unroll
             for (int m = 0; m < 5; ++m) {
-                B.fluxf[D](i, j, k, m) = ff[m];
+                fo[m * fns] = ff[m];
                 flx[m] = f2d_bits(ff[m]);
             }
         } else {
@@ -342,12 +359,18 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
             const uint32_t f = B.flag(i, j, k);
             float out[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
             const float vf = d2f_bits(B.vfrac(i, j, k));
+            // face-flux base pointers of the cell and the strides to its high faces
+            const float* fx0 = &B.fluxf[0](i, j, k, 0);
+            const float* fy0 = &B.fluxf[1](i, j, k, 0);
+            const float* fz0 = &B.fluxf[2](i, j, k, 0);
+            const long long nsx = B.fluxf[0].ns, nsy = B.fluxf[1].ns, nsz = B.fluxf[2].ns;
+            const long long sy = B.fluxf[1].js, sz = B.fluxf[2].ks;
             if (eb_regular(f)) {
 #pragma unroll
                 for (int m = 0; m < 5; ++m)
-                    out[m] = A.dxinv_f[0] * (B.fluxf[0](i + 1, j, k, m) - B.fluxf[0](i, j, k, m)) +
-                             A.dxinv_f[1] * (B.fluxf[1](i, j + 1, k, m) - B.fluxf[1](i, j, k, m)) +
-                             A.dxinv_f[2] * (B.fluxf[2](i, j, k + 1, m) - B.fluxf[2](i, j, k, m));
+                    out[m] = A.dxinv_f[0] * (fx0[m * nsx + 1] - fx0[m * nsx]) +
+                             A.dxinv_f[1] * (fy0[m * nsy + sy] - fy0[m * nsy]) +
+                             A.dxinv_f[2] * (fz0[m * nsz + sz] - fz0[m * nsz]);
             } else if (!eb_covered(f)) {
                 const float tmp = __fdividef(A.dxinv_f[0], vf);
                 const float axm = d2f_bits(B.ap[0](i, j, k)), axp = d2f_bits(B.ap[0](i + 1, j, k));
@@ -355,9 +378,8 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
                 const float azm = d2f_bits(B.ap[2](i, j, k)), azp = d2f_bits(B.ap[2](i, j, k + 1));
 #pragma unroll
                 for (int m = 0; m < 5; ++m)
-                    out[m] = tmp * (axp * B.fluxf[0](i + 1, j, k, m) - axm * B.fluxf[0](i, j, k, m) +
-                                    ayp * B.fluxf[1](i, j + 1, k, m) - aym * B.fluxf[1](i, j, k, m) +
-                                    azp * B.fluxf[2](i, j, k + 1, m) - azm * B.fluxf[2](i, j, k, m));
+                    out[m] = tmp * (axp * fx0[m * nsx + 1] - axm * fx0[m * nsx] + ayp * fy0[m * nsy + sy] -
+                                    aym * fy0[m * nsy] + azp * fz0[m * nsz + sz] - azm * fz0[m * nsz]);
                 const float pr = B.qf(i, j, k, QPRES);
                 out[1] += (axm - axp) * pr * tmp;
                 out[2] += (aym - ayp) * pr * tmp;
