@@ -353,7 +353,8 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
         const int r = loc / nx;
         const int i = B.lo[0] + (loc - r * nx), j = B.lo[1] + r % ny, k = B.lo[2] + r / ny;
         double L[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        if (F32 && !B.covered) {
+        if (F32) {
+          if (!B.covered) {
             // mixed form (inviscid): the divergence and the slip-wall pressure flux
             // in FP32 from the FP32 face fluxes, widened once per component
             const uint32_t f = B.flag(i, j, k);
@@ -388,6 +389,7 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
             const bool rescale = A.redist && vf < 0.5f && vf > 0.0f;
 #pragma unroll
             for (int m = 0; m < 5; ++m) L[m] = f2d_bits(rescale ? -(vf * out[m]) : -out[m]);
+          }
         } else if (!B.covered) {
             const uint32_t f = B.flag(i, j, k);
             const double vf = B.vfrac(i, j, k);
