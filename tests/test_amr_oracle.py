@@ -168,3 +168,52 @@ def test_regrid_tags_and_nests(oracle):
             for d in range(3):
                 ext = hi[d] - lo[d] + 1
                 assert ext <= 16 and lo[d] % min(8, A.n(l + 1)[d]) == 0
+
+
+def test_cut_cell_operators_with_the_body(oracle):
+    """The restatement with an embedded cylinder (the checker of the GPU's cut
+    hierarchy), on its own: box classes follow the geometry, the
+    volume-fraction average-down of a uniform fine level is that uniform state
+    (and the plain average where nothing is cut), and two coarse steps of the
+    jet past the cylinder stay finite with positive density and energy."""
+    from amr_oracle import BOX_CUT, BOX_REGULAR
+    from ocfd.cases import jet_eb_amr
+
+    case = jet_eb_amr(nx=64, ny=32, nz=4, max_level=2, blocking_factor=8, max_grid=16, n_error_buf=1,
+                      refine_dengrad=0.1, regrid_int=2)
+    boxes0 = chop(case["n"], 16)
+    A = AmrOracle(oracle, case["n"], case["dx"], case["lo_bc"], case["hi_bc"], boxes0, case["prob_lo"],
+                  case["bc_case"], case["case_params"], case["max_level"], case["blocking_factor"],
+                  case["max_grid_size"], case["n_error_buf"], case["refine_dengrad"], eb=case["eb"])
+    A.set_level_fabs(0, case["fab"])
+    for lev in range(A.max_level):
+        if len(A.levels) != lev + 1:
+            break
+        A.regrid(lev)
+        if len(A.levels) == lev + 2:
+            A.set_level_fabs(lev + 1, case["fab"])
+    A.average_down_all()
+    assert len(A.levels) == 3
+    cls0 = A.classes(0)
+    assert BOX_CUT in cls0 and BOX_REGULAR in cls0
+    # boxes far from the cylinder (more than 4 + 1 cells) are regular
+    c = np.array(case["eb"]["center"]) / case["dx"][0]
+    r = case["eb"]["radius"] / case["dx"][0]
+    for cl, (lo, hi) in zip(cls0, A.levels[0]["boxes"]):
+        near = [max(lo[d] - 5 - c[d], c[d] - (hi[d] + 6), 0.0) for d in (0, 1)]
+        if np.hypot(*near) > r:
+            assert cl == BOX_REGULAR
+    # average-down of a uniform fine state is that state wherever a child is fluid
+    F = A.levels[1]
+    keep = F["U"].copy()
+    F["U"][:] = 3.25
+    D = A.levels[0]["U"].copy()
+    A._avg_down(0, D)
+    cov = A._covered(0)
+    assert np.allclose(D[:, NG:-NG, NG:-NG, NG:-NG][:, cov], 3.25, rtol=1e-15)
+    F["U"][:] = keep
+    for _ in range(2):
+        A.step(0.5)
+    for l in range(len(A.levels)):
+        V, m = A.valid(l)
+        assert np.isfinite(V[:, m]).all() and V[0][m].min() > 0 and V[4][m].min() > 0

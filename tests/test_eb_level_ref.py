@@ -42,3 +42,23 @@ def test_no_body_equals_the_oracle_driver(oracle):
     t2, _ = oracle.advance_rk3(ref.make_bc(case), S, 0.5, 3, form=1)
     assert t == t2
     assert np.array_equal(got, S[:, NG:-NG, NG:-NG, NG:-NG])
+
+
+def test_fixture_geometry_measures_the_cylinder():
+    """The sub-sampled geometry (the fixture the device geometry must equal):
+    the covered area is the disc's area to the sampling resolution, the area
+    fractions of the faces crossing the circle lie strictly between 0 and 1,
+    and a cell is regular exactly when its volume fraction and its four face
+    fractions are 1."""
+    from ocfd import geometry
+    n, dx, r = (48, 48, 1), (1 / 48,) * 3, 0.3
+    g = geometry.box_geometry(geometry.cylinder_phi(0.5, 0.5, r), (0, 0, 0), n, dx, nsub=16)
+    vf = g["vfrac"][0, NG, NG:-NG, NG:-NG]
+    covered_area = float((1.0 - vf).sum()) * dx[0] * dx[1]
+    assert abs(covered_area - np.pi * r * r) < 2e-3
+    apx = g["apx"][0, 0]
+    assert ((apx > 0) & (apx < 1)).any()
+    typ = g["flag"][0, NG, NG:-NG, NG:-NG] & 3
+    full = (vf == 1.0) & (apx[:, :-1] == 1.0) & (apx[:, 1:] == 1.0) & \
+        (g["apy"][0, 0][:-1, :] == 1.0) & (g["apy"][0, 0][1:, :] == 1.0)
+    assert np.array_equal(typ == 0, full)
