@@ -573,6 +573,7 @@ static void rect_dist2(double cx, double cy, double x0, double x1, double y0, do
 
 ocfd_status eb_setup(ocfd_level* L, const ocfd_eb_desc& eb) {
     eb_free(L);
+    L->zvirt = L->zvirt_allowed;
     if (eb.kind == OCFD_EB_NONE) return OCFD_OK;
     if (eb.kind != OCFD_EB_CYLINDER_Z) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: unknown body kind");
     if (!(eb.radius > 0) || eb.nsub < 0 || eb.nsub > 256) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: radius / nsub");
@@ -706,7 +707,7 @@ ocfd_status eb_setup(ocfd_level* L, const ocfd_eb_desc& eb) {
         if (!E->d_scratch) return fail(OCFD_OUT_OF_MEMORY, "ocfd_level_set_eb: scratch");
     }
     // the cut-cell stencils read z ghost cells from the state: fill them
-    if (any_cut) L->zvirt = false;
+    L->zvirt = L->zvirt_allowed && !any_cut;
     return OCFD_OK;
 }
 

@@ -589,6 +589,7 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
             L->zsign[sd] = zb[sd] == 5 ? 7 : (zb[sd] >= 3 ? 4 : 0);
         }
         L->zvirt = simple;
+        L->zvirt_allowed = simple;
     }
     std::memcpy(L->bcinfo.params, desc->case_params, sizeof(L->bcinfo.params));
     // RHS tile: the shape with the least padded work summed over the boxes

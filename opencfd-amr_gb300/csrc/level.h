@@ -240,6 +240,7 @@ struct ocfd_level {
     // z faces with source-cell BCs on both sides: stepping leaves their outside
     // ghosts unfilled and the stencils map the loads (RegBoxArgs::zvirt)
     bool zvirt = false;
+    bool zvirt_allowed = false;  // the BCs allow it (the cut-cell stencils do not)
     int zmirror[2] = {0, 0}, zsign[2] = {0, 0};
     // device memory source: nullptr = cudaMalloc / cudaFree (standalone level),
     // else the owning hierarchy's pool (state buffers are then not zeroed)
