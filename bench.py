@@ -322,8 +322,9 @@ def jet_workload():
 
 
 def run_ours_jet(args, world, rank, local):
-    """configs[3]: the multi-level EB jet.  Forms timed from the same developed
-    state: the batched graph (one launch per level per RK stage for the regular
+    """The multi-level embedded-boundary workload (Mach 2 jet past a cylinder).
+    Forms timed from the same developed state: the batched graph (one launch
+    per level per RK stage for the regular
     boxes + three for the cut / covered boxes, autotuned tile shape and
     schedule) in FP32-flux and FP64, and the reference's execution model in
     FP64 (per-box launches issued from the host, no graph)."""
@@ -733,7 +734,7 @@ def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, sa
 
 
 def run_ours_react(args, world, rank, local):
-    """configs[2]: 128^3 periodic H2/air with 8 hot spots, Strang chemistry around
+    """The reacting workload: 128^3 periodic H2/air with 8 hot spots, Strang chemistry around
     the RK2 multispecies flow step, dt = 1e-8 s."""
     import numpy as np
     import torch

@@ -207,7 +207,7 @@ def hot_spot_temperature(n=128, length=0.01, seed=20261203, nspots=8, t0=1200.0,
 
 
 def react_cube(ctx, n=128, length=0.01, seed=20261203, p=101325.0):
-    """configs[2]: premixed phi = 1 H2/air at 1 atm, 1200 K with 8 seeded hot
+    """The reacting workload: premixed phi = 1 H2/air at 1 atm, 1200 K with 8 seeded hot
     spots, periodic cube of n^3 cells and edge `length`; the grown global state
     (14, n+8, n+8, n+8): conserved variables then partial densities."""
     from .react import state_tpx
