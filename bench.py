@@ -1,7 +1,7 @@
 """Benchmark: cell-steps/s of the OpenCFD-AMR RHS + RK3 update path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config dmr-amr|sod|dmr|cube] [--form fp32|fp64]
+                    [--config dmr-amr|jet-eb-amr|react|sod|dmr|cube] [--form fp32|fp64]
 
 Default workload (dmr-amr): double Mach reflection on a 1024x256x2 base grid
 with two refined levels (ratio 2, |d rho| >= 0.05 tagging, regrid every 2 coarse
@@ -22,6 +22,13 @@ e2e    = the same through the C ABI from pinned host buffers: every step uploads
          every level's state, advances, downloads every level's state
 --impl reference times the reference algorithm on the host CPU cores (the
          oracle port, OpenMP, all threads): RK3 steps of the base grid.
+jet-eb-amr: Mach 2 planar jet past a z-cylinder in 2x1x1, base 256x128x128 +
+         2 levels (~800 boxes of 8^3-32^3), the cut boxes in the cut-cell
+         scheme; timed in the batched graph (FP32 headline and FP64, each
+         autotuned) and in per-box launches from the host (FP64).
+react:   the 128^3 H2/air box with 8 hot spots (9 species, implicit chemistry,
+         mixture-averaged transport); plain FP64, binned FP64 and the mixed form
+         (headline), then the MLP surrogate trained inside the run.
 The single-level configs (sod, dmr, cube) time one level of boxes.
 Multi-GPU: independent replicas (the workload does not shard over GPUs here);
 value is summed over ranks with the max time.
