@@ -42,6 +42,24 @@ ocfd_status mech_upload(const ocfd_parm& p) {
         cudaError_t e = cudaGetLastError();
         return fail(OCFD_LAUNCH_FAIL, std::string("mechanism upload: ") + cudaGetErrorString(e));
     }
+    MechDerived md{};
+    for (int h = 0; h < 2; ++h)
+        for (int n = 0; n < NSP; ++n) {
+            const double* a = h ? t.hi[n] : t.lo[n];
+            md.q3[h][n] = a[2] / 3.0;
+            md.q5[h][n] = a[4] / 5.0;
+            md.g6[h][n] = a[2] / 6.0;
+            md.g12[h][n] = a[3] / 12.0;
+            md.g20[h][n] = a[4] / 20.0;
+        }
+    for (int a = 0; a < NSP; ++a) {
+        md.inv_mw[a] = 1.0 / t.mw[a];
+        for (int b = 0; b < NSP; ++b) md.wratio[a][b] = t.mw[a] / t.mw[b];
+    }
+    if (cudaMemcpyToSymbol(c_mder, &md, sizeof(md)) != cudaSuccess) {
+        cudaError_t e = cudaGetLastError();
+        return fail(OCFD_LAUNCH_FAIL, std::string("mechanism upload: ") + cudaGetErrorString(e));
+    }
     TransF tf{};
     for (int i = 0; i < NSP * 5; ++i) {
         tf.visc[i] = (float)t.visc[i];
@@ -76,7 +94,7 @@ __device__ __forceinline__ void chem_cell(const double* u, double& E, double* r,
     double cc[NSP], wdot[NSP], drho[NSP];
     const double T = get_t_given_ey(ei, r, P.Ru);
 #pragma unroll
-    for (int n = 0; n < NSP; n++) cc[n] = r[n] / c_mech.mw[n] * 1e-6;
+    for (int n = 0; n < NSP; n++) cc[n] = r[n] * c_mder.inv_mw[n] * 1e-6;
     for (int a = 0; a < NSP; ++a)
         for (int b = 0; b < NSP; ++b) U(a, b) = 0.0;
     production_rate(wdot, U, cc, T, P.Ru, P.Patm);
@@ -84,7 +102,7 @@ __device__ __forceinline__ void chem_cell(const double* u, double& E, double* r,
         for (int b = 0; b < NSP; ++b) {
             const double ar = U(a, b);
             double v = (a == b ? 1.0 : 0.0);
-            v -= ar * c_mech.mw[a] / c_mech.mw[b] * dt;
+            v -= ar * c_mder.wratio[a][b] * dt;
             U(a, b) = v;
         }
         U(a, NSP) = wdot[a] * c_mech.mw[a] * 1e6 * dt;
@@ -98,7 +116,7 @@ __device__ __forceinline__ void chem_cell(const double* u, double& E, double* r,
         r[n] = v;
     }
 #pragma unroll
-    for (int n = 0; n < NSP; ++n) dei += -c_mech.HP[n] * P.Ru / c_mech.mw[n] * drho[n];
+    for (int n = 0; n < NSP; ++n) dei += -c_mech.HP[n] * P.Ru * c_mder.inv_mw[n] * drho[n];
     E += dei;
 }
 

@@ -13,6 +13,21 @@ namespace ocfd {
 
 __constant__ MechTables c_mech;
 
+// Quantities derived from the tables once on the host, so that the per-cell
+// routines divide less (GB300's FP64 pipe runs a division as ~10 instructions):
+//   q3, q5   a2 / 3, a4 / 5 of the internal energy and enthalpy polynomials, and
+//   g6, g12, g20   a2 / 6, a3 / 12, a4 / 20 of the Gibbs polynomial - the same
+//            quotients the expressions form first, so these are bit-identical;
+//   inv_mw   1 / W_n and wratio[a][b] = W_a / W_b, which replace divisions by W
+//            (a rounding of the last bit differs from dividing).
+struct MechDerived {
+    double q3[2][NSP], q5[2][NSP];
+    double g6[2][NSP], g12[2][NSP], g20[2][NSP];
+    double inv_mw[NSP];
+    double wratio[NSP][NSP];
+};
+__constant__ MechDerived c_mder;
+
 // NASA-7 coefficient row of species n for temperature T
 __device__ __forceinline__ const double* nasa(double T, int n) {
     return T < 1000 ? c_mech.lo[n] : c_mech.hi[n];
@@ -26,11 +41,12 @@ __device__ __forceinline__ void species_internal_energy(double* e, const double*
     for (int n = 0; n < NSP; ++n) {
         if (T < 1000) {
             const double* a = c_mech.lo[n];
-            e[n] = a[0] - 1.0 + a[1] / 2.0 * tc[1] + a[2] / 3.0 * tc[2] + a[3] / 4.0 * tc[3] + a[4] / 5.0 * tc[4];
+            e[n] = a[0] - 1.0 + a[1] / 2.0 * tc[1] + c_mder.q3[0][n] * tc[2] + a[3] / 4.0 * tc[3] +
+                   c_mder.q5[0][n] * tc[4];
         } else {
             const double* a = c_mech.hi[n];
-            e[n] = a[0] - 1.0 + a[1] / 2.0 * tc[1] + a[2] / 3.0 * tc[2] + a[3] / 4.0 * tc[3] + a[4] / 5.0 * tc[4] +
-                   (a[5] - c_mech.lo[n][5]) * invT;
+            e[n] = a[0] - 1.0 + a[1] / 2.0 * tc[1] + c_mder.q3[1][n] * tc[2] + a[3] / 4.0 * tc[3] +
+                   c_mder.q5[1][n] * tc[4] + (a[5] - c_mech.lo[n][5]) * invT;
         }
     }
 }
@@ -42,11 +58,12 @@ __device__ __forceinline__ void species_enthalpy(double T, double* h) {
     for (int n = 0; n < NSP; ++n) {
         if (T < 1000) {
             const double* a = c_mech.lo[n];
-            h[n] = a[0] * tc[0] + a[1] / 2.0 * tc[1] + a[2] / 3.0 * tc[2] + a[3] / 4.0 * tc[3] + a[4] / 5.0 * tc[4];
+            h[n] = a[0] * tc[0] + a[1] / 2.0 * tc[1] + c_mder.q3[0][n] * tc[2] + a[3] / 4.0 * tc[3] +
+                   c_mder.q5[0][n] * tc[4];
         } else {
             const double* a = c_mech.hi[n];
-            h[n] = a[0] * tc[0] + a[1] / 2.0 * tc[1] + a[2] / 3.0 * tc[2] + a[3] / 4.0 * tc[3] + a[4] / 5.0 * tc[4] +
-                   (a[5] - c_mech.lo[n][5]);
+            h[n] = a[0] * tc[0] + a[1] / 2.0 * tc[1] + c_mder.q3[1][n] * tc[2] + a[3] / 4.0 * tc[3] +
+                   c_mder.q5[1][n] * tc[4] + (a[5] - c_mech.lo[n][5]);
         }
     }
 }
@@ -59,7 +76,7 @@ __device__ __forceinline__ double ckubms(double T, const double* rhoi, double Ru
     const double RT = Ru * T;
     species_internal_energy(ums, tc);
 #pragma unroll
-    for (int n = 0; n < NSP; ++n) result += rhoi[n] * ums[n] / c_mech.mw[n];
+    for (int n = 0; n < NSP; ++n) result += rhoi[n] * ums[n] * c_mder.inv_mw[n];
     return result * RT;
 }
 
@@ -71,7 +88,7 @@ __device__ __forceinline__ double ckcvbs(double T, const double* rhoi, double Ru
     for (int n = 0; n < NSP; ++n) {
         const double* a = nasa(T, n);
         const double cpor = a[0] + a[1] * tc[1] + a[2] * tc[2] + a[3] * tc[3] + a[4] * tc[4];
-        result += (cpor - 1.0) * rhoi[n] / c_mech.mw[n];
+        result += (cpor - 1.0) * rhoi[n] * c_mder.inv_mw[n];
     }
     return result * Ru;
 }
@@ -80,7 +97,7 @@ __device__ __forceinline__ double ckcvbs(double T, const double* rhoi, double Ru
 __device__ __forceinline__ double ckpy(const double* rhoi, double T, double Ru) {
     double YOW = 0;
 #pragma unroll
-    for (int i = 0; i < NSP; ++i) YOW += rhoi[i] / c_mech.mw[i];
+    for (int i = 0; i < NSP; ++i) YOW += rhoi[i] * c_mder.inv_mw[i];
     return Ru * T * YOW;
 }
 
@@ -106,7 +123,7 @@ __device__ __forceinline__ double get_t_given_ey(double e, const double* rhoi, d
     if (ein > emax) return tmax - (emax - ein) / ckcvbs(tmax, rhoi, Ru);
     double As = 0;
 #pragma unroll
-    for (int n = 0; n < NSP; ++n) As += c_mech.A0[n] * Ru / c_mech.mw[n] * rhoi[n];
+    for (int n = 0; n < NSP; ++n) As += c_mech.A0[n] * Ru * c_mder.inv_mw[n] * rhoi[n];
     double t1 = e / As;
     if (t1 < tmin || t1 > tmax) t1 = tmin + (tmax - tmin) / (emax - emin) * (ein - emin);
     for (int i = 0; i < maxiter; ++i) {
@@ -171,10 +188,12 @@ __device__ __forceinline__ void production_rate(double* wdot, Mat& A, const doub
 #pragma unroll
     for (int n = 0; n < NSP; ++n) {
         const double* a = nasa(T, n);
-        gi[n] = a[0] * (1.0 - tc[0]) - a[1] / 2.0 * tc[1] - a[2] / 6.0 * tc[2] - a[3] / 12.0 * tc[3] -
-                a[4] / 20.0 * tc[4] + a[5] * invT - a[6];
+        const int h = T < 1000 ? 0 : 1;
+        gi[n] = a[0] * (1.0 - tc[0]) - a[1] / 2.0 * tc[1] - c_mder.g6[h][n] * tc[2] - c_mder.g12[h][n] * tc[3] -
+                c_mder.g20[h][n] * tc[4] + a[5] * invT - a[6];
     }
     const double RsT = Ru / Patm * 1e6 * T;
+    const double iRsT = 1.0 / RsT;
     double mixture = 0.0;
 #pragma unroll
     for (int n = 0; n < NSP; ++n) {
@@ -186,54 +205,54 @@ __device__ __forceinline__ void production_rate(double* wdot, Mat& A, const doub
 #define KF(A_, b_, Ta_) ((A_) * exp((b_) * tc[0] - (Ta_) * invT))
 #define ST(s0, s1, s2, s3, f0, f1, f2, f3, r0, r1, r2, r3) \
     Stoich { {s0, s1, s2, s3}, {f0, f1, f2, f3}, {r0, r1, r2, r3} }
-    double wf, wr, kf, Kc;
+    double wf, wr, kf, iKc;  // the inverse equilibrium constant: kf * iKc is the reverse rate constant
     // 0: H + O2 <=> O + OH
     kf = KF(3.55e+15, -0.41, 8353.444256079512);
-    Kc = exp((gi[3] + gi[1]) - (gi[4] + gi[5]));
+    iKc = exp((gi[4] + gi[5]) - (gi[3] + gi[1]));
     wf = sc[3] * sc[1] * kf;
-    wr = sc[4] * sc[5] * (kf / Kc);
+    wr = sc[4] * sc[5] * (kf * iKc);
     rxn_accum(ST(3, 1, 4, 5, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 1: O + H2 <=> H + OH
     kf = KF(50800.0, 2.67, 3165.2508657072367);
-    Kc = exp((gi[4] + gi[0]) - (gi[3] + gi[5]));
+    iKc = exp((gi[3] + gi[5]) - (gi[4] + gi[0]));
     wf = sc[4] * sc[0] * kf;
-    wr = sc[3] * sc[5] * (kf / Kc);
+    wr = sc[3] * sc[5] * (kf * iKc);
     rxn_accum(ST(4, 0, 3, 5, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 2: H2 + OH <=> H2O + H
     kf = KF(2.16e+08, 1.51, 1726.0429999007667);
-    Kc = exp((gi[0] + gi[5]) - (gi[2] + gi[3]));
+    iKc = exp((gi[2] + gi[3]) - (gi[0] + gi[5]));
     wf = sc[0] * sc[5] * kf;
-    wr = sc[2] * sc[3] * (kf / Kc);
+    wr = sc[2] * sc[3] * (kf * iKc);
     rxn_accum(ST(0, 5, 2, 3, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 3: O + H2O <=> OH + OH
     kf = KF(2.97e+06, 2.02, 6743.141748883461);
-    Kc = exp((gi[4] + gi[2]) - (gi[5] + gi[5]));
+    iKc = exp((gi[5] + gi[5]) - (gi[4] + gi[2]));
     wf = sc[4] * sc[2] * kf;
-    wr = sc[5] * sc[5] * (kf / Kc);
+    wr = sc[5] * sc[5] * (kf * iKc);
     rxn_accum(ST(4, 2, 5, -1, 1, 1, 0, 0, 0, 0, 2, 0), wf, wr, sc, wdot, A);
     // 4: H2 + M <=> H + H + M
     kf = alpha_a * KF(4.58e+19, -1.4, 52526.05490660117);
-    Kc = 1.0 / RsT * exp((gi[0]) - (gi[3] + gi[3]));
+    iKc = RsT * exp((gi[3] + gi[3]) - (gi[0]));
     wf = sc[0] * kf;
-    wr = sc[3] * sc[3] * (kf / Kc);
+    wr = sc[3] * sc[3] * (kf * iKc);
     rxn_accum(ST(0, 3, -1, -1, 1, 0, 0, 0, 0, 2, 0, 0), wf, wr, sc, wdot, A);
     // 5: O + O + M <=> O2 + M
     kf = alpha_a * KF(6.16e+15, -0.5, 0.0);
-    Kc = RsT * exp((gi[4] + gi[4]) - (gi[1]));
+    iKc = iRsT * exp((gi[1]) - (gi[4] + gi[4]));
     wf = sc[4] * sc[4] * kf;
-    wr = sc[1] * (kf / Kc);
+    wr = sc[1] * (kf * iKc);
     rxn_accum(ST(4, 1, -1, -1, 2, 0, 0, 0, 0, 1, 0, 0), wf, wr, sc, wdot, A);
     // 6: O + H + M <=> OH + M
     kf = alpha_a * KF(4.71e+18, -1.0, 0.0);
-    Kc = RsT * exp((gi[4] + gi[3]) - (gi[5]));
+    iKc = iRsT * exp((gi[5]) - (gi[4] + gi[3]));
     wf = sc[4] * sc[3] * kf;
-    wr = sc[5] * (kf / Kc);
+    wr = sc[5] * (kf * iKc);
     rxn_accum(ST(4, 3, 5, -1, 1, 1, 0, 0, 0, 0, 1, 0), wf, wr, sc, wdot, A);
     // 7: H + OH + M <=> H2O + M
     kf = alpha_a * KF(3.8e+22, -2.0, 0.0);
-    Kc = RsT * exp((gi[3] + gi[5]) - (gi[2]));
+    iKc = iRsT * exp((gi[2]) - (gi[3] + gi[5]));
     wf = sc[3] * sc[5] * kf;
-    wr = sc[2] * (kf / Kc);
+    wr = sc[2] * (kf * iKc);
     rxn_accum(ST(3, 5, 2, -1, 1, 1, 0, 0, 0, 0, 1, 0), wf, wr, sc, wdot, A);
     // 8: H + O2 (+M) <=> HO2 (+M), Troe falloff, Fcent = 0.8
     {
@@ -248,44 +267,44 @@ __device__ __forceinline__ void production_rate(double* wdot, Mat& A, const doub
         const double F_troe = pow(10.0, logFcent / (1.0 + troe * troe));
         kf *= (redP / (1.0 + redP)) * F_troe;
     }
-    Kc = RsT * exp((gi[3] + gi[1]) - (gi[6]));
+    iKc = iRsT * exp((gi[6]) - (gi[3] + gi[1]));
     wf = sc[3] * sc[1] * kf;
-    wr = sc[6] * (kf / Kc);
+    wr = sc[6] * (kf * iKc);
     rxn_accum(ST(3, 1, 6, -1, 1, 1, 0, 0, 0, 0, 1, 0), wf, wr, sc, wdot, A);
     // 9: HO2 + H <=> H2 + O2
     kf = KF(1.66e+13, 0.0, 412.64001746898793);
-    Kc = exp((gi[6] + gi[3]) - (gi[0] + gi[1]));
+    iKc = exp((gi[0] + gi[1]) - (gi[6] + gi[3]));
     wf = sc[6] * sc[3] * kf;
-    wr = sc[0] * sc[1] * (kf / Kc);
+    wr = sc[0] * sc[1] * (kf * iKc);
     rxn_accum(ST(6, 3, 0, 1, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 10: HO2 + H <=> OH + OH
     kf = KF(7.08e+13, 0.0, 150.96586004962973);
-    Kc = exp((gi[6] + gi[3]) - (gi[5] + gi[5]));
+    iKc = exp((gi[5] + gi[5]) - (gi[6] + gi[3]));
     wf = sc[6] * sc[3] * kf;
-    wr = sc[5] * sc[5] * (kf / Kc);
+    wr = sc[5] * sc[5] * (kf * iKc);
     rxn_accum(ST(6, 3, 5, -1, 1, 1, 0, 0, 0, 0, 2, 0), wf, wr, sc, wdot, A);
     // 11: HO2 + O <=> O2 + OH
     kf = KF(3.25e+13, 0.0, 0.0);
-    Kc = exp((gi[6] + gi[4]) - (gi[1] + gi[5]));
+    iKc = exp((gi[1] + gi[5]) - (gi[6] + gi[4]));
     wf = sc[6] * sc[4] * kf;
-    wr = sc[1] * sc[5] * (kf / Kc);
+    wr = sc[1] * sc[5] * (kf * iKc);
     rxn_accum(ST(6, 4, 1, 5, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 12: HO2 + OH <=> H2O + O2
     kf = KF(2.89e+13, 0.0, -251.60976674938289);
-    Kc = exp((gi[6] + gi[5]) - (gi[2] + gi[1]));
+    iKc = exp((gi[2] + gi[1]) - (gi[6] + gi[5]));
     wf = sc[6] * sc[5] * kf;
-    wr = sc[2] * sc[1] * (kf / Kc);
+    wr = sc[2] * sc[1] * (kf * iKc);
     rxn_accum(ST(6, 5, 2, 1, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 13: HO2 + HO2 <=> H2O2 + O2 (two rate expressions, DUPLICATE)
     {
         const double kf1 = KF(4.2e+14, 0.0, 6028.570011315214);
         const double kf2 = KF(1.3e+11, 0.0, -820.2478396029883);
-        Kc = exp((gi[6] + gi[6]) - (gi[7] + gi[1]));
+        iKc = exp((gi[7] + gi[1]) - (gi[6] + gi[6]));
         const double phi_f = sc[6] * sc[6], phi_r = sc[7] * sc[1];
         wf = phi_f * kf1;
-        wr = phi_r * (kf1 / Kc);
+        wr = phi_r * (kf1 * iKc);
         wf += phi_f * kf2;
-        wr += phi_r * (kf2 / Kc);
+        wr += phi_r * (kf2 * iKc);
         rxn_accum(ST(6, 7, 1, -1, 2, 0, 0, 0, 0, 1, 1, 0), wf, wr, sc, wdot, A);
     }
     // 14: H2O2 (+M) <=> OH + OH (+M), Troe falloff, Fcent = 0.5
@@ -300,38 +319,38 @@ __device__ __forceinline__ void production_rate(double* wdot, Mat& A, const doub
         const double F_troe = pow(10.0, logFcent / (1.0 + troe * troe));
         kf *= (redP / (1.0 + redP)) * F_troe;
     }
-    Kc = 1.0 / RsT * exp((gi[7]) - (gi[5] + gi[5]));
+    iKc = RsT * exp((gi[5] + gi[5]) - (gi[7]));
     wf = sc[7] * kf;
-    wr = sc[5] * sc[5] * (kf / Kc);
+    wr = sc[5] * sc[5] * (kf * iKc);
     rxn_accum(ST(7, 5, -1, -1, 1, 0, 0, 0, 0, 2, 0, 0), wf, wr, sc, wdot, A);
     // 15: H2O2 + H <=> H2O + OH
     kf = KF(2.41e+13, 0.0, 1997.7815479901);
-    Kc = exp((gi[7] + gi[3]) - (gi[2] + gi[5]));
+    iKc = exp((gi[2] + gi[5]) - (gi[7] + gi[3]));
     wf = sc[7] * sc[3] * kf;
-    wr = sc[2] * sc[5] * (kf / Kc);
+    wr = sc[2] * sc[5] * (kf * iKc);
     rxn_accum(ST(7, 3, 2, 5, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 16: H2O2 + H <=> HO2 + H2
     kf = KF(4.82e+13, 0.0, 4000.595291315188);
-    Kc = exp((gi[7] + gi[3]) - (gi[6] + gi[0]));
+    iKc = exp((gi[6] + gi[0]) - (gi[7] + gi[3]));
     wf = sc[7] * sc[3] * kf;
-    wr = sc[6] * sc[0] * (kf / Kc);
+    wr = sc[6] * sc[0] * (kf * iKc);
     rxn_accum(ST(7, 3, 6, 0, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 17: H2O2 + O <=> OH + HO2
     kf = KF(9.55e+06, 2.0, 1997.7815479901);
-    Kc = exp((gi[7] + gi[4]) - (gi[5] + gi[6]));
+    iKc = exp((gi[5] + gi[6]) - (gi[7] + gi[4]));
     wf = sc[7] * sc[4] * kf;
-    wr = sc[5] * sc[6] * (kf / Kc);
+    wr = sc[5] * sc[6] * (kf * iKc);
     rxn_accum(ST(7, 4, 5, 6, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     // 18: H2O2 + OH <=> HO2 + H2O (two rate expressions, DUPLICATE)
     {
         const double kf1 = KF(1.0e+12, 0.0, 0.0);
         const double kf2 = KF(5.8e+14, 0.0, 4810.778740248201);
-        Kc = exp((gi[7] + gi[5]) - (gi[6] + gi[2]));
+        iKc = exp((gi[6] + gi[2]) - (gi[7] + gi[5]));
         const double phi_f = sc[7] * sc[5], phi_r = sc[6] * sc[2];
         wf = phi_f * kf1;
-        wr = phi_r * (kf1 / Kc);
+        wr = phi_r * (kf1 * iKc);
         wf += phi_f * kf2;
-        wr += phi_r * (kf2 / Kc);
+        wr += phi_r * (kf2 * iKc);
         rxn_accum(ST(7, 5, 6, 2, 1, 1, 0, 0, 0, 0, 1, 1), wf, wr, sc, wdot, A);
     }
 #undef KF
@@ -358,8 +377,10 @@ __device__ __forceinline__ void gauss_solve(Mat& U, double* x) {
                 U(pv, i) = U(k, i);
                 U(k, i) = t;
             }
+        // one reciprocal of the pivot instead of a division per row
+        const double ipiv = 1.0 / U(k, k);
         for (int i = k + 1; i < NSP; i++) {
-            const double m = U(i, k) / U(k, k);
+            const double m = U(i, k) * ipiv;
             for (int j = k; j < NSP + 1; j++) U(i, j) -= m * U(k, j);
         }
     }
