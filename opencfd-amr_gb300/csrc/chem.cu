@@ -55,6 +55,16 @@ ocfd_status mech_upload(const ocfd_parm& p) {
     for (int a = 0; a < NSP; ++a) {
         md.inv_mw[a] = 1.0 / t.mw[a];
         for (int b = 0; b < NSP; ++b) md.wratio[a][b] = t.mw[a] / t.mw[b];
+        // speciesInternalEnergy (LiDryer.H:531-614) at 250 K (low range) and 3500 K (high range)
+        auto ums = [&](double T, int hi) {
+            const double* c = hi ? t.hi[a] : t.lo[a];
+            double u = c[0] - 1.0 + c[1] / 2.0 * T + c[2] / 3.0 * T * T + c[3] / 4.0 * T * T * T +
+                       c[4] / 5.0 * T * T * T * T;
+            if (hi) u += (c[5] - t.lo[a][5]) / T;
+            return u;
+        };
+        md.umin_w[a] = ums(250.0, 0) * md.inv_mw[a];
+        md.umax_w[a] = ums(3500.0, 1) * md.inv_mw[a];
     }
     if (cudaMemcpyToSymbol(c_mder, &md, sizeof(md)) != cudaSuccess) {
         cudaError_t e = cudaGetLastError();

@@ -25,6 +25,9 @@ struct MechDerived {
     double g6[2][NSP], g12[2][NSP], g20[2][NSP];
     double inv_mw[NSP];
     double wratio[NSP][NSP];
+    // e_n(T)/(R T W_n) at the bounds 250 K and 3500 K of the temperature
+    // inversion (the mixture energies there are then 9 products)
+    double umin_w[NSP], umax_w[NSP];
 };
 __constant__ MechDerived c_mder;
 
@@ -118,7 +121,13 @@ __device__ __forceinline__ double get_t_given_ey(double e, const double* rhoi, d
     const int maxiter = 200;
     const double tol = 1e-7;
     const double ein = e, tmin = 250, tmax = 3500;
-    const double emin = ckubms(tmin, rhoi, Ru), emax = ckubms(tmax, rhoi, Ru);
+    double smin = 0, smax = 0;
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) {
+        smin += rhoi[n] * c_mder.umin_w[n];
+        smax += rhoi[n] * c_mder.umax_w[n];
+    }
+    const double emin = smin * (Ru * tmin), emax = smax * (Ru * tmax);
     if (ein < emin) return tmin - (emin - ein) / ckcvbs(tmin, rhoi, Ru);
     if (ein > emax) return tmax - (emax - ein) / ckcvbs(tmax, rhoi, Ru);
     double As = 0;
