@@ -663,6 +663,7 @@ static ocfd_status make_level(ocfd_amr* H, int l, const std::vector<IBox>& boxes
     ocfd_status s = level_alloc(H->ctx, &d, nbuf, out, &H->pool);
     if (s == OCFD_OK) (*out)->sched = H->tuned_sched[l];
     if (s == OCFD_OK && H->has_eb) s = eb_setup(*out, H->eb);
+    if (s == OCFD_OK && H->has_eb) s = rebuild_fill_tags(*out);
     return s;
 }
 
@@ -747,7 +748,7 @@ static void ghost_regions(const ocfd_amr* H, int f, std::vector<std::vector<IBox
     periodic_shifts(H, fdom, shifts);
     regions.assign(F.boxes.size(), {});
     for (size_t b = 0; b < F.boxes.size(); ++b) {
-        IBox R = ib_grow(F.boxes[b], NFILL);
+        IBox R = ib_grow(F.boxes[b], box_nfill(F.L, (int)b));
         for (int e = 0; e < 3; ++e)
             if (!H->periodic[e]) {
                 R.lo[e] = std::max(R.lo[e], fdom.lo[e]);
@@ -1559,6 +1560,7 @@ ocfd_status ocfd_amr_set_eb(ocfd_amr* H, const ocfd_eb_desc* eb) {
     H->eb = *eb;
     for (int l = 0; l < H->nlev; ++l) {
         ocfd_status s = eb_setup(H->lev[l].L, *eb);
+        if (s == OCFD_OK) s = rebuild_fill_tags(H->lev[l].L);
         if (s != OCFD_OK) return s;
     }
     ocfd_status s = rebuild_tables(H);

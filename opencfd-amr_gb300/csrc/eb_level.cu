@@ -921,7 +921,9 @@ extern "C" {
 ocfd_status ocfd_level_set_eb(ocfd_level* L, const ocfd_eb_desc* eb) {
     if (!L || !eb) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: null argument");
     if (L->ncomp != 5) return fail(OCFD_BAD_ARG, "ocfd_level_set_eb: the cut-cell level path is the ideal-gas one");
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_level_set_eb");
     ocfd_status s = eb_setup(L, *eb);
+    if (s == OCFD_OK) s = rebuild_fill_tags(L);
     if (s == OCFD_OK) s = build_stage_tables(L, StageRoles{});
     if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = fail(OCFD_LAUNCH_FAIL, "ocfd_level_set_eb");
     if (L->graph) {

@@ -212,7 +212,8 @@ static void build_exchange(ocfd_level* L, std::vector<ExTag>& tags) {
     for (int b = 0; b < nb; ++b) {
         const ocfd_box& B = L->boxes[b];
         int glo[3], ghi[3];
-        for (int d = 0; d < 3; ++d) { glo[d] = B.lo[d] - NFILL; ghi[d] = B.hi[d] + NFILL; }
+        const int nf = box_nfill(L, b);
+        for (int d = 0; d < 3; ++d) { glo[d] = B.lo[d] - nf; ghi[d] = B.hi[d] + nf; }
         for (int sx = -1; sx <= 1; ++sx)
             for (int sy = -1; sy <= 1; ++sy)
                 for (int sz = -1; sz <= 1; ++sz) {
@@ -270,8 +271,8 @@ static void build_physbc(ocfd_level* L, int d, std::vector<BcTag>& tags) {
             t.box = b;
             t.side = side;
             for (int e = 0; e < 3; ++e) {
-                t.lo[e] = B.lo[e] - NFILL;
-                t.hi[e] = B.hi[e] + NFILL;
+                t.lo[e] = B.lo[e] - box_nfill(L, b);
+                t.hi[e] = B.hi[e] + box_nfill(L, b);
                 if (e > d && L->desc.lo_bc[e] != OCFD_BC_INTERIOR) {
                     t.lo[e] = std::max(t.lo[e], dom.lo[e]);
                     t.hi[e] = std::min(t.hi[e], dom.hi[e]);
@@ -284,6 +285,38 @@ static void build_physbc(ocfd_level* L, int d, std::vector<BcTag>& tags) {
             if (!empty) tags.push_back(t);
         }
     }
+}
+
+int box_nfill(const ocfd_level* L, int b) {
+    const int c = eb_box_class(L, b);
+    return c == OCFD_BOX_REGULAR ? NFILL : (c == OCFD_BOX_CUT ? 2 : 1);
+}
+
+ocfd_status rebuild_fill_tags(ocfd_level* L) {
+    DevPool* pool = L->pool;
+    dev_free(L->d_ex, pool);
+    dev_free(L->d_ex_start, pool);
+    dev_free(L->d_ex_chunk, pool);
+    L->d_ex = nullptr;
+    L->d_ex_start = nullptr;
+    L->d_ex_chunk = nullptr;
+    std::vector<ExTag> ex;
+    build_exchange(L, ex);
+    L->nex = (int)ex.size();
+    ocfd_status s = upload_tags(ex, &L->d_ex, &L->d_ex_start, &L->ex_total, pool, &L->d_ex_chunk);
+    for (int d = 0; d < 3 && s == OCFD_OK; ++d) {
+        dev_free(L->d_bc[d], pool);
+        dev_free(L->d_bc_start[d], pool);
+        dev_free(L->d_bc_chunk[d], pool);
+        L->d_bc[d] = nullptr;
+        L->d_bc_start[d] = nullptr;
+        L->d_bc_chunk[d] = nullptr;
+        std::vector<BcTag> bt;
+        build_physbc(L, d, bt);
+        L->nbc[d] = (int)bt.size();
+        s = upload_tags(bt, &L->d_bc[d], &L->d_bc_start[d], &L->bc_total[d], pool, &L->d_bc_chunk[d]);
+    }
+    return s;
 }
 
 ocfd_status fill_exchange(ocfd_level* L, double* U, cudaStream_t st) {

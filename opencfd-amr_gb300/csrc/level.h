@@ -267,6 +267,12 @@ struct StageRoles {
 };
 
 ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles);
+// Ghost layers box b needs filled: NFILL for a regular box (WENO-Z +-3), 2 for a
+// cut box (its primitives span grow(bx, 2)), 1 for a covered box (tagging and
+// the coarse-fine slopes read +-1 around valid cells)
+int box_nfill(const ocfd_level* L, int b);
+// rebuild the exchange and physical-BC tables (after the box classes changed)
+ocfd_status rebuild_fill_tags(ocfd_level* L);
 // time every tile shape x schedule of the level's batched stage kernel, keep the
 // fastest (stage tables rebuilt with the level's last roles); synchronous
 ocfd_status level_autotune(ocfd_level* L, unsigned flags, int reps, cudaStream_t st);
