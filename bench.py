@@ -55,6 +55,39 @@ CFL = 0.5
 T_DEV = 0.05
 L1_STEPS = 20
 
+# DRAM traffic of each workload's roofline kernel, per cell of one launch:
+# (dram__bytes_read.sum + dram__bytes_write.sum) of a launch captured by ncu on the
+# same workload and form, divided by the cells that launch processed.  The
+# captures and their commands are summarised in profiles/.
+NCU_DRAM_BYTES_PER_CELL = {
+    # k_rhs_regular<float, 8, 8, 8>, DMR finest level: 310.9 MB over 2,048,000 cells
+    ("dmr-amr", "fp32"): 310.9e6 / 2048000,
+    # the jet's finest-level stage (k_rhs_regular + the cut-cell batch's three
+    # kernels): 2094.2 MB over 4,980,736 cells
+    ("jet-eb-amr", "fp32"): 2094.2e6 / 4980736,
+    # k_rhs_regular<float, 8, 8, 8>, 3D blast 256x256x64: 566.6 MB over 4,194,304 cells
+    ("cube", "fp32"): 566.6e6 / 4194304,
+    # k_chem_advance_list, 128^3 reacting box: 309 + 126 MB over 2,097,152 cells
+    ("react", "chem"): (309e6 + 126e6) / 2097152,
+}
+
+
+def ncu_traffic(workload, form, cells):
+    b = NCU_DRAM_BYTES_PER_CELL.get((workload, form))
+    return None if b is None else b * cells
+
+
+def roofline_stage_ms(level, flags, reps=10):
+    """Device ms of one RK-stage launch of `level` (CUDA events on its stream),
+    inside the NVTX range bench_roofline_stage that an ncu capture of the roofline
+    kernel filters on."""
+    import torch
+    torch.cuda.nvtx.range_push("bench_roofline_stage")
+    try:
+        return level.profile_stage(flags, reps=reps)
+    finally:
+        torch.cuda.nvtx.range_pop()
+
 
 def amr_workload():
     from ocfd import cases
@@ -401,7 +434,7 @@ def run_ours_jet(args, world, rank, local):
               for l in range(H.nlevels())]
     nbox = sum(x["boxes"] for x in levels)
     fin = H.level(H.nlevels() - 1)
-    stage_ms = fin.profile_stage(ocfd.FLUX_FP32, reps=10)
+    stage_ms = roofline_stage_ms(fin, ocfd.FLUX_FP32)
     fcells = fin.cells()
     hbm_peak, peak_src = peaks()
     achieved = 120.0 * fcells / (stage_ms * 1e-3) / 1e9
@@ -466,7 +499,8 @@ def run_ours_jet(args, world, rank, local):
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "frac": achieved / hbm_peak, "peak_source": peak_src,
+                         "traffic": ncu_traffic("jet-eb-amr", "fp32", fcells),
                          "kernel": "k_rhs_regular fused RK stage (FP32 flux), finest level (%d cells)" % fcells,
                          "ms_per_launch": stage_ms, "alg_bytes_per_cell": 120,
                          "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},
@@ -537,7 +571,7 @@ def run_ours_amr(args, world, rank, local):
 
     # dominant kernel, timed live: the fused RK-stage kernel on the finest level
     fin = H.level(H.nlevels() - 1)
-    stage_ms = fin.profile_stage(flags, reps=10)
+    stage_ms = roofline_stage_ms(fin, flags)
     fcells = fin.cells()
     alg_bytes = 120.0 * fcells
     hbm_peak, peak_src = peaks()
@@ -605,7 +639,8 @@ def run_ours_amr(args, world, rank, local):
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "frac": achieved / hbm_peak, "peak_source": peak_src,
+                         "traffic": ncu_traffic("dmr-amr", args.form, fcells),
                          "kernel": "k_rhs_regular fused RK stage, finest level (%d cells)" % fcells,
                          "ms_per_launch": stage_ms, "alg_bytes_per_cell": 120,
                          "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},
@@ -863,7 +898,8 @@ def run_ours_react(args, world, rank, local):
                        "rk3_vs_rk2_l1": rk3_vs_rk2, "surrogate": sur_rep, "boxes": len(boxes), "cells": cells,
                        "l2": "flushed between timed steps (512 MB write, untimed)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "frac": achieved / hbm_peak, "peak_source": peak_src,
+                         "traffic": ncu_traffic("react", "chem", cells),
                          "kernel": "k_chem_advance_list (one chemistry substep)", "ms_per_launch": chem_ms,
                          "alg_bytes_per_cell": 192, "fp64_fma_peak_gflops": fp64.value},
             "cpu_baseline": cpu,
@@ -923,7 +959,7 @@ def run_ours(args, world, rank, local):
     value_other = cells * args.steps * world / (ms_other * 1e-3)
 
     # dominant kernel, timed live: the fused RK-stage kernel (stage 2)
-    stage_ms = lev.profile_stage(flags, reps=10)
+    stage_ms = roofline_stage_ms(lev, flags)
     alg_bytes = 120.0 * cells          # read U_s and U_0, write U_out (5 doubles each)
     hbm_peak, peak_src = peaks()
     achieved = alg_bytes / (stage_ms * 1e-3) / 1e9
@@ -973,7 +1009,8 @@ def run_ours(args, world, rank, local):
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                         "frac": achieved / hbm_peak, "peak_source": peak_src,
+                         "traffic": ncu_traffic(args.config, args.form, cells),
                          "kernel": "k_rhs_regular fused RK stage", "ms_per_launch": stage_ms,
                          "alg_bytes_per_cell": 120,
                          "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},

@@ -260,7 +260,7 @@ typedef struct ocfd_level ocfd_level;
 
 typedef struct ocfd_level_desc {
     int32_t nbox;
-    const ocfd_box* boxes;   /* valid boxes, disjoint */
+    const ocfd_box* boxes;   /* valid boxes: disjoint, inside the domain (else OCFD_BAD_ARG) */
     ocfd_box domain;         /* problem domain in cell indices of this level */
     int32_t lo_bc[3];        /* ebr.lo_bc codes, OCFD_BC_* (0 = periodic) */
     int32_t hi_bc[3];

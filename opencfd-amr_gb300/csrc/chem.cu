@@ -764,8 +764,8 @@ __device__ __forceinline__ void chem_conv_f32(const ChemBoxArgs& B, int i, int j
     }
 #pragma unroll
     for (int n = 0; n < 5; ++n)
-        f[n] = f2d_bits(wenoz_norm_f(fp[0][n], fp[1][n], fp[2][n], fp[3][n], fp[4][n]) +
-                        wenoz_norm_f(fm[5][n], fm[4][n], fm[3][n], fm[2][n], fm[1][n]));
+        f[n] = f2d_bits(wenoz_pm_f(fp[0][n], fp[1][n], fp[2][n], fp[3][n], fp[4][n], fm[5][n], fm[4][n],
+                                   fm[3][n], fm[2][n], fm[1][n]));
 #pragma unroll
     for (int n = 0; n < NSP; ++n) {
         float a[6], b[6];
@@ -775,7 +775,7 @@ __device__ __forceinline__ void chem_conv_f32(const ChemBoxArgs& B, int i, int j
             a[s] = tmp0 * tp[s];
             b[s] = tmp0 * tm[s];
         }
-        fs[n] = f2d_bits(wenoz_norm_f(a[0], a[1], a[2], a[3], a[4]) + wenoz_norm_f(b[5], b[4], b[3], b[2], b[1]));
+        fs[n] = f2d_bits(wenoz_pm_f(a[0], a[1], a[2], a[3], a[4], b[5], b[4], b[3], b[2], b[1]));
     }
 }
 

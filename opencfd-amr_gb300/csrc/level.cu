@@ -538,6 +538,24 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     return s;
 }
 
+// The boxes of one level are disjoint (an AMReX BoxArray of a level): sweep
+// over the boxes in order of lo.x, testing each against those that start
+// before it ends in x.
+static bool boxes_disjoint(const std::vector<ocfd_box>& b) {
+    std::vector<int> ord(b.size());
+    for (size_t i = 0; i < b.size(); ++i) ord[i] = (int)i;
+    std::sort(ord.begin(), ord.end(), [&](int u, int v) { return b[u].lo[0] < b[v].lo[0]; });
+    for (size_t a = 0; a < ord.size(); ++a) {
+        const ocfd_box& A = b[ord[a]];
+        for (size_t c = a + 1; c < ord.size() && b[ord[c]].lo[0] <= A.hi[0]; ++c) {
+            const ocfd_box& C = b[ord[c]];
+            if (C.lo[1] <= A.hi[1] && A.lo[1] <= C.hi[1] && C.lo[2] <= A.hi[2] && A.lo[2] <= C.hi[2])
+                return false;
+        }
+    }
+    return true;
+}
+
 // Everything of a level but its stage tables: FABs, state buffers, exchange and
 // physical-BC tags, RHS tile choice, step state.
 ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
@@ -579,6 +597,10 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
         cell_start.push_back(L->ncells);
         L->ncells += region_cells(f.lo, f.hi);
         L->fabs.push_back(f);
+    }
+    if (!boxes_disjoint(L->boxes)) {
+        delete L;
+        return fail(OCFD_BAD_ARG, "ocfd_level_create: boxes overlap");
     }
     L->elems = off;
     for (int i = 0; i < nbuf; ++i) {

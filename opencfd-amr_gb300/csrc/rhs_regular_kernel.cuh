@@ -120,8 +120,7 @@ struct Prec<float> {
                            P.f_sw_gm1, fp, fm);
     }
     static __device__ __forceinline__ float weno(const float* a, const float* b, int s) {
-        return wenoz_norm_f(a[0], a[s], a[2 * s], a[3 * s], a[4 * s]) +
-               wenoz_norm_f(b[5 * s], b[4 * s], b[3 * s], b[2 * s], b[s]);
+        return wenoz_pm_f(a[0], a[s], a[2 * s], a[3 * s], a[4 * s], b[5 * s], b[4 * s], b[3 * s], b[2 * s], b[s]);
     }
     static __device__ __forceinline__ float mu(const DevParm& P, float T) {
         return P.f_C_s * T * sqrtf(T) / (T + P.f_T_s);

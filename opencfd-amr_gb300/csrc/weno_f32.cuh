@@ -13,38 +13,79 @@ namespace ocfd {
 // local state as eps / s^2 in the normalised units.  The scheme is therefore
 // the FP64 scheme up to FP32 rounding, and no smoothness indicator can overflow
 // whatever the magnitude of the flux.
-__device__ __forceinline__ float wenoz_side_f(float V1, float V2, float V3, float V4, float V5, float eps) {
-    float s11 = (13.0f / 12.0f) * (V1 - 2.0f * V2 + V3) * (V1 - 2.0f * V2 + V3) +
-                0.25f * (V1 - 4.0f * V2 + 3.0f * V3) * (V1 - 4.0f * V2 + 3.0f * V3);
-    float s22 = (13.0f / 12.0f) * (V2 - 2.0f * V3 + V4) * (V2 - 2.0f * V3 + V4) + 0.25f * (V2 - V4) * (V2 - V4);
-    float s33 = (13.0f / 12.0f) * (V3 - 2.0f * V4 + V5) * (V3 - 2.0f * V4 + V5) +
-                0.25f * (3.0f * V3 - 4.0f * V4 + V5) * (3.0f * V3 - 4.0f * V4 + V5);
-    const float s55 = fabsf(s11 - s33);
-    // tau / (eps + beta), capped at 1e18: a stencil side that is exactly flat
-    // (beta = 0) next to a jump gives tau / eps, which for |V| above ~1e5 in
-    // normalised units of a small eps would overflow (1 + r^2) in FP32; at the cap
-    // that side's weight already dominates the others by > 1e30
-    const float r1 = fminf(__fdividef(s55, eps + s11), 1e18f), r2 = fminf(__fdividef(s55, eps + s22), 1e18f),
-                r3 = fminf(__fdividef(s55, eps + s33), 1e18f);
-    const float a1 = 1.0f + r1 * r1, a2 = 6.0f * (1.0f + r2 * r2), a3 = 3.0f * (1.0f + r3 * r3);
-    const float v1 = 2.0f * V1 - 7.0f * V2 + 11.0f * V3;
-    const float v2 = -V2 + 5.0f * V3 + 2.0f * V4;
-    const float v3 = 2.0f * V3 + 5.0f * V4 - V5;
-    return __fdividef(a1 * v1 + a2 * v2 + a3 * v3, 6.0f * (a1 + a2 + a3));
-}
+//
+// A face flux is the f+ reconstruction plus the f- one, two independent
+// evaluations of the same expressions: they run as the two lanes of float2
+// values, so that every add / multiply / FMA of the scheme is one packed FP32
+// instruction (sm_100 and later) for both sides.  Only the normalisation, the
+// reciprocals and the ratio cap are per lane.
 
-// f+ at cells i-3..i+1, or f- at i+2..i-2 (the mirrored stencil): normalise,
-// reconstruct, scale back
-__device__ __forceinline__ float wenoz_norm_f(float V1, float V2, float V3, float V4, float V5) {
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 p_set(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 p_rcp(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
+
+// Normalisation of one side's stencil: scale sc, its inverse and the epsilon in
+// normalised units.  Zero / subnormal stencils, and inf / NaN, are reconstructed
+// as they are (sc = 1, epsilon 1e-6).
+__device__ __forceinline__ void wenoz_scale(float V1, float V2, float V3, float V4, float V5, float& sc,
+                                            float& inv, float& eps) {
     const float m = fmaxf(fmaxf(fmaxf(fabsf(V1), fabsf(V2)), fmaxf(fabsf(V3), fabsf(V4))), fabsf(V5));
     const int ex = (__float_as_int(m) >> 23) & 0xff;
-    // zero / subnormal stencils, and inf / NaN, are reconstructed as they are
-    if (ex == 0 || ex > 250) return wenoz_side_f(V1, V2, V3, V4, V5, 1e-6f);
-    const float sc = __int_as_float((254 - ex) << 23);      // 2^-(ex-127)
-    const float inv = __int_as_float(ex << 23);             // 2^(ex-127)
+    const bool plain = ex == 0 || ex > 250;
+    sc = plain ? 1.0f : __int_as_float((254 - ex) << 23);   // 2^-(ex-127)
+    inv = plain ? 1.0f : __int_as_float(ex << 23);          // 2^(ex-127)
     // 1e-6 absolute, in normalised units; kept > 0 so that 0/0 cannot occur
-    const float eps = fmaxf(1e-6f * sc * sc, 1e-37f);
-    return wenoz_side_f(V1 * sc, V2 * sc, V3 * sc, V4 * sc, V5 * sc, eps) * inv;
+    eps = plain ? 1e-6f : fmaxf(1e-6f * sc * sc, 1e-37f);
+}
+
+// f+ at cells i-3..i+1 (a1..a5) plus f- at i+2..i-2 (b1..b5, the mirrored
+// stencil): the WENO-Z face flux
+__device__ __forceinline__ float wenoz_pm_f(float a1, float a2, float a3, float a4, float a5, float b1,
+                                            float b2, float b3, float b4, float b5) {
+    float sa, ia, ea, sb, ib, eb;
+    wenoz_scale(a1, a2, a3, a4, a5, sa, ia, ea);
+    wenoz_scale(b1, b2, b3, b4, b5, sb, ib, eb);
+    const float2 sc = make_float2(sa, sb), eps = make_float2(ea, eb);
+    const float2 V1 = p_mul(make_float2(a1, b1), sc), V2 = p_mul(make_float2(a2, b2), sc),
+                 V3 = p_mul(make_float2(a3, b3), sc), V4 = p_mul(make_float2(a4, b4), sc),
+                 V5 = p_mul(make_float2(a5, b5), sc);
+    const float2 c1312 = p_set(13.0f / 12.0f), cq = p_set(0.25f), m1 = p_set(-1.0f), m2 = p_set(-2.0f),
+                 m4 = p_set(-4.0f), c2 = p_set(2.0f), c3 = p_set(3.0f), c5 = p_set(5.0f);
+    // Jiang-Shu smoothness indicators (Reconstruction.H:70-139)
+    const float2 d1 = p_fma(m2, V2, p_add(V1, V3));           // V1 - 2 V2 + V3
+    const float2 e1 = p_fma(c3, V3, p_fma(m4, V2, V1));       // V1 - 4 V2 + 3 V3
+    const float2 s1 = p_fma(p_mul(c1312, d1), d1, p_mul(p_mul(cq, e1), e1));
+    const float2 d2 = p_fma(m2, V3, p_add(V2, V4));           // V2 - 2 V3 + V4
+    const float2 e2 = p_fma(m1, V4, V2);                      // V2 - V4
+    const float2 s2 = p_fma(p_mul(c1312, d2), d2, p_mul(p_mul(cq, e2), e2));
+    const float2 d3 = p_fma(m2, V4, p_add(V3, V5));           // V3 - 2 V4 + V5
+    const float2 e3 = p_fma(c3, V3, p_fma(m4, V4, V5));       // 3 V3 - 4 V4 + V5
+    const float2 s3 = p_fma(p_mul(c1312, d3), d3, p_mul(p_mul(cq, e3), e3));
+    // tau / (eps + beta) with tau = |beta_1 - beta_3|, capped at 1e18: a stencil
+    // side that is exactly flat (beta = 0) next to a jump gives tau / eps, which
+    // for |V| above ~1e5 in normalised units of a small eps would overflow
+    // (1 + r^2) in FP32; at the cap that side's weight already dominates the
+    // others by > 1e30
+    const float2 tau = p_fma(m1, s3, s1);
+    float2 r1 = p_mul(tau, p_rcp(p_add(eps, s1))), r2 = p_mul(tau, p_rcp(p_add(eps, s2))),
+           r3 = p_mul(tau, p_rcp(p_add(eps, s3)));
+    r1 = make_float2(fminf(fabsf(r1.x), 1e18f), fminf(fabsf(r1.y), 1e18f));
+    r2 = make_float2(fminf(fabsf(r2.x), 1e18f), fminf(fabsf(r2.y), 1e18f));
+    r3 = make_float2(fminf(fabsf(r3.x), 1e18f), fminf(fabsf(r3.y), 1e18f));
+    // alpha_k = d_k (1 + r_k^2), d = (1, 6, 3) / 10 (the 1/10 cancels)
+    const float2 one = p_set(1.0f);
+    const float2 w1 = p_fma(r1, r1, one), w2 = p_mul(p_set(6.0f), p_fma(r2, r2, one)),
+                 w3 = p_mul(c3, p_fma(r3, r3, one));
+    // candidate stencils, times 6
+    const float2 v1 = p_fma(p_set(11.0f), V3, p_fma(p_set(-7.0f), V2, p_mul(c2, V1)));
+    const float2 v2 = p_fma(c2, V4, p_fma(c5, V3, p_mul(m1, V2)));
+    const float2 v3 = p_fma(m1, V5, p_fma(c5, V4, p_mul(c2, V3)));
+    const float2 num = p_fma(w1, v1, p_fma(w2, v2, p_mul(w3, v3)));
+    const float2 den = p_mul(p_set(6.0f), p_add(w1, p_add(w2, w3)));
+    const float2 f = p_mul(p_mul(num, p_rcp(den)), make_float2(ia, ib));
+    return f.x + f.y;
 }
 
 // Conversions between FP64 and FP32 on the integer pipes.  GB300 runs FP64
