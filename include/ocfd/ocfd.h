@@ -299,9 +299,10 @@ ocfd_status ocfd_level_set_stop_time(ocfd_level* level, double stop_time, void* 
 int64_t ocfd_level_cells(const ocfd_level* level);
 /* Kernels one ocfd_level_advance step launches with `flags`. */
 int ocfd_level_launches_per_step(const ocfd_level* level, unsigned flags);
-/* Average duration in ms of the level's fused RK-stage kernel (stage 2: reads
- * two states, writes one) over `reps` back-to-back launches, timed with CUDA
- * events on `stream`.  Overwrites the level's stage scratch buffer only. */
+/* Average duration in ms of the level's fused RK-stage kernel (SSP-RK3's
+ * stage 2 whatever the level's time integration: reads two states, writes one)
+ * over `reps` back-to-back launches, timed with CUDA events on `stream`.
+ * Overwrites the level's stage scratch buffer only. */
 ocfd_status ocfd_level_profile_stage(ocfd_level* level, unsigned flags, int reps, double* ms,
                                      void* stream);
 
@@ -316,6 +317,14 @@ ocfd_status ocfd_level_autotune(ocfd_level* level, unsigned flags, int reps, int
                                 void* stream);
 /* Set the tile shape (index, -1 keeps it) and schedule (0-2) explicitly. */
 ocfd_status ocfd_level_set_schedule(ocfd_level* level, int32_t tile, int32_t sched);
+/* Time integration of a standalone ideal-gas level, ebr.time_integration
+ * (Source/EBR.cpp:36, Source/Advance.cpp:115-149): 3 = SSP-RK3 (the default
+ * here; AmrLevel::RK(3, ...)), 2 = "RK2", Heun (U* = U^n + dt L(U^n), ghosts at
+ * t; U^{n+1} = U^n/2 + (U* + dt L(U*))/2, ghosts at t + dt; the reference's
+ * default), 1 = "Euler" (U^{n+1} = U^n + dt L(U^n), then a state copy).  The CFL
+ * bound of the new state is fused into the last stage.  Synchronous; levels of a
+ * hierarchy follow ocfd_amr_set_time_integration (OCFD_BAD_ARG here). */
+ocfd_status ocfd_level_set_time_integration(ocfd_level* level, int32_t order);
 
 /* ------------------------------------------- embedded boundary on a level
  * The box loop of EBR::compute_dSdt (Source/Advance.cpp:201-342) over a level
@@ -459,6 +468,14 @@ ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_a
  * whose parent or a face neighbour of it is cut or covered are interpolated
  * piecewise-constant.  kind OCFD_EB_NONE removes the body.  Synchronous. */
 ocfd_status ocfd_amr_set_eb(ocfd_amr* amr, const ocfd_eb_desc* eb);
+/* Time integration of every level, present and future (orders as
+ * ocfd_level_set_time_integration).  Under Heun and Euler the coarse-fine
+ * ghosts of a fine stage at time t are AMReX FillPatch's linear interpolation
+ * between the coarse old and new states (Source/Advance.cpp:119,126) and the
+ * stage fluxes enter the flux registers with weight 0.5 dt (Heun) or dt
+ * (Euler); under SSP-RK3 they come from the coarse stage states (above).
+ * Synchronous. */
+ocfd_status ocfd_amr_set_time_integration(ocfd_amr* amr, int32_t order);
 /* ocfd_level_autotune for every level; the choice per level index is kept for
  * the levels later regrids build.  ocfd_amr_tuned reads a level's tile shape and
  * schedule (0 on success, -1 for a bad level). */

@@ -591,6 +591,7 @@ struct ocfd_amr {
     long long steps = 0;
     int launches = 0;          // kernels of the captured coarse step
     bool has_eb = false;       // embedded body cutting every level
+    int rk_order = 3;          // time integration of every level (rk_scheme)
     ocfd_eb_desc eb{};
     // autotuned tile shape and schedule per level index (-1: not tuned)
     int tuned_tile[OCFD_AMR_MAX_LEVELS] = {-1, -1, -1, -1, -1, -1};
@@ -662,6 +663,7 @@ static ocfd_status make_level(ocfd_amr* H, int l, const std::vector<IBox>& boxes
     d.tile = H->tuned_tile[l];
     ocfd_status s = level_alloc(H->ctx, &d, nbuf, out, &H->pool);
     if (s == OCFD_OK) (*out)->sched = H->tuned_sched[l];
+    if (s == OCFD_OK) (*out)->rk_order = H->rk_order;
     if (s == OCFD_OK && H->has_eb) s = eb_setup(*out, H->eb);
     if (s == OCFD_OK && H->has_eb) s = rebuild_fill_tags(*out);
     return s;
@@ -1060,6 +1062,24 @@ static void mix_coefs(int kind, double theta, double r, double* a) {
     a[3] = 1.5 * w3;
 }
 
+// Coarse-level weights of (A, B, C, D) for the ghosts of fine stage k of the
+// substep starting at theta (k = 3: the coarse end state's ghosts, theta + r).
+// SSP-RK3: the dense output of the coarse stages (mix_coefs).  Heun and Euler:
+// AMReX FillPatch's linear interpolation between the coarse old (A) and new (D)
+// states at the stage's time (Source/Advance.cpp:119,126; the two-level
+// FillPatch of AmrLevel).
+static void cf_coefs(int order, int k, double theta, double r, double* a) {
+    if (order == 3) {
+        mix_coefs(k, theta, r, a);
+        return;
+    }
+    const double th = k == 3 ? theta + r : theta + r * rk_scheme(order).tfrac[k];
+    a[0] = 1.0 - th;
+    a[1] = 0.0;
+    a[2] = 0.0;
+    a[3] = th;
+}
+
 static ocfd_status launch_cf(ocfd_amr* H, int f, double* dst, const double* a, cudaStream_t st) {
     AmrLev& F = H->lev[f];
     AmrLev& C = H->lev[f - 1];
@@ -1106,23 +1126,26 @@ static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cud
     ocfd_level* L = A.L;
     const bool has_child = l < H->nlev - 1;
     const double theta = 0.5 * (it - 1), r = 0.5;
-    const double tfrac[3] = {0.0, 1.0, 0.5};
+    const RkScheme& R = rk_scheme(H->rk_order);
     ocfd_status s = OCFD_OK;
     if (has_child) {
         cudaMemsetAsync(A.creg, 0, sizeof(double) * std::max<long long>(1, A.creg_elems), st);
         cudaMemsetAsync(H->lev[l + 1].freg, 0, sizeof(double) * std::max<long long>(1, H->lev[l + 1].freg_elems), st);
     }
-    for (int k = 0; k < 3 && s == OCFD_OK; ++k) {
+    for (int k = 0; k < R.nst && s == OCFD_OK; ++k) {
         double a[4];
-        mix_coefs(k, theta, r, a);
-        s = fill_level(H, l, L->buf[k], a, tfrac[k], st);
+        cf_coefs(R.order, k, theta, r, a);
+        s = fill_level(H, l, L->buf[R.src[k]], a, R.tfrac[k], st);
         if (s == OCFD_OK) s = launch_stage(L, k, flags, st);
         launches_counter += stage_launches(L, flags);
     }
     if (s != OCFD_OK) return s;
+    if (R.copy_out && cudaMemcpyAsync(L->buf[has_child ? 3 : 0], L->buf[1], sizeof(double) * L->elems,
+                                      cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return check_launch("AMR stage output copy");
     if (has_child) {
         double a[4];
-        mix_coefs(3, theta, r, a);
+        cf_coefs(R.order, 3, theta, r, a);
         s = fill_level(H, l, L->buf[3], a, 1.0, st);
         for (int i = 1; i <= 2 && s == OCFD_OK; ++i) s = advance_level(H, l + 1, i, flags, st);
         if (s != OCFD_OK) return s;
@@ -1551,6 +1574,15 @@ int ocfd_amr_tuned(const ocfd_amr* H, int lev, int32_t* tile, int32_t* sched) {
     if (tile) *tile = H->lev[lev].L->tile;
     if (sched) *sched = H->lev[lev].L->sched;
     return 0;
+}
+
+ocfd_status ocfd_amr_set_time_integration(ocfd_amr* H, int32_t order) {
+    if (!H || order < 1 || order > 3) return fail(OCFD_BAD_ARG, "ocfd_amr_set_time_integration: order is 1, 2 or 3");
+    if (order == H->rk_order) return OCFD_OK;
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_amr_set_time_integration");
+    H->rk_order = order;
+    for (int l = 0; l < H->nlev; ++l) H->lev[l].L->rk_order = order;
+    return rebuild_tables(H);
 }
 
 ocfd_status ocfd_amr_set_eb(ocfd_amr* H, const ocfd_eb_desc* eb) {

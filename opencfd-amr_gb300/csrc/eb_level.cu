@@ -503,10 +503,10 @@ struct ocfd::EbLevel {
     std::vector<int> ebox;
     std::vector<long long> q_off, f_off[3];
     double* d_scratch = nullptr;
-    EbStageBox* d_stage[3] = {nullptr, nullptr, nullptr};
+    EbStageBox* d_stage[NUM_STAGE_SLOTS] = {nullptr, nullptr, nullptr, nullptr};
     long long *d_pstart = nullptr, *d_fstart = nullptr, *d_cstart = nullptr;
     long long ptotal = 0, ftotal = 0, ctotal = 0;
-    bool cfl3 = true;
+    bool cfl_slot[NUM_STAGE_SLOTS] = {false, false, true, false};  // fused CFL bound per stage slot
     // per-box launches: work of each box and its local prefix tables
     std::vector<long long> pcount, fcount, ccount;
     long long* d_floc = nullptr;  // (0, F0, F0 + F1) per box
@@ -518,7 +518,7 @@ namespace ocfd {
 
 static void eb_free_tables(ocfd_level* L) {
     EbLevel* E = L->eb;
-    for (int s = 0; s < 3; ++s) {
+    for (int s = 0; s < NUM_STAGE_SLOTS; ++s) {
         dev_free(E->d_stage[s], L->pool);
         E->d_stage[s] = nullptr;
     }
@@ -732,11 +732,12 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     eb_free_tables(L);
     const int ne = (int)E->ebox.size();
     if (ne == 0) return OCFD_OK;
-    E->cfl3 = roles.cfl;
-    const int S_of[3] = {0, 1, 2}, O_of[3] = {1, 2, roles.out3};
-    const double ra[3] = {0.0, 0.75, 1.0 / 3.0}, rb[3] = {1.0, 0.25, 2.0 / 3.0};
-    const double wflux[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
-    std::vector<EbStageBox> st[3];
+    StageSlot slot[NUM_STAGE_SLOTS];
+    for (int k = 0; k < NUM_STAGE_SLOTS; ++k) {
+        slot[k] = stage_slot(L->rk_order, roles, k);
+        E->cfl_slot[k] = slot[k].cfl;
+    }
+    std::vector<EbStageBox> st[NUM_STAGE_SLOTS];
     std::vector<long long> ps(ne), fs(3 * ne), cs(ne), floc(3 * ne);
     long long pt = 0, ft = 0, ct = 0;
     E->pcount.assign(ne, 0);
@@ -796,14 +797,15 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
         }
         ocfd_array4 a[4];
         for (int i = 0; i < L->nbuf; ++i) a[i] = fab_view(L, b, i);
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < NUM_STAGE_SLOTS; ++k) {
+            if (!slot[k].used) continue;
             EbStageBox x = base;
-            x.S = view_of<const double>(&a[S_of[k]]);
+            x.S = view_of<const double>(&a[slot[k].src]);
             x.U0 = view_of<const double>(&a[0]);
-            x.Uout = view_of<double>(&a[O_of[k]]);
-            x.rk_a = ra[k];
-            x.rk_b = rb[k];
-            x.flux_w = wflux[k];
+            x.Uout = view_of<double>(&a[slot[k].out]);
+            x.rk_a = slot[k].a;
+            x.rk_b = slot[k].b;
+            x.flux_w = slot[k].w;
             st[k].push_back(x);
         }
     }
@@ -811,7 +813,7 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     E->ftotal = ft;
     E->ctotal = ct;
     ocfd_status s = OCFD_OK;
-    for (int k = 0; k < 3 && s == OCFD_OK; ++k) s = upload(&E->d_stage[k], st[k], L->pool);
+    for (int k = 0; k < NUM_STAGE_SLOTS && s == OCFD_OK; ++k) s = upload(&E->d_stage[k], st[k], L->pool);
     if (s == OCFD_OK) s = upload(&E->d_pstart, ps, L->pool);
     if (s == OCFD_OK) s = upload(&E->d_fstart, fs, L->pool);
     if (s == OCFD_OK) s = upload(&E->d_cstart, cs, L->pool);
@@ -856,7 +858,7 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
         A.dx_f[d] = (float)L->desc.dx[d];
     }
     A.dt_ptr = &L->d_step->dt;
-    A.cfl_min = (s == 2 && E->cfl3) ? &L->d_step->cfl_min : nullptr;
+    A.cfl_min = E->cfl_slot[s] ? &L->d_step->cfl_min : nullptr;
     A.visc = (flags & OCFD_VISC) ? 1 : 0;
     A.redist = E->desc.redistribute ? 1 : 0;
     const bool f32 = (flags & OCFD_FLUX_FP32) && !A.visc;

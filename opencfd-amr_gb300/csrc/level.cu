@@ -398,9 +398,9 @@ ocfd_status level_autotune(ocfd_level* L, unsigned flags, int reps, cudaStream_t
             L->sched = sc;
             RegBoxArgs dummy{};
             auto go = [&]() {
-                return f32 ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[1], L->d_tile_start, L->nreg, dummy,
+                return f32 ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[STAGE_PROBE], L->d_tile_start, L->nreg, dummy,
                                                     L->ntiles, L->ctx->parm, st, L->sched, L->d_queue)
-                           : launch_rhs_regular(L->tile, visc, L->d_stage[1], L->d_tile_start, L->nreg, dummy,
+                           : launch_rhs_regular(L->tile, visc, L->d_stage[STAGE_PROBE], L->d_tile_start, L->nreg, dummy,
                                                 L->ntiles, L->ctx->parm, st, L->sched, L->d_queue);
             };
             s = go();  // warm-up
@@ -437,14 +437,16 @@ int stage_launches(const ocfd_level* L, unsigned flags) {
 
 static ocfd_status record_step(ocfd_level* L, unsigned flags, cudaStream_t st) {
     k_step_begin<<<1, 1, 0, st>>>(L->d_step);
-    const double tfrac[3] = {0.0, 1.0, 0.5};
-    const int src[3] = {0, 1, 2};
-    for (int s = 0; s < 3; ++s) {
-        ocfd_status r = fill_ghosts(L, L->buf[src[s]], tfrac[s], st);
+    const RkScheme& R = rk_scheme(L->rk_order);
+    for (int s = 0; s < R.nst; ++s) {
+        ocfd_status r = fill_ghosts(L, L->buf[R.src[s]], R.tfrac[s], st);
         if (r != OCFD_OK) return r;
         r = launch_stage(L, s, flags, st);
         if (r != OCFD_OK) return r;
     }
+    if (R.copy_out && cudaMemcpyAsync(L->buf[0], L->buf[1], sizeof(double) * L->elems, cudaMemcpyDeviceToDevice,
+                                      st) != cudaSuccess)
+        return check_launch("level step: B -> A");
     k_step_end<<<1, 1, 0, st>>>(L->d_step);
     return check_launch("level step");
 }
@@ -464,7 +466,36 @@ static ocfd_array4 fab_array(const ocfd_level* L, int b, int i) {
     return a;
 }
 
-// Stage tables: stage 1 A -> B, stage 2 (A, B) -> C, stage 3 (A, C) -> A (or D)
+const RkScheme& rk_scheme(int order) {
+    // SSP-RK3 in Shu-Osher form (AmrLevel::RK(3, ...), Source/Advance.cpp:141-148);
+    // AMReX registers the stage fluxes with the RK3 weights 1/6, 1/6, 2/3
+    static const RkScheme rk3{3, 3, {0, 1, 2}, {1, 2, RK_OUT}, {0.0, 0.75, 1.0 / 3.0}, {1.0, 0.25, 2.0 / 3.0},
+                              {0.0, 1.0, 0.5}, {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0}, false};
+    // Heun, Source/Advance.cpp:123-138: U* = U^n + dt L(U^n) (ghosts at t), then
+    // U^{n+1} = U^n / 2 + (U* + dt L(U*)) / 2 (ghosts at t + dt); each stage's
+    // fluxes are registered with 0.5 dt (compute_dSdt(..., 0.5*dt, ...))
+    static const RkScheme rk2{2, 2, {0, 1, 0}, {1, RK_OUT, 0}, {0.0, 0.5, 0.0}, {1.0, 0.5, 0.0},
+                              {0.0, 1.0, 0.0}, {0.5, 0.5, 0.0}, false};
+    // forward Euler, Source/Advance.cpp:117-122: U^{n+1} = U^n + dt L(U^n)
+    static const RkScheme rk1{1, 1, {0, 0, 0}, {1, 0, 0}, {0.0, 0.0, 0.0}, {1.0, 0.0, 0.0},
+                              {0.0, 0.0, 0.0}, {1.0, 0.0, 0.0}, true};
+    return order == 1 ? rk1 : (order == 2 ? rk2 : rk3);
+}
+
+StageSlot stage_slot(int order, const StageRoles& roles, int k) {
+    StageSlot z{};
+    if (k == STAGE_PROBE) {
+        const RkScheme& R = rk_scheme(3);
+        return StageSlot{true, R.src[1], R.out[1], R.a[1], R.b[1], R.w[1], false};
+    }
+    const RkScheme& R = rk_scheme(order);
+    if (k < 0 || k >= R.nst) return z;
+    const int out = R.out[k] == RK_OUT ? roles.out3 : R.out[k];
+    return StageSlot{true, R.src[k], out, R.a[k], R.b[k], R.w[k], k == R.nst - 1 && roles.cfl};
+}
+
+// Stage tables, one per slot (stage_slot): for SSP-RK3 stage 1 A -> B, stage 2
+// (A, B) -> C, stage 3 (A, C) -> A (or D)
 ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     if (L->roles != &roles) {
         delete L->roles;
@@ -474,23 +505,22 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     const double dxinv[3] = {1.0 / desc->dx[0], 1.0 / desc->dx[1], 1.0 / desc->dx[2]};
     std::vector<int> tile_start;
     int nt = 0;
-    std::vector<RegBoxArgs> st[3];
-    const int S_of[3] = {0, 1, 2}, O_of[3] = {1, 2, roles.out3};
-    const double ra[3] = {0.0, 0.75, 1.0 / 3.0}, rb[3] = {1.0, 0.25, 2.0 / 3.0};
-    // stage weights of the SSP-RK3 update U^{n+1} = U^n + dt (L0 + L1 + 4 L2) / 6
-    const double wflux[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
+    std::vector<RegBoxArgs> st[NUM_STAGE_SLOTS];
+    StageSlot slot[NUM_STAGE_SLOTS];
+    for (int k = 0; k < NUM_STAGE_SLOTS; ++k) slot[k] = stage_slot(L->rk_order, roles, k);
     for (size_t b = 0; b < L->boxes.size(); ++b) {
         if (!eb_box_regular(L, (int)b)) continue;  // cut / covered: eb_level.cu
         ocfd_array4 a[4];
         for (int i = 0; i < L->nbuf; ++i) a[i] = fab_array(L, (int)b, i);
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < NUM_STAGE_SLOTS; ++k) {
+            if (!slot[k].used) continue;
             RegBoxArgs r{};
-            fill_regular_args(r, &a[S_of[k]], nullptr, nullptr, L->boxes[b], dxinv, L->tile);
+            fill_regular_args(r, &a[slot[k].src], nullptr, nullptr, L->boxes[b], dxinv, L->tile);
             r.mode = RHS_FUSED_STAGE;
             r.U0 = view_of<const double>(&a[0]);
-            r.Uout = view_of<double>(&a[O_of[k]]);
-            r.rk_a = ra[k];
-            r.rk_b = rb[k];
+            r.Uout = view_of<double>(&a[slot[k].out]);
+            r.rk_a = slot[k].a;
+            r.rk_b = slot[k].b;
             r.dt_ptr = &L->d_step->dt;
             r.zvirt = L->zvirt ? 1 : 0;
             r.zdom[0] = desc->domain.lo[2];
@@ -499,14 +529,14 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
                 r.zmirror[sd] = L->zmirror[sd];
                 r.zsign[sd] = L->zsign[sd];
             }
-            r.cfl_min = (k == 2 && roles.cfl) ? &L->d_step->cfl_min : nullptr;
+            r.cfl_min = slot[k].cfl ? &L->d_step->cfl_min : nullptr;
             for (int d = 0; d < 3; ++d) {
                 r.dx[d] = desc->dx[d];
                 r.dx_f[d] = (float)desc->dx[d];
             }
             if (!roles.flux_bits.empty() && roles.flux_bits[b]) {
                 r.has_flux = roles.flux_bits[b];
-                r.flux_w = wflux[k];
+                r.flux_w = slot[k].w;
                 if (r.has_flux & FLUX_ACC_ALL)
                     for (int d = 0; d < 3; ++d) r.flux[d] = roles.creg[3 * b + d];
                 if (r.has_flux & FLUX_ACC_PLANES)
@@ -524,9 +554,9 @@ ocfd_status build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     L->nreg = (int)tile_start.size();
     L->h_ntiles.clear();
     for (int b = 0; b < L->nreg; ++b) L->h_ntiles.push_back((b + 1 < L->nreg ? tile_start[b + 1] : nt) - tile_start[b]);
-    for (int k = 0; k < 3; ++k) L->h_stage[k] = st[k];
+    for (int k = 0; k < NUM_STAGE_SLOTS; ++k) L->h_stage[k] = st[k];
     ocfd_status s = OCFD_OK;
-    for (int k = 0; k < 3 && s == OCFD_OK; ++k) {
+    for (int k = 0; k < NUM_STAGE_SLOTS && s == OCFD_OK; ++k) {
         dev_free(L->d_stage[k], L->pool);
         L->d_stage[k] = nullptr;
         s = upload(&L->d_stage[k], st[k], L->pool);
@@ -708,8 +738,8 @@ ocfd_status ocfd_level_destroy(ocfd_level* L) {
     delete L->roles;
     DevPool* pool = L->pool;
     for (int i = 0; i < 4; ++i) dev_free(L->buf[i], pool);
+    for (int i = 0; i < NUM_STAGE_SLOTS; ++i) dev_free(L->d_stage[i], pool);
     for (int i = 0; i < 3; ++i) {
-        dev_free(L->d_stage[i], pool);
         dev_free(L->d_bc[i], pool);
         dev_free(L->d_bc_start[i], pool);
         dev_free(L->d_bc_chunk[i], pool);
@@ -754,6 +784,22 @@ ocfd_status ocfd_level_set_schedule(ocfd_level* L, int32_t tile, int32_t sched) 
         const StageRoles roles = L->roles ? *L->roles : StageRoles{};
         s = build_stage_tables(L, roles);
     }
+    if (L->graph) {
+        cudaGraphExecDestroy(L->graph);
+        L->graph = nullptr;
+    }
+    return s;
+}
+
+ocfd_status ocfd_level_set_time_integration(ocfd_level* L, int32_t order) {
+    if (!L || order < 1 || order > 3) return fail(OCFD_BAD_ARG, "ocfd_level_set_time_integration: order is 1, 2 or 3");
+    if (L->ncomp != 5) return fail(OCFD_BAD_ARG, "ocfd_level_set_time_integration: a reacting level sets its order at creation");
+    if (L->pool) return fail(OCFD_BAD_ARG, "ocfd_level_set_time_integration: a hierarchy's level follows ocfd_amr_set_time_integration");
+    if (order == L->rk_order) return OCFD_OK;
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_level_set_time_integration");
+    L->rk_order = order;
+    const StageRoles roles = L->roles ? *L->roles : StageRoles{};
+    ocfd_status s = build_stage_tables(L, roles);
     if (L->graph) {
         cudaGraphExecDestroy(L->graph);
         L->graph = nullptr;
@@ -876,13 +922,13 @@ int ocfd_level_launches_per_step(const ocfd_level* L, unsigned flags) {
     if (!L) return 0;
     (void)flags;
     int fill = (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0 && !L->zvirt);
-    return 2 + 3 * (fill + stage_launches(L, flags));
+    return 2 + rk_scheme(L->rk_order).nst * (fill + stage_launches(L, flags));
 }
 
 ocfd_status ocfd_level_profile_stage(ocfd_level* L, unsigned flags, int reps, double* ms, void* stream) {
     if (!L || reps <= 0 || !ms) return fail(OCFD_BAD_ARG, "ocfd_level_profile_stage");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    auto launch = [&]() { return launch_stage(L, 1, flags, st); };
+    auto launch = [&]() { return launch_stage(L, STAGE_PROBE, flags, st); };
     ocfd_status s = launch();  // warm-up
     if (s != OCFD_OK) return s;
     cudaEvent_t e0, e1;

@@ -192,6 +192,35 @@ ocfd_status upload_tags(const std::vector<Tag>& tags, Tag** d_tags, long long** 
 struct EbLevel;
 struct StageRoles;
 
+// Time integration of a level (ebr.time_integration, Source/EBR.cpp:36 and
+// Source/Advance.cpp:115-149).  Stage k reads buffer src[k], its ghosts filled at
+// t + tfrac[k] dt, and writes U_out = a[k] U^n + b[k] (S + dt L(S)) into buffer
+// out[k] (RK_OUT: the step's output buffer, StageRoles::out3); its face fluxes
+// enter the flux registers with weight w[k] dt.  Forward Euler writes B and the
+// step then copies B to the output buffer (a stage never writes the buffer it
+// reads with halos).
+constexpr int RK_OUT = -1;
+struct RkScheme {
+    int order, nst;
+    int src[3], out[3];
+    double a[3], b[3], tfrac[3], w[3];
+    bool copy_out;
+};
+const RkScheme& rk_scheme(int order);
+
+// Stage-table slots of a level: 0..nst-1 the scheme's stages, STAGE_PROBE the
+// slot the autotuner and the stage timer launch (RK3's second stage, B -> C with
+// U^n from A: it overwrites scratch only, whatever the scheme).
+constexpr int NUM_STAGE_SLOTS = 4;
+constexpr int STAGE_PROBE = 3;
+struct StageSlot {
+    bool used;
+    int src, out;       // buffer indices
+    double a, b, w;     // U^n weight, stage weight, flux-register weight (x dt)
+    bool cfl;           // fused CFL bound of the new state
+};
+StageSlot stage_slot(int order, const StageRoles& roles, int k);
+
 }  // namespace ocfd
 
 struct ocfd_level {
@@ -221,14 +250,16 @@ struct ocfd_level {
     int nbc[3] = {0, 0, 0};
     long long bc_total[3] = {0, 0, 0};
     ocfd::BcInfo bcinfo{};
-    // RHS stage tables (3 stages)
+    // time integration order (3: SSP-RK3, 2: Heun, 1: forward Euler) and the RHS
+    // stage tables, one per stage slot (ocfd::stage_slot)
+    int rk_order = 3;
     int tile = 0;
-    ocfd::RegBoxArgs* d_stage[3] = {nullptr, nullptr, nullptr};
+    ocfd::RegBoxArgs* d_stage[ocfd::NUM_STAGE_SLOTS] = {nullptr, nullptr, nullptr, nullptr};
     int* d_tile_start = nullptr;
     int ntiles = 0;
     int nreg = 0;  // boxes in the regular stage tables
     // host copies of the regular stage tables and tiles per box (per-box launches)
-    std::vector<ocfd::RegBoxArgs> h_stage[3];
+    std::vector<ocfd::RegBoxArgs> h_stage[ocfd::NUM_STAGE_SLOTS];
     std::vector<int> h_ntiles;
     // tile schedule of the batched launch (TileSched) and its work-queue words
     int sched = ocfd::SCHED_GRID;
@@ -258,8 +289,8 @@ namespace ocfd {
 
 // Per-stage roles of a level inside an AMR hierarchy (defaults: single level).
 struct StageRoles {
-    int out3 = 0;              // buffer stage 3 writes: 0 (in place over U^n) or 3
-    bool cfl = true;           // fused CFL bound in stage 3
+    int out3 = 0;              // the step's output buffer: 0 (in place over U^n) or 3
+    bool cfl = true;           // fused CFL bound in the last stage
     // per box: flux-register accumulation flags and views (empty: none)
     std::vector<int> flux_bits;
     std::vector<View<double>> creg;   // 3 per box (FLUX_ACC_ALL)

@@ -9,7 +9,7 @@ import numpy as np
 
 from ._abi import Box, check, declare, load
 from .context import _stream_ptr
-from .level import NG, EbDesc, Level
+from .level import NG, TIME_INTEGRATION, EbDesc, Level
 
 MAX_LEVELS = 6
 
@@ -46,6 +46,7 @@ declare("ocfd_amr_state_elems", ctypes.c_size_t, [_vp, ctypes.c_int])
 declare("ocfd_amr_copy_in", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
 declare("ocfd_amr_copy_out", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
 declare("ocfd_amr_set_eb", ctypes.c_int, [_vp, ctypes.POINTER(EbDesc)])
+declare("ocfd_amr_set_time_integration", ctypes.c_int, [_vp, ctypes.c_int32])
 declare("ocfd_amr_autotune", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int, _vp])
 declare("ocfd_amr_tuned", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)])
 
@@ -134,6 +135,11 @@ class Hierarchy:
     def set_eb(self, desc):
         """Cut every level with an embedded body (ocfd.level.eb_desc(...))."""
         check(self.lib.ocfd_amr_set_eb(self.h, ctypes.byref(desc)), "ocfd_amr_set_eb")
+
+    def set_time_integration(self, scheme):
+        """Time integration of every level: "Euler", "RK2", "RK3" or 1 / 2 / 3."""
+        order = TIME_INTEGRATION.get(scheme, scheme)
+        check(self.lib.ocfd_amr_set_time_integration(self.h, int(order)), "ocfd_amr_set_time_integration")
 
     def box_classes(self, lev):
         return self.level(lev).box_classes()

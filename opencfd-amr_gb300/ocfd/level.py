@@ -60,6 +60,10 @@ def eb_desc(kind=EB_CYLINDER_Z, center=(0.5, 0.5), radius=0.1, nsub=16, redistri
 
 declare("ocfd_level_set_eb", ctypes.c_int, [_vp, ctypes.POINTER(EbDesc)])
 declare("ocfd_level_set_schedule", ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32])
+declare("ocfd_level_set_time_integration", ctypes.c_int, [_vp, ctypes.c_int32])
+
+# ebr.time_integration (Source/EBR.cpp:36): order of the level's RK scheme
+TIME_INTEGRATION = {"Euler": 1, "RK2": 2, "RK3": 3}
 declare("ocfd_level_autotune", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int, ctypes.POINTER(ctypes.c_int32),
                                               ctypes.POINTER(ctypes.c_int32), _vp])
 declare("ocfd_level_box_classes", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32)])
@@ -240,6 +244,12 @@ class Level:
         check(self.lib.ocfd_level_autotune(self.h, flags, reps, ctypes.byref(t), ctypes.byref(s), _stream_ptr(stream)),
               "ocfd_level_autotune")
         return t.value, s.value
+
+    def set_time_integration(self, scheme):
+        """"Euler", "RK2" (Heun, the reference's default) or "RK3" (SSP-RK3, the
+        default here), or the order 1 / 2 / 3."""
+        order = TIME_INTEGRATION.get(scheme, scheme)
+        check(self.lib.ocfd_level_set_time_integration(self.h, int(order)), "ocfd_level_set_time_integration")
 
     # ---- embedded body ---------------------------------------------------------
     def set_eb(self, desc):

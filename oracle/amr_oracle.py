@@ -54,6 +54,16 @@ RK_B = (1.0, 0.25, 2.0 / 3.0)
 TFRAC = (0.0, 1.0, 0.5)
 NEST = 2
 
+# ebr.time_integration (Source/EBR.cpp:36; Source/Advance.cpp:115-149): stages,
+# the buffer each stage reads, the times of its ghosts (fractions of dt) and the
+# flux-register weights (x dt).  RK3 stages write U^n-weighted Shu-Osher updates;
+# RK2 and Euler follow the reference's LinComb / Saxpy order.
+SCHEMES = {
+    3: dict(nst=3, src=(0, 1, 2), tfrac=TFRAC, w=W_RK3),
+    2: dict(nst=2, src=(0, 1), tfrac=(0.0, 1.0), w=(0.5, 0.5)),
+    1: dict(nst=1, src=(0,), tfrac=(0.0,), w=(1.0,)),
+}
+
 
 def mix_coefs(kind, theta, r=0.5):
     """Weights of (A, B, C, D) = (u0, U1, U2, U3) of the coarse RK3 step giving a
@@ -113,8 +123,9 @@ def _sl(lo, hi, g=0):
 class AmrOracle:
     def __init__(self, orc, n0, dx0, lo_bc, hi_bc, boxes0, prob_lo=(0.0, 0.0, 0.0), bc_case=0,
                  case_params=(), max_level=1, blocking_factor=(8, 8, 8), max_grid_size=(32, 32, 32),
-                 n_error_buf=1, refine_dengrad=0.05, eb=None):
+                 n_error_buf=1, refine_dengrad=0.05, eb=None, time_integration=3):
         self.orc = orc
+        self.rk = time_integration  # 3: SSP-RK3, 2: RK2 (Heun), 1: Euler
         self.eb = eb          # None or dict(center=(cx, cy), radius=r, nsub=16, redistribute=False)
         self._geoms = {}
         self.n0 = tuple(n0)
@@ -343,25 +354,33 @@ class AmrOracle:
         if has_child:
             L["creg"] = [0.0, 0.0, 0.0]
             self.levels[l + 1]["freg"] = [0.0, 0.0, 0.0]
-        out_of = (1, 2, 3 if has_child else 0)
-        for k in range(3):
-            S = bufs[k]
-            self.fill(l, S, mix_coefs(k, theta), TFRAC[k], parent)
+        sch = SCHEMES[self.rk]
+        nst = sch["nst"]
+        last = 3 if has_child else 0
+        out_of = (1, 2, last) if self.rk == 3 else ((1, last) if self.rk == 2 else (last,))
+        for k in range(nst):
+            S = bufs[sch["src"][k]]
+            self.fill(l, S, self._cf_coefs(k, theta), sch["tfrac"][k], parent)
             dS, F = self._rhs_level(l, S, has_child or l > 0)
             dt = L["dt"]
             O = bufs[out_of[k]]
             vs = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
             u0 = A[vs][:, mask]
             us = S[vs][:, mask]
-            O[vs][:, mask] = RK_A[k] * u0 + RK_B[k] * (us + dt * dS[:, mask])
-            w = W_RK3[k] * dt
+            if self.rk == 3:
+                O[vs][:, mask] = RK_A[k] * u0 + RK_B[k] * (us + dt * dS[:, mask])
+            elif k == 0:
+                O[vs][:, mask] = 1.0 * us + dt * dS[:, mask]
+            else:
+                O[vs][:, mask] = (0.5 * us + 0.5 * u0) + (0.5 * dt) * dS[:, mask]
+            w = sch["w"][k] * dt
             if has_child:
                 L["creg"] = [L["creg"][d] + w * F[d] for d in range(3)]
             if l > 0:
                 L["freg"] = [L["freg"][d] + w * F[d] for d in range(3)]
         if has_child:
             D = bufs[3]
-            self.fill(l, D, mix_coefs(3, theta), 1.0, parent)
+            self.fill(l, D, self._cf_coefs(3, theta), 1.0, parent)
             for i in (1, 2):
                 self._advance(l + 1, i)
             self._reflux(l, D)
@@ -369,6 +388,16 @@ class AmrOracle:
             L["U"] = D.copy()
         if l > 0:
             L["time"] += L["dt"]
+
+    def _cf_coefs(self, k, theta, r=0.5):
+        """Weights of the coarse (A, B, C, D) for fine stage k of the substep at
+        theta (k = 3: the coarse end state at theta + r): the RK3 dense output, or
+        for RK2 / Euler FillPatch's linear interpolation between the coarse old
+        (A) and new (D) states at the stage's time."""
+        if self.rk == 3:
+            return mix_coefs(k, theta, r)
+        th = theta + r if k == 3 else theta + r * SCHEMES[self.rk]["tfrac"][k]
+        return (1.0 - th, 0.0, 0.0, th)
 
     def _covered(self, c):
         m = self.levels[c + 1]["mask"]

@@ -1605,3 +1605,53 @@ double ocfdo_advance_rk3(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int
     for (int d = 0; d < 3; ++d) free(fl[d]);
     return time;
 }
+
+/* ======================================================= RK2 / Euler driver
+ * EBR::flow_advance, Source/Advance.cpp:115-138:
+ *   Euler: FillPatch(t); S_new = 1.0 * Sborder + dt * dSdt        (LinComb)
+ *   RK2:   FillPatch(t); S_new = 1.0 * Sborder + dt * dSdt        (stage 1)
+ *          FillPatch(t + dt) of S_new;
+ *          S_new = 0.5 * Sborder + 0.5 * S_old; S_new += 0.5 * dt * dSdt */
+double ocfdo_advance_rk12(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int nx, int ny,
+                          int nz, int do_visc, double cfl, int nsteps, int order, double* dts) {
+    box_t b = mkbox(nx, ny, nz);
+    long long N = gN(&b), BN = bN(&b);
+    double dxinv[3] = {1.0 / bc->dx[0], 1.0 / bc->dx[1], 1.0 / bc->dx[2]};
+    double* S0 = (double*)xcalloc(N * NCONS, sizeof(double));
+    double* k1 = (double*)xcalloc(BN * NCONS, sizeof(double));
+    double* fl[3];
+    for (int d = 0; d < 3; ++d) fl[d] = (double*)xcalloc(fN(&b, d) * NCONS, sizeof(double));
+    double time = 0.0, dt_prev = -1.0;
+    for (int s = 0; s < nsteps; ++s) {
+        ocfdo_fill_ghosts(bc, S, NCONS, nx, ny, nz, time);
+        double dt = cfl * ocfdo_estdt(p, S, nx, ny, nz, bc->dx);
+        if (dt_prev > 0 && dt > 1.1 * dt_prev) dt = 1.1 * dt_prev;
+        dt_prev = dt;
+        if (dts) dts[s] = dt;
+        memcpy(S0, S, sizeof(double) * N * NCONS);
+        ocfdo_rhs_regular(p, S, nx, ny, nz, dxinv, do_visc, k1, fl[0], fl[1], fl[2]);
+        for (int n = 0; n < NCONS; ++n)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) {
+                        long long g = n * N + gI(&b, i, j, k), c = n * BN + bI(&b, i, j, k);
+                        S[g] = 1.0 * S0[g] + dt * k1[c];
+                    }
+        if (order == 2) {
+            ocfdo_fill_ghosts(bc, S, NCONS, nx, ny, nz, time + dt);
+            ocfdo_rhs_regular(p, S, nx, ny, nz, dxinv, do_visc, k1, fl[0], fl[1], fl[2]);
+            for (int n = 0; n < NCONS; ++n)
+                for (int k = 0; k < nz; ++k)
+                    for (int j = 0; j < ny; ++j)
+                        for (int i = 0; i < nx; ++i) {
+                            long long g = n * N + gI(&b, i, j, k), c = n * BN + bI(&b, i, j, k);
+                            double v = 0.5 * S[g] + 0.5 * S0[g];
+                            S[g] = v + (0.5 * dt) * k1[c];
+                        }
+        }
+        time += dt;
+    }
+    free(S0); free(k1);
+    for (int d = 0; d < 3; ++d) free(fl[d]);
+    return time;
+}

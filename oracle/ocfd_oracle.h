@@ -126,6 +126,11 @@ void ocfdo_fill_ghosts(const ocfdo_bc* bc, double* S, int ncomp, int nx, int ny,
  * dts (nsteps entries, may be NULL) receives the steps taken. */
 double ocfdo_advance_rk3(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int nx, int ny,
                          int nz, int do_visc, double cfl, int nsteps, int form, double* dts);
+/* The same with ebr.time_integration = "RK2" (order 2, Heun) or "Euler"
+ * (order 1), Source/Advance.cpp:115-138, in the reference's LinComb / Saxpy
+ * operation order. */
+double ocfdo_advance_rk12(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int nx, int ny,
+                          int nz, int do_visc, double cfl, int nsteps, int order, double* dts);
 
 #ifdef __cplusplus
 }

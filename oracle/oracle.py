@@ -94,6 +94,7 @@ class Oracle:
         L = self.lib
         L.ocfdo_estdt.restype = ctypes.c_double
         L.ocfdo_advance_rk3.restype = ctypes.c_double
+        L.ocfdo_advance_rk12.restype = ctypes.c_double
         for n in ("ckrhoy", "ckubms", "ckcvbs", "ckpy", "get_t_given_ey"):
             getattr(L, "ocfdo_" + n).restype = ctypes.c_double
         L.ocfdo_ckrhoy.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
@@ -117,6 +118,7 @@ class Oracle:
         L.ocfdo_advance_rk3.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.ocfdo_advance_rk12.argtypes = L.ocfdo_advance_rk3.argtypes
         self.parm = ParmStruct()
         L.ocfdo_parm_default(ctypes.byref(self.parm))
         self.pp = ctypes.cast(ctypes.byref(self.parm), ctypes.c_void_p)
@@ -247,6 +249,18 @@ class Oracle:
         t = self.lib.ocfdo_advance_rk3(self.pp, ctypes.byref(bc), _ptr(S), gx - 2 * NG,
                                        gy - 2 * NG, gz - 2 * NG, int(do_visc), cfl, nsteps, form,
                                        _ptr(dts))
+        return t, dts
+
+    def advance_rk(self, bc, S, cfl, nsteps, order, do_visc=False):
+        """nsteps of ebr.time_integration = "Euler" (order 1), "RK2" (2) or RK3 (3,
+        Shu-Osher form) on a ghost-grown state, in place."""
+        if order == 3:
+            return self.advance_rk3(bc, S, cfl, nsteps, form=1, do_visc=do_visc)
+        _, gz, gy, gx = S.shape
+        dts = np.zeros(nsteps)
+        t = self.lib.ocfdo_advance_rk12(self.pp, ctypes.byref(bc), _ptr(S), gx - 2 * NG,
+                                        gy - 2 * NG, gz - 2 * NG, int(do_visc), cfl, nsteps, order,
+                                        _ptr(dts))
         return t, dts
 
 

@@ -55,18 +55,22 @@ def test_time_interpolation_weights():
         assert abs(got - want) < 5 * (abs(lam) * h) ** 3
 
 
-def periodic_oracle(orc, max_level=1):
+def periodic_oracle(orc, max_level=1, time_integration=3):
     n = (32, 16, 8)
     dx = 1.0 / 32
     A = AmrOracle(orc, n, (dx,) * 3, (0, 0, 0), (0, 0, 0), chop(n, 16), max_level=max_level,
-                  blocking_factor=(8, 8, 8), max_grid_size=(16, 16, 16))
+                  blocking_factor=(8, 8, 8), max_grid_size=(16, 16, 16), time_integration=time_integration)
     A.set_level_fabs(0, pulse_fab)
     A.fill_all_sync()
     return A
 
 
-def test_reflux_conserves(oracle):
-    A = periodic_oracle(oracle)
+@pytest.mark.parametrize("order", [3, 2, 1])
+def test_reflux_conserves(oracle, order):
+    """composite conservation under every time integration: the flux registers
+    take each stage's fluxes with the scheme's weights (RK3 1/6, 1/6, 2/3; RK2
+    1/2, 1/2; Euler 1)"""
+    A = periodic_oracle(oracle, time_integration=order)
     A.apply_grids(0, [[((16, 8, 4), (39, 23, 11)), ((56, 0, 0), (63, 15, 15))]])
     A.average_down_all()
     V, m = A.valid(0)
@@ -217,3 +221,29 @@ def test_cut_cell_operators_with_the_body(oracle):
     for l in range(len(A.levels)):
         V, m = A.valid(l)
         assert np.isfinite(V[:, m]).all() and V[0][m].min() > 0 and V[4][m].min() > 0
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_time_integration_single_level_matches_box_restatement(oracle, order):
+    """ebr.time_integration = RK2 (the reference's default) and Euler: the
+    hierarchy restatement on one level of eight boxes against the single-box C
+    restatement of Source/Advance.cpp:115-138 on the same periodic pulse"""
+    from oracle import BCStruct
+    n = (32, 16, 8)
+    dx = 1.0 / 32
+    A = periodic_oracle(oracle, max_level=0, time_integration=order)
+    S = np.ascontiguousarray(pulse_fab(0, (0, 0, 0), (n[0] - 1, n[1] - 1, n[2] - 1), (dx,) * 3))
+    bc = BCStruct()
+    bc.lo_bc[:] = [0, 0, 0]
+    bc.hi_bc[:] = [0, 0, 0]
+    bc.dx[:] = [dx] * 3
+    bc.dom_lo[:] = [0, 0, 0]
+    bc.dom_hi[:] = [n[0] - 1, n[1] - 1, n[2] - 1]
+    t, _ = oracle.advance_rk(bc, S, 0.5, 3, order)
+    for _ in range(3):
+        A.step(0.5)
+    V, m = A.valid(0)
+    assert m.all()
+    assert A.time == pytest.approx(t, rel=1e-14)
+    ref = S[:, NG:-NG, NG:-NG, NG:-NG]
+    assert np.abs(V - ref).max() <= 1e-13 * np.abs(ref).max()

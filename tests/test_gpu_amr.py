@@ -37,11 +37,12 @@ def make_hierarchy(ctx, case, regrid_int=None):
                      case["regrid_int"] if regrid_int is None else regrid_int, case["refine_dengrad"])
 
 
-def make_oracle(orc, case):
+def make_oracle(orc, case, time_integration=3):
     from amr_oracle import AmrOracle
     return AmrOracle(orc, case["n"], case["dx"], case["lo_bc"], case["hi_bc"], case["boxes0"], case["prob_lo"],
                      case["bc_case"], case["case_params"], case["max_level"], case["blocking_factor"],
-                     case["max_grid_size"], case["n_error_buf"], case["refine_dengrad"])
+                     case["max_grid_size"], case["n_error_buf"], case["refine_dengrad"],
+                     time_integration=time_integration)
 
 
 def oracle_build(A, fab):
@@ -134,6 +135,28 @@ def periodic_case(n=(32, 32, 8)):
 # two fine boxes of level 1 (domain 64 x 64 x 16); the second one touches the
 # periodic boundary x = 63 | 0
 PERIODIC_FINE = [((16, 16, 4), (39, 31, 11)), ((56, 40, 0), (63, 55, 15))]
+
+
+@pytest.mark.parametrize("scheme,order", [("RK2", 2), ("Euler", 1)])
+def test_dmr_steps_match_oracle_time_integration(ctx, oracle, scheme, order):
+    """RK2 (Heun) and Euler on the subcycled hierarchy: coarse-fine ghosts by
+    linear interpolation between the coarse old and new states (FillPatch), flux
+    registers weighted 0.5 dt / dt, three coarse steps with a regrid"""
+    case = small_dmr()
+    H = make_hierarchy(ctx, case)
+    H.set_time_integration(scheme)
+    H.build(case["fab"])
+    A = make_oracle(oracle, case, time_integration=order)
+    oracle_build(A, case["fab"])
+    cfl = 0.4
+    for step in range(3):
+        if step > 0 and step % case["regrid_int"] == 0:
+            A.regrid(0)
+        A.step(cfl)
+        H.advance(1, cfl)
+        t, _ = H.time()
+        assert abs(t - A.time) <= 1e-14 * A.time
+        compare_levels(H, A, 1e-11)
 
 
 def totals(H):

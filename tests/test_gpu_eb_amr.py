@@ -27,16 +27,18 @@ def small_jet(max_grid0=16):
     return case
 
 
-def make_pair(ctx, oracle, case):
+def make_pair(ctx, oracle, case, time_integration=3):
     from amr_oracle import AmrOracle
     from ocfd.level import eb_desc
     H = make_hierarchy(ctx, case)
+    H.set_time_integration(time_integration)
     H.set_eb(eb_desc(center=case["eb"]["center"], radius=case["eb"]["radius"],
                      redistribute=case["eb"]["redistribute"]))
     H.build(case["fab"])
     A = AmrOracle(oracle, case["n"], case["dx"], case["lo_bc"], case["hi_bc"], case["boxes0"], case["prob_lo"],
                   case["bc_case"], case["case_params"], case["max_level"], case["blocking_factor"],
-                  case["max_grid_size"], case["n_error_buf"], case["refine_dengrad"], eb=case["eb"])
+                  case["max_grid_size"], case["n_error_buf"], case["refine_dengrad"], eb=case["eb"],
+                  time_integration=time_integration)
     oracle_build(A, case["fab"])
     return H, A
 
@@ -52,9 +54,11 @@ def test_jet_eb_build_matches_oracle(ctx, oracle):
     compare_levels(H, A, 1e-15)
 
 
-def test_jet_eb_steps_match_oracle(ctx, oracle):
+@pytest.mark.parametrize("order", [3, 2])
+def test_jet_eb_steps_match_oracle(ctx, oracle, order):
+    """SSP-RK3, and RK2 (the time integration of the reference's jet inputs)"""
     case = small_jet()
-    H, A = make_pair(ctx, oracle, case)
+    H, A = make_pair(ctx, oracle, case, time_integration=order)
     cfl = 0.5
     for step in range(4):
         if step > 0 and step % case["regrid_int"] == 0:

@@ -124,3 +124,39 @@ def test_viscous_level_vs_oracle(ctx, oracle):
     ref, tr = run_oracle(oracle, case, 6, 0.4, visc=True)
     got, tg = run_gpu(ctx, case, 6, 0.4, (16, 12, 4), flags=1)
     assert relerr(got, ref) < 1e-10
+
+
+@pytest.mark.parametrize("scheme,order", [("RK2", 2), ("Euler", 1)])
+def test_time_integration_vs_oracle(ctx, oracle, scheme, order):
+    """ebr.time_integration = RK2 (the reference's default, Heun) and Euler
+    (Source/Advance.cpp:115-138) on the DMR boundary functor over eight boxes,
+    against the oracle's restatement in the reference's LinComb / Saxpy order"""
+    from ocfd.cases import dmr
+    case = dmr(64, 16, 2)
+    S = np.ascontiguousarray(case["G"].copy())
+    tr, _ = oracle.advance_rk(oracle_bc(case), S, 0.4, 8, order)
+    lev = make_level(ctx, case, (16, 8, 2))
+    lev.set_time_integration(scheme)
+    lev.set_global(case["G"])
+    lev.advance(8, 0.4)
+    tg, _ = lev.time()
+    got = lev.get_global()
+    lev.close()
+    assert tg == pytest.approx(tr, rel=1e-13)
+    assert relerr(got, valid(S)) < 1e-10
+
+
+def test_time_integration_switch_back_is_bit_identical(ctx):
+    """RK2 then back to RK3 on the same level rebuilds the RK3 stage tables: the
+    steps equal a level that never left RK3, bit for bit"""
+    from ocfd.cases import sod
+    case = sod(48, 16, 4)
+    ref, _ = run_gpu(ctx, case, 5, 0.5, (16, 16, 4))
+    lev = make_level(ctx, case, (16, 16, 4))
+    lev.set_time_integration("RK2")
+    lev.set_time_integration(3)
+    lev.set_global(case["G"])
+    lev.advance(5, 0.5)
+    got = lev.get_global()
+    lev.close()
+    assert np.array_equal(got, ref)
