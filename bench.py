@@ -19,7 +19,8 @@ value  = leaf cell-steps (cells not covered by a finer level, times the
          pressure between the forms after 20 coarse steps on identical grids
          (the FP64 run's regrids replayed in the FP32 run)
 e2e    = the same through the C ABI from pinned host buffers: every step uploads
-         every level's state, advances, downloads every level's state
+         every level's state (its valid cells), advances, downloads every
+         level's state
 --impl reference times the reference algorithm on the host CPU cores (the
          oracle port, OpenMP, all threads): RK3 steps of the base grid.
 jet-eb-amr: Mach 2 planar jet past a z-cylinder in 2x1x1, base 256x128x128 +
@@ -452,7 +453,7 @@ def run_ours_jet(args, world, rank, local):
             pins[l] = torch.empty(int(n * 1.5) + 1, dtype=torch.float64).pin_memory()
         return pins[l]
     for l in range(H.nlevels()):
-        H.copy_out(l, pin(l, H.state_elems(l)), stream)
+        H.copy_valid_out(l, pin(l, H.valid_elems(l)), stream)
     torch.cuda.synchronize()
     e2e_steps = max(2, min(args.steps, 5))
     h2d = d2h = 0
@@ -461,13 +462,13 @@ def run_ours_jet(args, world, rank, local):
     e0.record(stream)
     for _ in range(e2e_steps):
         for l in range(H.nlevels()):
-            H.copy_in(l, pins[l], stream)
-            h2d += 8 * H.state_elems(l)
+            H.copy_valid_in(l, pins[l], stream)
+            h2d += 8 * H.valid_elems(l)
         H.advance(1, CFL, ocfd.FLUX_FP32, stream)
         e2e_leaf += H.cell_steps()[0]
         for l in range(H.nlevels()):
-            n = H.state_elems(l)
-            H.copy_out(l, pin(l, n), stream)
+            n = H.valid_elems(l)
+            H.copy_valid_out(l, pin(l, n), stream)
             d2h += 8 * n
     e1.record(stream)
     torch.cuda.synchronize()
@@ -591,7 +592,7 @@ def run_ours_amr(args, world, rank, local):
             pins[l] = torch.empty(int(n * 1.5) + 1, dtype=torch.float64).pin_memory()
         return pins[l]
     for l in range(H.nlevels()):
-        H.copy_out(l, pin(l, H.state_elems(l)), stream)
+        H.copy_valid_out(l, pin(l, H.valid_elems(l)), stream)
     torch.cuda.synchronize()
     e2e_steps = max(2, min(args.steps, 10))
     h2d = d2h = 0
@@ -600,14 +601,14 @@ def run_ours_amr(args, world, rank, local):
     e0.record(stream)
     for _ in range(e2e_steps):
         for l in range(H.nlevels()):
-            n = H.state_elems(l)
-            H.copy_in(l, pins[l], stream)
+            n = H.valid_elems(l)
+            H.copy_valid_in(l, pins[l], stream)
             h2d += 8 * n
         H.advance(1, CFL, flags, stream)
         e2e_leaf += H.cell_steps()[0]
         for l in range(H.nlevels()):
-            n = H.state_elems(l)
-            H.copy_out(l, pin(l, n), stream)
+            n = H.valid_elems(l)
+            H.copy_valid_out(l, pin(l, n), stream)
             d2h += 8 * n
     e1.record(stream)
     torch.cuda.synchronize()
@@ -854,16 +855,18 @@ def run_ours_react(args, world, rank, local):
         if not args.no_surrogate else None
 
     # end to end: upload the state, one step, download, per step
-    flat = Rb.level.copy_out()
+    flat = Rb.level.copy_valid_out()
     pin = torch.from_numpy(flat).pin_memory()
     out = torch.empty_like(pin).pin_memory()
     e2e_steps = max(2, min(args.steps, 5))
     e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(e2e_steps):
-        Rb.level.lib.ocfd_level_copy_in(Rb.level.h, ctypes.c_void_p(pin.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        Rb.level.lib.ocfd_level_copy_valid_in(Rb.level.h, ctypes.c_void_p(pin.data_ptr()),
+                                              ctypes.c_void_p(stream.cuda_stream))
         Rb.advance(1, stream)
-        Rb.level.lib.ocfd_level_copy_out(Rb.level.h, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        Rb.level.lib.ocfd_level_copy_valid_out(Rb.level.h, ctypes.c_void_p(out.data_ptr()),
+                                               ctypes.c_void_p(stream.cuda_stream))
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_value = cells * e2e_steps * world / (allreduce_max(e0.elapsed_time(e1), world) * 1e-3)
@@ -966,19 +969,21 @@ def run_ours(args, world, rank, local):
     fp64 = ctypes.c_double(); fp32 = ctypes.c_double()
     ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
 
-    # end to end through the C ABI with host buffers
-    pin = torch.from_numpy(flat).pin_memory()
+    # end to end through the C ABI with host buffers (the valid cells)
+    lev.copy_in(flat)
+    vflat = lev.copy_valid_out()
+    pin = torch.from_numpy(vflat).pin_memory()
     out = torch.empty_like(pin).pin_memory()
     e2e_steps = max(2, min(args.steps, 10))
-    lev.copy_in(pin, stream)
+    lev.copy_valid_in(pin, stream)
     lev.advance(1, CFL, flags)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(e2e_steps):
-        lev.lib.ocfd_level_copy_in(lev.h, ctypes.c_void_p(pin.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        lev.lib.ocfd_level_copy_valid_in(lev.h, ctypes.c_void_p(pin.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
         lev.advance(1, CFL, flags, stream)
-        lev.lib.ocfd_level_copy_out(lev.h, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        lev.lib.ocfd_level_copy_valid_out(lev.h, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = allreduce_max(e0.elapsed_time(e1) / e2e_steps, world)
@@ -1016,7 +1021,7 @@ def run_ours(args, world, rank, local):
                          "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "cell-steps/s",
-                    "h2d_bytes_per_step": int(flat.nbytes), "d2h_bytes_per_step": int(flat.nbytes)},
+                    "h2d_bytes_per_step": int(vflat.nbytes), "d2h_bytes_per_step": int(vflat.nbytes)},
             "clocks": clk.summary(),
             "gpu_launches": lev.launches_per_step(flags) * args.steps,
         }

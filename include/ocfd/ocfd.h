@@ -279,6 +279,16 @@ ocfd_status ocfd_level_state(ocfd_level* level, int ibox, ocfd_array4* out);
  * boxes back to back in box order, each (ncomp, nz+8, ny+8, nx+8), i fastest). */
 ocfd_status ocfd_level_copy_in(ocfd_level* level, const double* buf, void* stream);
 ocfd_status ocfd_level_copy_out(ocfd_level* level, double* buf, void* stream);
+/* The same for the valid cells only (the level's state without ghost cells, as
+ * an AMReX MultiFab copy of valid regions): `buf` holds box after box in box
+ * order, each (ncomp, nz, ny, nx), i fastest - ocfd_level_valid_elems doubles.
+ * Host buffers go through a device staging list (one copy each way) and a
+ * gather / scatter kernel; device buffers are scattered / gathered directly.
+ * Ghost cells keep their values: every step fills them before it reads them.
+ * copy_valid_in resets the level's time to 0 as ocfd_level_copy_in does. */
+ocfd_status ocfd_level_copy_valid_in(ocfd_level* level, const double* buf, void* stream);
+ocfd_status ocfd_level_copy_valid_out(ocfd_level* level, double* buf, void* stream);
+int64_t ocfd_level_valid_elems(const ocfd_level* level);
 size_t ocfd_level_state_elems(const ocfd_level* level);
 ocfd_status ocfd_level_fill_ghosts(ocfd_level* level, double time, void* stream);
 /* Advance `nsteps` SSP-RK3 steps with CFL number `cfl` (flags: OCFD_VISC,
@@ -515,6 +525,11 @@ ocfd_status ocfd_amr_cell_steps(const ocfd_amr* amr, int64_t* leaf, int64_t* all
 size_t ocfd_amr_state_elems(const ocfd_amr* amr, int lev);
 ocfd_status ocfd_amr_copy_in(ocfd_amr* amr, int lev, const double* buf, void* stream);
 ocfd_status ocfd_amr_copy_out(ocfd_amr* amr, int lev, double* buf, void* stream);
+/* The valid cells of level `lev` only (layout of ocfd_level_copy_valid_in,
+ * ocfd_amr_valid_elems doubles); the hierarchy's clock is left alone. */
+int64_t ocfd_amr_valid_elems(const ocfd_amr* amr, int lev);
+ocfd_status ocfd_amr_copy_valid_in(ocfd_amr* amr, int lev, const double* buf, void* stream);
+ocfd_status ocfd_amr_copy_valid_out(ocfd_amr* amr, int lev, double* buf, void* stream);
 /* Plotfile of the hierarchy's current state: rho, xmom, ymom, zmom, Eden (the
  * state names of Source/Setup.cpp:202-206) and the derived ux, uy, uz and
  * pressure (Source/Setup.cpp:95-110, 164-178); level steps step * 2^lev. */

@@ -1880,6 +1880,23 @@ ocfd_status ocfd_amr_copy_out(ocfd_amr* H, int lev, double* buf, void* stream) {
     return OCFD_OK;
 }
 
+int64_t ocfd_amr_valid_elems(const ocfd_amr* H, int lev) {
+    if (!H || lev < 0 || lev >= H->nlev) return 0;
+    return (int64_t)H->lev[lev].L->ncells * H->lev[lev].L->ncomp;
+}
+
+ocfd_status ocfd_amr_copy_valid_in(ocfd_amr* H, int lev, const double* buf, void* stream) {
+    if (!H || lev < 0 || lev >= H->nlev || !buf) return fail(OCFD_BAD_ARG, "ocfd_amr_copy_valid_in");
+    ocfd_status s = level_copy_valid(H->lev[lev].L, const_cast<double*>(buf), true, static_cast<cudaStream_t>(stream));
+    H->need_estdt = true;
+    return s;
+}
+
+ocfd_status ocfd_amr_copy_valid_out(ocfd_amr* H, int lev, double* buf, void* stream) {
+    if (!H || lev < 0 || lev >= H->nlev || !buf) return fail(OCFD_BAD_ARG, "ocfd_amr_copy_valid_out");
+    return level_copy_valid(H->lev[lev].L, buf, false, static_cast<cudaStream_t>(stream));
+}
+
 int64_t ocfd_amr_kernels_launched(const ocfd_amr* H) { return H ? H->kernel_total : 0; }
 
 }  // extern "C"

@@ -713,6 +713,63 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
     return OCFD_OK;
 }
 
+// Valid cells of every box <-> the dense list `valid` (box after box in box
+// order, each (ncomp, nz, ny, nx), i fastest); to_fab = 1 writes the FABs.
+__global__ void k_valid_copy(const FabGeom* __restrict__ fabs, const long long* __restrict__ cell_start, int nbox,
+                             long long ncells, int ncomp, double* __restrict__ U, double* __restrict__ valid,
+                             int to_fab) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < ncells;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int b = find_tag<FabGeom>(cell_start, nbox, idx);
+        const FabGeom& f = fabs[b];
+        const long long local = idx - cell_start[b];
+        const int nx = f.hi[0] - f.lo[0] + 1, ny = f.hi[1] - f.lo[1] + 1;
+        const long long nb = (long long)nx * ny * (f.hi[2] - f.lo[2] + 1);
+        const int i = f.lo[0] + (int)(local % nx), j = f.lo[1] + (int)((local / nx) % ny),
+                  k = f.lo[2] + (int)(local / ((long long)nx * ny));
+        const long long g = fab_index(f, i, j, k);
+        double* v = valid + cell_start[b] * ncomp + local;
+        if (to_fab)
+            for (int n = 0; n < ncomp; ++n) U[g + n * f.ns] = v[n * nb];
+        else
+            for (int n = 0; n < ncomp; ++n) v[n * nb] = U[g + n * f.ns];
+    }
+}
+
+static bool is_device_pointer(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static ocfd_status valid_staging(ocfd_level* L) {
+    if (L->d_valid) return OCFD_OK;
+    L->d_valid = static_cast<double*>(dev_alloc(sizeof(double) * std::max<long long>(1, L->ncells * L->ncomp), L->pool));
+    return L->d_valid ? OCFD_OK : fail(OCFD_OUT_OF_MEMORY, "level valid-cell staging");
+}
+
+ocfd_status level_copy_valid(ocfd_level* L, double* buf, bool in, cudaStream_t st) {
+    const bool dev = is_device_pointer(buf);
+    if (!dev) {
+        ocfd_status s = valid_staging(L);
+        if (s != OCFD_OK) return s;
+    }
+    const size_t bytes = sizeof(double) * L->ncells * L->ncomp;
+    double* list = dev ? buf : L->d_valid;
+    if (in && !dev && cudaMemcpyAsync(L->d_valid, buf, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return check_launch("valid-cell copy in");
+    if (L->ncells > 0)
+        k_valid_copy<<<grid_for(L->ncells, 256, L->ctx->num_sms), 256, 0, st>>>(
+            L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->ncomp, L->buf[0], list, in ? 1 : 0);
+    ocfd_status s = check_launch("valid-cell copy");
+    if (s == OCFD_OK && !in && !dev && cudaMemcpyAsync(buf, L->d_valid, bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        s = check_launch("valid-cell copy out");
+    return s;
+}
+
 }  // namespace ocfd
 
 extern "C" {
@@ -739,6 +796,7 @@ ocfd_status ocfd_level_destroy(ocfd_level* L) {
     DevPool* pool = L->pool;
     for (int i = 0; i < 4; ++i) dev_free(L->buf[i], pool);
     for (int i = 0; i < NUM_STAGE_SLOTS; ++i) dev_free(L->d_stage[i], pool);
+    dev_free(L->d_valid, pool);
     for (int i = 0; i < 3; ++i) {
         dev_free(L->d_bc[i], pool);
         dev_free(L->d_bc_start[i], pool);
@@ -825,6 +883,23 @@ ocfd_status ocfd_level_copy_in(ocfd_level* L, const double* buf, void* stream) {
     k_set_time<<<1, 1, 0, st>>>(L->d_step, 0.0);
     return check_launch("ocfd_level_copy_in");
 }
+
+ocfd_status ocfd_level_copy_valid_in(ocfd_level* L, const double* buf, void* stream) {
+    if (!L || !buf) return fail(OCFD_BAD_ARG, "ocfd_level_copy_valid_in");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    ocfd_status s = level_copy_valid(L, const_cast<double*>(buf), true, st);
+    if (s != OCFD_OK) return s;
+    L->need_estdt = true;
+    k_set_time<<<1, 1, 0, st>>>(L->d_step, 0.0);
+    return check_launch("ocfd_level_copy_valid_in");
+}
+
+ocfd_status ocfd_level_copy_valid_out(ocfd_level* L, double* buf, void* stream) {
+    if (!L || !buf) return fail(OCFD_BAD_ARG, "ocfd_level_copy_valid_out");
+    return level_copy_valid(L, buf, false, static_cast<cudaStream_t>(stream));
+}
+
+int64_t ocfd_level_valid_elems(const ocfd_level* L) { return L ? (int64_t)L->ncells * L->ncomp : 0; }
 
 ocfd_status ocfd_level_copy_out(ocfd_level* L, double* buf, void* stream) {
     if (!L || !buf) return fail(OCFD_BAD_ARG, "ocfd_level_copy_out");

@@ -273,6 +273,9 @@ struct ocfd_level {
     bool zvirt = false;
     bool zvirt_allowed = false;  // the BCs allow it (the cut-cell stencils do not)
     int zmirror[2] = {0, 0}, zsign[2] = {0, 0};
+    // staging of the valid-cell copies from / to host memory (ncells x ncomp
+    // doubles, allocated on first use)
+    double* d_valid = nullptr;
     // device memory source: nullptr = cudaMalloc / cudaFree (standalone level),
     // else the owning hierarchy's pool (state buffers are then not zeroed)
     ocfd::DevPool* pool = nullptr;
@@ -315,6 +318,9 @@ ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st);
 // kernels one launch_stage call issues
 int stage_launches(const ocfd_level* L, unsigned flags);
 ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st);
+// the valid cells of state A <-> buf (host or device; box after box, (ncomp, nz,
+// ny, nx) each); in = true writes the level
+ocfd_status level_copy_valid(ocfd_level* L, double* buf, bool in, cudaStream_t st);
 ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
                         DevPool* pool = nullptr, int ncomp = 5);
 __global__ void k_set_time(StepState* st, double t);

@@ -47,6 +47,9 @@ declare("ocfd_amr_copy_in", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
 declare("ocfd_amr_copy_out", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
 declare("ocfd_amr_set_eb", ctypes.c_int, [_vp, ctypes.POINTER(EbDesc)])
 declare("ocfd_amr_set_time_integration", ctypes.c_int, [_vp, ctypes.c_int32])
+declare("ocfd_amr_valid_elems", ctypes.c_int64, [_vp, ctypes.c_int])
+declare("ocfd_amr_copy_valid_in", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
+declare("ocfd_amr_copy_valid_out", ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp])
 declare("ocfd_amr_autotune", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int, _vp])
 declare("ocfd_amr_tuned", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)])
 
@@ -243,6 +246,24 @@ class Hierarchy:
             buf = np.empty(self.state_elems(lev))
         ptr = buf.ctypes.data if isinstance(buf, np.ndarray) else buf.data_ptr()
         check(self.lib.ocfd_amr_copy_out(self.h, lev, ctypes.c_void_p(ptr), _stream_ptr(stream)), "amr copy_out")
+        return buf
+
+    def valid_elems(self, lev):
+        return int(self.lib.ocfd_amr_valid_elems(self.h, lev))
+
+    def copy_valid_in(self, lev, buf, stream=None):
+        """buf: host numpy array or CUDA tensor of valid_elems(lev) doubles (the
+        level's valid cells box after box, (5, nz, ny, nx) each)."""
+        ptr = buf.ctypes.data if isinstance(buf, np.ndarray) else buf.data_ptr()
+        check(self.lib.ocfd_amr_copy_valid_in(self.h, lev, ctypes.c_void_p(ptr), _stream_ptr(stream)),
+              "amr copy_valid_in")
+
+    def copy_valid_out(self, lev, buf=None, stream=None):
+        if buf is None:
+            buf = np.empty(self.valid_elems(lev))
+        ptr = buf.ctypes.data if isinstance(buf, np.ndarray) else buf.data_ptr()
+        check(self.lib.ocfd_amr_copy_valid_out(self.h, lev, ctypes.c_void_p(ptr), _stream_ptr(stream)),
+              "amr copy_valid_out")
         return buf
 
     def snapshot(self):

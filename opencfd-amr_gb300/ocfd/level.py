@@ -27,6 +27,9 @@ declare("ocfd_level_state", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(Arr
 declare("ocfd_level_copy_in", ctypes.c_int, [_vp, _vp, _vp])
 declare("ocfd_level_copy_out", ctypes.c_int, [_vp, _vp, _vp])
 declare("ocfd_level_state_elems", ctypes.c_size_t, [_vp])
+declare("ocfd_level_copy_valid_in", ctypes.c_int, [_vp, _vp, _vp])
+declare("ocfd_level_copy_valid_out", ctypes.c_int, [_vp, _vp, _vp])
+declare("ocfd_level_valid_elems", ctypes.c_int64, [_vp])
 declare("ocfd_level_fill_ghosts", ctypes.c_int, [_vp, ctypes.c_double, _vp])
 declare("ocfd_level_advance", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint, _vp])
 declare("ocfd_level_time", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double),
@@ -186,6 +189,32 @@ class Level:
             flat = np.empty(self.elems)
         ptr = flat.ctypes.data if isinstance(flat, np.ndarray) else flat.data_ptr()
         check(self.lib.ocfd_level_copy_out(self.h, ctypes.c_void_p(ptr), _stream_ptr(stream)), "copy_out")
+        self._sync(stream)
+        return flat
+
+    def valid_elems(self):
+        return int(self.lib.ocfd_level_valid_elems(self.h))
+
+    def copy_valid_in(self, flat, stream=None):
+        """flat: host numpy array or CUDA tensor of valid_elems() doubles, the
+        valid cells box after box, (ncomp, nz, ny, nx) each."""
+        n = self.valid_elems()
+        if isinstance(flat, np.ndarray):
+            assert flat.dtype == np.float64 and flat.size == n and flat.flags["C_CONTIGUOUS"]
+            ptr = flat.ctypes.data
+        else:
+            assert flat.numel() == n
+            ptr = flat.data_ptr()
+        check(self.lib.ocfd_level_copy_valid_in(self.h, ctypes.c_void_p(ptr), _stream_ptr(stream)),
+              "copy_valid_in")
+        self._sync(stream)
+
+    def copy_valid_out(self, flat=None, stream=None):
+        if flat is None:
+            flat = np.empty(self.valid_elems())
+        ptr = flat.ctypes.data if isinstance(flat, np.ndarray) else flat.data_ptr()
+        check(self.lib.ocfd_level_copy_valid_out(self.h, ctypes.c_void_p(ptr), _stream_ptr(stream)),
+              "copy_valid_out")
         self._sync(stream)
         return flat
 

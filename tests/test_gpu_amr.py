@@ -159,6 +159,31 @@ def test_dmr_steps_match_oracle_time_integration(ctx, oracle, scheme, order):
         compare_levels(H, A, 1e-11)
 
 
+def test_valid_copies_step_like_fabs(ctx):
+    """every level loaded through copy_valid_in over ghost cells holding garbage
+    steps bit-identically (two coarse steps, a regrid) to the hierarchy restored
+    from its ghost-filled FABs"""
+    case = small_dmr()
+    H = make_hierarchy(ctx, case)
+    H.build(case["fab"])
+    H.advance(1, 0.5)
+    snap = H.snapshot()
+    H.restore(snap)
+    H.advance(2, 0.5)
+    ref = [H.level_global(l) for l in range(H.nlevels())]
+    grids = H.all_grids()
+    H.restore(snap)
+    valid = [H.copy_valid_out(l) for l in range(H.nlevels())]
+    for l in range(H.nlevels()):
+        H.copy_in(l, np.full(H.state_elems(l), 1.0e30))
+        H.copy_valid_in(l, valid[l])
+    H.advance(2, 0.5)
+    assert H.all_grids() == grids
+    for l in range(H.nlevels()):
+        g, m = H.level_global(l)
+        assert (m == ref[l][1]).all() and np.array_equal(g[:, m], ref[l][0][:, m]), l
+
+
 def totals(H):
     g, m = H.level_global(0)
     return g[:, m].sum(axis=1)
