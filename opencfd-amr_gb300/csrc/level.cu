@@ -382,6 +382,8 @@ ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st) 
 
 ocfd_status level_autotune(ocfd_level* L, unsigned flags, int reps, cudaStream_t st) {
     if (L->nreg == 0 || reps <= 0) return OCFD_OK;
+    // the stage tables are rebuilt below: no launch may still read them
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("level autotune");
     const bool visc = flags & OCFD_VISC, f32 = flags & OCFD_FLUX_FP32;
     const StageRoles roles = L->roles ? *L->roles : StageRoles{};
     cudaEvent_t e0, e1;
@@ -838,6 +840,8 @@ ocfd_status ocfd_level_set_schedule(ocfd_level* L, int32_t tile, int32_t sched) 
     L->sched = sched;
     ocfd_status s = OCFD_OK;
     if (tile >= 0 && tile != L->tile) {
+        // the stage tables are rebuilt: no launch may still read them
+        if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_level_set_schedule");
         L->tile = tile;
         const StageRoles roles = L->roles ? *L->roles : StageRoles{};
         s = build_stage_tables(L, roles);
