@@ -415,6 +415,16 @@ ocfd_level* ocfd_react_level(ocfd_react* react);
 ocfd_status ocfd_react_advance(ocfd_react* react, int nsteps, void* stream);
 /* Kernels of one step (the captured graph). */
 int ocfd_react_launches_per_step(const ocfd_react* react);
+/* Cut the reacting level with an embedded body (ocfd_eb_desc, see
+ * ocfd_level_set_eb): the box loop of EBR::compute_dSdt_multi
+ * (Source/CHEM/FlowAdvance.cpp:92-496) - covered boxes get a zero right-hand
+ * side, regular boxes the multispecies chain, cut boxes the cut-cell chain of
+ * ebchem_compute_dSdt_box (Source/CHEM/FlowAdvanceBox.cpp:16-525, FP64 in every
+ * form) on the level's geometry - and the chemistry skips covered boxes
+ * (Source/CHEM/ChemAdvance.cpp:20).  kind OCFD_EB_NONE removes the body.
+ * Synchronous.  ocfd_react_box_classes: OCFD_BOX_* per box. */
+ocfd_status ocfd_react_set_eb(ocfd_react* react, const ocfd_eb_desc* eb);
+ocfd_status ocfd_react_box_classes(const ocfd_react* react, int32_t* cls);
 /* Mean device time of one chemistry substep over the level (the configured
  * form), `reps` substeps of dt/(2 n) applied to the current state. */
 ocfd_status ocfd_react_profile_chem(ocfd_react* react, int reps, double* ms, void* stream);

@@ -1057,6 +1057,40 @@ ocfd_status launch_chem_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cud
     return check_launch("multispecies RHS");
 }
 
+// The cut-cell multispecies chain of one box (ebchem_compute_dSdt_box,
+// Source/CHEM/FlowAdvanceBox.cpp:16-525): primitives over grow(bx, 2),
+// transport, the three directions' MUSCL + Van Leer faces with the species
+// fluxes, the cut-cell divergence; FP64 in every form.
+ocfd_status launch_chem_eb_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cudaStream_t st) {
+    const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
+    const long long qcells = (long long)(n[0] + 2 * B.qg) * (n[1] + 2 * B.qg) * (n[2] + 2 * B.qg);
+    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    k_chem_prims<<<chem_blocks(qcells, 128, sms), 128, 0, st>>>(B, P);
+    if (B.visc) k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
+    k_chem_eb_faces<0><<<chem_blocks((long long)(n[0] + 1) * n[1] * n[2], 128, sms), 128, 0, st>>>(B, P);
+    k_chem_eb_faces<1><<<chem_blocks((long long)n[0] * (n[1] + 1) * n[2], 128, sms), 128, 0, st>>>(B, P);
+    k_chem_eb_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, P);
+    k_chem_eb_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
+    return check_launch("multispecies cut-cell RHS");
+}
+
+void chem_args_as_cut(ChemBoxArgs& B, View<const uint32_t> flag, View<const double> vfrac,
+                      const View<const double> ap[3]) {
+    // the primitives over grow(bx, 2) at the start of the same scratch (the
+    // grow(bx, 3) block of the regular layout holds them)
+    const int g = 2;
+    const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
+    const long long qcells = (long long)(n[0] + 2 * g) * (n[1] + 2 * g) * (n[2] + 2 * g);
+    B.q = View<double>{B.q.p, n[0] + 2 * g, (long long)(n[0] + 2 * g) * (n[1] + 2 * g), qcells, B.lo[0] - g,
+                       B.lo[1] - g, B.lo[2] - g};
+    B.qg = g;
+    B.eb = 1;
+    B.f32 = 0;
+    B.flag = flag;
+    B.vfrac = vfrac;
+    for (int d = 0; d < 3; ++d) B.ap[d] = ap[d];
+}
+
 // Shared set-up of the regular and cut-cell multispecies box calls.
 static ocfd_status chem_box_setup(ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* spec,
                                   const ocfd_array4* dSdt, const ocfd_array4* dSdt_spec,
@@ -1176,18 +1210,7 @@ extern "C" ocfd_status ocfd_rhs_chem_eb_box_f64(ocfd_context* ctx, const ocfd_ar
     B.flag = view_of_flag(flag);
     B.vfrac = view_of<const double>(vfrac);
     for (int d = 0; d < 3; ++d) B.ap[d] = view_of<const double>(ap[d]);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int sms = ctx->num_sms;
-    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
-    const long long qcells = (long long)(n[0] + 2 * B.qg) * (n[1] + 2 * B.qg) * (n[2] + 2 * B.qg);
-    const long long tcells = (long long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
-    k_chem_prims<<<chem_blocks(qcells, 128, sms), 128, 0, st>>>(B, ctx->parm);
-    if (B.visc) k_chem_trans<<<chem_blocks(tcells, 128, sms), 128, 0, st>>>(B);
-    k_chem_eb_faces<0><<<chem_blocks((long long)(n[0] + 1) * n[1] * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
-    k_chem_eb_faces<1><<<chem_blocks((long long)n[0] * (n[1] + 1) * n[2], 128, sms), 128, 0, st>>>(B, ctx->parm);
-    k_chem_eb_faces<2><<<chem_blocks((long long)n[0] * n[1] * (n[2] + 1), 128, sms), 128, 0, st>>>(B, ctx->parm);
-    k_chem_eb_div<<<chem_blocks((long long)n[0] * n[1] * n[2], 256, sms), 256, 0, st>>>(B);
-    return check_launch("ocfd_rhs_chem_eb_box_f64");
+    return launch_chem_eb_rhs(B, ctx->parm, ctx->num_sms, static_cast<cudaStream_t>(stream));
 }
 
 // ------------------------------------------------------------ 0D cells

@@ -55,6 +55,11 @@ size_t chem_rhs_scratch_doubles(const ocfd_box& bx);
 void chem_rhs_args(ChemBoxArgs& B, View<const double> S, View<const double> sp, View<double> dsdt,
                    View<double> dsdts, const ocfd_box& bx, const double dxinv[3], bool visc, double* scr);
 ocfd_status launch_chem_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cudaStream_t st);
+// the cut-cell chain of a box (B.eb set) and the switch of regular arguments
+// (chem_rhs_args) to it: primitive halo 2, the box's cut-cell geometry; FP64
+ocfd_status launch_chem_eb_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cudaStream_t st);
+void chem_args_as_cut(ChemBoxArgs& B, View<const uint32_t> flag, View<const double> vfrac,
+                      const View<const double> ap[3]);
 ocfd_status launch_chem_advance(View<double> S, View<double> sp, const CellBox& B, double dt, const DevParm& P,
                                 cudaStream_t st);
 ocfd_status launch_chem_advance_list(const long long* off, const long long* stride, long long ncell, double* U,

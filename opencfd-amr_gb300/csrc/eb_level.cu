@@ -553,6 +553,20 @@ const uint32_t* eb_box_flag(const ocfd_level* L, int b) {
     return L->eb->d_flag + L->eb->geo[L->eb->geo_of[b]].off_fl;
 }
 
+bool eb_box_views(const ocfd_level* L, int b, View<const uint32_t>& flag, View<const double>& vfrac,
+                  View<const double> ap[3]) {
+    if (!L->eb || L->eb->geo_of[b] < 0 || L->eb->cls[b] != OCFD_BOX_CUT) return false;
+    const EbLevel* E = L->eb;
+    const GeoTag& g = E->geo[E->geo_of[b]];
+    const int b0 = g.lo[0], b1 = g.lo[1];
+    flag = View<const uint32_t>{E->d_flag + g.off_fl, g.gx, 0, 0, b0, b1, 0};
+    vfrac = View<const double>{E->d_geo + g.off_vf, g.gx, 0, 0, b0, b1, 0};
+    ap[0] = View<const double>{E->d_geo + g.off_ax, g.gx + 1, 0, 0, b0, b1, 0};
+    ap[1] = View<const double>{E->d_geo + g.off_ay, g.gx, 0, 0, b0, b1, 0};
+    ap[2] = vfrac;  // bodies extruded along z: the z faces' area fraction is the cell's volume fraction
+    return true;
+}
+
 const double* eb_box_vfrac(const ocfd_level* L, int b, int* gx) {
     if (!L->eb || L->eb->geo_of[b] < 0 || L->eb->cls[b] != OCFD_BOX_CUT) return nullptr;
     const GeoTag& g = L->eb->geo[L->eb->geo_of[b]];

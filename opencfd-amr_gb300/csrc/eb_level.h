@@ -30,5 +30,9 @@ const double* eb_box_vfrac(const ocfd_level* L, int b, int* gx);
 int eb_box_class(const ocfd_level* L, int b);
 // the box's z-invariant flag words over grow(bx, 5) in x, y (nullptr: no data)
 const uint32_t* eb_box_flag(const ocfd_level* L, int b);
+// views of a cut box's z-invariant geometry (kstride 0): flags, volume
+// fraction, area fractions in x, y, z; false when the box has no cut-cell data
+bool eb_box_views(const ocfd_level* L, int b, View<const uint32_t>& flag, View<const double>& vfrac,
+                  View<const double> ap[3]);
 
 }  // namespace ocfd

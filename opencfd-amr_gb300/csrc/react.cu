@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "chem_internal.h"
+#include "eb_level.h"
 #include "level.h"
 
 namespace ocfd {
@@ -134,6 +135,14 @@ struct ocfd_react {
     double* rhs = nullptr;       // L(U_s), same FAB layout
     double* scr = nullptr;       // multispecies RHS scratch of the largest box
     std::vector<ocfd::ChemBoxArgs> args[3];  // RHS chain of each box, per stage input buffer
+    // embedded body: box classes (empty: every box regular) and the boxes the
+    // chemistry visits (EBR::chemical_advance skips covered boxes,
+    // Source/CHEM/ChemAdvance.cpp:20): their FAB table, cell prefix and cells
+    std::vector<int> cls;
+    ocfd::FabGeom* d_afabs = nullptr;
+    long long* d_astart = nullptr;
+    int nabox = 0;
+    long long nactive = 0;
     // binned chemistry
     unsigned char* key = nullptr;
     unsigned* count = nullptr;
@@ -178,7 +187,7 @@ static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
         // cells the guard rejected
         for (int s = 0; s < R->desc.chem_substeps; ++s) {
             cudaMemsetAsync(R->fb_count, 0, sizeof(unsigned), st);
-            ocfd_status r = launch_chem_surrogate(R->mlp, R->off, R->stride, L->ncells, L->buf[0], dt2, R->ctx->parm,
+            ocfd_status r = launch_chem_surrogate(R->mlp, R->off, R->stride, R->nactive, L->buf[0], dt2, R->ctx->parm,
                                                   R->guard, R->fb_off, R->fb_stride, R->fb_count, R->fb_total,
                                                   R->ctx->d_error, sms, st);
             if (r == OCFD_OK)
@@ -191,14 +200,15 @@ static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
     }
     if (R->desc.binned_chem) {
         cudaMemsetAsync(R->count, 0, sizeof(unsigned) * NBIN, st);
-        k_react_keys<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(L->d_fabs, L->d_cell_start, (int)L->boxes.size(),
-                                                                   L->ncells, L->buf[0], R->a0w, R->key, R->count);
+        if (R->nactive == 0) return OCFD_OK;
+        k_react_keys<<<grid_for(R->nactive, 256, sms), 256, 0, st>>>(R->d_afabs, R->d_astart, R->nabox, R->nactive,
+                                                                    L->buf[0], R->a0w, R->key, R->count);
         k_react_scan<<<1, 1, 0, st>>>(R->count);
-        k_react_scatter<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(
-            L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, R->key, R->count, R->off, R->stride);
+        k_react_scatter<<<grid_for(R->nactive, 256, sms), 256, 0, st>>>(R->d_afabs, R->d_astart, R->nabox, R->nactive,
+                                                                       R->key, R->count, R->off, R->stride);
         launches += 3;
         for (int s = 0; s < R->desc.chem_substeps; ++s) {
-            ocfd_status r = launch_chem_advance_list(R->off, R->stride, L->ncells, L->buf[0], dt2, R->ctx->parm, st);
+            ocfd_status r = launch_chem_advance_list(R->off, R->stride, R->nactive, L->buf[0], dt2, R->ctx->parm, st);
             if (r != OCFD_OK) return r;
             ++launches;
         }
@@ -206,6 +216,7 @@ static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
     }
     for (int s = 0; s < R->desc.chem_substeps; ++s)
         for (size_t b = 0; b < L->boxes.size(); ++b) {
+            if (!R->cls.empty() && R->cls[b] == OCFD_BOX_COVERED) continue;
             ocfd_array4 S = fab_view(L, L->buf[0], (int)b, 0, 5), sp = fab_view(L, L->buf[0], (int)b, 5, NSP);
             CellBox cb{};
             for (int d = 0; d < 3; ++d) {
@@ -217,6 +228,58 @@ static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
             ++launches;
         }
     return OCFD_OK;
+}
+
+// The RHS argument blocks of every box for each stage input buffer: the regular
+// chain, or for a cut box the cut-cell chain on the level's geometry
+static void build_args(ocfd_react* R) {
+    ocfd_level* L = R->L;
+    const double dxinv[3] = {1.0 / L->desc.dx[0], 1.0 / L->desc.dx[1], 1.0 / L->desc.dx[2]};
+    for (int in = 0; in < 3; ++in) {
+        R->args[in].clear();
+        for (size_t b = 0; b < L->boxes.size(); ++b) {
+            ocfd_array4 S = fab_view(L, L->buf[in], (int)b, 0, 5), sp = fab_view(L, L->buf[in], (int)b, 5, NSP);
+            ocfd_array4 d = fab_view(L, R->rhs, (int)b, 0, 5), ds = fab_view(L, R->rhs, (int)b, 5, NSP);
+            ChemBoxArgs A{};
+            chem_rhs_args(A, view_of<const double>(&S), view_of<const double>(&sp), view_of<double>(&d),
+                          view_of<double>(&ds), L->boxes[b], dxinv, (R->desc.flags & OCFD_VISC) != 0, R->scr);
+            A.f32 = (R->desc.flags & OCFD_FLUX_FP32) ? 1 : 0;
+            if (!R->cls.empty() && R->cls[b] == OCFD_BOX_CUT) {
+                View<const uint32_t> fl;
+                View<const double> vf, ap[3];
+                if (eb_box_views(L, (int)b, fl, vf, ap)) chem_args_as_cut(A, fl, vf, ap);
+            }
+            R->args[in].push_back(A);
+        }
+    }
+}
+
+// The boxes the chemistry visits (all but the covered ones), their cells, and
+// the identity cell list over them (re-ordered by the binned form every half step)
+static ocfd_status build_active(ocfd_react* R) {
+    ocfd_level* L = R->L;
+    cudaFree(R->d_afabs);
+    cudaFree(R->d_astart);
+    R->d_afabs = nullptr;
+    R->d_astart = nullptr;
+    std::vector<FabGeom> af;
+    std::vector<long long> as;
+    long long n = 0;
+    for (size_t b = 0; b < L->boxes.size(); ++b) {
+        if (!R->cls.empty() && R->cls[b] == OCFD_BOX_COVERED) continue;
+        af.push_back(L->fabs[b]);
+        as.push_back(n);
+        n += region_cells(L->fabs[b].lo, L->fabs[b].hi);
+    }
+    ocfd_status s = upload(&R->d_afabs, af);
+    if (s == OCFD_OK) s = upload(&R->d_astart, as);
+    if (s != OCFD_OK) return s;
+    R->nabox = (int)af.size();
+    R->nactive = n;
+    if (n > 0)
+        k_react_identity<<<grid_for(n, 256, R->ctx->num_sms), 256>>>(R->d_afabs, R->d_astart, R->nabox, n, R->off,
+                                                                    R->stride);
+    return check_launch("reacting level cell list");
 }
 
 static ocfd_status record_react_step(ocfd_react* R, unsigned flags, cudaStream_t st) {
@@ -241,8 +304,10 @@ static ocfd_status record_react_step(ocfd_react* R, unsigned flags, cudaStream_t
         s = fill_ghosts(L, L->buf[in], rk3 ? tf3[k] : tf2[k], st, true);
         launches += (L->ex_total > 0) + (L->bc_total[0] > 0) + (L->bc_total[1] > 0) + (L->bc_total[2] > 0);
         for (size_t b = 0; b < L->boxes.size() && s == OCFD_OK; ++b) {
-            s = launch_chem_rhs(R->args[in][b], R->ctx->parm, sms, st);
-            launches += R->args[in][b].visc ? 6 : 5;
+            const ChemBoxArgs& A = R->args[in][b];
+            if (!R->cls.empty() && R->cls[b] == OCFD_BOX_COVERED) continue;  // dSdt = 0 (Advance.cpp:213-214)
+            s = A.eb ? launch_chem_eb_rhs(A, R->ctx->parm, sms, st) : launch_chem_rhs(A, R->ctx->parm, sms, st);
+            launches += A.visc ? 6 : 5;
         }
         if (s != OCFD_OK) break;
         k_react_combine<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(
@@ -315,10 +380,11 @@ ocfd_status ocfd_react_create(ocfd_context* ctx, const ocfd_react_desc* desc, oc
         return fail(OCFD_OUT_OF_MEMORY, "ocfd_react_create: fallback list");
     }
     cudaMemset(R->fb_total, 0, sizeof(unsigned long long));
-    // the level's cells in box order (re-ordered by the binned form every half step)
-    k_react_identity<<<grid_for(L->ncells, 256, ctx->num_sms), 256>>>(L->d_fabs, L->d_cell_start,
-                                                                       (int)L->boxes.size(), L->ncells, R->off,
-                                                                       R->stride);
+    s = build_active(R);
+    if (s != OCFD_OK) {
+        ocfd_react_destroy(R);
+        return s;
+    }
     // (a0 - 1) Ru / W_i of the Newton start (LiDryer.H:833-888)
     {
         MechTables t;
@@ -328,17 +394,7 @@ ocfd_status ocfd_react_create(ocfd_context* ctx, const ocfd_react_desc* desc, oc
         for (int n = 0; n < NSP; ++n) a0w[n] = t.A0[n] * hp.Ru / t.mw[n];
         cudaMemcpy(R->a0w, a0w, sizeof(a0w), cudaMemcpyHostToDevice);
     }
-    const double dxinv[3] = {1.0 / desc->level.dx[0], 1.0 / desc->level.dx[1], 1.0 / desc->level.dx[2]};
-    for (int in = 0; in < 3; ++in)
-        for (size_t b = 0; b < L->boxes.size(); ++b) {
-            ocfd_array4 S = fab_view(L, L->buf[in], (int)b, 0, 5), sp = fab_view(L, L->buf[in], (int)b, 5, NSP);
-            ocfd_array4 d = fab_view(L, R->rhs, (int)b, 0, 5), ds = fab_view(L, R->rhs, (int)b, 5, NSP);
-            ChemBoxArgs A{};
-            chem_rhs_args(A, view_of<const double>(&S), view_of<const double>(&sp), view_of<double>(&d),
-                          view_of<double>(&ds), L->boxes[b], dxinv, (desc->flags & OCFD_VISC) != 0, R->scr);
-            A.f32 = (desc->flags & OCFD_FLUX_FP32) ? 1 : 0;
-            R->args[in].push_back(A);
-        }
+    build_args(R);
     if (cudaDeviceSynchronize() != cudaSuccess) {
         ocfd_react_destroy(R);
         return check_launch("ocfd_react_create");
@@ -361,6 +417,8 @@ ocfd_status ocfd_react_destroy(ocfd_react* R) {
     cudaFree(R->fb_stride);
     cudaFree(R->fb_count);
     cudaFree(R->fb_total);
+    cudaFree(R->d_afabs);
+    cudaFree(R->d_astart);
     if (R->L) ocfd_level_destroy(R->L);
     delete R;
     return OCFD_OK;
@@ -415,6 +473,33 @@ ocfd_status ocfd_react_fallbacks(ocfd_react* R, int64_t* fallbacks, void* stream
         cudaStreamSynchronize(st) != cudaSuccess)
         return check_launch("ocfd_react_fallbacks");
     *fallbacks = (int64_t)h;
+    return OCFD_OK;
+}
+
+ocfd_status ocfd_react_set_eb(ocfd_react* R, const ocfd_eb_desc* eb) {
+    if (!R || !eb) return fail(OCFD_BAD_ARG, "ocfd_react_set_eb: null argument");
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_react_set_eb");
+    ocfd_level* L = R->L;
+    ocfd_status s = eb_setup(L, *eb);
+    if (s != OCFD_OK) return s;
+    R->cls.clear();
+    if (eb->kind != OCFD_EB_NONE)
+        for (size_t b = 0; b < L->boxes.size(); ++b) R->cls.push_back(eb_box_class(L, (int)b));
+    // covered boxes keep a zero right-hand side
+    if (cudaMemset(R->rhs, 0, sizeof(double) * L->elems) != cudaSuccess) return check_launch("ocfd_react_set_eb");
+    build_args(R);
+    s = build_active(R);
+    if (R->graph) {
+        cudaGraphExecDestroy(R->graph);
+        R->graph = nullptr;
+    }
+    if (s == OCFD_OK && cudaDeviceSynchronize() != cudaSuccess) s = check_launch("ocfd_react_set_eb");
+    return s;
+}
+
+ocfd_status ocfd_react_box_classes(const ocfd_react* R, int32_t* cls) {
+    if (!R || !cls) return fail(OCFD_BAD_ARG, "ocfd_react_box_classes");
+    for (size_t b = 0; b < R->L->boxes.size(); ++b) cls[b] = R->cls.empty() ? OCFD_BOX_REGULAR : R->cls[b];
     return OCFD_OK;
 }
 

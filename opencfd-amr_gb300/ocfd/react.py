@@ -8,7 +8,7 @@ import numpy as np
 
 from ._abi import Box, check, declare, load
 from .context import _stream_ptr
-from .level import Level, LevelDesc
+from .level import EbDesc, Level, LevelDesc
 
 NCOMP = 14
 _vp = ctypes.c_void_p
@@ -25,6 +25,8 @@ declare("ocfd_react_level", _vp, [_vp])
 declare("ocfd_react_advance", ctypes.c_int, [_vp, ctypes.c_int, _vp])
 declare("ocfd_react_launches_per_step", ctypes.c_int, [_vp])
 declare("ocfd_react_profile_chem", ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double), _vp])
+declare("ocfd_react_set_eb", ctypes.c_int, [_vp, ctypes.POINTER(EbDesc)])
+declare("ocfd_react_box_classes", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int32)])
 declare("ocfd_chem_state_tpx", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp])
 
 
@@ -71,6 +73,15 @@ class Reactor:
 
     def advance(self, nsteps, stream=None):
         check(self.lib.ocfd_react_advance(self.h, nsteps, _stream_ptr(stream)), "ocfd_react_advance")
+
+    def set_eb(self, desc):
+        """Cut the level with an embedded body (ocfd.level.eb_desc(...))."""
+        check(self.lib.ocfd_react_set_eb(self.h, ctypes.byref(desc)), "ocfd_react_set_eb")
+
+    def box_classes(self):
+        out = (ctypes.c_int32 * len(self.level.boxes))()
+        check(self.lib.ocfd_react_box_classes(self.h, out), "ocfd_react_box_classes")
+        return list(out)
 
     def launches_per_step(self):
         return int(self.lib.ocfd_react_launches_per_step(self.h))
