@@ -241,7 +241,7 @@ __global__ void k_ebl_prims(EbStageArgs A, DevParm P) {
             B.qf(i, j, k, QV) = uy;
             B.qf(i, j, k, QW) = uz;
             B.qf(i, j, k, QPRES) = p;
-            B.qf(i, j, k, QT) = p * rhoinv * P.f_invRg;
+            // no temperature: the inviscid FP32 faces and the divergence do not read it
             B.qf(i, j, k, QC) = sqrtf(g * p * rhoinv);
         } else {
             double q[7];
@@ -282,6 +282,10 @@ __global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
             float ql[7], qr[7], ff[5];
 #pragma unroll
             for (int m = 0; m < 7; ++m) {
+                if (m == QT) {  // the Van Leer flux does not read the temperature
+                    ql[m] = qr[m] = 0.0f;
+                    continue;
+                }
                 const float* pm = p0 + m * ns;
                 const float vm2 = pm[-2 * sd], vm1 = pm[-sd], v0 = pm[0], vp1 = pm[sd];
                 float l = vm1, r = v0;

@@ -7,8 +7,9 @@
 
 namespace ocfd {
 
-// WENO-Z in FP32.  The stencil values are normalised by the power of two s
-// nearest above their largest magnitude (an exact scaling), and the reference's
+// WENO-Z in FP32.  The stencil values of a face (its f+ and f- stencils) are
+// normalised by the power of two s nearest above their largest magnitude (an
+// exact scaling), and the reference's
 // absolute smoothness epsilon (1e-6, Reconstruction.H:83) is rescaled to the
 // local state as eps / s^2 in the normalised units.  The scheme is therefore
 // the FP64 scheme up to FP32 rounding, and no smoothness indicator can overflow
@@ -17,7 +18,7 @@ namespace ocfd {
 // A face flux is the f+ reconstruction plus the f- one, two independent
 // evaluations of the same expressions: they run as the two lanes of float2
 // values, so that every add / multiply / FMA of the scheme is one packed FP32
-// instruction (sm_100 and later) for both sides.  Only the normalisation, the
+// instruction (sm_100 and later) for both sides.  Only the approximate
 // reciprocals and the ratio cap are per lane.
 
 __device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -26,12 +27,10 @@ __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return _
 __device__ __forceinline__ float2 p_set(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 p_rcp(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
 
-// Normalisation of one side's stencil: scale sc, its inverse and the epsilon in
-// normalised units.  Zero / subnormal stencils, and inf / NaN, are reconstructed
-// as they are (sc = 1, epsilon 1e-6).
-__device__ __forceinline__ void wenoz_scale(float V1, float V2, float V3, float V4, float V5, float& sc,
-                                            float& inv, float& eps) {
-    const float m = fmaxf(fmaxf(fmaxf(fabsf(V1), fabsf(V2)), fmaxf(fabsf(V3), fabsf(V4))), fabsf(V5));
+// Normalisation of a face's two stencils by one power of two: the scale sc,
+// its inverse and the epsilon in normalised units.  Zero / subnormal stencils,
+// and inf / NaN, are reconstructed as they are (sc = 1, epsilon 1e-6).
+__device__ __forceinline__ void wenoz_scale(float m, float& sc, float& inv, float& eps) {
     const int ex = (__float_as_int(m) >> 23) & 0xff;
     const bool plain = ex == 0 || ex > 250;
     sc = plain ? 1.0f : __int_as_float((254 - ex) << 23);   // 2^-(ex-127)
@@ -44,10 +43,11 @@ __device__ __forceinline__ void wenoz_scale(float V1, float V2, float V3, float 
 // stencil): the WENO-Z face flux
 __device__ __forceinline__ float wenoz_pm_f(float a1, float a2, float a3, float a4, float a5, float b1,
                                             float b2, float b3, float b4, float b5) {
-    float sa, ia, ea, sb, ib, eb;
-    wenoz_scale(a1, a2, a3, a4, a5, sa, ia, ea);
-    wenoz_scale(b1, b2, b3, b4, b5, sb, ib, eb);
-    const float2 sc = make_float2(sa, sb), eps = make_float2(ea, eb);
+    const float ma = fmaxf(fmaxf(fmaxf(fabsf(a1), fabsf(a2)), fmaxf(fabsf(a3), fabsf(a4))), fabsf(a5));
+    const float mb = fmaxf(fmaxf(fmaxf(fabsf(b1), fabsf(b2)), fmaxf(fabsf(b3), fabsf(b4))), fabsf(b5));
+    float s, iv, e;
+    wenoz_scale(fmaxf(ma, mb), s, iv, e);
+    const float2 sc = p_set(s), eps = p_set(e);
     const float2 V1 = p_mul(make_float2(a1, b1), sc), V2 = p_mul(make_float2(a2, b2), sc),
                  V3 = p_mul(make_float2(a3, b3), sc), V4 = p_mul(make_float2(a4, b4), sc),
                  V5 = p_mul(make_float2(a5, b5), sc);
@@ -84,8 +84,8 @@ __device__ __forceinline__ float wenoz_pm_f(float a1, float a2, float a3, float 
     const float2 v3 = p_fma(m1, V5, p_fma(c5, V4, p_mul(c2, V3)));
     const float2 num = p_fma(w1, v1, p_fma(w2, v2, p_mul(w3, v3)));
     const float2 den = p_mul(p_set(6.0f), p_add(w1, p_add(w2, w3)));
-    const float2 f = p_mul(p_mul(num, p_rcp(den)), make_float2(ia, ib));
-    return f.x + f.y;
+    const float2 f = p_mul(num, p_rcp(den));
+    return (f.x + f.y) * iv;
 }
 
 // Conversions between FP64 and FP32 on the integer pipes.  GB300 runs FP64
