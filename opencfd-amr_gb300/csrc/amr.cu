@@ -993,6 +993,8 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     return OCFD_OK;
 }
 
+static bool fused_cfl(const ocfd_amr* H, int l) { return l == H->nlev - 1 && !H->has_eb; }
+
 static ocfd_status rebuild_tables(ocfd_amr* H) {
     // blocks of the old tables go back to the pool: nothing may still read them
     if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("AMR table rebuild");
@@ -1000,7 +1002,11 @@ static ocfd_status rebuild_tables(ocfd_amr* H) {
     for (int l = 0; l < H->nlev; ++l) {
         H->lev[l].release_tables(&H->pool);
         H->lev[l].leaf = H->lev[l].L->ncells;
-        roles[l].cfl = false;
+        // the finest level's final state is its last substep's stage output (no
+        // reflux or average-down follows), so its CFL estimate for the next step
+        // is fused into that stage; coarser levels and cut levels are estimated
+        // by a pass over their state at the end of the step
+        roles[l].cfl = fused_cfl(H, l);
         roles[l].out3 = (l < H->nlev - 1) ? 3 : 0;
         if (l < H->nlev - 1) {
             ocfd_status s = ensure_d(H->lev[l].L);
@@ -1132,6 +1138,10 @@ static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cud
         cudaMemsetAsync(A.creg, 0, sizeof(double) * std::max<long long>(1, A.creg_elems), st);
         cudaMemsetAsync(H->lev[l + 1].freg, 0, sizeof(double) * std::max<long long>(1, H->lev[l + 1].freg_elems), st);
     }
+    if (fused_cfl(H, l)) {  // the estimate is the last substep's
+        k_reset_cfl<<<1, 1, 0, st>>>(L->d_step);
+        ++launches_counter;
+    }
     for (int k = 0; k < R.nst && s == OCFD_OK; ++k) {
         double a[4];
         cf_coefs(R.order, k, theta, r, a);
@@ -1168,8 +1178,11 @@ static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cud
     return check_launch("AMR level advance");
 }
 
-static ocfd_status launch_estdt_all(ocfd_amr* H, cudaStream_t st) {
+// CFL estimates of every level from its state (all = false: the levels whose
+// estimate the step's stages did not fuse)
+static ocfd_status launch_estdt_all(ocfd_amr* H, cudaStream_t st, bool all = true) {
     for (int l = 0; l < H->nlev; ++l) {
+        if (!all && fused_cfl(H, l)) continue;
         ocfd_level* L = H->lev[l].L;
         k_estdt_into<<<grid_for(L->ncells, 256, H->ctx->num_sms), 256, 0, st>>>(
             L->d_fabs, L->d_cell_start, (int)L->boxes.size(), L->ncells, L->buf[0], H->ctx->parm, L->desc.dx[0],
@@ -1183,7 +1196,7 @@ static ocfd_status record_amr_step(ocfd_amr* H, unsigned flags, cudaStream_t st)
     launches_counter = 0;
     k_amr_begin<<<1, 1, 0, st>>>(states(H));
     ocfd_status s = advance_level(H, 0, 1, flags, st);
-    if (s == OCFD_OK) s = launch_estdt_all(H, st);
+    if (s == OCFD_OK) s = launch_estdt_all(H, st, false);
     k_amr_end<<<1, 1, 0, st>>>(states(H));
     launches_counter += 2;
     H->launches = launches_counter;

@@ -324,5 +324,6 @@ ocfd_status level_copy_valid(ocfd_level* L, double* buf, bool in, cudaStream_t s
 ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf, ocfd_level** out,
                         DevPool* pool = nullptr, int ncomp = 5);
 __global__ void k_set_time(StepState* st, double t);
+__global__ void k_reset_cfl(StepState* st);
 
 }  // namespace ocfd

@@ -89,3 +89,33 @@ def test_regular_rejects_short_ghosts(ctx):
     with pytest.raises(ocfd.OcfdError) as e:
         ctx.rhs_regular_box(S, dS, (0, 0, 0), (7, 7, 7), [1.0, 1.0, 1.0], S_begin=(-1, -1, -1))
     assert e.value.status == 1
+
+
+def _periodic_grown(core, n):
+    """(5, nz+8, ny+8, nx+8) state of box 0..n-1 (grown by 4) tiled from the
+    8-periodic cell pattern core (5, 8, 8, 8): grown index g holds core[(g-4) % 8]."""
+    reps = [(m + 12) // 8 + 1 for m in (n[2], n[1], n[0])]
+    big = core.repeat(1, *reps)
+    return big[:, 4:12 + n[2], 4:12 + n[1], 4:12 + n[0]].contiguous()
+
+
+@pytest.mark.parametrize("flags", [0, 4])
+def test_large_box_equals_periodic_tile(ctx, flags):
+    """One box of 512 x 256 x 64 cells (8.4 M cells, thousands of tiles in one
+    launch) holding an 8-periodic state: its RHS is the RHS of the 8^3 box with
+    periodic ghosts, tiled, bit for bit in the FP64 and the mixed form (the
+    arithmetic of a cell depends on neither the box nor the tile decomposition)"""
+    import torch
+    P = inputs.ideal_state(8, 8, 8, 11)
+    core = torch.from_numpy(np.ascontiguousarray(P[:, 4:12, 4:12, 4:12])).cuda()
+    dx = [8.0, 8.0, 8.0]
+    Ss = _periodic_grown(core, (8, 8, 8))
+    dSs = torch.empty((5, 8, 8, 8), dtype=torch.float64, device="cuda")
+    ctx.rhs_regular_box(Ss, dSs, (0, 0, 0), (7, 7, 7), dx, flags)
+    n = (512, 256, 64)
+    Sb = _periodic_grown(core, n)
+    dSb = torch.full((5, n[2], n[1], n[0]), float("nan"), dtype=torch.float64, device="cuda")
+    ctx.rhs_regular_box(Sb, dSb, (0, 0, 0), (n[0] - 1, n[1] - 1, n[2] - 1), dx, flags)
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(dSs).all())
+    assert torch.equal(dSb, dSs.repeat(1, n[2] // 8, n[1] // 8, n[0] // 8))
