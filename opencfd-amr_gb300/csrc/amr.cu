@@ -1,4 +1,6 @@
-// AMR hierarchy on the GPU: subcycled SSP-RK3 over levels of ratio 2 with
+// AMR hierarchy on the GPU: subcycled SSP-RK3 (or RK2 / Euler: the rows of
+// rk_scheme, coarse-fine ghosts then interpolated linearly in time between the
+// coarse old and new states) over levels of ratio 2 with
 // coarse-fine ghost interpolation (space and time), flux registers + reflux,
 // average-down, CFL over all levels, density-gradient regridding.
 //

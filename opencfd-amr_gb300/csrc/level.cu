@@ -1,7 +1,8 @@
-// Level driver: box table, device ghost fill, fused SSP-RK3 steps in a CUDA graph.
+// Level driver: box table, device ghost fill, fused RK steps in a CUDA graph.
 //
 // Storage: three state buffers A, B, C holding every box's FAB (box grown by
-// NUM_GROW, components slowest, i fastest), boxes back to back.  A step is
+// NUM_GROW, components slowest, i fastest), boxes back to back.  An SSP-RK3
+// step (the default) is
 //   k_step_begin          dt = min(cfl * CFLmin, 1.1 dt_prev)  (device)
 //   fill(A, t)      stage 1: B = A + dt L(A)
 //   fill(B, t+dt)   stage 2: C = 3/4 A + 1/4 (B + dt L(B))
@@ -9,7 +10,9 @@
 //   k_step_end            t += dt
 // which is the Shu-Osher form of the SSP-RK3 that AmrLevel::RK(3, ...) runs
 // (Source/Advance.cpp:141-148), with the stage times AMReX's RK3 fills ghosts
-// at (t, t+dt, t+dt/2).
+// at (t, t+dt, t+dt/2).  RK2 (Heun) and Euler, the other ebr.time_integration
+// schemes (Source/Advance.cpp:115-138), are the two- and one-stage rows of the
+// same table (rk_scheme).
 //
 // Ghost fill = same-level exchange (incl. periodic images; AMReX FillBoundary)
 // followed by one pass per direction over the ghost cells outside the domain,

@@ -230,7 +230,7 @@ struct ocfd_level {
     std::vector<ocfd::FabGeom> fabs;
     long long elems = 0;      // per state buffer
     int ncomp = 5;
-    // A (U^n), B, C: RK3 stage states; D: end-of-step state of a level that has
+    // A (U^n), B, C: RK stage states; D: end-of-step state of a level that has
     // a finer level (U^n stays in A while the finer level interpolates in time)
     int nbuf = 3;
     double* buf[4] = {nullptr, nullptr, nullptr, nullptr};
