@@ -1,5 +1,7 @@
-// Point-level physics of the ideal-gas path, written for the GPU.  Each
-// function keeps the operation order of the reference expression it replaces,
+// Point-level physics of the ideal-gas path, written for the GPU (and callable
+// on the host: include/ocfd/compat.H builds the reference's per-point functions
+// from them).  Each function keeps the operation order of the reference
+// expression it replaces,
 // so the FP64 kernels agree with the reference to rounding (the parity tests
 // use 1e-12 norm-wise; differences come only from FMA contraction).
 #pragma once
@@ -11,11 +13,11 @@ namespace ocfd {
 enum { URHO = 0, UMX = 1, UMY = 2, UMZ = 3, UEDEN = 4, NCONS = 5 };
 enum { QRHO = 0, QU = 1, QV = 2, QW = 3, QPRES = 4, QT = 5, QC = 6, QGAMA = 7 };
 
-__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
-__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+__host__ __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+__host__ __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
 
 // c2prim, Source/kernel/Kernels.H:13-40.  q = rho, u, v, w, p, T, c.
-__device__ __forceinline__ void c2prim_ideal(const DevParm& P, double u0, double u1, double u2,
+__host__ __device__ __forceinline__ void c2prim_ideal(const DevParm& P, double u0, double u1, double u2,
                                              double u3, double u4, double* q) {
     double rho = dmax(u0, P.smallr);
     double rhoinv = 1.0 / rho;
@@ -38,7 +40,7 @@ __device__ __forceinline__ void c2prim_ideal(const DevParm& P, double u0, double
 // T = double keeps the reference's expressions; T = float serves the
 // mixed-precision form.
 template <int D, class T = double>
-__device__ __forceinline__ void sw_split(T d, T u, T v, T w, T c, T t1, T t2, T t3, T gm1, T* fp,
+__host__ __device__ __forceinline__ void sw_split(T d, T u, T v, T w, T c, T t1, T t2, T t3, T gm1, T* fp,
                                          T* fm) {
     const T vel[3] = {u, v, w};
     const T un = vel[D];
@@ -74,7 +76,7 @@ __device__ __forceinline__ void sw_split(T d, T u, T v, T w, T c, T t1, T t2, T 
 }
 
 // WENO-Z, Source/kernel/Reconstruction.H:83-138: f+ stencil at cells i-3..i+1
-__device__ __forceinline__ double wenoz_plus(double V1, double V2, double V3, double V4, double V5) {
+__host__ __device__ __forceinline__ double wenoz_plus(double V1, double V2, double V3, double V4, double V5) {
     const double eps = 1e-6;
     double s11 = (13.0 / 12.0) * (V1 - 2.0 * V2 + V3) * (V1 - 2.0 * V2 + V3) +
                  0.25 * (V1 - 4.0 * V2 + 3.0 * V3) * (V1 - 4.0 * V2 + 3.0 * V3);
@@ -94,7 +96,7 @@ __device__ __forceinline__ double wenoz_plus(double V1, double V2, double V3, do
 }
 
 // ... and the mirrored f- stencil at cells i-2..i+2
-__device__ __forceinline__ double wenoz_minus(double V1, double V2, double V3, double V4, double V5) {
+__host__ __device__ __forceinline__ double wenoz_minus(double V1, double V2, double V3, double V4, double V5) {
     const double eps = 1e-6;
     double s11 = (13.0 / 12.0) * (V5 - 2.0 * V4 + V3) * (V5 - 2.0 * V4 + V3) +
                  0.25 * (V5 - 4.0 * V4 + 3.0 * V3) * (V5 - 4.0 * V4 + 3.0 * V3);
@@ -113,7 +115,7 @@ __device__ __forceinline__ double wenoz_minus(double V1, double V2, double V3, d
     return (1.0 / 6.0) * invsum * (a1 * v1 + a2 * v2 + a3 * v3);
 }
 
-__device__ __forceinline__ double sutherland(const DevParm& P, double T) {
+__host__ __device__ __forceinline__ double sutherland(const DevParm& P, double T) {
     return P.C_s * T * sqrt(T) / (T + P.T_s);
 }
 
