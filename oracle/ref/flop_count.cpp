@@ -1,0 +1,121 @@
+// Operation counts of OpenCFD-AMR's ideal-gas point functions (test and
+// measurement infrastructure; make -C oracle flops).  The reference's kernel
+// headers are compiled unmodified with amrex::Real = CountedReal
+// (oracle/shim/flop_real.H); each function is called once at one point of a
+// small state and the tally it leaves is printed as JSON.  The algorithmic
+// FLOPs of one cell's right-hand side follow the chain of
+// Source/Advance.cpp:245-329 per cell: c2prim once, the Steger-Warming split once
+// per direction, WENO-Z for 5 components on one face per direction, the
+// viscous flux on one face per direction, divop for 5 components.
+#include <AMReX_FArrayBox.H>
+#include <IndexDefines.H>
+#include <Constants.H>
+#include <Kernels.H>
+#include <FluxSplit.H>
+#include <Reconstruction.H>
+#include <Diffusion.H>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+using amrex::Array4;
+using amrex::Dim3;
+using amrex::Real;
+
+namespace {
+
+constexpr int NG = 4, N = 2 * NG + 1;  // a 9^3 block around cell (0, 0, 0)
+
+struct Block {
+    std::vector<Real> data;
+    Array4<Real> a;
+    explicit Block(int nc) : data((size_t)nc * N * N * N) {
+        a = Array4<Real>(data.data(), N, N * N, (long long)N * N * N, Dim3{-NG, -NG, -NG}, Dim3{NG + 1, NG + 1, NG + 1},
+                         nc);
+    }
+};
+
+FlopTally since(const FlopTally& t0) {
+    const FlopTally& t = flop_tally();
+    FlopTally d;
+    d.add = t.add - t0.add;
+    d.mul = t.mul - t0.mul;
+    d.div = t.div - t0.div;
+    d.sqrt = t.sqrt - t0.sqrt;
+    d.cmp = t.cmp - t0.cmp;
+    d.other = t.other - t0.other;
+    return d;
+}
+
+void put(const char* name, const FlopTally& d, bool last = false) {
+    std::printf("  \"%s\": {\"add\": %lld, \"mul\": %lld, \"div\": %lld, \"sqrt\": %lld, \"cmp\": %lld, "
+                "\"other\": %lld}%s\n",
+                name, d.add, d.mul, d.div, d.sqrt, d.cmp, d.other, last ? "" : ",");
+}
+
+}  // namespace
+
+int main() {
+    Parm parm;
+    parm.Rg = parm.Ru / parm.eos_m;
+    parm.cp = parm.eos_gamma * parm.Rg / (parm.eos_gamma - 1.0);
+    parm.cv = parm.cp / parm.eos_gamma;
+    parm.kOverMu = parm.cp / parm.Pr;
+    Block u(NCONS), q(NPRIM), fp(NCONS), fm(NCONS), fx(NCONS), fy(NCONS), fz(NCONS), dsdt(NCONS);
+    // a smooth state: rho 1 +, velocity and pressure of order one
+    for (int k = -NG; k <= NG; ++k)
+        for (int j = -NG; j <= NG; ++j)
+            for (int i = -NG; i <= NG; ++i) {
+                const double r = 1.0 + 0.01 * (i + 2 * j + 3 * k + 20), vx = 0.3, vy = -0.2, vz = 0.1, p = 1.0;
+                u.a(i, j, k, URHO) = r;
+                u.a(i, j, k, UMX) = r * vx;
+                u.a(i, j, k, UMY) = r * vy;
+                u.a(i, j, k, UMZ) = r * vz;
+                u.a(i, j, k, UEDEN) = p / 0.4 + 0.5 * r * (vx * vx + vy * vy + vz * vz);
+            }
+    Array4<Real const> uc = u.a;
+    for (int k = -NG; k <= NG; ++k)
+        for (int j = -NG; j <= NG; ++j)
+            for (int i = -NG; i <= NG; ++i) c2prim(i, j, k, uc, q.a, parm);
+    Array4<Real const> qc = q.a;
+    amrex::GpuArray<Real, 3> dxinv{{Real(64.0), Real(64.0), Real(64.0)}};
+    std::printf("{\n");
+    FlopTally t0 = flop_tally();
+    c2prim(0, 0, 0, uc, q.a, parm);
+    put("c2prim", since(t0));
+    const char* split_names[3] = {"flux_split_x", "flux_split_y", "flux_split_z"};
+    const char* recon_names[3] = {"reconstruction_x", "reconstruction_y", "reconstruction_z"};
+    const char* visc_names[3] = {"compute_visc_x", "compute_visc_y", "compute_visc_z"};
+    for (int d = 0; d < 3; ++d) {
+        for (int k = -NG; k <= NG; ++k)
+            for (int j = -NG; j <= NG; ++j)
+                for (int i = -NG; i <= NG; ++i) {
+                    if (d == 0) flux_split_x(i, j, k, fp.a, fm.a, qc, uc, parm);
+                    if (d == 1) flux_split_y(i, j, k, fp.a, fm.a, qc, uc, parm);
+                    if (d == 2) flux_split_z(i, j, k, fp.a, fm.a, qc, uc, parm);
+                }
+        t0 = flop_tally();
+        if (d == 0) flux_split_x(0, 0, 0, fp.a, fm.a, qc, uc, parm);
+        if (d == 1) flux_split_y(0, 0, 0, fp.a, fm.a, qc, uc, parm);
+        if (d == 2) flux_split_z(0, 0, 0, fp.a, fm.a, qc, uc, parm);
+        put(split_names[d], since(t0));
+        Array4<Real const> fpc = fp.a, fmc = fm.a;
+        t0 = flop_tally();
+        if (d == 0) reconstruction_x(0, 0, 0, 0, fpc, fmc, fx.a, parm);
+        if (d == 1) reconstruction_y(0, 0, 0, 0, fpc, fmc, fy.a, parm);
+        if (d == 2) reconstruction_z(0, 0, 0, 0, fpc, fmc, fz.a, parm);
+        put(recon_names[d], since(t0));
+        t0 = flop_tally();
+        if (d == 0) compute_visc_x(0, 0, 0, qc, fx.a, dxinv, parm);
+        if (d == 1) compute_visc_y(0, 0, 0, qc, fy.a, dxinv, parm);
+        if (d == 2) compute_visc_z(0, 0, 0, qc, fz.a, dxinv, parm);
+        put(visc_names[d], since(t0));
+    }
+    Array4<Real const> fxc = fx.a, fyc = fy.a, fzc = fz.a;
+    t0 = flop_tally();
+    divop(0, 0, 0, 0, dsdt.a, fxc, fyc, fzc, dxinv);
+    put("divop", since(t0), true);
+    std::printf("}\n");
+    return 0;
+}

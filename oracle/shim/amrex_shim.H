@@ -28,9 +28,17 @@
 #define AMREX_SPACEDIM 3
 #define AMREX_DEVICE_PRINTF(...) std::printf(__VA_ARGS__)
 
+#ifdef OCFD_COUNT_FLOPS
+#include "flop_real.H"
+#endif
+
 namespace amrex {
 
+#ifdef OCFD_COUNT_FLOPS
+using Real = CountedReal;
+#else
 using Real = double;
+#endif
 
 namespace literals {
 inline constexpr Real operator""_rt(long double x) { return Real(x); }

@@ -176,3 +176,26 @@ def test_reference_chemical_test_program(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True, cwd=str(tmp_path)).stdout
     assert "rho = 0.963512265437802995" in out
     assert "E = 245428.076382951345" in out
+
+
+def test_reference_flop_counts():
+    """Operation counts of the reference's ideal-gas point functions, from its
+    own headers compiled with a counting Real (make -C oracle flops); these are
+    the algorithmic FLOPs per cell-stage quoted for the roofline."""
+    import json
+    if not os.path.isdir("/root/reference/Source"):
+        pytest.skip("reference sources not present on this machine")
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "flops"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "flop_count")], capture_output=True, text=True)
+    c = json.loads(out.stdout)
+    flops = {k: v["add"] + v["mul"] + v["div"] + v["sqrt"] for k, v in c.items()}
+    assert flops["c2prim"] == 19 and c["c2prim"]["div"] == 2 and c["c2prim"]["sqrt"] == 1
+    for d in "xyz":
+        assert flops["flux_split_" + d] == 103
+        assert flops["reconstruction_" + d] == 191 and c["reconstruction_" + d]["div"] == 14
+        assert flops["compute_visc_" + d] == 68
+    assert flops["divop"] == 8
+    per_cell = flops["c2prim"] + sum(flops["flux_split_" + d] + 5 * flops["reconstruction_" + d] for d in "xyz") \
+        + 5 * flops["divop"]
+    assert per_cell == 3233
