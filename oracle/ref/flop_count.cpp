@@ -1,5 +1,6 @@
-// Operation counts of OpenCFD-AMR's ideal-gas point functions (test and
-// measurement infrastructure; make -C oracle flops).  The reference's kernel
+// Operation counts of OpenCFD-AMR's point functions (test and measurement
+// infrastructure; make -C oracle flops builds this ideal-gas and, with -DCHEM
+// and Source/Constants.cpp, multispecies).  The reference's kernel
 // headers are compiled unmodified with amrex::Real = CountedReal
 // (oracle/shim/flop_real.H); each function is called once at one point of a
 // small state and the tally it leaves is printed as JSON.  The algorithmic
@@ -14,6 +15,10 @@
 #include <FluxSplit.H>
 #include <Reconstruction.H>
 #include <Diffusion.H>
+#ifdef CHEM
+#include <LiDryer.H>
+#include <ChemViscous.H>
+#endif
 
 #include <cstdio>
 #include <string>
@@ -56,7 +61,98 @@ void put(const char* name, const FlopTally& d, bool last = false) {
 
 }  // namespace
 
+#ifdef CHEM
+// The multispecies build: one cell of H2/air (phi = 1) at 1500 K, 1 atm, with a
+// few radicals.  Counts of the temperature inversion (its Newton iteration count
+// depends on the state), the production rates with their Jacobian, the
+// elimination, the whole implicit substep (the lambda of
+// Source/CHEM/ChemAdvance.cpp:27-82, restated as the reference driver does) and
+// the mixture-averaged transport of one cell.
+int chem_main() {
+    Parm parm;
+    parm.Initialize();
+    const Parm* lparm = &parm;
+    Real X[NSPECS] = {0.28, 0.14, 0.02, 0.002, 0.001, 0.004, 0.0005, 0.0001, 0.0};
+    Real xs = 0.0;
+    for (int n = 0; n < NSPECS - 1; ++n) xs += X[n];
+    X[NSPECS - 1] = 1.0 - xs;
+    Real Y[NSPECS], rho, e, rhoi[NSPECS];
+    CKXTY(X, Y, parm);
+    CKRHOY(Real(101325.0), Real(1500.0), Y, rho, parm);
+    for (int n = 0; n < NSPECS; ++n) rhoi[n] = rho * Y[n];
+    CKUBMS(Real(1500.0), rhoi, e, parm);
+    const Real ei = e, dt = 1.25e-9;
+    std::printf("{\n");
+    FlopTally t0 = flop_tally();
+    Real T;
+    {
+        Real r[NSPECS];
+        for (int n = 0; n < NSPECS; ++n) r[n] = rhoi[n];
+        GET_T_GIVEN_EY(ei, r, T, parm);
+    }
+    put("get_t_given_ey", since(t0));
+    Real cc[NSPECS], wdot[NSPECS], Arate[NSPECS][NSPECS];
+    for (int n = 0; n < NSPECS; n++) cc[n] = rhoi[n] / lparm->mw[n] * 1e-6;
+    t0 = flop_tally();
+    vproductionRate(wdot, Arate, cc, T, parm);
+    put("vproductionRate", since(t0));
+    Real A1[NSPECS][NSPECS], b[NSPECS], x[NSPECS];
+    for (int i = 0; i < NSPECS; ++i) {
+        b[i] = wdot[i];
+        for (int j = 0; j < NSPECS; ++j) A1[i][j] = (i == j ? 1.0 : 0.0) - Arate[i][j] * 1e-9;
+    }
+    t0 = flop_tally();
+    gauss(x, A1, b);
+    put("gauss", since(t0));
+    // the whole substep of one cell (state at rest)
+    t0 = flop_tally();
+    {
+        Real rhoi_0[NSPECS], wd[NSPECS], c2[NSPECS], Ar[NSPECS][NSPECS], B1[NSPECS][NSPECS], rhoi_1[NSPECS],
+            drho[NSPECS], T2, dei = 0;
+        const Real rr = amrex::max(rho, lparm->smallr);
+        const Real rhoinv = Real(1.0) / rr;
+        const Real ux = Real(0.0) * rhoinv, uy = Real(0.0) * rhoinv, uz = Real(0.0) * rhoinv;
+        const Real kineng = Real(0.5) * (ux * ux + uy * uy + uz * uz);
+        Real e2 = ei - rr * kineng;
+        for (int n = 0; n < NSPECS; ++n) rhoi_0[n] = rhoi[n];
+        GET_T_GIVEN_EY(e2, rhoi_0, T2, *lparm);
+        for (int n = 0; n < NSPECS; n++) c2[n] = rhoi_0[n] / lparm->mw[n] * 1e-6;
+        vproductionRate(wd, Ar, c2, T2, *lparm);
+        for (int i = 0; i < NSPECS; ++i)
+            for (int j = 0; j < NSPECS; ++j) {
+                B1[i][j] = (i == j ? 1.0 : 0.0);
+                B1[i][j] -= Ar[i][j] * lparm->mw[i] / lparm->mw[j] * dt;
+            }
+        for (int n = 0; n < NSPECS; ++n) rhoi_1[n] = wd[n] * lparm->mw[n] * 1e6 * dt;
+        gauss(drho, B1, rhoi_1);
+        Real out[NSPECS];
+        for (int n = 0; n < NSPECS; ++n) {
+            out[n] = rhoi_0[n] + drho[n];
+            if (out[n] < 0) out[n] = Real(0.0);
+        }
+        for (int n = 0; n < NSPECS; ++n) dei += -lparm->HP[n] * lparm->Ru / lparm->mw[n] * drho[n];
+        (void)out;
+        (void)dei;
+    }
+    put("chemical_advance_cell", since(t0));
+    Real mu, lam;
+    t0 = flop_tally();
+    mixtureProperties(T, X, mu, lam, parm);
+    put("mixtureProperties", since(t0));
+    std::vector<Real> Dv(NSPECS);
+    Array4<Real> D(Dv.data(), 1, 1, 1, Dim3{0, 0, 0}, Dim3{1, 1, 1}, NSPECS);
+    t0 = flop_tally();
+    getMixDiffCoeffsMass(0, 0, 0, T, Real(101325.0), X, D, parm);
+    put("getMixDiffCoeffsMass", since(t0), true);
+    std::printf("}\n");
+    return 0;
+}
+#endif
+
 int main() {
+#ifdef CHEM
+    return chem_main();
+#endif
     Parm parm;
     parm.Rg = parm.Ru / parm.eos_m;
     parm.cp = parm.eos_gamma * parm.Rg / (parm.eos_gamma - 1.0);

@@ -25,8 +25,14 @@ struct CountedReal {
     CountedReal& operator*=(CountedReal o) { ++flop_tally().mul; v *= o.v; return *this; }
     CountedReal& operator/=(CountedReal o) { ++flop_tally().div; v /= o.v; return *this; }
     CountedReal operator-() const { return CountedReal(-v); }  // a sign flip, not counted
-    explicit operator double() const { return v; }
+    // the reference keeps some intermediates in plain double (LiDryer.H)
+    operator double() const { return v; }
 };
+
+inline double& operator+=(double& a, CountedReal b) { ++flop_tally().add; a += b.v; return a; }
+inline double& operator-=(double& a, CountedReal b) { ++flop_tally().add; a -= b.v; return a; }
+inline double& operator*=(double& a, CountedReal b) { ++flop_tally().mul; a *= b.v; return a; }
+inline double& operator/=(double& a, CountedReal b) { ++flop_tally().div; a /= b.v; return a; }
 
 #define OCFD_FLOP_BINOP(OP, FIELD)                                                                         \
     inline CountedReal operator OP(CountedReal a, CountedReal b) { ++flop_tally().FIELD; return CountedReal(a.v OP b.v); } \
@@ -55,7 +61,10 @@ inline CountedReal abs(CountedReal a) { return CountedReal(std::fabs(a.v)); }  /
 inline CountedReal fabs(CountedReal a) { return CountedReal(std::fabs(a.v)); }
 inline CountedReal exp(CountedReal a) { ++flop_tally().other; return CountedReal(std::exp(a.v)); }
 inline CountedReal log(CountedReal a) { ++flop_tally().other; return CountedReal(std::log(a.v)); }
+inline CountedReal log10(CountedReal a) { ++flop_tally().other; return CountedReal(std::log10(a.v)); }
 inline CountedReal pow(CountedReal a, CountedReal b) { ++flop_tally().other; return CountedReal(std::pow(a.v, b.v)); }
+inline CountedReal pow(double a, CountedReal b) { ++flop_tally().other; return CountedReal(std::pow(a, b.v)); }
+inline CountedReal pow(CountedReal a, double b) { ++flop_tally().other; return CountedReal(std::pow(a.v, b)); }
 inline CountedReal cos(CountedReal a) { ++flop_tally().other; return CountedReal(std::cos(a.v)); }
 inline CountedReal sin(CountedReal a) { ++flop_tally().other; return CountedReal(std::sin(a.v)); }
 
@@ -65,6 +74,10 @@ inline CountedReal sqrt(CountedReal a) { return ::sqrt(a); }
 inline CountedReal abs(CountedReal a) { return ::abs(a); }
 inline CountedReal exp(CountedReal a) { return ::exp(a); }
 inline CountedReal log(CountedReal a) { return ::log(a); }
+inline CountedReal log10(CountedReal a) { return ::log10(a); }
+inline CountedReal pow(CountedReal a, CountedReal b) { return ::pow(a, b); }
+inline CountedReal pow(double a, CountedReal b) { return ::pow(a, b); }
+inline CountedReal pow(CountedReal a, double b) { return ::pow(a, b); }
 inline CountedReal cos(CountedReal a) { return ::cos(a); }
 inline CountedReal sin(CountedReal a) { return ::sin(a); }
 }  // namespace std

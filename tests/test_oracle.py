@@ -199,3 +199,9 @@ def test_reference_flop_counts():
     per_cell = flops["c2prim"] + sum(flops["flux_split_" + d] + 5 * flops["reconstruction_" + d] for d in "xyz") \
         + 5 * flops["divop"]
     assert per_cell == 3233
+    out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "flop_count_chem")], capture_output=True, text=True)
+    c = json.loads(out.stdout)
+    step = c["chemical_advance_cell"]
+    # one implicit substep of an H2/air cell at 1500 K: ~9.9 k FLOPs, ~1000 of them
+    # divisions, 47 exp / log / pow
+    assert step["add"] + step["mul"] + step["div"] == 9869 and step["div"] == 995 and step["other"] == 47
