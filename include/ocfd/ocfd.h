@@ -346,7 +346,9 @@ ocfd_status ocfd_level_set_time_integration(ocfd_level* level, int32_t order);
  * a level are batched: three launches per RK stage (primitives, faces of all
  * three directions, divergence fused with the RK stage update and the CFL
  * bound) beside the regular boxes' launch, inside the same step graph.  The
- * cut-cell scheme runs in FP64 in every form.
+ * cut-cell scheme runs in FP64 in the plain form; with OCFD_FLUX_FP32 (inviscid)
+ * its primitives, face states, Van Leer flux and divergence are FP32 and the RK
+ * stage update stays FP64.
  *
  * AMReX's EB2 (Source/Geometry.cpp:9-29) is absent: the geometry is built on
  * the device from an implicit function by sub-sampling - flags with the
@@ -442,7 +444,7 @@ ocfd_status ocfd_chem_state_tpx(ocfd_context* ctx, int64_t n, const double* T, c
  *     level with MC-limited conservative linear slopes, in time from the coarse
  *     SSP-RK3 stage states (the role of FillPatch / FillPatcher::fillRK under
  *     AmrLevel::RK, Source/Advance.cpp:141-148; Source/Setup.cpp:194-196),
- *   - flux registers collect the RK3-weighted face fluxes on both sides of each
+ *   - flux registers collect the RK-weighted face fluxes on both sides of each
  *     coarse-fine face and reflux the uncovered coarse cells
  *     (EBFluxRegister CrseAdd / FineAdd / Reflux, Source/Advance.cpp:344-360,
  *     Source/EBR.cpp:322-330),

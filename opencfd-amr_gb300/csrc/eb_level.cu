@@ -8,7 +8,7 @@
 // of the level run as one batch per RK stage:
 //   k_ebl_prims       primitives over grow(bx, 2) of every cut box     (c2prim)
 //   k_ebl_faces       every face of every cut box in x, y and z: MUSCL-minmod
-//                     states, Van Leer flux, EB viscous flux; RK3-weighted
+//                     states, Van Leer flux, EB viscous flux; RK-weighted
 //                     area-fraction fluxes into the flux registers (AMR)
 //   k_ebl_div_stage   per cell: cut-cell divergence with the wall flux, negated
 //                     (zero in covered boxes), fused with the Shu-Osher stage
