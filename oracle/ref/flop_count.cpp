@@ -62,6 +62,8 @@ void put(const char* name, const FlopTally& d, bool last = false) {
 }  // namespace
 
 #ifdef CHEM
+amrex::GpuArray<Real, 3> dxinv_of(const Parm&) { return amrex::GpuArray<Real, 3>{{Real(1e4), Real(1e4), Real(1e4)}}; }
+
 // The multispecies build: one cell of H2/air (phi = 1) at 1500 K, 1 atm, with a
 // few radicals.  Counts of the temperature inversion (its Newton iteration count
 // depends on the state), the production rates with their Jacobian, the
@@ -143,7 +145,98 @@ int chem_main() {
     Array4<Real> D(Dv.data(), 1, 1, 1, Dim3{0, 0, 0}, Dim3{1, 1, 1}, NSPECS);
     t0 = flop_tally();
     getMixDiffCoeffsMass(0, 0, 0, T, Real(101325.0), X, D, parm);
-    put("getMixDiffCoeffsMass", since(t0), true);
+    put("getMixDiffCoeffsMass", since(t0));
+
+    // The multispecies right-hand side of Source/CHEM/FlowAdvance.cpp:157-403 on a
+    // 9^3 block of this mixture (slightly varied, moving): the per-cell pieces
+    Block u(NCONS), sp(NSPECS), q(NPRIM), mub(1), lamb(1), Db(NSPECS), fp(NCONS), fm(NCONS), fps(NSPECS),
+        fms(NSPECS), fx(NCONS), fxs(NSPECS), fxd(NSPECS), ds(NCONS), dss(NSPECS);
+    for (int k = -NG; k <= NG; ++k)
+        for (int j = -NG; j <= NG; ++j)
+            for (int i = -NG; i <= NG; ++i) {
+                const double f = 1.0 + 0.002 * (i + 2 * j + 3 * k);
+                Real r = 0.0;
+                for (int n = 0; n < NSPECS; ++n) {
+                    sp.a(i, j, k, n) = rhoi[n] * f;
+                    r += rhoi[n] * f;
+                }
+                u.a(i, j, k, URHO) = r;
+                u.a(i, j, k, UMX) = r * 30.0;
+                u.a(i, j, k, UMY) = r * -20.0;
+                u.a(i, j, k, UMZ) = r * 10.0;
+                u.a(i, j, k, UEDEN) = e * f + 0.5 * r * 1400.0;
+            }
+    Array4<Real const> uc = u.a, spc = sp.a;
+    for (int k = -NG; k <= NG; ++k)
+        for (int j = -NG; j <= NG; ++j)
+            for (int i = -NG; i <= NG; ++i) {
+                c2prim_rgas(i, j, k, uc, spc, q.a, parm);
+                Real Yt[NSPECS], Xt[NSPECS];
+                for (int n = 0; n < NSPECS; ++n) Yt[n] = sp.a(i, j, k, n) / q.a(i, j, k, QRHO);
+                CKYTX(Yt, Xt, parm);
+                mixtureProperties(q.a(i, j, k, QT), Xt, mub.a(i, j, k), lamb.a(i, j, k), parm);
+                Array4<Real> Dij(&Db.a(i, j, k, 0), 1, 1, Db.a.nstride, Dim3{i, j, k}, Dim3{i + 1, j + 1, k + 1},
+                                 NSPECS);
+                getMixDiffCoeffsMass(i, j, k, q.a(i, j, k, QT), q.a(i, j, k, QPRES), Xt, Dij, parm);
+            }
+    Array4<Real const> qc = q.a, muc = mub.a, lamc = lamb.a, Dc = Db.a;
+    t0 = flop_tally();
+    c2prim_rgas(0, 0, 0, uc, spc, q.a, parm);
+    put("c2prim_rgas", since(t0));
+    t0 = flop_tally();
+    {
+        Real Yt[NSPECS], Xt[NSPECS], m1, l1;
+        for (int n = 0; n < NSPECS; ++n) Yt[n] = sp.a(0, 0, 0, n) / q.a(0, 0, 0, QRHO);
+        CKYTX(Yt, Xt, parm);
+        mixtureProperties(q.a(0, 0, 0, QT), Xt, m1, l1, parm);
+        std::vector<Real> D1(NSPECS);
+        Array4<Real> Da(D1.data(), 1, 1, 1, Dim3{0, 0, 0}, Dim3{1, 1, 1}, NSPECS);
+        getMixDiffCoeffsMass(0, 0, 0, q.a(0, 0, 0, QT), q.a(0, 0, 0, QPRES), Xt, Da, parm);
+    }
+    put("transport_cell", since(t0));
+    for (int k = -NG; k <= NG; ++k)
+        for (int j = -NG; j <= NG; ++j)
+            for (int i = -NG; i <= NG; ++i) flux_split_x(i, j, k, fp.a, fm.a, qc, uc, parm);
+    t0 = flop_tally();
+    flux_split_x(0, 0, 0, fp.a, fm.a, qc, uc, parm);
+    put("flux_split_x_chem", since(t0));
+    // the species split lambda of Source/CHEM/FlowAdvance.cpp:214-242, restated
+    auto spec_split = [&](int i, int j, int k) {
+        Real un = q.a(i, j, k, QU), c = q.a(i, j, k, QC), gamma = q.a(i, j, k, QGAMA);
+        Real E1 = un, E2 = un - c, E3 = un + c;
+        Real E1P = (E1 + amrex::Math::abs(E1)) * Real(0.5);
+        Real E2P = (E2 + amrex::Math::abs(E2)) * Real(0.5);
+        Real E3P = (E3 + amrex::Math::abs(E3)) * Real(0.5);
+        Real E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
+        Real tmp1 = Real(1.0) / (Real(2.0) * gamma);
+        Real tmp2 = Real(2.0) * (gamma - Real(1.0));
+        Real tmp2_p = tmp2 * E1P + E2P + E3P;
+        Real tmp2_m = tmp2 * E1M + E2M + E3M;
+        for (int n = 0; n < NSPECS; ++n) {
+            Real tmp0 = sp.a(i, j, k, n) * tmp1;
+            fps.a(i, j, k, n) = tmp0 * tmp2_p;
+            fms.a(i, j, k, n) = tmp0 * tmp2_m;
+        }
+    };
+    for (int k = -NG; k <= NG; ++k)
+        for (int j = -NG; j <= NG; ++j)
+            for (int i = -NG; i <= NG; ++i) spec_split(i, j, k);
+    t0 = flop_tally();
+    spec_split(0, 0, 0);
+    put("species_split_x", since(t0));
+    Array4<Real const> fpc = fp.a, fmc = fm.a, fpsc = fps.a, fmsc = fms.a;
+    t0 = flop_tally();
+    reconstruction_x(0, 0, 0, 0, fpc, fmc, fx.a, parm);
+    put("reconstruction_x_chem", since(t0));
+    t0 = flop_tally();
+    diffusion_x(0, 0, 0, qc, spc, Dc, fxs.a, fxd.a, dxinv_of(parm));
+    put("diffusion_x", since(t0));
+    Array4<Real const> fxdc = fxd.a;
+    t0 = flop_tally();
+    compute_visc_x_multi(0, 0, 0, qc, spc, lamc, muc, fx.a, fxdc, dxinv_of(parm), parm);
+    put("compute_visc_x_multi", since(t0), true);
+    (void)ds;
+    (void)dss;
     std::printf("}\n");
     return 0;
 }

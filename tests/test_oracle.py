@@ -205,3 +205,10 @@ def test_reference_flop_counts():
     # one implicit substep of an H2/air cell at 1500 K: ~9.9 k FLOPs, ~1000 of them
     # divisions, 47 exp / log / pow
     assert step["add"] + step["mul"] + step["div"] == 9869 and step["div"] == 995 and step["other"] == 47
+    # the viscous multispecies RHS of one cell (Source/CHEM/FlowAdvance.cpp:157-403):
+    # c2prim_rgas and transport once, per direction the splits, 14 components'
+    # WENO-Z, the diffusive and viscous fluxes, then divop on 14 components
+    f = {k: v["add"] + v["mul"] + v["div"] + v["sqrt"] for k, v in c.items()}
+    per_dir = f["flux_split_x_chem"] + f["species_split_x"] + 14 * f["reconstruction_x_chem"] + f["diffusion_x"] \
+        + f["compute_visc_x_multi"]
+    assert f["c2prim_rgas"] + f["transport_cell"] + 3 * per_dir + 14 * 8 == 13708
