@@ -165,10 +165,11 @@ ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S, const o
  * (2^21 doubles), held by every GPU that loads the library until exit; a box
  * needing more (7 (nx+4)(ny+4)(nz+4) doubles, plus 5 per face of the three face
  * boxes when flux is NULL) is rejected with OCFD_BAD_ARG.  It allocates nothing.
- * The first call on a device looks up the array's device address (the
- * context's device must be current); make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race and
- * must be serialised by the caller. */
+ * ocfd_context_create looks up the array's device address for its device and
+ * loads the device code of this call, so the array is resident from context
+ * creation on and no call loads anything; the context's device must be current
+ * at each call.  All calls share the array, which keeps what the last call left:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
 ocfd_status ocfd_rhs_eb_box_f64_static_scratch(
     ocfd_context* ctx, const ocfd_array4* S, const ocfd_array4* dSdt, const ocfd_array4* flux,
     const ocfd_flag4* flag, const ocfd_array4* vfrac, const ocfd_array4* apx,

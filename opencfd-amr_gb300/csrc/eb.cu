@@ -10,7 +10,6 @@
 // in registers of the face thread.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "eb_physics.cuh"
@@ -156,38 +155,53 @@ static int blocks_for(long long n, int threads, int sms) {
 
 using namespace ocfd;
 
-extern "C" ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S,
-                                           const ocfd_array4* dSdt, const ocfd_array4* flux,
-                                           const ocfd_flag4* flag, const ocfd_array4* vfrac,
-                                           const ocfd_array4* apx, const ocfd_array4* apy,
-                                           const ocfd_array4* apz, const ocfd_array4* const* fc,
-                                           const ocfd_array4* bcent, ocfd_box bx,
-                                           const double dxinv[3], unsigned flags, void* stream) {
-    (void)fc;
-    (void)bcent;
-    if (!ctx || !dxinv) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: null argument");
+namespace ocfd {
+
+// Argument checks and scratch size of one cut-cell box (shared by both entry
+// points, so that they accept and reject exactly the same boxes).
+struct EbBoxPlan {
+    int n[3];
+    long long gcells, fcells[3];
+    long long need;  // scratch doubles: primitives over grow(bx, 2), + face fluxes without `flux`
+};
+
+static ocfd_status eb_box_check(const char* who, ocfd_context* ctx, const ocfd_array4* S,
+                                const ocfd_array4* dSdt, const ocfd_array4* flux, const ocfd_flag4* flag,
+                                const ocfd_array4* vfrac, const ocfd_array4* const ap[3], ocfd_box bx,
+                                const double dxinv[3], unsigned flags, EbBoxPlan* plan) {
+    const std::string w(who);
+    if (!ctx || !dxinv) return fail(OCFD_BAD_ARG, w + ": null argument");
     for (int d = 0; d < 3; ++d)
-        if (bx.hi[d] < bx.lo[d]) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: empty box");
-    if (!covers(S, bx, 2, 5)) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: S must cover grow(bx,2)");
-    if (!covers(dSdt, bx, 0, 5)) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: dSdt must cover bx");
-    if (!covers_flag(flag, bx, 1)) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: flag must cover grow(bx,1)");
-    if (!covers(vfrac, bx, 0, 1)) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: vfrac must cover bx");
-    const ocfd_array4* ap[3] = {apx, apy, apz};
+        if (bx.hi[d] < bx.lo[d]) return fail(OCFD_BAD_ARG, w + ": empty box");
+    if (!covers(S, bx, 2, 5)) return fail(OCFD_BAD_ARG, w + ": S must cover grow(bx,2)");
+    if (!covers(dSdt, bx, 0, 5)) return fail(OCFD_BAD_ARG, w + ": dSdt must cover bx");
+    if (!covers_flag(flag, bx, 1)) return fail(OCFD_BAD_ARG, w + ": flag must cover grow(bx,1)");
+    if (!covers(vfrac, bx, 0, 1)) return fail(OCFD_BAD_ARG, w + ": vfrac must cover bx");
     for (int d = 0; d < 3; ++d)
-        if (!covers(ap[d], bx, 0, 1, d)) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: area fractions must cover surroundingNodes(bx,d)");
+        if (!covers(ap[d], bx, 0, 1, d))
+            return fail(OCFD_BAD_ARG, w + ": area fractions must cover surroundingNodes(bx,d)");
     if (flux)
         for (int d = 0; d < 3; ++d)
-            if (!covers(&flux[d], bx, 0, 5, d)) return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: flux[d]");
-    if (flags & ~(unsigned)(OCFD_VISC | OCFD_REDISTRIBUTE))
-        return fail(OCFD_BAD_ARG, "ocfd_rhs_eb_box_f64: unsupported flags");
-    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
-    const long long gcells = (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
-    long long fcells[3];
-    for (int d = 0; d < 3; ++d) fcells[d] = (long long)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
-    size_t need = sizeof(double) * 7 * gcells;
-    if (!flux) need += sizeof(double) * 5 * (fcells[0] + fcells[1] + fcells[2]);
-    double* scr = static_cast<double*>(scratch(ctx, need));
-    if (!scr) return fail(OCFD_OUT_OF_MEMORY, "ocfd_rhs_eb_box_f64: scratch");
+            if (!covers(&flux[d], bx, 0, 5, d)) return fail(OCFD_BAD_ARG, w + ": flux[d]");
+    if (flags & ~(unsigned)(OCFD_VISC | OCFD_REDISTRIBUTE)) return fail(OCFD_BAD_ARG, w + ": unsupported flags");
+    for (int d = 0; d < 3; ++d) plan->n[d] = bx.hi[d] - bx.lo[d] + 1;
+    const int* n = plan->n;
+    plan->gcells = (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
+    for (int d = 0; d < 3; ++d)
+        plan->fcells[d] = (long long)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
+    plan->need = 7 * plan->gcells;
+    if (!flux) plan->need += 5 * (plan->fcells[0] + plan->fcells[1] + plan->fcells[2]);
+    return OCFD_OK;
+}
+
+// The kernel chain of one cut-cell box (primitives, three face passes,
+// divergence) with its scratch at `scr` (plan.need doubles).
+static ocfd_status eb_box_launch(const char* who, ocfd_context* ctx, const ocfd_array4* S,
+                                 const ocfd_array4* dSdt, const ocfd_array4* flux, const ocfd_flag4* flag,
+                                 const ocfd_array4* vfrac, const ocfd_array4* const ap[3], ocfd_box bx,
+                                 const double dxinv[3], unsigned flags, const EbBoxPlan& plan, double* scr,
+                                 void* stream) {
+    const int* n = plan.n;
     EbBoxArgs B{};
     B.S = view_of<const double>(S);
     B.dsdt = view_of<double>(dSdt);
@@ -199,28 +213,49 @@ extern "C" ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4*
         B.hi[d] = bx.hi[d];
         B.dxinv[d] = dxinv[d];
     }
-    B.q = View<double>{scr, n[0] + 4, (long long)(n[0] + 4) * (n[1] + 4), gcells,
+    B.q = View<double>{scr, n[0] + 4, (long long)(n[0] + 4) * (n[1] + 4), plan.gcells,
                        bx.lo[0] - 2, bx.lo[1] - 2, bx.lo[2] - 2};
-    double* fp = scr + 7 * gcells;
+    double* fp = scr + 7 * plan.gcells;
     for (int d = 0; d < 3; ++d) {
         if (flux) {
             B.flux[d] = view_of<double>(&flux[d]);
         } else {
             const int sx = n[0] + (d == 0), sy = n[1] + (d == 1);
-            B.flux[d] = View<double>{fp, sx, (long long)sx * sy, fcells[d], bx.lo[0], bx.lo[1], bx.lo[2]};
-            fp += 5 * fcells[d];
+            B.flux[d] = View<double>{fp, sx, (long long)sx * sy, plan.fcells[d], bx.lo[0], bx.lo[1], bx.lo[2]};
+            fp += 5 * plan.fcells[d];
         }
     }
     B.visc = (flags & OCFD_VISC) != 0;
     B.redist = (flags & OCFD_REDISTRIBUTE) != 0;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int T = 256, sms = ctx->num_sms;
-    k_eb_prims<<<blocks_for(gcells, T, sms), T, 0, st>>>(B, ctx->parm);
-    k_eb_faces<0><<<blocks_for(fcells[0], T, sms), T, 0, st>>>(B, ctx->parm);
-    k_eb_faces<1><<<blocks_for(fcells[1], T, sms), T, 0, st>>>(B, ctx->parm);
-    k_eb_faces<2><<<blocks_for(fcells[2], T, sms), T, 0, st>>>(B, ctx->parm);
+    k_eb_prims<<<blocks_for(plan.gcells, T, sms), T, 0, st>>>(B, ctx->parm);
+    k_eb_faces<0><<<blocks_for(plan.fcells[0], T, sms), T, 0, st>>>(B, ctx->parm);
+    k_eb_faces<1><<<blocks_for(plan.fcells[1], T, sms), T, 0, st>>>(B, ctx->parm);
+    k_eb_faces<2><<<blocks_for(plan.fcells[2], T, sms), T, 0, st>>>(B, ctx->parm);
     k_eb_div<<<blocks_for((long long)n[0] * n[1] * n[2], T, sms), T, 0, st>>>(B, ctx->parm);
-    return check_launch("ocfd_rhs_eb_box_f64");
+    return check_launch(who);
+}
+
+}  // namespace ocfd
+
+extern "C" ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4* S,
+                                           const ocfd_array4* dSdt, const ocfd_array4* flux,
+                                           const ocfd_flag4* flag, const ocfd_array4* vfrac,
+                                           const ocfd_array4* apx, const ocfd_array4* apy,
+                                           const ocfd_array4* apz, const ocfd_array4* const* fc,
+                                           const ocfd_array4* bcent, ocfd_box bx,
+                                           const double dxinv[3], unsigned flags, void* stream) {
+    (void)fc;
+    (void)bcent;
+    const char* who = "ocfd_rhs_eb_box_f64";
+    const ocfd_array4* ap[3] = {apx, apy, apz};
+    EbBoxPlan plan{};
+    ocfd_status s = eb_box_check(who, ctx, S, dSdt, flux, flag, vfrac, ap, bx, dxinv, flags, &plan);
+    if (s != OCFD_OK) return s;
+    double* scr = static_cast<double*>(scratch(ctx, sizeof(double) * (size_t)plan.need));
+    if (!scr) return fail(OCFD_OUT_OF_MEMORY, std::string(who) + ": scratch");
+    return eb_box_launch(who, ctx, S, dSdt, flux, flag, vfrac, ap, bx, dxinv, flags, plan, scr, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -231,17 +266,21 @@ extern "C" ocfd_status ocfd_rhs_eb_box_f64(ocfd_context* ctx, const ocfd_array4*
 // a memory-capped service) and must not see allocations appear behind their
 // back, and code paths where a cudaMalloc / cudaFree - which can synchronise
 // the whole device - would stall other streams at the wrong moment.  This
-// variant runs the same three kernels as ocfd_rhs_eb_box_f64 but takes its
-// scratch (cell primitives, and the face fluxes when the caller passes no flux
-// arrays) from a fixed array compiled into the library, so it allocates
-// nothing at any call.
+// variant runs the same kernel chain as ocfd_rhs_eb_box_f64 (primitives, three
+// face passes, divergence) but takes its scratch (cell primitives, and the face
+// fluxes when the caller passes no flux arrays) from a fixed array compiled
+// into the library, so it allocates nothing at any call.
 //
 // The array is kEbStaticScratchDoubles doubles (16 MiB) and is held by every
-// GPU that loads the library until the process exits.  All calls share it and
-// it keeps whatever the last call left there: calls that overlap on the GPU
-// (different streams, or different host threads) race on it and must be
-// serialised by the caller.  Nothing in it has to start at zero - every value
-// a kernel reads was written earlier in the same call.
+// GPU that loads the library until the process exits.  Its device address is
+// looked up when a context is created (eb_static_scratch_resolve, called by
+// ocfd_context_create with the context's device current); that lookup loads
+// this file's device code, so the array is resident before the first call and
+// no call can trigger a lazy module load.  All calls share it and it keeps
+// whatever the last call left there: calls that overlap on the GPU (different
+// streams, or different host threads) race on it and must be serialised by
+// the caller.  Nothing in it has to start at zero - every value a kernel reads
+// was written earlier in the same call.
 // ---------------------------------------------------------------------------
 namespace ocfd {
 
@@ -249,24 +288,26 @@ constexpr long long kEbStaticScratchDoubles = 2LL * 1024 * 1024;
 
 static __device__ __align__(256) double g_eb_static_scratch[kEbStaticScratchDoubles];
 
-// Device address of g_eb_static_scratch, looked up once per device (the host
-// symbol is only a stand-in for the device array and must not be passed to a
-// kernel).
-static std::mutex g_eb_static_mutex;
-static double* g_eb_static_ptr[64] = {nullptr};
-
-static ocfd_status eb_static_scratch(int device, double** out) {
-    if (device < 0 || device >= 64) return fail(OCFD_BAD_ARG, "static scratch: device index out of range");
-    std::lock_guard<std::mutex> lock(g_eb_static_mutex);
-    if (!g_eb_static_ptr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_eb_static_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(OCFD_LAUNCH_FAIL, std::string("static scratch: cudaGetSymbolAddress failed: ") +
-                                              cudaGetErrorString(e));
-        g_eb_static_ptr[device] = static_cast<double*>(p);
+// In host code g_eb_static_scratch names a host-side stand-in, not the device
+// array: a kernel must be given the address cudaGetSymbolAddress returns.
+// With lazy module loading the lookup also loads this file's device code, and
+// the attribute queries load the five kernels of the chain, so that no later
+// call has code or data of this file to bring onto the device.
+ocfd_status eb_static_scratch_resolve(ocfd_context* ctx) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_eb_static_scratch);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_eb_prims);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_eb_faces<0>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_eb_faces<1>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_eb_faces<2>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_eb_div);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return fail(OCFD_LAUNCH_FAIL, std::string("static scratch: device code of the cut-cell box not loadable: ") +
+                                          cudaGetErrorString(e));
     }
-    *out = g_eb_static_ptr[device];
+    ctx->eb_static_scratch = static_cast<double*>(p);
     return OCFD_OK;
 }
 
@@ -280,30 +321,12 @@ extern "C" ocfd_status ocfd_rhs_eb_box_f64_static_scratch(
     (void)fc;
     (void)bcent;
     const char* who = "ocfd_rhs_eb_box_f64_static_scratch";
-    if (!ctx || !dxinv) return fail(OCFD_BAD_ARG, std::string(who) + ": null argument");
-    for (int d = 0; d < 3; ++d)
-        if (bx.hi[d] < bx.lo[d]) return fail(OCFD_BAD_ARG, std::string(who) + ": empty box");
-    if (!covers(S, bx, 2, 5)) return fail(OCFD_BAD_ARG, std::string(who) + ": S must cover grow(bx,2)");
-    if (!covers(dSdt, bx, 0, 5)) return fail(OCFD_BAD_ARG, std::string(who) + ": dSdt must cover bx");
-    if (!covers_flag(flag, bx, 1)) return fail(OCFD_BAD_ARG, std::string(who) + ": flag must cover grow(bx,1)");
-    if (!covers(vfrac, bx, 0, 1)) return fail(OCFD_BAD_ARG, std::string(who) + ": vfrac must cover bx");
     const ocfd_array4* ap[3] = {apx, apy, apz};
-    for (int d = 0; d < 3; ++d)
-        if (!covers(ap[d], bx, 0, 1, d))
-            return fail(OCFD_BAD_ARG, std::string(who) + ": area fractions must cover surroundingNodes(bx,d)");
-    if (flux)
-        for (int d = 0; d < 3; ++d)
-            if (!covers(&flux[d], bx, 0, 5, d)) return fail(OCFD_BAD_ARG, std::string(who) + ": flux[d]");
-    if (flags & ~(unsigned)(OCFD_VISC | OCFD_REDISTRIBUTE))
-        return fail(OCFD_BAD_ARG, std::string(who) + ": unsupported flags");
-    const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
-    const long long gcells = (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
-    long long fcells[3];
-    for (int d = 0; d < 3; ++d) fcells[d] = (long long)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
-    long long need = 7 * gcells;
-    if (!flux) need += 5 * (fcells[0] + fcells[1] + fcells[2]);
-    if (need > kEbStaticScratchDoubles)
-        return fail(OCFD_BAD_ARG, std::string(who) + ": box needs " + std::to_string(need) +
+    EbBoxPlan plan{};
+    ocfd_status s = eb_box_check(who, ctx, S, dSdt, flux, flag, vfrac, ap, bx, dxinv, flags, &plan);
+    if (s != OCFD_OK) return s;
+    if (plan.need > kEbStaticScratchDoubles)
+        return fail(OCFD_BAD_ARG, std::string(who) + ": box needs " + std::to_string(plan.need) +
                                       " scratch doubles, the static scratch holds " +
                                       std::to_string(kEbStaticScratchDoubles) +
                                       " (pass flux arrays or split the box)");
@@ -311,40 +334,7 @@ extern "C" ocfd_status ocfd_rhs_eb_box_f64_static_scratch(
     if (cudaGetDevice(&dev) != cudaSuccess) return check_launch(who);
     if (dev != ctx->device)
         return fail(OCFD_BAD_ARG, std::string(who) + ": the context's device must be the current device");
-    double* scr = nullptr;
-    ocfd_status s = eb_static_scratch(dev, &scr);
-    if (s != OCFD_OK) return s;
-    EbBoxArgs B{};
-    B.S = view_of<const double>(S);
-    B.dsdt = view_of<double>(dSdt);
-    B.flag = view_of_flag(flag);
-    B.vfrac = view_of<const double>(vfrac);
-    for (int d = 0; d < 3; ++d) {
-        B.ap[d] = view_of<const double>(ap[d]);
-        B.lo[d] = bx.lo[d];
-        B.hi[d] = bx.hi[d];
-        B.dxinv[d] = dxinv[d];
-    }
-    B.q = View<double>{scr, n[0] + 4, (long long)(n[0] + 4) * (n[1] + 4), gcells,
-                       bx.lo[0] - 2, bx.lo[1] - 2, bx.lo[2] - 2};
-    double* fp = scr + 7 * gcells;
-    for (int d = 0; d < 3; ++d) {
-        if (flux) {
-            B.flux[d] = view_of<double>(&flux[d]);
-        } else {
-            const int sx = n[0] + (d == 0), sy = n[1] + (d == 1);
-            B.flux[d] = View<double>{fp, sx, (long long)sx * sy, fcells[d], bx.lo[0], bx.lo[1], bx.lo[2]};
-            fp += 5 * fcells[d];
-        }
-    }
-    B.visc = (flags & OCFD_VISC) != 0;
-    B.redist = (flags & OCFD_REDISTRIBUTE) != 0;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int T = 256, sms = ctx->num_sms;
-    k_eb_prims<<<blocks_for(gcells, T, sms), T, 0, st>>>(B, ctx->parm);
-    k_eb_faces<0><<<blocks_for(fcells[0], T, sms), T, 0, st>>>(B, ctx->parm);
-    k_eb_faces<1><<<blocks_for(fcells[1], T, sms), T, 0, st>>>(B, ctx->parm);
-    k_eb_faces<2><<<blocks_for(fcells[2], T, sms), T, 0, st>>>(B, ctx->parm);
-    k_eb_div<<<blocks_for((long long)n[0] * n[1] * n[2], T, sms), T, 0, st>>>(B, ctx->parm);
-    return check_launch(who);
+    if (!ctx->eb_static_scratch) return fail(OCFD_LAUNCH_FAIL, std::string(who) + ": static scratch not resolved");
+    return eb_box_launch(who, ctx, S, dSdt, flux, flag, vfrac, ap, bx, dxinv, flags, plan, ctx->eb_static_scratch,
+                         stream);
 }

@@ -55,6 +55,7 @@ struct ocfd_context {
     void* scratch = nullptr;       // scratch pool owned by the context
     size_t scratch_bytes = 0;
     int num_sms = 0;
+    double* eb_static_scratch = nullptr;  // device address of the allocation-free variant's array
 };
 
 namespace ocfd {
@@ -70,5 +71,10 @@ bool covers_flag(const ocfd_flag4* a, const ocfd_box& bx, int grow);
 
 // Ensures the context scratch pool holds at least `bytes`; returns its pointer.
 void* scratch(ocfd_context* ctx, size_t bytes);
+
+// Looks up the device address of the allocation-free cut-cell entry point's
+// static array for ctx's device (which must be current); loads eb.cu's device
+// code, so that the array is resident from context creation on.
+ocfd_status eb_static_scratch_resolve(ocfd_context* ctx);
 
 }  // namespace ocfd

@@ -349,7 +349,6 @@ class AmrOracle:
         A = L["U"]
         bufs = [A, A.copy(), A.copy(), A.copy() if has_child else None]
         L["bufs"] = bufs
-        mask = L["mask"]
         parent = self.levels[l - 1]["bufs"] if l > 0 else None
         if has_child:
             L["creg"] = [0.0, 0.0, 0.0]
@@ -364,15 +363,18 @@ class AmrOracle:
             dS, F = self._rhs_level(l, S, has_child or l > 0)
             dt = L["dt"]
             O = bufs[out_of[k]]
-            vs = (slice(None), slice(NG, -NG), slice(NG, -NG), slice(NG, -NG))
-            u0 = A[vs][:, mask]
-            us = S[vs][:, mask]
-            if self.rk == 3:
-                O[vs][:, mask] = RK_A[k] * u0 + RK_B[k] * (us + dt * dS[:, mask])
-            elif k == 0:
-                O[vs][:, mask] = 1.0 * us + dt * dS[:, mask]
-            else:
-                O[vs][:, mask] = (0.5 * us + 0.5 * u0) + (0.5 * dt) * dS[:, mask]
+            # box by box over the valid cells (the boxes of a level are disjoint;
+            # the same elementwise arithmetic as over the level's valid mask)
+            for lo, hi in L["boxes"]:
+                gs = (slice(None),) + _sl(lo, hi, NG)
+                vs = (slice(None),) + _sl(lo, hi)
+                u0, us = A[gs], S[gs]
+                if self.rk == 3:
+                    O[gs] = RK_A[k] * u0 + RK_B[k] * (us + dt * dS[vs])
+                elif k == 0:
+                    O[gs] = 1.0 * us + dt * dS[vs]
+                else:
+                    O[gs] = (0.5 * us + 0.5 * u0) + (0.5 * dt) * dS[vs]
             w = sch["w"][k] * dt
             if has_child:
                 L["creg"] = [L["creg"][d] + w * F[d] for d in range(3)]

@@ -1481,29 +1481,37 @@ void ocfdo_fill_ghosts(const ocfdo_bc* bc, double* S, int ncomp, int nx, int ny,
             lo[t] = t < d ? -NG : 0;
             hi[t] = t < d ? n3[t] + NG : n3[t];
         }
+        /* transverse directions, the slower one outermost (the inner loop walks
+         * the faster index; every write is a distinct ghost cell and every read
+         * a cell that is not a ghost in direction d, so the order is free) */
+        const int ta = (d + 1) % 3 > (d + 2) % 3 ? (d + 1) % 3 : (d + 2) % 3;
+        const int tb = 3 - d - ta;
         for (int side = 0; side < 2; ++side) {
             int phys = side == 0 ? bc->lo_bc[d] : bc->hi_bc[d];
             for (int gcell = 0; gcell < NG; ++gcell) {
                 int gi_d = side == 0 ? -1 - gcell : n3[d] + gcell;
                 for (int n = 0; n < ncomp; ++n) {
                     int t = comp_bc(phys, n, d);
-                    for (int a = lo[(d + 1) % 3]; a < hi[(d + 1) % 3]; ++a)
-                        for (int bb = lo[(d + 2) % 3]; bb < hi[(d + 2) % 3]; ++bb) {
+                    if (t != BC_INT_DIR && t != BC_FOEXTRAP && t != BC_REFLECT_EVEN && t != BC_REFLECT_ODD)
+                        continue; /* ext_dir: left to the case functor */
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+                    for (int a = lo[ta]; a < hi[ta]; ++a)
+                        for (int bb = lo[tb]; bb < hi[tb]; ++bb) {
                             int idx[3];
                             idx[d] = gi_d;
-                            idx[(d + 1) % 3] = a;
-                            idx[(d + 2) % 3] = bb;
+                            idx[ta] = a;
+                            idx[tb] = bb;
                             int src[3] = {idx[0], idx[1], idx[2]};
                             double sign = 1.0;
                             if (t == BC_INT_DIR) {
                                 src[d] = side == 0 ? gi_d + n3[d] : gi_d - n3[d];
                             } else if (t == BC_FOEXTRAP) {
                                 src[d] = side == 0 ? 0 : n3[d] - 1;
-                            } else if (t == BC_REFLECT_EVEN || t == BC_REFLECT_ODD) {
+                            } else {
                                 src[d] = side == 0 ? -1 - gi_d : 2 * n3[d] - 1 - gi_d;
                                 if (t == BC_REFLECT_ODD) sign = -1.0;
-                            } else {
-                                continue; /* ext_dir: left to the case functor */
                             }
                             S[n * N + gI(&b, idx[0], idx[1], idx[2])] =
                                 sign * S[n * N + gI(&b, src[0], src[1], src[2])];
@@ -1513,19 +1521,25 @@ void ocfdo_fill_ghosts(const ocfdo_bc* bc, double* S, int ncomp, int nx, int ny,
         }
         if (bc->dirichlet_case == 3 && d == 0 && bc->lo_bc[0] == 1) {
             for (int gcell = 0; gcell < NG; ++gcell)
-                for (int a = lo[1]; a < hi[1]; ++a)
-                    for (int bb = lo[2]; bb < hi[2]; ++bb) jet_fill(bc, S, N, &b, -1 - gcell, a, bb, ncomp);
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+                for (int bb = lo[2]; bb < hi[2]; ++bb)
+                    for (int a = lo[1]; a < hi[1]; ++a) jet_fill(bc, S, N, &b, -1 - gcell, a, bb, ncomp);
         }
         if (bc->dirichlet_case == 1) {
             for (int side = 0; side < 2; ++side)
                 for (int gcell = 0; gcell < NG; ++gcell) {
                     int gi_d = side == 0 ? -1 - gcell : n3[d] + gcell;
-                    for (int a = lo[(d + 1) % 3]; a < hi[(d + 1) % 3]; ++a)
-                        for (int bb = lo[(d + 2) % 3]; bb < hi[(d + 2) % 3]; ++bb) {
+#ifdef OCFDO_OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+                    for (int a = lo[ta]; a < hi[ta]; ++a)
+                        for (int bb = lo[tb]; bb < hi[tb]; ++bb) {
                             int idx[3];
                             idx[d] = gi_d;
-                            idx[(d + 1) % 3] = a;
-                            idx[(d + 2) % 3] = bb;
+                            idx[ta] = a;
+                            idx[tb] = bb;
                             dmr_fill(bc, S, N, &b, idx[0], idx[1], idx[2], ncomp, time);
                         }
                 }

@@ -65,11 +65,32 @@ def build_oracle(quiet=True):
     return os.path.join(HERE, "_build", "liboracle.so")
 
 
+def reference_dir():
+    """Root of the OpenCFD-AMR source tree the reference build compiles from:
+    $OCFD_REFERENCE_DIR, else the tree this build was pinned against (the
+    ``REF`` default of oracle/Makefile); None where neither holds the sources
+    (machines without the reference, e.g. the GPU host)."""
+    d = os.environ.get("OCFD_REFERENCE_DIR") or _MAKEFILE_REF
+    return d if os.path.isdir(os.path.join(d, "Source")) else None
+
+
+def _makefile_ref():
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REF") and "?=" in line:
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
+_MAKEFILE_REF = _makefile_ref()
+
+
 def build_ref():
     """Build oracle/_ref from the reference sources, if they are present."""
-    if not os.path.isdir("/root/reference/Source"):
+    ref = reference_dir()
+    if ref is None:
         return False
-    out = subprocess.run(["make", "-C", HERE, "ref"], capture_output=True, text=True)
+    out = subprocess.run(["make", "-C", HERE, "ref", "REF=" + ref], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("reference build failed:\n" + out.stdout + out.stderr)
     return True

@@ -27,11 +27,19 @@ def oracle():
 
 @pytest.fixture(scope="session")
 def ref():
-    from oracle import RefOracle, build_ref
-    if not os.path.isdir("/root/reference/Source"):
+    from oracle import RefOracle, build_ref, reference_dir
+    if reference_dir() is None:
         pytest.skip("reference sources not present on this machine")
     build_ref()
     return RefOracle()
+
+
+@pytest.fixture(scope="session")
+def oracle_omp():
+    """The oracle's OpenMP build (bit-identical to the serial one: the threads
+    split independent cells), for the runs at the configurations' sizes."""
+    from oracle import Oracle
+    return Oracle(openmp=True)
 
 
 def golden(name):

@@ -183,9 +183,12 @@ def test_reference_flop_counts():
     own headers compiled with a counting Real (make -C oracle flops); these are
     the algorithmic FLOPs per cell-stage quoted for the roofline."""
     import json
-    if not os.path.isdir("/root/reference/Source"):
+    from oracle import reference_dir
+    ref = reference_dir()
+    if ref is None:
         pytest.skip("reference sources not present on this machine")
-    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "flops"], capture_output=True, text=True)
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "flops", "REF=" + ref],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "flop_count")], capture_output=True, text=True)
     c = json.loads(out.stdout)
