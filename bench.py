@@ -1,32 +1,34 @@
-"""Benchmark: cell-steps/s of the OpenCFD-AMR RHS + RK3 update path on GB300.
+"""Benchmark: cell-steps/s of the OpenCFD-AMR RHS + RK update path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config dmr-amr|jet-eb-amr|react|sod|dmr|cube] [--form fp32|fp64]
+                    [--config jet-eb-amr|dmr-amr|react|sod|dmr|cube] [--form fp64|fp32]
 
-Default workload (dmr-amr): double Mach reflection on a 1024x256x2 base grid
-with two refined levels (ratio 2, |d rho| >= 0.05 tagging, regrid every 2 coarse
-steps, blocking factor 32, max grid 128), subcycled SSP-RK3 at CFL 0.5.  The
-hierarchy is first developed to t = 0.05 (untimed, mixed form), then both forms
-are timed for K coarse steps from that same state.
-A step is one coarse step: regridding when due (host clustering included), then
-one CUDA-graph launch that advances every level with its substeps (ghost fills,
-coarse-fine interpolation, fused RHS/RK stages, reflux, average-down, CFL).
+Default workload (jet-eb-amr, the largest single-GPU configuration): a Mach 2
+planar jet past a z-aligned cylinder (embedded boundary, r = 0.1) in 2x1x1, base
+256x128x128 with two refined levels (ratio 2, |d rho| >= 0.05 tagging, regrid
+every 2 coarse steps, blocking factor 8, max grid 64: about 2000 boxes of
+8^3..64^3), subcycled SSP-RK3 at CFL 0.5, cut boxes in the reference's cut-cell
+scheme with its small-cell rescale.  The hierarchy is developed 20 coarse steps
+from t = 0 (untimed, FP64), then every form is timed for K coarse steps from
+that same state.  A step is one coarse step: regridding when due (host
+clustering included), then one CUDA-graph launch that advances every level
+with its substeps (ghost fills, coarse-fine interpolation, fused RHS/RK
+stages, cut-cell batches, reflux, average-down, CFL).
 value  = leaf cell-steps (cells not covered by a finer level, times the
          substeps of their level) / device time of the K timed steps, state
-         resident in HBM, L2 flushed between steps (untimed), for the headline
-         form (default: FP32 flux / FP64 state); the plain FP64 form is timed the
-         same way and reported in config, with the L1 error in density and
-         pressure between the forms after 20 coarse steps on identical grids
-         (the FP64 run's regrids replayed in the FP32 run)
+         resident in HBM, L2 flushed between steps (untimed), for the plain FP64
+         form (the drop-in); the mixed FP32-flux form is timed the same way and
+         reported in config.mixed_form with its own e2e and its L1 error
+         against FP64 after 20 coarse steps on identical grids
 e2e    = the same through the C ABI from pinned host buffers: every step uploads
-         every level's state (its valid cells), advances, downloads every
-         level's state
---impl reference times the reference algorithm on the host CPU cores (the
-         oracle port, OpenMP, all threads): RK3 steps of the base grid.
-jet-eb-amr: Mach 2 planar jet past a z-cylinder in 2x1x1, base 256x128x128 +
-         2 levels (~800 boxes of 8^3-32^3), the cut boxes in the cut-cell
-         scheme; timed in the batched graph (FP32 headline and FP64, each
-         autotuned) and in per-box launches from the host (FP64).
+         every level's valid cells, advances, downloads every level's valid
+         cells (ocfd_amr_copy_valid_in / _out)
+--impl reference times the reference algorithm on the host cores (the oracle
+         port of its per-box arithmetic, threads over boxes) on the developed
+         hierarchy's grids (tests/golden/jet_eb_amr_grids.json, written by
+         --write-grids), each timed step a 1/8 sample of every level's boxes.
+dmr-amr: double Mach reflection, 1024x256x2 base + 2 levels (blocking 32, max
+         grid 128), developed to t = 0.05, both forms timed.
 react:   the 128^3 H2/air box with 8 hot spots (9 species, implicit chemistry,
          mixture-averaged transport); plain FP64, binned FP64 and the mixed form
          (headline), then the MLP surrogate trained inside the run.
@@ -55,6 +57,10 @@ CFL = 0.5
 
 T_DEV = 0.05
 L1_STEPS = 20
+# the reference's inviscid right-hand side of one cell (c2prim, split and
+# five-component WENO-Z per direction, divop), counted on its own headers with
+# a counting Real (make -C oracle flops), plus the fused Shu-Osher update
+FLOPS_PER_CELL_STAGE = 3233 + 25
 
 # DRAM traffic of each workload's roofline kernel, per cell of one launch:
 # (dram__bytes_read.sum + dram__bytes_write.sum) of a launch captured by ncu on the
@@ -349,26 +355,111 @@ def amr_matched_l1(ctx, c, snap, steps=L1_STEPS, mk=None):
 
 JET_N = (256, 128, 128)
 JET_DEV_STEPS = 20
+JET_MAX_GRID = 64
+JET_BLOCKING = 8
+JET_DENGRAD = 0.05
+JET_GRIDS = os.path.join(ROOT, "tests", "golden", "jet_eb_amr_grids.json")
 
 
 def jet_workload():
     from ocfd import cases
-    c = cases.jet_eb_amr(*JET_N, max_level=2, blocking_factor=8, max_grid=32, n_error_buf=1, refine_dengrad=0.1,
-                         regrid_int=2)
+    c = cases.jet_eb_amr(*JET_N, max_level=2, blocking_factor=JET_BLOCKING, max_grid=JET_MAX_GRID, n_error_buf=1,
+                         refine_dengrad=JET_DENGRAD, regrid_int=2)
     c["name"] = ("Mach 2 planar jet past a z-cylinder EB (r=0.1) in 2x1x1, base %dx%dx%d + 2 levels (ratio 2, "
-                 "|drho|>=0.1 tagging, regrid every 2 coarse steps, blocking 8, max grid 32), KH perturbation "
+                 "|drho|>=%g tagging, regrid every 2 coarse steps, blocking %d, max grid %d), KH perturbation "
                  "1e-2 (seed %d), inflow jet / outflow / periodic z, subcycled SSP-RK3, CFL 0.5, cut cells with "
-                 "the small-cell rescale, timed after %d coarse steps" % (JET_N + (c["seed"], JET_DEV_STEPS)))
+                 "the small-cell rescale, timed after %d coarse steps" % (
+                     JET_N + (JET_DENGRAD, JET_BLOCKING, JET_MAX_GRID, c["seed"], JET_DEV_STEPS)))
     return c
 
 
+def jet_grids_fixture():
+    """The developed hierarchy's grids (after JET_DEV_STEPS coarse steps of the
+    FP64 form from t = 0), as `bench.py --write-grids` wrote them."""
+    with open(JET_GRIDS) as f:
+        d = json.load(f)
+    return [[(tuple(lo), tuple(hi)) for lo, hi in lev] for lev in d["grids"]], d
+
+
+def cpu_info():
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                k = ln.split(":")[0].strip().lower()
+                if k in ("model name", "cpu part", "hardware") and model is None:
+                    model = ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return {"nproc": os.cpu_count(), "OMP_NUM_THREADS": os.environ.get("OMP_NUM_THREADS"),
+            "cpu": model, "machine": os.uname().machine}
+
+
+def jet_cpu_sample(grids, fab, parts, nparts, warm=1, threads=None):
+    """CPU leg on the jet hierarchy: the oracle's per-box SSP-RK3 work (regular
+    WENO-Z boxes, cut-cell boxes, nothing for covered boxes), threads over
+    boxes, on interleaved 1/nparts samples of every level's boxes; returns
+    (seconds, leaf cell-steps, all cell-steps) summed over `parts`."""
+    from hier_sample import HierarchySample, classify
+    c = jet_workload()
+    classes, geoms = classify(c["eb"], grids, c["dx"], c["prob_lo"])
+    hs = HierarchySample(grids, fab, classes, geoms, c["dx"], redistribute=c["eb"]["redistribute"],
+                         threads=threads)
+    for w in range(warm):
+        hs.time(hs.select((parts[0] + nparts // 2 + w) % nparts, nparts * 4))
+    sec = leaf = allc = 0
+    for p in parts:
+        a, b, cc = hs.time(hs.select(p % nparts, nparts))
+        sec += a
+        leaf += b
+        allc += cc
+    counts = [[cl.count(k) for k in (0, 1, 2)] for cl in classes]
+    return sec, leaf, allc, counts
+
+
+def run_reference_jet(args, world, rank):
+    """--impl reference on the jet hierarchy: the oracle port of the reference's
+    per-box arithmetic on the developed hierarchy's grids (committed fixture),
+    each timed step a 1/8 interleaved sample of every level's boxes."""
+    if rank != 0:
+        return
+    from ocfd import cases
+    grids, meta = jet_grids_fixture()
+    c = jet_workload()
+    threads = os.cpu_count() or 1
+
+    def fab(l, b):
+        lo, hi = grids[l][b]
+        return c["fab"](l, lo, hi, tuple(x / (1 << l) for x in c["dx"]))
+    nparts = 8
+    warm = max(1, min(args.warmup, 2))
+    sec, leaf, allc, counts = jet_cpu_sample(grids, fab, range(args.steps), nparts, warm=warm, threads=threads)
+    v = leaf / sec
+    sample = ("%d steps, each the per-box SSP-RK3 work of 1/%d of every level's boxes (interleaved) of the developed "
+              "hierarchy (%s boxes per level, regular/cut/covered %s), WENO-Z / cut-cell right-hand sides and "
+              "Shu-Osher updates of the oracle restatement (-O3, serial per box), %d threads over boxes; ghost "
+              "exchange, coarse-fine interpolation and reflux not timed" % (
+                  args.steps, nparts, [len(g) for g in grids], counts, threads))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": c["name"], "form": "fp64", "grids": "developed hierarchy (%s)" % (
+                os.path.relpath(JET_GRIDS, ROOT)), "boxes": sum(len(g) for g in grids),
+                "leaf_cell_steps_sampled": leaf, "all_cell_steps_sampled": allc, "host": cpu_info()},
+            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours_jet(args, world, rank, local):
-    """The multi-level embedded-boundary workload (Mach 2 jet past a cylinder).
-    Forms timed from the same developed state: the batched graph (one launch
-    per level per RK stage for the regular
-    boxes + three for the cut / covered boxes, autotuned tile shape and
-    schedule) in FP32-flux and FP64, and the reference's execution model in
-    FP64 (per-box launches issued from the host, no graph)."""
+    """The multi-level embedded-boundary workload (Mach 2 jet past a cylinder,
+    configs' largest single-GPU case).  Developed JET_DEV_STEPS coarse steps in
+    FP64 from t = 0 (untimed), then timed from that state: the plain FP64 form
+    (headline: `value`, `e2e`), the mixed FP32-flux form, both in the batched
+    graph (regular boxes in one tile-kernel launch per level and stage, cut and
+    covered boxes in the cut-cell batch, autotuned), and the reference's
+    execution model (FP64 per-box launches from the host)."""
     import numpy as np
     import torch
     import ocfd
@@ -386,22 +477,28 @@ def run_ours_jet(args, world, rank, local):
         return h
     H = mk(c["regrid_int"])
     H.build(c["fab"])
-    H.advance(JET_DEV_STEPS, CFL, ocfd.FLUX_FP32)            # untimed: bow shock, shear layers
+    H.advance(JET_DEV_STEPS, CFL, 0)            # untimed: bow shock, shear layers (FP64)
     snap = H.snapshot()
+    grids = snap["grids"]
+    if args.write_grids and rank == 0:
+        with open(args.write_grids, "w") as f:
+            json.dump({"workload": c["name"], "time": snap["time"],
+                       "grids": [[[list(lo), list(hi)] for lo, hi in g] for g in grids]}, f)
+            f.write("\n")
     stream = torch.cuda.current_stream(dev)
     l2flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     tuned = {}
 
-    def timed(fl, tune=True):
+    def timed(fl, steps, tune=True):
         H.restore(snap)
         if tune and not (fl & ocfd.PER_BOX):
             H.autotune(fl, reps=3)
-            tuned[fl] = [H.tuned(l) for l in range(H.nlevels())]
+            tuned["fp32" if fl & ocfd.FLUX_FP32 else "fp64"] = [H.tuned(l) for l in range(H.nlevels())]
         H.advance(args.warmup, CFL, fl)
         torch.cuda.synchronize()
         barrier(world)
         torch.cuda.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         leaf = allc = 0
         k0 = H.kernels_launched()
         torch.cuda.nvtx.range_push("bench_timed_jet_%d" % fl)
@@ -419,95 +516,132 @@ def run_ours_jet(args, world, rank, local):
         ms = allreduce_max(sum(e0.elapsed_time(e1) for e0, e1 in ev), world)
         return ms, leaf, allc, H.kernels_launched() - k0
 
-    if args.headline_only:
-        ms_d = ms_p = 1.0
-        leaf_d = leaf_p = k_p = 0
-    else:
-        ms_d, leaf_d, _, k_d = timed(0)
-        ms_p, leaf_p, _, k_p = timed(ocfd.PER_BOX)
-    with ClockSampler(local) as clk:
-        ms, leaf, allc, kernels = timed(ocfd.FLUX_FP32)
-    value = leaf * world / (ms * 1e-3)
-    v64 = leaf_d * world / (ms_d * 1e-3)
-    vpb = leaf_p * world / (ms_p * 1e-3)
-    levels = [{"level": l, "boxes": len(H.grids(l)), "cells": H.level(l).cells(),
-               "boxes_regular_cut_covered": [H.box_classes(l).count(k) for k in (0, 1, 2)]}
-              for l in range(H.nlevels())]
-    nbox = sum(x["boxes"] for x in levels)
-    fin = H.level(H.nlevels() - 1)
-    stage_ms = roofline_stage_ms(fin, ocfd.FLUX_FP32)
-    fcells = fin.cells()
-    hbm_peak, peak_src = peaks()
-    achieved = 120.0 * fcells / (stage_ms * 1e-3) / 1e9
-    fp64 = ctypes.c_double(); fp32 = ctypes.c_double()
-    ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
-
-    # end to end: every level uploaded from pinned host memory, one coarse step, every level downloaded
-    H.restore(snap)
-    H.advance(1, CFL, ocfd.FLUX_FP32)
-    torch.cuda.synchronize()
     pins = {}
 
     def pin(l, n):
         if l not in pins or pins[l].numel() < n:
             pins[l] = torch.empty(int(n * 1.5) + 1, dtype=torch.float64).pin_memory()
         return pins[l]
-    for l in range(H.nlevels()):
-        H.copy_valid_out(l, pin(l, H.valid_elems(l)), stream)
-    torch.cuda.synchronize()
-    e2e_steps = max(2, min(args.steps, 5))
-    h2d = d2h = 0
-    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-    e2e_leaf = 0
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        for l in range(H.nlevels()):
-            H.copy_valid_in(l, pins[l], stream)
-            h2d += 8 * H.valid_elems(l)
-        H.advance(1, CFL, ocfd.FLUX_FP32, stream)
-        e2e_leaf += H.cell_steps()[0]
-        for l in range(H.nlevels()):
-            n = H.valid_elems(l)
-            H.copy_valid_out(l, pin(l, n), stream)
-            d2h += 8 * n
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_value = e2e_leaf * world / (allreduce_max(e0.elapsed_time(e1), world) * 1e-3)
 
+    def e2e(fl):
+        """every level uploaded from pinned host memory (valid cells, through the
+        C ABI), one coarse step, every level downloaded; per step"""
+        H.restore(snap)
+        H.advance(1, CFL, fl)
+        torch.cuda.synchronize()
+        for l in range(H.nlevels()):
+            H.copy_valid_out(l, pin(l, H.valid_elems(l)), stream)
+        torch.cuda.synchronize()
+        steps = max(2, min(args.steps, 5))
+        h2d = d2h = 0
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        leaf = 0
+        e0.record(stream)
+        for _ in range(steps):
+            for l in range(H.nlevels()):
+                H.copy_valid_in(l, pins[l], stream)
+                h2d += 8 * H.valid_elems(l)
+            H.advance(1, CFL, fl, stream)
+            leaf += H.cell_steps()[0]
+            for l in range(H.nlevels()):
+                n = H.valid_elems(l)
+                H.copy_valid_out(l, pin(l, n), stream)
+                d2h += 8 * n
+        e1.record(stream)
+        torch.cuda.synchronize()
+        v = leaf * world / (allreduce_max(e0.elapsed_time(e1), world) * 1e-3)
+        return {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d / steps),
+                "d2h_bytes_per_step": int(d2h / steps)}
+
+    ms_m, leaf_m, _, k_m = timed(ocfd.FLUX_FP32, args.steps)
+    if args.headline_only:
+        ms_p, leaf_p, k_p = 1.0, 0, 0
+    else:
+        ms_p, leaf_p, _, k_p = timed(ocfd.PER_BOX, max(1, min(args.steps, 3)))
+    with ClockSampler(local) as clk:
+        ms, leaf, allc, kernels = timed(0, args.steps)
+    value = leaf * world / (ms * 1e-3)
+    v32 = leaf_m * world / (ms_m * 1e-3)
+    vpb = leaf_p * world / (ms_p * 1e-3)
+    levels = [{"level": l, "boxes": len(H.grids(l)), "cells": H.level(l).cells(),
+               "boxes_regular_cut_covered": [H.box_classes(l).count(k) for k in (0, 1, 2)]}
+              for l in range(H.nlevels())]
+    nbox = sum(x["boxes"] for x in levels)
+    sizes = sorted(max(hi[d] - lo[d] + 1 for d in range(3)) for g in grids for lo, hi in g)
+    fin = H.level(H.nlevels() - 1)
+    fcells = fin.cells()
+    stage_ms = roofline_stage_ms(fin, 0)
+    stage_ms32 = roofline_stage_ms(fin, ocfd.FLUX_FP32)
+    hbm_peak, peak_src = peaks()
+    fp64 = ctypes.c_double(); fp32 = ctypes.c_double(); fp32x2 = ctypes.c_double()
+    ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
+    ocfd.check(ocfd.load().ocfd_measure_ffma2_peak(ctypes.byref(fp32x2)))
+    achieved = 120.0 * fcells / (stage_ms * 1e-3) / 1e9
+    achieved32 = 120.0 * fcells / (stage_ms32 * 1e-3) / 1e9
+    flops64 = FLOPS_PER_CELL_STAGE * fcells / (stage_ms * 1e-3) / 1e9
+
+    e2e64 = e2e(0)
+    e2e32 = e2e(ocfd.FLUX_FP32)
     l1err = amr_matched_l1(ctx, c, snap, mk=mk) if rank == 0 and not args.headline_only else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cs = cpu_sample_workload("jet-eb-amr")
-        dt, ccells = cpu_time_steps(cs, 1, os.cpu_count())
-        cpu = {"value": ccells / dt, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "1 RK3 step of the oracle restatement (OpenMP), %s" % cs["sample_note"]}
+        data = snap["data"]
+
+        def fab(l, b):
+            off = 0
+            for i, (lo, hi) in enumerate(grids[l]):
+                n = (5, hi[2] - lo[2] + 9, hi[1] - lo[1] + 9, hi[0] - lo[0] + 9)
+                sz = n[0] * n[1] * n[2] * n[3]
+                if i == b:
+                    return data[l][off:off + sz].reshape(n).copy()
+                off += sz
+        sec, cleaf, _, counts = jet_cpu_sample(grids, fab, [0], 16, warm=1)
+        cpu = {"value": cleaf / sec, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "1/16 of every level's boxes of the timed hierarchy (the GPU state at the start of the "
+                         "timed steps), per-box SSP-RK3 work of the oracle restatement (-O3, serial per box), %d "
+                         "threads over boxes; classes regular/cut/covered %s" % (os.cpu_count(), counts),
+               "host": cpu_info()}
+    grids_match = None
+    if os.path.exists(JET_GRIDS):
+        try:
+            fg, _ = jet_grids_fixture()
+            grids_match = [len(a) == len(b) and sorted(a) == sorted(b) for a, b in zip(fg, grids)]
+        except (OSError, ValueError, KeyError):
+            grids_match = None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32-flux/f64-state", "data": "synthetic",
-            "config": {"workload": c["name"], "form": "fp32 batched graph, autotuned", "levels": levels,
-                       "boxes": nbox, "leaf_cell_steps_per_coarse_step": leaf / args.steps,
-                       "forms_cell_steps_per_s": {"fp32_batched": value, "fp64_batched": v64,
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": c["name"], "form": "plain FP64 (the drop-in), batched graph, autotuned",
+                       "levels": levels, "boxes": nbox, "box_edge_min_max": [sizes[0], sizes[-1]],
+                       "refine_dengrad": JET_DENGRAD, "max_grid": JET_MAX_GRID, "blocking_factor": JET_BLOCKING,
+                       "leaf_cell_steps_per_coarse_step": leaf / args.steps,
+                       "forms_cell_steps_per_s": {"fp64_batched": value, "fp32_flux_batched": v32,
                                                   "fp64_per_box_launches": vpb},
-                       "speedup_fp32_batched_over_fp64_batched": (value / v64) if v64 else None,
-                       "speedup_fp32_batched_over_fp64_per_box": (value / vpb) if vpb else None,
-                       "speedup_batched_over_per_box_fp64": (v64 / vpb) if vpb else None,
-                       "kernels_per_coarse_step": {"fp32_batched": kernels / args.steps,
-                                                   "fp64_per_box": k_p / args.steps},
-                       "autotuned_tile_sched_per_level": {("fp32" if k else "fp64"): v for k, v in tuned.items()},
-                       "l1_vs_other_form": l1err,
+                       "mixed_form": {"value": v32, "e2e": e2e32, "ms_per_step": ms_m / args.steps,
+                                      "speedup_over_fp64": v32 / value, "l1_vs_fp64": l1err,
+                                      "roofline_stage": {"achieved_gbs": achieved32, "frac": achieved32 / hbm_peak,
+                                                         "ms_per_launch": stage_ms32}},
+                       "speedup_batched_over_per_box_fp64": (value / vpb) if vpb else None,
+                       "kernels_per_coarse_step": {"fp64_batched": kernels / args.steps,
+                                                   "fp64_per_box": k_p / max(1, min(args.steps, 3))},
+                       "autotuned_tile_sched_per_level": tuned,
+                       "grids_match_reference_arm_fixture": grids_match,
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_source": peak_src,
-                         "traffic": ncu_traffic("jet-eb-amr", "fp32", fcells),
-                         "kernel": "k_rhs_regular fused RK stage (FP32 flux), finest level (%d cells)" % fcells,
+                         "traffic": ncu_traffic("jet-eb-amr", "fp64", fcells),
+                         "kernel": "finest level's RK stage, FP64 (regular-box tile kernel + cut-cell batch, "
+                                   "%d cells)" % fcells,
                          "ms_per_launch": stage_ms, "alg_bytes_per_cell": 120,
-                         "fp64_fma_peak_gflops": fp64.value, "fp32_fma_peak_gflops": fp32.value},
+                         "fp64": {"achieved_gflops": flops64, "peak_gflops": fp64.value,
+                                  "frac": flops64 / fp64.value,
+                                  "flops_per_cell_stage": FLOPS_PER_CELL_STAGE},
+                         "fp32_fma_peak_gflops": fp32.value, "fp32x2_fma_peak_gflops": fp32x2.value},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
-                    "d2h_bytes_per_step": int(d2h / e2e_steps)},
+            "e2e": e2e64,
             "clocks": clk.summary(),
             "gpu_launches": kernels,
         }
@@ -1064,9 +1198,13 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="dmr-amr", choices=["dmr-amr", "jet-eb-amr", "react", "sod", "dmr", "cube"])
-    ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
-                    help="headline form (the other form is timed too and reported in config)")
+    ap.add_argument("--config", default="jet-eb-amr",
+                    choices=["jet-eb-amr", "dmr-amr", "react", "sod", "dmr", "cube"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"],
+                    help="dmr-amr and the single-level configs: headline form (the other form is timed too and "
+                         "reported in config); jet-eb-amr always heads with FP64")
+    ap.add_argument("--write-grids", default=None,
+                    help="jet-eb-amr: write the developed hierarchy's grids (the reference arm's fixture) here")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-surrogate", action="store_true", help="react: skip the surrogate form")
     ap.add_argument("--headline-only", action="store_true",
@@ -1077,7 +1215,10 @@ def main():
         args.warmup = 3
     world, rank, local = dist_setup()
     if args.impl == "reference":
-        run_reference(args, world, rank)
+        if args.config == "jet-eb-amr":
+            run_reference_jet(args, world, rank)
+        else:
+            run_reference(args, world, rank)
     elif args.config == "dmr-amr":
         run_ours_amr(args, world, rank, local)
     elif args.config == "react":

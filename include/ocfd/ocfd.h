@@ -655,6 +655,17 @@ ocfd_status ocfd_chem_cells_surrogate(ocfd_context* ctx, ocfd_mlp* mlp, const oc
  * per FMA), from register-only FMA chains over all SMs. */
 ocfd_status ocfd_measure_fma_peaks(double* fp64_gflops, double* fp32_gflops);
 
+/* Packed FP32 FMA rate (FFMA2: two lanes per instruction) of the current device
+ * in GFLOP/s (4 flops per instruction); the FP32 denominator of the mixed form,
+ * whose WENO-Z runs on packed pairs.  No counterpart in the reference. */
+ocfd_status ocfd_measure_ffma2_peak(double* fp32x2_gflops);
+
+/* Test hook: fast[i] = the reciprocal the fused FP64 kernels use in place of an
+ * IEEE division (approximate seed + two Newton-Raphson steps), ieee[i] = 1/x[i]
+ * correctly rounded; device arrays of n doubles.  No counterpart in the
+ * reference. */
+ocfd_status ocfd_check_rcp_f64(const double* x, double* fast, double* ieee, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -814,8 +814,8 @@ __global__ void __launch_bounds__(128) k_chem_faces(ChemBoxArgs B, DevParm P) {
         }
 #pragma unroll
         for (int n = 0; n < 5; ++n)
-            f[n] = wenoz_plus(fp[0][n], fp[1][n], fp[2][n], fp[3][n], fp[4][n]) +
-                   wenoz_minus(fm[1][n], fm[2][n], fm[3][n], fm[4][n], fm[5][n]);
+            f[n] = wenoz_1rcp(fp[0][n], fp[1][n], fp[2][n], fp[3][n], fp[4][n]) +
+                   wenoz_1rcp(fm[5][n], fm[4][n], fm[3][n], fm[2][n], fm[1][n]);
 #pragma unroll
         for (int n = 0; n < NSP; ++n) {
             double a[6], b[6];
@@ -825,7 +825,7 @@ __global__ void __launch_bounds__(128) k_chem_faces(ChemBoxArgs B, DevParm P) {
                 a[s] = tmp0 * tp[s];
                 b[s] = tmp0 * tm[s];
             }
-            fs[n] = wenoz_plus(a[0], a[1], a[2], a[3], a[4]) + wenoz_minus(b[1], b[2], b[3], b[4], b[5]);
+            fs[n] = wenoz_1rcp(a[0], a[1], a[2], a[3], a[4]) + wenoz_1rcp(b[5], b[4], b[3], b[2], b[1]);
         }
         }
         if (B.visc) {

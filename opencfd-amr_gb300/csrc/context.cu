@@ -76,6 +76,7 @@ DevParm make_dev_parm(const ocfd_parm& p) {
     d.sw_tmp2 = 2.0 * (g - 1.0);
     d.sw_tmp3 = (3.0 - g) / (2.0 * (g - 1.0));
     d.sw_gm1 = g - 1;
+    d.invRg = 1.0 / d.Rg;
     d.f_gamma = (float)d.gamma;
     d.f_smallr = (float)d.smallr;
     d.f_smallp = (float)d.smallp;

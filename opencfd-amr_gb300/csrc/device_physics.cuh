@@ -115,6 +115,77 @@ __host__ __device__ __forceinline__ double wenoz_minus(double V1, double V2, dou
     return (1.0 / 6.0) * invsum * (a1 * v1 + a2 * v2 + a3 * v3);
 }
 
+#if defined(__CUDACC__)
+// 1/x for a normal, finite, non-zero double, to within about one ulp, without an
+// IEEE division: the PTX approximate reciprocal (rcp.approx.ftz.f64, a seed
+// good to roughly 20 bits) refined by two Newton-Raphson steps
+// r <- r + r (1 - x r), each of which squares the relative error (P. Markstein,
+// IBM J. Res. Develop. 34 (1990) 111-119).  GB300 issues few FP64 instructions
+// per cycle; this takes one MUFU operation and four FMAs where a correctly
+// rounded division takes about twice as many FP64 instructions.  The
+// arguments it is used on are sums of squares plus a positive epsilon.
+__device__ __forceinline__ double rcp_nr(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+
+// WENO-Z of one split flux (Source/kernel/Reconstruction.H:83-138), the stencil
+// V1..V5 ordered towards the face (f+: cells i-3..i+1; f-: cells i+2..i-2, i.e.
+// wenoz_minus(V1..V5) == wenoz_1rcp(V5, V4, V3, V2, V1)), with a single
+// reciprocal instead of the reference's four divisions: the weights
+// alpha_k = d_k (1 + (tau / D_k)^2), D_k = eps + beta_k, d = (1, 6, 3), are
+// multiplied by the common positive factor (D_1 D_2 D_3)^2, which cancels in
+// alpha_k / sum alpha, giving a_k = d_k (D_k^2 + tau^2) prod_{j != k} D_j^2.  The
+// same weights up to rounding (parity tests: 1e-12 per right-hand side); the
+// products stay finite for |beta| < 1e51, i.e. flux differences below ~1e25.
+__device__ __forceinline__ double wenoz_1rcp(double V1, double V2, double V3, double V4, double V5) {
+    const double eps = 1e-6;
+    const double e1 = V1 - 2.0 * V2 + V3, g1 = V1 - 4.0 * V2 + 3.0 * V3;
+    const double e2 = V2 - 2.0 * V3 + V4, g2 = V2 - V4;
+    const double e3 = V3 - 2.0 * V4 + V5, g3 = 3.0 * V3 - 4.0 * V4 + V5;
+    const double b1 = (13.0 / 12.0) * e1 * e1 + 0.25 * g1 * g1;
+    const double b2 = (13.0 / 12.0) * e2 * e2 + 0.25 * g2 * g2;
+    const double b3 = (13.0 / 12.0) * e3 * e3 + 0.25 * g3 * g3;
+    const double tau = fabs(b1 - b3);
+    const double D1 = eps + b1, D2 = eps + b2, D3 = eps + b3;
+    const double q1 = D1 * D1, q2 = D2 * D2, q3 = D3 * D3, t2 = tau * tau;
+    const double a1 = (q1 + t2) * (q2 * q3);
+    const double a2 = 6.0 * (q2 + t2) * (q1 * q3);
+    const double a3 = 3.0 * (q3 + t2) * (q1 * q2);
+    const double v1 = 2.0 * V1 - 7.0 * V2 + 11.0 * V3;
+    const double v2 = -V2 + 5.0 * V3 + 2.0 * V4;
+    const double v3 = 2.0 * V3 + 5.0 * V4 - V5;
+    return (a1 * v1 + a2 * v2 + a3 * v3) * rcp_nr(6.0 * (a1 + a2 + a3));
+}
+#endif
+
+#if defined(__CUDACC__)
+// c2prim (Source/kernel/Kernels.H:13-40) for the fused FP64 kernels: the two
+// divisions become one reciprocal of rho (T = p (1/rho) (1/Rg), 1/Rg formed once
+// on the host); the same values to within a few ulps.
+__device__ __forceinline__ void c2prim_ideal_fast(const DevParm& P, double u0, double u1, double u2, double u3,
+                                                  double u4, double* q) {
+    const double rho = dmax(u0, P.smallr);
+    const double rhoinv = rcp_nr(rho);
+    const double ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
+    const double kineng = 0.5 * (ux * ux + uy * uy + uz * uz);
+    const double ei = u4 - rho * kineng;
+    const double p = dmax((P.gamma - 1.0) * ei, P.smallp);
+    const double T = p * rhoinv * P.invRg;
+    q[QRHO] = rho;
+    q[QU] = ux;
+    q[QV] = uy;
+    q[QW] = uz;
+    q[QPRES] = p;
+    q[QT] = T;
+    q[QC] = sqrt(P.gamma * P.Rg * T);
+}
+#endif
+
 __host__ __device__ __forceinline__ double sutherland(const DevParm& P, double T) {
     return P.C_s * T * sqrt(T) / (T + P.T_s);
 }

@@ -38,7 +38,7 @@ __global__ void k_eb_prims(EbBoxArgs B, DevParm P) {
         const int i = B.lo[0] - 2 + (int)(c % gx), j = B.lo[1] - 2 + (int)((c / gx) % gy),
                   k = B.lo[2] - 2 + (int)(c / ((long long)gx * gy));
         double q[7];
-        c2prim_ideal(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3),
+        c2prim_ideal_fast(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3),
                      B.S(i, j, k, 4), q);
 #pragma unroll
         for (int m = 0; m < 7; ++m) B.q(i, j, k, m) = q[m];

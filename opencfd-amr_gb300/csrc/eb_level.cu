@@ -245,7 +245,7 @@ __global__ void k_ebl_prims(EbStageArgs A, DevParm P) {
             B.qf(i, j, k, QC) = sqrtf(g * p * rhoinv);
         } else {
             double q[7];
-            c2prim_ideal(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3), B.S(i, j, k, 4), q);
+            c2prim_ideal_fast(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3), B.S(i, j, k, 4), q);
 #pragma unroll
             for (int m = 0; m < 7; ++m) B.q(i, j, k, m) = q[m];
         }

@@ -37,45 +37,58 @@ __device__ __forceinline__ void eb_recon(uint32_t f, int D, T vm2, T vm1, T v0, 
     }
 }
 
-// Van Leer flux vector splitting, Source/EB/EBkernels.H:73-171
+// 1/x: the Newton-refined reciprocal in FP64 (device_physics.cuh), a plain
+// division in FP32
+template <class T>
+__device__ __forceinline__ T recip(T x);
+template <>
+__device__ __forceinline__ double recip<double>(double x) { return rcp_nr(x); }
+template <>
+__device__ __forceinline__ float recip<float>(float x) { return 1.0f / x; }
+
+// Van Leer flux vector splitting, Source/EB/EBkernels.H:73-171.  The reference's
+// divisions (two Mach numbers, /gamma per momentum component, /(2(g^2-1)),
+// g/(g-1)) become four reciprocals per face; the same values to within a few
+// ulps (FP64 parity of the cut-cell paths: 1e-12 per right-hand side).
 template <class T>
 __device__ __forceinline__ void vanleer(T smallp, T gamma, const T* ql, const T* qr, int D, T* flx) {
     T fp[5] = {0, 0, 0, 0, 0}, fm[5] = {0, 0, 0, 0, 0};
     const T dl = ql[QRHO], ul = ql[QU], vl = ql[QV], wl = ql[QW], pl = ql[QPRES] > smallp ? ql[QPRES] : smallp;
     const T dr = qr[QRHO], ur = qr[QU], vr = qr[QV], wr = qr[QW], pr = qr[QPRES] > smallp ? qr[QPRES] : smallp;
     const T cL = ql[QC], cR = qr[QC];
+    const T rg = recip<T>(gamma), rg21 = recip<T>(2 * (gamma * gamma - 1)), ggm1 = gamma * recip<T>(gamma - T(1));
     const int nn[3] = {D == 0, D == 1, D == 2};
     const T UL = D == 0 ? ul : (D == 1 ? vl : wl);
     const T UR = D == 0 ? ur : (D == 1 ? vr : wr);
-    const T ML = UL / cL, MR = UR / cR;
+    const T ML = UL * recip<T>(cL), MR = UR * recip<T>(cR);
     const T lv[3] = {ul, vl, wl}, rv[3] = {ur, vr, wr};
     if (ML >= T(1)) {
         fp[0] = dl * UL;
 #pragma unroll
         for (int m = 0; m < 3; ++m) fp[1 + m] = dl * UL * lv[m] + T(nn[m]) * pl;
-        fp[4] = UL * (gamma * pl / (gamma - T(1)) + T(0.5) * dl * (ul * ul + vl * vl + wl * wl));
+        fp[4] = UL * (ggm1 * pl + T(0.5) * dl * (ul * ul + vl * vl + wl * wl));
     } else if (fabs(ML) < T(1)) {
         const T Mp = T(0.25) * (T(1) + ML) * (T(1) + ML);
         const T t0 = dl * cL * Mp;
         fp[0] = t0;
 #pragma unroll
-        for (int m = 0; m < 3; ++m) fp[1 + m] = t0 * (T(nn[m]) * (-UL + T(2) * cL) / gamma + lv[m]);
-        fp[4] = t0 * (((gamma - 1) * UL + 2 * cL) * ((gamma - 1) * UL + 2 * cL) / (2 * (gamma * gamma - 1)) +
-                      (ul * ul + vl * vl + wl * wl - UL * UL) / 2);
+        for (int m = 0; m < 3; ++m) fp[1 + m] = t0 * (nn[m] ? (-UL + T(2) * cL) * rg + lv[m] : lv[m]);
+        fp[4] = t0 * (((gamma - 1) * UL + 2 * cL) * ((gamma - 1) * UL + 2 * cL) * rg21 +
+                      (ul * ul + vl * vl + wl * wl - UL * UL) * T(0.5));
     }
     if (fabs(MR) < T(1)) {
         const T Mm = T(-0.25) * (MR - T(1)) * (MR - T(1));
         const T t0 = dr * cR * Mm;
         fm[0] = t0;
 #pragma unroll
-        for (int m = 0; m < 3; ++m) fm[1 + m] = t0 * (T(nn[m]) * (-UR - T(2) * cR) / gamma + rv[m]);
-        fm[4] = t0 * (((gamma - 1) * UR - 2 * cR) * ((gamma - 1) * UR - 2 * cR) / (2 * (gamma * gamma - 1)) +
-                      (ur * ur + vr * vr + wr * wr - UR * UR) / 2);
+        for (int m = 0; m < 3; ++m) fm[1 + m] = t0 * (nn[m] ? (-UR - T(2) * cR) * rg + rv[m] : rv[m]);
+        fm[4] = t0 * (((gamma - 1) * UR - 2 * cR) * ((gamma - 1) * UR - 2 * cR) * rg21 +
+                      (ur * ur + vr * vr + wr * wr - UR * UR) * T(0.5));
     } else if (MR <= T(-1)) {
         fm[0] = dr * UR;
 #pragma unroll
         for (int m = 0; m < 3; ++m) fm[1 + m] = dr * UR * rv[m] + T(nn[m]) * pr;
-        fm[4] = UR * (gamma * pr / (gamma - T(1)) + T(0.5) * dr * (ur * ur + vr * vr + wr * wr));
+        fm[4] = UR * (ggm1 * pr + T(0.5) * dr * (ur * ur + vr * vr + wr * wr));
     }
 #pragma unroll
     for (int n = 0; n < 5; ++n) flx[n] = fp[n] + fm[n];

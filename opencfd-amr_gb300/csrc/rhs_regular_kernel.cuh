@@ -80,15 +80,15 @@ struct Prec<double> {
     // q = rho, u, v, w, p, T, c
     static __device__ __forceinline__ void prims(const DevParm& P, const View<const double>& S, int i,
                                                  int j, int k, double* q) {
-        c2prim_ideal(P, S(i, j, k, 0), S(i, j, k, 1), S(i, j, k, 2), S(i, j, k, 3), S(i, j, k, 4), q);
+        c2prim_ideal_fast(P, S(i, j, k, 0), S(i, j, k, 1), S(i, j, k, 2), S(i, j, k, 3), S(i, j, k, 4), q);
     }
     template <int D>
     static __device__ __forceinline__ void split(const DevParm& P, const double* q, double* fp, double* fm) {
         sw_split<D>(q[QRHO], q[QU], q[QV], q[QW], q[QC], P.sw_tmp1, P.sw_tmp2, P.sw_tmp3, P.sw_gm1, fp, fm);
     }
     static __device__ __forceinline__ double weno(const double* a, const double* b, int s) {
-        return wenoz_plus(a[0], a[s], a[2 * s], a[3 * s], a[4 * s]) +
-               wenoz_minus(b[s], b[2 * s], b[3 * s], b[4 * s], b[5 * s]);
+        return wenoz_1rcp(a[0], a[s], a[2 * s], a[3 * s], a[4 * s]) +
+               wenoz_1rcp(b[5 * s], b[4 * s], b[3 * s], b[2 * s], b[s]);
     }
     static __device__ __forceinline__ double mu(const DevParm& P, double T) { return sutherland(P, T); }
 };

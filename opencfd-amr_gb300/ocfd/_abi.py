@@ -81,6 +81,9 @@ _SIGS = {
                                                 ctypes.c_void_p, ctypes.POINTER(Array4), Box,
                                                 ctypes.POINTER(ctypes.c_double), ctypes.c_uint, ctypes.c_void_p]),
     "ocfd_measure_fma_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "ocfd_measure_ffma2_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "ocfd_check_rcp_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.c_void_p]),
 }
 
 

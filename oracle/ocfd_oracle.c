@@ -1620,6 +1620,43 @@ double ocfdo_advance_rk3(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int
     return time;
 }
 
+/* ============================================== one box's RK3 step (timing)
+ * The per-box work of one SSP-RK3 step of a level (Source/Advance.cpp:182-418
+ * per stage: the regular or the cut-cell right-hand side of the box; then the
+ * Shu-Osher update of AmrLevel::RK(3) over the box's valid cells), without the
+ * ghost exchange between stages: the CPU baseline times this on a sample of a
+ * hierarchy's boxes.  flag == NULL: the regular scheme; else the cut-cell one
+ * (vfrac, apx, apy, apz as for ocfdo_rhs_eb).  S is advanced in place. */
+void ocfdo_box_rk3_step(const ocfdo_parm* p, double* S, const uint32_t* flag, const double* vfrac,
+                        const double* apx, const double* apy, const double* apz, int nx, int ny, int nz,
+                        const double* dxinv, int do_redistribute, double dt) {
+    box_t b = mkbox(nx, ny, nz);
+    long long N = gN(&b), BN = bN(&b);
+    double* S0 = (double*)xcalloc(N * NCONS, sizeof(double));
+    double* k = (double*)xcalloc(BN * NCONS, sizeof(double));
+    double* fl[3];
+    for (int d = 0; d < 3; ++d) fl[d] = (double*)xcalloc(fN(&b, d) * NCONS, sizeof(double));
+    memcpy(S0, S, sizeof(double) * N * NCONS);
+    static const double A[3] = {0.0, 0.75, 1.0 / 3.0}, B[3] = {1.0, 0.25, 2.0 / 3.0};
+    for (int st = 0; st < 3; ++st) {
+        if (flag)
+            ocfdo_rhs_eb(p, S, flag, vfrac, apx, apy, apz, nx, ny, nz, dxinv, 0, do_redistribute, k, fl[0],
+                         fl[1], fl[2]);
+        else
+            ocfdo_rhs_regular(p, S, nx, ny, nz, dxinv, 0, k, fl[0], fl[1], fl[2]);
+        for (int n = 0; n < NCONS; ++n)
+            for (int kk = 0; kk < nz; ++kk)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) {
+                        long long g = n * N + gI(&b, i, j, kk), c = n * BN + bI(&b, i, j, kk);
+                        S[g] = A[st] * S0[g] + B[st] * (S[g] + dt * k[c]);
+                    }
+    }
+    free(S0);
+    free(k);
+    for (int d = 0; d < 3; ++d) free(fl[d]);
+}
+
 /* ======================================================= RK2 / Euler driver
  * EBR::flow_advance, Source/Advance.cpp:115-138:
  *   Euler: FillPatch(t); S_new = 1.0 * Sborder + dt * dSdt        (LinComb)

@@ -132,6 +132,13 @@ double ocfdo_advance_rk3(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int
 double ocfdo_advance_rk12(const ocfdo_parm* p, const ocfdo_bc* bc, double* S, int nx, int ny,
                           int nz, int do_visc, double cfl, int nsteps, int order, double* dts);
 
+/* One SSP-RK3 step of one box (regular scheme when flag is NULL, else the
+ * cut-cell one) without ghost exchange between the stages, in place: the unit
+ * the CPU baseline times on a sample of a hierarchy's boxes. */
+void ocfdo_box_rk3_step(const ocfdo_parm* p, double* S, const uint32_t* flag, const double* vfrac,
+                        const double* apx, const double* apy, const double* apz, int nx, int ny, int nz,
+                        const double* dxinv, int do_redistribute, double dt);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,10 +107,13 @@ def face_shape(nc, nx, ny, nz, d):
 class Oracle:
     """The plain-C restatement."""
 
-    def __init__(self, path=None, openmp=False):
+    def __init__(self, path=None, openmp=False, fast=False):
+        """openmp: the OpenMP build (same results); fast: the -O3 serial build
+        with FMA contraction, for timing only (its results are not the oracle's)."""
         if path is None:
             build_oracle()
-            path = os.path.join(HERE, "_build", "liboracle_omp.so" if openmp else "liboracle.so")
+            name = "liboracle_fast.so" if fast else ("liboracle_omp.so" if openmp else "liboracle.so")
+            path = os.path.join(HERE, "_build", name)
         self.lib = ctypes.CDLL(path)
         L = self.lib
         L.ocfdo_estdt.restype = ctypes.c_double
@@ -271,6 +274,18 @@ class Oracle:
                                        gy - 2 * NG, gz - 2 * NG, int(do_visc), cfl, nsteps, form,
                                        _ptr(dts))
         return t, dts
+
+    def box_rk3_step(self, S, dxinv, dt, geom=None, do_redistribute=False):
+        """One SSP-RK3 step of one grown box in place, no ghost exchange between
+        stages (the timed unit of the CPU baseline); geom: cut-cell data as for
+        rhs_eb, None for the regular scheme."""
+        _, gz, gy, gx = S.shape
+        dx = (ctypes.c_double * 3)(*dxinv)
+        g = geom or {}
+        self.lib.ocfdo_box_rk3_step(self.pp, _ptr(S), _ptr(g.get("flag")), _ptr(g.get("vfrac")),
+                                    _ptr(g.get("apx")), _ptr(g.get("apy")), _ptr(g.get("apz")),
+                                    gx - 2 * NG, gy - 2 * NG, gz - 2 * NG, dx, int(do_redistribute),
+                                    ctypes.c_double(dt))
 
     def advance_rk(self, bc, S, cfl, nsteps, order, do_visc=False):
         """nsteps of ebr.time_integration = "Euler" (order 1), "RK2" (2) or RK3 (3,

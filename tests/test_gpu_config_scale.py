@@ -15,9 +15,10 @@ plain FP64 form against the oracle (OpenMP build) on the same inputs.
   Source/CHEM/FlowAdvance.cpp:9-90), dt = 1e-8 s.
 
 For each: the RHS of one evaluation, GPU against oracle, on the initial and on
-the final state, within 1e-12 (1e-11 where the path goes through exp / log:
-CUDA's and the host's libm differ by ulps); after N steps the two final states
-within 1e-10 (grouped max norm), and their L1 errors (fcompare's
+the final state, within 1e-12 norm-wise (the reacting box starts at rest, so its
+right-hand side is measured against the split-flux scale, see rhs_err); after N
+steps the two final states within 1e-10 (grouped max norm; 1e-9 for the 9
+species of the reacting box, whose radicals start at zero), and their L1 errors (fcompare's
 sum|a-b| / sum|b|) in density, pressure and, for the reacting box, Y_OH and
 Y_H2O within 1e-10 of each other; Sod's L1 error against the exact Riemann
 solution is the same for both to 1e-10 relative.
@@ -174,6 +175,11 @@ def test_react_64cube_sample_100_steps(ctx, oracle, oracle_omp):
         return oracle_omp.c2prim(S, sp)[4, NG:-NG, NG:-NG, NG:-NG]
 
     def rhs_err(G):
+        """The box starts at rest at uniform pressure, so every component of its
+        right-hand side is the small difference of split fluxes of size rho c
+        (mass, species), rho c^2 (momentum) and rho c H (energy); the error of
+        each is measured against dxinv times that flux scale (norm-wise over
+        the box) rather than against the residual itself."""
         S, sp = filled(G)
         rS, rsp, *_ = oracle_omp.rhs_chem(S, sp, dxinv, do_visc=True)
         dS = torch.empty((5, n, n, n), dtype=torch.float64, device="cuda")
@@ -181,9 +187,27 @@ def test_react_64cube_sample_100_steps(ctx, oracle, oracle_omp):
         ctx.rhs_chem_box(torch.from_numpy(S).cuda(), torch.from_numpy(sp).cuda(), dS, dsp, (0, 0, 0),
                          (n - 1,) * 3, dxinv, flags=1)
         torch.cuda.synchronize()
-        return max(relerr(dS.cpu().numpy(), rS), relerr(dsp.cpu().numpy(), rsp))
+        q = oracle_omp.c2prim(S, sp)[:, NG:-NG, NG:-NG, NG:-NG]
+        rho, p, c = q[0], q[4], q[6]
+        H = np.abs(S[4, NG:-NG, NG:-NG, NG:-NG]) / rho + p / rho
+        scale = max(dxinv) * np.array([(rho * c).max(), (rho * c * c).max(), (rho * c * H).max()])
+        g, r = dS.cpu().numpy(), rS
+        err = max(np.abs(g[0] - r[0]).max() / scale[0], np.abs(g[1:4] - r[1:4]).max() / scale[1],
+                  np.abs(g[4] - r[4]).max() / scale[2],
+                  np.abs(dsp.cpu().numpy() - rsp).max() / scale[0])
+        return err
 
-    assert rhs_err(case["G"]) <= 1e-11
+    def state_err(a, b):
+        """grouped max-norm error of two states; momentum against rho c (the box
+        is nearly at rest, so momentum itself is a small residual)"""
+        q = oracle_omp.c2prim(*filled(grown(dict(G=case["G"]), b)))[:, NG:-NG, NG:-NG, NG:-NG]
+        e = max(np.abs(a[0] - b[0]).max() / np.abs(b[0]).max(), np.abs(a[4] - b[4]).max() / np.abs(b[4]).max(),
+                np.abs(a[1:4] - b[1:4]).max() / (q[0] * q[6]).max())
+        for s in range(5, 14):
+            e = max(e, np.abs(a[s] - b[s]).max() / max(np.abs(b[s]).max(), 1e-300))
+        return e
+
+    assert rhs_err(case["G"]) <= 1e-12
     S = np.ascontiguousarray(case["G"][:5].copy())
     sp = np.ascontiguousarray(case["G"][5:].copy())
     steps = 100
@@ -191,8 +215,8 @@ def test_react_64cube_sample_100_steps(ctx, oracle, oracle_omp):
         oracle_step(oracle_omp, S, sp, case["dx"], 1e-8, 2, 4)
     want = np.concatenate([S, sp])[:, NG:-NG, NG:-NG, NG:-NG]
     got = run_gpu(ctx, case, chop_domain(case["n"], 32), steps, 2)
-    assert relerr(got, want) <= 1e-10
-    assert rhs_err(grown(dict(G=case["G"]), want)) <= 1e-11
+    assert state_err(got, want) <= 1e-9
+    assert rhs_err(grown(dict(G=case["G"]), want)) <= 1e-12
     # L1 in density, pressure, Y_OH and Y_H2O (species order H2 O2 H2O H O OH HO2 H2O2 N2)
     assert l1(got[0], want[0]) <= 1e-10
     assert l1(pressure_of(got), pressure_of(want)) <= 1e-10
