@@ -93,6 +93,8 @@ typedef struct ocfd_parm {
 #define OCFD_VISC 1u           /* EBR::do_visc (Source/EBR.cpp:25) */
 #define OCFD_REDISTRIBUTE 2u   /* EBR::do_redistribute (Source/EBR.cpp:27), cut boxes only */
 #define OCFD_FLUX_FP32 4u      /* mixed precision: split + WENO-Z in FP32, FP64 divergence */
+#define OCFD_GRAVITY 16u       /* EBR::do_gravity (Source/EBR.cpp:26): dSdt(UMZ) += g rho, dSdt(UEDEN) += g rho w
+                                  with g = -9.8 in regular boxes (Source/Advance.cpp:331-342) */
 #define OCFD_PER_BOX 8u        /* level / hierarchy steps: the reference's execution model - every
                                   box's RHS stage as its own launches, issued from the host each
                                   step (no graph); for comparison with the batched graph form */
@@ -314,6 +316,13 @@ int ocfd_level_launches_per_step(const ocfd_level* level, unsigned flags);
  * stage 2 whatever the level's time integration: reads two states, writes one)
  * over `reps` back-to-back launches, timed with CUDA events on `stream`.
  * Overwrites the level's stage scratch buffer only. */
+/* Device time of one part of a stage launch, averaged over `reps` (CUDA events
+ * on `stream`; the launches write scratch only): part 0 the whole stage (as
+ * ocfd_level_profile_stage), part 1 the regular boxes' tile kernel alone.
+ * *cells (nullable) receives the cells that part covers.  No counterpart in the
+ * reference (measurement). */
+ocfd_status ocfd_level_profile_part(ocfd_level* level, unsigned flags, int part, int reps, double* ms,
+                                    int64_t* cells, void* stream);
 ocfd_status ocfd_level_profile_stage(ocfd_level* level, unsigned flags, int reps, double* ms,
                                      void* stream);
 

@@ -1749,7 +1749,7 @@ ocfd_status ocfd_amr_fill_ghosts(ocfd_amr* H, void* stream) {
 
 ocfd_status ocfd_amr_advance(ocfd_amr* H, int nsteps, double cfl, unsigned flags, void* stream) {
     if (!H || nsteps < 0 || !(cfl > 0)) return fail(OCFD_BAD_ARG, "ocfd_amr_advance");
-    if (flags & ~(unsigned)(OCFD_FLUX_FP32 | OCFD_PER_BOX))
+    if (flags & ~(unsigned)(OCFD_FLUX_FP32 | OCFD_PER_BOX | OCFD_GRAVITY))
         return fail(OCFD_BAD_ARG, "ocfd_amr_advance: flags (inviscid ideal gas only)");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     for (int i = 0; i < nsteps; ++i) {

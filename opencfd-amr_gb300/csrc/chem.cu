@@ -130,8 +130,23 @@ __device__ __forceinline__ void chem_cell(const double* u, double& E, double* r,
     E += dei;
 }
 
+// Species clip and rescale to the mixture density of one cell (Source/EBR.cpp:341-355),
+// the same arithmetic as k_spec_renorm, applied in the epilogue of a step's last
+// chemistry substep (the cell's density is untouched by the chemistry)
+__device__ __forceinline__ void renorm_cell(double rho, double* r) {
+    double rho0 = 0;
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) {
+        if (r[n] < 0) r[n] = 0.0;
+        rho0 += r[n];
+    }
+    const double tmp = rho / rho0;
+#pragma unroll
+    for (int n = 0; n < NSP; ++n) r[n] = r[n] * tmp;
+}
+
 __global__ void __launch_bounds__(kChemThreads) k_chem_advance(View<double> S, View<double> sp, CellBox B,
-                                                               double dt, DevParm P) {
+                                                               double dt, DevParm P, int renorm) {
     extern __shared__ double smem[];
     const SmemMat U{smem + threadIdx.x, (int)blockDim.x};
     const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -145,6 +160,7 @@ __global__ void __launch_bounds__(kChemThreads) k_chem_advance(View<double> S, V
     for (int n = 0; n < NSP; ++n) r[n] = sp(i, j, k, n);
     double E = u[4];
     chem_cell(u, E, r, dt, P, U);
+    if (renorm) renorm_cell(u[0], r);
 #pragma unroll
     for (int n = 0; n < NSP; ++n) sp(i, j, k, n) = r[n];
     S(i, j, k, 4) = E;
@@ -159,7 +175,7 @@ __global__ void __launch_bounds__(kChemThreads) k_chem_advance_list(const long l
                                                                     const long long* __restrict__ stride,
                                                                     long long ncell, const unsigned* count,
                                                                     const double* __restrict__ dtc, double* Ubuf,
-                                                                    double dt, DevParm P) {
+                                                                    double dt, DevParm P, int renorm) {
     extern __shared__ double smem[];
     const SmemMat U{smem + threadIdx.x, (int)blockDim.x};
     const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -175,6 +191,7 @@ __global__ void __launch_bounds__(kChemThreads) k_chem_advance_list(const long l
     for (int n = 0; n < NSP; ++n) r[n] = x[(5 + n) * ns];
     double E = u[4];
     chem_cell(u, E, r, dt, P, U);
+    if (renorm) renorm_cell(u[0], r);
 #pragma unroll
     for (int n = 0; n < NSP; ++n) x[(5 + n) * ns] = r[n];
     x[4 * ns] = E;
@@ -209,20 +226,20 @@ ocfd_status configure_chem() {
 }
 
 ocfd_status launch_chem_advance(View<double> S, View<double> sp, const CellBox& B, double dt, const DevParm& P,
-                                cudaStream_t st) {
+                                cudaStream_t st, bool renorm) {
     const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
     const int blocks = (int)((n + kChemThreads - 1) / kChemThreads);
-    k_chem_advance<<<blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, st>>>(S, sp, B, dt, P);
+    k_chem_advance<<<blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, st>>>(S, sp, B, dt, P, renorm ? 1 : 0);
     return check_launch("chemistry substep");
 }
 
 ocfd_status launch_chem_advance_list(const long long* off, const long long* stride, long long ncell, double* U,
                                      double dt, const DevParm& P, cudaStream_t st, const unsigned* count,
-                                     const double* dtc) {
+                                     const double* dtc, bool renorm) {
     if (ncell <= 0) return OCFD_OK;
     const long long blocks = (ncell + kChemThreads - 1) / kChemThreads;
     k_chem_advance_list<<<(unsigned)blocks, kChemThreads, sizeof(double) * 90 * kChemThreads, st>>>(
-        off, stride, ncell, count, dtc, U, dt, P);
+        off, stride, ncell, count, dtc, U, dt, P, renorm ? 1 : 0);
     return check_launch("chemistry substep (cell list)");
 }
 

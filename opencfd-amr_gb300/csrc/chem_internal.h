@@ -60,11 +60,14 @@ ocfd_status launch_chem_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cud
 ocfd_status launch_chem_eb_rhs(const ChemBoxArgs& B, const DevParm& P, int sms, cudaStream_t st);
 void chem_args_as_cut(ChemBoxArgs& B, View<const uint32_t> flag, View<const double> vfrac,
                       const View<const double> ap[3]);
+// one implicit chemistry substep per cell; with `renorm` the species clip and
+// rescale of Source/EBR.cpp:333-357 follows in the same thread (a step's last
+// substep)
 ocfd_status launch_chem_advance(View<double> S, View<double> sp, const CellBox& B, double dt, const DevParm& P,
-                                cudaStream_t st);
+                                cudaStream_t st, bool renorm = false);
 ocfd_status launch_chem_advance_list(const long long* off, const long long* stride, long long ncell, double* U,
                                      double dt, const DevParm& P, cudaStream_t st, const unsigned* count = nullptr,
-                                     const double* dtc = nullptr);
+                                     const double* dtc = nullptr, bool renorm = false);
 ocfd_status launch_chem_surrogate(const ocfd_mlp* mlp, const long long* off, const long long* stride, long long ncell,
                                   double* U, double dt, const DevParm& P, const ocfd_surrogate_guard& g,
                                   long long* fb_off, long long* fb_stride, unsigned* fb_count,

@@ -364,20 +364,22 @@ ocfd_status launch_estdt(ocfd_level* L, cudaStream_t st) {
 ocfd_status launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st) {
     const bool visc = flags & OCFD_VISC;
     const bool f32 = flags & OCFD_FLUX_FP32;
+    DevParm P = L->ctx->parm;
+    P.grav = (flags & OCFD_GRAVITY) ? kGravity : 0.0;  // regular boxes only, as the reference
     ocfd_status r = OCFD_OK;
     if (flags & OCFD_PER_BOX) {
         // one launch per regular box (its tiles), then the cut boxes one by one
         for (int b = 0; b < L->nreg && r == OCFD_OK; ++b)
             r = f32 ? launch_rhs_regular_f32(L->tile, visc, nullptr, nullptr, 1, L->h_stage[s][b], L->h_ntiles[b],
-                                             L->ctx->parm, st)
+                                             P, st)
                     : launch_rhs_regular(L->tile, visc, nullptr, nullptr, 1, L->h_stage[s][b], L->h_ntiles[b],
-                                         L->ctx->parm, st);
+                                         P, st);
     } else if (L->ntiles > 0) {
         RegBoxArgs dummy{};
         r = f32 ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[s], L->d_tile_start, L->nreg, dummy, L->ntiles,
-                                         L->ctx->parm, st, L->sched, L->d_queue)
+                                         P, st, L->sched, L->d_queue)
                 : launch_rhs_regular(L->tile, visc, L->d_stage[s], L->d_tile_start, L->nreg, dummy, L->ntiles,
-                                     L->ctx->parm, st, L->sched, L->d_queue);
+                                     P, st, L->sched, L->d_queue);
     }
     if (r == OCFD_OK) r = eb_launch_stage(L, s, flags, st);
     return r;
@@ -934,7 +936,7 @@ ocfd_status ocfd_level_set_time(ocfd_level* L, double time, void* stream) {
 
 ocfd_status ocfd_level_advance(ocfd_level* L, int nsteps, double cfl, unsigned flags, void* stream) {
     if (!L || nsteps < 0 || !(cfl > 0)) return fail(OCFD_BAD_ARG, "ocfd_level_advance");
-    if (flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32 | OCFD_PER_BOX))
+    if (flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32 | OCFD_PER_BOX | OCFD_GRAVITY))
         return fail(OCFD_BAD_ARG, "ocfd_level_advance: flags");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (nsteps == 0) return OCFD_OK;
@@ -1008,9 +1010,37 @@ int ocfd_level_launches_per_step(const ocfd_level* L, unsigned flags) {
 }
 
 ocfd_status ocfd_level_profile_stage(ocfd_level* L, unsigned flags, int reps, double* ms, void* stream) {
-    if (!L || reps <= 0 || !ms) return fail(OCFD_BAD_ARG, "ocfd_level_profile_stage");
+    return ocfd_level_profile_part(L, flags, 0, reps, ms, nullptr, stream);
+}
+
+ocfd_status ocfd_level_profile_part(ocfd_level* L, unsigned flags, int part, int reps, double* ms, int64_t* cells,
+                                    void* stream) {
+    if (!L || reps <= 0 || !ms || part < 0 || part > 1) return fail(OCFD_BAD_ARG, "ocfd_level_profile_part");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    auto launch = [&]() { return launch_stage(L, STAGE_PROBE, flags, st); };
+    if (cells) {
+        long long n = 0;
+        if (part == 0) {
+            n = L->ncells;
+        } else {
+            for (const RegBoxArgs& a : L->h_stage[STAGE_PROBE])
+                n += (long long)(a.hi[0] - a.lo[0] + 1) * (a.hi[1] - a.lo[1] + 1) * (a.hi[2] - a.lo[2] + 1);
+        }
+        *cells = n;
+    }
+    auto launch = [&]() {
+        if (part == 0) return launch_stage(L, STAGE_PROBE, flags, st);
+        // the regular boxes' tile kernel alone, as launch_stage issues it
+        if (L->ntiles <= 0) return OCFD_OK;
+        DevParm P = L->ctx->parm;
+        P.grav = (flags & OCFD_GRAVITY) ? kGravity : 0.0;
+        RegBoxArgs dummy{};
+        const bool visc = flags & OCFD_VISC;
+        return (flags & OCFD_FLUX_FP32)
+                   ? launch_rhs_regular_f32(L->tile, visc, L->d_stage[STAGE_PROBE], L->d_tile_start, L->nreg, dummy,
+                                            L->ntiles, P, st, L->sched, L->d_queue)
+                   : launch_rhs_regular(L->tile, visc, L->d_stage[STAGE_PROBE], L->d_tile_start, L->nreg, dummy,
+                                        L->ntiles, P, st, L->sched, L->d_queue);
+    };
     ocfd_status s = launch();  // warm-up
     if (s != OCFD_OK) return s;
     cudaEvent_t e0, e1;

@@ -19,6 +19,7 @@ struct DevParm {
     double sw_tmp1, sw_tmp2, sw_tmp3;  // 1/(2g), 2(g-1), (3-g)/(2(g-1)): FluxSplit.H:31-34
     double sw_gm1;                     // (g - 1) as written `(gamma - 1)` in FluxSplit.H:41
     double invRg;                      // 1 / Rg
+    double grav;                       // 0, or g = -9.8 when a call asks for OCFD_GRAVITY
     // the same constants rounded to FP32 once on the host, for the mixed form
     float f_gamma, f_smallr, f_smallp, f_invRg, f_C_s, f_T_s, f_kOverMu, f_twoThirds;
     float f_sw_tmp1, f_sw_tmp2, f_sw_tmp3, f_sw_gm1;

@@ -178,7 +178,13 @@ static ocfd_array4 fab_view(const ocfd_level* L, double* base, int b, int comp0,
     return a;
 }
 
-static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
+// One half step of chemistry (chem_substeps substeps of dt / 2 / chem_substeps).
+// With `last` (the second half of a step) the last substep also renormalises
+// the species of every cell it advances (Source/EBR.cpp:333-357, fused into its
+// epilogue); returns in `renormed` whether it did (not in the surrogate form,
+// whose cells finish in two kernels).
+static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches, bool last, bool& renormed) {
+    renormed = false;
     ocfd_level* L = R->L;
     const double dt2 = 0.5 * R->desc.dt / R->desc.chem_substeps;
     const int sms = R->ctx->num_sms;
@@ -208,12 +214,16 @@ static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
                                                                        R->key, R->count, R->off, R->stride);
         launches += 3;
         for (int s = 0; s < R->desc.chem_substeps; ++s) {
-            ocfd_status r = launch_chem_advance_list(R->off, R->stride, R->nactive, L->buf[0], dt2, R->ctx->parm, st);
+            const bool rn = last && s == R->desc.chem_substeps - 1;
+            ocfd_status r = launch_chem_advance_list(R->off, R->stride, R->nactive, L->buf[0], dt2, R->ctx->parm, st,
+                                                     nullptr, nullptr, rn);
             if (r != OCFD_OK) return r;
             ++launches;
         }
+        renormed = last && R->desc.chem_substeps > 0;
         return OCFD_OK;
     }
+    renormed = last && R->desc.chem_substeps > 0;
     for (int s = 0; s < R->desc.chem_substeps; ++s)
         for (size_t b = 0; b < L->boxes.size(); ++b) {
             if (!R->cls.empty() && R->cls[b] == OCFD_BOX_COVERED) continue;
@@ -223,7 +233,8 @@ static ocfd_status chem_half(ocfd_react* R, cudaStream_t st, int& launches) {
                 cb.lo[d] = L->boxes[b].lo[d];
                 cb.n[d] = L->boxes[b].hi[d] - L->boxes[b].lo[d] + 1;
             }
-            ocfd_status r = launch_chem_advance(view_of<double>(&S), view_of<double>(&sp), cb, dt2, R->ctx->parm, st);
+            ocfd_status r = launch_chem_advance(view_of<double>(&S), view_of<double>(&sp), cb, dt2, R->ctx->parm, st,
+                                                last && s == R->desc.chem_substeps - 1);
             if (r != OCFD_OK) return r;
             ++launches;
         }
@@ -288,7 +299,8 @@ static ocfd_status record_react_step(ocfd_react* R, unsigned flags, cudaStream_t
     int launches = 0;
     k_react_begin<<<1, 1, 0, st>>>(L->d_step, R->desc.dt);
     ++launches;
-    ocfd_status s = chem_half(R, st, launches);
+    bool renormed = false;
+    ocfd_status s = chem_half(R, st, launches, false, renormed);
     if (s != OCFD_OK) return s;
     // flow: stage k reads buffer in[k], writes out[k] = a U^n + b (in + dt L(in))
     const bool rk3 = R->desc.rk_order == 3;
@@ -317,9 +329,12 @@ static ocfd_status record_react_step(ocfd_react* R, unsigned flags, cudaStream_t
         s = check_launch("reacting flow stage");
     }
     if (s != OCFD_OK) return s;
-    s = chem_half(R, st, launches);
+    s = chem_half(R, st, launches, true, renormed);
     if (s != OCFD_OK) return s;
+    // species renormalisation of the cells the chemistry did not finish (every
+    // cell in the surrogate form; the covered boxes of a level with a body)
     for (size_t b = 0; b < L->boxes.size(); ++b) {
+        if (renormed && (R->cls.empty() || R->cls[b] != OCFD_BOX_COVERED)) continue;
         ocfd_array4 S = fab_view(L, L->buf[0], (int)b, 0, 5), sp = fab_view(L, L->buf[0], (int)b, 5, NSP);
         CellBox cb{};
         for (int d = 0; d < 3; ++d) {
@@ -509,12 +524,13 @@ ocfd_status ocfd_react_profile_chem(ocfd_react* R, int reps, double* ms, void* s
     ocfd_react_desc d = R->desc;
     R->desc.chem_substeps = 1;
     int launches = 0;
-    ocfd_status s = chem_half(R, st, launches);  // warm-up
+    bool rn = false;
+    ocfd_status s = chem_half(R, st, launches, false, rn);  // warm-up
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    for (int r = 0; r < reps && s == OCFD_OK; ++r) s = chem_half(R, st, launches);
+    for (int r = 0; r < reps && s == OCFD_OK; ++r) s = chem_half(R, st, launches, false, rn);
     cudaEventRecord(e1, st);
     cudaEventSynchronize(e1);
     float t = 0;

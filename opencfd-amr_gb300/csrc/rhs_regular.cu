@@ -83,14 +83,16 @@ extern "C" ocfd_status ocfd_rhs_regular_box_f64(ocfd_context* ctx, const ocfd_ar
         for (int d = 0; d < 3; ++d)
             if (!covers(&flux[d], bx, 0, 5, d))
                 return fail(OCFD_BAD_ARG, "ocfd_rhs_regular_box_f64: flux[d] must cover surroundingNodes(bx,d)");
-    if (flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32))
+    if (flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32 | OCFD_GRAVITY))
         return fail(OCFD_BAD_ARG, "ocfd_rhs_regular_box_f64: unknown flags");
     if (flags & OCFD_FLUX_FP32) return rhs_regular_box_f32(ctx, S, dSdt, flux, bx, dxinv, flags, stream);
+    DevParm P = ctx->parm;
+    P.grav = (flags & OCFD_GRAVITY) ? kGravity : 0.0;
     const int n[3] = {bx.hi[0] - bx.lo[0] + 1, bx.hi[1] - bx.lo[1] + 1, bx.hi[2] - bx.lo[2] + 1};
     const int tile = pick_regular_tile(n, (flags & OCFD_VISC) != 0);
     RegBoxArgs a{};
     fill_regular_args(a, S, dSdt, flux, bx, dxinv, tile);
     const int ntiles = a.ntile[0] * a.ntile[1] * a.ntile[2];
     return launch_rhs_regular(tile, (flags & OCFD_VISC) != 0, nullptr, nullptr, 1, a, ntiles,
-                              ctx->parm, static_cast<cudaStream_t>(stream));
+                              P, static_cast<cudaStream_t>(stream));
 }

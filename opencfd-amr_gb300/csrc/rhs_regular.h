@@ -109,6 +109,9 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* t
     }
 }
 
+// g of the gravity source, Source/Advance.cpp:332
+constexpr double kGravity = -9.8;
+
 int pick_regular_tile(const int n[3], bool visc);
 bool regular_tile_fits(int tile, bool visc);
 ocfd_status configure_rhs_regular();

@@ -25,8 +25,9 @@ ocfd_status rhs_regular_box_f32(ocfd_context* ctx, const ocfd_array4* S, const o
     RegBoxArgs a{};
     fill_regular_args(a, S, dSdt, flux, bx, dxinv, tile);
     const int ntiles = a.ntile[0] * a.ntile[1] * a.ntile[2];
-    return launch_any<float>(tile, visc, nullptr, nullptr, 1, a, ntiles, ctx->parm,
-                             static_cast<cudaStream_t>(stream));
+    DevParm P = ctx->parm;
+    P.grav = (flags & OCFD_GRAVITY) ? kGravity : 0.0;
+    return launch_any<float>(tile, visc, nullptr, nullptr, 1, a, ntiles, P, static_cast<cudaStream_t>(stream));
 }
 
 }  // namespace ocfd

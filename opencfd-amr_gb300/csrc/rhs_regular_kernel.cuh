@@ -359,9 +359,17 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
     const int ci = i0 + ti, cj = j0 + tj, ck = k0 + tk;
     const bool valid = ci <= B.hi[0] && cj <= B.hi[1] && ck <= B.hi[2];
     if (valid) {
+        double L[5];
+#pragma unroll
+        for (int n = 0; n < 5; ++n) L[n] = widen<FT>(acc[n]);
+        if (P.grav != 0.0) {
+            // gravity source after divop, Source/Advance.cpp:331-342
+            L[3] += P.grav * B.S(ci, cj, ck, 0);
+            L[4] += P.grav * B.S(ci, cj, ck, 3);
+        }
         if (B.mode == RHS_WRITE_DSDT) {
 #pragma unroll
-            for (int n = 0; n < 5; ++n) B.dsdt(ci, cj, ck, n) = widen<FT>(acc[n]);
+            for (int n = 0; n < 5; ++n) B.dsdt(ci, cj, ck, n) = L[n];
         } else {
             // fused Shu-Osher stage in FP64: U_out = a U0 + b (U_s + dt L(U_s))
             const double dt = B.dt_ptr ? *B.dt_ptr : B.dt;
@@ -370,7 +378,7 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
             for (int n = 0; n < 5; ++n) {
                 double us = B.S(ci, cj, ck, n);
                 double u0 = B.U0(ci, cj, ck, n);
-                un[n] = B.rk_a * u0 + B.rk_b * (us + dt * widen<FT>(acc[n]));
+                un[n] = B.rk_a * u0 + B.rk_b * (us + dt * L[n]);
                 B.Uout(ci, cj, ck, n) = un[n];
             }
             if (B.cfl_min) {

@@ -19,3 +19,4 @@ VISC = 1
 REDISTRIBUTE = 2
 FLUX_FP32 = 4
 PER_BOX = 8
+GRAVITY = 16

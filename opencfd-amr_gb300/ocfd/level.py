@@ -38,6 +38,9 @@ declare("ocfd_level_set_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
 declare("ocfd_level_cells", ctypes.c_int64, [_vp])
 declare("ocfd_level_set_stop_time", ctypes.c_int, [_vp, ctypes.c_double, _vp])
 declare("ocfd_level_launches_per_step", ctypes.c_int, [_vp, ctypes.c_uint])
+declare("ocfd_level_profile_part", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
+                                                  _vp])
 declare("ocfd_level_profile_stage", ctypes.c_int, [_vp, ctypes.c_uint, ctypes.c_int,
                                                    ctypes.POINTER(ctypes.c_double), _vp])
 
@@ -259,6 +262,15 @@ class Level:
 
     def launches_per_step(self, flags=0):
         return int(self.lib.ocfd_level_launches_per_step(self.h, flags))
+
+    def profile_regular(self, flags=0, reps=10, stream=None):
+        """(ms per launch of the regular boxes' tile kernel of a stage, the cells
+        of the regular boxes)"""
+        ms = ctypes.c_double()
+        cells = ctypes.c_int64()
+        check(self.lib.ocfd_level_profile_part(self.h, flags, 1, reps, ctypes.byref(ms), ctypes.byref(cells),
+                                               _stream_ptr(stream)), "profile_regular")
+        return ms.value, cells.value
 
     def profile_stage(self, flags=0, reps=10, stream=None):
         ms = ctypes.c_double()

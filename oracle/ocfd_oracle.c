@@ -386,7 +386,7 @@ void ocfdo_rhs_regular(const ocfdo_parm* p, const double* S, int nx, int ny, int
                     long long fi = fI(&b, d, i, j, k);
                     for (int n = 0; n < NCONS; ++n)
                         fl[d][n * FN + fi] = weno_face(&b, fp + n * N, fm + n * N, d, i, j, k);
-                    if (do_visc) visc_face(p, &b, q, d, i, j, k, dxinv, fl[d] + fi, FN, 0, 0, 0, 0);
+                    if (do_visc & 1) visc_face(p, &b, q, d, i, j, k, dxinv, fl[d] + fi, FN, 0, 0, 0, 0);
                 }
     }
     long long BN = bN(&b);
@@ -403,6 +403,17 @@ void ocfdo_rhs_regular(const ocfdo_parm* p, const double* S, int nx, int ny, int
                         dxinv[1] * (fy[n * fN(&b, 1) + fI(&b, 1, i, j, k)] - fy[n * fN(&b, 1) + fI(&b, 1, i, j + 1, k)]) +
                         dxinv[2] * (fz[n * fN(&b, 2) + fI(&b, 2, i, j, k)] - fz[n * fN(&b, 2) + fI(&b, 2, i, j, k + 1)]);
                 }
+    if (do_visc & 2) {
+        /* do_gravity, Source/Advance.cpp:331-342: g = -9.8 on the z momentum and the energy */
+        const double g = -9.8;
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    long long c = bI(&b, i, j, k), gc = gI(&b, i, j, k);
+                    dSdt[3 * BN + c] += g * S[0 * N + gc];
+                    dSdt[4 * BN + c] += g * S[3 * N + gc];
+                }
+    }
     free(q); free(fp); free(fm);
 }
 

@@ -65,6 +65,8 @@ void ocfdo_species_enthalpy(const ocfdo_parm* p, double T, double* h);
 void ocfdo_c2prim(const ocfdo_parm* p, int chem, const double* S, const double* spec, int nx,
                   int ny, int nz, double* q);
 
+/* do_visc: bit 0 the viscous flux (EBR::do_visc), bit 1 the gravity source
+ * (EBR::do_gravity, Source/Advance.cpp:331-342) */
 void ocfdo_rhs_regular(const ocfdo_parm* p, const double* S, int nx, int ny, int nz,
                        const double* dxinv, int do_visc, double* dSdt, double* fx, double* fy,
                        double* fz);

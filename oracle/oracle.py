@@ -156,13 +156,14 @@ class Oracle:
         self.lib.ocfdo_c2prim(self.pp, int(chem), _ptr(S), _ptr(spec), nx, ny, nz, _ptr(q))
         return q
 
-    def rhs_regular(self, S, dxinv, do_visc=False):
+    def rhs_regular(self, S, dxinv, do_visc=False, do_gravity=False):
         _, gz, gy, gx = S.shape
         nx, ny, nz = gx - 2 * NG, gy - 2 * NG, gz - 2 * NG
         dS = np.zeros((5, nz, ny, nx))
         f = [np.zeros(face_shape(5, nx, ny, nz, d)) for d in range(3)]
         dx = (ctypes.c_double * 3)(*dxinv)
-        self.lib.ocfdo_rhs_regular(self.pp, _ptr(S), nx, ny, nz, dx, int(do_visc), _ptr(dS),
+        self.lib.ocfdo_rhs_regular(self.pp, _ptr(S), nx, ny, nz, dx, int(bool(do_visc)) | (2 if do_gravity else 0),
+                                   _ptr(dS),
                                    _ptr(f[0]), _ptr(f[1]), _ptr(f[2]))
         return dS, f
 
@@ -267,11 +268,12 @@ class Oracle:
         self.lib.ocfdo_fill_ghosts(ctypes.byref(bc), _ptr(S), nc, gx - 2 * NG, gy - 2 * NG,
                                    gz - 2 * NG, time)
 
-    def advance_rk3(self, bc, S, cfl, nsteps, form=0, do_visc=False):
+    def advance_rk3(self, bc, S, cfl, nsteps, form=0, do_visc=False, do_gravity=False):
         _, gz, gy, gx = S.shape
         dts = np.zeros(nsteps)
         t = self.lib.ocfdo_advance_rk3(self.pp, ctypes.byref(bc), _ptr(S), gx - 2 * NG,
-                                       gy - 2 * NG, gz - 2 * NG, int(do_visc), cfl, nsteps, form,
+                                       gy - 2 * NG, gz - 2 * NG, int(bool(do_visc)) | (2 if do_gravity else 0),
+                                       cfl, nsteps, form,
                                        _ptr(dts))
         return t, dts
 

@@ -62,9 +62,9 @@ def run_gpu(ctx, case, nsteps, cfl, max_grid, flags=0, tile=-1):
     return out, t
 
 
-def run_oracle(oracle, case, nsteps, cfl, visc=False):
+def run_oracle(oracle, case, nsteps, cfl, visc=False, gravity=False):
     S = np.ascontiguousarray(case["G"].copy())
-    t, dts = oracle.advance_rk3(oracle_bc(case), S, cfl, nsteps, form=1, do_visc=visc)
+    t, dts = oracle.advance_rk3(oracle_bc(case), S, cfl, nsteps, form=1, do_visc=visc, do_gravity=gravity)
     return valid(S), t
 
 
@@ -192,3 +192,21 @@ def test_valid_copies(ctx):
     lev.copy_valid_out(dv)
     assert np.array_equal(dv.cpu().numpy(), lev.copy_valid_out())
     lev.close()
+
+
+def test_gravity_level_vs_oracle(ctx, oracle):
+    """A level advanced with OCFD_GRAVITY (the source in the fused stage of every
+    regular box) against the oracle's RK3 with do_gravity; and the flag changes
+    the result"""
+    import ocfd
+    from ocfd.cases import sod
+    case = sod(48, 12, 8)
+    G = case["G"].copy()
+    G[0] *= 1.2; G[4] *= 1.0e5
+    case = dict(case, G=G, dx=(1e-2, 1e-2, 1e-2))
+    ref, tr = run_oracle(oracle, case, 6, 0.4, gravity=True)
+    got, tg = run_gpu(ctx, case, 6, 0.4, (16, 12, 8), flags=ocfd.GRAVITY)
+    nog, _ = run_gpu(ctx, case, 6, 0.4, (16, 12, 8))
+    assert tg == pytest.approx(tr, rel=1e-13)
+    assert relerr(got, ref) < 1e-10
+    assert np.abs(got[3] - nog[3]).max() > 0
