@@ -8,6 +8,7 @@
 #include "ocfd_internal.h"
 #include "mechanism.h"
 #include "rhs_regular.h"
+#include "eb_level.h"
 
 namespace ocfd {
 
@@ -151,6 +152,7 @@ ocfd_status ocfd_context_create(const ocfd_parm* parm, int device, ocfd_context*
     if (s == OCFD_OK) s = configure_rhs_regular();
     if (s == OCFD_OK) s = configure_rhs_regular_f32();
     if (s == OCFD_OK) s = configure_chem();
+    if (s == OCFD_OK) s = configure_eb_tile();
     if (s == OCFD_OK) s = eb_static_scratch_resolve(ctx);
     if (s != OCFD_OK) {
         cudaFree(ctx->d_error);

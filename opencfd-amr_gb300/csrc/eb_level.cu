@@ -42,6 +42,7 @@
 #include <cmath>
 #include <map>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "eb_level.h"
@@ -493,6 +494,318 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
     if (A.cfl_min) block_min_atomic(local_dt, A.cfl_min);
 }
 
+// ------------------------------------------------------------ fused tile kernel
+// The batched cut-cell stage as one kernel: one CTA per 8x8x4 tile of a cut or
+// covered box.  The primitives of grow(tile, 2) and the tile's face fluxes in x,
+// y and z stay in shared memory; each cell thread then forms the cut-cell
+// divergence with the wall flux (Source/EB/EBkernels.H:216-338, negated, the
+// small-cell rescale of flux_redist :341-377), the Shu-Osher stage and the CFL
+// bound.  Only the state (read over grow(tile, 2), the stage input U0, the
+// output) and the z-invariant geometry touch memory: no primitive or face-flux
+// scratch round trip.  A face on a tile boundary is computed by both tiles and
+// added to the flux registers by the one that owns it (faces 0 .. T_D - 1 of the
+// tile, plus the box's high face), so that every face is accumulated once.  The
+// arithmetic per face and per cell is that of k_ebl_faces / k_ebl_div_stage;
+// the per-box form (OCFD_PER_BOX) keeps those three kernels.
+constexpr int EBT_X = 8, EBT_Y = 8, EBT_Z = 4, EBT_N = EBT_X * EBT_Y * EBT_Z;
+constexpr int EBQ_X = EBT_X + 4, EBQ_Y = EBT_Y + 4, EBQ_Z = EBT_Z + 4, EBQ_N = EBQ_X * EBQ_Y * EBQ_Z;
+constexpr int EBF_N0 = (EBT_X + 1) * EBT_Y * EBT_Z, EBF_N1 = EBT_X * (EBT_Y + 1) * EBT_Z,
+              EBF_N2 = EBT_X * EBT_Y * (EBT_Z + 1);
+
+template <bool F32>
+__host__ __device__ constexpr size_t ebt_smem_bytes() {
+    return (F32 ? sizeof(float) : sizeof(double)) * (7 * EBQ_N + 5 * (EBF_N0 + EBF_N1 + EBF_N2));
+}
+
+// faces of direction D of the tile at (i0, j0, k0) of box B into sf (5 x EBF_N[D])
+template <bool F32, int D>
+__device__ __forceinline__ void ebt_faces(const EbStageArgs& A, const EbStageBox& B, const DevParm& P, int i0,
+                                          int j0, int k0, double dt,
+                                          typename std::conditional<F32, float, double>::type* sq,
+                                          typename std::conditional<F32, float, double>::type* sf) {
+    using FT = typename std::conditional<F32, float, double>::type;
+    constexpr int FX = EBT_X + (D == 0), FY = EBT_Y + (D == 1), FZ = EBT_Z + (D == 2), NF = FX * FY * FZ;
+    constexpr int di = D == 0, dj = D == 1, dk = D == 2;
+    constexpr int SD = D == 0 ? 1 : (D == 1 ? EBQ_X : EBQ_X * EBQ_Y);
+    for (int f = threadIdx.x; f < NF; f += EBT_N) {
+        const int fx = f % FX, fy = (f / FX) % FY, fz = f / (FX * FY);
+        const int i = i0 + fx, j = j0 + fy, k = k0 + fz;
+        if (i > B.hi[0] + di || j > B.hi[1] + dj || k > B.hi[2] + dk) continue;
+        const uint32_t fl = B.flag(i, j, k);
+        const FT* p0 = sq + (fx + 2) + (fy + 2) * EBQ_X + (fz + 2) * EBQ_X * EBQ_Y;
+        double flx[5];
+        if (F32) {
+            const bool cm1 = eb_conn(fl, -di, -dj, -dk), cm2 = eb_conn(fl, -2 * di, -2 * dj, -2 * dk),
+                       cp1 = eb_conn(fl, di, dj, dk);
+            float ql[7], qr[7], ff[5];
+#pragma unroll
+            for (int m = 0; m < 7; ++m) {
+                if (m == QT) {
+                    ql[m] = qr[m] = 0.0f;
+                    continue;
+                }
+                const FT* pm = p0 + m * EBQ_N;
+                const float vm2 = pm[-2 * SD], vm1 = pm[-SD], v0 = pm[0], vp1 = pm[SD];
+                float l = vm1, r = v0;
+                if (cm1) {
+                    if (cm2) l = vm1 + 0.5f * minmod<float>(v0 - vm1, vm1 - vm2);
+                    if (cp1) r = v0 - 0.5f * minmod<float>(vp1 - v0, v0 - vm1);
+                }
+                ql[m] = l;
+                qr[m] = r;
+            }
+            vanleer<float>(P.f_smallp, P.f_gamma, ql, qr, D, ff);
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                sf[m * NF + f] = ff[m];
+                flx[m] = f2d_bits(ff[m]);
+            }
+        } else {
+            double ql[7], qr[7];
+#pragma unroll
+            for (int m = 0; m < 7; ++m) {
+                const FT* pm = p0 + m * EBQ_N;
+                eb_recon(fl, D, (double)pm[-2 * SD], (double)pm[-SD], (double)pm[0], (double)pm[SD], ql[m], qr[m]);
+            }
+            vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
+            if (A.visc) {
+                const View<const double> qv{reinterpret_cast<const double*>(sq), EBQ_X, (long long)EBQ_X * EBQ_Y,
+                                            EBQ_N, i0 - 2, j0 - 2, k0 - 2};
+                eb_visc_face(P, qv, B.flag, D, i, j, k, A.dxinv, flx, 1, false, 0, 0, 0);
+            }
+#pragma unroll
+            for (int m = 0; m < 5; ++m) sf[m * NF + f] = flx[m];
+        }
+        if (B.has_flux) {
+            const int g = D == 0 ? i : (D == 1 ? j : k);
+            const int fd = D == 0 ? fx : (D == 1 ? fy : fz);
+            constexpr int TD = D == 0 ? EBT_X : (D == 1 ? EBT_Y : EBT_Z);
+            if (fd < TD || g == B.hi[D] + 1) {
+                const double w = B.flux_w * dt * B.ap[D](i, j, k);
+                if (B.has_flux & FLUX_ACC_ALL) {
+#pragma unroll
+                    for (int m = 0; m < 5; ++m) B.creg[D](i, j, k, m) += w * flx[m];
+                }
+                if ((B.has_flux & FLUX_ACC_PLANES) && (g == B.lo[D] || g == B.hi[D] + 1)) {
+                    const View<double>& pl = B.fplane[D][g == B.lo[D] ? 0 : 1];
+#pragma unroll
+                    for (int m = 0; m < 5; ++m) pl(i, j, k, m) += w * flx[m];
+                }
+            }
+        }
+    }
+}
+
+template <bool F32>
+__global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __restrict__ tstart, DevParm P) {
+    using FT = typename std::conditional<F32, float, double>::type;
+    extern __shared__ __align__(16) unsigned char ebt_raw[];
+    FT* sq = reinterpret_cast<FT*>(ebt_raw);
+    FT* sf0 = sq + 7 * EBQ_N;
+    FT* sf1 = sf0 + 5 * EBF_N0;
+    FT* sf2 = sf1 + 5 * EBF_N1;
+    const double dt = *A.dt_ptr;
+    double local_dt = __longlong_as_double(0x7FF0000000000000LL);
+    // the box of this tile (prefix table over the cut / covered boxes)
+    int t = blockIdx.x;
+    int lo = 0, hi = A.nbox - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tstart[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const EbStageBox& B = A.boxes[lo];
+    t -= tstart[lo];
+    const int ntx = (B.hi[0] - B.lo[0] + EBT_X) / EBT_X, nty = (B.hi[1] - B.lo[1] + EBT_Y) / EBT_Y;
+    const int i0 = B.lo[0] + (t % ntx) * EBT_X, j0 = B.lo[1] + ((t / ntx) % nty) * EBT_Y,
+              k0 = B.lo[2] + (t / (ntx * nty)) * EBT_Z;
+    const int tid = threadIdx.x;
+    if (!B.covered) {
+        // 1. primitives over grow(tile, 2) (within the box's grow(bx, 2))
+        for (int c = tid; c < EBQ_N; c += EBT_N) {
+            const int qx = c % EBQ_X, qy = (c / EBQ_X) % EBQ_Y, qz = c / (EBQ_X * EBQ_Y);
+            const int i = i0 - 2 + qx, j = j0 - 2 + qy, k = k0 - 2 + qz;
+            if (i > B.hi[0] + 2 || j > B.hi[1] + 2 || k > B.hi[2] + 2) continue;
+            if (F32) {
+                const float g = P.f_gamma;
+                const float u0 = d2f_bits(B.S(i, j, k, 0)), u1 = d2f_bits(B.S(i, j, k, 1)),
+                            u2 = d2f_bits(B.S(i, j, k, 2)), u3 = d2f_bits(B.S(i, j, k, 3)),
+                            u4 = d2f_bits(B.S(i, j, k, 4));
+                const float rho = fmaxf(u0, P.f_smallr);
+                const float rhoinv = __frcp_rn(rho);
+                const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
+                const float p = fmaxf((g - 1.0f) * (u4 - rho * (0.5f * (ux * ux + uy * uy + uz * uz))), P.f_smallp);
+                sq[QRHO * EBQ_N + c] = rho;
+                sq[QU * EBQ_N + c] = ux;
+                sq[QV * EBQ_N + c] = uy;
+                sq[QW * EBQ_N + c] = uz;
+                sq[QPRES * EBQ_N + c] = p;
+                sq[QT * EBQ_N + c] = 0.0f;
+                sq[QC * EBQ_N + c] = sqrtf(g * p * rhoinv);
+            } else {
+                double q[7];
+                c2prim_ideal_fast(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3),
+                                  B.S(i, j, k, 4), q);
+#pragma unroll
+                for (int m = 0; m < 7; ++m) sq[m * EBQ_N + c] = q[m];
+            }
+        }
+        __syncthreads();
+        // 2. face fluxes of the tile in x, y, z
+        ebt_faces<F32, 0>(A, B, P, i0, j0, k0, dt, sq, sf0);
+        ebt_faces<F32, 1>(A, B, P, i0, j0, k0, dt, sq, sf1);
+        ebt_faces<F32, 2>(A, B, P, i0, j0, k0, dt, sq, sf2);
+        __syncthreads();
+    }
+    // 3. cut-cell divergence, stage and CFL bound per cell
+    const int ti = tid % EBT_X, tj = (tid / EBT_X) % EBT_Y, tk = tid / (EBT_X * EBT_Y);
+    const int i = i0 + ti, j = j0 + tj, k = k0 + tk;
+    if (i <= B.hi[0] && j <= B.hi[1] && k <= B.hi[2]) {
+        // face fluxes of the cell: low and high face per direction, component stride
+        const int fxl = ti + tj * (EBT_X + 1) + tk * (EBT_X + 1) * EBT_Y;
+        const int fyl = ti + tj * EBT_X + tk * EBT_X * (EBT_Y + 1);
+        const int fzl = ti + tj * EBT_X + tk * EBT_X * EBT_Y;
+        const int qc = (ti + 2) + (tj + 2) * EBQ_X + (tk + 2) * EBQ_X * EBQ_Y;
+        auto FXm = [&](int m) { return sf0[m * EBF_N0 + fxl]; };
+        auto FXp = [&](int m) { return sf0[m * EBF_N0 + fxl + 1]; };
+        auto FYm = [&](int m) { return sf1[m * EBF_N1 + fyl]; };
+        auto FYp = [&](int m) { return sf1[m * EBF_N1 + fyl + EBT_X]; };
+        auto FZm = [&](int m) { return sf2[m * EBF_N2 + fzl]; };
+        auto FZp = [&](int m) { return sf2[m * EBF_N2 + fzl + EBT_X * EBT_Y]; };
+        double L[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (!B.covered) {
+            const uint32_t f = B.flag(i, j, k);
+            if (F32) {
+                float out[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                const float vf = d2f_bits(B.vfrac(i, j, k));
+                if (eb_regular(f)) {
+#pragma unroll
+                    for (int m = 0; m < 5; ++m)
+                        out[m] = A.dxinv_f[0] * ((float)FXp(m) - (float)FXm(m)) +
+                                 A.dxinv_f[1] * ((float)FYp(m) - (float)FYm(m)) +
+                                 A.dxinv_f[2] * ((float)FZp(m) - (float)FZm(m));
+                } else if (!eb_covered(f)) {
+                    const float tmp = __fdividef(A.dxinv_f[0], vf);
+                    const float axm = d2f_bits(B.ap[0](i, j, k)), axp = d2f_bits(B.ap[0](i + 1, j, k));
+                    const float aym = d2f_bits(B.ap[1](i, j, k)), ayp = d2f_bits(B.ap[1](i, j + 1, k));
+                    const float azm = d2f_bits(B.ap[2](i, j, k)), azp = d2f_bits(B.ap[2](i, j, k + 1));
+#pragma unroll
+                    for (int m = 0; m < 5; ++m)
+                        out[m] = tmp * (axp * (float)FXp(m) - axm * (float)FXm(m) + ayp * (float)FYp(m) -
+                                        aym * (float)FYm(m) + azp * (float)FZp(m) - azm * (float)FZm(m));
+                    const float pr = (float)sq[QPRES * EBQ_N + qc];
+                    out[1] += (axm - axp) * pr * tmp;
+                    out[2] += (aym - ayp) * pr * tmp;
+                    out[3] += (azm - azp) * pr * tmp;
+                }
+                const bool rescale = A.redist && vf < 0.5f && vf > 0.0f;
+#pragma unroll
+                for (int m = 0; m < 5; ++m) L[m] = f2d_bits(rescale ? -(vf * out[m]) : -out[m]);
+            } else {
+                const double vf = B.vfrac(i, j, k);
+                double out[5];
+                if (eb_covered(f)) {
+#pragma unroll
+                    for (int m = 0; m < 5; ++m) out[m] = 0.0;
+                } else if (eb_regular(f)) {
+#pragma unroll
+                    for (int m = 0; m < 5; ++m)
+                        out[m] = A.dxinv[0] * ((double)FXp(m) - (double)FXm(m)) +
+                                 A.dxinv[1] * ((double)FYp(m) - (double)FYm(m)) +
+                                 A.dxinv[2] * ((double)FZp(m) - (double)FZm(m));
+                } else {
+                    const double tmp = A.dxinv[0] / vf;
+                    const double axm = B.ap[0](i, j, k), axp = B.ap[0](i + 1, j, k);
+                    const double aym = B.ap[1](i, j, k), ayp = B.ap[1](i, j + 1, k);
+                    const double azm = B.ap[2](i, j, k), azp = B.ap[2](i, j, k + 1);
+#pragma unroll
+                    for (int m = 0; m < 5; ++m)
+                        out[m] = tmp * (axp * (double)FXp(m) - axm * (double)FXm(m) + ayp * (double)FYp(m) -
+                                        aym * (double)FYm(m) + azp * (double)FZp(m) - azm * (double)FZm(m));
+                    double fw[5];
+                    const double pr = (double)sq[QPRES * EBQ_N + qc];
+                    if (!A.visc) {
+                        // slip-wall pressure flux, EBkernels.H:305-311
+                        fw[0] = 0.0;
+                        fw[1] = (axm - axp) * pr;
+                        fw[2] = (aym - ayp) * pr;
+                        fw[3] = (azm - azp) * pr;
+                        fw[4] = 0.0;
+                    } else {
+                        // eb_wallflux, EBkernels.H:173-214
+                        const double d = (double)sq[QRHO * EBQ_N + qc], u = (double)sq[QU * EBQ_N + qc],
+                                     v = (double)sq[QV * EBQ_N + qc], w = (double)sq[QW * EBQ_N + qc],
+                                     cs = (double)sq[QC * EBQ_N + qc];
+                        const double apnorm = sqrt((axm - axp) * (axm - axp) + (aym - ayp) * (aym - ayp) +
+                                                   (azm - azp) * (azm - azp));
+                        const double un = u * (axm - axp) + v * (aym - ayp) + w * (azm - azp);
+                        const double lambda0 = fabs(un) + cs * apnorm;
+                        const double gamma = P.gamma;
+                        const double E0 = pr / (gamma - 1) + 0.50 * d * (u * u + v * v + w * w);
+                        double fpw[5], fmw[5];
+                        fpw[0] = 0.5 * (d * un + lambda0 * d);
+                        fpw[1] = 0.5 * (d * u * un + (axm - axp) * pr + lambda0 * d * u);
+                        fpw[2] = 0.5 * (d * v * un + (aym - ayp) * pr + lambda0 * d * v);
+                        fpw[3] = 0.5 * (d * w * un + (azm - azp) * pr + lambda0 * d * w);
+                        fpw[4] = 0.5 * ((E0 + pr) * un + lambda0 * E0);
+                        fmw[0] = 0.5 * (d * (-un) - lambda0 * d);
+                        fmw[1] = fpw[1];
+                        fmw[2] = fpw[2];
+                        fmw[3] = fpw[3];
+                        fmw[4] = 0.5 * (-(E0 + pr) * un - lambda0 * E0);
+#pragma unroll
+                        for (int m = 0; m < 5; ++m) fw[m] = fpw[m] + fmw[m];
+                    }
+#pragma unroll
+                    for (int m = 0; m < 5; ++m) out[m] += fw[m] * tmp;
+                }
+                const bool rescale = A.redist && vf < 0.5 && vf > 0.0;
+#pragma unroll
+                for (int m = 0; m < 5; ++m) {
+                    const double divc = out[m] * -1.0;
+                    L[m] = rescale ? vf * divc : divc;
+                }
+            }
+        }
+        double un[5];
+#pragma unroll
+        for (int n = 0; n < 5; ++n) {
+            const double us = B.S(i, j, k, n);
+            const double u0 = B.U0(i, j, k, n);
+            un[n] = B.rk_a * u0 + B.rk_b * (us + dt * L[n]);
+            B.Uout(i, j, k, n) = un[n];
+        }
+        if (A.cfl_min) {
+            double v;
+            if (F32) {
+                const float g = P.f_gamma;
+                const float rho = d2f_bits(un[0]);
+                const float rhoinv = __frcp_rn(fmaxf(rho, P.f_smallr));
+                const float vx = d2f_bits(un[1]) * rhoinv, vy = d2f_bits(un[2]) * rhoinv, vz = d2f_bits(un[3]) * rhoinv;
+                const float p = fmaxf((g - 1.0f) * (d2f_bits(un[4]) - 0.5f * rho * (vx * vx + vy * vy + vz * vz)),
+                                      P.f_smallp);
+                const float cs = sqrtf(g * p * rhoinv);
+                const float dtx = __fdividef(A.dx_f[0], fabsf(vx) + cs);
+                const float dty = __fdividef(A.dx_f[1], fabsf(vy) + cs);
+                const float dtz = __fdividef(A.dx_f[2], fabsf(vz) + cs);
+                v = f2d_bits(fminf(dtx, fminf(dty, dtz)));
+            } else {
+                v = cfl_bound(P, un, A.dx);
+            }
+            local_dt = v < local_dt ? v : local_dt;
+        }
+    }
+    if (A.cfl_min) block_min_atomic(local_dt, A.cfl_min);
+}
+
+ocfd_status configure_eb_tile() {
+    if (cudaFuncSetAttribute(k_ebl_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)ebt_smem_bytes<false>()) != cudaSuccess ||
+        cudaFuncSetAttribute(k_ebl_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)ebt_smem_bytes<true>()) != cudaSuccess)
+        return check_launch("configure cut-cell tile kernel");
+    return OCFD_OK;
+}
+
 }  // namespace ocfd
 
 // ------------------------------------------------------------------ host side
@@ -515,6 +828,9 @@ struct ocfd::EbLevel {
     std::vector<long long> pcount, fcount, ccount;
     long long* d_floc = nullptr;  // (0, F0, F0 + F1) per box
     long long* d_zero = nullptr;
+    // fused tile kernel: first tile of each cut / covered box, tiles in total
+    int* d_tstart = nullptr;
+    int ntiles = 0;
     int *d_pchunk = nullptr, *d_fchunk = nullptr, *d_cchunk = nullptr;
 };
 
@@ -534,6 +850,9 @@ static void eb_free_tables(ocfd_level* L) {
     dev_free(E->d_pchunk, L->pool);
     dev_free(E->d_fchunk, L->pool);
     dev_free(E->d_cchunk, L->pool);
+    dev_free(E->d_tstart, L->pool);
+    E->d_tstart = nullptr;
+    E->ntiles = 0;
     E->d_pstart = E->d_fstart = E->d_cstart = E->d_floc = E->d_zero = nullptr;
     E->d_pchunk = E->d_fchunk = E->d_cchunk = nullptr;
 }
@@ -757,7 +1076,9 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     }
     std::vector<EbStageBox> st[NUM_STAGE_SLOTS];
     std::vector<long long> ps(ne), fs(3 * ne), cs(ne), floc(3 * ne);
+    std::vector<int> ts(ne);
     long long pt = 0, ft = 0, ct = 0;
+    int tt = 0;
     E->pcount.assign(ne, 0);
     E->fcount.assign(ne, 0);
     E->ccount.assign(ne, 0);
@@ -778,6 +1099,8 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
         cs[e] = ct;
         ct += (long long)n[0] * n[1] * n[2];
         E->ccount[e] = ct - cs[e];
+        ts[e] = tt;
+        tt += ((n[0] + EBT_X - 1) / EBT_X) * ((n[1] + EBT_Y - 1) / EBT_Y) * ((n[2] + EBT_Z - 1) / EBT_Z);
         EbStageBox base{};
         for (int d = 0; d < 3; ++d) {
             base.lo[d] = B.lo[d];
@@ -830,7 +1153,9 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
     E->ptotal = pt;
     E->ftotal = ft;
     E->ctotal = ct;
+    E->ntiles = tt;
     ocfd_status s = OCFD_OK;
+    s = upload(&E->d_tstart, ts, L->pool);
     for (int k = 0; k < NUM_STAGE_SLOTS && s == OCFD_OK; ++k) s = upload(&E->d_stage[k], st[k], L->pool);
     if (s == OCFD_OK) s = upload(&E->d_pstart, ps, L->pool);
     if (s == OCFD_OK) s = upload(&E->d_fstart, fs, L->pool);
@@ -908,16 +1233,13 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
         }
         return check_launch("level cut-cell stage (per box)");
     }
-    if (A.ptotal > 0) {
-        if (f32) k_ebl_prims<true><<<grid_for(A.ptotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
-        else k_ebl_prims<false><<<grid_for(A.ptotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
+    // batched: every cut and covered box in one launch of the fused tile kernel
+    if (E->ntiles > 0) {
+        if (f32)
+            k_ebl_tile<true><<<E->ntiles, EBT_N, ebt_smem_bytes<true>(), st>>>(A, E->d_tstart, L->ctx->parm);
+        else
+            k_ebl_tile<false><<<E->ntiles, EBT_N, ebt_smem_bytes<false>(), st>>>(A, E->d_tstart, L->ctx->parm);
     }
-    if (A.ftotal > 0) {
-        if (f32) k_ebl_faces<true><<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
-        else k_ebl_faces<false><<<grid_for(A.ftotal, 128, sms), 128, 0, st>>>(A, L->ctx->parm);
-    }
-    if (f32) k_ebl_div_stage<true><<<grid_for(A.ctotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
-    else k_ebl_div_stage<false><<<grid_for(A.ctotal, 256, sms), 256, 0, st>>>(A, L->ctx->parm);
     return check_launch("level cut-cell stage");
 }
 
@@ -929,7 +1251,7 @@ int eb_launches_per_stage(const ocfd_level* L, unsigned flags) {
         for (int b : E->ebox) n += E->cls[b] == OCFD_BOX_CUT ? 3 : 1;
         return n;
     }
-    return (E->ptotal > 0) + (E->ftotal > 0) + 1;
+    return E->ntiles > 0 ? 1 : 0;
 }
 
 }  // namespace ocfd

@@ -21,6 +21,8 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles);
 // The cut-cell stage s of L: primitives, faces, divergence + RK update (+ CFL).
 ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st);
 int eb_launches_per_stage(const ocfd_level* L, unsigned flags);
+// shared-memory opt-in of the fused cut-cell tile kernel (context creation)
+ocfd_status configure_eb_tile();
 // true when box b takes the regular path (no body, or classified regular)
 bool eb_box_regular(const ocfd_level* L, int b);
 // device pointer to the z-invariant volume fraction of box b over grow(bx, 5)
