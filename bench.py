@@ -76,6 +76,9 @@ NCU_DRAM_BYTES_PER_CELL = {
     ("cube", "fp32"): 566.6e6 / 4194304,
     # k_chem_advance_list, 128^3 reacting box: 309 + 126 MB over 2,097,152 cells
     ("react", "chem"): (309e6 + 126e6) / 2097152,
+    # k_rhs_regular<double, 8, 8, 8> (the jet's FP64 headline kernel), captured on the 3D blast
+    # 256x256x64 (64^3 boxes, as the jet's regular boxes): 416.4 + 141.2 MB over 4,194,304 cells
+    ("jet-eb-amr", "fp64"): (416.4e6 + 141.2e6) / 4194304,
 }
 
 
@@ -353,7 +356,7 @@ def amr_matched_l1(ctx, c, snap, steps=L1_STEPS, mk=None):
     return out
 
 
-JET_N = (256, 128, 128)
+JET_N = tuple(int(x) for x in os.environ.get("OCFD_BENCH_JET_BASE", "256,128,128").split(","))
 JET_DEV_STEPS = 20
 JET_MAX_GRID = 64
 JET_BLOCKING = 8

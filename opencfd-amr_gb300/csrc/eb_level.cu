@@ -5,19 +5,17 @@
 // cut and covered cells -> the regular WENO-Z chain (:231); otherwise the
 // cut-cell scheme eb_compute_dSdt_box (Source/EB/AdvanceBox.cpp:16-228).  Here
 // the regular boxes stay in the fused tile kernel, and all cut and covered boxes
-// of the level run as one batch per RK stage:
-//   k_ebl_prims       primitives over grow(bx, 2) of every cut box     (c2prim)
-//   k_ebl_faces       every face of every cut box in x, y and z: MUSCL-minmod
-//                     states, Van Leer flux, EB viscous flux; RK-weighted
-//                     area-fraction fluxes into the flux registers (AMR)
-//   k_ebl_div_stage   per cell: cut-cell divergence with the wall flux, negated
-//                     (zero in covered boxes), fused with the Shu-Osher stage
-//                     update and the CFL bound of the new state
-// In the mixed form (OCFD_FLUX_FP32, inviscid) the primitives (from the narrowed
-// state), the face states, the Van Leer flux, the cut-cell divergence with the
-// slip-wall pressure flux and the CFL bound are FP32 (FP32 scratch); the RK
-// stage update stays FP64.
-// Work items of a batch are addressed through prefix sums over the boxes.
+// of the level run as one launch per RK stage of k_ebl_tile: one CTA per 8x8x4
+// tile, primitives over grow(tile, 2) (c2prim), the tile's faces in x, y and z
+// (MUSCL-minmod states, Van Leer flux, EB viscous flux; RK-weighted
+// area-fraction fluxes into the flux registers of an AMR level) in shared
+// memory, then per cell the cut-cell divergence with the wall flux, negated
+// (zero in covered boxes), fused with the Shu-Osher stage update and the CFL
+// bound of the new state.  In the mixed form (OCFD_FLUX_FP32, inviscid) the
+// primitives (from the narrowed state), the face states, the Van Leer flux, the
+// cut-cell divergence with the slip-wall pressure flux and the CFL bound are
+// FP32; the RK stage update stays FP64.  Tiles are addressed through a prefix
+// table over the boxes.
 //
 // Geometry.  AMReX EB2 (Source/Geometry.cpp:9-29) is absent.  For a body
 // extruded along z the cut-cell data do not depend on z, so each box keeps 2D
@@ -176,9 +174,6 @@ struct EbStageBox {
     View<double> Uout;
     View<const uint32_t> flag;
     View<const double> vfrac, ap[3];
-    View<double> q, flux[3];
-    // the same scratch read as FP32 arrays (same element strides) in the mixed form
-    View<float> qf, fluxf[3];
     int lo[3], hi[3];
     double rk_a, rk_b;
     int covered;
@@ -188,311 +183,15 @@ struct EbStageBox {
     View<double> fplane[3][2];
 };
 
-// Work items of a batch are found through the prefix sums over the boxes; a
-// chunk table (the tag holding item 128 c, for every c) replaces the binary
-// search by one load and a short forward scan.
-constexpr int EB_CHUNK_LOG2 = 7;
-
-__device__ __forceinline__ int tag_of(const long long* start, const int* chunk, int ntag, long long idx) {
-    if (!chunk) return find_tag<int>(start, ntag, idx);
-    int t = chunk[idx >> EB_CHUNK_LOG2];
-    while (t + 1 < ntag && start[t + 1] <= idx) ++t;
-    return t;
-}
-
 struct EbStageArgs {
     const EbStageBox* boxes;
     int nbox;
-    const int *pchunk, *fchunk, *cchunk;  // chunk tables (nullptr: binary search)
-    const long long* pstart;  // grow(bx, 2) cells of each box (0 for covered boxes)
-    long long ptotal;
-    const long long* fstart;  // faces, tag 3 b + d (0 for covered boxes)
-    long long ftotal;
-    const long long* cstart;  // valid cells of each box
-    long long ctotal;
     double dxinv[3], dx[3];
     float dxinv_f[3], dx_f[3];  // FP32 copies for the mixed form
     const double* dt_ptr;
     unsigned long long* cfl_min;
     int visc, redist;
 };
-
-// F32 (mixed form): c2prim in FP32 from the state narrowed on the integer
-// pipes, stored as FP32 primitives for the FP32 faces
-template <bool F32>
-__global__ void k_ebl_prims(EbStageArgs A, DevParm P) {
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ptotal;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const int b = tag_of(A.pstart, A.pchunk, A.nbox, idx);
-        const EbStageBox& B = A.boxes[b];
-        const int loc = (int)(idx - A.pstart[b]);
-        const int gx = B.hi[0] - B.lo[0] + 5, gy = B.hi[1] - B.lo[1] + 5;
-        const int r = loc / gx;
-        const int i = B.lo[0] - 2 + (loc - r * gx), j = B.lo[1] - 2 + r % gy, k = B.lo[2] - 2 + r / gy;
-        if (F32) {
-            const float g = P.f_gamma;
-            const float u0 = d2f_bits(B.S(i, j, k, 0)), u1 = d2f_bits(B.S(i, j, k, 1)), u2 = d2f_bits(B.S(i, j, k, 2)),
-                        u3 = d2f_bits(B.S(i, j, k, 3)), u4 = d2f_bits(B.S(i, j, k, 4));
-            const float rho = fmaxf(u0, P.f_smallr);
-            const float rhoinv = __frcp_rn(rho);
-            const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
-            const float p = fmaxf((g - 1.0f) * (u4 - rho * (0.5f * (ux * ux + uy * uy + uz * uz))), P.f_smallp);
-            B.qf(i, j, k, QRHO) = rho;
-            B.qf(i, j, k, QU) = ux;
-            B.qf(i, j, k, QV) = uy;
-            B.qf(i, j, k, QW) = uz;
-            B.qf(i, j, k, QPRES) = p;
-            // no temperature: the inviscid FP32 faces and the divergence do not read it
-            B.qf(i, j, k, QC) = sqrtf(g * p * rhoinv);
-        } else {
-            double q[7];
-            c2prim_ideal_fast(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3), B.S(i, j, k, 4), q);
-#pragma unroll
-            for (int m = 0; m < 7; ++m) B.q(i, j, k, m) = q[m];
-        }
-    }
-}
-
-// F32: the mixed form - primitives narrowed on the integer pipes, MUSCL-minmod
-// states and the Van Leer flux in FP32, the flux widened back (inviscid only;
-// the EB viscous flux and everything after the face flux stay FP64)
-template <bool F32>
-__global__ void k_ebl_faces(EbStageArgs A, DevParm P) {
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ftotal;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const int t = tag_of(A.fstart, A.fchunk, 3 * A.nbox, idx);
-        const int b = t / 3, D = t % 3;
-        const EbStageBox& B = A.boxes[b];
-        const int loc = (int)(idx - A.fstart[t]);
-        const int fx = B.hi[0] - B.lo[0] + 1 + (D == 0), fy = B.hi[1] - B.lo[1] + 1 + (D == 1);
-        const int r = loc / fx;
-        const int i = B.lo[0] + (loc - r * fx), j = B.lo[1] + r % fy, k = B.lo[2] + r / fy;
-        const int di = D == 0, dj = D == 1, dk = D == 2;
-        const View<const double> q{B.q.p, B.q.js, B.q.ks, B.q.ns, B.q.b0, B.q.b1, B.q.b2};
-        const uint32_t f = B.flag(i, j, k);
-        double flx[5];
-        if (F32) {
-            // eb_recon with the connectivity tests and the addressing hoisted out of
-            // the component loop: one base pointer, the stride along D, the
-            // component stride
-            const View<float>& qf = B.qf;
-            const float* p0 = &qf(i, j, k, 0);
-            const long long sd = D == 0 ? 1 : (D == 1 ? qf.js : qf.ks), ns = qf.ns;
-            const bool cm1 = eb_conn(f, -di, -dj, -dk), cm2 = eb_conn(f, -2 * di, -2 * dj, -2 * dk),
-                       cp1 = eb_conn(f, di, dj, dk);
-            float ql[7], qr[7], ff[5];
-#pragma unroll
-            for (int m = 0; m < 7; ++m) {
-                if (m == QT) {  // the Van Leer flux does not read the temperature
-                    ql[m] = qr[m] = 0.0f;
-                    continue;
-                }
-                const float* pm = p0 + m * ns;
-                const float vm2 = pm[-2 * sd], vm1 = pm[-sd], v0 = pm[0], vp1 = pm[sd];
-                float l = vm1, r = v0;
-                if (cm1) {
-                    if (cm2) l = vm1 + 0.5f * minmod<float>(v0 - vm1, vm1 - vm2);
-                    if (cp1) r = v0 - 0.5f * minmod<float>(vp1 - v0, v0 - vm1);
-                }
-                ql[m] = l;
-                qr[m] = r;
-            }
-            vanleer<float>(P.f_smallp, P.f_gamma, ql, qr, D, ff);
-            float* fo = &B.fluxf[D](i, j, k, 0);
-            const long long fns = B.fluxf[D].ns;
-#pragma unroll
-            for (int m = 0; m < 5; ++m) {
-                fo[m * fns] = ff[m];
-                flx[m] = f2d_bits(ff[m]);
-            }
-        } else {
-            double ql[7], qr[7];
-#pragma unroll
-            for (int m = 0; m < 7; ++m)
-                eb_recon(f, D, q(i - 2 * di, j - 2 * dj, k - 2 * dk, m), q(i - di, j - dj, k - dk, m), q(i, j, k, m),
-                         q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
-            vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
-            if (A.visc) eb_visc_face(P, q, B.flag, D, i, j, k, A.dxinv, flx, 1, false, 0, 0, 0);
-#pragma unroll
-            for (int m = 0; m < 5; ++m) B.flux[D](i, j, k, m) = flx[m];
-        }
-        if (B.has_flux) {
-            const double w = B.flux_w * *A.dt_ptr * B.ap[D](i, j, k);
-            if (B.has_flux & FLUX_ACC_ALL) {
-#pragma unroll
-                for (int m = 0; m < 5; ++m) B.creg[D](i, j, k, m) += w * flx[m];
-            }
-            const int g = D == 0 ? i : (D == 1 ? j : k);
-            if ((B.has_flux & FLUX_ACC_PLANES) && (g == B.lo[D] || g == B.hi[D] + 1)) {
-                const View<double>& pl = B.fplane[D][g == B.lo[D] ? 0 : 1];
-#pragma unroll
-                for (int m = 0; m < 5; ++m) pl(i, j, k, m) += w * flx[m];
-            }
-        }
-    }
-}
-
-// cut-cell divergence of one cell (Source/EB/EBkernels.H:216-338, negated and
-// optionally rescaled as flux_redist, :341-377) + the Shu-Osher stage.  F32: the
-// face fluxes and primitives come from the FP32 scratch (widened; the divergence,
-// wall flux and stage stay FP64)
-template <bool F32>
-__device__ __forceinline__ double eb_fx(const EbStageBox& B, int D, int i, int j, int k, int m) {
-    return F32 ? f2d_bits(B.fluxf[D](i, j, k, m)) : B.flux[D](i, j, k, m);
-}
-template <bool F32>
-__device__ __forceinline__ double eb_q(const EbStageBox& B, int i, int j, int k, int m) {
-    return F32 ? f2d_bits(B.qf(i, j, k, m)) : B.q(i, j, k, m);
-}
-
-template <bool F32>
-__global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
-    const double dt = *A.dt_ptr;
-    double local_dt = __longlong_as_double(0x7FF0000000000000LL);
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < A.ctotal;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const int b = tag_of(A.cstart, A.cchunk, A.nbox, idx);
-        const EbStageBox& B = A.boxes[b];
-        const int loc = (int)(idx - A.cstart[b]);
-        const int nx = B.hi[0] - B.lo[0] + 1, ny = B.hi[1] - B.lo[1] + 1;
-        const int r = loc / nx;
-        const int i = B.lo[0] + (loc - r * nx), j = B.lo[1] + r % ny, k = B.lo[2] + r / ny;
-        double L[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        if (F32) {
-          if (!B.covered) {
-            // mixed form (inviscid): the divergence and the slip-wall pressure flux
-            // in FP32 from the FP32 face fluxes, widened once per component
-            const uint32_t f = B.flag(i, j, k);
-            float out[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-            const float vf = d2f_bits(B.vfrac(i, j, k));
-            // face-flux base pointers of the cell and the strides to its high faces
-            const float* fx0 = &B.fluxf[0](i, j, k, 0);
-            const float* fy0 = &B.fluxf[1](i, j, k, 0);
-            const float* fz0 = &B.fluxf[2](i, j, k, 0);
-            const long long nsx = B.fluxf[0].ns, nsy = B.fluxf[1].ns, nsz = B.fluxf[2].ns;
-            const long long sy = B.fluxf[1].js, sz = B.fluxf[2].ks;
-            if (eb_regular(f)) {
-#pragma unroll
-                for (int m = 0; m < 5; ++m)
-                    out[m] = A.dxinv_f[0] * (fx0[m * nsx + 1] - fx0[m * nsx]) +
-                             A.dxinv_f[1] * (fy0[m * nsy + sy] - fy0[m * nsy]) +
-                             A.dxinv_f[2] * (fz0[m * nsz + sz] - fz0[m * nsz]);
-            } else if (!eb_covered(f)) {
-                const float tmp = __fdividef(A.dxinv_f[0], vf);
-                const float axm = d2f_bits(B.ap[0](i, j, k)), axp = d2f_bits(B.ap[0](i + 1, j, k));
-                const float aym = d2f_bits(B.ap[1](i, j, k)), ayp = d2f_bits(B.ap[1](i, j + 1, k));
-                const float azm = d2f_bits(B.ap[2](i, j, k)), azp = d2f_bits(B.ap[2](i, j, k + 1));
-#pragma unroll
-                for (int m = 0; m < 5; ++m)
-                    out[m] = tmp * (axp * fx0[m * nsx + 1] - axm * fx0[m * nsx] + ayp * fy0[m * nsy + sy] -
-                                    aym * fy0[m * nsy] + azp * fz0[m * nsz + sz] - azm * fz0[m * nsz]);
-                const float pr = B.qf(i, j, k, QPRES);
-                out[1] += (axm - axp) * pr * tmp;
-                out[2] += (aym - ayp) * pr * tmp;
-                out[3] += (azm - azp) * pr * tmp;
-            }
-            const bool rescale = A.redist && vf < 0.5f && vf > 0.0f;
-#pragma unroll
-            for (int m = 0; m < 5; ++m) L[m] = f2d_bits(rescale ? -(vf * out[m]) : -out[m]);
-          }
-        } else if (!B.covered) {
-            const uint32_t f = B.flag(i, j, k);
-            const double vf = B.vfrac(i, j, k);
-            double out[5];
-            if (eb_covered(f)) {
-#pragma unroll
-                for (int m = 0; m < 5; ++m) out[m] = 0.0;
-            } else if (eb_regular(f)) {
-#pragma unroll
-                for (int m = 0; m < 5; ++m)
-                    out[m] = A.dxinv[0] * (eb_fx<F32>(B, 0, i + 1, j, k, m) - eb_fx<F32>(B, 0, i, j, k, m)) +
-                             A.dxinv[1] * (eb_fx<F32>(B, 1, i, j + 1, k, m) - eb_fx<F32>(B, 1, i, j, k, m)) +
-                             A.dxinv[2] * (eb_fx<F32>(B, 2, i, j, k + 1, m) - eb_fx<F32>(B, 2, i, j, k, m));
-            } else {
-                const double tmp = A.dxinv[0] / vf;
-                const double axm = B.ap[0](i, j, k), axp = B.ap[0](i + 1, j, k);
-                const double aym = B.ap[1](i, j, k), ayp = B.ap[1](i, j + 1, k);
-                const double azm = B.ap[2](i, j, k), azp = B.ap[2](i, j, k + 1);
-#pragma unroll
-                for (int m = 0; m < 5; ++m)
-                    out[m] = tmp * (axp * eb_fx<F32>(B, 0, i + 1, j, k, m) - axm * eb_fx<F32>(B, 0, i, j, k, m) +
-                                    ayp * eb_fx<F32>(B, 1, i, j + 1, k, m) - aym * eb_fx<F32>(B, 1, i, j, k, m) +
-                                    azp * eb_fx<F32>(B, 2, i, j, k + 1, m) - azm * eb_fx<F32>(B, 2, i, j, k, m));
-                double fw[5];
-                const double pr = eb_q<F32>(B, i, j, k, QPRES);
-                if (!A.visc) {
-                    // slip-wall pressure flux, EBkernels.H:305-311
-                    fw[0] = 0.0;
-                    fw[1] = (axm - axp) * pr;
-                    fw[2] = (aym - ayp) * pr;
-                    fw[3] = (azm - azp) * pr;
-                    fw[4] = 0.0;
-                } else {
-                    // eb_wallflux, EBkernels.H:173-214
-                    const double d = eb_q<F32>(B, i, j, k, QRHO), u = eb_q<F32>(B, i, j, k, QU),
-                                 v = eb_q<F32>(B, i, j, k, QV), w = eb_q<F32>(B, i, j, k, QW),
-                                 cs = eb_q<F32>(B, i, j, k, QC);
-                    const double apnorm = sqrt((axm - axp) * (axm - axp) + (aym - ayp) * (aym - ayp) +
-                                               (azm - azp) * (azm - azp));
-                    const double un = u * (axm - axp) + v * (aym - ayp) + w * (azm - azp);
-                    const double lambda0 = fabs(un) + cs * apnorm;
-                    const double gamma = P.gamma;
-                    const double E0 = pr / (gamma - 1) + 0.50 * d * (u * u + v * v + w * w);
-                    double fpw[5], fmw[5];
-                    fpw[0] = 0.5 * (d * un + lambda0 * d);
-                    fpw[1] = 0.5 * (d * u * un + (axm - axp) * pr + lambda0 * d * u);
-                    fpw[2] = 0.5 * (d * v * un + (aym - ayp) * pr + lambda0 * d * v);
-                    fpw[3] = 0.5 * (d * w * un + (azm - azp) * pr + lambda0 * d * w);
-                    fpw[4] = 0.5 * ((E0 + pr) * un + lambda0 * E0);
-                    fmw[0] = 0.5 * (d * (-un) - lambda0 * d);
-                    fmw[1] = fpw[1];
-                    fmw[2] = fpw[2];
-                    fmw[3] = fpw[3];
-                    fmw[4] = 0.5 * (-(E0 + pr) * un - lambda0 * E0);
-#pragma unroll
-                    for (int m = 0; m < 5; ++m) fw[m] = fpw[m] + fmw[m];
-                }
-#pragma unroll
-                for (int m = 0; m < 5; ++m) out[m] += fw[m] * tmp;
-            }
-            const bool rescale = A.redist && vf < 0.5 && vf > 0.0;
-#pragma unroll
-            for (int m = 0; m < 5; ++m) {
-                const double divc = out[m] * -1.0;
-                L[m] = rescale ? vf * divc : divc;
-            }
-        }
-        double un[5];
-#pragma unroll
-        for (int n = 0; n < 5; ++n) {
-            const double us = B.S(i, j, k, n);
-            const double u0 = B.U0(i, j, k, n);
-            un[n] = B.rk_a * u0 + B.rk_b * (us + dt * L[n]);
-            B.Uout(i, j, k, n) = un[n];
-        }
-        if (A.cfl_min) {
-            double v;
-            if (F32) {
-                // CFL bound of the new state in FP32 (as the mixed regular kernel)
-                const float g = P.f_gamma;
-                const float rho = d2f_bits(un[0]);
-                const float rhoinv = __frcp_rn(fmaxf(rho, P.f_smallr));
-                const float vx = d2f_bits(un[1]) * rhoinv, vy = d2f_bits(un[2]) * rhoinv, vz = d2f_bits(un[3]) * rhoinv;
-                const float p = fmaxf((g - 1.0f) * (d2f_bits(un[4]) - 0.5f * rho * (vx * vx + vy * vy + vz * vz)),
-                                      P.f_smallp);
-                const float cs = sqrtf(g * p * rhoinv);
-                const float dtx = __fdividef(A.dx_f[0], fabsf(vx) + cs);
-                const float dty = __fdividef(A.dx_f[1], fabsf(vy) + cs);
-                const float dtz = __fdividef(A.dx_f[2], fabsf(vz) + cs);
-                v = f2d_bits(fminf(dtx, fminf(dty, dtz)));
-            } else {
-                v = cfl_bound(P, un, A.dx);
-            }
-            local_dt = v < local_dt ? v : local_dt;
-        }
-    }
-    if (A.cfl_min) block_min_atomic(local_dt, A.cfl_min);
-}
 
 // ------------------------------------------------------------ fused tile kernel
 // The batched cut-cell stage as one kernel: one CTA per 8x8x4 tile of a cut or
@@ -505,8 +204,7 @@ __global__ void k_ebl_div_stage(EbStageArgs A, DevParm P) {
 // scratch round trip.  A face on a tile boundary is computed by both tiles and
 // added to the flux registers by the one that owns it (faces 0 .. T_D - 1 of the
 // tile, plus the box's high face), so that every face is accumulated once.  The
-// arithmetic per face and per cell is that of k_ebl_faces / k_ebl_div_stage;
-// the per-box form (OCFD_PER_BOX) keeps those three kernels.
+// per-box form (OCFD_PER_BOX) launches the same kernel box by box.
 constexpr int EBT_X = 8, EBT_Y = 8, EBT_Z = 4, EBT_N = EBT_X * EBT_Y * EBT_Z;
 constexpr int EBQ_X = EBT_X + 4, EBQ_Y = EBT_Y + 4, EBQ_Z = EBT_Z + 4, EBQ_N = EBQ_X * EBQ_Y * EBQ_Z;
 constexpr int EBF_N0 = (EBT_X + 1) * EBT_Y * EBT_Z, EBF_N1 = EBT_X * (EBT_Y + 1) * EBT_Z,
@@ -816,22 +514,16 @@ struct ocfd::EbLevel {
     std::vector<GeoTag> geo;    // host copies of the geometry tags
     double* d_geo = nullptr;
     uint32_t* d_flag = nullptr;
-    // cut and covered boxes (level box indices) and their scratch
+    // cut and covered boxes (level box indices)
     std::vector<int> ebox;
-    std::vector<long long> q_off, f_off[3];
-    double* d_scratch = nullptr;
     EbStageBox* d_stage[NUM_STAGE_SLOTS] = {nullptr, nullptr, nullptr, nullptr};
-    long long *d_pstart = nullptr, *d_fstart = nullptr, *d_cstart = nullptr;
-    long long ptotal = 0, ftotal = 0, ctotal = 0;
     bool cfl_slot[NUM_STAGE_SLOTS] = {false, false, true, false};  // fused CFL bound per stage slot
-    // per-box launches: work of each box and its local prefix tables
-    std::vector<long long> pcount, fcount, ccount;
-    long long* d_floc = nullptr;  // (0, F0, F0 + F1) per box
-    long long* d_zero = nullptr;
-    // fused tile kernel: first tile of each cut / covered box, tiles in total
+    // fused tile kernel: first tile of each cut / covered box (device) and the
+    // tiles of each box (host, per-box launches), tiles in total; d_zero: a 0
     int* d_tstart = nullptr;
+    int* d_zero = nullptr;
+    std::vector<int> tcount;
     int ntiles = 0;
-    int *d_pchunk = nullptr, *d_fchunk = nullptr, *d_cchunk = nullptr;
 };
 
 namespace ocfd {
@@ -842,19 +534,11 @@ static void eb_free_tables(ocfd_level* L) {
         dev_free(E->d_stage[s], L->pool);
         E->d_stage[s] = nullptr;
     }
-    dev_free(E->d_pstart, L->pool);
-    dev_free(E->d_fstart, L->pool);
-    dev_free(E->d_cstart, L->pool);
-    dev_free(E->d_floc, L->pool);
-    dev_free(E->d_zero, L->pool);
-    dev_free(E->d_pchunk, L->pool);
-    dev_free(E->d_fchunk, L->pool);
-    dev_free(E->d_cchunk, L->pool);
     dev_free(E->d_tstart, L->pool);
+    dev_free(E->d_zero, L->pool);
     E->d_tstart = nullptr;
+    E->d_zero = nullptr;
     E->ntiles = 0;
-    E->d_pstart = E->d_fstart = E->d_cstart = E->d_floc = E->d_zero = nullptr;
-    E->d_pchunk = E->d_fchunk = E->d_cchunk = nullptr;
 }
 
 void eb_free(ocfd_level* L) {
@@ -863,7 +547,6 @@ void eb_free(ocfd_level* L) {
     eb_free_tables(L);
     dev_free(E->d_geo, L->pool);
     dev_free(E->d_flag, L->pool);
-    dev_free(E->d_scratch, L->pool);
     delete E;
     L->eb = nullptr;
 }
@@ -1018,30 +701,12 @@ ocfd_status eb_setup(ocfd_level* L, const ocfd_eb_desc& eb) {
         else if (counts[2 * g] == 0) E->cls[b] = OCFD_BOX_REGULAR;
         else E->cls[b] = OCFD_BOX_CUT;
     }
-    // scratch of the cut boxes: primitives over grow(bx, 2), face fluxes
-    long long off = 0;
+    // the cut and covered boxes, in level order
     bool any_cut = false;
     for (int b = 0; b < nb; ++b) {
         if (E->cls[b] == OCFD_BOX_REGULAR) continue;
         E->ebox.push_back(b);
-        const ocfd_box& B = L->boxes[b];
-        const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
-        if (E->cls[b] == OCFD_BOX_CUT) {
-            any_cut = true;
-            E->q_off.push_back(off);
-            off += 7LL * (n[0] + 4) * (n[1] + 4) * (n[2] + 4);
-            for (int d = 0; d < 3; ++d) {
-                E->f_off[d].push_back(off);
-                off += 5LL * (n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
-            }
-        } else {
-            E->q_off.push_back(-1);
-            for (int d = 0; d < 3; ++d) E->f_off[d].push_back(-1);
-        }
-    }
-    if (off > 0) {
-        E->d_scratch = static_cast<double*>(dev_alloc(sizeof(double) * off, L->pool));
-        if (!E->d_scratch) return fail(OCFD_OUT_OF_MEMORY, "ocfd_level_set_eb: scratch");
+        if (E->cls[b] == OCFD_BOX_CUT) any_cut = true;
     }
     // the cut-cell stencils read z ghost cells from the state: fill them
     L->zvirt = L->zvirt_allowed && !any_cut;
@@ -1075,32 +740,17 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
         E->cfl_slot[k] = slot[k].cfl;
     }
     std::vector<EbStageBox> st[NUM_STAGE_SLOTS];
-    std::vector<long long> ps(ne), fs(3 * ne), cs(ne), floc(3 * ne);
     std::vector<int> ts(ne);
-    long long pt = 0, ft = 0, ct = 0;
     int tt = 0;
-    E->pcount.assign(ne, 0);
-    E->fcount.assign(ne, 0);
-    E->ccount.assign(ne, 0);
+    E->tcount.assign(ne, 0);
     for (int e = 0; e < ne; ++e) {
         const int b = E->ebox[e];
         const ocfd_box& B = L->boxes[b];
         const int n[3] = {B.hi[0] - B.lo[0] + 1, B.hi[1] - B.lo[1] + 1, B.hi[2] - B.lo[2] + 1};
         const bool cut = E->cls[b] == OCFD_BOX_CUT;
-        ps[e] = pt;
-        if (cut) pt += (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
-        E->pcount[e] = pt - ps[e];
-        for (int d = 0; d < 3; ++d) {
-            fs[3 * e + d] = ft;
-            floc[3 * e + d] = ft - fs[3 * e];
-            if (cut) ft += (long long)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
-        }
-        E->fcount[e] = ft - fs[3 * e];
-        cs[e] = ct;
-        ct += (long long)n[0] * n[1] * n[2];
-        E->ccount[e] = ct - cs[e];
         ts[e] = tt;
-        tt += ((n[0] + EBT_X - 1) / EBT_X) * ((n[1] + EBT_Y - 1) / EBT_Y) * ((n[2] + EBT_Z - 1) / EBT_Z);
+        E->tcount[e] = ((n[0] + EBT_X - 1) / EBT_X) * ((n[1] + EBT_Y - 1) / EBT_Y) * ((n[2] + EBT_Z - 1) / EBT_Z);
+        tt += E->tcount[e];
         EbStageBox base{};
         for (int d = 0; d < 3; ++d) {
             base.lo[d] = B.lo[d];
@@ -1115,18 +765,6 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
             base.ap[0] = View<const double>{E->d_geo + g.off_ax, g.gx + 1, 0, 0, b0, b1, 0};
             base.ap[1] = View<const double>{E->d_geo + g.off_ay, g.gx, 0, 0, b0, b1, 0};
             base.ap[2] = base.vfrac;
-            const long long gq = (long long)(n[0] + 4) * (n[1] + 4) * (n[2] + 4);
-            base.q = View<double>{E->d_scratch + E->q_off[e], n[0] + 4, (long long)(n[0] + 4) * (n[1] + 4), gq,
-                                  B.lo[0] - 2, B.lo[1] - 2, B.lo[2] - 2};
-            base.qf = View<float>{reinterpret_cast<float*>(base.q.p), base.q.js, base.q.ks, base.q.ns,
-                                  base.q.b0, base.q.b1, base.q.b2};
-            for (int d = 0; d < 3; ++d) {
-                const int sx = n[0] + (d == 0), sy = n[1] + (d == 1), sz = n[2] + (d == 2);
-                base.flux[d] = View<double>{E->d_scratch + E->f_off[d][e], sx, (long long)sx * sy,
-                                            (long long)sx * sy * sz, B.lo[0], B.lo[1], B.lo[2]};
-                base.fluxf[d] = View<float>{reinterpret_cast<float*>(base.flux[d].p), base.flux[d].js,
-                                            base.flux[d].ks, base.flux[d].ns, B.lo[0], B.lo[1], B.lo[2]};
-            }
         }
         if (!roles.flux_bits.empty() && roles.flux_bits[b] && cut) {
             base.has_flux = roles.flux_bits[b] & (FLUX_ACC_ALL | FLUX_ACC_PLANES);
@@ -1150,50 +788,20 @@ ocfd_status eb_build_stage_tables(ocfd_level* L, const StageRoles& roles) {
             st[k].push_back(x);
         }
     }
-    E->ptotal = pt;
-    E->ftotal = ft;
-    E->ctotal = ct;
     E->ntiles = tt;
     ocfd_status s = OCFD_OK;
-    s = upload(&E->d_tstart, ts, L->pool);
     for (int k = 0; k < NUM_STAGE_SLOTS && s == OCFD_OK; ++k) s = upload(&E->d_stage[k], st[k], L->pool);
-    if (s == OCFD_OK) s = upload(&E->d_pstart, ps, L->pool);
-    if (s == OCFD_OK) s = upload(&E->d_fstart, fs, L->pool);
-    if (s == OCFD_OK) s = upload(&E->d_cstart, cs, L->pool);
-    if (s == OCFD_OK) s = upload(&E->d_floc, floc, L->pool);
-    if (s == OCFD_OK) s = upload(&E->d_zero, std::vector<long long>(1, 0), L->pool);
-    // chunk tables: the tag holding item (c << EB_CHUNK_LOG2)
-    auto chunks = [](const std::vector<long long>& start, long long total) {
-        std::vector<int> out((size_t)((total >> EB_CHUNK_LOG2) + 1), 0);
-        int t = 0;
-        for (size_t c = 0; c < out.size(); ++c) {
-            const long long idx = (long long)c << EB_CHUNK_LOG2;
-            while (t + 1 < (int)start.size() && start[t + 1] <= idx) ++t;
-            out[c] = t;
-        }
-        return out;
-    };
-    if (s == OCFD_OK) s = upload(&E->d_pchunk, chunks(ps, pt), L->pool);
-    if (s == OCFD_OK) s = upload(&E->d_fchunk, chunks(fs, ft), L->pool);
-    if (s == OCFD_OK) s = upload(&E->d_cchunk, chunks(cs, ct), L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_tstart, ts, L->pool);
+    if (s == OCFD_OK) s = upload(&E->d_zero, std::vector<int>(1, 0), L->pool);
     return s;
 }
 
 ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t st) {
     EbLevel* E = L->eb;
-    if (!E || E->ebox.empty()) return OCFD_OK;
+    if (!E || E->ebox.empty() || E->ntiles == 0) return OCFD_OK;
     EbStageArgs A{};
     A.boxes = E->d_stage[s];
     A.nbox = (int)E->ebox.size();
-    A.pstart = E->d_pstart;
-    A.ptotal = E->ptotal;
-    A.fstart = E->d_fstart;
-    A.ftotal = E->ftotal;
-    A.cstart = E->d_cstart;
-    A.ctotal = E->ctotal;
-    A.pchunk = E->d_pchunk;
-    A.fchunk = E->d_fchunk;
-    A.cchunk = E->d_cchunk;
     for (int d = 0; d < 3; ++d) {
         A.dxinv[d] = 1.0 / L->desc.dx[d];
         A.dx[d] = L->desc.dx[d];
@@ -1205,52 +813,29 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
     A.visc = (flags & OCFD_VISC) ? 1 : 0;
     A.redist = E->desc.redistribute ? 1 : 0;
     const bool f32 = (flags & OCFD_FLUX_FP32) && !A.visc;
-    const int sms = L->ctx->num_sms;
+    auto go = [&](const EbStageArgs& X, const int* tstart, int ntiles) {
+        if (f32) k_ebl_tile<true><<<ntiles, EBT_N, ebt_smem_bytes<true>(), st>>>(X, tstart, L->ctx->parm);
+        else k_ebl_tile<false><<<ntiles, EBT_N, ebt_smem_bytes<false>(), st>>>(X, tstart, L->ctx->parm);
+    };
     if (flags & OCFD_PER_BOX) {
-        // one box at a time (the reference's per-box kernel chain)
-        const EbStageBox* base = E->d_stage[s];
+        // one launch per box (the reference's per-box execution model), the same kernel
         for (int e = 0; e < (int)E->ebox.size(); ++e) {
             EbStageArgs B = A;
-            B.boxes = base + e;
+            B.boxes = E->d_stage[s] + e;
             B.nbox = 1;
-            B.pstart = E->d_zero;
-            B.ptotal = E->pcount[e];
-            B.fstart = E->d_floc + 3 * e;
-            B.ftotal = E->fcount[e];
-            B.cstart = E->d_zero;
-            B.ctotal = E->ccount[e];
-            B.pchunk = B.fchunk = B.cchunk = nullptr;
-            if (B.ptotal > 0) {
-                if (f32) k_ebl_prims<true><<<grid_for(B.ptotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
-                else k_ebl_prims<false><<<grid_for(B.ptotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
-            }
-            if (B.ftotal > 0) {
-                if (f32) k_ebl_faces<true><<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
-                else k_ebl_faces<false><<<grid_for(B.ftotal, 128, sms), 128, 0, st>>>(B, L->ctx->parm);
-            }
-            if (f32) k_ebl_div_stage<true><<<grid_for(B.ctotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
-            else k_ebl_div_stage<false><<<grid_for(B.ctotal, 256, sms), 256, 0, st>>>(B, L->ctx->parm);
+            go(B, E->d_zero, E->tcount[e]);
         }
         return check_launch("level cut-cell stage (per box)");
     }
-    // batched: every cut and covered box in one launch of the fused tile kernel
-    if (E->ntiles > 0) {
-        if (f32)
-            k_ebl_tile<true><<<E->ntiles, EBT_N, ebt_smem_bytes<true>(), st>>>(A, E->d_tstart, L->ctx->parm);
-        else
-            k_ebl_tile<false><<<E->ntiles, EBT_N, ebt_smem_bytes<false>(), st>>>(A, E->d_tstart, L->ctx->parm);
-    }
+    // batched: every cut and covered box of the level in one launch
+    go(A, E->d_tstart, E->ntiles);
     return check_launch("level cut-cell stage");
 }
 
 int eb_launches_per_stage(const ocfd_level* L, unsigned flags) {
     const EbLevel* E = L->eb;
     if (!E || E->ebox.empty()) return 0;
-    if (flags & OCFD_PER_BOX) {
-        int n = 0;
-        for (int b : E->ebox) n += E->cls[b] == OCFD_BOX_CUT ? 3 : 1;
-        return n;
-    }
+    if (flags & OCFD_PER_BOX) return (int)E->ebox.size();
     return E->ntiles > 0 ? 1 : 0;
 }
 
