@@ -490,6 +490,30 @@ typedef struct ocfd_amr_desc {
 } ocfd_amr_desc;
 
 ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_amr** amr);
+
+/* A reacting hierarchy (the CHEM build's EBR::advance over subcycled levels,
+ * Source/Advance.cpp:158-174, Source/CHEM/FlowAdvance.cpp:9-90, Source/EBR.cpp:
+ * 313-357): 5 + 9 components per level (conserved state, then the partial
+ * densities in the mechanism's order), on every level and substep
+ *   chemistry over dt_l / 2 in iter_l substeps (iter_l = chem_substeps / 2^l on
+ *   levels 0..2, 1 finer: the reference's 4 / 2^level), the multispecies flow
+ *   step (RK2 by default, as the reference's flow_advance_multi; flux registers
+ *   of the flow and of the species, flux_reg / flux_reg_spec), chemistry over
+ *   dt_l / 2 again;
+ * after the finer level's substeps: reflux of flow and species, species
+ * renormalisation (clip, rescale to rho), average-down.  The coarse step is the
+ * fixed `dt` (the CHEM build's fixed time step, Source/Advance.cpp:54-57), dt_l
+ * = dt / 2^l.  Regridding tags on the density gradient as for the ideal gas.
+ * No embedded body. */
+typedef struct ocfd_amr_react_desc {
+    double dt;                   /* coarse step (s) */
+    int32_t chem_substeps;       /* substeps per half step on level 0 (the reference: 4) */
+    uint32_t flags;              /* OCFD_VISC: mixture-averaged viscous and species transport;
+                                    OCFD_FLUX_FP32: the mixed form of the face fluxes */
+} ocfd_amr_react_desc;
+
+ocfd_status ocfd_amr_create_reacting(ocfd_context* ctx, const ocfd_amr_desc* desc,
+                                     const ocfd_amr_react_desc* react, ocfd_amr** amr);
 /* Cut every level, present and future, with an embedded body (see
  * ocfd_level_set_eb): per box the regular, cut-cell or covered scheme of
  * EBR::compute_dSdt; cut-cell fluxes enter the flux registers weighted by their

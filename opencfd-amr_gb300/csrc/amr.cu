@@ -52,6 +52,7 @@
 
 #include "level.h"
 #include "eb_level.h"
+#include "chem_internal.h"
 
 namespace ocfd {
 
@@ -253,6 +254,7 @@ struct TagGeom {
 struct AmrStates {
     StepState* s[OCFD_AMR_MAX_LEVELS];
     int n;
+    double fixed_dt;  // > 0: the coarse step is this dt (reacting hierarchy, Source/Advance.cpp:54-57)
 };
 
 __device__ __forceinline__ double mc_slope(double m, double c, double p) {
@@ -378,13 +380,13 @@ __global__ void k_avg_down(const AvgTag* __restrict__ tags, const long long* __r
 
 __global__ void k_reflux(const RefluxCell* __restrict__ cells, int ncell, const RefluxFace* __restrict__ faces,
                          const double* __restrict__ creg, const double* __restrict__ freg, double* U,
-                         double dxi0, double dxi1, double dxi2) {
+                         double dxi0, double dxi1, double dxi2, int ncomp) {
     const double dxinv[3] = {dxi0, dxi1, dxi2};
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
         const RefluxCell& C = cells[c];
         const double vf = C.vf ? *C.vf : 1.0;
         if (!(vf > 0.0)) continue;
-        for (int n = 0; n < 5; ++n) {
+        for (int n = 0; n < ncomp; ++n) {
             double acc = 0.0;
             for (int q = C.first; q < C.first + C.count; ++q) {
                 const RefluxFace& F = faces[q];
@@ -455,9 +457,13 @@ __global__ void k_amr_begin(AmrStates S) {
         est = e < est ? e : est;
     }
     double dt = s0->cfl * est;
-    if (s0->dt_prev > 0 && dt > 1.1 * s0->dt_prev) dt = 1.1 * s0->dt_prev;
-    if (s0->time + dt > s0->stop_time - 0.001 * dt) dt = s0->stop_time - s0->time;
-    if (dt < 0) dt = 0;
+    if (S.fixed_dt > 0) {
+        dt = S.fixed_dt;
+    } else {
+        if (s0->dt_prev > 0 && dt > 1.1 * s0->dt_prev) dt = 1.1 * s0->dt_prev;
+        if (s0->time + dt > s0->stop_time - 0.001 * dt) dt = s0->stop_time - s0->time;
+        if (dt < 0) dt = 0;
+    }
     for (int l = 0; l < S.n; ++l) {
         S.s[l]->dt = dt / (double)(1 << l);
         S.s[l]->time = s0->time;
@@ -543,6 +549,71 @@ struct DevTags {
     }
 };
 
+// ------------------------------------------------------- reacting hierarchy
+// One stage's combination over every component of a level's cells,
+// out = a U^n + b (S + dt L(S)) (the Heun / Shu-Osher forms of the flow step,
+// Source/CHEM/FlowAdvance.cpp:64-88), dt the level's step.
+__global__ void k_amr_combine(const FabGeom* __restrict__ fabs, const long long* __restrict__ start, int nbox,
+                              long long total, double* out, const double* __restrict__ U0,
+                              const double* __restrict__ S, const double* __restrict__ R, double a, double b,
+                              const StepState* st, int ncomp) {
+    const double dt = st->dt;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int bx = find_tag<FabGeom>(start, nbox, idx);
+        const FabGeom& f = fabs[bx];
+        int i, j, k;
+        region_cell(f.lo, f.hi, idx - start[bx], i, j, k);
+        const long long c = fab_index(f, i, j, k);
+        for (int n = 0; n < ncomp; ++n) {
+            const long long q = c + n * f.ns;
+            out[q] = a * U0[q] + b * (S[q] + dt * R[q]);
+        }
+    }
+}
+
+// The flow (5) and species (9) face fluxes of one box, as its multispecies
+// kernel chain left them, into the flux registers of its level: weight w dt on
+// every face of a coarse box next to a finer level (flux_reg CrseAdd), on the
+// box's own boundary faces of a fine box (FineAdd) - the flux_reg and
+// flux_reg_spec additions of compute_dSdt_multi (Source/CHEM/FlowAdvance.cpp:
+// 92-496)
+struct ChemRegBox {
+    View<double> flux[3], fluxs[3];
+    View<double> creg[3];
+    View<double> fplane[3][2];
+    int bits;
+    int lo[3], hi[3];
+    double w;
+};
+
+__global__ void k_amr_chem_reg(ChemRegBox R, const StepState* st) {
+    const double wdt = R.w * st->dt;
+    const int n[3] = {R.hi[0] - R.lo[0] + 1, R.hi[1] - R.lo[1] + 1, R.hi[2] - R.lo[2] + 1};
+    const long long nf[3] = {(long long)(n[0] + 1) * n[1] * n[2], (long long)n[0] * (n[1] + 1) * n[2],
+                             (long long)n[0] * n[1] * (n[2] + 1)};
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nf[0] + nf[1] + nf[2];
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int d = idx < nf[0] ? 0 : (idx < nf[0] + nf[1] ? 1 : 2);
+        const long long loc = idx - (d == 0 ? 0 : (d == 1 ? nf[0] : nf[0] + nf[1]));
+        const int fx = n[0] + (d == 0), fy = n[1] + (d == 1);
+        const int i = R.lo[0] + (int)(loc % fx), j = R.lo[1] + (int)((loc / fx) % fy),
+                  k = R.lo[2] + (int)(loc / ((long long)fx * fy));
+        const int g = d == 0 ? i : (d == 1 ? j : k);
+        const bool plane = (R.bits & FLUX_ACC_PLANES) && (g == R.lo[d] || g == R.hi[d] + 1);
+        if (!(R.bits & FLUX_ACC_ALL) && !plane) continue;
+        double F[14];
+        for (int m = 0; m < 5; ++m) F[m] = R.flux[d](i, j, k, m);
+        for (int m = 0; m < NSP; ++m) F[5 + m] = R.fluxs[d](i, j, k, m);
+        if (R.bits & FLUX_ACC_ALL)
+            for (int m = 0; m < 14; ++m) R.creg[d](i, j, k, m) += wdt * F[m];
+        if (plane) {
+            const View<double>& pl = R.fplane[d][g == R.lo[d] ? 0 : 1];
+            for (int m = 0; m < 14; ++m) pl(i, j, k, m) += wdt * F[m];
+        }
+    }
+}
+
 struct AmrLev {
     ocfd_level* L = nullptr;
     std::vector<IBox> boxes;
@@ -561,6 +632,12 @@ struct AmrLev {
     long long leaf = 0;
     unsigned char* d_blk = nullptr;  // tag blocks of lev + 1
     long long nblk_cap = 0;
+    // reacting hierarchy: the multispecies right-hand side (FAB layout of the
+    // level's state), the per-box scratch of its kernel chain, and the argument
+    // blocks of every box per state buffer
+    double* rhs = nullptr;
+    double* cscr = nullptr;
+    std::vector<ChemBoxArgs> cargs[4];
     void release_tables(DevPool* pool) {
         cf.release(pool);
         avg.release(pool);
@@ -568,10 +645,14 @@ struct AmrLev {
         dev_free(d_rf, pool);
         dev_free(freg, pool);
         dev_free(creg, pool);
+        dev_free(rhs, pool);
+        dev_free(cscr, pool);
         d_rc = nullptr;
         d_rf = nullptr;
         nrc = 0;
         freg = creg = nullptr;
+        rhs = cscr = nullptr;
+        for (auto& c : cargs) c.clear();
         freg_elems = creg_elems = 0;
     }
 };
@@ -599,6 +680,11 @@ struct ocfd_amr {
     int tuned_tile[OCFD_AMR_MAX_LEVELS] = {-1, -1, -1, -1, -1, -1};
     int tuned_sched[OCFD_AMR_MAX_LEVELS] = {0, 0, 0, 0, 0, 0};
     long long kernel_total = 0;  // kernels launched by this hierarchy so far
+    // reacting hierarchy (ocfd_amr_create_reacting): 5 + 9 components, the
+    // multispecies path of every level, chemistry substeps, species reflux
+    int ncomp = 5;
+    bool react = false;
+    ocfd_amr_react_desc rdesc{};
 };
 
 namespace ocfd {
@@ -635,6 +721,7 @@ static long long fab_index_h(const FabGeom& f, int i, int j, int k) {
 static AmrStates states(const ocfd_amr* H) {
     AmrStates S{};
     S.n = H->nlev;
+    S.fixed_dt = H->react ? H->rdesc.dt : 0.0;
     for (int l = 0; l < H->nlev; ++l) S.s[l] = H->lev[l].L->d_step;
     return S;
 }
@@ -663,7 +750,7 @@ static ocfd_status make_level(ocfd_amr* H, int l, const std::vector<IBox>& boxes
     d.bc_case = H->desc.bc_case;
     std::memcpy(d.case_params, H->desc.case_params, sizeof(d.case_params));
     d.tile = H->tuned_tile[l];
-    ocfd_status s = level_alloc(H->ctx, &d, nbuf, out, &H->pool);
+    ocfd_status s = level_alloc(H->ctx, &d, nbuf, out, &H->pool, H->ncomp);
     if (s == OCFD_OK) (*out)->sched = H->tuned_sched[l];
     if (s == OCFD_OK) (*out)->rk_order = H->rk_order;
     if (s == OCFD_OK && H->has_eb) s = eb_setup(*out, H->eb);
@@ -829,7 +916,7 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
                 pl.lo[d] = pl.hi[d] = (sd == 0) ? F.boxes[fb].lo[d] : F.boxes[fb].hi[d] + 1;
                 plane_off[fb * 6 + 2 * d + sd] = fe;
                 plane_box[fb * 6 + 2 * d + sd] = pl;
-                fe += ib_cells(pl) * 5;
+                fe += ib_cells(pl) * H->ncomp;
             }
     // ---- reflux faces grouped by uncovered coarse cell
     struct Face {
@@ -894,7 +981,7 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
         for (int d = 0; d < 3; ++d) {
             IBox fa = B;
             fa.hi[d] += 1;
-            ce += ib_cells(fa) * 5;
+            ce += ib_cells(fa) * H->ncomp;
         }
     }
     auto creg_face = [&](int cb, int d, const int* fc, long long* cns) {
@@ -903,7 +990,7 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
         for (int e = 0; e < d; ++e) {
             IBox fa = B;
             fa.hi[e] += 1;
-            off += ib_cells(fa) * 5;
+            off += ib_cells(fa) * H->ncomp;
         }
         IBox fa = B;
         fa.hi[d] += 1;
@@ -989,13 +1076,60 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
             fa.hi[d] += 1;
             const long long ex = fa.hi[0] - fa.lo[0] + 1, ey = fa.hi[1] - fa.lo[1] + 1;
             rc.creg[cb * 3 + d] = View<double>{C.creg + off, ex, ex * ey, ib_cells(fa), fa.lo[0], fa.lo[1], fa.lo[2]};
-            off += ib_cells(fa) * 5;
+            off += ib_cells(fa) * H->ncomp;
         }
     }
     return OCFD_OK;
 }
 
 static bool fused_cfl(const ocfd_amr* H, int l) { return l == H->nlev - 1 && !H->has_eb; }
+
+// Array4 view of components comp0 .. comp0 + ncomp - 1 of box b's FAB in `base`
+static ocfd_array4 fab_view_c(const ocfd_level* L, double* base, int b, int comp0, int ncomp) {
+    const FabGeom& f = L->fabs[b];
+    ocfd_array4 a{};
+    a.p = base + f.off + comp0 * f.ns;
+    a.jstride = f.g[0];
+    a.kstride = (long long)f.g[0] * f.g[1];
+    a.nstride = f.ns;
+    for (int d = 0; d < 3; ++d) {
+        a.begin[d] = f.lo[d] - NGR;
+        a.end[d] = f.hi[d] + NGR + 1;
+    }
+    a.ncomp = ncomp;
+    return a;
+}
+
+// Reacting hierarchy: the right-hand-side buffer of level l, one scratch for its
+// boxes' multispecies kernel chains (the boxes run one after the other on the
+// stream, so the largest box sizes it), and every box's argument block per
+// state buffer
+static ocfd_status build_chem_level(ocfd_amr* H, int l) {
+    AmrLev& A = H->lev[l];
+    ocfd_level* L = A.L;
+    dev_free(A.rhs, &H->pool);
+    dev_free(A.cscr, &H->pool);
+    A.rhs = static_cast<double*>(dev_alloc(sizeof(double) * L->elems, &H->pool));
+    size_t need = 1;
+    for (const ocfd_box& b : L->boxes) need = std::max(need, chem_rhs_scratch_doubles(b));
+    A.cscr = static_cast<double*>(dev_alloc(sizeof(double) * need, &H->pool));
+    if (!A.rhs || !A.cscr) return fail(OCFD_OUT_OF_MEMORY, "reacting hierarchy: right-hand-side buffers");
+    const double dxinv[3] = {1.0 / L->desc.dx[0], 1.0 / L->desc.dx[1], 1.0 / L->desc.dx[2]};
+    const bool visc = (H->rdesc.flags & OCFD_VISC) != 0;
+    for (int i = 0; i < 4; ++i) {
+        A.cargs[i].clear();
+        if (i >= L->nbuf) continue;
+        for (int b = 0; b < (int)L->boxes.size(); ++b) {
+            ocfd_array4 S = fab_view_c(L, L->buf[i], b, 0, 5), sp = fab_view_c(L, L->buf[i], b, 5, NSP);
+            ocfd_array4 d = fab_view_c(L, A.rhs, b, 0, 5), ds = fab_view_c(L, A.rhs, b, 5, NSP);
+            ChemBoxArgs X{};
+            chem_rhs_args(X, view_of<const double>(&S), view_of<const double>(&sp), view_of<double>(&d),
+                          view_of<double>(&ds), L->boxes[b], dxinv, visc, A.cscr);
+            A.cargs[i].push_back(X);
+        }
+    }
+    return OCFD_OK;
+}
 
 static ocfd_status rebuild_tables(ocfd_amr* H) {
     // blocks of the old tables go back to the pool: nothing may still read them
@@ -1030,6 +1164,7 @@ static ocfd_status rebuild_tables(ocfd_amr* H) {
             r.fplane.resize((size_t)nb * 6);
         }
         ocfd_status s = build_stage_tables(H->lev[l].L, r);
+        if (s == OCFD_OK && H->react) s = build_chem_level(H, l);
         if (s != OCFD_OK) return s;
     }
     pt.mark("    stage tables", 0);
@@ -1129,7 +1264,138 @@ static ocfd_status launch_avg(ocfd_amr* H, int f, const double* fsrc, double* cd
     return check_launch("AMR average-down");
 }
 
+// chemistry of level l over half its step, in place on U: iter_l substeps of the
+// implicit cell update (Source/Advance.cpp:158-173); `renorm`: the last substep
+// also renormalises the species (the finest level, whose post_timestep has no
+// reflux)
+static ocfd_status chem_level(ocfd_amr* H, int l, double* U, bool renorm, cudaStream_t st) {
+    ocfd_level* L = H->lev[l].L;
+    const int iter = l <= 2 ? std::max(1, H->rdesc.chem_substeps >> l) : 1;
+    const double dt2 = 0.5 * (H->rdesc.dt / (double)(1 << l)) / iter;
+    for (int s = 0; s < iter; ++s)
+        for (int b = 0; b < (int)L->boxes.size(); ++b) {
+            ocfd_array4 S = fab_view_c(L, U, b, 0, 5), sp = fab_view_c(L, U, b, 5, NSP);
+            CellBox cb{};
+            for (int d = 0; d < 3; ++d) {
+                cb.lo[d] = L->boxes[b].lo[d];
+                cb.n[d] = L->boxes[b].hi[d] - L->boxes[b].lo[d] + 1;
+            }
+            ocfd_status r = launch_chem_advance(view_of<double>(&S), view_of<double>(&sp), cb, dt2, H->ctx->parm, st,
+                                                renorm && s == iter - 1);
+            if (r != OCFD_OK) return r;
+            ++launches_counter;
+        }
+    return OCFD_OK;
+}
+
+// species renormalisation of level l's state U (EBR::post_timestep, Source/EBR.cpp:333-357)
+static ocfd_status renorm_level(ocfd_amr* H, int l, double* U, cudaStream_t st) {
+    ocfd_level* L = H->lev[l].L;
+    for (int b = 0; b < (int)L->boxes.size(); ++b) {
+        ocfd_array4 S = fab_view_c(L, U, b, 0, 5), sp = fab_view_c(L, U, b, 5, NSP);
+        CellBox cb{};
+        for (int d = 0; d < 3; ++d) {
+            cb.lo[d] = L->boxes[b].lo[d];
+            cb.n[d] = L->boxes[b].hi[d] - L->boxes[b].lo[d] + 1;
+        }
+        ocfd_status r = launch_spec_renorm(view_of<const double>(&S), view_of<double>(&sp), cb, H->ctx->num_sms, st);
+        if (r != OCFD_OK) return r;
+        ++launches_counter;
+    }
+    return OCFD_OK;
+}
+
+// One substep of a reacting level (EBR::advance with CHEM, then post_timestep):
+// chemistry over dt_l / 2, the multispecies flow step with its flux registers,
+// chemistry over dt_l / 2; with a finer level: its two substeps, reflux of flow
+// and species, renormalisation, average-down.
+static ocfd_status advance_level_react(ocfd_amr* H, int l, int it, unsigned flags, cudaStream_t st) {
+    AmrLev& A = H->lev[l];
+    ocfd_level* L = A.L;
+    const bool has_child = l < H->nlev - 1;
+    const double theta = 0.5 * (it - 1), r = 0.5;
+    const RkScheme& R = rk_scheme(H->rk_order);
+    const StageRoles roles = L->roles ? *L->roles : StageRoles{};
+    const int sms = H->ctx->num_sms;
+    ocfd_status s = chem_level(H, l, L->buf[0], false, st);
+    if (s != OCFD_OK) return s;
+    if (has_child) {
+        cudaMemsetAsync(A.creg, 0, sizeof(double) * std::max<long long>(1, A.creg_elems), st);
+        cudaMemsetAsync(H->lev[l + 1].freg, 0, sizeof(double) * std::max<long long>(1, H->lev[l + 1].freg_elems), st);
+    }
+    for (int k = 0; k < R.nst && s == OCFD_OK; ++k) {
+        double a[4];
+        cf_coefs(R.order, k, theta, r, a);
+        s = fill_level(H, l, L->buf[R.src[k]], a, R.tfrac[k], st);
+        for (int b = 0; b < (int)L->boxes.size() && s == OCFD_OK; ++b) {
+            ChemBoxArgs X = A.cargs[R.src[k]][b];
+            X.f32 = (flags & OCFD_FLUX_FP32) ? 1 : 0;
+            s = launch_chem_rhs(X, H->ctx->parm, sms, st);
+            launches_counter += X.visc ? 6 : 5;
+            const int bits = roles.flux_bits.empty() ? 0 : roles.flux_bits[b];
+            if (s == OCFD_OK && bits) {
+                ChemRegBox G{};
+                for (int d = 0; d < 3; ++d) {
+                    G.flux[d] = X.flux[d];
+                    G.fluxs[d] = X.fluxs[d];
+                    if (bits & FLUX_ACC_ALL) G.creg[d] = roles.creg[3 * b + d];
+                    if (bits & FLUX_ACC_PLANES)
+                        for (int sd = 0; sd < 2; ++sd) G.fplane[d][sd] = roles.fplane[6 * b + 2 * d + sd];
+                    G.lo[d] = L->boxes[b].lo[d];
+                    G.hi[d] = L->boxes[b].hi[d];
+                }
+                G.bits = bits;
+                G.w = R.w[k];
+                const ocfd_box& B = L->boxes[b];
+                const long long nfc = 3LL * (B.hi[0] - B.lo[0] + 2) * (B.hi[1] - B.lo[1] + 2) * (B.hi[2] - B.lo[2] + 2);
+                k_amr_chem_reg<<<grid_for(nfc, 256, sms), 256, 0, st>>>(G, L->d_step);
+                ++launches_counter;
+                s = check_launch("reacting hierarchy: flux registers");
+            }
+        }
+        if (s != OCFD_OK) break;
+        const int out = R.out[k] == RK_OUT ? roles.out3 : R.out[k];
+        k_amr_combine<<<grid_for(L->ncells, 256, sms), 256, 0, st>>>(L->d_fabs, L->d_cell_start, (int)L->boxes.size(),
+                                                                   L->ncells, L->buf[out], L->buf[0], L->buf[R.src[k]],
+                                                                   A.rhs, R.a[k], R.b[k], L->d_step, L->ncomp);
+        ++launches_counter;
+        s = check_launch("reacting hierarchy: stage");
+    }
+    if (s != OCFD_OK) return s;
+    const int fin = has_child ? 3 : 0;
+    if (R.copy_out && cudaMemcpyAsync(L->buf[fin], L->buf[1], sizeof(double) * L->elems, cudaMemcpyDeviceToDevice,
+                                      st) != cudaSuccess)
+        return check_launch("reacting hierarchy: stage output copy");
+    s = chem_level(H, l, L->buf[fin], !has_child, st);
+    if (s != OCFD_OK) return s;
+    if (has_child) {
+        double a[4];
+        cf_coefs(R.order, 3, theta, r, a);
+        s = fill_level(H, l, L->buf[3], a, 1.0, st);
+        for (int i = 1; i <= 2 && s == OCFD_OK; ++i) s = advance_level_react(H, l + 1, i, flags, st);
+        if (s != OCFD_OK) return s;
+        AmrLev& F = H->lev[l + 1];
+        if (F.nrc > 0) {
+            k_reflux<<<(F.nrc + 127) / 128, 128, 0, st>>>(F.d_rc, F.nrc, F.d_rf, A.creg, F.freg, L->buf[3],
+                                                         1.0 / A.dx[0], 1.0 / A.dx[1], 1.0 / A.dx[2], L->ncomp);
+            ++launches_counter;
+        }
+        s = renorm_level(H, l, L->buf[3], st);
+        if (s == OCFD_OK) s = launch_avg(H, l + 1, F.L->buf[0], L->buf[3], st);
+        if (s != OCFD_OK) return s;
+        if (cudaMemcpyAsync(L->buf[0], L->buf[3], sizeof(double) * L->elems, cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess)
+            return check_launch("reacting hierarchy: D -> A");
+    }
+    if (l > 0) {
+        k_sub_end<<<1, 1, 0, st>>>(L->d_step);
+        ++launches_counter;
+    }
+    return check_launch("reacting hierarchy: level advance");
+}
+
 static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cudaStream_t st) {
+    if (H->react) return advance_level_react(H, l, it, flags, st);
     AmrLev& A = H->lev[l];
     ocfd_level* L = A.L;
     const bool has_child = l < H->nlev - 1;
@@ -1164,7 +1430,7 @@ static ocfd_status advance_level(ocfd_amr* H, int l, int it, unsigned flags, cud
         AmrLev& F = H->lev[l + 1];
         if (F.nrc > 0) {
             k_reflux<<<(F.nrc + 127) / 128, 128, 0, st>>>(F.d_rc, F.nrc, F.d_rf, A.creg, F.freg, L->buf[3],
-                                                         1.0 / A.dx[0], 1.0 / A.dx[1], 1.0 / A.dx[2]);
+                                                         1.0 / A.dx[0], 1.0 / A.dx[1], 1.0 / A.dx[2], L->ncomp);
             ++launches_counter;
         }
         s = launch_avg(H, l + 1, F.L->buf[0], L->buf[3], st);
@@ -1198,7 +1464,7 @@ static ocfd_status record_amr_step(ocfd_amr* H, unsigned flags, cudaStream_t st)
     launches_counter = 0;
     k_amr_begin<<<1, 1, 0, st>>>(states(H));
     ocfd_status s = advance_level(H, 0, 1, flags, st);
-    if (s == OCFD_OK) s = launch_estdt_all(H, st, false);
+    if (s == OCFD_OK && !H->react) s = launch_estdt_all(H, st, false);
     k_amr_end<<<1, 1, 0, st>>>(states(H));
     launches_counter += 2;
     H->launches = launches_counter;
@@ -1593,6 +1859,8 @@ int ocfd_amr_tuned(const ocfd_amr* H, int lev, int32_t* tile, int32_t* sched) {
 
 ocfd_status ocfd_amr_set_time_integration(ocfd_amr* H, int32_t order) {
     if (!H || order < 1 || order > 3) return fail(OCFD_BAD_ARG, "ocfd_amr_set_time_integration: order is 1, 2 or 3");
+    if (H->react && order == 3)
+        return fail(OCFD_UNSUPPORTED, "ocfd_amr_set_time_integration: the reacting hierarchy steps with RK2 or Euler");
     if (order == H->rk_order) return OCFD_OK;
     if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_amr_set_time_integration");
     H->rk_order = order;
@@ -1602,6 +1870,8 @@ ocfd_status ocfd_amr_set_time_integration(ocfd_amr* H, int32_t order) {
 
 ocfd_status ocfd_amr_set_eb(ocfd_amr* H, const ocfd_eb_desc* eb) {
     if (!H || !eb) return fail(OCFD_BAD_ARG, "ocfd_amr_set_eb: null argument");
+    if (H->react && eb->kind != OCFD_EB_NONE)
+        return fail(OCFD_UNSUPPORTED, "ocfd_amr_set_eb: the reacting hierarchy has no embedded body");
     if (cudaDeviceSynchronize() != cudaSuccess) return check_launch("ocfd_amr_set_eb");
     H->has_eb = eb->kind != OCFD_EB_NONE;
     H->eb = *eb;
@@ -1615,7 +1885,23 @@ ocfd_status ocfd_amr_set_eb(ocfd_amr* H, const ocfd_eb_desc* eb) {
     return s;
 }
 
+static ocfd_status amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, const ocfd_amr_react_desc* react,
+                              ocfd_amr** out);
+
 ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_amr** out) {
+    return amr_create(ctx, desc, nullptr, out);
+}
+
+ocfd_status ocfd_amr_create_reacting(ocfd_context* ctx, const ocfd_amr_desc* desc, const ocfd_amr_react_desc* react,
+                                     ocfd_amr** out) {
+    if (!react) return fail(OCFD_BAD_ARG, "ocfd_amr_create_reacting: null react description");
+    if (!(react->dt > 0) || react->chem_substeps < 0 || (react->flags & ~(unsigned)(OCFD_VISC | OCFD_FLUX_FP32)))
+        return fail(OCFD_BAD_ARG, "ocfd_amr_create_reacting: dt > 0, chem_substeps >= 0, flags OCFD_VISC | OCFD_FLUX_FP32");
+    return amr_create(ctx, desc, react, out);
+}
+
+static ocfd_status amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, const ocfd_amr_react_desc* react,
+                              ocfd_amr** out) {
     if (!ctx || !desc || !out || desc->nbox0 <= 0 || !desc->boxes0) return fail(OCFD_BAD_ARG, "ocfd_amr_create: bad arguments");
     *out = nullptr;
     if (desc->max_level < 0 || desc->max_level >= OCFD_AMR_MAX_LEVELS)
@@ -1635,6 +1921,12 @@ ocfd_status ocfd_amr_create(ocfd_context* ctx, const ocfd_amr_desc* desc, ocfd_a
     ocfd_amr* H = new ocfd_amr();
     H->ctx = ctx;
     H->desc = *desc;
+    if (react) {
+        H->react = true;
+        H->ncomp = 5 + NSP;
+        H->rdesc = *react;
+        H->rk_order = 2;  // the reference's multispecies flow step supports Euler and RK2 (FlowAdvance.cpp:49-88)
+    }
     H->boxes0.assign(desc->boxes0, desc->boxes0 + desc->nbox0);
     H->desc.boxes0 = nullptr;
     for (int e = 0; e < 3; ++e) H->periodic[e] = desc->lo_bc[e] == OCFD_BC_INTERIOR;
@@ -1751,6 +2043,8 @@ ocfd_status ocfd_amr_advance(ocfd_amr* H, int nsteps, double cfl, unsigned flags
     if (!H || nsteps < 0 || !(cfl > 0)) return fail(OCFD_BAD_ARG, "ocfd_amr_advance");
     if (flags & ~(unsigned)(OCFD_FLUX_FP32 | OCFD_PER_BOX | OCFD_GRAVITY))
         return fail(OCFD_BAD_ARG, "ocfd_amr_advance: flags (inviscid ideal gas only)");
+    if (H->react && (flags & ~(unsigned)OCFD_FLUX_FP32))
+        return fail(OCFD_BAD_ARG, "ocfd_amr_advance: a reacting hierarchy takes OCFD_FLUX_FP32 only");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     for (int i = 0; i < nsteps; ++i) {
         if (H->desc.regrid_int > 0 && H->steps > 0 && H->steps % H->desc.regrid_int == 0) {

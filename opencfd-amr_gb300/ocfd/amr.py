@@ -24,8 +24,14 @@ class AmrDesc(ctypes.Structure):
                 ("regrid_int", ctypes.c_int32), ("refine_dengrad", ctypes.c_double)]
 
 
+class AmrReactDesc(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("chem_substeps", ctypes.c_int32), ("flags", ctypes.c_uint32)]
+
+
 _vp = ctypes.c_void_p
 declare("ocfd_amr_create", ctypes.c_int, [_vp, ctypes.POINTER(AmrDesc), ctypes.POINTER(_vp)])
+declare("ocfd_amr_create_reacting", ctypes.c_int, [_vp, ctypes.POINTER(AmrDesc), ctypes.POINTER(AmrReactDesc),
+                                                   ctypes.POINTER(_vp)])
 declare("ocfd_amr_destroy", ctypes.c_int, [_vp])
 declare("ocfd_amr_nlevels", ctypes.c_int, [_vp])
 declare("ocfd_amr_level", _vp, [_vp, ctypes.c_int])
@@ -63,12 +69,15 @@ def _boxes_array(boxes):
 
 
 class Hierarchy:
-    """A refined hierarchy over the level-0 `boxes0` of the domain 0..n0-1."""
+    """A refined hierarchy over the level-0 `boxes0` of the domain 0..n0-1.
+    react = dict(dt=..., chem_substeps=4, visc=True): a reacting hierarchy
+    (5 + 9 components, ocfd_amr_create_reacting)."""
 
     def __init__(self, ctx, boxes0, n0, lo_bc, hi_bc, dx, prob_lo=(0.0, 0.0, 0.0), bc_case=0,
                  case_params=(), max_level=2, blocking_factor=(32, 32, 32), max_grid_size=(128, 128, 128),
-                 n_error_buf=1, regrid_int=2, refine_dengrad=0.05):
+                 n_error_buf=1, regrid_int=2, refine_dengrad=0.05, react=None):
         self.ctx = ctx
+        self.ncomp = 14 if react else 5
         self.lib = load()
         self.n0 = tuple(n0)
         self.dx0 = tuple(dx)
@@ -93,7 +102,16 @@ class Hierarchy:
         d.refine_dengrad = refine_dengrad
         self.desc = d
         h = ctypes.c_void_p()
-        check(self.lib.ocfd_amr_create(ctx.h, ctypes.byref(d), ctypes.byref(h)), "ocfd_amr_create")
+        if react:
+            r = AmrReactDesc()
+            r.dt = react["dt"]
+            r.chem_substeps = react.get("chem_substeps", 4)
+            r.flags = (1 if react.get("visc", True) else 0) | (4 if react.get("flux_fp32", False) else 0)
+            self.rdesc = r
+            check(self.lib.ocfd_amr_create_reacting(ctx.h, ctypes.byref(d), ctypes.byref(r), ctypes.byref(h)),
+                  "ocfd_amr_create_reacting")
+        else:
+            check(self.lib.ocfd_amr_create(ctx.h, ctypes.byref(d), ctypes.byref(h)), "ocfd_amr_create")
         self.h = h
 
     def close(self):
@@ -133,7 +151,7 @@ class Hierarchy:
         if not h:
             raise IndexError(lev)
         lo, hi = self.domain(lev)
-        return Level.wrap(self.ctx, h, self.grids(lev), lo, hi)
+        return Level.wrap(self.ctx, h, self.grids(lev), lo, hi, ncomp=self.ncomp)
 
     def set_eb(self, desc):
         """Cut every level with an embedded body (ocfd.level.eb_desc(...))."""
@@ -226,7 +244,7 @@ class Hierarchy:
         L = self.level(lev)
         lo, hi = self.domain(lev)
         n = [hi[d] + 1 for d in range(3)]
-        out = np.full((5, n[2], n[1], n[0]), np.nan)
+        out = np.full((self.ncomp, n[2], n[1], n[0]), np.nan)
         L.unpack_valid(L.copy_out(stream=stream), out)
         mask = np.zeros((n[2], n[1], n[0]), bool)
         for blo, bhi in L.boxes:

@@ -29,7 +29,15 @@ tables, what one coarse step of the GPU hierarchy does:
   stop time (EBR::computeNewDt, Source/EBR.cpp:240-305);
 * regridding: |d rho| >= refine_dengrad (Source/Tagging.H:11-36) buffered by
   n_error_buf, blocks of blocking_factor cells, proper nesting by 2 coarse
-  cells, greedy clustering into boxes of at most max_grid_size.
+  cells, greedy clustering into boxes of at most max_grid_size;
+* with `react`: the CHEM build's EBR::advance on every level and substep
+  (Source/Advance.cpp:158-174): 5 + 9 components (conserved state, partial
+  densities), chemistry over dt_l / 2 in 4 / 2^l substeps (ocfdo_chem_advance,
+  Source/CHEM/ChemAdvance.cpp:27-82), the RK2 multispecies flow step
+  (ocfdo_rhs_chem per box, Source/CHEM/FlowAdvance.cpp:9-90) with flow and
+  species flux registers (flux_reg / flux_reg_spec), chemistry over dt_l / 2;
+  post_timestep: reflux, species renormalisation (Source/EBR.cpp:313-357),
+  average-down; the fixed coarse step of the CHEM build (Source/Advance.cpp:54-57).
 
 Parity note: AMReX is not part of the reference tree (empty submodule), so the
 coarse-fine operators restate published methods rather than AMReX's code:
@@ -123,8 +131,13 @@ def _sl(lo, hi, g=0):
 class AmrOracle:
     def __init__(self, orc, n0, dx0, lo_bc, hi_bc, boxes0, prob_lo=(0.0, 0.0, 0.0), bc_case=0,
                  case_params=(), max_level=1, blocking_factor=(8, 8, 8), max_grid_size=(32, 32, 32),
-                 n_error_buf=1, refine_dengrad=0.05, eb=None, time_integration=3):
+                 n_error_buf=1, refine_dengrad=0.05, eb=None, time_integration=None, react=None):
         self.orc = orc
+        # react: None or dict(dt=..., chem_substeps=4, visc=True)
+        self.react = react
+        self.nc = 14 if react else 5
+        if time_integration is None:
+            time_integration = 2 if react else 3
         self.rk = time_integration  # 3: SSP-RK3, 2: RK2 (Heun), 1: Euler
         self.eb = eb          # None or dict(center=(cx, cy), radius=r, nsub=16, redistribute=False)
         self._geoms = {}
@@ -172,7 +185,7 @@ class AmrOracle:
 
     def _new_level(self, l, boxes):
         n = self.n(l)
-        U = np.full((5, n[2] + 2 * NG, n[1] + 2 * NG, n[0] + 2 * NG), np.nan)
+        U = np.full((self.nc, n[2] + 2 * NG, n[1] + 2 * NG, n[0] + 2 * NG), np.nan)
         mask = np.zeros((n[2], n[1], n[0]), bool)
         for lo, hi in boxes:
             mask[_sl(lo, hi)] = True
@@ -286,10 +299,11 @@ class AmrOracle:
         L = self.levels[l]
         n = self.n(l)
         dxinv = tuple(1.0 / x for x in self.dx(l))
-        dS = np.full((5, n[2], n[1], n[0]), np.nan)
+        nc = self.nc
+        dS = np.full((nc, n[2], n[1], n[0]), np.nan)
         F = None
         if with_flux:
-            F = [np.zeros((5, n[2] + (d == 2), n[1] + (d == 1), n[0] + (d == 0))) for d in range(3)]
+            F = [np.zeros((nc, n[2] + (d == 2), n[1] + (d == 1), n[0] + (d == 0))) for d in range(3)]
         g = self.geom(l)
         cls = self.classes(l)
         for b, (lo, hi) in enumerate(L["boxes"]):
@@ -298,7 +312,12 @@ class AmrOracle:
                 continue
             Sb = np.ascontiguousarray(S[(slice(None),) + _sl((lo[0] - NG, lo[1] - NG, lo[2] - NG),
                                                              (hi[0] + NG, hi[1] + NG, hi[2] + NG), NG)])
-            if cls[b] == BOX_REGULAR:
+            if self.react:
+                d5, ds, f5, fs, _ = self.orc.rhs_chem(np.ascontiguousarray(Sb[:5]), np.ascontiguousarray(Sb[5:]),
+                                                      dxinv, do_visc=self.react.get("visc", True))
+                d_ = np.concatenate([d5, ds])
+                f = [np.concatenate([f5[d], fs[d]]) for d in range(3)]
+            elif cls[b] == BOX_REGULAR:
                 d_, f = self.orc.rhs_regular(Sb, dxinv)
             else:
                 gsl = (slice(None), slice(lo[2], hi[2] + 2 * NG + 1), slice(lo[1], hi[1] + 2 * NG + 1),
@@ -322,15 +341,18 @@ class AmrOracle:
 
     def step(self, cfl):
         """One coarse step; returns dt_0."""
-        if self.est is None:
-            self.est = [self._estdt(l) for l in range(len(self.levels))]
-        est = min(e * (1 << l) for l, e in enumerate(self.est))
-        dt = cfl * est
-        if self.dt_prev > 0 and dt > 1.1 * self.dt_prev:
-            dt = 1.1 * self.dt_prev
-        if self.time + dt > self.stop_time - 0.001 * dt:
-            dt = self.stop_time - self.time
-        dt = max(dt, 0.0)
+        if self.react:
+            dt = self.react["dt"]
+        else:
+            if self.est is None:
+                self.est = [self._estdt(l) for l in range(len(self.levels))]
+            est = min(e * (1 << l) for l, e in enumerate(self.est))
+            dt = cfl * est
+            if self.dt_prev > 0 and dt > 1.1 * self.dt_prev:
+                dt = 1.1 * self.dt_prev
+            if self.time + dt > self.stop_time - 0.001 * dt:
+                dt = self.stop_time - self.time
+            dt = max(dt, 0.0)
         for l, L in enumerate(self.levels):
             L["dt"] = dt / (1 << l)
             L["time"] = self.time
@@ -339,8 +361,33 @@ class AmrOracle:
         self.dt_prev = dt
         for L in self.levels:
             L["time"] = self.time
-        self.est = [self._estdt(l) for l in range(len(self.levels))]
+        if not self.react:
+            self.est = [self._estdt(l) for l in range(len(self.levels))]
         return dt
+
+    def _boxes_cells(self, l, U, fn):
+        """fn(S (5, n), spec (9, n)) on the valid cells of every box of level l, in place"""
+        for lo, hi in self.levels[l]["boxes"]:
+            gs = (slice(None),) + _sl(lo, hi, NG)
+            blk = U[gs]
+            a = np.ascontiguousarray(blk[:5].reshape(5, -1))
+            b = np.ascontiguousarray(blk[5:].reshape(9, -1))
+            fn(a, b)
+            U[gs] = np.concatenate([a, b]).reshape(blk.shape)
+
+    def _chem(self, l, U):
+        """chemistry over half of level l's step (Source/Advance.cpp:158-173)"""
+        it = max(1, self.react.get("chem_substeps", 4) >> l) if l <= 2 else 1
+        dt2 = 0.5 * self.levels[l]["dt"] / it
+
+        def go(a, b):
+            for _ in range(it):
+                self.orc.chem_advance(a, b, dt2)
+        self._boxes_cells(l, U, go)
+
+    def _renorm(self, l, U):
+        """species clip and rescale, EBR::post_timestep (Source/EBR.cpp:333-357)"""
+        self._boxes_cells(l, U, self.orc.spec_renorm)
 
     def _advance(self, l, it):
         L = self.levels[l]
@@ -357,6 +404,8 @@ class AmrOracle:
         nst = sch["nst"]
         last = 3 if has_child else 0
         out_of = (1, 2, last) if self.rk == 3 else ((1, last) if self.rk == 2 else (last,))
+        if self.react:
+            self._chem(l, A)
         for k in range(nst):
             S = bufs[sch["src"][k]]
             self.fill(l, S, self._cf_coefs(k, theta), sch["tfrac"][k], parent)
@@ -380,12 +429,18 @@ class AmrOracle:
                 L["creg"] = [L["creg"][d] + w * F[d] for d in range(3)]
             if l > 0:
                 L["freg"] = [L["freg"][d] + w * F[d] for d in range(3)]
+        if self.react:
+            self._chem(l, bufs[last])
+            if not has_child:
+                self._renorm(l, bufs[last])
         if has_child:
             D = bufs[3]
             self.fill(l, D, self._cf_coefs(3, theta), 1.0, parent)
             for i in (1, 2):
                 self._advance(l + 1, i)
             self._reflux(l, D)
+            if self.react:
+                self._renorm(l, D)
             self._avg_down(l, D)
             L["U"] = D.copy()
         if l > 0:

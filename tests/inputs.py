@@ -84,3 +84,40 @@ def cylinder_box(nx, ny, nz, lo=(0, 0, 0), r_cells=None, center_cells=None):
         r_cells = 0.3 * min(nx, ny)
     phi = cylinder_phi(center_cells[0], center_cells[1], r_cells)
     return box_geometry(phi, lo, (nx, ny, nz), (1.0, 1.0, 1.0), nsub=16)
+
+
+def react_hot_spot_fab(oracle, n_domain, dx, T0=1200.0, dT=600.0, radius_cells=3.0, p=101325.0):
+    """fab_of_box(lev, lo, hi, dx_l) for a periodic phi = 1 H2/air box with one
+    Gaussian hot spot at the domain centre (radius in level-0 cells): the grown
+    FAB (14, nz+8, ny+8, nx+8) of conserved state and partial densities,
+    built on the host with the oracle's CKXTY / CKRHOY / CKUBMS."""
+    from ocfd.cases import PHI1_AIR_X
+    y = oracle.ckxty(np.array(PHI1_AIR_X))
+    L = [n * dx for n in n_domain]
+    centre = [0.5 * x for x in L]
+    cache = {}
+
+    def fab(lev, lo, hi, dxl):
+        key = (lev, tuple(lo), tuple(hi))
+        if key in cache:
+            return cache[key].copy()
+        coords = [(np.arange(lo[d] - NG, hi[d] + NG + 1) + 0.5) * dxl[d] for d in range(3)]
+        Z, Y, X = np.meshgrid(coords[2], coords[1], coords[0], indexing="ij")
+        r2 = 0.0
+        for C, c, Ld in ((X, centre[0], L[0]), (Y, centre[1], L[1]), (Z, centre[2], L[2])):
+            dd = np.abs(np.mod(C, Ld) - c)
+            dd = np.minimum(dd, Ld - dd)
+            r2 = r2 + dd * dd
+        T = T0 + dT * np.exp(-r2 / (radius_cells * dx) ** 2)
+        F = np.zeros((5 + NSPEC,) + T.shape)
+        flat = T.ravel()
+        for i, t in enumerate(flat):
+            idx = np.unravel_index(i, T.shape)
+            rho = oracle.ckrhoy(p, float(t), y)
+            r = rho * y
+            F[(0,) + idx] = rho
+            F[(4,) + idx] = oracle.ckubms(float(t), r)
+            F[(slice(5, None),) + idx] = r
+        cache[key] = F
+        return F.copy()
+    return fab
