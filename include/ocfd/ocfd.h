@@ -659,10 +659,13 @@ ocfd_status ocfd_mlp_train_step(ocfd_mlp* mlp, const float* X, const float* T, i
 /* Guard of the surrogate chemistry substep: a cell takes the network's increments
  * only when its inputs lie in the training range and the increments keep every
  * Y in [-y_tol, 1 + y_tol] and the H, O, N element contents within elem_tol
- * (relative); otherwise the FP64 implicit substep is applied to it. */
+ * (relative), and, when dy_rel_max > 0, change no Y_n by more than
+ * dy_rel_max * max(Y_n, y_floor) (the per-output error criterion); otherwise
+ * the FP64 implicit substep is applied to it. */
 typedef struct ocfd_surrogate_guard {
     double T_min, T_max, p_min, p_max, dt_min, dt_max;
     double y_tol, elem_tol;
+    double dy_rel_max, y_floor;
 } ocfd_surrogate_guard;
 
 /* Chemistry of a reacting level by the network (NULL: back to the FP64
@@ -678,6 +681,11 @@ ocfd_status ocfd_chem_cells_advance(ocfd_context* ctx, int64_t n, double* U, con
                                     void* stream);
 /* T, p, Y[9] of each cell into out [11][n] */
 ocfd_status ocfd_chem_cells_props(ocfd_context* ctx, int64_t n, const double* U, double* out, void* stream);
+/* constant-pressure restoration after a constant-volume substep: each cell at
+ * rest is brought to p_target[i] (device, n doubles) at the enthalpy
+ * e + p_target / rho (mass fractions kept); the generator of constant-pressure
+ * ignition states.  No counterpart in the reference. */
+ocfd_status ocfd_chem_cells_isobaric(ocfd_context* ctx, int64_t n, double* U, const double* p_target, void* stream);
 /* one surrogate substep of dt per cell (with the FP64 fallback); *fallbacks
  * receives the number of cells the guard sent to the FP64 substep */
 ocfd_status ocfd_chem_cells_surrogate(ocfd_context* ctx, ocfd_mlp* mlp, const ocfd_surrogate_guard* guard,
@@ -692,6 +700,12 @@ ocfd_status ocfd_measure_fma_peaks(double* fp64_gflops, double* fp32_gflops);
  * in GFLOP/s (4 flops per instruction); the FP32 denominator of the mixed form,
  * whose WENO-Z runs on packed pairs.  No counterpart in the reference. */
 ocfd_status ocfd_measure_ffma2_peak(double* fp32x2_gflops);
+
+/* Test hook: the FP32-flux form stages the cross of each tile of depth >= 4
+ * (the tile and its +-3 halos along x, y and z) by TMA (on != 0, the default)
+ * or with plain loads (0), in stage tables built from now on; both give the
+ * same results.  No counterpart in the reference. */
+void ocfd_set_tma_staging(int32_t on);
 
 /* Test hook: fast[i] = the reciprocal the fused FP64 kernels use in place of an
  * IEEE division (approximate seed + two Newton-Raphson steps), ieee[i] = 1/x[i]

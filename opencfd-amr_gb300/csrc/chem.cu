@@ -274,6 +274,56 @@ __global__ void k_chem_props(const long long* __restrict__ off, const long long*
     }
 }
 
+// Constant-pressure restoration of 0D cells at rest after a constant-volume
+// substep.  A closed adiabatic system at pressure p keeps its enthalpy; the
+// constant-volume substep kept e and rho, so the enthalpy of the isobaric step
+// is h = e + p_target / rho with the density before the substep.  T' solves
+// sum_n Y_n h_n(T') = h (Newton on the NASA-7 enthalpy with its cp), then
+// rho' = p_target / (Ru T' sum_n Y_n / W_n) and rho' E' = rho' h - p_target.
+// Generator of constant-pressure ignition states; no counterpart in the
+// reference, whose reactor is the constant-volume cell of
+// Source/CHEM/ChemAdvance.cpp:27-82.
+__global__ void k_chem_isobaric(long long ncell, double* __restrict__ U, const double* __restrict__ p_target,
+                                DevParm P) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+         c += (long long)gridDim.x * blockDim.x) {
+        double T, p, Y[NSP], rho, r[NSP];
+        double* x = U + c;
+        cell_props(x, ncell, P, &T, &p, Y, &rho, r);
+        const double pt = p_target[c];
+        const double rhoinv = 1.0 / rho;
+        const double ux = x[ncell] * rhoinv, uy = x[2 * ncell] * rhoinv, uz = x[3 * ncell] * rhoinv;
+        const double e = x[4 * ncell] * rhoinv - 0.5 * (ux * ux + uy * uy + uz * uz);
+        const double h = e + pt * rhoinv;
+        double yw = 0.0;
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) yw += Y[n] * c_mder.inv_mw[n];
+        for (int it = 0; it < 50; ++it) {
+            double hs[NSP];
+            species_enthalpy(T, hs);
+            double hm = 0.0, cp = 0.0;
+            const double T2 = T * T;
+#pragma unroll
+            for (int n = 0; n < NSP; ++n) {
+                const double* a = nasa(T, n);
+                const double w = Y[n] * c_mder.inv_mw[n];
+                hm += w * hs[n];
+                cp += w * (a[0] + a[1] * T + a[2] * T2 + a[3] * T2 * T + a[4] * T2 * T2);
+            }
+            double dT = (h / P.Ru - hm) / cp;
+            dT = fmin(fmax(dT, -200.0), 200.0);
+            T += dT;
+            if (fabs(dT) <= 1e-10 * T) break;
+        }
+        const double rn = pt / (P.Ru * T * yw);
+        x[0] = rn;
+        x[ncell] = x[2 * ncell] = x[3 * ncell] = 0.0;
+        x[4 * ncell] = rn * h - pt;
+#pragma unroll
+        for (int n = 0; n < NSP; ++n) x[(5 + n) * ncell] = rn * Y[n];
+    }
+}
+
 // H, O, N atoms of H2, O2, H2O, H, O, OH, HO2, H2O2, N2
 __constant__ float c_elem[3][NSP] = {{2, 0, 2, 1, 0, 1, 1, 2, 0}, {0, 2, 1, 0, 1, 1, 2, 2, 0}, {0, 0, 0, 0, 0, 0, 0, 0, 2}};
 
@@ -376,6 +426,7 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
     const float Ru = (float)P.Ru, fdt = (float)dt;
     const float T_min = (float)g.T_min, T_max = (float)g.T_max, p_min = (float)g.p_min, p_max = (float)g.p_max;
     const float y_tol = (float)g.y_tol, elem_tol = (float)g.elem_tol;
+    const float dy_rel = (float)g.dy_rel_max, y_floor = (float)g.y_floor;
     for (long long t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
         const long long c = t * 128 + tid;
         const bool valid = c < ncell;
@@ -426,6 +477,15 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
         bool pass = dt_in && T >= T_min && T <= T_max && p >= p_min && p <= p_max;
 #pragma unroll
         for (int n = 0; n < NSP; ++n) pass = pass && Y[n] + dY[n] >= -y_tol && Y[n] + dY[n] <= 1.0f + y_tol;
+        // per-output criterion: the network's error in a rate is roughly a fixed
+        // fraction of the rate (its targets are logarithms of the rates), so a
+        // cell whose increments change no Y by more than dy_rel of itself (or of
+        // y_floor, for traces) keeps the relative error of every Y below that
+        // fraction of dy_rel per substep; the rest (ignition fronts) go to FP64
+        if (dy_rel > 0.0f) {
+#pragma unroll
+            for (int n = 0; n < NSP; ++n) pass = pass && fabsf(dY[n]) <= dy_rel * fmaxf(Y[n], y_floor);
+        }
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
             float have = 0.0f, d = 0.0f;
@@ -1284,6 +1344,19 @@ extern "C" ocfd_status ocfd_chem_cells_props(ocfd_context* ctx, int64_t n, const
     k_chem_props<<<(int)b, 128, 0, st>>>(L.off, L.stride, n, U, out, ctx->parm);
     ocfd_status s = check_launch("ocfd_chem_cells_props");
     if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("ocfd_chem_cells_props");
+    return s;
+}
+
+extern "C" ocfd_status ocfd_chem_cells_isobaric(ocfd_context* ctx, int64_t n, double* U, const double* p_target,
+                                                void* stream) {
+    using namespace ocfd;
+    if (!ctx || n <= 0 || !U || !p_target) return fail(OCFD_BAD_ARG, "ocfd_chem_cells_isobaric");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    long long b = (n + 127) / 128;
+    if (b > (long long)ctx->num_sms * 32) b = (long long)ctx->num_sms * 32;
+    k_chem_isobaric<<<(int)b, 128, 0, st>>>(n, U, p_target, ctx->parm);
+    ocfd_status s = check_launch("ocfd_chem_cells_isobaric");
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_launch("ocfd_chem_cells_isobaric");
     return s;
 }
 

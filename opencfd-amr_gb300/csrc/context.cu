@@ -148,6 +148,7 @@ ocfd_status ocfd_context_create(const ocfd_parm* parm, int device, ocfd_context*
         delete ctx;
         return fail(OCFD_OUT_OF_MEMORY, "ocfd_context_create: error word allocation");
     }
+    ctx->parm.err = ctx->d_error;
     ocfd_status s = mech_upload(*parm);
     if (s == OCFD_OK) s = configure_rhs_regular();
     if (s == OCFD_OK) s = configure_rhs_regular_f32();

@@ -4,7 +4,9 @@
 // 231-329): c2prim over the grown box, then per direction flux_split (full
 // grown box), reconstruction (WENO-Z, per face and component), compute_visc,
 // and finally divop - fused into one launch (rhs_regular_kernel.cuh).
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include "rhs_regular_kernel.cuh"
 
@@ -64,6 +66,63 @@ void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* d
     a.mode = RHS_WRITE_DSDT;
     a.dt_ptr = nullptr;
     a.cfl_min = nullptr;
+    encode_regular_tmaps(a, S, tile);
+}
+
+static bool g_regular_tma = true;
+
+void set_regular_tma(bool on) { g_regular_tma = on; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null when the driver does not offer it
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// The four box shapes of a tile's cross (centre, x halo 4 wide, y halo 3 deep,
+// z halo 3 deep) over S as a (x, y, z, component) tensor of doubles.  TMA wants
+// a 16-byte aligned base, strides that are multiples of 16 bytes and an x
+// offset times 8 bytes that is a multiple of 16 for every box: the tiles start
+// at lo + t TX with TX even and the x halo box at 4 cells before a tile, so
+// (lo - begin) must be even.  Only tiles of depth >= 4 are staged this way.
+bool encode_regular_tmaps(RegBoxArgs& a, const ocfd_array4* S, int tile) {
+    a.use_tma = 0;
+    if (!g_regular_tma || !S || tile < 0 || tile >= kNumRegularTiles) return false;
+    const TileShape& t = kRegularTiles[tile];
+    if (t.z < 4 || t.x % 2 != 0 || S->ncomp < 5) return false;
+    const uintptr_t base = reinterpret_cast<uintptr_t>(S->p);
+    if (base % 16 != 0 || S->jstride % 2 != 0 || S->kstride % 2 != 0 || S->nstride % 2 != 0) return false;
+    if (((a.lo[0] - S->begin[0]) & 1) != 0) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dim[4] = {(cuuint64_t)(S->end[0] - S->begin[0]), (cuuint64_t)(S->end[1] - S->begin[1]),
+                               (cuuint64_t)(S->end[2] - S->begin[2]), 5};
+    const cuuint64_t stride[3] = {(cuuint64_t)S->jstride * 8, (cuuint64_t)S->kstride * 8,
+                                  (cuuint64_t)S->nstride * 8};
+    const cuuint32_t box[4][4] = {{(cuuint32_t)t.x, (cuuint32_t)t.y, (cuuint32_t)t.z, 5},
+                                  {4, (cuuint32_t)t.y, (cuuint32_t)t.z, 5},
+                                  {(cuuint32_t)t.x, 3, (cuuint32_t)t.z, 5},
+                                  {(cuuint32_t)t.x, (cuuint32_t)t.y, 3, 5}};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    for (int m = 0; m < 4; ++m) {
+        if (enc(&a.tmap[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, S->p, dim, stride, box[m], estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    a.use_tma = 1;
+    return true;
 }
 
 }  // namespace ocfd
@@ -96,3 +155,5 @@ extern "C" ocfd_status ocfd_rhs_regular_box_f64(ocfd_context* ctx, const ocfd_ar
     return launch_rhs_regular(tile, (flags & OCFD_VISC) != 0, nullptr, nullptr, 1, a, ntiles,
                               P, static_cast<cudaStream_t>(stream));
 }
+
+extern "C" void ocfd_set_tma_staging(int32_t on) { ocfd::set_regular_tma(on != 0); }

@@ -2,6 +2,7 @@
 // entry point, the level driver and the batched (box-list) form.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "ocfd_internal.h"
@@ -56,6 +57,16 @@ struct RegBoxArgs {
     int zdom[2];
     int zmirror[2];
     int zsign[2];
+    // TMA staging of a tile's cross (the FP32-flux form on tiles of depth >= 4):
+    // tiled tensor maps of S as a 4-D tensor (x, y, z, component) whose boxes are
+    // the tile's centre (TX x TY x TZ), x halo (4 x TY x TZ: the low one starts 4
+    // cells before the tile, keeping every x offset even), y halo (TX x 3 x TZ)
+    // and z halo (TX x TY x 3), 5 components each.  use_tma = 0 when S does not
+    // meet TMA's rules (16-byte base and strides, even x offset of the box) or
+    // the tile is not staged this way: the kernel then loads the cross with
+    // plain loads, to the same values.
+    CUtensorMap tmap[4];
+    int use_tma;
 };
 
 // the cell a load at z index gk reads, and the velocity signs to flip
@@ -119,6 +130,12 @@ ocfd_status configure_rhs_regular_f32();
 void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* dSdt,
                        const ocfd_array4* flux, const ocfd_box& bx, const double dxinv[3],
                        int tile);
+// tensor maps of a.tmap for S and `tile` (sets a.use_tma); false when S does not
+// meet TMA's alignment rules or the driver entry point is missing
+bool encode_regular_tmaps(RegBoxArgs& a, const ocfd_array4* S, int tile);
+// process-wide switch of the TMA staging (tables built while it is off use
+// plain loads); a test hook: both ways give the same results
+void set_regular_tma(bool on);
 
 // d_boxes == nullptr: one box given by `single`, ntiles CTAs.
 // otherwise: nbox boxes, d_tile_start[b] = first CTA of box b, ntiles in total.

@@ -21,16 +21,27 @@
 //      reference's summation order x, y, z (Source/kernel/Kernels.H:94-96);
 //      face fluxes are written out when the caller asked for them (reflux).
 // Only U (read) and the output touch HBM.
+//
+// FP32-flux form on tiles of depth >= 4 (CrossOn): step 1 reads no global
+// memory.  Before the sweeps, the tile's cross - its centre and the +-3 halos
+// along x, y and z, every cell a pencil reads - is copied from the state FAB
+// into shared memory by seven TMA box loads (cp.async.bulk.tensor, completing
+// on an mbarrier with a bounded wait), narrowed and turned into primitives once
+// per cell (Q), and each direction's pencil is split from Q.  The primitives of
+// a cell are the same function of the same state either way, so the results
+// are bit-identical to the pencil-by-pencil form.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "device_physics.cuh"
 #include "weno_f32.cuh"
 #include "ocfd_internal.h"
 #include "rhs_regular.h"
+#include "tma.cuh"
 
 namespace ocfd {
 
@@ -65,8 +76,60 @@ __host__ __device__ constexpr int pencil_elems() {
     return a > b ? (a > c ? a : c) : (b > c ? b : c);
 }
 
+// tiles whose cross is staged by TMA (see the file comment)
+template <class FT, int TX, int TY, int TZ, bool VISC>
+struct CrossOn {
+    static constexpr bool value = std::is_same<FT, float>::value && !VISC && TZ >= 4 && TX % 2 == 0;
+};
+
+// Shared memory of a TMA-staged tile (offsets from a 128-byte aligned base):
+//   region A  the FP64 staging boxes - centre TX x TY x TZ, x halos 4 x TY x TZ
+//             (low one from 4 cells before the tile), y halos TX x 3 x TZ, z halos
+//             TX x TY x 3, 5 components each, x fastest, each 128-byte aligned -
+//             reused by the sweeps for the split and face fluxes;
+//   Q         FP32 primitives rho, u, v, w, c of the cross, 5 planes of NQ cells:
+//             centre, x halo (6 x TY x TZ: 3 low then 3 high), y halo
+//             (TX x 6 x TZ), z halo (TX x TY x 6).
+template <int TX, int TY, int TZ>
+struct Cross {
+    static constexpr int NC = TX * TY * TZ;
+    static constexpr int NXH = 6 * TY * TZ, NYH = 6 * TX * TZ, NZH = 6 * TX * TY;
+    static constexpr int NQ = NC + NXH + NYH + NZH;
+    static constexpr int SX = 4 * TY * TZ, SY = 3 * TX * TZ, SZ = 3 * TX * TY;  // cells of one halo box
+    static constexpr int al(int d) { return (d + 15) / 16 * 16; }              // doubles, to 128 bytes
+    static constexpr int OC = 0, OXL = al(5 * NC), OXH = OXL + al(5 * SX), OYL = OXH + al(5 * SX),
+                         OYH = OYL + al(5 * SY), OZL = OYH + al(5 * SY), OZH = OZL + al(5 * SZ),
+                         NSTAGE = OZH + al(5 * SZ);
+    static constexpr uint32_t BYTES_CXY = 8u * 5u * (NC + 2 * SX + 2 * SY), BYTES_Z = 8u * 5u * 2 * SZ;
+    // Q index of tile-local (x, y, z) of a pencil along D: only the D coordinate
+    // may lie outside the tile
+    template <int D>
+    __device__ static __forceinline__ int q_along(int x, int y, int z) {
+        if (D == 0) {
+            if (x < 0) return NC + (x + 3) + 6 * (y + TY * z);
+            if (x >= TX) return NC + (x - TX + 3) + 6 * (y + TY * z);
+        } else if (D == 1) {
+            if (y < 0) return NC + NXH + x + TX * ((y + 3) + 6 * z);
+            if (y >= TY) return NC + NXH + x + TX * ((y - TY + 3) + 6 * z);
+        } else {
+            if (z < 0) return NC + NXH + NYH + x + TX * (y + TY * (z + 3));
+            if (z >= TZ) return NC + NXH + NYH + x + TX * (y + TY * (z - TZ + 3));
+        }
+        return x + TX * (y + TY * z);
+    }
+};
+
+template <class FT, int TX, int TY, int TZ>
+__host__ __device__ constexpr size_t cross_region_a() {
+    const size_t st = 8 * (size_t)Cross<TX, TY, TZ>::NSTAGE;
+    const size_t pe = (sizeof(FT) * pencil_elems<TX, TY, TZ>() + 127) / 128 * 128;
+    return st > pe ? st : pe;
+}
+
 template <class FT, int TX, int TY, int TZ, bool VISC>
 __host__ __device__ constexpr size_t regular_smem_bytes() {
+    if (CrossOn<FT, TX, TY, TZ, VISC>::value)
+        return 128 + cross_region_a<FT, TX, TY, TZ>() + sizeof(float) * 5 * Cross<TX, TY, TZ>::NQ;
     return sizeof(FT) * (pencil_elems<TX, TY, TZ>() + (VISC ? 4 * Ring<TX, TY, TZ>::N : 0));
 }
 
@@ -98,9 +161,12 @@ struct Prec<float> {
     // c2prim in FP32 from the narrowed conserved state
     static __device__ __forceinline__ void prims(const DevParm& P, const View<const double>& S, int i,
                                                  int j, int k, float* q) {
+        prims_vals(P, S(i, j, k, 0), S(i, j, k, 1), S(i, j, k, 2), S(i, j, k, 3), S(i, j, k, 4), q);
+    }
+    static __device__ __forceinline__ void prims_vals(const DevParm& P, double s0, double s1, double s2, double s3,
+                                                      double s4, float* q) {
         const float g = P.f_gamma;
-        const float u0 = d2f_bits(S(i, j, k, 0)), u1 = d2f_bits(S(i, j, k, 1)), u2 = d2f_bits(S(i, j, k, 2)),
-                    u3 = d2f_bits(S(i, j, k, 3)), u4 = d2f_bits(S(i, j, k, 4));
+        const float u0 = d2f_bits(s0), u1 = d2f_bits(s1), u2 = d2f_bits(s2), u3 = d2f_bits(s3), u4 = d2f_bits(s4);
         const float rho = fmaxf(u0, P.f_smallr);
         const float rhoinv = __frcp_rn(rho);
         const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
@@ -113,6 +179,12 @@ struct Prec<float> {
         q[QPRES] = p;
         q[QT] = p * rhoinv * P.f_invRg;
         q[QC] = sqrtf(g * p * rhoinv);
+        // the primitives leave as values the optimiser cannot see through: the
+        // split forms its own products (u u, v v, ...) instead of sharing them
+        // with the kinetic energy above, which would change which products fuse
+        // into FMAs; so primitives split inline and primitives reloaded from
+        // shared memory (TMA-staged tiles) give the same fluxes
+        asm("" : "+f"(q[QRHO]), "+f"(q[QU]), "+f"(q[QV]), "+f"(q[QW]), "+f"(q[QC]));
     }
     template <int D>
     static __device__ __forceinline__ void split(const DevParm& P, const float* q, float* fp, float* fm) {
@@ -207,13 +279,101 @@ __device__ __forceinline__ void visc_face(const DevParm& P, const FT* ring, int 
                              (qu[2 * R::N + c] + qu[2 * R::N + l]) * tau[2] + (ktl + ktr) * dT);
 }
 
-template <class FT, int D, int TX, int TY, int TZ, bool VISC>
+// Primitives of a TMA-staged tile's cross into Q (layout: Cross), once per cell:
+// from the staged boxes, or with plain loads when the tile was not staged, for
+// the z halo of a slab whose z ghosts are mirrored (zvirt: those boxes are not
+// loaded) and for its cells outside the z domain.  Cells a pencil would not
+// read (beyond hi + 3) are left 0; the sweeps never use them.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void cross_prims(const RegBoxArgs& B, const DevParm& P, int i0, int j0, int k0,
+                                            const double* stage, bool staged, float* Q) {
+    using C = Cross<TX, TY, TZ>;
+    constexpr int NT = TX * TY * TZ;
+    for (int idx = threadIdx.x; idx < C::NQ; idx += NT) {
+        int x, y, z, so, sc;
+        bool zhalo = false;
+        if (idx < C::NC) {
+            x = idx % TX;
+            y = (idx / TX) % TY;
+            z = idx / (TX * TY);
+            so = C::OC + idx;
+            sc = C::NC;
+        } else if (idx < C::NC + C::NXH) {
+            const int r = idx - C::NC, h = r % 6;
+            y = (r / 6) % TY;
+            z = r / (6 * TY);
+            x = h < 3 ? h - 3 : TX + h - 3;
+            so = (h < 3 ? C::OXL + h + 1 : C::OXH + h - 3) + 4 * (y + TY * z);
+            sc = C::SX;
+        } else if (idx < C::NC + C::NXH + C::NYH) {
+            const int r = idx - C::NC - C::NXH, h = (r / TX) % 6;
+            x = r % TX;
+            z = r / (6 * TX);
+            y = h < 3 ? h - 3 : TY + h - 3;
+            so = (h < 3 ? C::OYL + TX * h : C::OYH + TX * (h - 3)) + x + 3 * TX * z;
+            sc = C::SY;
+        } else {
+            const int r = idx - C::NC - C::NXH - C::NYH, h = r / (TX * TY);
+            x = r % TX;
+            y = (r / TX) % TY;
+            z = h < 3 ? h - 3 : TZ + h - 3;
+            so = (h < 3 ? C::OZL + TX * TY * h : C::OZH + TX * TY * (h - 3)) + x + TX * y;
+            sc = C::SZ;
+            zhalo = true;
+        }
+        const int gi = i0 + x, gj = j0 + y, gk = k0 + z;
+        float q[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        const bool zout = B.zvirt && (gk < B.zdom[0] || gk > B.zdom[1]);
+        if (staged && !zout && !(zhalo && B.zvirt)) {
+            Prec<float>::prims_vals(P, stage[so], stage[so + sc], stage[so + 2 * sc], stage[so + 3 * sc],
+                                    stage[so + 4 * sc], q);
+        } else if (gi <= B.hi[0] + 3 && gj <= B.hi[1] + 3 && (B.zvirt || gk <= B.hi[2] + 3)) {
+            int sg;
+            Prec<float>::prims(P, B.S, gi, gj, zmap(B, gk, sg), q);
+            if (sg & 1) q[QU] = -q[QU];
+            if (sg & 2) q[QV] = -q[QV];
+            if (sg & 4) q[QW] = -q[QW];
+        }
+        Q[idx] = q[QRHO];
+        Q[C::NQ + idx] = q[QU];
+        Q[2 * C::NQ + idx] = q[QV];
+        Q[3 * C::NQ + idx] = q[QW];
+        Q[4 * C::NQ + idx] = q[QC];
+    }
+}
+
+template <class FT, int D, int TX, int TY, int TZ, bool VISC, bool CROSS = false>
 __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int i0, int j0, int k0,
-                                      FT* F, FT* FF, const FT* ring, FT* acc) {
+                                      FT* F, FT* FF, const FT* ring, FT* acc, const FT* Q = nullptr) {
     using PC = Pencil<D, TX, TY, TZ>;
     constexpr int NT = TX * TY * TZ;
     const int tid = threadIdx.x;
-    // ---- 1. primitives and Steger-Warming split over the pencil
+    // ---- 1. primitives and Steger-Warming split over the pencil (primitives
+    // from Q when the cross was staged)
+    if constexpr (CROSS) {
+        using C = Cross<TX, TY, TZ>;
+        for (int c = tid; c < PC::N; c += NT) {
+            const int px = c % PC::PX, py = (c / PC::PX) % PC::PY, pz = c / (PC::PX * PC::PY);
+            const int lx = px - (D == 0 ? 3 : 0), ly = py - (D == 1 ? 3 : 0), lz = pz - (D == 2 ? 3 : 0);
+            FT fp[5] = {0, 0, 0, 0, 0}, fm[5] = {0, 0, 0, 0, 0};
+            if (i0 + lx <= B.hi[0] + (D == 0 ? 3 : 0) && j0 + ly <= B.hi[1] + (D == 1 ? 3 : 0) &&
+                k0 + lz <= B.hi[2] + (D == 2 ? 3 : 0)) {
+                const int qi = C::template q_along<D>(lx, ly, lz);
+                FT q[7];
+                q[QRHO] = Q[qi];
+                q[QU] = Q[C::NQ + qi];
+                q[QV] = Q[2 * C::NQ + qi];
+                q[QW] = Q[3 * C::NQ + qi];
+                q[QC] = Q[4 * C::NQ + qi];
+                Prec<FT>::template split<D>(P, q, fp, fm);
+            }
+#pragma unroll
+            for (int n = 0; n < 5; ++n) {
+                F[n * PC::N + c] = fp[n];
+                F[(5 + n) * PC::N + c] = fm[n];
+            }
+        }
+    } else
     for (int c = tid; c < PC::N; c += NT) {
         const int px = c % PC::PX, py = (c / PC::PX) % PC::PY, pz = c / (PC::PX * PC::PY);
         const int gi = i0 + px - (D == 0 ? 3 : 0);
@@ -308,7 +468,8 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
 // RHS / stage; the CFL bound of its cells is folded into local_dt.
 template <class FT, int TX, int TY, int TZ, bool VISC>
 __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
-                                         int nbox, const RegBoxArgs& single, const DevParm& P, int t, FT* smem,
+                                         int nbox, const RegBoxArgs& single, const DevParm& P, int t,
+                                         unsigned char* sbase, uint64_t* bar, uint32_t& phase, bool& abort,
                                          double& local_dt) {
     constexpr int NT = TX * TY * TZ;
     // locate the box of this tile: a single box, or a prefix table over a box list
@@ -327,7 +488,53 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
     const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
     const int i0 = B.lo[0] + tx * TX, j0 = B.lo[1] + ty * TY, k0 = B.lo[2] + tz * TZ;
 
+    FT acc[5];
+    if constexpr (CrossOn<FT, TX, TY, TZ, VISC>::value) {
+        using C = Cross<TX, TY, TZ>;
+        double* stage = reinterpret_cast<double*>(sbase);
+        float* Q = reinterpret_cast<float*>(sbase + cross_region_a<FT, TX, TY, TZ>());
+        const bool staged = B.use_tma != 0;
+        if (staged) {
+            // region A was last written by the generic proxy (the previous tile's
+            // sweeps): order those accesses before this tile's TMA writes
+            tma::fence_proxy_async();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (boxes)  // maps of a box table in global memory (a kernel parameter needs no fence)
+                    for (int m = 0; m < 4; ++m) tma::fence_tensormap_acquire(&B.tmap[m]);
+                const bool stz = !B.zvirt;
+                tma::expect_tx(bar, C::BYTES_CXY + (stz ? C::BYTES_Z : 0u));
+                const int x = i0 - B.S.b0, y = j0 - B.S.b1, z = k0 - B.S.b2;
+                tma::load_4d(stage + C::OC, &B.tmap[0], x, y, z, 0, bar);
+                tma::load_4d(stage + C::OXL, &B.tmap[1], x - 4, y, z, 0, bar);
+                tma::load_4d(stage + C::OXH, &B.tmap[1], x + TX, y, z, 0, bar);
+                tma::load_4d(stage + C::OYL, &B.tmap[2], x, y - 3, z, 0, bar);
+                tma::load_4d(stage + C::OYH, &B.tmap[2], x, y + TY, z, 0, bar);
+                if (stz) {
+                    tma::load_4d(stage + C::OZL, &B.tmap[3], x, y, z - 3, 0, bar);
+                    tma::load_4d(stage + C::OZH, &B.tmap[3], x, y, z + TZ, 0, bar);
+                }
+            }
+            const bool done = tc::mbar_wait(bar, phase);
+            phase ^= 1u;
+            if (!__syncthreads_and(done)) {
+                // the bounded wait ran out: report it, give the copies in flight the
+                // same time to land, and leave the remaining tiles
+                if (threadIdx.x == 0 && P.err) atomicOr(P.err, 2u);
+                tc::mbar_wait(bar, phase ^ 1u);
+                abort = true;
+                return;
+            }
+        }
+        cross_prims<TX, TY, TZ>(B, P, i0, j0, k0, stage, staged, Q);
+        __syncthreads();
+        FT* F = reinterpret_cast<FT*>(sbase);
+        sweep<FT, 0, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<0, TX, TY, TZ>::N, nullptr, acc, Q);
+        sweep<FT, 1, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<1, TX, TY, TZ>::N, nullptr, acc, Q);
+        sweep<FT, 2, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<2, TX, TY, TZ>::N, nullptr, acc, Q);
+    } else {
     constexpr int PMAX = pencil_elems<TX, TY, TZ>();
+    FT* smem = reinterpret_cast<FT*>(sbase);
     FT* F = smem;
     FT* ring = smem + PMAX;
     if (VISC) {
@@ -350,10 +557,10 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
         }
         __syncthreads();
     }
-    FT acc[5];
     sweep<FT, 0, TX, TY, TZ, VISC>(B, P, i0, j0, k0, F, F + 10 * Pencil<0, TX, TY, TZ>::N, ring, acc);
     sweep<FT, 1, TX, TY, TZ, VISC>(B, P, i0, j0, k0, F, F + 10 * Pencil<1, TX, TY, TZ>::N, ring, acc);
     sweep<FT, 2, TX, TY, TZ, VISC>(B, P, i0, j0, k0, F, F + 10 * Pencil<2, TX, TY, TZ>::N, ring, acc);
+    }
 
     const int ti = threadIdx.x % TX, tj = (threadIdx.x / TX) % TY, tk = threadIdx.x / (TX * TY);
     const int ci = i0 + ti, cj = j0 + tj, ck = k0 + tk;
@@ -395,19 +602,44 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
 //   SCHED_QUEUE   persistent: CTAs take the next tile from a counter in `queue`
 //                 (queue[0] next tile, queue[1] CTAs done); the last CTA to finish
 //                 resets both, so every launch starts from zero (graph replays too)
+// CTAs per SM that a tile's shared memory admits (228 KB per SM, 1 KB of it
+// reserved per CTA; at most 2048 threads): the register budget follows from it,
+// so the compiler neither spills below nor plans above the occupancy the tile gets
 template <class FT, int TX, int TY, int TZ, bool VISC>
-__global__ void __launch_bounds__(TX* TY* TZ)
+__host__ __device__ constexpr int regular_min_blocks() {
+    const int b = (int)((228u * 1024u) / (regular_smem_bytes<FT, TX, TY, TZ, VISC>() + 1024u));
+    const int t = 2048 / (TX * TY * TZ);
+    const int m = b < t ? b : t;
+    return m < 1 ? 1 : m;
+}
+
+template <class FT, int TX, int TY, int TZ, bool VISC>
+__global__ void __launch_bounds__(TX* TY* TZ, (regular_min_blocks<FT, TX, TY, TZ, VISC>()))
     k_rhs_regular(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
-                  int nbox, RegBoxArgs single, DevParm P, int ntiles, int sched, unsigned* queue) {
+                  int nbox, const __grid_constant__ RegBoxArgs single, DevParm P, int ntiles, int sched,
+                  unsigned* queue) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    FT* smem = reinterpret_cast<FT*>(smem_raw);
+    __shared__ uint64_t tma_bar;
+    constexpr bool cross = CrossOn<FT, TX, TY, TZ, VISC>::value;
+    // the TMA-staged layout starts at a 128-byte boundary (its size includes the slack)
+    unsigned char* sbase =
+        cross ? reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127))
+              : smem_raw;
+    uint32_t phase = 0;
+    bool abort = false;
+    if constexpr (cross) {
+        if (threadIdx.x == 0) tc::mbar_init(&tma_bar, 1);
+        __syncthreads();
+    }
     double local_dt = __longlong_as_double(0x7FF0000000000000LL);
     unsigned long long* cfl = boxes ? boxes[0].cfl_min : single.cfl_min;  // one target per stage
     if (sched == SCHED_GRID) {
-        rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, blockIdx.x, smem, local_dt);
+        rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, blockIdx.x, sbase, &tma_bar, phase, abort,
+                                       local_dt);
     } else if (sched == SCHED_STRIDE) {
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, smem, local_dt);
+        for (int t = blockIdx.x; t < ntiles && !abort; t += gridDim.x) {
+            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, sbase, &tma_bar, phase, abort,
+                                           local_dt);
             __syncthreads();
         }
     } else {
@@ -417,8 +649,9 @@ __global__ void __launch_bounds__(TX* TY* TZ)
             __syncthreads();
             const int t = next;
             __syncthreads();
-            if (t >= ntiles) break;
-            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, smem, local_dt);
+            if (t >= ntiles || abort) break;
+            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, sbase, &tma_bar, phase, abort,
+                                           local_dt);
             __syncthreads();
         }
         if (threadIdx.x == 0) {

@@ -20,3 +20,10 @@ REDISTRIBUTE = 2
 FLUX_FP32 = 4
 PER_BOX = 8
 GRAVITY = 16
+
+
+def set_tma_staging(on):
+    """Stage the FP32-flux form's tiles of depth >= 4 by TMA (the default) or with
+    plain loads, in stage tables built from now on (a test hook: both give the
+    same results)."""
+    load().ocfd_set_tma_staging(1 if on else 0)

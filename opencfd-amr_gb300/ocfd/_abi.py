@@ -84,6 +84,7 @@ _SIGS = {
     "ocfd_measure_ffma2_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "ocfd_check_rcp_f64": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.c_void_p]),
+    "ocfd_set_tma_staging": (None, [ctypes.c_int32]),
 }
 
 

@@ -1,13 +1,15 @@
 """Chemistry surrogate: data from the FP64 implicit substep, training on the
 tensor-core kernels, the guard, and evaluation against the FP64 substep.
 
-Data: 0D constant-volume trajectories (the operator the surrogate replaces is
-the constant-volume substep of EBR::chemical_advance,
-Source/CHEM/ChemAdvance.cpp:27-82) of H2/O2/N2 mixtures with T0 in
-[1000, 2500] K, equivalence ratio in [0.5, 2] and p0 in [0.8, 10] atm (the
-configured [1, 10] atm extended below 1 atm, where the reacting box lies), advanced by
-the FP64 substep with a per-trajectory step; at every snapshot each state takes
-one FP64 substep of a step drawn log-uniformly in [1e-9, 1e-6] s, and the pair
+Data: 0D ignition trajectories of H2/O2/N2 mixtures with T0 in [1000, 2500] K,
+equivalence ratio in [0.5, 2] and p0 in [0.8, 10] atm (the configured [1, 10]
+atm extended below 1 atm, where the reacting box lies), advanced by the FP64
+substep with a per-trajectory step, either at constant volume (the reactor of
+EBR::chemical_advance, Source/CHEM/ChemAdvance.cpp:27-82) or at constant
+pressure (each constant-volume step followed by the isobaric restoration of
+ocfd_chem_cells_isobaric: enthalpy kept, the cell brought back to p0).  At every
+snapshot each state takes one FP64 substep (the operator the surrogate
+replaces) of a step drawn log-uniformly in [1e-9, 1e-6] s, and the pair
 (T, p, Y, log10 dt) -> (dT, dY) is a training sample.  The lower end extends
 the configured [1e-8, 1e-6] s so that the substeps of the reacting box
 (dt / 8 = 1.25e-9 s) lie inside the training range.
@@ -44,11 +46,21 @@ SPECIES = ("H2", "O2", "H2O", "H", "O", "OH", "HO2", "H2O2", "N2")
 class Guard(ctypes.Structure):
     _fields_ = [("T_min", ctypes.c_double), ("T_max", ctypes.c_double), ("p_min", ctypes.c_double),
                 ("p_max", ctypes.c_double), ("dt_min", ctypes.c_double), ("dt_max", ctypes.c_double),
-                ("y_tol", ctypes.c_double), ("elem_tol", ctypes.c_double)]
+                ("y_tol", ctypes.c_double), ("elem_tol", ctypes.c_double),
+                ("dy_rel_max", ctypes.c_double), ("y_floor", ctypes.c_double)]
+
+    def with_dy_rel(self, dy_rel_max, y_floor=None):
+        """a copy with the per-output criterion set (0: off)"""
+        g = Guard.from_buffer_copy(self)
+        g.dy_rel_max = dy_rel_max
+        if y_floor is not None:
+            g.y_floor = y_floor
+        return g
 
 
 declare("ocfd_chem_cells_advance", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, ctypes.c_double, _vp])
 declare("ocfd_chem_cells_props", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, _vp])
+declare("ocfd_chem_cells_isobaric", ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, _vp])
 declare("ocfd_chem_cells_surrogate", ctypes.c_int, [_vp, _vp, ctypes.POINTER(Guard), ctypes.c_int64, _vp,
                                                     ctypes.c_double, ctypes.POINTER(ctypes.c_int64), _vp])
 declare("ocfd_react_set_surrogate", ctypes.c_int, [_vp, _vp, ctypes.POINTER(Guard)])
@@ -74,6 +86,13 @@ def cells_props(ctx, U):
     return out
 
 
+def cells_isobaric(ctx, U, p_target):
+    """bring every 0D cell of U (at rest) back to p_target (CUDA float64 [n]) at
+    its enthalpy e + p_target / rho"""
+    check(load().ocfd_chem_cells_isobaric(ctx.h, U.shape[1], U.data_ptr(), p_target.data_ptr(), _stream_ptr(None)),
+          "ocfd_chem_cells_isobaric")
+
+
 def cells_surrogate(ctx, net, guard, U, dt):
     fb = ctypes.c_int64()
     check(load().ocfd_chem_cells_surrogate(ctx.h, net.h, ctypes.byref(guard), U.shape[1], U.data_ptr(), dt,
@@ -95,13 +114,18 @@ def mixtures(rng, n, p_atm=(P_LO_ATM, 10.0)):
     return T, p, X
 
 
-def generate(ctx, n_traj=32768, n_snap=300, seed=20261203, dt_lo=1e-9, dt_hi=1e-6, log=None):
-    """Training samples (features [N x 12], targets [N x 10]) as CUDA float32."""
+def generate(ctx, n_traj=32768, n_snap=300, seed=20261203, dt_lo=1e-9, dt_hi=1e-6, mode="volume", log=None):
+    """Training samples (features [N x 12], targets [N x 10]) as CUDA float32,
+    from constant-volume (mode "volume") or constant-pressure ("pressure")
+    ignition trajectories."""
+    if mode not in ("volume", "pressure"):
+        raise ValueError("mode must be 'volume' or 'pressure'")
     import torch
     from .react import state_tpx
     rng = np.random.default_rng(seed)
     T, p, X = mixtures(rng, n_traj)
     U = torch.as_tensor(state_tpx(ctx, T, p, X), device="cuda").contiguous()
+    p0 = torch.as_tensor(p, dtype=torch.float64, device="cuda").contiguous()
     gen = torch.Generator(device="cuda")
     gen.manual_seed(seed)
     # per-trajectory integration step, log-uniform in [1e-8, 1e-7] s
@@ -125,6 +149,8 @@ def generate(ctx, n_traj=32768, n_snap=300, seed=20261203, dt_lo=1e-9, dt_hi=1e-
         # step (Source/EBR.cpp:333-357)
         r = U[5:].clamp_min(0.0)
         U[5:] = r * (U[0] / r.sum(0))
+        if mode == "pressure":
+            cells_isobaric(ctx, U, p0)
     Xs = torch.cat(feats, 0)
     Ts = torch.cat(targs, 0)
     # keep states inside the NASA-7 fit range (250-3500 K) before and after the
@@ -218,7 +244,8 @@ def train(ctx, X, T, epochs=12, batch=8192, lr=2e-3, seed=1, val_frac=0.02, rate
     elem_tol = float(torch.quantile(elem_err.float(), 0.99))
     guard = Guard(T_min=float(Xraw[tr, 0].min()), T_max=float(Xraw[tr, 0].max()), p_min=float(Xraw[tr, 1].min()),
                   p_max=float(Xraw[tr, 1].max()), dt_min=float(10 ** Xraw[tr, 11].min()),
-                  dt_max=float(10 ** Xraw[tr, 11].max()), y_tol=1e-3, elem_tol=elem_tol)
+                  dt_max=float(10 ** Xraw[tr, 11].max()), y_tol=1e-3, elem_tol=elem_tol,
+                  dy_rel_max=0.0, y_floor=1e-6)
     rel = lambda k: float(((Yv[:, k] - Tv[:, k]).abs().mean() / Tv[:, k].abs().mean()))
     report = {"samples": int(n), "train_samples": int(tr.numel()), "val_samples": int(nval), "epochs": epochs,
               "batch": batch, "train_seconds": train_s, "final_train_loss": losses[-1], "val_loss": val_loss,

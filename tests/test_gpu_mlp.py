@@ -115,3 +115,29 @@ def test_mlp_learns_smooth_map(ctx):
         loss, _, _ = net.train_step(Xd[s:s + 1024], Td[s:s + 1024], lr=2e-3)
         first = loss if first is None else first
     assert loss < first / 10, (first, loss)
+
+
+def test_mlp_forward_throughput(ctx):
+    """Rate of the network on the tensor cores: 2^20 rows through the five
+    layers (2 (12 128 + 3 128^2 + 128 10) = 103,936 FLOP per row with the first
+    layer's K padded to 16), the training forward with its stash of Z and H,
+    timed with CUDA events after a warm-up.  The figure is printed; the bound
+    only catches a broken pipeline."""
+    import torch
+    M = 1 << 20
+    net = make_mlp(ctx, max_batch=M, seed=7)
+    X = torch.randn((M, 12), dtype=torch.float32, device="cuda")
+    Y = net.forward(X)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record()
+    for _ in range(reps):
+        Y = net.forward(X)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    tflops = 103936.0 * M / (ms * 1e-3) / 1e12
+    print("mlp forward: %.3f ms per 2^20 rows, %.1f TFLOP/s" % (ms, tflops))
+    assert torch.isfinite(Y).all()
+    assert tflops > 5.0

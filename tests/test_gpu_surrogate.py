@@ -136,3 +136,94 @@ def test_reacting_level_with_surrogate(ctx, trained):
     props = lambda U: surrogate.cells_props(ctx, torch.as_tensor(U.reshape(14, -1), device="cuda").contiguous())
     Ta, Tb = props(a)[0], props(b)[0]
     assert float((Tb - Ta).abs().sum() / Ta.abs().sum()) < 5e-3
+
+
+def _advanced_states(ctx, n, seed, steps=40):
+    """0D H2/air states advanced at constant volume for steps x 10 ns (radicals
+    present), inside the tables' 250-3500 K"""
+    import torch
+    from ocfd import surrogate
+    from ocfd.react import state_tpx
+    rng = np.random.default_rng(seed)
+    Tm, p, X = surrogate.mixtures(rng, n)
+    U = torch.as_tensor(state_tpx(ctx, Tm, p, X), device="cuda").contiguous()
+    for _ in range(steps):
+        surrogate.cells_advance(ctx, U, dt=1e-8)
+    T0 = surrogate.cells_props(ctx, U)[0]
+    keep = torch.isfinite(U).all(0) & (T0 >= 250.0) & (T0 <= 3500.0)
+    return U[:, keep].contiguous()
+
+
+def test_isobaric_restoration(ctx):
+    """After a constant-volume substep the isobaric restoration brings each cell
+    back to its pressure at the enthalpy e + p0 / rho (rho before the
+    restoration), keeps the mass fractions, and leaves a cell already at p0
+    unchanged."""
+    import torch
+    from ocfd import surrogate
+    U = _advanced_states(ctx, 4096, seed=11, steps=5)
+    n = U.shape[1]
+    p0 = surrogate.cells_props(ctx, U)[1].contiguous()
+    # a cell already at its pressure: unchanged
+    V = U.clone()
+    surrogate.cells_isobaric(ctx, V, p0)
+    assert float(((V - U).abs().amax(1) / U.abs().amax(1).clamp_min(1e-300)).max()) < 1e-9
+    # one constant-volume substep raises p in the igniting cells; restore
+    surrogate.cells_advance(ctx, U, dt=1e-7)
+    pr = surrogate.cells_props(ctx, U)
+    h_target = U[4] / U[0] + p0 / U[0]
+    W = U.clone()
+    surrogate.cells_isobaric(ctx, W, p0)
+    pw = surrogate.cells_props(ctx, W)
+    assert float(((pr[1] - p0).abs() / p0).max()) > 1e-3      # the substep moved p
+    assert float(((pw[1] - p0).abs() / p0).max()) < 1e-9
+    h = W[4] / W[0] + pw[1] / W[0]
+    assert float(((h - h_target).abs() / h_target.abs().clamp_min(1e3)).max()) < 1e-9
+    assert float((pw[2:] - pr[2:]).abs().max()) < 1e-12
+    assert torch.equal(W[1:4], torch.zeros_like(W[1:4]))
+    assert n > 4000
+
+
+def test_constant_pressure_generator(ctx):
+    """mode="pressure" samples every snapshot of a trajectory at its initial
+    pressure"""
+    import torch
+    from ocfd import surrogate
+    n_traj, n_snap = 512, 6
+    X, T = surrogate.generate(ctx, n_traj=n_traj, n_snap=n_snap, seed=3, mode="pressure")
+    assert X.shape[0] == n_traj * n_snap
+    _, p0, _ = surrogate.mixtures(np.random.default_rng(3), n_traj)
+    p = X[:, 1].double().cpu().numpy().reshape(n_snap, n_traj)
+    assert np.abs(p / p0[None] - 1.0).max() < 1e-6          # float32 features
+    # the trajectories evolved: some cells ignite (T rises at constant p)
+    Tf = X[:, 0].double().cpu().numpy().reshape(n_snap, n_traj)
+    assert (Tf[-1] - Tf[0]).max() > 10.0
+    with pytest.raises(ValueError):
+        surrogate.generate(ctx, n_traj=8, n_snap=1, mode="enthalpy")
+
+
+def test_per_output_guard_is_monotone(ctx, trained):
+    """Tightening the per-output criterion sends a growing share of cells to the
+    FP64 substep and brings the species error down toward it."""
+    import torch
+    from ocfd import surrogate
+    _, _, sur, _ = trained
+    U0 = _advanced_states(ctx, 1 << 18, seed=21)
+    dt = 1.25e-9
+    ref = U0.clone()
+    surrogate.cells_advance(ctx, ref, dt=dt)
+    pr = surrogate.cells_props(ctx, ref)
+    fbs, errs = [], []
+    for d in (0.0, 1.0, 0.1, 0.01, 0.001):
+        g = sur.guard.with_dy_rel(d)
+        b = U0.clone()
+        fbs.append(surrogate.cells_surrogate(ctx, sur.net, g, b, dt))
+        pb = surrogate.cells_props(ctx, b)
+        errs.append(float((pb[2 + 5] - pr[2 + 5]).abs().sum() / pr[2 + 5].abs().sum()))
+    assert all(a <= b for a, b in zip(fbs, fbs[1:])), fbs
+    assert fbs[-1] > fbs[0]
+    assert errs[-1] <= errs[0] + 1e-12, errs
+    # the struct passed through the C ABI carries the two new fields
+    g = sur.guard.with_dy_rel(0.5, 1e-5)
+    h = surrogate.Guard.from_buffer_copy(g)
+    assert (h.dy_rel_max, h.y_floor, h.elem_tol) == (0.5, 1e-5, sur.guard.elem_tol)
