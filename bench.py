@@ -782,6 +782,7 @@ def run_ours_amr(args, world, rank, local):
                        "l1_vs_other_form": l1err,
                        "forms_cell_steps_per_s": {args.form: value, ("fp64" if flags else "fp32"): value_other},
                        "speedup_fp32_over_fp64": (value / value_other) if flags else (value_other / value),
+                       "regular_kernel_ms_per_tile_shape": tile_ms,
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -1164,6 +1165,18 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         l1err = matched_l1(ctx, c, boxes, flags)
 
+    # the regular tile kernel of one stage for every tile shape (the pencil
+    # shapes 0-5, and in the FP32-flux form the TMA-staged shapes 6-8), one-CTA-
+    # per-tile schedule (last: it leaves the level on the last shape)
+    from ocfd._abi import OcfdError
+    tile_ms = {}
+    for t in range(9):
+        try:
+            lev.set_schedule(t, 0)
+            tile_ms[str(t)] = lev.profile_regular(flags, reps=10)[0]
+        except OcfdError:
+            tile_ms[str(t)] = None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu_steps = 2
@@ -1181,6 +1194,7 @@ def run_ours(args, world, rank, local):
                        "l1_vs_other_form": l1err,
                        "forms_cell_steps_per_s": {args.form: value, ("fp64" if flags else "fp32"): value_other},
                        "speedup_fp32_over_fp64": (value / value_other) if flags else (value_other / value),
+                       "regular_kernel_ms_per_tile_shape": tile_ms,
                        "l2": "flushed between timed steps (512 MB write, untimed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

@@ -48,6 +48,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "level.h"
@@ -918,18 +919,20 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
                 plane_box[fb * 6 + 2 * d + sd] = pl;
                 fe += ib_cells(pl) * H->ncomp;
             }
-    // ---- reflux faces grouped by uncovered coarse cell
+    // ---- reflux faces grouped by uncovered coarse cell.  The coarse cells just
+    // outside each fine box (one plane per side, periodic planes wrapped into
+    // the domain) minus the coarsened fine boxes: rectangles, not cells, are
+    // tested for cover.  A coarse cell gathers its faces in discovery order
+    // (fine box, direction, side), the summation order of its reflux; the
+    // cells themselves are independent, so they are kept in first-discovery
+    // order.
     struct Face {
         int d, side, cb, fb;
         int cf[3];  // coarse face index
         int c[3];   // unwrapped coarse cell (transverse coordinates pick the fine faces)
     };
-    struct Keyed {
-        int cb;
-        long long u;  // coarse cell: box and element index
-        Face f;
-    };
-    std::vector<Keyed> faces_k;
+    std::vector<Face> faces;
+    std::vector<long long> face_u;
     const IBox& cd = C.dom;
     for (int fb = 0; fb < nfb; ++fb) {
         const IBox& Fc = fcoarse[fb];
@@ -937,52 +940,75 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
             for (int sd = 0; sd < 2; ++sd) {
                 IBox pl = Fc;
                 pl.lo[d] = pl.hi[d] = (sd == 0) ? Fc.lo[d] - 1 : Fc.hi[d] + 1;
-                if (!H->periodic[d] && (pl.lo[d] < cd.lo[d] || pl.lo[d] > cd.hi[d])) continue;  // physical boundary
-                for (int k = pl.lo[2]; k <= pl.hi[2]; ++k)
-                    for (int j = pl.lo[1]; j <= pl.hi[1]; ++j)
-                        for (int i = pl.lo[0]; i <= pl.hi[0]; ++i) {
-                            int c[3] = {i, j, k}, w[3] = {i, j, k};
-                            bool inside = true;
-                            for (int e = 0; e < 3; ++e) {
-                                const int per = cd.hi[e] - cd.lo[e] + 1;
-                                if (w[e] < cd.lo[e] || w[e] > cd.hi[e]) {
-                                    if (!H->periodic[e]) inside = false;
-                                    else w[e] = cd.lo[e] + (((w[e] - cd.lo[e]) % per) + per) % per;
-                                }
+                const int per = cd.hi[d] - cd.lo[d] + 1;
+                IBox wp = pl;  // the plane in the domain (transverse extents lie in Fc, inside it)
+                if (pl.lo[d] < cd.lo[d] || pl.lo[d] > cd.hi[d]) {
+                    if (!H->periodic[d]) continue;  // physical boundary
+                    wp.lo[d] = wp.hi[d] = cd.lo[d] + (((pl.lo[d] - cd.lo[d]) % per) + per) % per;
+                }
+                std::vector<IBox> open{wp};
+                for (int ob : fcidx.query(wp)) list_subtract(open, fcoarse[ob]);
+                for (const IBox& r : open)
+                    for (int k = r.lo[2]; k <= r.hi[2]; ++k)
+                        for (int j = r.lo[1]; j <= r.hi[1]; ++j)
+                            for (int i = r.lo[0]; i <= r.hi[0]; ++i) {
+                                int w[3] = {i, j, k};
+                                const int cb = cidx.find(w);
+                                if (cb < 0) return fail(OCFD_BAD_ARG, "AMR: reflux cell outside the coarse level");
+                                Face fc{};
+                                fc.d = d;
+                                fc.side = sd;
+                                fc.cb = cb;
+                                fc.fb = fb;
+                                for (int e = 0; e < 3; ++e) { fc.cf[e] = w[e]; fc.c[e] = w[e]; }
+                                fc.c[d] = pl.lo[d];
+                                if (sd == 0) fc.cf[d] = w[d] + 1;
+                                faces.push_back(fc);
+                                face_u.push_back(fab_index_h(C.L->fabs[cb], w[0], w[1], w[2]));
                             }
-                            if (!inside) continue;
-                            if (fcidx.find(w) >= 0) continue;  // covered: fine-fine face
-                            const int cb = cidx.find(w);
-                            if (cb < 0) return fail(OCFD_BAD_ARG, "AMR: reflux cell outside the coarse level");
-                            Face fc{};
-                            fc.d = d;
-                            fc.side = sd;
-                            fc.cb = cb;
-                            fc.fb = fb;
-                            for (int e = 0; e < 3; ++e) { fc.cf[e] = w[e]; fc.c[e] = c[e]; }
-                            if (sd == 0) fc.cf[d] = w[d] + 1;
-                            faces_k.push_back({cb, fab_index_h(C.L->fabs[cb], w[0], w[1], w[2]), fc});
-                        }
             }
     }
     pt.mark("      reflux scan", 0);
-    // coarse register: face arrays of the coarse boxes that own a reflux cell
-    // group by coarse cell, faces of a cell in discovery order
-    std::stable_sort(faces_k.begin(), faces_k.end(), [](const Keyed& x, const Keyed& y) {
-        return x.cb != y.cb ? x.cb < y.cb : x.u < y.u;
-    });
+    // group the faces by coarse cell (an element index of the level's state is
+    // unique across its boxes), keeping discovery order within a group
+    std::vector<int> gid(faces.size());
+    std::vector<int> gfirst;  // first face of each group
+    {
+        std::unordered_map<long long, int> group;
+        group.reserve(faces.size() * 2);
+        for (size_t q = 0; q < faces.size(); ++q) {
+            auto it = group.emplace(face_u[q], (int)gfirst.size());
+            if (it.second) gfirst.push_back((int)q);
+            gid[q] = it.first->second;
+        }
+    }
+    const int ngroup = (int)gfirst.size();
+    std::vector<int> gstart((size_t)ngroup + 1, 0), order(faces.size());
+    for (int g : gid) ++gstart[(size_t)g + 1];
+    for (int g = 0; g < ngroup; ++g) gstart[(size_t)g + 1] += gstart[g];
+    {
+        std::vector<int> fill(gstart.begin(), gstart.end() - 1);
+        for (size_t q = 0; q < faces.size(); ++q) order[(size_t)fill[gid[q]]++] = (int)q;
+    }
+    // coarse register: face arrays of the coarse boxes that own a reflux cell,
+    // in box order
     std::vector<long long> creg_off((size_t)ncb, -1);
     long long ce = 0;
-    for (const Keyed& kf : faces_k) {
-        const int cb = kf.cb;
-        if (creg_off[cb] >= 0) continue;
-        creg_off[cb] = ce;
-        const IBox& B = C.boxes[cb];
-        for (int d = 0; d < 3; ++d) {
-            IBox fa = B;
-            fa.hi[d] += 1;
-            ce += ib_cells(fa) * H->ncomp;
+    {
+        std::vector<char> owns((size_t)ncb, 0);
+        for (const Face& fc : faces) owns[fc.cb] = 1;
+        long long ce0 = 0;
+        for (int cb = 0; cb < ncb; ++cb) {
+            if (!owns[cb]) continue;
+            creg_off[cb] = ce0;
+            const IBox& B = C.boxes[cb];
+            for (int d = 0; d < 3; ++d) {
+                IBox fa = B;
+                fa.hi[d] += 1;
+                ce0 += ib_cells(fa) * H->ncomp;
+            }
         }
+        ce = ce0;
     }
     auto creg_face = [&](int cb, int d, const int* fc, long long* cns) {
         const IBox& B = C.boxes[cb];
@@ -999,27 +1025,25 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     };
     std::vector<RefluxCell> rc_h;
     std::vector<RefluxFace> rf_h;
-    for (size_t q0 = 0; q0 < faces_k.size();) {
-        size_t q1 = q0;
-        while (q1 < faces_k.size() && faces_k[q1].cb == faces_k[q0].cb && faces_k[q1].u == faces_k[q0].u) ++q1;
-        const EbRef ce = eb_ref(C.L, faces_k[q0].cb);
-        if (ce.kind == OCFD_BOX_COVERED) {  // covered coarse cells take no reflux
-            q0 = q1;
-            continue;
-        }
+    rc_h.reserve(ngroup);
+    rf_h.reserve(faces.size());
+    for (int g = 0; g < ngroup; ++g) {
+        const int q0 = gstart[g], q1 = gstart[(size_t)g + 1];
+        const Face& f0 = faces[order[q0]];
+        const EbRef ceb = eb_ref(C.L, f0.cb);
+        if (ceb.kind == OCFD_BOX_COVERED) continue;  // covered coarse cells take no reflux
         RefluxCell cell{};
-        cell.u = faces_k[q0].u;
-        cell.uns = C.L->fabs[faces_k[q0].cb].ns;
-        if (ce.kind == OCFD_BOX_CUT) {
-            const Face& f0 = faces_k[q0].f;
+        cell.u = face_u[order[q0]];
+        cell.uns = C.L->fabs[f0.cb].ns;
+        if (ceb.kind == OCFD_BOX_CUT) {
             int w[3] = {f0.cf[0], f0.cf[1], f0.cf[2]};
             if (f0.side == 0) w[f0.d] -= 1;
-            cell.vf = ce.vf + (w[0] - ce.x0) + (long long)(w[1] - ce.y0) * ce.gx;
+            cell.vf = ceb.vf + (w[0] - ceb.x0) + (long long)(w[1] - ceb.y0) * ceb.gx;
         }
         cell.first = (int)rf_h.size();
-        cell.count = (int)(q1 - q0);
-        for (size_t qi = q0; qi < q1; ++qi) {
-            const Face& fc = faces_k[qi].f;
+        cell.count = q1 - q0;
+        for (int qi = q0; qi < q1; ++qi) {
+            const Face& fc = faces[order[qi]];
             RefluxFace q{};
             q.d = fc.d;
             q.sgn = fc.side == 0 ? 1.0 : -1.0;
@@ -1031,16 +1055,15 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
             int m = 0;
             for (int b2 = 0; b2 < 2; ++b2)
                 for (int b1 = 0; b1 < 2; ++b1) {
-                    int g[3];
-                    g[fc.d] = pl.lo[fc.d];
-                    g[t1] = 2 * fc.c[t1] + b1;
-                    g[t2] = 2 * fc.c[t2] + b2;
-                    q.f[m++] = plane_off[pidx] + region_offset_plane(pl, g[0], g[1], g[2]);
+                    int gg[3];
+                    gg[fc.d] = pl.lo[fc.d];
+                    gg[t1] = 2 * fc.c[t1] + b1;
+                    gg[t2] = 2 * fc.c[t2] + b2;
+                    q.f[m++] = plane_off[pidx] + region_offset_plane(pl, gg[0], gg[1], gg[2]);
                 }
             rf_h.push_back(q);
         }
         rc_h.push_back(cell);
-        q0 = q1;
     }
     pt.mark("      reflux tables", 0);
     F.nrc = (int)rc_h.size();
@@ -1811,6 +1834,7 @@ static ocfd_status ensure_graph(ocfd_amr* H, unsigned flags) {
         cudaGraphExecDestroy(H->graph);
         H->graph = nullptr;
     }
+    PhaseTimer pt;
     cudaStream_t cap;
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return check_launch("capture stream");
     cudaGraph_t g;
@@ -1828,6 +1852,7 @@ static ocfd_status ensure_graph(ocfd_amr* H, unsigned flags) {
     if (e != cudaSuccess) return fail(OCFD_LAUNCH_FAIL, std::string("AMR graph instantiate: ") + cudaGetErrorString(e));
     H->graph_flags = flags;
     H->graph_ok = true;
+    pt.mark("graph capture", 0);
     return OCFD_OK;
 }
 

@@ -390,14 +390,15 @@ __device__ __forceinline__ float sur_temperature(const SurThermo& th, const floa
 }
 
 // One chemistry substep by the network for the cells of a list, 128 cells per
-// tile (thread = cell): inputs (T, p, Y, log10 dt) -> rates of T and Y (the
-// increments over the substep divided by dt).
+// tile (thread t < 128 of the first warpgroup = cell t of the tile; all MLP_G
+// warpgroups share the network's epilogues): inputs (T, p, Y, log10 dt) ->
+// rates of T and Y (the increments over the substep divided by dt).
 // Cells whose inputs leave the training range, or whose increments break the
 // species bounds or the H / O / N element balance beyond the guard's
 // tolerances, are appended to the fallback list for the FP64 substep.
 // Accepted cells update rho Y_n (clipped at 0) and rho E as the FP64 substep
 // does (ChemAdvance.cpp:62-80).
-__global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long long* __restrict__ off,
+__global__ void __launch_bounds__(128 * MLP_G) k_chem_surrogate(MlpNet net, const long long* __restrict__ off,
                                                         const long long* __restrict__ stride, long long ncell,
                                                         double* Ubuf, double dt, DevParm P, ocfd_surrogate_guard g,
                                                         long long* fb_off, long long* fb_stride, unsigned* fb_count,
@@ -429,7 +430,7 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
     const float dy_rel = (float)g.dy_rel_max, y_floor = (float)g.y_floor;
     for (long long t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
         const long long c = t * 128 + tid;
-        const bool valid = c < ncell;
+        const bool valid = tid < 128 && c < ncell;
         double* x = nullptr;
         long long ns = 0;
         double rho = 1.0, r[NSP];
@@ -461,11 +462,13 @@ __global__ void __launch_bounds__(128) k_chem_surrogate(MlpNet net, const long l
 #pragma unroll
         for (int n = 0; n < NSP; ++n) f[2 + n] = (sqrtf(fmaxf(Y[n], 0.0f)) - net.in_mu[2 + n]) * net.in_isd[2 + n];
         f[11] = (ldt - net.in_mu[11]) * net.in_isd[11];
+        if (tid < 128) {
 #pragma unroll
-        for (int k = 0; k < 16; ++k)
-            *reinterpret_cast<uint16_t*>(sm + S_A0 + kmajor_offset(tid, k, 128)) = k < MLP_IN ? bf16_bits(f[k]) : 0;
+            for (int k = 0; k < 16; ++k)
+                *reinterpret_cast<uint16_t*>(sm + S_A0 + kmajor_offset(tid, k, 128)) = k < MLP_IN ? bf16_bits(f[k]) : 0;
+        }
         float out[16];
-        ok = mlp_tile(sm, tbase, bar, phase, out, nullptr, nullptr, 0);
+        ok = mlp_tile<MLP_G>(sm, tbase, bar, phase, out, nullptr, nullptr, 0);
         if (!ok || !valid) continue;
         float dY[NSP];
 #pragma unroll
@@ -565,7 +568,7 @@ ocfd_status launch_chem_surrogate(const ocfd_mlp* mlp, const long long* off, con
     }
     if (ncell <= 0) return OCFD_OK;
     const long long ntile = (ncell + 127) / 128;
-    k_chem_surrogate<<<(unsigned)std::min<long long>(ntile, sms), 128, S_SUR_TOT, st>>>(
+    k_chem_surrogate<<<(unsigned)std::min<long long>(ntile, sms), 128 * MLP_G, S_SUR_TOT, st>>>(
         mlp_net(mlp), off, stride, ncell, U, dt, P, g, fb_off, fb_stride, fb_count, fb_total, err);
     return check_launch("surrogate chemistry substep");
 }

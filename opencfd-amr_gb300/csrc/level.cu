@@ -399,6 +399,7 @@ ocfd_status level_autotune(ocfd_level* L, unsigned flags, int reps, cudaStream_t
     ocfd_status s = OCFD_OK;
     for (int t = 0; t < kNumRegularTiles && s == OCFD_OK; ++t) {
         if (!regular_tile_fits(t, visc)) continue;
+        if (kRegularTiles[t].staged && (!f32 || visc)) continue;  // the pencil kernel again
         L->tile = t;
         s = build_stage_tables(L, roles);
         for (int sc = 0; sc < NUM_SCHED && s == OCFD_OK; ++sc) {
@@ -690,7 +691,7 @@ ocfd_status level_alloc(ocfd_context* ctx, const ocfd_level_desc* desc, int nbuf
     } else {
         double best = 1e300;
         for (int t = 0; t < kNumRegularTiles; ++t) {
-            if (!regular_tile_fits(t, true)) continue;
+            if (!regular_tile_fits(t, true) || kRegularTiles[t].staged) continue;
             const TileShape& ts = kRegularTiles[t];
             double cost = 0;
             for (const ocfd_box& B : L->boxes) {

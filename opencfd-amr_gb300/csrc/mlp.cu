@@ -66,9 +66,10 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const uint16_t* __restrict__ A,
 }
 
 // Training forward: X [M x 16] BF16 normalised inputs (row-major) -> Y [M x 16]
-// FP32, stashing Z_l, H_l (l = 1..4) as [4][M/128][128 x 128] blocks.
-__global__ void __launch_bounds__(128) k_mlp_forward(MlpNet net, const uint16_t* __restrict__ X, float* Y,
-                                                     float* Z, uint16_t* H, int ntile, unsigned* err) {
+// FP32, stashing Z_l, H_l (l = 1..4) as [4][M/128][128 x 128] blocks; MLP_G
+// warpgroups per 128-row tile (the first stages the inputs and writes Y).
+__global__ void __launch_bounds__(128 * MLP_G) k_mlp_forward(MlpNet net, const uint16_t* __restrict__ X, float* Y,
+                                                             float* Z, uint16_t* H, int ntile, unsigned* err) {
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S_BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S_BAR + 8);
@@ -87,14 +88,17 @@ __global__ void __launch_bounds__(128) k_mlp_forward(MlpNet net, const uint16_t*
     bool ok = true;
     for (int t = blockIdx.x; t < ntile && ok; t += gridDim.x) {
         const long long row = (long long)t * 128 + tid;
-#pragma unroll
-        for (int k = 0; k < 16; ++k)
-            *reinterpret_cast<uint16_t*>(sm + S_A0 + kmajor_offset(tid, k, 128)) = X[row * 16 + k];
+        if (tid < 128) {
+            // one row of 16 BF16 inputs: two 16-byte core-matrix rows
+            const uint4* xr = reinterpret_cast<const uint4*>(X + row * 16);
+            *reinterpret_cast<uint4*>(sm + S_A0 + kmajor_offset(tid, 0, 128)) = xr[0];
+            *reinterpret_cast<uint4*>(sm + S_A0 + kmajor_offset(tid, 8, 128)) = xr[1];
+        }
         float out[16];
         // stash layout: block t of layer l at ((l * ntile + t) * 128 + row) * 128
-        ok = mlp_tile(sm, tbase, bar, phase, out, Z ? Z + (long long)t * 128 * 128 : nullptr,
-                      H ? H + (long long)t * 128 * 128 : nullptr, (long long)ntile * 128);
-        if (ok)
+        ok = mlp_tile<MLP_G>(sm, tbase, bar, phase, out, Z ? Z + (long long)t * 128 * 128 : nullptr,
+                             H ? H + (long long)t * 128 * 128 : nullptr, (long long)ntile * 128);
+        if (ok && tid < 128)
 #pragma unroll
             for (int i = 0; i < 16; ++i) Y[row * 16 + i] = out[i];
     }
@@ -380,7 +384,8 @@ static ocfd_status mlp_forward(ocfd_mlp* n, const float* X, long long M, cudaStr
     const int sms = n->ctx->num_sms;
     k_mlp_pack<<<grid_for(M * 16, 256, sms), 256, 0, st>>>(X, n->Xb, M);
     const int ntile = (int)(M / 128);
-    k_mlp_forward<<<std::min(ntile, sms), 128, S_TOT, st>>>(net_of(n), n->Xb, n->Y, n->Z, n->H, ntile, n->ctx->d_error);
+    k_mlp_forward<<<std::min(ntile, sms), 128 * MLP_G, S_TOT, st>>>(net_of(n), n->Xb, n->Y, n->Z, n->H, ntile,
+                                                                    n->ctx->d_error);
     return check_launch("MLP forward");
 }
 

@@ -74,15 +74,27 @@ __device__ __forceinline__ void mlp_stage_weights(const MlpNet& net, unsigned ch
     for (int e = threadIdx.x; e < BTOT; e += blockDim.x) sb[e] = net.b[e];
 }
 
+// warpgroups (of 128 threads) that share one 128-row tile: the bias + GELU
+// epilogue of a hidden layer (128 columns per row, erf and BF16 packing per
+// element) takes far longer than the layer's MMAs, so it is split over MLP_G
+// warpgroups by columns
+constexpr int MLP_G = 4;
+
 // one 128-row tile through the five layers; the input operand (S_A0) is staged.
-// Thread t owns row t.  Hidden activations go to `zs` / `hs` (FP32
-// pre-activations, BF16 activations; may be null) and the 16 outputs to out[].
-// Returns false when an MMA completion wait ran out.
+// The CTA has 128 G threads: thread t serves row t % 128 (warp w reads TMEM
+// lanes 32 (w % 4) .. 32 (w % 4) + 31) and columns [(t / 128) 128 / G,
+// (t / 128 + 1) 128 / G) of every hidden layer; the output layer's 16 columns go
+// to the first warpgroup (out[]).  Hidden activations go to `zs` / `hs` (FP32
+// pre-activations, BF16 activations; may be null).  Returns false when an MMA
+// completion wait ran out.
+template <int G>
 __device__ __forceinline__ bool mlp_tile(unsigned char* sm, uint32_t tbase, uint64_t* bar, uint32_t& phase,
                                          float* out, float* zs, uint16_t* hs, long long ld) {
-    const int tid = threadIdx.x, warp = tid >> 5;
+    static_assert(G == 1 || G == 2 || G == 4, "warpgroups per tile");
+    constexpr int CW = MLP_H / G;
+    const int tid = threadIdx.x, row = tid & 127, cg = tid >> 7;
     const float* sb = reinterpret_cast<const float*>(sm + S_B);
-    const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
+    const uint32_t trow = tbase + ((uint32_t)(((tid >> 5) & 3) * 32) << 16);
     for (int l = 0; l < 5; ++l) {
         fence_async_smem();
         fence_before_sync();
@@ -102,21 +114,32 @@ __device__ __forceinline__ bool mlp_tile(unsigned char* sm, uint32_t tbase, uint
         fence_after_sync();
         if (!ok) return false;
         if (l < 4) {
-            // bias + GELU, BF16 into the hidden operand (row tid)
-            for (int c0 = 0; c0 < MLP_H; c0 += 32) {
+            // bias + GELU, BF16 into the hidden operand: 8 consecutive columns of a
+            // row are one 16-byte core-matrix row, stored at once
+            for (int c0 = cg * CW; c0 < (cg + 1) * CW; c0 += 32) {
                 float v[32];
                 tmem_ld32(trow + (uint32_t)c0, v);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float z = v[i] + sb[BOFF(l) + c0 + i];
-                    const float h = gelu(z);
-                    const uint16_t hb = bf16_bits(h);
-                    *reinterpret_cast<uint16_t*>(sm + S_H + kmajor_offset(tid, c0 + i, 128)) = hb;
-                    if (zs) zs[(long long)l * 128 * ld + (long long)tid * 128 + c0 + i] = z;
-                    if (hs) hs[(long long)l * 128 * ld + (long long)tid * 128 + c0 + i] = hb;
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t pk[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int i = q * 8 + e * 2;
+                        const float z0 = v[i] + sb[BOFF(l) + c0 + i], z1 = v[i + 1] + sb[BOFF(l) + c0 + i + 1];
+                        pk[e] = (uint32_t)bf16_bits(gelu(z0)) | ((uint32_t)bf16_bits(gelu(z1)) << 16);
+                        if (zs) {
+                            float* zr = zs + (long long)l * 128 * ld + (long long)row * 128 + c0 + i;
+                            zr[0] = z0;
+                            zr[1] = z1;
+                        }
+                    }
+                    const uint4 w = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    *reinterpret_cast<uint4*>(sm + S_H + kmajor_offset(row, c0 + q * 8, 128)) = w;
+                    if (hs)
+                        *reinterpret_cast<uint4*>(hs + (long long)l * 128 * ld + (long long)row * 128 + c0 + q * 8) = w;
                 }
             }
-        } else {
+        } else if (cg == 0) {
             float v[16];
             tmem_ld16(trow, v);
 #pragma unroll

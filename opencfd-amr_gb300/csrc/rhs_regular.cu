@@ -16,7 +16,8 @@ ocfd_status configure_rhs_regular() { return configure_all<double>(); }
 
 bool regular_tile_fits(int tile, bool visc) { return tile_fits<double>(tile, visc); }
 
-const TileShape kRegularTiles[] = {{8, 8, 8}, {8, 8, 4}, {16, 8, 4}, {16, 16, 2}, {32, 8, 2}, {16, 8, 2}};
+const TileShape kRegularTiles[] = {{8, 8, 8, 0},  {8, 8, 4, 0}, {16, 8, 4, 0}, {16, 16, 2, 0}, {32, 8, 2, 0},
+                                   {16, 8, 2, 0}, {8, 8, 8, 1}, {8, 8, 4, 1}, {16, 8, 4, 1}};
 const int kNumRegularTiles = sizeof(kRegularTiles) / sizeof(kRegularTiles[0]);
 
 ocfd_status launch_rhs_regular(int tile, bool visc, const RegBoxArgs* d_boxes,
@@ -30,7 +31,7 @@ int pick_regular_tile(const int n[3], bool visc) {
     int best = 1;
     double best_cost = 1e300;
     for (int t = 0; t < kNumRegularTiles; ++t) {
-        if (!regular_tile_fits(t, visc)) continue;
+        if (!regular_tile_fits(t, visc) || kRegularTiles[t].staged) continue;
         const TileShape& s = kRegularTiles[t];
         long long tiles = (long long)((n[0] + s.x - 1) / s.x) * ((n[1] + s.y - 1) / s.y) *
                           ((n[2] + s.z - 1) / s.z);
@@ -69,6 +70,15 @@ void fill_regular_args(RegBoxArgs& a, const ocfd_array4* S, const ocfd_array4* d
     encode_regular_tmaps(a, S, tile);
 }
 
+int staged_regular_tile(int tile) {
+    const TileShape& s = kRegularTiles[tile];
+    for (int t = 0; t < kNumRegularTiles; ++t)
+        if (kRegularTiles[t].staged && kRegularTiles[t].x == s.x && kRegularTiles[t].y == s.y &&
+            kRegularTiles[t].z == s.z)
+            return t;
+    return tile;
+}
+
 static bool g_regular_tma = true;
 
 void set_regular_tma(bool on) { g_regular_tma = on; }
@@ -100,7 +110,7 @@ bool encode_regular_tmaps(RegBoxArgs& a, const ocfd_array4* S, int tile) {
     a.use_tma = 0;
     if (!g_regular_tma || !S || tile < 0 || tile >= kNumRegularTiles) return false;
     const TileShape& t = kRegularTiles[tile];
-    if (t.z < 4 || t.x % 2 != 0 || S->ncomp < 5) return false;
+    if (!t.staged || t.z < 4 || t.x % 2 != 0 || S->ncomp < 5) return false;
     const uintptr_t base = reinterpret_cast<uintptr_t>(S->p);
     if (base % 16 != 0 || S->jstride % 2 != 0 || S->kstride % 2 != 0 || S->nstride % 2 != 0) return false;
     if (((a.lo[0] - S->begin[0]) & 1) != 0) return false;

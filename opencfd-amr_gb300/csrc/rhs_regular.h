@@ -16,6 +16,7 @@ enum FluxBits { FLUX_WRITE = 1, FLUX_ACC_ALL = 2, FLUX_ACC_PLANES = 4 };
 
 struct TileShape {
     int x, y, z;
+    int staged;  // the TMA-staged variant of the shape (FP32-flux form, inviscid)
 };
 extern const TileShape kRegularTiles[];
 extern const int kNumRegularTiles;
@@ -124,6 +125,8 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* t
 constexpr double kGravity = -9.8;
 
 int pick_regular_tile(const int n[3], bool visc);
+// the TMA-staged variant of tile's shape, or tile itself when it has none
+int staged_regular_tile(int tile);
 bool regular_tile_fits(int tile, bool visc);
 ocfd_status configure_rhs_regular();
 ocfd_status configure_rhs_regular_f32();

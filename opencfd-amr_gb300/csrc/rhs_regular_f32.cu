@@ -22,6 +22,7 @@ ocfd_status rhs_regular_box_f32(ocfd_context* ctx, const ocfd_array4* S, const o
     const bool visc = (flags & OCFD_VISC) != 0;
     int tile = pick_regular_tile(n, visc);
     if (!tile_fits<float>(tile, visc)) tile = 1;
+    if (!visc) tile = staged_regular_tile(tile);  // TMA staging where the shape has it
     RegBoxArgs a{};
     fill_regular_args(a, S, dSdt, flux, bx, dxinv, tile);
     const int ntiles = a.ntile[0] * a.ntile[1] * a.ntile[2];

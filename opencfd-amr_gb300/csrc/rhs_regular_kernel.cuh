@@ -76,10 +76,11 @@ __host__ __device__ constexpr int pencil_elems() {
     return a > b ? (a > c ? a : c) : (b > c ? b : c);
 }
 
-// tiles whose cross is staged by TMA (see the file comment)
-template <class FT, int TX, int TY, int TZ, bool VISC>
+// tiles whose cross is staged by TMA (see the file comment): the staged
+// variants (XS) of the tile shapes of depth >= 4 in the FP32-flux form
+template <class FT, int TX, int TY, int TZ, bool VISC, bool XS>
 struct CrossOn {
-    static constexpr bool value = std::is_same<FT, float>::value && !VISC && TZ >= 4 && TX % 2 == 0;
+    static constexpr bool value = XS && std::is_same<FT, float>::value && !VISC && TZ >= 4 && TX % 2 == 0;
 };
 
 // Shared memory of a TMA-staged tile (offsets from a 128-byte aligned base):
@@ -126,9 +127,9 @@ __host__ __device__ constexpr size_t cross_region_a() {
     return st > pe ? st : pe;
 }
 
-template <class FT, int TX, int TY, int TZ, bool VISC>
+template <class FT, int TX, int TY, int TZ, bool VISC, bool XS = false>
 __host__ __device__ constexpr size_t regular_smem_bytes() {
-    if (CrossOn<FT, TX, TY, TZ, VISC>::value)
+    if (CrossOn<FT, TX, TY, TZ, VISC, XS>::value)
         return 128 + cross_region_a<FT, TX, TY, TZ>() + sizeof(float) * 5 * Cross<TX, TY, TZ>::NQ;
     return sizeof(FT) * (pencil_elems<TX, TY, TZ>() + (VISC ? 4 * Ring<TX, TY, TZ>::N : 0));
 }
@@ -167,29 +168,26 @@ struct Prec<float> {
                                                       double s4, float* q) {
         const float g = P.f_gamma;
         const float u0 = d2f_bits(s0), u1 = d2f_bits(s1), u2 = d2f_bits(s2), u3 = d2f_bits(s3), u4 = d2f_bits(s4);
+        // every rounding written out (see sw_split_f32): the primitives do not
+        // depend on the code around the call
         const float rho = fmaxf(u0, P.f_smallr);
         const float rhoinv = __frcp_rn(rho);
-        const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
-        const float ei = u4 - rho * (0.5f * (ux * ux + uy * uy + uz * uz));
-        const float p = fmaxf((g - 1.0f) * ei, P.f_smallp);
+        const float ux = __fmul_rn(u1, rhoinv), uy = __fmul_rn(u2, rhoinv), uz = __fmul_rn(u3, rhoinv);
+        const float ke = __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, __fmul_rn(ux, ux)));
+        const float ei = __fmaf_rn(-rho, __fmul_rn(0.5f, ke), u4);
+        const float p = fmaxf(__fmul_rn(__fsub_rn(g, 1.0f), ei), P.f_smallp);
         q[QRHO] = rho;
         q[QU] = ux;
         q[QV] = uy;
         q[QW] = uz;
         q[QPRES] = p;
-        q[QT] = p * rhoinv * P.f_invRg;
-        q[QC] = sqrtf(g * p * rhoinv);
-        // the primitives leave as values the optimiser cannot see through: the
-        // split forms its own products (u u, v v, ...) instead of sharing them
-        // with the kinetic energy above, which would change which products fuse
-        // into FMAs; so primitives split inline and primitives reloaded from
-        // shared memory (TMA-staged tiles) give the same fluxes
-        asm("" : "+f"(q[QRHO]), "+f"(q[QU]), "+f"(q[QV]), "+f"(q[QW]), "+f"(q[QC]));
+        q[QT] = __fmul_rn(__fmul_rn(p, rhoinv), P.f_invRg);
+        q[QC] = __fsqrt_rn(__fmul_rn(__fmul_rn(g, p), rhoinv));
     }
     template <int D>
     static __device__ __forceinline__ void split(const DevParm& P, const float* q, float* fp, float* fm) {
-        sw_split<D, float>(q[QRHO], q[QU], q[QV], q[QW], q[QC], P.f_sw_tmp1, P.f_sw_tmp2, P.f_sw_tmp3,
-                           P.f_sw_gm1, fp, fm);
+        sw_split_f32<D>(q[QRHO], q[QU], q[QV], q[QW], q[QC], P.f_sw_tmp1, P.f_sw_tmp2, P.f_sw_tmp3, P.f_sw_gm1,
+                        fp, fm);
     }
     static __device__ __forceinline__ float weno(const float* a, const float* b, int s) {
         return wenoz_pm_f(a[0], a[s], a[2 * s], a[3 * s], a[4 * s], b[5 * s], b[4 * s], b[3 * s], b[2 * s], b[s]);
@@ -212,12 +210,16 @@ __device__ __forceinline__ double stage_cfl_bound<float>(const DevParm& P, const
     const float g = P.f_gamma;
     const float rho = d2f_bits(un[0]);
     const float rhoinv = __frcp_rn(fmaxf(rho, P.f_smallr));
-    const float vx = d2f_bits(un[1]) * rhoinv, vy = d2f_bits(un[2]) * rhoinv, vz = d2f_bits(un[3]) * rhoinv;
-    const float p = fmaxf((g - 1.0f) * (d2f_bits(un[4]) - 0.5f * rho * (vx * vx + vy * vy + vz * vz)), P.f_smallp);
-    const float cs = sqrtf(g * p * rhoinv);
-    const float dtx = __fdividef(B.dx_f[0], fabsf(vx) + cs);
-    const float dty = __fdividef(B.dx_f[1], fabsf(vy) + cs);
-    const float dtz = __fdividef(B.dx_f[2], fabsf(vz) + cs);
+    // every rounding written out (see sw_split_f32)
+    const float vx = __fmul_rn(d2f_bits(un[1]), rhoinv), vy = __fmul_rn(d2f_bits(un[2]), rhoinv),
+                vz = __fmul_rn(d2f_bits(un[3]), rhoinv);
+    const float ke = __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, __fmul_rn(vx, vx)));
+    const float p =
+        fmaxf(__fmul_rn(__fsub_rn(g, 1.0f), __fmaf_rn(-__fmul_rn(0.5f, rho), ke, d2f_bits(un[4]))), P.f_smallp);
+    const float cs = __fsqrt_rn(__fmul_rn(__fmul_rn(g, p), rhoinv));
+    const float dtx = __fdividef(B.dx_f[0], __fadd_rn(fabsf(vx), cs));
+    const float dty = __fdividef(B.dx_f[1], __fadd_rn(fabsf(vy), cs));
+    const float dtz = __fdividef(B.dx_f[2], __fadd_rn(fabsf(vz), cs));
     return f2d_bits(fminf(dtx, fminf(dty, dtz)));
 }
 
@@ -423,8 +425,14 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
         const FT dxi = dxinv_of<FT>(B, D);
 #pragma unroll
         for (int n = 0; n < 5; ++n) {
-            FT v = dxi * (FF[n * PC::NF + f] - FF[n * PC::NF + f + PC::FST]);
-            acc[n] = (D == 0) ? v : acc[n] + v;
+            if constexpr (std::is_same<FT, float>::value) {
+                // explicit roundings (see sw_split_f32)
+                const float df = __fsub_rn(FF[n * PC::NF + f], FF[n * PC::NF + f + PC::FST]);
+                acc[n] = (D == 0) ? __fmul_rn(dxi, df) : __fmaf_rn(dxi, df, acc[n]);
+            } else {
+                FT v = dxi * (FF[n * PC::NF + f] - FF[n * PC::NF + f + PC::FST]);
+                acc[n] = (D == 0) ? v : acc[n] + v;
+            }
         }
     }
     if (B.has_flux) {
@@ -451,12 +459,14 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
                     for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) = widen<FT>(FF[n * PC::NF + f]);
                 } else if (fl & FLUX_ACC_ALL) {
 #pragma unroll
-                    for (int n = 0; n < 5; ++n) out(gi, gj, gk, n) += wdt * widen<FT>(FF[n * PC::NF + f]);
+                    for (int n = 0; n < 5; ++n)
+                        out(gi, gj, gk, n) = __fma_rn(wdt, widen<FT>(FF[n * PC::NF + f]), out(gi, gj, gk, n));
                 }
                 if ((fl & FLUX_ACC_PLANES) && (g[D] == B.lo[D] || g[D] == B.hi[D] + 1)) {
                     const View<double>& pl = B.fplane[D][g[D] == B.lo[D] ? 0 : 1];
 #pragma unroll
-                    for (int n = 0; n < 5; ++n) pl(gi, gj, gk, n) += wdt * widen<FT>(FF[n * PC::NF + f]);
+                    for (int n = 0; n < 5; ++n)
+                        pl(gi, gj, gk, n) = __fma_rn(wdt, widen<FT>(FF[n * PC::NF + f]), pl(gi, gj, gk, n));
                 }
             }
         }
@@ -466,7 +476,7 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
 
 // One tile (index t over the box list, or over the single box) of the fused
 // RHS / stage; the CFL bound of its cells is folded into local_dt.
-template <class FT, int TX, int TY, int TZ, bool VISC>
+template <class FT, int TX, int TY, int TZ, bool VISC, bool XS>
 __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
                                          int nbox, const RegBoxArgs& single, const DevParm& P, int t,
                                          unsigned char* sbase, uint64_t* bar, uint32_t& phase, bool& abort,
@@ -489,7 +499,7 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
     const int i0 = B.lo[0] + tx * TX, j0 = B.lo[1] + ty * TY, k0 = B.lo[2] + tz * TZ;
 
     FT acc[5];
-    if constexpr (CrossOn<FT, TX, TY, TZ, VISC>::value) {
+    if constexpr (CrossOn<FT, TX, TY, TZ, VISC, XS>::value) {
         using C = Cross<TX, TY, TZ>;
         double* stage = reinterpret_cast<double*>(sbase);
         float* Q = reinterpret_cast<float*>(sbase + cross_region_a<FT, TX, TY, TZ>());
@@ -571,8 +581,8 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
         for (int n = 0; n < 5; ++n) L[n] = widen<FT>(acc[n]);
         if (P.grav != 0.0) {
             // gravity source after divop, Source/Advance.cpp:331-342
-            L[3] += P.grav * B.S(ci, cj, ck, 0);
-            L[4] += P.grav * B.S(ci, cj, ck, 3);
+            L[3] = __fma_rn(P.grav, B.S(ci, cj, ck, 0), L[3]);
+            L[4] = __fma_rn(P.grav, B.S(ci, cj, ck, 3), L[4]);
         }
         if (B.mode == RHS_WRITE_DSDT) {
 #pragma unroll
@@ -585,7 +595,10 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
             for (int n = 0; n < 5; ++n) {
                 double us = B.S(ci, cj, ck, n);
                 double u0 = B.U0(ci, cj, ck, n);
-                un[n] = B.rk_a * u0 + B.rk_b * (us + dt * L[n]);
+                if constexpr (std::is_same<FT, float>::value)  // explicit roundings (see sw_split_f32)
+                    un[n] = __fma_rn(B.rk_b, __fma_rn(dt, L[n], us), __dmul_rn(B.rk_a, u0));
+                else
+                    un[n] = B.rk_a * u0 + B.rk_b * (us + dt * L[n]);
                 B.Uout(ci, cj, ck, n) = un[n];
             }
             if (B.cfl_min) {
@@ -603,24 +616,27 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
 //                 (queue[0] next tile, queue[1] CTAs done); the last CTA to finish
 //                 resets both, so every launch starts from zero (graph replays too)
 // CTAs per SM that a tile's shared memory admits (228 KB per SM, 1 KB of it
-// reserved per CTA; at most 2048 threads): the register budget follows from it,
-// so the compiler neither spills below nor plans above the occupancy the tile gets
-template <class FT, int TX, int TY, int TZ, bool VISC>
+// reserved per CTA; at most 2048 threads), capped at 3: the register budget
+// follows from it, so the compiler neither spills below nor plans above the
+// occupancy the tile gets (the cap keeps 8^3 FP32 pencil tiles at three CTAs,
+// measured faster than two without spills and than four with 32 registers)
+template <class FT, int TX, int TY, int TZ, bool VISC, bool XS>
 __host__ __device__ constexpr int regular_min_blocks() {
-    const int b = (int)((228u * 1024u) / (regular_smem_bytes<FT, TX, TY, TZ, VISC>() + 1024u));
+    const int b = (int)((228u * 1024u) / (regular_smem_bytes<FT, TX, TY, TZ, VISC, XS>() + 1024u));
     const int t = 2048 / (TX * TY * TZ);
-    const int m = b < t ? b : t;
+    int m = b < t ? b : t;
+    m = m < 3 ? m : 3;
     return m < 1 ? 1 : m;
 }
 
-template <class FT, int TX, int TY, int TZ, bool VISC>
-__global__ void __launch_bounds__(TX* TY* TZ, (regular_min_blocks<FT, TX, TY, TZ, VISC>()))
+template <class FT, int TX, int TY, int TZ, bool VISC, bool XS>
+__global__ void __launch_bounds__(TX* TY* TZ, (regular_min_blocks<FT, TX, TY, TZ, VISC, XS>()))
     k_rhs_regular(const RegBoxArgs* __restrict__ boxes, const int* __restrict__ tile_start,
                   int nbox, const __grid_constant__ RegBoxArgs single, DevParm P, int ntiles, int sched,
                   unsigned* queue) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint64_t tma_bar;
-    constexpr bool cross = CrossOn<FT, TX, TY, TZ, VISC>::value;
+    constexpr bool cross = CrossOn<FT, TX, TY, TZ, VISC, XS>::value;
     // the TMA-staged layout starts at a 128-byte boundary (its size includes the slack)
     unsigned char* sbase =
         cross ? reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127))
@@ -634,11 +650,11 @@ __global__ void __launch_bounds__(TX* TY* TZ, (regular_min_blocks<FT, TX, TY, TZ
     double local_dt = __longlong_as_double(0x7FF0000000000000LL);
     unsigned long long* cfl = boxes ? boxes[0].cfl_min : single.cfl_min;  // one target per stage
     if (sched == SCHED_GRID) {
-        rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, blockIdx.x, sbase, &tma_bar, phase, abort,
+        rhs_tile<FT, TX, TY, TZ, VISC, XS>(boxes, tile_start, nbox, single, P, blockIdx.x, sbase, &tma_bar, phase, abort,
                                        local_dt);
     } else if (sched == SCHED_STRIDE) {
         for (int t = blockIdx.x; t < ntiles && !abort; t += gridDim.x) {
-            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, sbase, &tma_bar, phase, abort,
+            rhs_tile<FT, TX, TY, TZ, VISC, XS>(boxes, tile_start, nbox, single, P, t, sbase, &tma_bar, phase, abort,
                                            local_dt);
             __syncthreads();
         }
@@ -650,7 +666,7 @@ __global__ void __launch_bounds__(TX* TY* TZ, (regular_min_blocks<FT, TX, TY, TZ
             const int t = next;
             __syncthreads();
             if (t >= ntiles || abort) break;
-            rhs_tile<FT, TX, TY, TZ, VISC>(boxes, tile_start, nbox, single, P, t, sbase, &tma_bar, phase, abort,
+            rhs_tile<FT, TX, TY, TZ, VISC, XS>(boxes, tile_start, nbox, single, P, t, sbase, &tma_bar, phase, abort,
                                            local_dt);
             __syncthreads();
         }
@@ -666,13 +682,13 @@ __global__ void __launch_bounds__(TX* TY* TZ, (regular_min_blocks<FT, TX, TY, TZ
     if (cfl) block_min_atomic(local_dt, cfl);
 }
 
-template <class FT, int TX, int TY, int TZ, bool VISC>
+template <class FT, int TX, int TY, int TZ, bool VISC, bool XS>
 static ocfd_status launch_t(const RegBoxArgs* d_boxes, const int* d_tile_start, int nbox,
                             const RegBoxArgs& single, int ntiles, const DevParm& P,
                             cudaStream_t st, int sched, unsigned* queue) {
     constexpr int NT = TX * TY * TZ;
-    constexpr size_t smem = regular_smem_bytes<FT, TX, TY, TZ, VISC>();
-    auto kern = k_rhs_regular<FT, TX, TY, TZ, VISC>;
+    constexpr size_t smem = regular_smem_bytes<FT, TX, TY, TZ, VISC, XS>();
+    auto kern = k_rhs_regular<FT, TX, TY, TZ, VISC, XS>;
     if (smem > kMaxSmem) return fail(OCFD_BAD_ARG, "regular RHS tile does not fit shared memory in this mode");
     if (ntiles <= 0) return OCFD_OK;
     if (sched == SCHED_QUEUE && !queue) return fail(OCFD_BAD_ARG, "regular RHS: work-queue schedule without a queue");
@@ -693,21 +709,32 @@ static ocfd_status launch_t(const RegBoxArgs* d_boxes, const int* d_tile_start, 
     return check_launch("k_rhs_regular");
 }
 
-template <class FT, int TX, int TY, int TZ, bool VISC>
+template <class FT, int TX, int TY, int TZ, bool VISC, bool XS>
 static bool configure_one() {
-    const size_t smem = regular_smem_bytes<FT, TX, TY, TZ, VISC>();
+    const size_t smem = regular_smem_bytes<FT, TX, TY, TZ, VISC, XS>();
     if (smem > kMaxSmem) return true;  // shape not offered in this mode
-    return cudaFuncSetAttribute(k_rhs_regular<FT, TX, TY, TZ, VISC>,
+    return cudaFuncSetAttribute(k_rhs_regular<FT, TX, TY, TZ, VISC, XS>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
 }
 
-// Every compiled tile shape (index = position in kRegularTiles)
-#define OCFD_REGULAR_TILES(X) X(0, 8, 8, 8) X(1, 8, 8, 4) X(2, 16, 8, 4) X(3, 16, 16, 2) X(4, 32, 8, 2) X(5, 16, 8, 2)
+// Every compiled tile: index (position in kRegularTiles), shape, and whether it
+// is the TMA-staged variant (XS) of its shape.  A staged index runs the staged
+// kernel only in the inviscid FP32-flux form; in every other mode it runs the
+// pencil kernel of its shape (the same instantiation as the plain index).
+#define OCFD_REGULAR_TILES(X)                                                                              \
+    X(0, 8, 8, 8, false) X(1, 8, 8, 4, false) X(2, 16, 8, 4, false) X(3, 16, 16, 2, false) X(4, 32, 8, 2, false) \
+        X(5, 16, 8, 2, false) X(6, 8, 8, 8, true) X(7, 8, 8, 4, true) X(8, 16, 8, 4, true)
+
+template <class FT>
+struct StagedIn {  // the staged variants exist in the FP32-flux form only
+    static constexpr bool value = std::is_same<FT, float>::value;
+};
 
 template <class FT>
 static ocfd_status configure_all() {
     bool ok = true;
-#define OCFD_CONF(I, X, Y, Z) ok = ok && configure_one<FT, X, Y, Z, false>() && configure_one<FT, X, Y, Z, true>();
+#define OCFD_CONF(I, X, Y, Z, XS) \
+    ok = ok && configure_one<FT, X, Y, Z, false, XS && StagedIn<FT>::value>() && configure_one<FT, X, Y, Z, true, false>();
     OCFD_REGULAR_TILES(OCFD_CONF)
 #undef OCFD_CONF
     if (!ok) return check_launch("configure regular RHS kernels");
@@ -718,9 +745,10 @@ template <class FT>
 static bool tile_fits(int tile, bool visc) {
     size_t b = 0;
     switch (tile) {
-#define OCFD_FIT(I, X, Y, Z)                                                                                \
-    case I:                                                                                                 \
-        b = visc ? regular_smem_bytes<FT, X, Y, Z, true>() : regular_smem_bytes<FT, X, Y, Z, false>(); \
+#define OCFD_FIT(I, X, Y, Z, XS)                                                                                \
+    case I:                                                                                                     \
+        b = visc ? regular_smem_bytes<FT, X, Y, Z, true, false>()                                               \
+                 : regular_smem_bytes<FT, X, Y, Z, false, XS && StagedIn<FT>::value>();                         \
         break;
         OCFD_REGULAR_TILES(OCFD_FIT)
 #undef OCFD_FIT
@@ -735,12 +763,12 @@ static ocfd_status launch_any(int tile, bool visc, const RegBoxArgs* d_boxes, co
                               int nbox, const RegBoxArgs& single, int ntiles, const DevParm& P,
                               cudaStream_t st, int sched = SCHED_GRID, unsigned* queue = nullptr) {
     switch (tile) {
-#define OCFD_CASE(I, X, Y, Z)                                                                             \
-    case I:                                                                                               \
-        return visc ? launch_t<FT, X, Y, Z, true>(d_boxes, d_tile_start, nbox, single, ntiles, P, st, sched, \
-                                                  queue)                                                  \
-                    : launch_t<FT, X, Y, Z, false>(d_boxes, d_tile_start, nbox, single, ntiles, P, st, sched, \
-                                                   queue);
+#define OCFD_CASE(I, X, Y, Z, XS)                                                                               \
+    case I:                                                                                                     \
+        return visc ? launch_t<FT, X, Y, Z, true, false>(d_boxes, d_tile_start, nbox, single, ntiles, P, st,    \
+                                                         sched, queue)                                          \
+                    : launch_t<FT, X, Y, Z, false, XS && StagedIn<FT>::value>(d_boxes, d_tile_start, nbox,      \
+                                                                              single, ntiles, P, st, sched, queue);
         OCFD_REGULAR_TILES(OCFD_CASE)
 #undef OCFD_CASE
     }

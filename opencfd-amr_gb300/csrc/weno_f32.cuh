@@ -88,6 +88,48 @@ __device__ __forceinline__ float wenoz_pm_f(float a1, float a2, float a3, float 
     return (f.x + f.y) * iv;
 }
 
+// Steger-Warming split in FP32 (FluxSplit.H:11-193, the same terms as
+// sw_split) with every rounding written out: __fmul_rn / __fadd_rn / __fsub_rn
+// are never fused and __fmaf_rn always is, so the compiler has no choice left
+// and the fluxes of a cell do not depend on the code around the call (primitives
+// formed inline or reloaded from shared memory split to the same values).
+template <int D>
+__device__ __forceinline__ void sw_split_f32(float d, float u, float v, float w, float c, float t1, float t2,
+                                             float t3, float gm1, float* fp, float* fm) {
+    const float vel[3] = {u, v, w};
+    const float un = vel[D];
+    const float uc1 = __fsub_rn(un, c), uc2 = __fadd_rn(un, c);
+    float a0 = u, a1 = v, a2 = w, b0 = u, b1 = v, b2 = w;
+    if (D == 0) { a0 = uc1; b0 = uc2; }
+    if (D == 1) { a1 = uc1; b1 = uc2; }
+    if (D == 2) { a2 = uc1; b2 = uc2; }
+    const float vvc1 = __fmul_rn(0.5f, __fmaf_rn(a2, a2, __fmaf_rn(a1, a1, __fmul_rn(a0, a0))));
+    const float vvc2 = __fmul_rn(0.5f, __fmaf_rn(b2, b2, __fmaf_rn(b1, b1, __fmul_rn(b0, b0))));
+    const float v2 = __fmul_rn(gm1, __fmaf_rn(w, w, __fmaf_rn(v, v, __fmul_rn(u, u))));
+    const float w2 = __fmul_rn(__fmul_rn(t3, c), c);
+    const float E1P = __fmul_rn(__fadd_rn(un, fabsf(un)), 0.5f), E2P = __fmul_rn(__fadd_rn(uc1, fabsf(uc1)), 0.5f),
+                E3P = __fmul_rn(__fadd_rn(uc2, fabsf(uc2)), 0.5f);
+    const float E1M = __fsub_rn(un, E1P), E2M = __fsub_rn(uc1, E2P), E3M = __fsub_rn(uc2, E3P);
+    const float t0 = __fmul_rn(d, t1);
+    const float sp = __fadd_rn(__fmaf_rn(t2, E1P, E2P), E3P), sm = __fadd_rn(__fmaf_rn(t2, E1M, E2M), E3M);
+    fp[0] = __fmul_rn(t0, sp);
+    fm[0] = __fmul_rn(t0, sm);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        if (m == D) {
+            fp[1 + m] = __fmul_rn(t0, __fmaf_rn(E3P, uc2, __fmaf_rn(E2P, uc1, __fmul_rn(__fmul_rn(t2, E1P), un))));
+            fm[1 + m] = __fmul_rn(t0, __fmaf_rn(E3M, uc2, __fmaf_rn(E2M, uc1, __fmul_rn(__fmul_rn(t2, E1M), un))));
+        } else {
+            fp[1 + m] = __fmul_rn(__fmul_rn(t0, vel[m]), sp);
+            fm[1 + m] = __fmul_rn(__fmul_rn(t0, vel[m]), sm);
+        }
+    }
+    fp[4] = __fmul_rn(t0, __fmaf_rn(w2, __fadd_rn(E2P, E3P),
+                                     __fmaf_rn(E3P, vvc2, __fmaf_rn(E2P, vvc1, __fmul_rn(E1P, v2)))));
+    fm[4] = __fmul_rn(t0, __fmaf_rn(w2, __fadd_rn(E2M, E3M),
+                                     __fmaf_rn(E3M, vvc2, __fmaf_rn(E2M, vvc1, __fmul_rn(E1M, v2)))));
+}
+
 // Conversions between FP64 and FP32 on the integer pipes.  GB300 runs FP64
 // (and its conversions) at 2 instructions / cycle / SM, so in the mixed form the
 // state is narrowed and the FP32 divergence widened with bit operations:

@@ -278,6 +278,10 @@ class Level:
               "profile_stage")
         return ms.value
 
+    def set_schedule(self, tile, sched=0):
+        """Tile shape (index, -1: keep) and schedule of the batched stage kernel."""
+        check(self.lib.ocfd_level_set_schedule(self.h, tile, sched), "ocfd_level_set_schedule")
+
     def autotune(self, flags=0, reps=5, stream=None):
         """Pick the fastest tile shape x schedule of the batched stage kernel;
         returns (tile, sched)."""

@@ -113,12 +113,12 @@ def _periodic_case(n, seed):
 
 @pytest.mark.parametrize("grid", [(16, 16, 16), (20, 12, 13)])
 def test_fp32_tma_staged_tiles(ctx, grid):
-    """The FP32-flux form stages each tile of depth >= 4 (shapes 0-2) by TMA -
-    the tile and its +-3 halos along x, y and z - and forms the primitives once
-    per staged cell; shapes 3-5 form each pencil's primitives from global loads.
-    Every shape, with TMA on or with plain loads, gives bit-identical states
-    after a few steps of a 3D periodic flow with shocks, with boxes that leave
-    partial tiles (20 x 12 x 13)."""
+    """Tiles 6-8 of the FP32-flux form stage the tile's cross - the tile and its
+    +-3 halos along x, y and z - by TMA and form the primitives once per staged
+    cell; tiles 0-5 form each pencil's primitives from global loads.  Every
+    tile, with TMA on or with plain loads, gives bit-identical states after a
+    few steps of a 3D periodic flow with shocks, with boxes that leave partial
+    tiles (20 x 12 x 13)."""
     import ocfd
     from test_gpu_level import run_gpu
     case = _periodic_case((40, 24, 26), seed=31)
@@ -126,7 +126,7 @@ def test_fp32_tma_staged_tiles(ctx, grid):
     try:
         for on in (True, False):
             ocfd.set_tma_staging(on)
-            for t in range(6):
+            for t in range(9):
                 res[(on, t)], _ = run_gpu(ctx, case, 3, 0.4, grid, flags=ocfd.FLUX_FP32, tile=t)
     finally:
         ocfd.set_tma_staging(True)
