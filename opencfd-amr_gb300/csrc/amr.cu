@@ -48,7 +48,6 @@
 #include <cstring>
 #include <map>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "level.h"
@@ -970,26 +969,19 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     }
     pt.mark("      reflux scan", 0);
     // group the faces by coarse cell (an element index of the level's state is
-    // unique across its boxes), keeping discovery order within a group
-    std::vector<int> gid(faces.size());
-    std::vector<int> gfirst;  // first face of each group
-    {
-        std::unordered_map<long long, int> group;
-        group.reserve(faces.size() * 2);
-        for (size_t q = 0; q < faces.size(); ++q) {
-            auto it = group.emplace(face_u[q], (int)gfirst.size());
-            if (it.second) gfirst.push_back((int)q);
-            gid[q] = it.first->second;
-        }
+    // unique across its boxes) with discovery order kept inside a group: one
+    // sort of 64-bit keys (element index, discovery index)
+    if (faces.size() >= (size_t(1) << 22)) return fail(OCFD_BAD_ARG, "AMR: too many reflux faces");
+    std::vector<uint64_t> key(faces.size());
+    for (size_t q = 0; q < faces.size(); ++q) key[q] = ((uint64_t)face_u[q] << 22) | (uint64_t)q;
+    std::sort(key.begin(), key.end());
+    std::vector<int> order(faces.size()), gstart;
+    for (size_t q = 0; q < key.size(); ++q) {
+        order[q] = (int)(key[q] & ((1u << 22) - 1));
+        if (q == 0 || (key[q] >> 22) != (key[q - 1] >> 22)) gstart.push_back((int)q);
     }
-    const int ngroup = (int)gfirst.size();
-    std::vector<int> gstart((size_t)ngroup + 1, 0), order(faces.size());
-    for (int g : gid) ++gstart[(size_t)g + 1];
-    for (int g = 0; g < ngroup; ++g) gstart[(size_t)g + 1] += gstart[g];
-    {
-        std::vector<int> fill(gstart.begin(), gstart.end() - 1);
-        for (size_t q = 0; q < faces.size(); ++q) order[(size_t)fill[gid[q]]++] = (int)q;
-    }
+    const int ngroup = (int)gstart.size();
+    gstart.push_back((int)faces.size());
     // coarse register: face arrays of the coarse boxes that own a reflux cell,
     // in box order
     std::vector<long long> creg_off((size_t)ncb, -1);
