@@ -909,6 +909,9 @@ def react_cpu_sample(n=64, steps=1, threads=None):
 
 
 SUR_GUARD_SWEEP = (0.0, 1.0, 0.1, 0.01, 0.001)
+# the per-output criterion relative to each Y_k itself (a floor far below the
+# 1e-11 radical mass fractions of the induction phase)
+SUR_Y_FLOOR = 1e-20
 
 
 def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, same_steps, value_plain):
@@ -917,8 +920,8 @@ def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, sa
     the FP64 implicit substep taken from 0D constant-pressure ignition
     trajectories (T0 1000-2500 K, phi 0.5-2, p 0.8-10 atm), then embedded in the
     reacting level with the guard's FP64 fallback.  The per-output criterion of
-    the guard (no Y_n may change by more than dy_rel_max x max(Y_n, 1e-6) in a
-    substep) is swept over SUR_GUARD_SWEEP (0 = off); for each setting the
+    the guard (no Y_n may change by more than dy_rel_max x max(Y_n, SUR_Y_FLOOR)
+    in a substep) is swept over SUR_GUARD_SWEEP (0 = off); for each setting the
     fallback rate, the cell-steps/s and the L1 error in rho, p, T, Y_OH, Y_H2O
     against the plain FP64 run after the same steps.  matched_1e-4 is the
     loosest setting whose rho, p and Y_OH errors are all <= 1e-4 (None when
@@ -941,7 +944,7 @@ def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, sa
 
     sweep = []
     for d in SUR_GUARD_SWEEP:
-        guard = sur.guard.with_dy_rel(d)
+        guard = sur.guard.with_dy_rel(d, SUR_Y_FLOOR)
         R = make(True, f32=True)
         check(load().ocfd_react_set_surrogate(R.h, sur.net.h, ctypes.byref(guard)), "set_surrogate")
         R.advance(args.warmup)
@@ -961,7 +964,8 @@ def react_surrogate_form(args, world, ctx, make, stream, l2flush, ref, cells, sa
         R.close()
         pb = props(got)
         v = cells * args.steps * world / (ms * 1e-3)
-        sweep.append({"dy_rel_max": d, "cell_steps_per_s": v, "speedup_over_fp64_plain": v / value_plain,
+        sweep.append({"dy_rel_max": d, "y_floor": SUR_Y_FLOOR, "cell_steps_per_s": v,
+                      "speedup_over_fp64_plain": v / value_plain,
                       "fallback_rate": fb.value / float(cells * substeps), "fallback_cells": int(fb.value),
                       "l1_vs_fp64_after_steps": {
                           "steps": same_steps, "T": l1(pb[0], pa[0]), "Y_OH": l1(pb[2 + 5], pa[2 + 5]),

@@ -335,7 +335,12 @@ ocfd_status ocfd_level_profile_stage(ocfd_level* level, unsigned flags, int reps
  * tile / sched (may be NULL) receive the choice. */
 ocfd_status ocfd_level_autotune(ocfd_level* level, unsigned flags, int reps, int32_t* tile, int32_t* sched,
                                 void* stream);
-/* Set the tile shape (index, -1 keeps it) and schedule (0-2) explicitly. */
+/* Set the tile shape (index, -1 keeps it) and schedule (0-2) explicitly.  Tile
+ * indices 0-5 are the pencil shapes (8,8,8), (8,8,4), (16,8,4), (16,16,2),
+ * (32,8,2), (16,8,2); 6-8 the TMA-staged variants of the first three, which
+ * stage in the inviscid FP32-flux form and run the pencil kernel otherwise.
+ * A shape whose shared memory does not fit the form a step asks for makes
+ * that step fail with OCFD_BAD_ARG. */
 ocfd_status ocfd_level_set_schedule(ocfd_level* level, int32_t tile, int32_t sched);
 /* Time integration of a standalone ideal-gas level, ebr.time_integration
  * (Source/EBR.cpp:36, Source/Advance.cpp:115-149): 3 = SSP-RK3 (the default

@@ -841,7 +841,7 @@ size_t ocfd_level_state_elems(const ocfd_level* L) { return L ? (size_t)L->elems
 
 ocfd_status ocfd_level_set_schedule(ocfd_level* L, int32_t tile, int32_t sched) {
     if (!L || sched < 0 || sched >= NUM_SCHED || tile < -1 || tile >= kNumRegularTiles ||
-        (tile >= 0 && !regular_tile_fits(tile, true)))
+        (tile >= 0 && !regular_tile_fits(tile, false)))
         return fail(OCFD_BAD_ARG, "ocfd_level_set_schedule");
     L->sched = sched;
     ocfd_status s = OCFD_OK;
