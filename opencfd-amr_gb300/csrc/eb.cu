@@ -59,9 +59,14 @@ __global__ void k_eb_faces(EbBoxArgs B, DevParm P) {
         const uint32_t f = B.flag(i, j, k);
         double ql[7], qr[7];
 #pragma unroll
-        for (int m = 0; m < 7; ++m)
+        for (int m = 0; m < 7; ++m) {
+            if (m == QT) {  // the Van Leer flux does not read the temperature
+                ql[m] = qr[m] = 0.0;
+                continue;
+            }
             eb_recon(f, D, q(i - 2 * di, j - 2 * dj, k - 2 * dk, m), q(i - di, j - dj, k - dk, m),
                      q(i, j, k, m), q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
+        }
         double flx[5];
         vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
         if (B.visc) eb_visc_face(P, q, B.flag, D, i, j, k, B.dxinv, flx, 1, false, 0, 0, 0);

@@ -262,6 +262,10 @@ __device__ __forceinline__ void ebt_faces(const EbStageArgs& A, const EbStageBox
             double ql[7], qr[7];
 #pragma unroll
             for (int m = 0; m < 7; ++m) {
+                if (m == QT) {  // the Van Leer flux does not read the temperature
+                    ql[m] = qr[m] = 0.0;
+                    continue;
+                }
                 const FT* pm = p0 + m * EBQ_N;
                 eb_recon(fl, D, (double)pm[-2 * SD], (double)pm[-SD], (double)pm[0], (double)pm[SD], ql[m], qr[m]);
             }
