@@ -48,6 +48,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "level.h"
@@ -861,23 +862,33 @@ static long long region_offset_plane(const IBox& pl, int i, int j, int k) {
     return (long long)(i - pl.lo[0]) + (long long)(j - pl.lo[1]) * ex + (long long)(k - pl.lo[2]) * ex * ey;
 }
 
-// Tables between level c = f-1 and level f: ghost interpolation, average-down,
-// reflux cells and the two sides of the flux register.
-static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf) {
-    AmrLev& C = H->lev[f - 1];
-    AmrLev& F = H->lev[f];
+// Host side of the tables between level c = f-1 and level f (ghost
+// interpolation, average-down, reflux cells, the flux register layout): reads
+// the hierarchy only, so the pairs of a hierarchy are built concurrently.
+struct PairTables {
+    ocfd_status status = OCFD_OK;
+    std::vector<CfTag> cf_tags;
+    std::vector<AvgTag> avg_tags;
+    long long covered = 0;
+    std::vector<long long> plane_off;
+    std::vector<IBox> plane_box;
+    long long fe = 0;
+    std::vector<long long> creg_off;
+    long long ce = 0;
+    std::vector<RefluxCell> rc_h;
+    std::vector<RefluxFace> rf_h;
+};
+
+static ocfd_status compute_pair(const ocfd_amr* H, int f, PairTables& T) {
+    const AmrLev& C = H->lev[f - 1];
+    const AmrLev& F = H->lev[f];
     ocfd_status s;
-    PhaseTimer pt;
     {
         std::vector<std::vector<IBox>> regions;
         ghost_regions(H, f, regions);
-        std::vector<CfTag> tags;
-        s = build_cf_tags(H, f, regions, tags);
-        if (s != OCFD_OK) return s;
-        s = F.cf.set(tags, &H->pool);
+        s = build_cf_tags(H, f, regions, T.cf_tags);
         if (s != OCFD_OK) return s;
     }
-    pt.mark("      ghost cf tags", 0);
     BoxIndex cidx;
     cidx.build(C.boxes, C.dom);
     std::vector<IBox> fcoarse;
@@ -885,7 +896,7 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     BoxIndex fcidx;
     fcidx.build(fcoarse, C.dom);
     {
-        std::vector<AvgTag> tags;
+        std::vector<AvgTag>& tags = T.avg_tags;
         long long covered = 0;
         for (int fb = 0; fb < (int)F.boxes.size(); ++fb)
             for (int cb : cidx.query(fcoarse[fb])) {
@@ -899,15 +910,14 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
                 tags.push_back(t);
                 covered += ib_cells(I);
             }
-        s = F.avg.set(tags, &H->pool);
-        if (s != OCFD_OK) return s;
-        C.leaf = C.L->ncells - covered;
+        T.covered = covered;
     }
-    pt.mark("      avg tags", 0);
     // ---- flux register layout: fine planes of every fine box
     const int nfb = (int)F.boxes.size(), ncb = (int)C.boxes.size();
-    std::vector<long long> plane_off((size_t)nfb * 6);
-    std::vector<IBox> plane_box((size_t)nfb * 6);
+    std::vector<long long>& plane_off = T.plane_off;
+    std::vector<IBox>& plane_box = T.plane_box;
+    plane_off.assign((size_t)nfb * 6, 0);
+    plane_box.assign((size_t)nfb * 6, IBox{});
     long long fe = 0;
     for (int fb = 0; fb < nfb; ++fb)
         for (int d = 0; d < 3; ++d)
@@ -967,7 +977,6 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
                             }
             }
     }
-    pt.mark("      reflux scan", 0);
     // group the faces by coarse cell (an element index of the level's state is
     // unique across its boxes) with discovery order kept inside a group: one
     // sort of 64-bit keys (element index, discovery index)
@@ -984,7 +993,8 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
     gstart.push_back((int)faces.size());
     // coarse register: face arrays of the coarse boxes that own a reflux cell,
     // in box order
-    std::vector<long long> creg_off((size_t)ncb, -1);
+    std::vector<long long>& creg_off = T.creg_off;
+    creg_off.assign((size_t)ncb, -1);
     long long ce = 0;
     {
         std::vector<char> owns((size_t)ncb, 0);
@@ -1015,8 +1025,8 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
         *cns = ib_cells(fa);
         return off + region_offset_plane(fa, fc[0], fc[1], fc[2]);
     };
-    std::vector<RefluxCell> rc_h;
-    std::vector<RefluxFace> rf_h;
+    std::vector<RefluxCell>& rc_h = T.rc_h;
+    std::vector<RefluxFace>& rf_h = T.rf_h;
     rc_h.reserve(ngroup);
     rf_h.reserve(faces.size());
     for (int g = 0; g < ngroup; ++g) {
@@ -1057,17 +1067,34 @@ static ocfd_status build_pair(ocfd_amr* H, int f, StageRoles& rc, StageRoles& rf
         }
         rc_h.push_back(cell);
     }
-    pt.mark("      reflux tables", 0);
-    F.nrc = (int)rc_h.size();
-    s = upload(&F.d_rc, rc_h, &H->pool);
-    if (s == OCFD_OK) s = upload(&F.d_rf, rf_h, &H->pool);
+    T.fe = fe;
+    T.ce = ce;
+    return OCFD_OK;
+}
+
+// Device side of a pair's tables: uploads, flux registers, the stage roles'
+// register views.  Serial (the device pool is not shared between threads).
+static ocfd_status apply_pair(ocfd_amr* H, int f, PairTables& T, StageRoles& rc, StageRoles& rf) {
+    AmrLev& C = H->lev[f - 1];
+    AmrLev& F = H->lev[f];
+    const int nfb = (int)F.boxes.size(), ncb = (int)C.boxes.size();
+    const std::vector<long long>& plane_off = T.plane_off;
+    const std::vector<IBox>& plane_box = T.plane_box;
+    const std::vector<long long>& creg_off = T.creg_off;
+    const long long fe = T.fe, ce = T.ce;
+    ocfd_status s = F.cf.set(T.cf_tags, &H->pool);
+    if (s == OCFD_OK) s = F.avg.set(T.avg_tags, &H->pool);
+    if (s != OCFD_OK) return s;
+    C.leaf = C.L->ncells - T.covered;
+    F.nrc = (int)T.rc_h.size();
+    s = upload(&F.d_rc, T.rc_h, &H->pool);
+    if (s == OCFD_OK) s = upload(&F.d_rf, T.rf_h, &H->pool);
     if (s != OCFD_OK) return s;
     F.freg_elems = fe;
     C.creg_elems = ce;
     F.freg = static_cast<double*>(dev_alloc(sizeof(double) * std::max<long long>(1, fe), &H->pool));
     C.creg = static_cast<double*>(dev_alloc(sizeof(double) * std::max<long long>(1, ce), &H->pool));
     if (!F.freg || !C.creg) return fail(OCFD_OUT_OF_MEMORY, "AMR: flux registers");
-    pt.mark("      uploads", 0);
     // stage roles: register views
     rf.flux_bits.resize(nfb, 0);
     rf.fplane.resize((size_t)nfb * 6);
@@ -1165,10 +1192,20 @@ static ocfd_status rebuild_tables(ocfd_amr* H) {
         }
     }
     PhaseTimer pt;
-    for (int f = 1; f < H->nlev; ++f) {
-        ocfd_status s = build_pair(H, f, roles[f - 1], roles[f]);
-        if (s != OCFD_OK) return s;
-        pt.mark("    pair tables", 0);
+    {
+        // host tables of every level pair at once, then their uploads in order
+        std::vector<PairTables> T(H->nlev);
+        std::vector<std::thread> workers;
+        for (int f = 1; f < H->nlev; ++f)
+            workers.emplace_back([H, f, &T] { T[f].status = compute_pair(H, f, T[f]); });
+        for (std::thread& w : workers) w.join();
+        pt.mark("    pair tables (host)", 0);
+        for (int f = 1; f < H->nlev; ++f) {
+            ocfd_status s = T[f].status;
+            if (s == OCFD_OK) s = apply_pair(H, f, T[f], roles[f - 1], roles[f]);
+            if (s != OCFD_OK) return s;
+        }
+        pt.mark("    pair tables (device)", 0);
     }
     for (int l = 0; l < H->nlev; ++l) {
         StageRoles& r = roles[l];

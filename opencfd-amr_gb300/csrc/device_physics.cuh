@@ -164,6 +164,69 @@ __device__ __forceinline__ double wenoz_1rcp(double V1, double V2, double V3, do
 #endif
 
 #if defined(__CUDACC__)
+// WENO-Z of three consecutive faces of a pencil line (the FP64 regular-box
+// kernel's work item), the arithmetic of wenoz_1rcp with every rounding written
+// out.  The second differences e = V1 - 2 V2 + V3 of the smoothness indicators
+// and their (13/12) e^2 belong to a cell triple, and a triple serves as
+// stencil 1, 2 and 3 of three consecutive faces: a run of three faces forms
+// five of them instead of nine.
+__device__ __forceinline__ double wenoz_e2(double Va, double Vb, double Vc) {
+    const double e = __dadd_rn(__fma_rn(-2.0, Vb, Va), Vc);
+    return __dmul_rn(__dmul_rn(13.0 / 12.0, e), e);
+}
+// one side's face from its stencil V1..V5 (ordered towards the face) and the
+// (13/12) e^2 of its triples (V1 V2 V3), (V2 V3 V4), (V3 V4 V5)
+__device__ __forceinline__ double wenoz_face_e(double V1, double V2, double V3, double V4, double V5, double E1,
+                                               double E2, double E3) {
+    const double eps = 1e-6;
+    const double g1 = __fma_rn(3.0, V3, __fma_rn(-4.0, V2, V1));
+    const double g2 = __dsub_rn(V2, V4);
+    const double g3 = __dadd_rn(__fma_rn(-4.0, V4, __dmul_rn(3.0, V3)), V5);
+    const double b1 = __fma_rn(__dmul_rn(0.25, g1), g1, E1);
+    const double b2 = __fma_rn(__dmul_rn(0.25, g2), g2, E2);
+    const double b3 = __fma_rn(__dmul_rn(0.25, g3), g3, E3);
+    const double tau = fabs(__dsub_rn(b1, b3));
+    const double D1 = __dadd_rn(eps, b1), D2 = __dadd_rn(eps, b2), D3 = __dadd_rn(eps, b3);
+    const double q1 = __dmul_rn(D1, D1), q2 = __dmul_rn(D2, D2), q3 = __dmul_rn(D3, D3), t2 = __dmul_rn(tau, tau);
+    const double a1 = __dmul_rn(__dadd_rn(q1, t2), __dmul_rn(q2, q3));
+    const double a2 = __dmul_rn(__dmul_rn(6.0, __dadd_rn(q2, t2)), __dmul_rn(q1, q3));
+    const double a3 = __dmul_rn(__dmul_rn(3.0, __dadd_rn(q3, t2)), __dmul_rn(q1, q2));
+    const double v1 = __fma_rn(11.0, V3, __fma_rn(-7.0, V2, __dmul_rn(2.0, V1)));
+    const double v2 = __fma_rn(2.0, V4, __fma_rn(5.0, V3, -V2));
+    const double v3 = __dsub_rn(__fma_rn(5.0, V4, __dmul_rn(2.0, V3)), V5);
+    const double num = __fma_rn(a3, v3, __fma_rn(a2, v2, __dmul_rn(a1, v1)));
+    const double den = __dmul_rn(6.0, __dadd_rn(__dadd_rn(a1, a2), a3));
+    return __dmul_rn(num, rcp_nr(den));
+}
+// one side of faces m = 0, 1, 2 whose stencils (ordered towards the face) are
+// a[m s] .. a[(m + 4) s], as a window sliding along the line (five values and
+// three (13/12) e^2 live at a time).  The f+ side of a run is a = f+ at the
+// first face's stencil start, s = the pencil stride; its f- side is a = f- at
+// (start + 7 s), s = -stride, and yields the faces in reverse order.
+__device__ __forceinline__ void wenoz_run3(const double* a, int s, double& o0, double& o1, double& o2) {
+    double A0 = a[0], A1 = a[s], A2 = a[2 * s], A3 = a[3 * s], A4 = a[4 * s];
+    double E0 = wenoz_e2(A0, A1, A2), E1 = wenoz_e2(A1, A2, A3), E2 = wenoz_e2(A2, A3, A4);
+#pragma unroll 1
+    for (int m = 0; m < 3; ++m) {
+        const double v = wenoz_face_e(A0, A1, A2, A3, A4, E0, E1, E2);
+        if (m == 0) o0 = v;
+        else if (m == 1) o1 = v;
+        else o2 = v;
+        if (m < 2) {
+            A0 = A1;
+            A1 = A2;
+            A2 = A3;
+            A3 = A4;
+            A4 = a[(m + 5) * s];
+            E0 = E1;
+            E1 = E2;
+            E2 = wenoz_e2(A2, A3, A4);
+        }
+    }
+}
+#endif
+
+#if defined(__CUDACC__)
 // c2prim (Source/kernel/Kernels.H:13-40) for the fused FP64 kernels: the two
 // divisions become one reciprocal of rho (T = p (1/rho) (1/Rg), 1/Rg formed once
 // on the host); the same values to within a few ulps.

@@ -401,11 +401,58 @@ __device__ __forceinline__ void sweep(const RegBoxArgs& B, const DevParm& P, int
     }
     __syncthreads();
     // ---- 2. WENO-Z face fluxes
-    for (int it = tid; it < 5 * PC::NF; it += NT) {
-        const int n = it / PC::NF, f = it - n * PC::NF;
-        const int fx = f % PC::FX, fy = (f / PC::FX) % PC::FY, fz = f / (PC::FX * PC::FY);
-        const int base = fx + fy * PC::PX + fz * PC::PX * PC::PY;
-        FF[n * PC::NF + f] = Prec<FT>::weno(F + n * PC::N + base, F + (5 + n) * PC::N + base, PC::PST);
+    if constexpr (std::is_same<FT, double>::value) {
+        // FP64: a work item is a run of three consecutive faces of a line along
+        // D (component n); runs start every three faces, the last one at FD - 3
+        // so that every stencil stays in the pencil, and a run writes only the
+        // faces from its own start on
+        constexpr int FD = D == 0 ? PC::FX : (D == 1 ? PC::FY : PC::FZ);
+        constexpr int NLINE = PC::NF / FD, NRUN = (FD + 2) / 3;
+        static_assert(FD >= 3, "runs of three faces");
+        for (int it = tid; it < 5 * NLINE * NRUN; it += NT) {
+            const int n = it / (NLINE * NRUN), r = it - n * (NLINE * NRUN);
+            const int line = r / NRUN, run = r - line * NRUN;
+            const int fw = 3 * run, f0 = fw < FD - 3 ? fw : FD - 3;
+            int fx, fy, fz;
+            if (D == 0) {
+                fx = f0; fy = line % PC::FY; fz = line / PC::FY;
+            } else if (D == 1) {
+                fx = line % PC::FX; fy = f0; fz = line / PC::FX;
+            } else {
+                fx = line % PC::FX; fy = line / PC::FX; fz = f0;
+            }
+            const int f = fx + fy * PC::FX + fz * PC::FX * PC::FY;
+            const int base = fx + fy * PC::PX + fz * PC::PX * PC::PY;
+            // f+ then f- (one side's registers at a time); the face flux is
+            // f+ + f- as in the reference
+            // f+ (side 0) then f- (side 1, faces in reverse order), one side's
+            // window live at a time; the face flux is f+ + f-
+            double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+            FT* out = FF + n * PC::NF + f;
+#pragma unroll 1
+            for (int side = 0; side < 2; ++side) {
+                const double* a = side == 0 ? F + n * PC::N + base : F + (5 + n) * PC::N + base + 7 * PC::PST;
+                const int st = side == 0 ? PC::PST : -PC::PST;
+                double o0, o1, o2;
+                wenoz_run3(a, st, o0, o1, o2);
+                if (side == 0) {
+                    p0 = o0;
+                    p1 = o1;
+                    p2 = o2;
+                } else {
+                    if (f0 >= fw) out[0] = __dadd_rn(p0, o2);
+                    if (f0 + 1 >= fw) out[PC::FST] = __dadd_rn(p1, o1);
+                    out[2 * PC::FST] = __dadd_rn(p2, o0);
+                }
+            }
+        }
+    } else {
+        for (int it = tid; it < 5 * PC::NF; it += NT) {
+            const int n = it / PC::NF, f = it - n * PC::NF;
+            const int fx = f % PC::FX, fy = (f / PC::FX) % PC::FY, fz = f / (PC::FX * PC::FY);
+            const int base = fx + fy * PC::PX + fz * PC::PX * PC::PY;
+            FF[n * PC::NF + f] = Prec<FT>::weno(F + n * PC::N + base, F + (5 + n) * PC::N + base, PC::PST);
+        }
     }
     __syncthreads();
     // ---- 3. viscous part of the face flux
@@ -622,6 +669,7 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
 // measured faster than two without spills and than four with 32 registers)
 template <class FT, int TX, int TY, int TZ, bool VISC, bool XS>
 __host__ __device__ constexpr int regular_min_blocks() {
+    if (std::is_same<FT, double>::value) return 1;  // the FP64 WENO-Z runs hold a sliding window
     const int b = (int)((228u * 1024u) / (regular_smem_bytes<FT, TX, TY, TZ, VISC, XS>() + 1024u));
     const int t = 2048 / (TX * TY * TZ);
     int m = b < t ? b : t;
