@@ -1312,7 +1312,7 @@ def main():
                     help="jet-eb-amr: time the headline form only (no other forms, no L1 run); for profiling")
     ap.add_argument("--sur-epochs", type=int, default=6, help="react: surrogate training epochs")
     ap.add_argument("--l1-time", type=float, default=None,
-                    help="dmr-amr: matched L1 of a whole run from t = 0 to this time (configs[1] names 0.2) in "
+                    help="dmr-amr: matched L1 of a whole run from t = 0 to this time (the double Mach reflection's end time is 0.2) in "
                          "place of the 20 coarse steps from the developed state")
     args = ap.parse_args()
     if args.warmup < 3:
