@@ -210,9 +210,55 @@ constexpr int EBQ_X = EBT_X + 4, EBQ_Y = EBT_Y + 4, EBQ_Z = EBT_Z + 4, EBQ_N = E
 constexpr int EBF_N0 = (EBT_X + 1) * EBT_Y * EBT_Z, EBF_N1 = EBT_X * (EBT_Y + 1) * EBT_Z,
               EBF_N2 = EBT_X * EBT_Y * (EBT_Z + 1);
 
+// Inviscid stages keep only the cross of the tile - the tile and 2 cells on
+// each side along x, y and z, the cells the faces' MUSCL stencils read - and 6
+// primitive planes (the Van Leer flux reads no temperature): 768 cells against
+// 1152 of grow(tile, 2).  The viscous stage (FP64) keeps grow(tile, 2) whole
+// and 7 planes (its face stress reads transverse neighbours).
+constexpr int EBX_NC = EBT_X * EBT_Y * EBT_Z, EBX_NX = 4 * EBT_Y * EBT_Z, EBX_NY = 4 * EBT_X * EBT_Z,
+              EBX_NZ = 4 * EBT_X * EBT_Y, EBX_N = EBX_NC + EBX_NX + EBX_NY + EBX_NZ;
+
 template <bool F32>
-__host__ __device__ constexpr size_t ebt_smem_bytes() {
-    return (F32 ? sizeof(float) : sizeof(double)) * (7 * EBQ_N + 5 * (EBF_N0 + EBF_N1 + EBF_N2));
+__host__ __device__ constexpr size_t ebt_smem_bytes(bool visc = true) {
+    return (F32 ? sizeof(float) : sizeof(double)) *
+           ((visc ? 7 * EBQ_N : 6 * EBX_N) + 5 * (EBF_N0 + EBF_N1 + EBF_N2));
+}
+
+// primitive plane of component m (cross layout: no temperature plane)
+__device__ __forceinline__ int ebt_plane(bool cross, int m) { return cross && m > QT ? m - 1 : m; }
+
+// shared-memory index of tile-local cell (x, y, z), -2 <= x < EBT_X + 2 etc.;
+// in the cross layout at most one coordinate lies outside the tile
+__device__ __forceinline__ int ebt_q(bool cross, int x, int y, int z) {
+    if (!cross) return (x + 2) + (y + 2) * EBQ_X + (z + 2) * EBQ_X * EBQ_Y;
+    if (x < 0 || x >= EBT_X) return EBX_NC + (x < 0 ? x + 2 : x - EBT_X + 2) + 4 * (y + EBT_Y * z);
+    if (y < 0 || y >= EBT_Y) return EBX_NC + EBX_NX + x + EBT_X * ((y < 0 ? y + 2 : y - EBT_Y + 2) + 4 * z);
+    if (z < 0 || z >= EBT_Z) return EBX_NC + EBX_NX + EBX_NY + x + EBT_X * (y + EBT_Y * (z < 0 ? z + 2 : z - EBT_Z + 2));
+    return x + EBT_X * (y + EBT_Y * z);
+}
+
+// tile-local cell of index c of the cross layout (the inverse of ebt_q)
+__device__ __forceinline__ void ebt_cross_cell(int c, int& x, int& y, int& z) {
+    if (c < EBX_NC) {
+        x = c % EBT_X;
+        y = (c / EBT_X) % EBT_Y;
+        z = c / (EBT_X * EBT_Y);
+    } else if (c < EBX_NC + EBX_NX) {
+        const int r = c - EBX_NC, h = r % 4;
+        y = (r / 4) % EBT_Y;
+        z = r / (4 * EBT_Y);
+        x = h < 2 ? h - 2 : EBT_X + h - 2;
+    } else if (c < EBX_NC + EBX_NX + EBX_NY) {
+        const int r = c - EBX_NC - EBX_NX, h = (r / EBT_X) % 4;
+        x = r % EBT_X;
+        z = r / (4 * EBT_X);
+        y = h < 2 ? h - 2 : EBT_Y + h - 2;
+    } else {
+        const int r = c - EBX_NC - EBX_NX - EBX_NY, h = r / (EBT_X * EBT_Y);
+        x = r % EBT_X;
+        y = (r / EBT_X) % EBT_Y;
+        z = h < 2 ? h - 2 : EBT_Z + h - 2;
+    }
 }
 
 // faces of direction D of the tile at (i0, j0, k0) of box B into sf (5 x EBF_N[D])
@@ -224,13 +270,18 @@ __device__ __forceinline__ void ebt_faces(const EbStageArgs& A, const EbStageBox
     using FT = typename std::conditional<F32, float, double>::type;
     constexpr int FX = EBT_X + (D == 0), FY = EBT_Y + (D == 1), FZ = EBT_Z + (D == 2), NF = FX * FY * FZ;
     constexpr int di = D == 0, dj = D == 1, dk = D == 2;
-    constexpr int SD = D == 0 ? 1 : (D == 1 ? EBQ_X : EBQ_X * EBQ_Y);
+    const bool cross = !A.visc;
+    const int NP = cross ? EBX_N : EBQ_N;
     for (int f = threadIdx.x; f < NF; f += EBT_N) {
         const int fx = f % FX, fy = (f / FX) % FY, fz = f / (FX * FY);
         const int i = i0 + fx, j = j0 + fy, k = k0 + fz;
         if (i > B.hi[0] + di || j > B.hi[1] + dj || k > B.hi[2] + dk) continue;
         const uint32_t fl = B.flag(i, j, k);
-        const FT* p0 = sq + (fx + 2) + (fy + 2) * EBQ_X + (fz + 2) * EBQ_X * EBQ_Y;
+        // the face's four stencil cells along D (offsets -2, -1, 0, +1)
+        const int s0 = ebt_q(cross, fx - 2 * di, fy - 2 * dj, fz - 2 * dk);
+        const int s1 = ebt_q(cross, fx - di, fy - dj, fz - dk);
+        const int s2 = ebt_q(cross, fx, fy, fz);
+        const int s3 = ebt_q(cross, fx + di, fy + dj, fz + dk);
         double flx[5];
         if (F32) {
             const bool cm1 = eb_conn(fl, -di, -dj, -dk), cm2 = eb_conn(fl, -2 * di, -2 * dj, -2 * dk),
@@ -242,8 +293,8 @@ __device__ __forceinline__ void ebt_faces(const EbStageArgs& A, const EbStageBox
                     ql[m] = qr[m] = 0.0f;
                     continue;
                 }
-                const FT* pm = p0 + m * EBQ_N;
-                const float vm2 = pm[-2 * SD], vm1 = pm[-SD], v0 = pm[0], vp1 = pm[SD];
+                const FT* pm = sq + ebt_plane(cross, m) * NP;
+                const float vm2 = pm[s0], vm1 = pm[s1], v0 = pm[s2], vp1 = pm[s3];
                 float l = vm1, r = v0;
                 if (cm1) {
                     if (cm2) l = vm1 + 0.5f * minmod<float>(v0 - vm1, vm1 - vm2);
@@ -266,8 +317,8 @@ __device__ __forceinline__ void ebt_faces(const EbStageArgs& A, const EbStageBox
                     ql[m] = qr[m] = 0.0;
                     continue;
                 }
-                const FT* pm = p0 + m * EBQ_N;
-                eb_recon(fl, D, (double)pm[-2 * SD], (double)pm[-SD], (double)pm[0], (double)pm[SD], ql[m], qr[m]);
+                const FT* pm = sq + ebt_plane(cross, m) * NP;
+                eb_recon(fl, D, (double)pm[s0], (double)pm[s1], (double)pm[s2], (double)pm[s3], ql[m], qr[m]);
             }
             vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
             if (A.visc) {
@@ -303,7 +354,9 @@ __global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __
     using FT = typename std::conditional<F32, float, double>::type;
     extern __shared__ __align__(16) unsigned char ebt_raw[];
     FT* sq = reinterpret_cast<FT*>(ebt_raw);
-    FT* sf0 = sq + 7 * EBQ_N;
+    const bool cross = !A.visc;
+    const int NP = cross ? EBX_N : EBQ_N;
+    FT* sf0 = sq + (cross ? 6 * EBX_N : 7 * EBQ_N);
     FT* sf1 = sf0 + 5 * EBF_N0;
     FT* sf2 = sf1 + 5 * EBF_N1;
     const double dt = *A.dt_ptr;
@@ -322,10 +375,18 @@ __global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __
               k0 = B.lo[2] + (t / (ntx * nty)) * EBT_Z;
     const int tid = threadIdx.x;
     if (!B.covered) {
-        // 1. primitives over grow(tile, 2) (within the box's grow(bx, 2))
-        for (int c = tid; c < EBQ_N; c += EBT_N) {
-            const int qx = c % EBQ_X, qy = (c / EBQ_X) % EBQ_Y, qz = c / (EBQ_X * EBQ_Y);
-            const int i = i0 - 2 + qx, j = j0 - 2 + qy, k = k0 - 2 + qz;
+        // 1. primitives over the tile's cross (inviscid) or grow(tile, 2)
+        // (viscous), within the box's grow(bx, 2)
+        for (int c = tid; c < NP; c += EBT_N) {
+            int qx, qy, qz;
+            if (cross) {
+                ebt_cross_cell(c, qx, qy, qz);
+            } else {
+                qx = c % EBQ_X - 2;
+                qy = (c / EBQ_X) % EBQ_Y - 2;
+                qz = c / (EBQ_X * EBQ_Y) - 2;
+            }
+            const int i = i0 + qx, j = j0 + qy, k = k0 + qz;
             if (i > B.hi[0] + 2 || j > B.hi[1] + 2 || k > B.hi[2] + 2) continue;
             if (F32) {
                 const float g = P.f_gamma;
@@ -336,19 +397,19 @@ __global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __
                 const float rhoinv = __frcp_rn(rho);
                 const float ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
                 const float p = fmaxf((g - 1.0f) * (u4 - rho * (0.5f * (ux * ux + uy * uy + uz * uz))), P.f_smallp);
-                sq[QRHO * EBQ_N + c] = rho;
-                sq[QU * EBQ_N + c] = ux;
-                sq[QV * EBQ_N + c] = uy;
-                sq[QW * EBQ_N + c] = uz;
-                sq[QPRES * EBQ_N + c] = p;
-                sq[QT * EBQ_N + c] = 0.0f;
-                sq[QC * EBQ_N + c] = sqrtf(g * p * rhoinv);
+                sq[QRHO * NP + c] = rho;
+                sq[QU * NP + c] = ux;
+                sq[QV * NP + c] = uy;
+                sq[QW * NP + c] = uz;
+                sq[QPRES * NP + c] = p;
+                sq[ebt_plane(cross, QC) * NP + c] = sqrtf(g * p * rhoinv);
             } else {
                 double q[7];
                 c2prim_ideal_fast(P, B.S(i, j, k, 0), B.S(i, j, k, 1), B.S(i, j, k, 2), B.S(i, j, k, 3),
                                   B.S(i, j, k, 4), q);
 #pragma unroll
-                for (int m = 0; m < 7; ++m) sq[m * EBQ_N + c] = q[m];
+                for (int m = 0; m < 7; ++m)
+                    if (!(cross && m == QT)) sq[ebt_plane(cross, m) * NP + c] = q[m];
             }
         }
         __syncthreads();
@@ -366,7 +427,7 @@ __global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __
         const int fxl = ti + tj * (EBT_X + 1) + tk * (EBT_X + 1) * EBT_Y;
         const int fyl = ti + tj * EBT_X + tk * EBT_X * (EBT_Y + 1);
         const int fzl = ti + tj * EBT_X + tk * EBT_X * EBT_Y;
-        const int qc = (ti + 2) + (tj + 2) * EBQ_X + (tk + 2) * EBQ_X * EBQ_Y;
+        const int qc = ebt_q(cross, ti, tj, tk);  // the cell in the primitive planes
         auto FXm = [&](int m) { return sf0[m * EBF_N0 + fxl]; };
         auto FXp = [&](int m) { return sf0[m * EBF_N0 + fxl + 1]; };
         auto FYm = [&](int m) { return sf1[m * EBF_N1 + fyl]; };
@@ -394,7 +455,7 @@ __global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __
                     for (int m = 0; m < 5; ++m)
                         out[m] = tmp * (axp * (float)FXp(m) - axm * (float)FXm(m) + ayp * (float)FYp(m) -
                                         aym * (float)FYm(m) + azp * (float)FZp(m) - azm * (float)FZm(m));
-                    const float pr = (float)sq[QPRES * EBQ_N + qc];
+                    const float pr = (float)sq[QPRES * NP + qc];
                     out[1] += (axm - axp) * pr * tmp;
                     out[2] += (aym - ayp) * pr * tmp;
                     out[3] += (azm - azp) * pr * tmp;
@@ -424,7 +485,7 @@ __global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __
                         out[m] = tmp * (axp * (double)FXp(m) - axm * (double)FXm(m) + ayp * (double)FYp(m) -
                                         aym * (double)FYm(m) + azp * (double)FZp(m) - azm * (double)FZm(m));
                     double fw[5];
-                    const double pr = (double)sq[QPRES * EBQ_N + qc];
+                    const double pr = (double)sq[QPRES * NP + qc];
                     if (!A.visc) {
                         // slip-wall pressure flux, EBkernels.H:305-311
                         fw[0] = 0.0;
@@ -434,9 +495,9 @@ __global__ void __launch_bounds__(EBT_N) k_ebl_tile(EbStageArgs A, const int* __
                         fw[4] = 0.0;
                     } else {
                         // eb_wallflux, EBkernels.H:173-214
-                        const double d = (double)sq[QRHO * EBQ_N + qc], u = (double)sq[QU * EBQ_N + qc],
-                                     v = (double)sq[QV * EBQ_N + qc], w = (double)sq[QW * EBQ_N + qc],
-                                     cs = (double)sq[QC * EBQ_N + qc];
+                        const double d = (double)sq[QRHO * NP + qc], u = (double)sq[QU * NP + qc],
+                                     v = (double)sq[QV * NP + qc], w = (double)sq[QW * NP + qc],
+                                     cs = (double)sq[QC * NP + qc];
                         const double apnorm = sqrt((axm - axp) * (axm - axp) + (aym - ayp) * (aym - ayp) +
                                                    (azm - azp) * (azm - azp));
                         const double un = u * (axm - axp) + v * (aym - ayp) + w * (azm - azp);
@@ -818,8 +879,8 @@ ocfd_status eb_launch_stage(ocfd_level* L, int s, unsigned flags, cudaStream_t s
     A.redist = E->desc.redistribute ? 1 : 0;
     const bool f32 = (flags & OCFD_FLUX_FP32) && !A.visc;
     auto go = [&](const EbStageArgs& X, const int* tstart, int ntiles) {
-        if (f32) k_ebl_tile<true><<<ntiles, EBT_N, ebt_smem_bytes<true>(), st>>>(X, tstart, L->ctx->parm);
-        else k_ebl_tile<false><<<ntiles, EBT_N, ebt_smem_bytes<false>(), st>>>(X, tstart, L->ctx->parm);
+        if (f32) k_ebl_tile<true><<<ntiles, EBT_N, ebt_smem_bytes<true>(A.visc), st>>>(X, tstart, L->ctx->parm);
+        else k_ebl_tile<false><<<ntiles, EBT_N, ebt_smem_bytes<false>(A.visc), st>>>(X, tstart, L->ctx->parm);
     };
     if (flags & OCFD_PER_BOX) {
         // one launch per box (the reference's per-box execution model), the same kernel
