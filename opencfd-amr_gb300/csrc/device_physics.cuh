@@ -133,74 +133,63 @@ __device__ __forceinline__ double rcp_nr(double x) {
     return fma(r, e, r);
 }
 
-// WENO-Z of one split flux (Source/kernel/Reconstruction.H:83-138), the stencil
-// V1..V5 ordered towards the face (f+: cells i-3..i+1; f-: cells i+2..i-2, i.e.
-// wenoz_minus(V1..V5) == wenoz_1rcp(V5, V4, V3, V2, V1)), with a single
-// reciprocal instead of the reference's four divisions: the weights
-// alpha_k = d_k (1 + (tau / D_k)^2), D_k = eps + beta_k, d = (1, 6, 3), are
-// multiplied by the common positive factor (D_1 D_2 D_3)^2, which cancels in
-// alpha_k / sum alpha, giving a_k = d_k (D_k^2 + tau^2) prod_{j != k} D_j^2.  The
-// same weights up to rounding (parity tests: 1e-12 per right-hand side); the
-// products stay finite for |beta| < 1e51, i.e. flux differences below ~1e25.
-__device__ __forceinline__ double wenoz_1rcp(double V1, double V2, double V3, double V4, double V5) {
-    const double eps = 1e-6;
-    const double e1 = V1 - 2.0 * V2 + V3, g1 = V1 - 4.0 * V2 + 3.0 * V3;
-    const double e2 = V2 - 2.0 * V3 + V4, g2 = V2 - V4;
-    const double e3 = V3 - 2.0 * V4 + V5, g3 = 3.0 * V3 - 4.0 * V4 + V5;
-    const double b1 = (13.0 / 12.0) * e1 * e1 + 0.25 * g1 * g1;
-    const double b2 = (13.0 / 12.0) * e2 * e2 + 0.25 * g2 * g2;
-    const double b3 = (13.0 / 12.0) * e3 * e3 + 0.25 * g3 * g3;
-    const double tau = fabs(b1 - b3);
-    const double D1 = eps + b1, D2 = eps + b2, D3 = eps + b3;
-    const double q1 = D1 * D1, q2 = D2 * D2, q3 = D3 * D3, t2 = tau * tau;
-    const double a1 = (q1 + t2) * (q2 * q3);
-    const double a2 = 6.0 * (q2 + t2) * (q1 * q3);
-    const double a3 = 3.0 * (q3 + t2) * (q1 * q2);
-    const double v1 = 2.0 * V1 - 7.0 * V2 + 11.0 * V3;
-    const double v2 = -V2 + 5.0 * V3 + 2.0 * V4;
-    const double v3 = 2.0 * V3 + 5.0 * V4 - V5;
-    return (a1 * v1 + a2 * v2 + a3 * v3) * rcp_nr(6.0 * (a1 + a2 + a3));
-}
-#endif
-
-#if defined(__CUDACC__)
-// WENO-Z of three consecutive faces of a pencil line (the FP64 regular-box
-// kernel's work item), the arithmetic of wenoz_1rcp with every rounding written
-// out.  The second differences e = V1 - 2 V2 + V3 of the smoothness indicators
-// and their (13/12) e^2 belong to a cell triple, and a triple serves as
-// stencil 1, 2 and 3 of three consecutive faces: a run of three faces forms
-// five of them instead of nine.
+// WENO-Z of one split flux (Source/kernel/Reconstruction.H:83-138) with a
+// single reciprocal in place of the reference's four divisions, in the
+// fewest FP64 operations (GB300 issues two FP64 instructions per cycle per SM).
+// The stencil V1..V5 is ordered towards the face (f+: cells i-3..i+1; f-:
+// cells i+2..i-2, i.e. wenoz_minus(V1..V5) == wenoz_1rcp(V5, V4, V3, V2, V1)).
+//   - The smoothness indicators are carried as 4 beta_k = (13/3) e_k^2 + g_k^2
+//     (e, g the second and first differences of the reference's beta_k), with
+//     eps -> 4 eps: tau / (eps + beta_k) is unchanged, and the scaling by 4 is
+//     exact.
+//   - The weights alpha_k = d_k (1 + (tau / D_k)^2), D_k = eps + beta_k,
+//     d = (1, 6, 3), are multiplied by the common positive factor
+//     (D_1 D_2 D_3)^2, which cancels in alpha_k / sum alpha: with q_k = D_k^2
+//     and P = q_1 q_2 q_3, alpha_k becomes d_k A_k, A_k = P + tau^2 q_j q_l
+//     ({j, l} the other two).
+//   - The face value sum_k alpha_k v_k / (6 sum_k alpha_k), v_k the candidate
+//     polynomials (2, -7, 11), (-1, 5, 2), (2, 5, -1), is formed as
+//     (A_1 v_1 / 6 + A_2 v_2 + A_3 v_3 / 2) / (A_1 + 6 A_2 + 3 A_3), the 1/6 and
+//     the d_k folded into the polynomials' coefficients.
+// The same value up to rounding (parity tests: 1e-12 per right-hand side); the
+// products stay finite for |beta| < 2e50, i.e. flux differences below ~1e25.
+//
+// The second differences' (13/3) e^2 belong to a cell triple, and a triple
+// serves as stencil 1, 2 and 3 of three consecutive faces: wenoz_run3 forms
+// five of them for a run of three faces instead of nine.
 __device__ __forceinline__ double wenoz_e2(double Va, double Vb, double Vc) {
     const double e = __dadd_rn(__fma_rn(-2.0, Vb, Va), Vc);
-    return __dmul_rn(__dmul_rn(13.0 / 12.0, e), e);
+    return __dmul_rn(__dmul_rn(13.0 / 3.0, e), e);
 }
 // one side's face from its stencil V1..V5 (ordered towards the face) and the
-// (13/12) e^2 of its triples (V1 V2 V3), (V2 V3 V4), (V3 V4 V5)
+// (13/3) e^2 of its triples (V1 V2 V3), (V2 V3 V4), (V3 V4 V5); every rounding
+// written out, so the value does not depend on the code around the call
 __device__ __forceinline__ double wenoz_face_e(double V1, double V2, double V3, double V4, double V5, double E1,
                                                double E2, double E3) {
-    const double eps = 1e-6;
+    const double eps4 = 4e-6;
     const double g1 = __fma_rn(3.0, V3, __fma_rn(-4.0, V2, V1));
     const double g2 = __dsub_rn(V2, V4);
-    const double g3 = __dadd_rn(__fma_rn(-4.0, V4, __dmul_rn(3.0, V3)), V5);
-    const double b1 = __fma_rn(__dmul_rn(0.25, g1), g1, E1);
-    const double b2 = __fma_rn(__dmul_rn(0.25, g2), g2, E2);
-    const double b3 = __fma_rn(__dmul_rn(0.25, g3), g3, E3);
+    const double g3 = __fma_rn(-4.0, V4, __fma_rn(3.0, V3, V5));
+    const double b1 = __fma_rn(g1, g1, E1), b2 = __fma_rn(g2, g2, E2), b3 = __fma_rn(g3, g3, E3);
     const double tau = fabs(__dsub_rn(b1, b3));
-    const double D1 = __dadd_rn(eps, b1), D2 = __dadd_rn(eps, b2), D3 = __dadd_rn(eps, b3);
+    const double D1 = __dadd_rn(eps4, b1), D2 = __dadd_rn(eps4, b2), D3 = __dadd_rn(eps4, b3);
     const double q1 = __dmul_rn(D1, D1), q2 = __dmul_rn(D2, D2), q3 = __dmul_rn(D3, D3), t2 = __dmul_rn(tau, tau);
-    const double a1 = __dmul_rn(__dadd_rn(q1, t2), __dmul_rn(q2, q3));
-    const double a2 = __dmul_rn(__dmul_rn(6.0, __dadd_rn(q2, t2)), __dmul_rn(q1, q3));
-    const double a3 = __dmul_rn(__dmul_rn(3.0, __dadd_rn(q3, t2)), __dmul_rn(q1, q2));
-    const double v1 = __fma_rn(11.0, V3, __fma_rn(-7.0, V2, __dmul_rn(2.0, V1)));
-    const double v2 = __fma_rn(2.0, V4, __fma_rn(5.0, V3, -V2));
-    const double v3 = __dsub_rn(__fma_rn(5.0, V4, __dmul_rn(2.0, V3)), V5);
-    const double num = __fma_rn(a3, v3, __fma_rn(a2, v2, __dmul_rn(a1, v1)));
-    const double den = __dmul_rn(6.0, __dadd_rn(__dadd_rn(a1, a2), a3));
+    const double q12 = __dmul_rn(q1, q2), q13 = __dmul_rn(q1, q3), q23 = __dmul_rn(q2, q3);
+    const double Pq = __dmul_rn(q12, q3);
+    const double A1 = __fma_rn(t2, q23, Pq), A2 = __fma_rn(t2, q13, Pq), A3 = __fma_rn(t2, q12, Pq);
+    const double c1 = __fma_rn(11.0 / 6.0, V3, __fma_rn(-7.0 / 6.0, V2, __dmul_rn(1.0 / 3.0, V1)));
+    const double c2 = __fma_rn(2.0, V4, __fma_rn(5.0, V3, -V2));
+    const double c3 = __fma_rn(-0.5, V5, __fma_rn(2.5, V4, V3));
+    const double num = __fma_rn(A3, c3, __fma_rn(A2, c2, __dmul_rn(A1, c1)));
+    const double den = __fma_rn(3.0, A3, __fma_rn(6.0, A2, A1));
     return __dmul_rn(num, rcp_nr(den));
+}
+__device__ __forceinline__ double wenoz_1rcp(double V1, double V2, double V3, double V4, double V5) {
+    return wenoz_face_e(V1, V2, V3, V4, V5, wenoz_e2(V1, V2, V3), wenoz_e2(V2, V3, V4), wenoz_e2(V3, V4, V5));
 }
 // one side of faces m = 0, 1, 2 whose stencils (ordered towards the face) are
 // a[m s] .. a[(m + 4) s], as a window sliding along the line (five values and
-// three (13/12) e^2 live at a time).  The f+ side of a run is a = f+ at the
+// three (13/3) e^2 live at a time).  The f+ side of a run is a = f+ at the
 // first face's stencil start, s = the pencil stride; its f- side is a = f- at
 // (start + 7 s), s = -stride, and yields the faces in reverse order.
 __device__ __forceinline__ void wenoz_run3(const double* a, int s, double& o0, double& o1, double& o2) {

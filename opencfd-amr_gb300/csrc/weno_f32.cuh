@@ -28,62 +28,67 @@ __device__ __forceinline__ float2 p_set(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 p_rcp(float2 a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
 
 // Normalisation of a face's two stencils by one power of two: the scale sc,
-// its inverse and the epsilon in normalised units.  Zero / subnormal stencils,
-// and inf / NaN, are reconstructed as they are (sc = 1, epsilon 1e-6).
-__device__ __forceinline__ void wenoz_scale(float m, float& sc, float& inv, float& eps) {
+// its inverse and 4 epsilon in normalised units (the smoothness indicators are
+// carried as 4 beta, see wenoz_pm_f).  Zero / subnormal stencils, and inf /
+// NaN, are reconstructed as they are (sc = 1, epsilon 1e-6).
+__device__ __forceinline__ void wenoz_scale(float m, float& sc, float& inv, float& eps4) {
     const int ex = (__float_as_int(m) >> 23) & 0xff;
     const bool plain = ex == 0 || ex > 250;
     sc = plain ? 1.0f : __int_as_float((254 - ex) << 23);   // 2^-(ex-127)
     inv = plain ? 1.0f : __int_as_float(ex << 23);          // 2^(ex-127)
-    // 1e-6 absolute, in normalised units; kept > 0 so that 0/0 cannot occur
-    eps = plain ? 1e-6f : fmaxf(1e-6f * sc * sc, 1e-37f);
+    // 4 x 1e-6 absolute, in normalised units; kept > 0 so that 0/0 cannot occur
+    eps4 = plain ? 4e-6f : fmaxf(4e-6f * sc * sc, 4e-37f);
 }
 
 // f+ at cells i-3..i+1 (a1..a5) plus f- at i+2..i-2 (b1..b5, the mirrored
-// stencil): the WENO-Z face flux
+// stencil): the WENO-Z face flux.  The smoothness indicators are carried as
+// 4 beta_k = (13/3) d_k^2 + e_k^2 with the epsilon scaled by 4 (an exact
+// scaling that leaves tau / (eps + beta_k) unchanged), and with the weights
+// alpha_k = d_k W_k, W_k = 1 + (tau / (eps + beta_k))^2, d = (1, 6, 3), the face
+// value sum alpha_k v_k / (6 sum alpha_k) is formed as
+// (W_1 v_1 / 6 + W_2 v_2 + W_3 v_3 / 2) / (W_1 + 6 W_2 + 3 W_3), the 1/6 and
+// the d_k folded into the candidate polynomials' coefficients.
 __device__ __forceinline__ float wenoz_pm_f(float a1, float a2, float a3, float a4, float a5, float b1,
                                             float b2, float b3, float b4, float b5) {
     const float ma = fmaxf(fmaxf(fmaxf(fabsf(a1), fabsf(a2)), fmaxf(fabsf(a3), fabsf(a4))), fabsf(a5));
     const float mb = fmaxf(fmaxf(fmaxf(fabsf(b1), fabsf(b2)), fmaxf(fabsf(b3), fabsf(b4))), fabsf(b5));
-    float s, iv, e;
-    wenoz_scale(fmaxf(ma, mb), s, iv, e);
-    const float2 sc = p_set(s), eps = p_set(e);
+    float s, iv, e4;
+    wenoz_scale(fmaxf(ma, mb), s, iv, e4);
+    const float2 sc = p_set(s), eps4 = p_set(e4);
     const float2 V1 = p_mul(make_float2(a1, b1), sc), V2 = p_mul(make_float2(a2, b2), sc),
                  V3 = p_mul(make_float2(a3, b3), sc), V4 = p_mul(make_float2(a4, b4), sc),
                  V5 = p_mul(make_float2(a5, b5), sc);
-    const float2 c1312 = p_set(13.0f / 12.0f), cq = p_set(0.25f), m1 = p_set(-1.0f), m2 = p_set(-2.0f),
-                 m4 = p_set(-4.0f), c2 = p_set(2.0f), c3 = p_set(3.0f), c5 = p_set(5.0f);
-    // Jiang-Shu smoothness indicators (Reconstruction.H:70-139)
+    const float2 c133 = p_set(13.0f / 3.0f), m1 = p_set(-1.0f), m2 = p_set(-2.0f), m4 = p_set(-4.0f),
+                 c2 = p_set(2.0f), c3 = p_set(3.0f), c5 = p_set(5.0f);
+    // Jiang-Shu smoothness indicators (Reconstruction.H:70-139), times 4
     const float2 d1 = p_fma(m2, V2, p_add(V1, V3));           // V1 - 2 V2 + V3
     const float2 e1 = p_fma(c3, V3, p_fma(m4, V2, V1));       // V1 - 4 V2 + 3 V3
-    const float2 s1 = p_fma(p_mul(c1312, d1), d1, p_mul(p_mul(cq, e1), e1));
+    const float2 s1 = p_fma(p_mul(c133, d1), d1, p_mul(e1, e1));
     const float2 d2 = p_fma(m2, V3, p_add(V2, V4));           // V2 - 2 V3 + V4
     const float2 e2 = p_fma(m1, V4, V2);                      // V2 - V4
-    const float2 s2 = p_fma(p_mul(c1312, d2), d2, p_mul(p_mul(cq, e2), e2));
+    const float2 s2 = p_fma(p_mul(c133, d2), d2, p_mul(e2, e2));
     const float2 d3 = p_fma(m2, V4, p_add(V3, V5));           // V3 - 2 V4 + V5
     const float2 e3 = p_fma(c3, V3, p_fma(m4, V4, V5));       // 3 V3 - 4 V4 + V5
-    const float2 s3 = p_fma(p_mul(c1312, d3), d3, p_mul(p_mul(cq, e3), e3));
+    const float2 s3 = p_fma(p_mul(c133, d3), d3, p_mul(e3, e3));
     // tau / (eps + beta) with tau = |beta_1 - beta_3|, capped at 1e18: a stencil
     // side that is exactly flat (beta = 0) next to a jump gives tau / eps, which
     // for |V| above ~1e5 in normalised units of a small eps would overflow
     // (1 + r^2) in FP32; at the cap that side's weight already dominates the
     // others by > 1e30
     const float2 tau = p_fma(m1, s3, s1);
-    float2 r1 = p_mul(tau, p_rcp(p_add(eps, s1))), r2 = p_mul(tau, p_rcp(p_add(eps, s2))),
-           r3 = p_mul(tau, p_rcp(p_add(eps, s3)));
+    float2 r1 = p_mul(tau, p_rcp(p_add(eps4, s1))), r2 = p_mul(tau, p_rcp(p_add(eps4, s2))),
+           r3 = p_mul(tau, p_rcp(p_add(eps4, s3)));
     r1 = make_float2(fminf(fabsf(r1.x), 1e18f), fminf(fabsf(r1.y), 1e18f));
     r2 = make_float2(fminf(fabsf(r2.x), 1e18f), fminf(fabsf(r2.y), 1e18f));
     r3 = make_float2(fminf(fabsf(r3.x), 1e18f), fminf(fabsf(r3.y), 1e18f));
-    // alpha_k = d_k (1 + r_k^2), d = (1, 6, 3) / 10 (the 1/10 cancels)
     const float2 one = p_set(1.0f);
-    const float2 w1 = p_fma(r1, r1, one), w2 = p_mul(p_set(6.0f), p_fma(r2, r2, one)),
-                 w3 = p_mul(c3, p_fma(r3, r3, one));
-    // candidate stencils, times 6
-    const float2 v1 = p_fma(p_set(11.0f), V3, p_fma(p_set(-7.0f), V2, p_mul(c2, V1)));
+    const float2 w1 = p_fma(r1, r1, one), w2 = p_fma(r2, r2, one), w3 = p_fma(r3, r3, one);
+    // candidate stencils v_1 / 6, v_2, v_3 / 2
+    const float2 v1 = p_fma(p_set(11.0f / 6.0f), V3, p_fma(p_set(-7.0f / 6.0f), V2, p_mul(p_set(1.0f / 3.0f), V1)));
     const float2 v2 = p_fma(c2, V4, p_fma(c5, V3, p_mul(m1, V2)));
-    const float2 v3 = p_fma(m1, V5, p_fma(c5, V4, p_mul(c2, V3)));
+    const float2 v3 = p_fma(p_set(-0.5f), V5, p_fma(p_set(2.5f), V4, V3));
     const float2 num = p_fma(w1, v1, p_fma(w2, v2, p_mul(w3, v3)));
-    const float2 den = p_mul(p_set(6.0f), p_add(w1, p_add(w2, w3)));
+    const float2 den = p_fma(c3, w3, p_fma(p_set(6.0f), w2, w1));
     const float2 f = p_mul(num, p_rcp(den));
     return (f.x + f.y) * iv;
 }
