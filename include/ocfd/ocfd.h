@@ -72,7 +72,8 @@ typedef struct ocfd_box {
 
 /* Parm, Source/Constants.H:7-64 (CHEM member set).  Table pointers may be NULL
  * (the built-in Li-Dryer tables of Source/Constants.cpp:15-150 are used) or
- * point to host or device memory holding the reference's table layout. */
+ * point to host or device memory holding the reference's table layout.  The
+ * floors smallr and smallp must be >= 0 (ocfd_context_create: OCFD_BAD_ARG). */
 typedef struct ocfd_parm {
     double eos_gamma, eos_m, Patm;
     double cv, cp, Ru, Rg, kOverMu;

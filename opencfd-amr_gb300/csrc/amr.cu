@@ -509,7 +509,7 @@ __global__ void k_estdt_into(const FabGeom* __restrict__ fabs, const long long* 
                              long long total, const double* __restrict__ U, DevParm P, double dx0, double dx1,
                              double dx2, unsigned long long* out) {
     const double dx[3] = {dx0, dx1, dx2};
-    double m = __longlong_as_double(0x7FF0000000000000LL);
+    CflSpeeds spd;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
         const int b = find_tag<FabGeom>(start, nbox, idx);
@@ -519,10 +519,9 @@ __global__ void k_estdt_into(const FabGeom* __restrict__ fabs, const long long* 
         const long long c = fab_index(f, i, j, k);
         double u[5];
         for (int n = 0; n < 5; ++n) u[n] = U[c + n * f.ns];
-        const double v = cfl_bound(P, u, dx);
-        m = v < m ? v : m;
+        spd.add(P, u);
     }
-    block_min_atomic(m, out);
+    block_cfl_atomic(spd, dx, out);
 }
 
 // ================================================================ hierarchy

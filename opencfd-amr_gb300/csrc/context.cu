@@ -78,6 +78,9 @@ DevParm make_dev_parm(const ocfd_parm& p) {
     d.sw_tmp3 = (3.0 - g) / (2.0 * (g - 1.0));
     d.sw_gm1 = g - 1;
     d.invRg = 1.0 / d.Rg;
+    d.vl_rg = 1.0 / d.gamma;
+    d.vl_rg21 = 1.0 / (2.0 * (d.gamma * d.gamma - 1.0));
+    d.vl_ggm1 = d.gamma * (1.0 / (d.gamma - 1.0));
     d.f_gamma = (float)d.gamma;
     d.f_smallr = (float)d.smallr;
     d.f_smallp = (float)d.smallp;
@@ -90,6 +93,11 @@ DevParm make_dev_parm(const ocfd_parm& p) {
     d.f_sw_tmp2 = (float)d.sw_tmp2;
     d.f_sw_tmp3 = (float)d.sw_tmp3;
     d.f_sw_gm1 = (float)d.sw_gm1;
+    // as the FP32 faces formed them from the rounded gamma
+    const float fg = d.f_gamma;
+    d.f_vl_rg = 1.0f / fg;
+    d.f_vl_rg21 = 1.0f / (2.0f * (fg * fg - 1.0f));
+    d.f_vl_ggm1 = fg * (1.0f / (fg - 1.0f));
     return d;
 }
 
@@ -124,6 +132,10 @@ ocfd_status ocfd_parm_default(ocfd_parm* p) {
 
 ocfd_status ocfd_context_create(const ocfd_parm* parm, int device, ocfd_context** out) {
     if (!parm || !out) return fail(OCFD_BAD_ARG, "ocfd_context_create: null argument");
+    // the kernels apply the density and pressure floors by integer compares,
+    // which order doubles correctly against a non-negative floor
+    if (!(parm->smallr >= 0.0) || !(parm->smallp >= 0.0))
+        return fail(OCFD_BAD_ARG, "ocfd_context_create: smallr and smallp must be >= 0");
     *out = nullptr;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {

@@ -216,25 +216,83 @@ __device__ __forceinline__ void wenoz_run3(const double* a, int s, double& o0, d
 #endif
 
 #if defined(__CUDACC__)
-// c2prim (Source/kernel/Kernels.H:13-40) for the fused FP64 kernels: the two
-// divisions become one reciprocal of rho (T = p (1/rho) (1/Rg), 1/Rg formed once
-// on the host); the same values to within a few ulps.
+// The positive and negative parts the reference forms as (x + |x|)/2 and
+// x - (x + |x|)/2 (FluxSplit.H:46-51) are exactly x or +0 (and -0 for the
+// negative part of -0): selected on the sign bit, on the integer pipes.
+__device__ __forceinline__ double pos_part(double x) { return __double_as_longlong(x) > 0 ? x : 0.0; }
+__device__ __forceinline__ double neg_part(double x) { return __double_as_longlong(x) < 0 ? x : 0.0; }
+
+// Steger-Warming split along D (Source/kernel/FluxSplit.H:11-193) for the fused
+// FP64 kernels, in fewer FP64 operations than sw_split's reference order: with
+// un the normal and ua, ub the tangential velocities, qt = ua^2 + ub^2 is shared
+// by the three |.|^2 terms, the energy flux's E2 vvc1 + E3 vvc2 + w2 (E2 + E3)
+// is E2 (vvc1 + w2) + E3 (vvc2 + w2), and the tangential momentum fluxes are
+// the mass flux times the velocity.  The eigenvalue parts are exact selects.
+// The same values up to rounding (parity tests: 1e-12 per right-hand side);
+// every rounding is written out, so the fluxes of a cell do not depend on the
+// code around the call.
+template <int D>
+__device__ __forceinline__ void sw_split_d(double d, double u, double v, double w, double c, double t1, double t2,
+                                           double t3, double gm1, double* fp, double* fm) {
+    const double vel[3] = {u, v, w};
+    const double un = vel[D], ua = vel[(D + 1) % 3], ub = vel[(D + 2) % 3];
+    const double qt = __fma_rn(ub, ub, __dmul_rn(ua, ua));
+    const double uc1 = __dsub_rn(un, c), uc2 = __dadd_rn(un, c);
+    const double w2 = __dmul_rn(__dmul_rn(t3, c), c);
+    const double v2 = __dmul_rn(gm1, __fma_rn(un, un, qt));
+    const double h1 = __fma_rn(0.5, __fma_rn(uc1, uc1, qt), w2);  // vvc1 + w2
+    const double h2 = __fma_rn(0.5, __fma_rn(uc2, uc2, qt), w2);  // vvc2 + w2
+    const double E1P = pos_part(un), E2P = pos_part(uc1), E3P = pos_part(uc2);
+    const double E1M = neg_part(un), E2M = neg_part(uc1), E3M = neg_part(uc2);
+    const double t0 = __dmul_rn(d, t1);
+    const double a1p = __dmul_rn(t2, E1P), a1m = __dmul_rn(t2, E1M);
+    const double rp = __dmul_rn(t0, __dadd_rn(__dadd_rn(a1p, E2P), E3P));
+    const double rm = __dmul_rn(t0, __dadd_rn(__dadd_rn(a1m, E2M), E3M));
+    fp[URHO] = rp;
+    fm[URHO] = rm;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        if (m == D) {
+            fp[UMX + m] = __dmul_rn(t0, __fma_rn(E3P, uc2, __fma_rn(E2P, uc1, __dmul_rn(a1p, un))));
+            fm[UMX + m] = __dmul_rn(t0, __fma_rn(E3M, uc2, __fma_rn(E2M, uc1, __dmul_rn(a1m, un))));
+        } else {
+            fp[UMX + m] = __dmul_rn(rp, vel[m]);
+            fm[UMX + m] = __dmul_rn(rm, vel[m]);
+        }
+    }
+    fp[UEDEN] = __dmul_rn(t0, __fma_rn(E3P, h2, __fma_rn(E2P, h1, __dmul_rn(E1P, v2))));
+    fm[UEDEN] = __dmul_rn(t0, __fma_rn(E3M, h2, __fma_rn(E2M, h1, __dmul_rn(E1M, v2))));
+}
+#endif
+
+#if defined(__CUDACC__)
+// max(a, b) for b > 0 (the density and pressure floors) on the integer pipes:
+// a double's bits read as a signed integer order as the double does against a
+// positive b, a negative a or -0 reading below it (NaN a is the only case that
+// differs from a > b ? a : b)
+__device__ __forceinline__ double max_floor(double a, double b) {
+    return __double_as_longlong(a) > __double_as_longlong(b) ? a : b;
+}
+
+// c2prim (Source/kernel/Kernels.H:13-40) for the fused FP64 kernels, in fewer
+// FP64 operations: the two divisions become one reciprocal of rho
+// (T = p (1/rho) (1/Rg), 1/Rg formed once on the host), the floors are integer
+// compares, rho |u|^2 is formed as the momenta times the velocities, and
+// c^2 = gamma Rg T as gamma p (1/rho); the same values to within a few ulps.
 __device__ __forceinline__ void c2prim_ideal_fast(const DevParm& P, double u0, double u1, double u2, double u3,
                                                   double u4, double* q) {
-    const double rho = dmax(u0, P.smallr);
+    const double rho = max_floor(u0, P.smallr);
     const double rhoinv = rcp_nr(rho);
     const double ux = u1 * rhoinv, uy = u2 * rhoinv, uz = u3 * rhoinv;
-    const double kineng = 0.5 * (ux * ux + uy * uy + uz * uz);
-    const double ei = u4 - rho * kineng;
-    const double p = dmax((P.gamma - 1.0) * ei, P.smallp);
-    const double T = p * rhoinv * P.invRg;
+    const double ei = fma(-0.5, fma(u3, uz, fma(u2, uy, u1 * ux)), u4);
+    const double p = max_floor((P.gamma - 1.0) * ei, P.smallp);
     q[QRHO] = rho;
     q[QU] = ux;
     q[QV] = uy;
     q[QW] = uz;
     q[QPRES] = p;
-    q[QT] = T;
-    q[QC] = sqrt(P.gamma * P.Rg * T);
+    q[QT] = p * rhoinv * P.invRg;
+    q[QC] = sqrt(P.gamma * p * rhoinv);
 }
 #endif
 

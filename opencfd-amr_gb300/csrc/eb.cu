@@ -68,7 +68,7 @@ __global__ void k_eb_faces(EbBoxArgs B, DevParm P) {
                      q(i, j, k, m), q(i + di, j + dj, k + dk, m), ql[m], qr[m]);
         }
         double flx[5];
-        vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
+        vanleer_g<double>(P.smallp, P.gamma, P.vl_rg, P.vl_rg21, P.vl_ggm1, ql, qr, D, flx);
         if (B.visc) eb_visc_face(P, q, B.flag, D, i, j, k, B.dxinv, flx, 1, false, 0, 0, 0);
 #pragma unroll
         for (int m = 0; m < 5; ++m) B.flux[D](i, j, k, m) = flx[m];

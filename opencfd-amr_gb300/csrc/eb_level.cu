@@ -303,7 +303,7 @@ __device__ __forceinline__ void ebt_faces(const EbStageArgs& A, const EbStageBox
                 ql[m] = l;
                 qr[m] = r;
             }
-            vanleer<float>(P.f_smallp, P.f_gamma, ql, qr, D, ff);
+            vanleer_g<float>(P.f_smallp, P.f_gamma, P.f_vl_rg, P.f_vl_rg21, P.f_vl_ggm1, ql, qr, D, ff);
 #pragma unroll
             for (int m = 0; m < 5; ++m) {
                 sf[m * NF + f] = ff[m];
@@ -320,7 +320,7 @@ __device__ __forceinline__ void ebt_faces(const EbStageArgs& A, const EbStageBox
                 const FT* pm = sq + ebt_plane(cross, m) * NP;
                 eb_recon(fl, D, (double)pm[s0], (double)pm[s1], (double)pm[s2], (double)pm[s3], ql[m], qr[m]);
             }
-            vanleer<double>(P.smallp, P.gamma, ql, qr, D, flx);
+            vanleer_g<double>(P.smallp, P.gamma, P.vl_rg, P.vl_rg21, P.vl_ggm1, ql, qr, D, flx);
             if (A.visc) {
                 const View<const double> qv{reinterpret_cast<const double*>(sq), EBQ_X, (long long)EBQ_X * EBQ_Y,
                                             EBQ_N, i0 - 2, j0 - 2, k0 - 2};

@@ -23,6 +23,18 @@ __device__ __forceinline__ T minmod(T a, T b) {
     if (a * b > 0) return fabs(a) > fabs(b) ? b : a;
     return T(0);
 }
+// FP64: the same selections with both tests on the integer pipes (GB300's FP64
+// pipe, two instructions per cycle per SM, also executes FP64 comparisons).
+// The bit pattern of a double read as a signed integer is positive exactly when
+// the double is positive and non-zero, and |x|'s bits order as |x| does; NaN
+// operands, which the flow never carries, are the only ones selected otherwise.
+template <>
+__device__ __forceinline__ double minmod<double>(double a, double b) {
+    const long long mag = 0x7fffffffffffffffLL;
+    if (__double_as_longlong(a * b) > 0)
+        return (__double_as_longlong(a) & mag) > (__double_as_longlong(b) & mag) ? b : a;
+    return 0.0;
+}
 
 // eb_recon_x/y/z for one component: left/right states at the D-face of cell c
 // given the values at c-2e, c-e, c, c+e and the flag of c.
@@ -47,16 +59,19 @@ template <>
 __device__ __forceinline__ float recip<float>(float x) { return 1.0f / x; }
 
 // Van Leer flux vector splitting, Source/EB/EBkernels.H:73-171.  The reference's
-// divisions (two Mach numbers, /gamma per momentum component, /(2(g^2-1)),
-// g/(g-1)) become four reciprocals per face; the same values to within a few
-// ulps (FP64 parity of the cut-cell paths: 1e-12 per right-hand side).
+// divisions become two reciprocals per face (the Mach numbers) and three
+// constants of gamma: rg = 1/gamma (the /gamma of the normal momentum),
+// rg21 = 1/(2(gamma^2 - 1)) and ggm1 = gamma/(gamma - 1); the same values to
+// within a few ulps (FP64 parity of the cut-cell paths: 1e-12 per right-hand
+// side).  The ideal-gas paths pass the constants formed once on the host
+// (DevParm::vl_*); vanleer() forms them per face for a face-varying gamma.
 template <class T>
-__device__ __forceinline__ void vanleer(T smallp, T gamma, const T* ql, const T* qr, int D, T* flx) {
+__device__ __forceinline__ void vanleer_g(T smallp, T gamma, T rg, T rg21, T ggm1, const T* ql, const T* qr, int D,
+                                          T* flx) {
     T fp[5] = {0, 0, 0, 0, 0}, fm[5] = {0, 0, 0, 0, 0};
     const T dl = ql[QRHO], ul = ql[QU], vl = ql[QV], wl = ql[QW], pl = ql[QPRES] > smallp ? ql[QPRES] : smallp;
     const T dr = qr[QRHO], ur = qr[QU], vr = qr[QV], wr = qr[QW], pr = qr[QPRES] > smallp ? qr[QPRES] : smallp;
     const T cL = ql[QC], cR = qr[QC];
-    const T rg = recip<T>(gamma), rg21 = recip<T>(2 * (gamma * gamma - 1)), ggm1 = gamma * recip<T>(gamma - T(1));
     const int nn[3] = {D == 0, D == 1, D == 2};
     const T UL = D == 0 ? ul : (D == 1 ? vl : wl);
     const T UR = D == 0 ? ur : (D == 1 ? vr : wr);
@@ -92,6 +107,11 @@ __device__ __forceinline__ void vanleer(T smallp, T gamma, const T* ql, const T*
     }
 #pragma unroll
     for (int n = 0; n < 5; ++n) flx[n] = fp[n] + fm[n];
+}
+template <class T>
+__device__ __forceinline__ void vanleer(T smallp, T gamma, const T* ql, const T* qr, int D, T* flx) {
+    vanleer_g<T>(smallp, gamma, recip<T>(gamma), recip<T>(2 * (gamma * gamma - 1)), gamma * recip<T>(gamma - T(1)),
+                 ql, qr, D, flx);
 }
 
 // connectivity-aware transverse derivative of component `m` of q along t at the

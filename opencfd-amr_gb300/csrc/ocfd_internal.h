@@ -19,11 +19,13 @@ struct DevParm {
     double sw_tmp1, sw_tmp2, sw_tmp3;  // 1/(2g), 2(g-1), (3-g)/(2(g-1)): FluxSplit.H:31-34
     double sw_gm1;                     // (g - 1) as written `(gamma - 1)` in FluxSplit.H:41
     double invRg;                      // 1 / Rg
+    double vl_rg, vl_rg21, vl_ggm1;    // 1/g, 1/(2(g^2-1)), g/(g-1): the Van Leer flux (EBkernels.H:73-171)
     double grav;                       // 0, or g = -9.8 when a call asks for OCFD_GRAVITY
     uint32_t* err;                     // the context's device error word (bit 1: a bounded wait ran out)
     // the same constants rounded to FP32 once on the host, for the mixed form
     float f_gamma, f_smallr, f_smallp, f_invRg, f_C_s, f_T_s, f_kOverMu, f_twoThirds;
     float f_sw_tmp1, f_sw_tmp2, f_sw_tmp3, f_sw_gm1;
+    float f_vl_rg, f_vl_rg21, f_vl_ggm1;
 };
 
 // Device view of an Array4 (same addressing as amrex::Array4).

@@ -121,6 +121,66 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* t
     }
 }
 
+// The CFL bound over many cells, min over cells of min_d dx_d / (|v_d| + c)
+// (Source/Advance.cpp:26-49), kept as the three largest signal speeds
+// s_d = |v_d| + c: correctly rounded division is monotone in the divisor, so the
+// minimum over cells of dx_d / s_d is exactly dx_d / max s_d, and a block divides
+// three times instead of three times per cell (GB300's FP64 pipe executes the
+// divisions).  The speeds follow the reference's expression with every rounding
+// written out (no contraction), so the bound is the correctly rounded value of
+// that expression on any host or device.
+struct CflSpeeds {
+    double s[3] = {0.0, 0.0, 0.0};
+    __device__ __forceinline__ void add(const DevParm& P, const double* u) {
+        const double rho = u[0];
+        const double rhoinv = __ddiv_rn(1.0, rho > P.smallr ? rho : P.smallr);
+        const double vx = __dmul_rn(u[1], rhoinv), vy = __dmul_rn(u[2], rhoinv), vz = __dmul_rn(u[3], rhoinv);
+        const double ke = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+        const double pe = __dmul_rn(__dsub_rn(P.gamma, 1.0), __dsub_rn(u[4], __dmul_rn(__dmul_rn(0.5, rho), ke)));
+        const double p = pe > P.smallp ? pe : P.smallp;
+        const double cs = __dsqrt_rn(__dmul_rn(__dmul_rn(P.gamma, p), rhoinv));
+        s[0] = fmax(s[0], __dadd_rn(fabs(vx), cs));
+        s[1] = fmax(s[1], __dadd_rn(fabs(vy), cs));
+        s[2] = fmax(s[2], __dadd_rn(fabs(vz), cs));
+    }
+};
+
+// block-wide CFL bound from the threads' largest speeds (all threads
+// participate), one atomicMin per block; a block without cells adds +inf
+__device__ __forceinline__ void block_cfl_atomic(const CflSpeeds& c, const double* dx, unsigned long long* target) {
+    __shared__ double red[3][32];
+    double s0 = c.s[0], s1 = c.s[1], s2 = c.s[2];
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 = fmax(s0, __shfl_xor_sync(0xffffffffu, s0, o));
+        s1 = fmax(s1, __shfl_xor_sync(0xffffffffu, s1, o));
+        s2 = fmax(s2, __shfl_xor_sync(0xffffffffu, s2, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][warp] = s0;
+        red[1][warp] = s1;
+        red[2][warp] = s2;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        s0 = lane < nw ? red[0][lane] : 0.0;
+        s1 = lane < nw ? red[1][lane] : 0.0;
+        s2 = lane < nw ? red[2][lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 = fmax(s0, __shfl_xor_sync(0xffffffffu, s0, o));
+            s1 = fmax(s1, __shfl_xor_sync(0xffffffffu, s1, o));
+            s2 = fmax(s2, __shfl_xor_sync(0xffffffffu, s2, o));
+        }
+        if (lane == 0) {
+            const double tx = dx[0] / s0, ty = dx[1] / s1, tz = dx[2] / s2;
+            const double m = ty < tz ? ty : tz;
+            const double v = tx < m ? tx : m;
+            if (v >= 0.0) atomicMin(target, (unsigned long long)__double_as_longlong(v));
+        }
+    }
+}
+
 // g of the gravity source, Source/Advance.cpp:332
 constexpr double kGravity = -9.8;
 

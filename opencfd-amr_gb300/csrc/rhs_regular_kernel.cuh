@@ -148,7 +148,7 @@ struct Prec<double> {
     }
     template <int D>
     static __device__ __forceinline__ void split(const DevParm& P, const double* q, double* fp, double* fm) {
-        sw_split<D>(q[QRHO], q[QU], q[QV], q[QW], q[QC], P.sw_tmp1, P.sw_tmp2, P.sw_tmp3, P.sw_gm1, fp, fm);
+        sw_split_d<D>(q[QRHO], q[QU], q[QV], q[QW], q[QC], P.sw_tmp1, P.sw_tmp2, P.sw_tmp3, P.sw_gm1, fp, fm);
     }
     static __device__ __forceinline__ double weno(const double* a, const double* b, int s) {
         return wenoz_1rcp(a[0], a[s], a[2 * s], a[3 * s], a[4 * s]) +

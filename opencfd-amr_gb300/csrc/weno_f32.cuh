@@ -93,8 +93,12 @@ __device__ __forceinline__ float wenoz_pm_f(float a1, float a2, float a3, float 
     return (f.x + f.y) * iv;
 }
 
-// Steger-Warming split in FP32 (FluxSplit.H:11-193, the same terms as
-// sw_split) with every rounding written out: __fmul_rn / __fadd_rn / __fsub_rn
+// Steger-Warming split in FP32 (FluxSplit.H:11-193) in the grouping of the FP64
+// sw_split_d: qt = ua^2 + ub^2 of the tangential velocities shared by the
+// |.|^2 terms, the energy flux as E1 v2 + E2 (vvc1 + w2) + E3 (vvc2 + w2), the
+// tangential momentum fluxes as the mass flux times the velocity, and the
+// eigenvalue parts (x + |x|)/2, x - (x + |x|)/2 as the exact max(x, 0),
+// min(x, 0).  Every rounding is written out: __fmul_rn / __fadd_rn / __fsub_rn
 // are never fused and __fmaf_rn always is, so the compiler has no choice left
 // and the fluxes of a cell do not depend on the code around the call (primitives
 // formed inline or reloaded from shared memory split to the same values).
@@ -102,37 +106,33 @@ template <int D>
 __device__ __forceinline__ void sw_split_f32(float d, float u, float v, float w, float c, float t1, float t2,
                                              float t3, float gm1, float* fp, float* fm) {
     const float vel[3] = {u, v, w};
-    const float un = vel[D];
+    const float un = vel[D], ua = vel[(D + 1) % 3], ub = vel[(D + 2) % 3];
+    const float qt = __fmaf_rn(ub, ub, __fmul_rn(ua, ua));
     const float uc1 = __fsub_rn(un, c), uc2 = __fadd_rn(un, c);
-    float a0 = u, a1 = v, a2 = w, b0 = u, b1 = v, b2 = w;
-    if (D == 0) { a0 = uc1; b0 = uc2; }
-    if (D == 1) { a1 = uc1; b1 = uc2; }
-    if (D == 2) { a2 = uc1; b2 = uc2; }
-    const float vvc1 = __fmul_rn(0.5f, __fmaf_rn(a2, a2, __fmaf_rn(a1, a1, __fmul_rn(a0, a0))));
-    const float vvc2 = __fmul_rn(0.5f, __fmaf_rn(b2, b2, __fmaf_rn(b1, b1, __fmul_rn(b0, b0))));
-    const float v2 = __fmul_rn(gm1, __fmaf_rn(w, w, __fmaf_rn(v, v, __fmul_rn(u, u))));
     const float w2 = __fmul_rn(__fmul_rn(t3, c), c);
-    const float E1P = __fmul_rn(__fadd_rn(un, fabsf(un)), 0.5f), E2P = __fmul_rn(__fadd_rn(uc1, fabsf(uc1)), 0.5f),
-                E3P = __fmul_rn(__fadd_rn(uc2, fabsf(uc2)), 0.5f);
-    const float E1M = __fsub_rn(un, E1P), E2M = __fsub_rn(uc1, E2P), E3M = __fsub_rn(uc2, E3P);
+    const float v2 = __fmul_rn(gm1, __fmaf_rn(un, un, qt));
+    const float h1 = __fmaf_rn(0.5f, __fmaf_rn(uc1, uc1, qt), w2);
+    const float h2 = __fmaf_rn(0.5f, __fmaf_rn(uc2, uc2, qt), w2);
+    const float E1P = fmaxf(un, 0.0f), E2P = fmaxf(uc1, 0.0f), E3P = fmaxf(uc2, 0.0f);
+    const float E1M = fminf(un, 0.0f), E2M = fminf(uc1, 0.0f), E3M = fminf(uc2, 0.0f);
     const float t0 = __fmul_rn(d, t1);
-    const float sp = __fadd_rn(__fmaf_rn(t2, E1P, E2P), E3P), sm = __fadd_rn(__fmaf_rn(t2, E1M, E2M), E3M);
-    fp[0] = __fmul_rn(t0, sp);
-    fm[0] = __fmul_rn(t0, sm);
+    const float a1p = __fmul_rn(t2, E1P), a1m = __fmul_rn(t2, E1M);
+    const float rp = __fmul_rn(t0, __fadd_rn(__fadd_rn(a1p, E2P), E3P));
+    const float rm = __fmul_rn(t0, __fadd_rn(__fadd_rn(a1m, E2M), E3M));
+    fp[0] = rp;
+    fm[0] = rm;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         if (m == D) {
-            fp[1 + m] = __fmul_rn(t0, __fmaf_rn(E3P, uc2, __fmaf_rn(E2P, uc1, __fmul_rn(__fmul_rn(t2, E1P), un))));
-            fm[1 + m] = __fmul_rn(t0, __fmaf_rn(E3M, uc2, __fmaf_rn(E2M, uc1, __fmul_rn(__fmul_rn(t2, E1M), un))));
+            fp[1 + m] = __fmul_rn(t0, __fmaf_rn(E3P, uc2, __fmaf_rn(E2P, uc1, __fmul_rn(a1p, un))));
+            fm[1 + m] = __fmul_rn(t0, __fmaf_rn(E3M, uc2, __fmaf_rn(E2M, uc1, __fmul_rn(a1m, un))));
         } else {
-            fp[1 + m] = __fmul_rn(__fmul_rn(t0, vel[m]), sp);
-            fm[1 + m] = __fmul_rn(__fmul_rn(t0, vel[m]), sm);
+            fp[1 + m] = __fmul_rn(rp, vel[m]);
+            fm[1 + m] = __fmul_rn(rm, vel[m]);
         }
     }
-    fp[4] = __fmul_rn(t0, __fmaf_rn(w2, __fadd_rn(E2P, E3P),
-                                     __fmaf_rn(E3P, vvc2, __fmaf_rn(E2P, vvc1, __fmul_rn(E1P, v2)))));
-    fm[4] = __fmul_rn(t0, __fmaf_rn(w2, __fadd_rn(E2M, E3M),
-                                     __fmaf_rn(E3M, vvc2, __fmaf_rn(E2M, vvc1, __fmul_rn(E1M, v2)))));
+    fp[4] = __fmul_rn(t0, __fmaf_rn(E3P, h2, __fmaf_rn(E2P, h1, __fmul_rn(E1P, v2))));
+    fm[4] = __fmul_rn(t0, __fmaf_rn(E3M, h2, __fmaf_rn(E2M, h1, __fmul_rn(E1M, v2))));
 }
 
 // Conversions between FP64 and FP32 on the integer pipes.  GB300 runs FP64

@@ -84,3 +84,16 @@ def test_no_device_fails_loudly(L):
     with pytest.raises(ocfd.OcfdError) as e:
         ocfd.Context()
     assert e.value.status == 6
+
+
+def test_negative_floor_rejected(L):
+    """The density / pressure floors must be >= 0 (the kernels compare against
+    them on the integer bits): checked before any device work, so on any host."""
+    import ocfd
+    from ocfd.context import default_parm
+    for field in ("smallr", "smallp"):
+        p = default_parm()
+        setattr(p, field, -1e-10)
+        with pytest.raises(ocfd.OcfdError) as e:
+            ocfd.Context(parm=p)
+        assert e.value.status == 1, field  # OCFD_BAD_ARG

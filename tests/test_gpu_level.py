@@ -77,6 +77,17 @@ def test_sod_vs_oracle(ctx, oracle):
     assert relerr(got, ref) < 1e-10
 
 
+def test_first_dt_is_the_oracles(ctx, oracle):
+    """The time step from the initial state, over boxes of several blocks, is the
+    oracle's estdt bit for bit (the GPU reduces the largest signal speeds and
+    divides once per block; correctly rounded division is monotone)."""
+    from ocfd.cases import dmr, sod
+    for case, grid in ((sod(64, 16, 4), (16, 8, 4)), (dmr(64, 16, 2), (24, 5, 2))):
+        _, tr = run_oracle(oracle, case, 1, 0.5)
+        _, tg = run_gpu(ctx, case, 1, 0.5, grid)
+        assert tg == tr
+
+
 def test_box_split_is_bit_identical(ctx):
     from ocfd.cases import sod
     case = sod(64, 16, 4)

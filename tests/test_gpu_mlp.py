@@ -121,8 +121,9 @@ def test_mlp_forward_throughput(ctx):
     """Rate of the network on the tensor cores: 2^20 rows through the five
     layers (2 (12 128 + 3 128^2 + 128 10) = 103,936 FLOP per row with the first
     layer's K padded to 16), the training forward with its stash of Z and H,
-    timed with CUDA events after a warm-up.  The figure is printed; the bound
-    only catches a broken pipeline."""
+    timed with CUDA events after a warm-up, the best of three trials of five
+    passes (the GPU may be shared for a moment).  The figure is printed; the
+    bound only catches a broken pipeline, and no bounded wait may have run out."""
     import torch
     M = 1 << 20
     net = make_mlp(ctx, max_batch=M, seed=7)
@@ -130,14 +131,18 @@ def test_mlp_forward_throughput(ctx):
     Y = net.forward(X)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 5
-    e0.record()
-    for _ in range(reps):
-        Y = net.forward(X)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
+    reps, trials = 5, []
+    for _ in range(3):
+        e0.record()
+        for _ in range(reps):
+            Y = net.forward(X)
+        e1.record()
+        torch.cuda.synchronize()
+        trials.append(e0.elapsed_time(e1) / reps)
+    ms = min(trials)
     tflops = 103936.0 * M / (ms * 1e-3) / 1e12
-    print("mlp forward: %.3f ms per 2^20 rows, %.1f TFLOP/s" % (ms, tflops))
+    print("mlp forward: %.3f ms per 2^20 rows, %.1f TFLOP/s (trials %s ms)" %
+          (ms, tflops, ", ".join("%.2f" % t for t in trials)))
     assert torch.isfinite(Y).all()
+    assert ctx.check() == 0
     assert tflops > 5.0
