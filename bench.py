@@ -616,7 +616,15 @@ def run_ours_jet(args, world, rank, local):
     torch.cuda.nvtx.range_push("bench_roofline_stage")
     reg_ms, reg_cells = fin.profile_regular(0, reps=10)
     reg_ms32, _ = fin.profile_regular(ocfd.FLUX_FP32, reps=10)
+    # the whole stage of the finest level: its regular boxes' tile kernel, then
+    # the cut and covered boxes' tile kernel
+    stage_ms = {"fp64": fin.profile_stage(0, reps=10), "fp32": fin.profile_stage(ocfd.FLUX_FP32, reps=10)}
     torch.cuda.nvtx.range_pop()
+    fin_stage = {"cells": fin.cells(), "regular_cells": reg_cells, "cut_and_covered_cells": fin.cells() - reg_cells,
+                 "fp64": {"stage_ms": stage_ms["fp64"], "regular_ms": reg_ms,
+                          "cut_ms": stage_ms["fp64"] - reg_ms},
+                 "fp32": {"stage_ms": stage_ms["fp32"], "regular_ms": reg_ms32,
+                          "cut_ms": stage_ms["fp32"] - reg_ms32}}
     hbm_peak, peak_src = peaks()
     fp64 = ctypes.c_double(); fp32 = ctypes.c_double(); fp32x2 = ctypes.c_double()
     ocfd.check(ocfd.load().ocfd_measure_fma_peaks(ctypes.byref(fp64), ctypes.byref(fp32)))
@@ -674,6 +682,7 @@ def run_ours_jet(args, world, rank, local):
                                           "fp32_fma_peak_gflops": fp32.value,
                                           "frac_of_fp32_fma_peak": flops32 / fp32.value}},
                        "speedup_batched_over_per_box_fp64": (value / vpb) if vpb else None,
+                       "finest_level_stage": fin_stage,
                        "kernels_per_coarse_step": {"fp64_batched": kernels / args.steps,
                                                    "fp64_per_box": k_p / max(1, min(args.steps, 3))},
                        "autotuned_tile_sched_per_level": tuned,

@@ -24,15 +24,17 @@ __device__ __forceinline__ T minmod(T a, T b) {
     return T(0);
 }
 // FP64: the same selections with both tests on the integer pipes (GB300's FP64
-// pipe, two instructions per cycle per SM, also executes FP64 comparisons).
-// The bit pattern of a double read as a signed integer is positive exactly when
-// the double is positive and non-zero, and |x|'s bits order as |x| does; NaN
-// operands, which the flow never carries, are the only ones selected otherwise.
+// pipe, two instructions per cycle per SM, also executes FP64 multiplies and
+// comparisons).  a b > 0 is: both non-zero with equal sign bits; |x|'s bits order
+// as |x| does.  The selections differ from the reference's only for NaN operands,
+// which the flow never carries, and where a b underflows to 0 (|a b| below
+// 5e-324), where the slope selected is below the last bit of any state value.
 template <>
 __device__ __forceinline__ double minmod<double>(double a, double b) {
     const long long mag = 0x7fffffffffffffffLL;
-    if (__double_as_longlong(a * b) > 0)
-        return (__double_as_longlong(a) & mag) > (__double_as_longlong(b) & mag) ? b : a;
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & mag, mb = ib & mag;
+    if ((ia ^ ib) >= 0 && ma != 0 && mb != 0) return ma > mb ? b : a;
     return 0.0;
 }
 

@@ -30,6 +30,10 @@
 // per cell (Q), and each direction's pencil is split from Q.  The primitives of
 // a cell are the same function of the same state either way, so the results
 // are bit-identical to the pencil-by-pencil form.
+// FP64 inviscid tiles (CrossPlain) keep the same cross of primitives in FP64,
+// formed once per cell with plain loads (no TMA: one CTA per SM is resident, and
+// its loads are the FP64 pipe's shadow), where the cross and the pencil region
+// fit a CTA's shared memory.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -120,6 +124,20 @@ struct Cross {
     }
 };
 
+// FP64 inviscid tiles keep the same cross of primitives (layout Cross, FP64
+// values) behind the pencil region, formed once per cell with plain loads, where
+// the two fit a CTA's shared memory (one 512-thread CTA per SM: registers, not
+// shared memory, bound the FP64 tiles)
+template <int TX, int TY, int TZ>
+__host__ __device__ constexpr size_t cross_plain_bytes() {
+    return sizeof(double) * (pencil_elems<TX, TY, TZ>() + 5 * (size_t)Cross<TX, TY, TZ>::NQ);
+}
+template <class FT, int TX, int TY, int TZ, bool VISC>
+struct CrossPlain {
+    static constexpr bool value =
+        std::is_same<FT, double>::value && !VISC && cross_plain_bytes<TX, TY, TZ>() <= kMaxSmem;
+};
+
 template <class FT, int TX, int TY, int TZ>
 __host__ __device__ constexpr size_t cross_region_a() {
     const size_t st = 8 * (size_t)Cross<TX, TY, TZ>::NSTAGE;
@@ -131,6 +149,7 @@ template <class FT, int TX, int TY, int TZ, bool VISC, bool XS = false>
 __host__ __device__ constexpr size_t regular_smem_bytes() {
     if (CrossOn<FT, TX, TY, TZ, VISC, XS>::value)
         return 128 + cross_region_a<FT, TX, TY, TZ>() + sizeof(float) * 5 * Cross<TX, TY, TZ>::NQ;
+    if (CrossPlain<FT, TX, TY, TZ, VISC>::value) return cross_plain_bytes<TX, TY, TZ>();
     return sizeof(FT) * (pencil_elems<TX, TY, TZ>() + (VISC ? 4 * Ring<TX, TY, TZ>::N : 0));
 }
 
@@ -332,6 +351,55 @@ __device__ __forceinline__ void cross_prims(const RegBoxArgs& B, const DevParm& 
         } else if (gi <= B.hi[0] + 3 && gj <= B.hi[1] + 3 && (B.zvirt || gk <= B.hi[2] + 3)) {
             int sg;
             Prec<float>::prims(P, B.S, gi, gj, zmap(B, gk, sg), q);
+            if (sg & 1) q[QU] = -q[QU];
+            if (sg & 2) q[QV] = -q[QV];
+            if (sg & 4) q[QW] = -q[QW];
+        }
+        Q[idx] = q[QRHO];
+        Q[C::NQ + idx] = q[QU];
+        Q[2 * C::NQ + idx] = q[QV];
+        Q[3 * C::NQ + idx] = q[QW];
+        Q[4 * C::NQ + idx] = q[QC];
+    }
+}
+
+// Primitives of an FP64 tile's cross into Q (layout Cross, FP64 values), once
+// per cell, with plain loads: the same cells, mirrored z ghosts and bounds as
+// cross_prims (cells beyond hi + 3 are left 0; the sweeps never use them), and
+// the same function of the state as the pencil-by-pencil form, so the sweeps
+// give the same bits either way.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void cross_prims_plain(const RegBoxArgs& B, const DevParm& P, int i0, int j0, int k0,
+                                                  double* Q) {
+    using C = Cross<TX, TY, TZ>;
+    constexpr int NT = TX * TY * TZ;
+    for (int idx = threadIdx.x; idx < C::NQ; idx += NT) {
+        int x, y, z;
+        if (idx < C::NC) {
+            x = idx % TX;
+            y = (idx / TX) % TY;
+            z = idx / (TX * TY);
+        } else if (idx < C::NC + C::NXH) {
+            const int r = idx - C::NC, h = r % 6;
+            y = (r / 6) % TY;
+            z = r / (6 * TY);
+            x = h < 3 ? h - 3 : TX + h - 3;
+        } else if (idx < C::NC + C::NXH + C::NYH) {
+            const int r = idx - C::NC - C::NXH, h = (r / TX) % 6;
+            x = r % TX;
+            z = r / (6 * TX);
+            y = h < 3 ? h - 3 : TY + h - 3;
+        } else {
+            const int r = idx - C::NC - C::NXH - C::NYH, h = r / (TX * TY);
+            x = r % TX;
+            y = (r / TX) % TY;
+            z = h < 3 ? h - 3 : TZ + h - 3;
+        }
+        const int gi = i0 + x, gj = j0 + y, gk = k0 + z;
+        double q[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (gi <= B.hi[0] + 3 && gj <= B.hi[1] + 3 && (B.zvirt || gk <= B.hi[2] + 3)) {
+            int sg;
+            Prec<double>::prims(P, B.S, gi, gj, zmap(B, gk, sg), q);
             if (sg & 1) q[QU] = -q[QU];
             if (sg & 2) q[QV] = -q[QV];
             if (sg & 4) q[QW] = -q[QW];
@@ -586,6 +654,14 @@ __device__ __forceinline__ void rhs_tile(const RegBoxArgs* __restrict__ boxes, c
         cross_prims<TX, TY, TZ>(B, P, i0, j0, k0, stage, staged, Q);
         __syncthreads();
         FT* F = reinterpret_cast<FT*>(sbase);
+        sweep<FT, 0, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<0, TX, TY, TZ>::N, nullptr, acc, Q);
+        sweep<FT, 1, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<1, TX, TY, TZ>::N, nullptr, acc, Q);
+        sweep<FT, 2, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<2, TX, TY, TZ>::N, nullptr, acc, Q);
+    } else if constexpr (CrossPlain<FT, TX, TY, TZ, VISC>::value) {
+        FT* F = reinterpret_cast<FT*>(sbase);
+        double* Q = F + pencil_elems<TX, TY, TZ>();
+        cross_prims_plain<TX, TY, TZ>(B, P, i0, j0, k0, Q);
+        __syncthreads();
         sweep<FT, 0, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<0, TX, TY, TZ>::N, nullptr, acc, Q);
         sweep<FT, 1, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<1, TX, TY, TZ>::N, nullptr, acc, Q);
         sweep<FT, 2, TX, TY, TZ, VISC, true>(B, P, i0, j0, k0, F, F + 10 * Pencil<2, TX, TY, TZ>::N, nullptr, acc, Q);
