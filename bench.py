@@ -69,16 +69,14 @@ FLOPS_PER_CELL_STAGE = 3233 + 25
 NCU_DRAM_BYTES_PER_CELL = {
     # k_rhs_regular<float, 8, 8, 8>, DMR finest level: 310.9 MB over 2,048,000 cells
     ("dmr-amr", "fp32"): 310.9e6 / 2048000,
-    # the jet's finest-level stage (k_rhs_regular + the cut-cell batch's three
-    # kernels): 2094.2 MB over 4,980,736 cells
-    ("jet-eb-amr", "fp32"): 2094.2e6 / 4980736,
     # k_rhs_regular<float, 8, 8, 8>, 3D blast 256x256x64: 566.6 MB over 4,194,304 cells
     ("cube", "fp32"): 566.6e6 / 4194304,
     # k_chem_advance_list, 128^3 reacting box: 309 + 126 MB over 2,097,152 cells
     ("react", "chem"): (309e6 + 126e6) / 2097152,
     # k_rhs_regular<double, 8, 8, 8> (the jet's FP64 headline kernel), captured on the 3D blast
-    # 256x256x64 (64^3 boxes, as the jet's regular boxes): 416.4 + 141.2 MB over 4,194,304 cells
-    ("jet-eb-amr", "fp64"): (416.4e6 + 141.2e6) / 4194304,
+    # 256x256x64 (64^3 boxes, as the jet's regular boxes): 414.7 + 140.8 MB over 4,194,304 cells
+    ("jet-eb-amr", "fp64"): (414.7e6 + 140.8e6) / 4194304,
+    ("cube", "fp64"): (414.7e6 + 140.8e6) / 4194304,
 }
 
 
