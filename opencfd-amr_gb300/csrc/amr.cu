@@ -51,6 +51,7 @@
 #include <thread>
 #include <vector>
 
+#include "host_sort.h"
 #include "level.h"
 #include "eb_level.h"
 #include "chem_internal.h"
@@ -978,11 +979,11 @@ static ocfd_status compute_pair(const ocfd_amr* H, int f, PairTables& T) {
     }
     // group the faces by coarse cell (an element index of the level's state is
     // unique across its boxes) with discovery order kept inside a group: one
-    // sort of 64-bit keys (element index, discovery index)
+    // radix sort of 64-bit keys (element index, discovery index), all distinct
     if (faces.size() >= (size_t(1) << 22)) return fail(OCFD_BAD_ARG, "AMR: too many reflux faces");
     std::vector<uint64_t> key(faces.size());
     for (size_t q = 0; q < faces.size(); ++q) key[q] = ((uint64_t)face_u[q] << 22) | (uint64_t)q;
-    std::sort(key.begin(), key.end());
+    radix_sort_u64(key);
     std::vector<int> order(faces.size()), gstart;
     for (size_t q = 0; q < key.size(); ++q) {
         order[q] = (int)(key[q] & ((1u << 22) - 1));
