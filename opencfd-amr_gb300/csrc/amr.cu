@@ -259,12 +259,23 @@ struct AmrStates {
     double fixed_dt;  // > 0: the coarse step is this dt (reacting hierarchy, Source/Advance.cpp:54-57)
 };
 
+// monotonized-central slope of c between m and p: 0 unless both one-sided
+// differences are non-zero with one sign, else min(|dc|, 2 min(|dl|, |dr|)) with
+// the sign of dc.  The sign tests and the minima run on the integer pipes (the
+// bits of non-negative doubles order as their values; dc has the sign of dl);
+// only NaN differences, and a product dl dr that would underflow (|dl dr| below
+// 5e-324), select differently from the floating-point tests.
 __device__ __forceinline__ double mc_slope(double m, double c, double p) {
     const double dl = c - m, dr = p - c;
-    if (dl * dr <= 0.0) return 0.0;
+    const long long mag = 0x7fffffffffffffffLL;
+    const long long il = __double_as_longlong(dl), ir = __double_as_longlong(dr);
+    const long long al = il & mag, ar = ir & mag;
+    if ((il ^ ir) < 0 || al == 0 || ar == 0) return 0.0;
     const double dc = 0.5 * (dl + dr);
-    const double a = fmin(fabs(dc), 2.0 * fmin(fabs(dl), fabs(dr)));
-    return dc > 0.0 ? a : -a;
+    const long long adc = __double_as_longlong(dc) & mag;
+    const long long a2 = __double_as_longlong(2.0 * __longlong_as_double(al < ar ? al : ar));
+    const double a = __longlong_as_double(adc < a2 ? adc : a2);
+    return il < 0 ? -a : a;
 }
 
 __device__ __forceinline__ double mixed(const TimeMix& m, long long q) {
@@ -320,13 +331,17 @@ __global__ void k_cf_interp(const CfTag* __restrict__ tags, const long long* __r
             const double sx_ = flat ? 0.0 : mc_slope(mixed(mix, q - 1), v0, mixed(mix, q + 1));
             const double sy_ = flat ? 0.0 : mc_slope(mixed(mix, q - sy), v0, mixed(mix, q + sy));
             const double sz_ = flat ? 0.0 : mc_slope(vzm, v0, vzp);
+            // child (ii, jj, kk) = v0 +- s_x / 4 +- s_y / 4 +- s_z / 4, summed in x, y, z
+            // order from shared partial sums (s / 4 is exact, so each sum is the
+            // same rounding as the fused multiply-add of the slope)
+            const double hx = 0.25 * sx_, hy = 0.25 * sy_, hz = 0.25 * sz_;
+            const double px[2] = {v0 - hx, v0 + hx};
+            const double pxy[4] = {px[0] - hy, px[1] - hy, px[0] + hy, px[1] + hy};
             double* d = dst + o + n * ff.ns;
 #pragma unroll
             for (int q8 = 0; q8 < 8; ++q8) {
                 const int ii = q8 & 1, jj = (q8 >> 1) & 1, kk = q8 >> 2;
-                if (inside & (1u << q8))
-                    d[ii + jj * fy + kk * fz] = v0 + (ii ? 0.25 : -0.25) * sx_ + (jj ? 0.25 : -0.25) * sy_ +
-                                               (kk ? 0.25 : -0.25) * sz_;
+                if (inside & (1u << q8)) d[ii + jj * fy + kk * fz] = kk ? pxy[q8 & 3] + hz : pxy[q8 & 3] - hz;
             }
         }
     }
