@@ -100,7 +100,8 @@ __device__ __forceinline__ double cfl_bound(const DevParm& P, const double* u, c
     return dtx < m ? dtx : m;
 }
 
-// block-wide min of v (all threads participate), one atomicMin per block
+// block-wide min of v (all threads participate; the block is whole warps, at
+// most 1024 threads), one atomicMin per block
 __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* target) {
     __shared__ double red[32];
     for (int o = 16; o > 0; o >>= 1) {
@@ -146,7 +147,8 @@ struct CflSpeeds {
 };
 
 // block-wide CFL bound from the threads' largest speeds (all threads
-// participate), one atomicMin per block; a block without cells adds +inf
+// participate; the block is whole warps, at most 1024 threads), one atomicMin
+// per block; a block without cells adds +inf
 __device__ __forceinline__ void block_cfl_atomic(const CflSpeeds& c, const double* dx, unsigned long long* target) {
     __shared__ double red[3][32];
     double s0 = c.s[0], s1 = c.s[1], s2 = c.s[2];
