@@ -6,7 +6,8 @@
 // cut-cell scheme eb_compute_dSdt_box (Source/EB/AdvanceBox.cpp:16-228).  Here
 // the regular boxes stay in the fused tile kernel, and all cut and covered boxes
 // of the level run as one launch per RK stage of k_ebl_tile: one CTA per 8x8x4
-// tile, primitives over grow(tile, 2) (c2prim), the tile's faces in x, y and z
+// tile, primitives (c2prim) over grow(tile, 2), or over the tile's cross in
+// inviscid stages, the tile's faces in x, y and z
 // (MUSCL-minmod states, Van Leer flux, EB viscous flux; RK-weighted
 // area-fraction fluxes into the flux registers of an AMR level) in shared
 // memory, then per cell the cut-cell divergence with the wall flux, negated
@@ -195,16 +196,17 @@ struct EbStageArgs {
 
 // ------------------------------------------------------------ fused tile kernel
 // The batched cut-cell stage as one kernel: one CTA per 8x8x4 tile of a cut or
-// covered box.  The primitives of grow(tile, 2) and the tile's face fluxes in x,
-// y and z stay in shared memory; each cell thread then forms the cut-cell
-// divergence with the wall flux (Source/EB/EBkernels.H:216-338, negated, the
-// small-cell rescale of flux_redist :341-377), the Shu-Osher stage and the CFL
-// bound.  Only the state (read over grow(tile, 2), the stage input U0, the
-// output) and the z-invariant geometry touch memory: no primitive or face-flux
-// scratch round trip.  A face on a tile boundary is computed by both tiles and
-// added to the flux registers by the one that owns it (faces 0 .. T_D - 1 of the
-// tile, plus the box's high face), so that every face is accumulated once.  The
-// per-box form (OCFD_PER_BOX) launches the same kernel box by box.
+// covered box.  The primitives (over grow(tile, 2), or over the tile's cross in
+// an inviscid stage) and the tile's face fluxes in x, y and z stay in shared
+// memory; each cell thread then forms the cut-cell divergence with the wall flux
+// (Source/EB/EBkernels.H:216-338, negated, the small-cell rescale of flux_redist
+// :341-377), the Shu-Osher stage and the CFL bound.  Only the state (read once
+// per cell of that region), the stage input U0, the output and the z-invariant
+// geometry touch memory: no primitive or face-flux scratch round trip.  A face
+// on a tile boundary is computed by both tiles and added to the flux registers
+// by the one that owns it (faces 0 .. T_D - 1 of the tile, plus the box's high
+// face), so that every face is accumulated once.  The per-box form
+// (OCFD_PER_BOX) launches the same kernel box by box.
 constexpr int EBT_X = 8, EBT_Y = 8, EBT_Z = 4, EBT_N = EBT_X * EBT_Y * EBT_Z;
 constexpr int EBQ_X = EBT_X + 4, EBQ_Y = EBT_Y + 4, EBQ_Z = EBT_Z + 4, EBQ_N = EBQ_X * EBQ_Y * EBQ_Z;
 constexpr int EBF_N0 = (EBT_X + 1) * EBT_Y * EBT_Z, EBF_N1 = EBT_X * (EBT_Y + 1) * EBT_Z,
